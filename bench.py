@@ -1,0 +1,376 @@
+"""Benchmark of the CNN-CRF stereo hot path (one JSON line on rank 0).
+
+Workload (the reference's metric "stereo pairs/s at 1242x375 D=128"): one
+KITTI-shaped RGB pair per step, 1242x375, D = 128 (disparities 0..127), the
+7-layer all-3x3 100-channel feature CNN with L2-normalised features and the
+1 - <fL,fR> unary, the 2-layer 3x3 (+1x1) pairwise CNN, a 4-connected CRF
+with truncated-linear pairwise (L1 = 0.5, truncation 3) solved with 8
+iterations, Xavier weights from seed 0, seeded synthetic scene (ground plane
++ 15 boxes; the KITTI images are not available).
+
+  value   pairs/s with the input pair already in HBM (device-to-device
+          staging + CNN + correlation + CRF + remap per step), CUDA events on
+          the library's stream, L2 flushed (256 MiB write) between steps
+  e2e     same through the public API from pinned HOST buffers: H2D of both
+          RGBA images, the whole path, D2H of the disparity map per step
+  --impl reference   the CPU restatement of the reference path (OpenMP, all
+          host threads) on the same workload; see the design doc.
+
+Multi-GPU: pairs are independent, so N ranks run N replicas (no
+collective on the data path); value = pairs of all ranks / max rank time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "cnn-crf-stereo_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "stereo pairs/s at 1242x375 D=128, BF16 vs FP32 GPU (<=0.5% disparity change)"
+
+WORKLOAD = dict(name="kitti1242x375_d128", W=1242, H=375, D=128, layers=7, topology="all3x3",
+                feat=100, pw=64, unary="one_minus_dot", L1=0.5, L2=1.5, delta=3, shape="linear",
+                crf_iters=8, lam=1.0, seed=0)
+
+
+def conv_flops(W, H, layers=7, feat=100, ic=3, pw=64, k=3):
+    """Algorithmic FLOPs of the convs of one pair: 2 x output pixels x Cout x
+    (kh kw Cin), summed over the layers of both sides + the pairwise net."""
+    p = layers  # all-3x3: padding = number of layers
+    h, w = H + 2 * p, W + 2 * p
+    f = 0
+    cin = ic
+    for _ in range(layers):
+        h, w = h - (k - 1), w - (k - 1)
+        f += 2 * h * w * feat * k * k * cin
+        cin = feat
+    feat_flops = 2 * f
+    pw_flops = 2 * (H + 2) * (W + 2) * pw * 9 * 3 + 2 * H * W * pw * 9 * pw + 2 * H * W * 2 * pw
+    return feat_flops, pw_flops
+
+
+def crf_bytes_per_pass(W, H, D):
+    """Algorithmic bytes of one chain pass: read unary, read message, write
+    message, N*D floats each."""
+    return 3 * W * H * D * 4
+
+
+class ClockSampler:
+    def __init__(self, index):
+        self.index, self.samples, self.proc = index, [], None
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "100"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def dist_setup():
+    import torch
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def oracle_cfg(O, wl, threads=0):
+    return O.make_cfg(num_layers=wl["layers"], topology=1, unary=1, feat_channels=wl["feat"],
+                      pw_channels=wl["pw"], disp_max=float(wl["D"] - 1), lam=wl["lam"], L1=wl["L1"],
+                      L2=wl["L2"], delta=float(wl["delta"]), crf_iters=wl["crf_iters"], crf_shape=1,
+                      threads=threads)
+
+
+def cpu_pairs_per_s(wl, scene, pairs=1):
+    """Time the CPU oracle (all host threads) on `pairs` full pairs."""
+    from oracle import oracle as O
+    cfg = oracle_cfg(O, wl)
+    params = O.xavier_params(cfg, seed=wl["seed"])
+    O.run_pair(cfg, params, scene["left"][:16], scene["right"][:16])  # warm the library / threads
+    t = time.perf_counter()
+    for _ in range(pairs):
+        O.run_pair(cfg, params, scene["left"], scene["right"])
+    dt = time.perf_counter() - t
+    return pairs / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_setup()
+    if rank != 0:
+        return 0
+    from cnncrf import scenes
+    wl = WORKLOAD
+    scene = scenes.kitti_scene(wl["W"], wl["H"], wl["D"], seed=0)
+    cores = os.cpu_count()
+    times = []
+    for i in range(args.warmup + args.steps):
+        v, dt = cpu_pairs_per_s(wl, scene, 1)
+        if i >= args.warmup:
+            times.append(dt)
+    value = len(times) / sum(times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded KITTI-shaped scene)",
+        "config": {"workload": wl["name"], "W": wl["W"], "H": wl["H"], "D": wl["D"], "crf_iters": wl["crf_iters"],
+                   "net": "7x3x3 conv, 100 ch, 1-dot unary, pairwise CNN", "parallelism": "host OpenMP"},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": cores, "kind": "port",
+                         "sample": "one full 1242x375 D=128 pair per step (CNN, correlation, CRF, remap)"},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def build_stereo(cnncrf, wl, precision, stream):
+    from cnncrf.api import Stereo
+    st = Stereo(precision=precision, unary=cnncrf.UNARY_ONE_MINUS_DOT, topology=cnncrf.TOPO_ALL3X3,
+                feat_channels=wl["feat"], pw_channels=wl["pw"], ref_depth_rounding=False,
+                crf_shape=cnncrf.RHO_LINEAR, stream=stream)
+    st.initialize(wl["W"], wl["H"], 0.0, 1.0, float(wl["D"] - 1))
+    st.set_matching_function(cnncrf.MATCH_COLORCNN_PAIRWISE)
+    st.set_num_layers(wl["layers"])
+    st.set_xavier_seed(wl["seed"])
+    return st
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import cnncrf
+    from cnncrf import scenes, _lib
+
+    rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    wl = WORKLOAD
+    W, H, D = wl["W"], wl["H"], wl["D"]
+    precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
+    stream = torch.cuda.Stream()
+    scene = scenes.kitti_scene(W, H, D, seed=rank)
+    with torch.cuda.stream(stream):
+        st = build_stereo(cnncrf, wl, precision, stream)
+        dl = torch.from_numpy(scene["left"]).cuda()
+        dr = torch.from_numpy(scene["right"]).cuda()
+        hl = torch.from_numpy(scene["left"]).pin_memory()
+        hr = torch.from_numpy(scene["right"]).pin_memory()
+        hout = torch.empty((H, W), dtype=torch.float32).pin_memory()
+        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+        def step_device():
+            st.set_color_images(dl, dr)
+            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+
+        def step_e2e():
+            st.set_color_images(hl, hr)
+            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+            st.get_output_into(hout)
+
+        for _ in range(max(args.warmup, 3)):
+            step_device()
+        step_e2e()
+        torch.cuda.synchronize()
+
+        # ---- timed region (device-resident inputs)
+        clocks = ClockSampler(local)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        barrier(world)
+        torch.cuda.synchronize()
+        clocks.start()
+        _lib.profile_reset()
+        _lib.profile_enable(True)
+        l0 = _lib.kernel_launches()
+        for a, b in evs:
+            flush.zero_()
+            a.record(stream)
+            step_device()
+            b.record(stream)
+        torch.cuda.synchronize()
+        launches = _lib.kernel_launches() - l0
+        _lib.profile_enable(False)
+        barrier(world)
+        clk = clocks.stop()
+        t_ms = sum(a.elapsed_time(b) for a, b in evs)
+        t_ms = allmax(t_ms, world)
+        value = args.steps * world / (t_ms / 1000.0)
+
+        prof = {}
+        for kname in _lib.profile_kernels():
+            n, tot = _lib.profile_query(kname)
+            prof[kname] = (n, tot)
+        _lib.profile_reset()
+
+        # ---- end to end through the public API, host buffers
+        evs2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        barrier(world)
+        torch.cuda.synchronize()
+        for a, b in evs2:
+            flush.zero_()
+            a.record(stream)
+            step_e2e()
+            b.record(stream)
+        torch.cuda.synchronize()
+        e_ms = allmax(sum(a.elapsed_time(b) for a, b in evs2), world)
+        e2e = args.steps * world / (e_ms / 1000.0)
+
+        labels = st.labels_device().cpu().numpy()
+        disp = st.get_output()
+
+    # ---- BF16 vs FP32: disparity change on the same pair, FP32 pairs/s
+    cmp = {}
+    if precision == cnncrf.BF16:
+        with torch.cuda.stream(stream):
+            st32 = build_stereo(cnncrf, wl, cnncrf.FP32, stream)
+            st32.set_color_images(dl, dr)
+            st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            n32 = 3
+            ev[0].record(stream)
+            for _ in range(n32):
+                st32.set_color_images(dl, dr)
+                st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            lab32 = st32.labels_device().cpu().numpy()
+            cmp = {"fp32_pairs_per_s": n32 / (ev[0].elapsed_time(ev[1]) / 1000.0),
+                   "disparity_change_vs_fp32": float((lab32 != labels).mean())}
+            cmp["speedup_vs_fp32"] = value / world / cmp["fp32_pairs_per_s"]
+
+    if rank != 0:
+        return 0
+
+    peaks, peak_src = measured_peaks()
+    feat_f, pw_f = conv_flops(W, H, wl["layers"], wl["feat"], 3, wl["pw"])
+    conv_name = "conv_tc" if "conv_tc" in prof else "conv_simt"
+    kernels = {k: {"launches": n, "total_ms": round(t, 4), "share": None} for k, (n, t) in prof.items()}
+    tot = sum(t for _, t in prof.values()) or 1.0
+    for k in kernels:
+        kernels[k]["share"] = round(prof[k][1] / tot, 4)
+    roof = None
+    if conv_name in prof:
+        n, t = prof[conv_name]
+        achieved = (feat_f + pw_f) * args.steps / (t / 1000.0) / 1e12
+        if conv_name == "conv_tc":
+            roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved,
+                    "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+                    "traffic": None, "peak_source": peak_src + " (bf16 dense burst)"}
+        else:
+            roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
+                    "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                    "peak_source": peak_src + " (bf16 dense burst; this FP32 SIMT kernel cannot reach it)"}
+    crf = None
+    if "crf_h" in prof and "crf_v" in prof:
+        n = prof["crf_h"][0] + prof["crf_v"][0]
+        t = prof["crf_h"][1] + prof["crf_v"][1]
+        gbs = crf_bytes_per_pass(W, H, D) * n / (t / 1000.0) / 1e9
+        crf = {"kernel": "crf_h+crf_v", "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+               "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src}
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        v, dt = cpu_pairs_per_s(wl, scene, 1)
+        cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full 1242x375 D=128 pair (CNN, correlation, CRF, remap), %.1f s" % dt}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16" if precision == cnncrf.BF16 else "f32",
+        "data": "synthetic (seeded KITTI-shaped scene: ground plane + 15 boxes)",
+        "config": {"workload": wl["name"], "W": W, "H": H, "D": D, "crf_iters": wl["crf_iters"],
+                   "net": "7x3x3 conv 100ch + L2 norm, 1-dot unary, pairwise CNN 3x3-3x3-1x1",
+                   "crf": "truncated linear L1=0.5 T=3", "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": 2 * W * H * 4 * 4,
+                "d2h_bytes_per_step": W * H * 4},
+        "gpu_launches": launches,
+        "roofline": roof, "crf_roofline": crf, "kernels": kernels, "clocks": clk,
+        "cpu_baseline": cpu,
+        "precision_check": cmp,
+        "disparity_stats": {"mean": float(np.mean(disp)), "bad3px_vs_gt": scenes.bad_pixels(disp, scene["disp"])},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

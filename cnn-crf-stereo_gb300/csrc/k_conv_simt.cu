@@ -1,0 +1,190 @@
+// k_conv_simt.cu -- the FP32 convolution of the bit-exact path.
+//
+// Implicit GEMM on the CUDA cores: out[p][co] = act(bias[co] + sum_k A[p][k] W[k][co])
+// with p = output pixel, k = (ky, kx, ci) ci fastest.  Each output is
+// accumulated in ascending k with one fmaf per term, so it equals the CPU
+// oracle bit for bit (reference: cudnnConvolutionForward in
+// CUDNN_CONVOLUTION mode + cudnnAddTensor + tanh, stereo/operators/
+// convolution.cpp:141-152, bias.cpp:58-67, activation.cpp:33-41).
+//
+// Tiling: CTA = 128 pixels of one output row x 128 output channels, k-slices
+// of 8 double-buffered in shared memory, 256 threads with 8x8 register tiles.
+#include "../../include/cnncrf_fmath.h"
+#include "common.h"
+#include "kernels.h"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+constexpr int BM = 128, BN = 128, BK = 8, APAD = 4;
+
+__device__ __forceinline__ float act_fn(float v, int act)
+{
+    if (act == 1) return cnncrf_tanhf(v);
+    if (act == 2) return fabsf(v);
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, int K)
+{
+    __shared__ __align__(16) float As[2][BK][BM + APAD];
+    __shared__ __align__(16) float Bs[2][BK][BN];
+    const int tid = threadIdx.x;
+    const int oy = blockIdx.y;
+    const int ox0 = blockIdx.x * BM;
+    const int a_kk = tid & 7, a_p = tid >> 3;
+    const int b_kk = tid >> 5, b_n = (tid & 31) * 4;
+    const int tx = tid & 15, ty = tid >> 4;
+    const int nsl = (K + BK - 1) / BK;
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+
+    float ra[4];
+    float4 rb;
+    auto loadA = [&](int s) {
+        int kk = s * BK + a_kk;
+        bool kv = kk < K;
+        int ky = 0, kx = 0, ci = 0;
+        if (kv) {
+            int tap = kk / a.Cin;
+            ci = kk - tap * a.Cin;
+            ky = tap / a.kw;
+            kx = tap - ky * a.kw;
+        }
+        const float *rowp = a.in + (long)(oy + ky) * a.in_row + (long)kx * a.in_pix + ci;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            int ox = ox0 + a_p + 32 * e;
+            ra[e] = (kv && ox < Wo) ? __ldg(rowp + (long)ox * a.in_pix) : 0.0f;
+        }
+    };
+    auto loadB = [&](int s) {
+        int kk = s * BK + b_kk;
+        rb = kk < K ? __ldg((const float4 *)(a.wt + (long)kk * BN + b_n)) : make_float4(0, 0, 0, 0);
+    };
+    auto storeAB = [&](int buf) {
+#pragma unroll
+        for (int e = 0; e < 4; ++e) As[buf][a_kk][a_p + 32 * e] = ra[e];
+        *(float4 *)&Bs[buf][b_kk][b_n] = rb;
+    };
+
+    loadA(0);
+    loadB(0);
+    storeAB(0);
+    __syncthreads();
+    for (int s = 0; s < nsl; ++s) {
+        const int cur = s & 1;
+        if (s + 1 < nsl) {
+            loadA(s + 1);
+            loadB(s + 1);
+        }
+        const int kmax = min(BK, K - s * BK);
+#pragma unroll
+        for (int kk = 0; kk < BK; ++kk) {
+            if (kk < kmax) {
+                float4 a0 = *(const float4 *)&As[cur][kk][ty * 4];
+                float4 a1 = *(const float4 *)&As[cur][kk][64 + ty * 4];
+                float4 b0 = *(const float4 *)&Bs[cur][kk][tx * 4];
+                float4 b1 = *(const float4 *)&Bs[cur][kk][64 + tx * 4];
+                float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+                float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
+            }
+        }
+        if (s + 1 < nsl) storeAB(cur ^ 1);
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        int p = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
+        int ox = ox0 + p;
+        if (ox >= Wo) continue;
+        float *dst = a.out + ((long)oy * Wo + ox) * a.Cout;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            int co = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
+            if (co < a.Cout) {
+                float v = acc[i][j];
+                if (a.bias) v = __fadd_rn(v, a.bias[co]);
+                dst[co] = act_fn(v, a.act);
+            }
+        }
+    }
+}
+
+__global__ void k_head2(const float *__restrict__ in, int npx, int Cin, const float *__restrict__ w,
+                        float *__restrict__ out)
+{
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npx) return;
+    const float *x = in + (long)p * Cin;
+    float a0 = 0.0f, a1 = 0.0f;
+    for (int ci = 0; ci < Cin; ++ci) {
+        float v = x[ci];
+        a0 = __fmaf_rn(w[ci], v, a0);
+        a1 = __fmaf_rn(w[Cin + ci], v, a1);
+    }
+    out[p] = fabsf(a0);
+    out[(long)npx + p] = fabsf(a1);
+}
+
+__global__ void k_l2norm(float *__restrict__ f, long npx, int C)
+{
+    long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npx) return;
+    float *x = f + p * C;
+    float s = 0.0f;
+    for (int c = 0; c < C; ++c) s = __fmaf_rn(x[c], x[c], s);
+    float n = __fsqrt_rn(s);
+    for (int c = 0; c < C; ++c) x[c] = n > 0.0f ? __fdiv_rn(x[c], n) : 0.0f;
+}
+
+} // namespace
+
+int conv_simt(const ConvArgs &a, cudaStream_t st)
+{
+    if (a.Cout > BN) return fail(CNNCRF_EINVAL, "conv_simt: Cout %d > %d", a.Cout, BN);
+    int Ho = a.H - a.kh + 1, Wo = a.W - a.kw + 1;
+    if (Ho <= 0 || Wo <= 0) return fail(CNNCRF_ESHAPE, "conv_simt: empty output");
+    int K = a.kh * a.kw * a.Cin;
+    dim3 grid(ceil_div(Wo, BM), Ho);
+    {
+        CNNCRF_PROF("conv_simt", st);
+        k_conv_simt<<<grid, 256, 0, st>>>(a, Ho, Wo, K);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int conv_head2(const float *in, int npx, int Cin, const float *w, float *out, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("head2", st);
+        k_head2<<<ceil_div(npx, 256), 256, 0, st>>>(in, npx, Cin, w, out);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int l2norm(float *f, long npx, int C, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("l2norm", st);
+        k_l2norm<<<ceil_div(npx, 256), 256, 0, st>>>(f, npx, C);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace k
+} // namespace cnncrf

@@ -1,0 +1,150 @@
+// k_corr.cu -- FP32 correlation cost volume with the unary fused in.
+//
+// Restates kCorrelation_NHWC / kCorrelation_NHWC_interpolation
+// (stereo/operators/stereocorrelation.cu:66-142, rectCorr = 0) followed by the
+// channel softmax over D and the negation (stereo/operators/softmax.cpp:30-38,
+// stereo/utils.cu:289-292), or by 1 - <fL,fR> for L2-normalised features.
+// Compiled with --fmad=false; the dot products use explicit fmaf in channel
+// order and the softmax sum follows the lane layout below, so the output is
+// bit-identical to the CPU oracle.
+//
+// Block = one image row y, 32 pixels; the left tile and the band of right
+// pixels those pixels can see are staged in shared memory (odd row stride:
+// lanes read consecutive rows without bank conflicts).  One warp per pixel;
+// lane j owns disparity indices k = j + 32 r.
+#include <cfloat>
+
+#include "../../include/cnncrf_fmath.h"
+#include "common.h"
+#include "kernels.h"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+constexpr int PIX = 32;
+constexpr int MAXP = 16; // D <= 512
+
+__global__ void __launch_bounds__(256)
+    k_corr(const float *__restrict__ fl, const float *__restrict__ fr, int H, int W, int C,
+           const float *__restrict__ list, int D, int omin, int omax, int interp, int unary,
+           float *__restrict__ out)
+{
+    extern __shared__ float sm[];
+    const int y = blockIdx.y;
+    const int x0 = blockIdx.x * PIX;
+    const int CS = C + 1;
+    const int xlo = max(0, x0 + omin);
+    const int xhi = min(W - 1, x0 + PIX - 1 + omax);
+    const int R = max(0, xhi - xlo + 1);
+    const int npx = min(PIX, W - x0);
+    float *sl = sm;                     // [PIX][CS]
+    float *sr = sl + PIX * CS;          // [R][CS]
+    float *sd = sr + (size_t)R * CS;    // [D]
+    for (int i = threadIdx.x; i < npx * C; i += blockDim.x) {
+        int p = i / C, c = i - p * C;
+        sl[p * CS + c] = fl[((long)y * W + x0 + p) * C + c];
+    }
+    for (int i = threadIdx.x; i < R * C; i += blockDim.x) {
+        int p = i / C, c = i - p * C;
+        sr[p * CS + c] = fr[((long)y * W + xlo + p) * C + c];
+    }
+    for (int i = threadIdx.x; i < D; i += blockDim.x) sd[i] = list[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int P = (D + 31) >> 5;
+    for (int pi = warp; pi < npx; pi += 8) {
+        const int x = x0 + pi;
+        const float *a = sl + pi * CS;
+        float cv[MAXP];
+#pragma unroll
+        for (int r = 0; r < MAXP; ++r) {
+            cv[r] = 0.0f;
+            int kk = lane + 32 * r;
+            if (r < P && kk < D) {
+                float s = sd[kk];
+                float w2 = (float)x + s;
+                float acc = 0.0f;
+                if (!interp) {
+                    if (w2 >= 0.0f) {
+                        int xs = x + (int)s;
+                        if (xs <= W - 1) {
+                            const float *b = sr + (xs - xlo) * CS;
+                            for (int c = 0; c < C; ++c) acc = __fmaf_rn(a[c], b[c], acc);
+                        }
+                    }
+                } else if (w2 >= 0.0f) {
+                    int xa = (int)floorf(w2);
+                    int xb = (int)(w2 + 1.0f);
+                    float num = w2 - (float)xa;
+                    float den = (float)xb - (float)xa;
+                    const float *b0 = sr + (min(xa, W - 1) - xlo) * CS;
+                    const float *b1 = sr + (min(xb, W - 1) - xlo) * CS;
+                    for (int c = 0; c < C; ++c) {
+                        float y0 = b0[c], y1 = b1[c];
+                        float it = y0 + ((y1 - y0) * num) / den;
+                        acc = __fmaf_rn(a[c], it, acc);
+                    }
+                }
+                cv[r] = acc;
+            }
+        }
+        float *o = out + ((long)y * W + x) * D;
+        if (unary == 0) {
+            float m = -FLT_MAX;
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r)
+                if (r < P && lane + 32 * r < D) m = fmaxf(m, cv[r]);
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+            float s = 0.0f;
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                if (r < P) {
+                    int kk = lane + 32 * r;
+                    float e = kk < D ? cnncrf_expf(cv[r] - m) : 0.0f;
+                    cv[r] = e;
+                    s = (r == 0) ? e : s + e;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                int kk = lane + 32 * r;
+                if (r < P && kk < D) o[kk] = -(cv[r] / s);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                int kk = lane + 32 * r;
+                if (r < P && kk < D) o[kk] = unary == 1 ? 1.0f - cv[r] : cv[r];
+            }
+        }
+    }
+}
+
+} // namespace
+
+int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list, int D,
+                int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
+{
+    if (D < 1 || D > 32 * MAXP) return fail(CNNCRF_EINVAL, "correlation: D=%d outside [1,%d]", D, 32 * MAXP);
+    int R = PIX + omax - omin + 1;
+    size_t smem = sizeof(float) * ((size_t)(PIX + R) * (C + 1) + D);
+    if (smem > 227 * 1024)
+        return fail(CNNCRF_EINVAL, "correlation: disparity band too wide (%zu bytes of shared memory)", smem);
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid(ceil_div(W, PIX), H);
+    {
+        CNNCRF_PROF("corr", st);
+        k_corr<<<grid, 256, smem, st>>>(fl, fr, H, W, C, d_list, D, omin, omax, interp ? 1 : 0, unary, out);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace k
+} // namespace cnncrf

@@ -1,0 +1,140 @@
+// k_front.cu -- mirror padding and RGB normalisation (the front end of
+// ColorStereoNet::predict).  Compiled with --fmad=false: results must match
+// the CPU oracle bit for bit.
+#include "common.h"
+#include "kernels.h"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+// cudaAddressModeMirror at texel centres (stereo/stereo.cu:879-911): symmetric
+// reflection, edge sample repeated, period 2n.
+__device__ __forceinline__ int mirror_idx(int i, int n)
+{
+    int m = i % (2 * n);
+    if (m < 0) m += 2 * n;
+    return m >= n ? 2 * n - 1 - m : m;
+}
+
+__global__ void k_pad(const float4 *__restrict__ in, int W, int H, int p, float4 *__restrict__ out)
+{
+    int Wp = W + 2 * p, Hp = H + 2 * p;
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)Wp * Hp) return;
+    int y = (int)(i / Wp), x = (int)(i - (long)y * Wp);
+    out[i] = in[(long)mirror_idx(y - p, H) * W + mirror_idx(x - p, W)];
+}
+
+// value of plane c at pixel i: RGB channel, or rgb_to_gray_kernel's weights
+// (stereo/stereo.cu:853-863) evaluated in double and rounded once.
+__device__ __forceinline__ float plane_val(const float *rgba, long i, int c, int gray)
+{
+    const float *px = rgba + 4 * i;
+    if (gray)
+        return (float)(0.2989 * (double)px[0] + 0.5870 * (double)px[1] + 0.1140 * (double)px[2]);
+    return px[c];
+}
+
+// One thread per (plane, row): FP64 row sums in x order.  pass 0 sums values,
+// pass 1 sums squares of (v - mean_c) rounded to float, as the oracle does.
+__global__ void k_rowsums(const float *__restrict__ rgba, int Wp, int Hp, int planes, int gray,
+                          int pass, const float *__restrict__ stats, double *__restrict__ rows)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= planes * Hp) return;
+    int c = t / Hp, y = t - c * Hp;
+    double s = 0.0;
+    long base = (long)y * Wp;
+    if (pass == 0) {
+        for (int x = 0; x < Wp; ++x) s += (double)plane_val(rgba, base + x, c, gray);
+    } else {
+        float mean = stats[c];
+        for (int x = 0; x < Wp; ++x) {
+            float v = __fsub_rn(plane_val(rgba, base + x, c, gray), mean);
+            s += (double)__fmul_rn(v, v);
+        }
+    }
+    rows[t] = s;
+}
+
+// One thread per plane: the row partials in y order -> mean (pass 0) or std.
+__global__ void k_finalize(const double *__restrict__ rows, int Hp, int planes, long N, int pass,
+                           float *__restrict__ stats)
+{
+    int c = threadIdx.x;
+    if (c >= planes) return;
+    double tot = 0.0;
+    for (int y = 0; y < Hp; ++y) tot += rows[c * Hp + y];
+    if (pass == 0) stats[c] = (float)(tot / (double)N);
+    else stats[4 + c] = (float)sqrt(tot / (double)N);
+}
+
+__global__ void k_norm_write(const float *__restrict__ rgba, int Wp, int Hp, int ic,
+                             const float *__restrict__ stats, float *__restrict__ out)
+{
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)Wp * Hp) return;
+    int gray = ic == 1;
+    int planes = gray ? 1 : 3;
+    for (int c = 0; c < planes; ++c) {
+        float v = __fsub_rn(plane_val(rgba, i, c, gray), stats[c]);
+        float sd = stats[4 + c];
+        out[i * ic + c] = sd > 0.0f ? __fdiv_rn(v, sd) : 0.0f;
+    }
+    if (ic == 5) { // stereo/colorstereonet.cpp:102-121
+        int y = (int)(i / Wp), x = (int)(i - (long)y * Wp);
+        out[i * ic + 3] = (float)(((double)x - (double)Wp / 2.0) / (double)Wp);
+        out[i * ic + 4] = (float)(((double)y - (double)Hp / 2.0) / (double)Hp);
+    }
+}
+
+} // namespace
+
+int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st)
+{
+    long n = (long)(W + 2 * p) * (H + 2 * p);
+    {
+        CNNCRF_PROF("pad", st);
+        k_pad<<<ceil_div(n, 256), 256, 0, st>>>((const float4 *)in, W, H, p, (float4 *)out);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+size_t normalize_scratch_bytes(int Hp) { return sizeof(double) * 3 * (size_t)Hp + 64; }
+
+int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scratch, cudaStream_t st)
+{
+    int gray = ic == 1, planes = gray ? 1 : 3;
+    double *rows = (double *)scratch;
+    float *stats = (float *)((char *)scratch + sizeof(double) * 3 * (size_t)Hp);
+    long N = (long)Wp * Hp;
+    int nt = planes * Hp;
+    {
+        CNNCRF_PROF("rowsums", st);
+        k_rowsums<<<ceil_div(nt, 128), 128, 0, st>>>(rgba, Wp, Hp, planes, gray, 0, stats, rows);
+    }
+    {
+        CNNCRF_PROF("finalize", st);
+        k_finalize<<<1, 32, 0, st>>>(rows, Hp, planes, N, 0, stats);
+    }
+    {
+        CNNCRF_PROF("rowsums", st);
+        k_rowsums<<<ceil_div(nt, 128), 128, 0, st>>>(rgba, Wp, Hp, planes, gray, 1, stats, rows);
+    }
+    {
+        CNNCRF_PROF("finalize", st);
+        k_finalize<<<1, 32, 0, st>>>(rows, Hp, planes, N, 1, stats);
+    }
+    {
+        CNNCRF_PROF("norm_write", st);
+        k_norm_write<<<ceil_div(N, 256), 256, 0, st>>>(rgba, Wp, Hp, ic, stats, out);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace k
+} // namespace cnncrf

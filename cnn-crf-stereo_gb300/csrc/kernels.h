@@ -1,0 +1,73 @@
+// kernels.h -- host-side launchers of the CUDA kernels of libcnncrf.
+// Every launcher enqueues on `st` and returns a cnncrf_status.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace cnncrf {
+namespace k {
+
+// ------------------------------------------------------------ front end
+// mirror pad of an RGBA image (stereo/stereo.cu:879-911)
+int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st);
+// zero-mean / unit-std planes of a padded RGBA image -> NHWC [Hp][Wp][ic]
+// (stereo/colorstereonet.cpp:53-64,102-121; stereo/utils.cu:169-237).
+// scratch: >= 6*Hp doubles + 8 floats.
+int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scratch,
+              cudaStream_t st);
+size_t normalize_scratch_bytes(int Hp);
+
+// ------------------------------------------------------------ FP32 conv
+struct ConvArgs {
+    const float *in;
+    int H, W, Cin;        // input extent (valid conv)
+    long in_pix, in_row;  // element strides of a pixel and of a row
+    const float *wt;      // [K][128] flipped, transposed, zero padded
+    const float *bias;    // [128] or nullptr
+    int Cout, kh, kw, act; // act: 0 none, 1 tanh, 2 abs
+    float *out;           // NHWC dense [Ho][Wo][Cout]
+};
+int conv_simt(const ConvArgs &a, cudaStream_t st);
+// 1x1 conv Cin -> 2, no bias, |.| (stereo/stereonet.cpp:167,401): planar [2][H][W]
+int conv_head2(const float *in, int npx, int Cin, const float *w /*[2][Cin]*/, float *out,
+               cudaStream_t st);
+// per-pixel L2 normalisation of NHWC features
+int l2norm(float *f, long npx, int C, cudaStream_t st);
+
+// ------------------------------------------------------------ correlation
+// raw correlation (+ unary: -1 none, 0 -softmax, 1 one-minus) of NHWC FP32
+// features; list = the reference's stored (negated) disparities.
+int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list,
+                int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st);
+
+// ------------------------------------------------------------ CRF
+struct CrfParams {
+    float L1, L2;
+    int delta;
+    int shape;
+    float slack;
+};
+// workspace layout helpers
+size_t crf_workspace_bytes(int W, int H, int D);
+int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D,
+              const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
+              double *h_lb, cudaStream_t st);
+// theta - phi of the last solve (get_C1)
+int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st);
+
+// ------------------------------------------------------------ small ops
+int remap(float *out, const int32_t *labels, long n, float dmin, float dstep, cudaStream_t st);
+int argmin(float *out, const float *vol, long npx, int D, float dmin, float dstep,
+           cudaStream_t st);
+int scale(float *x, long n, float s, cudaStream_t st);
+int nchw_to_nhwc(const float *in, float *out, int C, long npx, cudaStream_t st);
+int warp_rgba(float *out, const float *in, const float *u, int W, int H, cudaStream_t st);
+int tv_fit(const float *vol3, float *qf, int W, int H, float step, float lam, cudaStream_t st);
+int tv_iterate(float *u, float *u_, const float *u0, const float *qf, float *p, float *q,
+               const float *wx, const float *wy, int W, int H, float C, float eps, float step,
+               int iters, cudaStream_t st);
+
+} // namespace k
+} // namespace cnncrf

@@ -1,0 +1,420 @@
+// net.cpp -- StereoNet / ColorStereoNet: layer bookkeeping, parameters,
+// disparities and predict() over the CUDA kernels (C ABI cnncrf_net_*).
+//
+// Reference: stereo/stereonet.cpp (initNet 65-182, setAllParams 184-227,
+// setDisparities 229-248, performPrediction 250-421) and
+// stereo/colorstereonet.cpp:38-133 (predict / predictXY).
+#include "net.h"
+
+#include <cmath>
+#include <cstring>
+
+#include "../../include/cnncrf_xavier.h"
+#include "kernels.h"
+#include "npz.h"
+
+using namespace cnncrf;
+
+namespace {
+
+constexpr int NPAD = 128; // output-channel padding of the FP32 weight layout
+
+void build_layers(cnncrf_net *n)
+{
+    const cnncrf_net_desc &d = n->d;
+    int F = d.feat_channels;
+    n->feat.clear();
+    n->pw.clear();
+    // stereo/stereonet.cpp:69-133: 3x3 first, 2x2 after (REF), every layer tanh
+    n->feat.push_back({d.in_channels, F, 3, 3, 1, 0, 1});
+    int k = d.topology == CNNCRF_TOPO_REF ? 2 : 3;
+    for (int l = 1; l < d.num_layers; ++l) n->feat.push_back({F, F, k, k, 1, 2 * l, 2 * l + 1});
+    if (d.with_pairwise) { // stereo/stereonet.cpp:159-167
+        int base = 2 * d.num_layers, pc = d.in_channels == 1 ? 1 : 3, P = d.pw_channels;
+        n->pw.push_back({pc, P, 3, 3, 1, base, base + 1});
+        n->pw.push_back({P, P, 3, 3, 1, base + 2, base + 3});
+        n->pw.push_back({P, 2, 1, 1, 2, base + 4, -1});
+    }
+    int nparams = 2 * d.num_layers + (d.with_pairwise ? 5 : 0);
+    n->host.assign(nparams, {});
+    n->have.assign(nparams, 0);
+}
+
+cnncrf_net::Layer *layer_of_slot(cnncrf_net *n, int slot, bool *is_bias)
+{
+    for (auto *v : {&n->feat, &n->pw})
+        for (auto &L : *v) {
+            if (L.wslot == slot) {
+                *is_bias = false;
+                return &L;
+            }
+            if (L.bslot == slot) {
+                *is_bias = true;
+                return &L;
+            }
+        }
+    return nullptr;
+}
+
+} // namespace
+
+int cnncrf_net::expected_shape(int i, int64_t s[4], int *nd) const
+{
+    bool b;
+    auto *L = layer_of_slot(const_cast<cnncrf_net *>(this), i, &b);
+    if (!L) return fail(CNNCRF_EINVAL, "parameter index %d outside 0..%d", i, num_params() - 1);
+    if (b) {
+        s[0] = L->cout;
+        *nd = 1;
+    } else {
+        s[0] = L->cout, s[1] = L->cin, s[2] = L->kh, s[3] = L->kw;
+        *nd = 4;
+    }
+    return CNNCRF_OK;
+}
+
+// Upload the device copies of the layer owning `slot`.
+int cnncrf_net::upload(int slot)
+{
+    bool isb;
+    Layer *L = layer_of_slot(this, slot, &isb);
+    if (!L) return fail(CNNCRF_EINVAL, "no layer for slot %d", slot);
+    const std::vector<float> &src = host[slot];
+    if (isb) {
+        std::vector<float> b(NPAD, 0.0f);
+        for (int co = 0; co < L->cout; ++co) b[co] = src[co];
+        CNNCRF_TRY(L->bias.reserve(NPAD * sizeof(float)));
+        CNNCRF_CUDA(cudaMemcpy(L->bias.get(), b.data(), NPAD * sizeof(float), cudaMemcpyHostToDevice));
+        return CNNCRF_OK;
+    }
+    if (L->kh == 1 && L->kw == 1 && L->cout == 2) { // pairwise head: [2][Cin]
+        std::vector<float> w(2 * L->cin);
+        for (int co = 0; co < 2; ++co)
+            for (int ci = 0; ci < L->cin; ++ci) w[co * L->cin + ci] = src[co * L->cin + ci];
+        CNNCRF_TRY(L->wt.reserve(w.size() * sizeof(float)));
+        CNNCRF_CUDA(cudaMemcpy(L->wt.get(), w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+        return CNNCRF_OK;
+    }
+    // CUDNN_CONVOLUTION flips the kernel: wt[(ky*kw+kx)*Cin+ci][co] = w[co][ci][kh-1-ky][kw-1-kx]
+    int K = L->kh * L->kw * L->cin;
+    std::vector<float> wt((size_t)K * NPAD, 0.0f);
+    for (int co = 0; co < L->cout; ++co)
+        for (int ci = 0; ci < L->cin; ++ci)
+            for (int ky = 0; ky < L->kh; ++ky)
+                for (int kx = 0; kx < L->kw; ++kx) {
+                    int k = (ky * L->kw + kx) * L->cin + ci;
+                    wt[(size_t)k * NPAD + co] =
+                        src[(((size_t)co * L->cin + ci) * L->kh + (L->kh - 1 - ky)) * L->kw + (L->kw - 1 - kx)];
+                }
+    CNNCRF_TRY(L->wt.reserve(wt.size() * sizeof(float)));
+    CNNCRF_CUDA(cudaMemcpy(L->wt.get(), wt.data(), wt.size() * sizeof(float), cudaMemcpyHostToDevice));
+    return CNNCRF_OK;
+}
+
+// StereoCorrelation::setDisparities (stereo/operators/stereocorrelation.cpp:71-144)
+int cnncrf_net::set_disparities(float mn, float mx, float step, float *d_out)
+{
+    if (!(step > 0.0f)) return fail(CNNCRF_EINVAL, "setDisparities: step must be > 0");
+    std::vector<float> l;
+    for (float dd = mn; dd <= mx; dd += step) {
+        l.push_back(-dd);
+        if (l.size() > 4096) return fail(CNNCRF_EINVAL, "setDisparities: more than 4096 disparities");
+    }
+    if (l.empty()) return fail(CNNCRF_EINVAL, "setDisparities: empty range [%g, %g]", mn, mx);
+    list = l;
+    D = (int)l.size();
+    float v = D >= 2 ? l[1] : l[0]; // stereo/operators/stereocorrelation.cu:364-373
+    interp = std::fabs(v - std::round(v)) > 0.001f;
+    bool ip = interp || force_interp;
+    omin = 1 << 30, omax = -(1 << 30);
+    for (float s : l) {
+        int a, b;
+        if (ip) {
+            a = (int)std::floor(s) - 1;
+            b = (int)std::floor(s) + 2;
+        } else {
+            a = b = (int)s;
+        }
+        omin = std::min(omin, a);
+        omax = std::max(omax, b);
+    }
+    CNNCRF_TRY(d_list.reserve(sizeof(float) * D));
+    CNNCRF_CUDA(cudaMemcpy(d_list.get(), l.data(), sizeof(float) * D, cudaMemcpyHostToDevice));
+    if (d_out) {
+        vol = d_out;
+    } else {
+        CNNCRF_TRY(vol_own.reserve(sizeof(float) * (size_t)H * W * D));
+        vol = vol_own.as<float>();
+    }
+    return CNNCRF_OK;
+}
+
+int cnncrf_net::pairwise_fp32()
+{
+    // crop by pad-2 of the normalised left image (stereo/colorstereonet.cpp:69-73)
+    int cr = pad - 2, ic = d.in_channels;
+    const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+    k::ConvArgs a1{in, H + 4, W + 4, pw[0].cin, (long)ic, (long)w * ic, pw[0].wt.as<float>(),
+                   pw[0].bias.as<float>(), pw[0].cout, 3, 3, 1, pwa.as<float>()};
+    CNNCRF_TRY(k::conv_simt(a1, st));
+    k::ConvArgs a2{pwa.as<float>(), H + 2, W + 2, pw[1].cin, (long)pw[1].cin, (long)(W + 2) * pw[1].cin,
+                   pw[1].wt.as<float>(), pw[1].bias.as<float>(), pw[1].cout, 3, 3, 1, pwb.as<float>()};
+    CNNCRF_TRY(k::conv_simt(a2, st));
+    return k::conv_head2(pwb.as<float>(), H * W, pw[2].cin, pw[2].wt.as<float>(), pwout, st);
+}
+
+int cnncrf_net::predict_fp32(const float *left, const float *right)
+{
+    const float *img[2] = {left, right};
+    int ic = d.in_channels;
+    for (int s = 0; s < 2; ++s) {
+        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st));
+        const float *cur = norm[s].as<float>();
+        int ch = h, cw = w, cc = ic;
+        for (size_t l = 0; l < feat.size(); ++l) {
+            Layer &L = feat[l];
+            float *out = act[s][l & 1].as<float>();
+            k::ConvArgs a{cur, ch, cw, cc, (long)cc, (long)cw * cc, L.wt.as<float>(), L.bias.as<float>(),
+                          L.cout, L.kh, L.kw, L.act, out};
+            CNNCRF_TRY(k::conv_simt(a, st));
+            ch -= L.kh - 1;
+            cw -= L.kw - 1;
+            cc = L.cout;
+            cur = out;
+        }
+        feats[s] = const_cast<float *>(cur);
+        if (d.unary == CNNCRF_UNARY_ONE_MINUS_DOT) CNNCRF_TRY(k::l2norm(feats[s], (long)H * W, d.feat_channels, st));
+    }
+    CNNCRF_TRY(k::correlation(feats[0], feats[1], H, W, d.feat_channels, d_list.as<float>(), D, omin, omax,
+                              interp || force_interp, d.unary, vol, st));
+    if (d.with_pairwise) CNNCRF_TRY(pairwise_fp32());
+    return CNNCRF_OK;
+}
+
+int cnncrf_net::predict(const float *left, const float *right)
+{
+    if (!inited) return fail(CNNCRF_ESTATE, "predict before initNet");
+    for (size_t i = 0; i < have.size(); ++i)
+        if (!have[i]) return fail(CNNCRF_ESTATE, "parameter arr_%zu not set", i);
+    if (!left || !right) return fail(CNNCRF_EINVAL, "predict: null image");
+    if (d.precision == CNNCRF_BF16) return predict_bf16(left, right);
+    return predict_fp32(left, right);
+}
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" {
+
+int cnncrf_net_create(cnncrf_net_t *out, const cnncrf_net_desc *desc, int n, int h, int w)
+{
+    clear_error();
+    if (!out || !desc) return fail(CNNCRF_EINVAL, "net_create: null argument");
+    *out = nullptr;
+    const cnncrf_net_desc &d = *desc;
+    if (n != 1) return fail(CNNCRF_EUNSUPPORTED, "net_create: only n = 1 (got %d)", n);
+    if (d.num_layers < 1 || d.num_layers > 16) return fail(CNNCRF_EINVAL, "net_create: num_layers %d", d.num_layers);
+    if (d.topology != CNNCRF_TOPO_REF && d.topology != CNNCRF_TOPO_ALL3X3)
+        return fail(CNNCRF_EINVAL, "net_create: topology %d", d.topology);
+    if (d.in_channels != 1 && d.in_channels != 3 && d.in_channels != 5)
+        return fail(CNNCRF_EINVAL, "net_create: in_channels must be 1, 3 or 5");
+    if (d.feat_channels < 1 || d.feat_channels > 128)
+        return fail(CNNCRF_EINVAL, "net_create: feat_channels %d outside 1..128", d.feat_channels);
+    if (d.with_pairwise && (d.pw_channels < 1 || d.pw_channels > 128))
+        return fail(CNNCRF_EINVAL, "net_create: pw_channels %d outside 1..128", d.pw_channels);
+    if (d.unary != CNNCRF_UNARY_NEG_SOFTMAX && d.unary != CNNCRF_UNARY_ONE_MINUS_DOT)
+        return fail(CNNCRF_EINVAL, "net_create: unary %d", d.unary);
+    if (d.precision != CNNCRF_FP32 && d.precision != CNNCRF_BF16)
+        return fail(CNNCRF_EINVAL, "net_create: precision %d", d.precision);
+    auto *net = new cnncrf_net;
+    net->d = d;
+    build_layers(net);
+    int loss = 0;
+    for (auto &L : net->feat) loss += L.kh - 1;
+    if (loss % 2) {
+        delete net;
+        return fail(CNNCRF_EINVAL, "net_create: receptive-field loss %d is odd", loss);
+    }
+    net->pad = loss / 2;
+    if (d.with_pairwise && net->pad < 2) {
+        delete net;
+        return fail(CNNCRF_EINVAL, "net_create: pairwise net needs padding >= 2");
+    }
+    net->n = n, net->h = h, net->w = w;
+    net->H = h - 2 * net->pad, net->W = w - 2 * net->pad;
+    if (net->H < 1 || net->W < 1) {
+        delete net;
+        return fail(CNNCRF_ESHAPE, "net_create: padded input %dx%d smaller than the receptive field", w, h);
+    }
+    *out = net;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_destroy(cnncrf_net_t net)
+{
+    delete net;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_set_stream(cnncrf_net_t net, cnncrf_stream_t stream)
+{
+    if (!net) return fail(CNNCRF_EINVAL, "null net");
+    net->st = (cudaStream_t)stream;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step, int rect_corr,
+                    float *d_unary_out, float *d_pairwise_out)
+{
+    clear_error();
+    if (!net) return fail(CNNCRF_EINVAL, "null net");
+    if (rect_corr != 0) return fail(CNNCRF_EUNSUPPORTED, "rect_corr != 0 is not built");
+    int ic = net->d.in_channels, h = net->h, w = net->w, H = net->H, W = net->W;
+    size_t np = (size_t)h * w;
+    for (int s = 0; s < 2; ++s) CNNCRF_TRY(net->norm[s].reserve(np * ic * sizeof(float)));
+    size_t amax = 0;
+    {
+        int ch = h, cw = w;
+        for (auto &L : net->feat) {
+            ch -= L.kh - 1, cw -= L.kw - 1;
+            amax = std::max(amax, (size_t)ch * cw * L.cout);
+        }
+    }
+    for (int s = 0; s < 2; ++s)
+        for (int b = 0; b < 2; ++b) CNNCRF_TRY(net->act[s][b].reserve(amax * sizeof(float)));
+    CNNCRF_TRY(net->scratch.reserve(k::normalize_scratch_bytes(h)));
+    if (net->d.with_pairwise) {
+        int P = net->d.pw_channels;
+        CNNCRF_TRY(net->pwa.reserve((size_t)(H + 2) * (W + 2) * P * sizeof(float)));
+        CNNCRF_TRY(net->pwb.reserve((size_t)H * W * P * sizeof(float)));
+        if (d_pairwise_out) {
+            net->pwout = d_pairwise_out;
+        } else {
+            CNNCRF_TRY(net->pw_own.reserve((size_t)2 * H * W * sizeof(float)));
+            net->pwout = net->pw_own.as<float>();
+        }
+    }
+    if (net->d.precision == CNNCRF_BF16) {
+        // tensor-core path buffers are sized on first use
+    }
+    CNNCRF_TRY(net->set_disparities(min_disp, max_disp, step, d_unary_out));
+    net->inited = true;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_set_param(cnncrf_net_t net, int index, const float *h_data, const int64_t *shape, int ndim)
+{
+    clear_error();
+    if (!net || !h_data || !shape) return fail(CNNCRF_EINVAL, "set_param: null argument");
+    int64_t s[4];
+    int nd;
+    CNNCRF_TRY(net->expected_shape(index, s, &nd));
+    // a 1-D bias may arrive as (C,) ; a filter must match (co, ci, kh, kw)
+    bool ok = ndim == nd;
+    for (int i = 0; ok && i < nd; ++i) ok = shape[i] == s[i];
+    if (!ok) {
+        std::string got, want;
+        for (int i = 0; i < ndim; ++i) got += std::to_string(shape[i]) + " ";
+        for (int i = 0; i < nd; ++i) want += std::to_string(s[i]) + " ";
+        return fail(CNNCRF_ESHAPE, "arr_%d: loaded shape (%s) but the layer needs (%s)", index, got.c_str(),
+                    want.c_str());
+    }
+    size_t cnt = 1;
+    for (int i = 0; i < nd; ++i) cnt *= (size_t)s[i];
+    net->host[index].assign(h_data, h_data + cnt);
+    net->have[index] = 1;
+    return net->upload(index);
+}
+
+int cnncrf_net_set_all_params(cnncrf_net_t net, const char *npz_path)
+{
+    clear_error();
+    if (!net || !npz_path) return fail(CNNCRF_EINVAL, "set_all_params: null argument");
+    for (int i = 0; i < net->num_params(); ++i) {
+        NpyArray a;
+        CNNCRF_TRY(npz_load(npz_path, "arr_" + std::to_string(i), &a));
+        CNNCRF_TRY(cnncrf_net_set_param(net, i, a.data.data(), a.shape.data(), (int)a.shape.size()));
+    }
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_num_params(cnncrf_net_t net, int *count)
+{
+    if (!net || !count) return fail(CNNCRF_EINVAL, "null argument");
+    *count = net->num_params();
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_param_shape(cnncrf_net_t net, int index, int64_t shape[4], int *ndim)
+{
+    if (!net || !shape || !ndim) return fail(CNNCRF_EINVAL, "null argument");
+    return net->expected_shape(index, shape, ndim);
+}
+
+int cnncrf_net_init_xavier(cnncrf_net_t net, uint64_t seed)
+{
+    clear_error();
+    if (!net) return fail(CNNCRF_EINVAL, "null net");
+    for (int i = 0; i < net->num_params(); ++i) {
+        int64_t s[4];
+        int nd;
+        CNNCRF_TRY(net->expected_shape(i, s, &nd));
+        std::vector<float> v;
+        if (nd == 1) {
+            v.assign((size_t)s[0], 0.0f);
+        } else {
+            v.resize((size_t)(s[0] * s[1] * s[2] * s[3]));
+            cnncrf_xavier_fill(v.data(), (int)s[0], (int)s[1], (int)s[2], (int)s[3], seed, i);
+        }
+        CNNCRF_TRY(cnncrf_net_set_param(net, i, v.data(), s, nd));
+    }
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_set_disparities(cnncrf_net_t net, float min_disp, float max_disp, float step, float *d_out)
+{
+    clear_error();
+    if (!net) return fail(CNNCRF_EINVAL, "null net");
+    return net->set_disparities(min_disp, max_disp, step, d_out);
+}
+
+int cnncrf_net_num_disparities(cnncrf_net_t net, int *num)
+{
+    if (!net || !num) return fail(CNNCRF_EINVAL, "null argument");
+    *num = net->D;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_predict(cnncrf_net_t net, const float *d_left_rgba, const float *d_right_rgba, float **d_volume)
+{
+    clear_error();
+    if (!net) return fail(CNNCRF_EINVAL, "null net");
+    CNNCRF_TRY(net->predict(d_left_rgba, d_right_rgba));
+    if (d_volume) *d_volume = net->vol;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_pairwise(cnncrf_net_t net, float **d_pairwise)
+{
+    if (!net || !d_pairwise) return fail(CNNCRF_EINVAL, "null argument");
+    if (!net->d.with_pairwise) return fail(CNNCRF_ESTATE, "net has no pairwise CNN");
+    *d_pairwise = net->pwout;
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_features(cnncrf_net_t net, int side, float *d_out)
+{
+    if (!net || !d_out || side < 0 || side > 1) return fail(CNNCRF_EINVAL, "features: bad argument");
+    if (!net->feats[side]) return fail(CNNCRF_ESTATE, "features: no prediction yet");
+    CNNCRF_CUDA(cudaMemcpyAsync(d_out, net->feats[side], sizeof(float) * (size_t)net->H * net->W * net->d.feat_channels,
+                                cudaMemcpyDeviceToDevice, net->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_net_padding(cnncrf_net_t net, int *pad)
+{
+    if (!net || !pad) return fail(CNNCRF_EINVAL, "null argument");
+    *pad = net->pad;
+    return CNNCRF_OK;
+}
+
+} // extern "C"

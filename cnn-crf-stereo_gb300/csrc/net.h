@@ -1,0 +1,48 @@
+// net.h -- the StereoNet / ColorStereoNet object behind cnncrf_net_t.
+#pragma once
+
+#include <vector>
+
+#include "common.h"
+
+struct cnncrf_net {
+    struct Layer {
+        int cin, cout, kh, kw, act, wslot, bslot;
+        cnncrf::DevBuf wt;   // FP32 [K][128] flipped / transposed / padded
+        cnncrf::DevBuf bias; // FP32 [128]
+        cnncrf::DevBuf wt16; // BF16 [Npad][taps][Cpad] K-major, for the tensor-core path
+    };
+
+    cnncrf_net_desc d{};
+    int n = 1, h = 0, w = 0, pad = 0, H = 0, W = 0;
+    cudaStream_t st = nullptr;
+    std::vector<Layer> feat, pw;
+    std::vector<std::vector<float>> host;
+    std::vector<char> have;
+
+    // disparities (StereoCorrelation state)
+    std::vector<float> list;
+    cnncrf::DevBuf d_list;
+    int D = 0;
+    bool interp = false, force_interp = false;
+    int omin = 0, omax = 0;
+    float *vol = nullptr;
+    cnncrf::DevBuf vol_own;
+    float *pwout = nullptr;
+    cnncrf::DevBuf pw_own;
+
+    // activations
+    cnncrf::DevBuf norm[2], act[2][2], pwa, pwb, scratch;
+    cnncrf::DevBuf act16[2][2], feat32[2];
+    float *feats[2] = {nullptr, nullptr};
+    bool inited = false;
+
+    int num_params() const { return (int)host.size(); }
+    int expected_shape(int i, int64_t s[4], int *nd) const;
+    int upload(int slot);
+    int predict(const float *left, const float *right);
+    int predict_fp32(const float *left, const float *right);
+    int predict_bf16(const float *left, const float *right);
+    int pairwise_fp32();
+    int set_disparities(float mn, float mx, float step, float *d_out);
+};

@@ -1,0 +1,431 @@
+// stereo.cpp -- the Stereo orchestrator behind cnncrf_stereo_t: buffers,
+// lazy net construction, the CRF call, label remap and the TV/Huber
+// refinement, all enqueued on one stream.
+//
+// Reference: stereo/stereo.cpp (initialize 64-105, setColorImages 117-126,
+// computeSlackPropagation 129-162, computeArgMax 164-177, computeVolume
+// 179-318, fuseTHuberQuadFit 388-404) and cuda::fuseTHuberQuadFit
+// (stereo/stereo.cu:1113-1170).
+#include <cmath>
+#include <string>
+
+#include "common.h"
+#include "kernels.h"
+#include "net.h"
+
+using namespace cnncrf;
+
+struct cnncrf_stereo {
+    cnncrf_stereo_options o{};
+    cudaStream_t st = nullptr;
+    int W = 0, H = 0, depth = 0;
+    float dmin = 0, dstep = 1, dmax = 0;
+    bool inited = false;
+    int matching = CNNCRF_MATCH_CENSUS;
+    int num_layers = 3; // stereo/stereo.cpp:103
+    std::string param_base = "params";
+    bool xavier = false;
+    uint64_t seed = 0;
+    int with_xy = 0;
+    DevBuf img[2], padded[2], warped, warped_pad, vol, pw, out, labels, out_, out0, qf, p, q, vol3;
+    cnncrf_net_t net = nullptr;
+    cnncrf_slackprop_t solver = nullptr;
+    double lb = 0.0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool ev_rec[4] = {false, false, false, false};
+
+    ~cnncrf_stereo()
+    {
+        destroy_net();
+        if (solver) cnncrf_slackprop_destroy(solver);
+        for (auto &e : ev)
+            if (e) cudaEventDestroy(e);
+    }
+    void destroy_net()
+    {
+        if (net) cnncrf_net_destroy(net);
+        net = nullptr;
+    }
+    bool pairwise() const
+    {
+        return matching == CNNCRF_MATCH_COLORCNN_PAIRWISE || matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
+    }
+    int record(int i)
+    {
+        if (!ev[i]) CNNCRF_CUDA(cudaEventCreate(&ev[i]));
+        CNNCRF_CUDA(cudaEventRecord(ev[i], st));
+        ev_rec[i] = true;
+        return CNNCRF_OK;
+    }
+    int build_net();
+    int compute_volume(int lr);
+};
+
+static int log2i(int num) // stereo/stereo.cpp:56-62
+{
+    int r = 0;
+    while (num >>= 1) ++r;
+    return r;
+}
+
+int cnncrf_stereo::build_net()
+{
+    if (matching == CNNCRF_MATCH_CENSUS)
+        return fail(CNNCRF_EUNSUPPORTED, "CENSUS matching is not on the CNN path and is not built");
+    if (matching == CNNCRF_MATCH_CONCATCNN || matching == CNNCRF_MATCH_CONCATCNN_PAIRWISE)
+        return fail(CNNCRF_EUNSUPPORTED, "ConcatStereoNet is not compiled in the reference either");
+    bool gray = matching == CNNCRF_MATCH_GRAYCNN || matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
+    if (o.topology == CNNCRF_TOPO_REF && num_layers != 3 && num_layers != 5 && num_layers != 7)
+        return fail(CNNCRF_EINVAL, "Only {3,5,7} layers are allowed"); // stereo/stereo.cpp:198-202
+    cnncrf_net_desc d{};
+    d.num_layers = num_layers;
+    d.topology = o.topology;
+    d.in_channels = gray ? 1 : (with_xy ? 5 : 3);
+    d.feat_channels = o.feat_channels;
+    d.unary = o.unary;
+    d.precision = o.precision;
+    d.with_pairwise = pairwise() ? 1 : 0;
+    d.pw_channels = o.pw_channels;
+    int loss = 2 + (num_layers - 1) * (o.topology == CNNCRF_TOPO_REF ? 1 : 2);
+    int pad = loss / 2;
+    CNNCRF_TRY(cnncrf_net_create(&net, &d, 1, H + 2 * pad, W + 2 * pad));
+    CNNCRF_TRY(cnncrf_net_set_stream(net, (cnncrf_stream_t)st));
+    net->force_interp = false;
+    CNNCRF_TRY(cnncrf_net_init(net, dmin, dmax, dstep, 0, vol.as<float>(), pairwise() ? pw.as<float>() : nullptr));
+    if (xavier) CNNCRF_TRY(cnncrf_net_init_xavier(net, seed));
+    else CNNCRF_TRY(cnncrf_net_set_all_params(net, (param_base + ".npz").c_str())); // stereo/stereo.cpp:188
+    size_t pb = sizeof(float) * 4 * (size_t)(W + 2 * pad) * (H + 2 * pad);
+    for (int s = 0; s < 2; ++s) CNNCRF_TRY(padded[s].reserve(pb));
+    CNNCRF_TRY(warped_pad.reserve(pb));
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo::compute_volume(int lr)
+{
+    if (!inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
+    if (matching == CNNCRF_MATCH_LOAD) return CNNCRF_OK;
+    if (!net) {
+        int rc = build_net();
+        if (rc != CNNCRF_OK) {
+            destroy_net();
+            return rc;
+        }
+    }
+    net->force_interp = false;
+    float mn = lr ? dmin : -dmax, mx = lr ? dmax : -dmin;
+    CNNCRF_TRY(net->set_disparities(mn, mx, dstep, vol.as<float>()));
+    if (net->D != depth)
+        return fail(CNNCRF_ESHAPE, "Size of provided cost-volume is not correct! disparities do not match! Given size = %d should be %d",
+                    depth, net->D);
+    int a = lr ? 0 : 1;
+    CNNCRF_TRY(k::pad_rgba(img[a].as<float>(), W, H, net->pad, padded[0].as<float>(), st));
+    CNNCRF_TRY(k::pad_rgba(img[1 - a].as<float>(), W, H, net->pad, padded[1].as<float>(), st));
+    return net->predict(padded[0].as<float>(), padded[1].as<float>());
+}
+
+extern "C" {
+
+int cnncrf_stereo_default_options(cnncrf_stereo_options *o)
+{
+    if (!o) return fail(CNNCRF_EINVAL, "null options");
+    o->precision = CNNCRF_FP32;
+    o->unary = CNNCRF_UNARY_NEG_SOFTMAX;
+    o->topology = CNNCRF_TOPO_REF;
+    o->feat_channels = 100;
+    o->pw_channels = 64;
+    o->ref_depth_rounding = 1;
+    o->crf_shape = CNNCRF_RHO_STEP;
+    o->crf_slack = 0.5f;
+    o->huber_eps = 0.1f;
+    o->refine_interp = 0;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_create(cnncrf_stereo_t *s, const cnncrf_stereo_options *opt)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null argument");
+    auto *st = new cnncrf_stereo;
+    if (opt) st->o = *opt;
+    else cnncrf_stereo_default_options(&st->o);
+    *s = st;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_destroy(cnncrf_stereo_t s)
+{
+    delete s;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_stream(cnncrf_stereo_t s, cnncrf_stream_t stream)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    s->st = (cudaStream_t)stream;
+    if (s->net) cnncrf_net_set_stream(s->net, stream);
+    if (s->solver) cnncrf_slackprop_set_stream(s->solver, stream);
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_initialize(cnncrf_stereo_t s, int width, int height, float disp_min, float disp_step,
+                             float disp_max)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (width < 1 || height < 1) return fail(CNNCRF_EINVAL, "initialize: bad size %dx%d", width, height);
+    if (!(disp_step > 0.0f)) return fail(CNNCRF_EINVAL, "initialize: disp_step must be > 0");
+    int depth = (int)((disp_max - disp_min) / disp_step + 1); // stereo/stereo.cpp:71
+    if (depth < 1) return fail(CNNCRF_EINVAL, "initialize: empty disparity range");
+    if (s->o.ref_depth_rounding) depth = std::min(256, 1 << (log2i(depth - 1) + 1)); // :72
+    s->W = width, s->H = height, s->depth = depth;
+    s->dmin = disp_min, s->dstep = disp_step;
+    s->dmax = disp_min + (depth - 1) * disp_step; // :73
+    size_t n = (size_t)width * height;
+    for (int i = 0; i < 2; ++i) CNNCRF_TRY(s->img[i].reserve(n * 4 * sizeof(float)));
+    CNNCRF_TRY(s->warped.reserve(n * 4 * sizeof(float)));
+    CNNCRF_TRY(s->vol.reserve(n * depth * sizeof(float)));
+    CNNCRF_TRY(s->pw.reserve(2 * n * sizeof(float)));
+    CNNCRF_TRY(s->out.reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->labels.reserve(n * sizeof(int32_t)));
+    CNNCRF_TRY(s->out_.reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->out0.reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->qf.reserve(2 * n * sizeof(float)));
+    CNNCRF_TRY(s->p.reserve(2 * n * sizeof(float)));
+    CNNCRF_TRY(s->q.reserve(2 * n * sizeof(float)));
+    CNNCRF_TRY(s->vol3.reserve(3 * n * sizeof(float)));
+    CNNCRF_CUDA(cudaMemsetAsync(s->pw.get(), 0, 2 * n * sizeof(float), s->st));
+    s->destroy_net();
+    if (s->solver) {
+        cnncrf_slackprop_destroy(s->solver);
+        s->solver = nullptr;
+    }
+    s->inited = true;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_matching_function(cnncrf_stereo_t s, int matching)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (matching < 0 || matching > CNNCRF_MATCH_LOAD) return fail(CNNCRF_EINVAL, "unknown matching %d", matching);
+    if (matching != s->matching) s->destroy_net();
+    s->matching = matching;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_num_layers(cnncrf_stereo_t s, int num_layers)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    s->num_layers = num_layers;
+    s->destroy_net(); // stereo/stereo.cpp:354-358
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_parameter_file(cnncrf_stereo_t s, const char *base_name)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (base_name) {
+        s->param_base = base_name;
+        s->xavier = false;
+    } else {
+        s->xavier = true;
+    }
+    s->destroy_net(); // stereo/stereo.cpp:360-364
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_xavier_seed(cnncrf_stereo_t s, uint64_t seed)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    s->xavier = true;
+    s->seed = seed;
+    s->destroy_net();
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_with_xy(cnncrf_stereo_t s, int with_xy)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (with_xy != s->with_xy) s->destroy_net();
+    s->with_xy = with_xy ? 1 : 0;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_color_images(cnncrf_stereo_t s, const float *h_left, const float *h_right)
+{
+    if (!s || !h_left || !h_right) return fail(CNNCRF_EINVAL, "set_color_images: null argument");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "setColorImages before initialize");
+    size_t b = sizeof(float) * 4 * (size_t)s->W * s->H;
+    CNNCRF_CUDA(cudaMemcpyAsync(s->img[0].get(), h_left, b, cudaMemcpyHostToDevice, s->st));
+    CNNCRF_CUDA(cudaMemcpyAsync(s->img[1].get(), h_right, b, cudaMemcpyHostToDevice, s->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_set_color_images_device(cnncrf_stereo_t s, const float *d_left, const float *d_right)
+{
+    if (!s || !d_left || !d_right) return fail(CNNCRF_EINVAL, "set_color_images_device: null argument");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "setColorImages before initialize");
+    size_t b = sizeof(float) * 4 * (size_t)s->W * s->H;
+    CNNCRF_CUDA(cudaMemcpyAsync(s->img[0].get(), d_left, b, cudaMemcpyDeviceToDevice, s->st));
+    CNNCRF_CUDA(cudaMemcpyAsync(s->img[1].get(), d_right, b, cudaMemcpyDeviceToDevice, s->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_compute_volume(cnncrf_stereo_t s, int lr)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
+    CNNCRF_TRY(s->record(0));
+    CNNCRF_TRY(s->compute_volume(lr));
+    return s->record(1);
+}
+
+int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C2, float delta, int iterations,
+                                            float alpha, float beta, float lambda_reg, int lr)
+{
+    clear_error();
+    (void)alpha, (void)beta;
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "computeSlackPropagation before initialize");
+    if (!s->pairwise() && s->matching != CNNCRF_MATCH_LOAD)
+        return fail(CNNCRF_EUNSUPPORTED,
+                    "CRF with image-gradient edge weights (non-pairwise matching) is not built");
+    CNNCRF_TRY(s->record(0));
+    CNNCRF_TRY(s->compute_volume(lr));
+    CNNCRF_TRY(s->record(1));
+    size_t n = (size_t)s->W * s->H;
+    CNNCRF_TRY(k::scale(s->pw.as<float>(), (long)(2 * n), lambda_reg, s->st)); // stereo/stereo.cpp:136-137
+    if (!s->solver) {
+        CNNCRF_TRY(cnncrf_slackprop_create(&s->solver));
+        CNNCRF_TRY(cnncrf_slackprop_init(s->solver, s->vol.as<float>(), s->W, s->H, s->depth, s->labels.as<int32_t>()));
+    }
+    cnncrf_slackprop_set_stream(s->solver, (cnncrf_stream_t)s->st);
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "L1", C1));
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "L2", C2));
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "delta", delta));
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "total_it", iterations));
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "shape", s->o.crf_shape));
+    CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "slack", s->o.crf_slack));
+    CNNCRF_TRY(cnncrf_slackprop_update_w(s->solver, s->pw.as<float>(), s->pw.as<float>() + n));
+    CNNCRF_TRY(cnncrf_slackprop_execute(s->solver));
+    CNNCRF_TRY(cnncrf_slackprop_lower_bound(s->solver, &s->lb));
+    if (lr) CNNCRF_TRY(k::remap(s->out.as<float>(), s->labels.as<int32_t>(), (long)n, s->dmin, s->dstep, s->st));
+    else CNNCRF_TRY(k::remap(s->out.as<float>(), s->labels.as<int32_t>(), (long)n, -s->dmax, s->dstep, s->st));
+    return s->record(2);
+}
+
+int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "computeArgMax before initialize");
+    CNNCRF_TRY(s->record(0));
+    CNNCRF_TRY(s->compute_volume(lr));
+    CNNCRF_TRY(s->record(1));
+    size_t n = (size_t)s->W * s->H;
+    CNNCRF_TRY(k::argmin(s->out.as<float>(), s->vol.as<float>(), (long)n, s->depth, lr ? s->dmin : -s->dmax,
+                         s->dstep, s->st));
+    return s->record(2);
+}
+
+int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, float C, int iterations, int warps)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->net || !s->pairwise())
+        return fail(CNNCRF_ESTATE, "fuseTHuberQuadFit needs a COLORPAIR net that has computed a volume");
+    cnncrf_net *net = s->net;
+    cudaStream_t st = s->st;
+    int W = s->W, H = s->H;
+    size_t n = (size_t)W * H;
+    float lam_c = 1.0f / lambda_reg; // stereo/stereo.cpp:395
+    float step = s->dstep;
+    float hq = (float)((double)step * 0.25), mn = (float)(-(double)step * 0.25);
+    CNNCRF_CUDA(cudaMemsetAsync(s->p.get(), 0, 2 * n * sizeof(float), st));
+    CNNCRF_CUDA(cudaMemsetAsync(s->q.get(), 0, 2 * n * sizeof(float), st));
+    CNNCRF_TRY(k::pad_rgba(s->img[0].as<float>(), W, H, net->pad, s->padded[0].as<float>(), st));
+    for (int w = 0; w < warps; ++w) {
+        CNNCRF_TRY(k::warp_rgba(s->warped.as<float>(), s->img[1].as<float>(), s->out.as<float>(), W, H, st));
+        CNNCRF_TRY(k::pad_rgba(s->warped.as<float>(), W, H, net->pad, s->warped_pad.as<float>(), st));
+        net->force_interp = s->o.refine_interp != 0;
+        CNNCRF_TRY(net->set_disparities(mn, hq, hq, s->vol3.as<float>()));
+        if (net->D != 3) return fail(CNNCRF_ESHAPE, "refinement volume has %d labels, expected 3", net->D);
+        CNNCRF_TRY(net->predict(s->padded[0].as<float>(), s->warped_pad.as<float>()));
+        net->force_interp = false;
+        CNNCRF_TRY(k::tv_fit(s->vol3.as<float>(), s->qf.as<float>(), W, H, step, lam_c, st));
+        CNNCRF_CUDA(cudaMemcpyAsync(s->out0.get(), s->out.get(), n * sizeof(float), cudaMemcpyDeviceToDevice, st));
+        // predict rewrote wx / wy (they alias the pairwise output) without lambda
+        CNNCRF_TRY(k::tv_iterate(s->out.as<float>(), s->out_.as<float>(), s->out0.as<float>(), s->qf.as<float>(),
+                                 s->p.as<float>(), s->q.as<float>(), s->pw.as<float>(), s->pw.as<float>() + n, W, H, C,
+                                 s->o.huber_eps, step, iterations, st));
+    }
+    return s->record(3);
+}
+
+int cnncrf_stereo_get_output(cnncrf_stereo_t s, float *h_out)
+{
+    if (!s || !h_out) return fail(CNNCRF_EINVAL, "null argument");
+    CNNCRF_CUDA(cudaMemcpyAsync(h_out, s->out.get(), sizeof(float) * (size_t)s->W * s->H, cudaMemcpyDeviceToHost, s->st));
+    CNNCRF_CUDA(cudaStreamSynchronize(s->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_get_output_device(cnncrf_stereo_t s, const float **d_out)
+{
+    if (!s || !d_out) return fail(CNNCRF_EINVAL, "null argument");
+    *d_out = s->out.as<float>();
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_get_labels_device(cnncrf_stereo_t s, const int32_t **d_labels)
+{
+    if (!s || !d_labels) return fail(CNNCRF_EINVAL, "null argument");
+    *d_labels = s->labels.as<int32_t>();
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_get_volume_device(cnncrf_stereo_t s, const float **d_volume)
+{
+    if (!s || !d_volume) return fail(CNNCRF_EINVAL, "null argument");
+    *d_volume = s->vol.as<float>();
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_get_weights_device(cnncrf_stereo_t s, const float **d_wx, const float **d_wy)
+{
+    if (!s || !d_wx || !d_wy) return fail(CNNCRF_EINVAL, "null argument");
+    *d_wx = s->pw.as<float>();
+    *d_wy = s->pw.as<float>() + (size_t)s->W * s->H;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_get_depth(cnncrf_stereo_t s, int *depth)
+{
+    if (!s || !depth) return fail(CNNCRF_EINVAL, "null argument");
+    *depth = s->depth;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_lower_bound(cnncrf_stereo_t s, double *lb)
+{
+    if (!s || !lb) return fail(CNNCRF_EINVAL, "null argument");
+    *lb = s->lb;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_stage_times(cnncrf_stereo_t s, float *cnn_ms, float *corr_ms, float *crf_ms, float *refine_ms)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    CNNCRF_CUDA(cudaStreamSynchronize(s->st));
+    float t01 = 0, t12 = 0, t23 = 0;
+    if (s->ev_rec[0] && s->ev_rec[1]) CNNCRF_CUDA(cudaEventElapsedTime(&t01, s->ev[0], s->ev[1]));
+    if (s->ev_rec[1] && s->ev_rec[2]) CNNCRF_CUDA(cudaEventElapsedTime(&t12, s->ev[1], s->ev[2]));
+    if (s->ev_rec[2] && s->ev_rec[3]) CNNCRF_CUDA(cudaEventElapsedTime(&t23, s->ev[2], s->ev[3]));
+    if (cnn_ms) *cnn_ms = t01;
+    if (corr_ms) *corr_ms = 0.0f; // fused into the CNN stage
+    if (crf_ms) *crf_ms = t12;
+    if (refine_ms) *refine_ms = t23;
+    return CNNCRF_OK;
+}
+
+} // extern "C"

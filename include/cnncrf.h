@@ -1,0 +1,327 @@
+/*
+ * cnncrf.h -- C ABI of the GB300-native CNN-CRF stereo hot path (libcnncrf.so).
+ *
+ * Every entry point replaces one call of the reference's C++ API for the path
+ * (VLOGroup/cnn-crf-stereo); the citation above each declaration names it.
+ * Plain pointers, sizes and a cudaStream_t only: no C++ or torch types.
+ *
+ * Conventions
+ *  - Every function returns a cnncrf_status; the reference aborted with
+ *    exit(-1) (stereo/error_util.h:29-52), this library never aborts.  The
+ *    message of the last failure on the calling thread is cnncrf_last_error().
+ *  - "d_" pointers are device pointers, "h_" pointers are host pointers.
+ *  - Images are RGBA float (4 interleaved channels), rows packed (pitch =
+ *    4*width floats) -- the iu::ImageGpu_32f_C4 the reference passes around.
+ *  - Cost volumes are H x W x D floats, D fastest ("NHWC" with C = D), the
+ *    layout of stereo/stereo.cpp:82,219-220 and slack_prop {K,W,H}.
+ *  - Pairwise weights are [2][H][W] floats, channel 0 = wx (edge (y,x)-(y,x+1)),
+ *    channel 1 = wy (edge (y,x)-(y+1,x)), aliasing as in stereo/stereo.cpp:84-86.
+ *  - Handles are not shared between threads; use one handle per host thread.
+ *    Nothing is process-global except the error message (thread-local).
+ *  - All work is enqueued on the stream given to the handle (default: the
+ *    legacy default stream); functions that return host data synchronise it.
+ */
+#ifndef CNNCRF_H
+#define CNNCRF_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CNNCRF_ABI_VERSION 1
+
+typedef struct CUstream_st *cnncrf_stream_t; /* == cudaStream_t */
+
+typedef enum cnncrf_status {
+    CNNCRF_OK = 0,
+    CNNCRF_EINVAL = 1,      /* bad argument (null pointer, negative size, ...) */
+    CNNCRF_ESHAPE = 2,      /* tensor / npz array shape mismatch */
+    CNNCRF_ENOMEM = 3,      /* device or host allocation failed */
+    CNNCRF_ECUDA = 4,       /* CUDA runtime / driver error */
+    CNNCRF_ETIMEOUT = 5,    /* a bounded device wait ran out (kernel error flag) */
+    CNNCRF_EIO = 6,         /* file missing / unreadable / corrupt */
+    CNNCRF_ESTATE = 7,      /* call order violated (e.g. predict before init) */
+    CNNCRF_EUNSUPPORTED = 8 /* valid in the reference, not built here */
+} cnncrf_status;
+
+/* Matching functions; values equal the reference enum (stereo/stereo.h:29-38). */
+typedef enum cnncrf_matching {
+    CNNCRF_MATCH_COLORCNN = 0,
+    CNNCRF_MATCH_GRAYCNN = 1,
+    CNNCRF_MATCH_CONCATCNN = 2,          /* dead code in the reference: EUNSUPPORTED */
+    CNNCRF_MATCH_GRAYCNN_PAIRWISE = 3,
+    CNNCRF_MATCH_COLORCNN_PAIRWISE = 4,  /* "COLORPAIR" on the command line */
+    CNNCRF_MATCH_CONCATCNN_PAIRWISE = 5, /* EUNSUPPORTED */
+    CNNCRF_MATCH_CENSUS = 6,             /* EUNSUPPORTED (not on the CNN path) */
+    CNNCRF_MATCH_LOAD = 7                /* volume supplied by the caller */
+} cnncrf_matching;
+
+typedef enum cnncrf_precision {
+    CNNCRF_FP32 = 0, /* SIMT FP32, bit-exact against the CPU oracle */
+    CNNCRF_BF16 = 1  /* tcgen05 BF16 operands, FP32 accumulation */
+} cnncrf_precision;
+
+typedef enum cnncrf_unary {
+    CNNCRF_UNARY_NEG_SOFTMAX = 0, /* -softmax_d(<fL,fR>) (stereo/stereonet.cpp:136-139,309,318) */
+    CNNCRF_UNARY_ONE_MINUS_DOT = 1 /* 1 - <fL,fR> on L2-normalised features */
+} cnncrf_unary;
+
+typedef enum cnncrf_topology {
+    CNNCRF_TOPO_REF = 0,   /* 3x3 first layer, 2x2 layers after (stereo/stereonet.cpp:69-133) */
+    CNNCRF_TOPO_ALL3X3 = 1 /* every layer 3x3 */
+} cnncrf_topology;
+
+typedef enum cnncrf_pairwise_shape {
+    CNNCRF_RHO_STEP = 0,  /* rho(0)=0, rho(t)=L1 for 1<=|t|<=delta, L2 beyond */
+    CNNCRF_RHO_LINEAR = 1 /* rho(t)=min(L1*|t|, L2) for |t|<=delta, L2 beyond */
+} cnncrf_pairwise_shape;
+
+/* ---------------------------------------------------------------- errors */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *cnncrf_last_error(void);
+/* Library ABI version (CNNCRF_ABI_VERSION). */
+int cnncrf_abi_version(void);
+
+/* ---------------------------------------------------------------- StereoNet */
+
+typedef struct cnncrf_net *cnncrf_net_t;
+
+typedef struct cnncrf_net_desc {
+    int num_layers;    /* feature CNN depth (REF topology: 3, 5 or 7) */
+    int topology;      /* cnncrf_topology */
+    int in_channels;   /* 1 (gray), 3 (RGB) or 5 (RGB + normalised x,y) */
+    int feat_channels; /* 100 in the reference */
+    int unary;         /* cnncrf_unary */
+    int precision;     /* cnncrf_precision */
+    int with_pairwise; /* build the pairwise-weight CNN (COLORPAIR) */
+    int pw_channels;   /* 64 in the reference */
+} cnncrf_net_desc;
+
+/* StereoNet(numLayers, n, c, h, w) (stereo/stereonet.h:30) / ColorStereoNet
+ * (stereo/colorstereonet.h:25).  h, w are the PADDED input size.  Only n = 1. */
+int cnncrf_net_create(cnncrf_net_t *net, const cnncrf_net_desc *desc, int n, int h, int w);
+int cnncrf_net_destroy(cnncrf_net_t net);
+/* Stream all later work of this net is enqueued on. */
+int cnncrf_net_set_stream(cnncrf_net_t net, cnncrf_stream_t stream);
+
+/* StereoNet::initNet(min, max, step, rect_corr, d_unaryOut, d_pairwiseOut)
+ * (stereo/stereonet.h:43-44, stereo/stereonet.cpp:65-182).  d_unary_out is a
+ * caller-owned H x W x D volume (may be NULL: owned internally); d_pairwise_out
+ * a caller-owned [2][H][W] buffer (may be NULL).  rect_corr must be 0. */
+int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step, int rect_corr,
+                    float *d_unary_out, float *d_pairwise_out);
+
+/* StereoNet::setAllParams(npzPath) (stereo/stereonet.cpp:184-227): arrays
+ * arr_0.. in op order, shapes checked (ESHAPE instead of exit(-1),
+ * stereo/operators/operator.cpp:72-79).  Reads STORED and DEFLATE members. */
+int cnncrf_net_set_all_params(cnncrf_net_t net, const char *npz_path);
+
+/* Operator::setParams(h_params) for one array (stereo/operators/operator.cpp:87-102).
+ * index = the arr_<index> slot; shape as in the npz (4-D filter or 1-D bias). */
+int cnncrf_net_set_param(cnncrf_net_t net, int index, const float *h_data, const int64_t *shape,
+                         int ndim);
+/* Number of parameter arrays (filters + biases) the net expects. */
+int cnncrf_net_num_params(cnncrf_net_t net, int *count);
+/* Shape of arr_<index>. */
+int cnncrf_net_param_shape(cnncrf_net_t net, int index, int64_t shape[4], int *ndim);
+/* Xavier-uniform filters from a seeded generator, zero biases (no reference
+ * counterpart: the synthetic-weight workloads use it). */
+int cnncrf_net_init_xavier(cnncrf_net_t net, uint64_t seed);
+
+/* StereoNet::setDisparities(min, max, step, d_out) (stereo/stereonet.cpp:229-248,
+ * stereo/operators/stereocorrelation.cpp:71-144): the list is built as
+ * `for (d = min; d <= max; d += step)` in float. */
+int cnncrf_net_set_disparities(cnncrf_net_t net, float min_disp, float max_disp, float step,
+                               float *d_out);
+int cnncrf_net_num_disparities(cnncrf_net_t net, int *num);
+
+/* ColorStereoNet::predict(d_left, d_right) (stereo/colorstereonet.cpp:38-77):
+ * padded RGBA device images (h x w as created) -> H x W x D unary volume
+ * (H = h - 2*pad, W = w - 2*pad), returned as a non-owned device pointer;
+ * the pairwise weights (if built) land in the pairwise buffer. */
+int cnncrf_net_predict(cnncrf_net_t net, const float *d_left_rgba, const float *d_right_rgba,
+                       float **d_volume);
+/* Device pointer of the [2][H][W] pairwise output (|conv|, before lambda). */
+int cnncrf_net_pairwise(cnncrf_net_t net, float **d_pairwise);
+/* Copy the final feature maps of one side (0 left, 1 right) as FP32
+ * H x W x C (C = feat_channels) into d_out (debug / parity). */
+int cnncrf_net_features(cnncrf_net_t net, int side, float *d_out);
+/* Mirror padding amount the topology needs (stereo/stereo.cpp:204-217). */
+int cnncrf_net_padding(cnncrf_net_t net, int *pad);
+
+/* ---------------------------------------------------------------- operators */
+
+/* StereoCorrelation::forward(d_input0, d_input1, d_disparities, d_output, in,
+ * ic, ih, iw, lenDisps, layout, rectCorr) (stereo/operators/stereocorrelation.cpp:146-152,
+ * stereo/operators/stereocorrelation.cu:358-408): NCHW feature inputs, NHWC
+ * output, disparity list given as stored by the reference (negated values).
+ * The fractional-disparity (interpolating) kernel is chosen exactly when the
+ * reference chooses it.  FP32, rect_corr must be 0. */
+int cnncrf_correlation_forward(const float *d_input0, const float *d_input1,
+                               const float *h_disparities, float *d_output, int n, int c, int h,
+                               int w, int num_disps, cnncrf_stream_t stream);
+
+/* ---------------------------------------------------------------- CRF */
+
+typedef struct cnncrf_crf_options {
+    float L1;       /* ops["L1"] */
+    float L2;       /* ops["L2"] */
+    float delta;    /* ops["delta"]: rho's window, integer 1..8 */
+    int total_it;   /* ops["total_it"]: horizontal+vertical passes */
+    int shape;      /* cnncrf_pairwise_shape */
+    float slack;    /* fraction of a subproblem's slack handed over per pass, (0,1] */
+} cnncrf_crf_options;
+
+/* Defaults: L1 1, L2 12, delta 2, total_it 4 (stereo/stereo_img.cpp:78-81), STEP shape, slack 0.5. */
+int cnncrf_crf_default_options(cnncrf_crf_options *opt);
+
+/* Device workspace one solve needs (bytes). */
+int cnncrf_crf_workspace_size(int width, int height, int depth, size_t *bytes);
+
+/* slack_prop_2D_alg: init(C{K,W,H}, sols) + ops + update_W(wx, wy) + execute()
+ * + LB() (call sites stereo/stereo.cpp:140-154, stereo/operators/slackprop.cpp:111-139).
+ * d_cost: H x W x D; d_wx, d_wy: H x W (>= 0); d_labels: H x W int32 output.
+ * lower_bound: host, may be NULL (the FP64 dual bound after the last pass).
+ * d_workspace >= cnncrf_crf_workspace_size bytes, 256-byte aligned. */
+int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, int width,
+                     int height, int depth, const cnncrf_crf_options *opt, int32_t *d_labels,
+                     double *lower_bound, void *d_workspace, size_t workspace_bytes,
+                     cnncrf_stream_t stream);
+
+/* Object form of the same solver, mirroring slack_prop_2D_alg's members. */
+typedef struct cnncrf_slackprop *cnncrf_slackprop_t;
+int cnncrf_slackprop_create(cnncrf_slackprop_t *sp);
+int cnncrf_slackprop_destroy(cnncrf_slackprop_t sp);
+int cnncrf_slackprop_set_stream(cnncrf_slackprop_t sp, cnncrf_stream_t stream);
+/* init(ndarray_ref<float,3> C{K,W,H}, ndarray_ref<int,2> sols) */
+int cnncrf_slackprop_init(cnncrf_slackprop_t sp, const float *d_cost, int width, int height,
+                          int depth, int32_t *d_labels);
+/* ops["L1"|"L2"|"delta"|"total_it"|"slack"|"shape"] = value */
+int cnncrf_slackprop_set_op(cnncrf_slackprop_t sp, const char *name, double value);
+/* update_W(wx, wy) */
+int cnncrf_slackprop_update_w(cnncrf_slackprop_t sp, const float *d_wx, const float *d_wy);
+/* execute() */
+int cnncrf_slackprop_execute(cnncrf_slackprop_t sp);
+/* LB() */
+int cnncrf_slackprop_lower_bound(cnncrf_slackprop_t sp, double *lb);
+/* get_C1(): device pointer to the H x W x D unary share of the horizontal
+ * subproblem after the last pass (the reparametrised volume). */
+int cnncrf_slackprop_get_c1(cnncrf_slackprop_t sp, float **d_c1);
+
+/* cuda::remapSolution (stereo/stereo.cu:841-850,1229-1246): disp = label*step + min. */
+int cnncrf_remap_solution(float *d_out, const int32_t *d_labels, int width, int height,
+                          float disp_min, float disp_step, cnncrf_stream_t stream);
+
+/* ---------------------------------------------------------------- refinement */
+
+/* warp_image_kernel (stereo/stereo.cu:830-839): out(x,y) = in(floor(x+0.5-u), y),
+ * index clamped to the image (point sampling, clamp addressing). */
+int cnncrf_warp_image(float *d_out_rgba, const float *d_in_rgba, const float *d_u, int width,
+                      int height, cnncrf_stream_t stream);
+/* do_fitting_kernel (stereo/stereo.cu:419-442, do_abs = false): H x W x 3
+ * volume -> qf, H x W x 2 interleaved (a, b) like ImageGpu_32f_C2. */
+int cnncrf_tv_fit(const float *d_volume3, float *d_qf, int width, int height, float disp_step,
+                  float lambda_census, cnncrf_stream_t stream);
+/* The inner loop of cuda::fuseTHuberQuadFit (stereo/stereo.cu:1133-1135,1159-1166):
+ * p = q = 0, then `iterations` x (u_ = u; primal; dual) with tau = sigma = 1/sqrt(8).
+ * d_u, d_u_, d_u0: H x W; d_qf, d_p, d_q: H x W x 2; huber_eps = 0.1 in the
+ * reference (stereo/stereo.cu:792). */
+int cnncrf_tv_iterate(float *d_u, float *d_u_, const float *d_u0, const float *d_qf, float *d_p,
+                      float *d_q, const float *d_wx, const float *d_wy, int width, int height,
+                      float C, float huber_eps, float disp_step, int iterations,
+                      cnncrf_stream_t stream);
+
+/* ---------------------------------------------------------------- Stereo */
+
+typedef struct cnncrf_stereo *cnncrf_stereo_t;
+
+typedef struct cnncrf_stereo_options {
+    int precision;       /* cnncrf_precision (default FP32) */
+    int unary;           /* cnncrf_unary (default NEG_SOFTMAX) */
+    int topology;        /* cnncrf_topology (default REF) */
+    int feat_channels;   /* 100 */
+    int pw_channels;     /* 64 */
+    int ref_depth_rounding; /* 1: depth -> min(256, next pow2) as stereo/stereo.cpp:71-73 */
+    int crf_shape;       /* cnncrf_pairwise_shape (default STEP) */
+    float crf_slack;     /* default 0.5 */
+    float huber_eps;     /* default 0.1 (stereo/stereo.cu:792) */
+    int refine_interp;   /* 0: the reference's 3-label dispatch; 1: always interpolate */
+} cnncrf_stereo_options;
+
+int cnncrf_stereo_default_options(cnncrf_stereo_options *opt);
+/* Stereo() (stereo/stereo.h:43) */
+int cnncrf_stereo_create(cnncrf_stereo_t *s, const cnncrf_stereo_options *opt);
+int cnncrf_stereo_destroy(cnncrf_stereo_t s);
+int cnncrf_stereo_set_stream(cnncrf_stereo_t s, cnncrf_stream_t stream);
+/* Stereo::initialize(size, disp_min, disp_step, disp_max) (stereo/stereo.cpp:64-105) */
+int cnncrf_stereo_initialize(cnncrf_stereo_t s, int width, int height, float disp_min,
+                             float disp_step, float disp_max);
+/* setMatchingFunction / setNumLayers / setParameterFile / setWithXy
+ * (stereo/stereo.h:52-54,82).  The parameter file gets ".npz" appended
+ * (stereo/stereo.cpp:188).  Pass NULL to keep Xavier weights (seed). */
+int cnncrf_stereo_set_matching_function(cnncrf_stereo_t s, int matching);
+int cnncrf_stereo_set_num_layers(cnncrf_stereo_t s, int num_layers);
+int cnncrf_stereo_set_parameter_file(cnncrf_stereo_t s, const char *base_name);
+int cnncrf_stereo_set_xavier_seed(cnncrf_stereo_t s, uint64_t seed);
+int cnncrf_stereo_set_with_xy(cnncrf_stereo_t s, int with_xy);
+/* Stereo::setColorImages(ImageCpu_32f_C4 x2) (stereo/stereo.cpp:117-126): host RGBA. */
+int cnncrf_stereo_set_color_images(cnncrf_stereo_t s, const float *h_left_rgba,
+                                   const float *h_right_rgba);
+/* Same with device RGBA buffers (device-to-device copy). */
+int cnncrf_stereo_set_color_images_device(cnncrf_stereo_t s, const float *d_left_rgba,
+                                          const float *d_right_rgba);
+/* Stereo::computeVolume(lr) (stereo/stereo.cpp:179-318) */
+int cnncrf_stereo_compute_volume(cnncrf_stereo_t s, int lr);
+/* Stereo::computeSlackPropagation(C1, C2, delta, iterations, alpha, beta,
+ * lambda, lr) (stereo/stereo.cpp:129-162).  alpha/beta only matter for the
+ * CENSUS edge weights, which are not built (they are ignored). */
+int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C2, float delta,
+                                            int iterations, float alpha, float beta,
+                                            float lambda_reg, int lr);
+/* Stereo::computeArgMax(lr) (stereo/stereo.cpp:164-177; arg_min_kernel stereo/stereo.cu:348-370) */
+int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr);
+/* Stereo::fuseTHuberQuadFit(lambda, C, iterations, warps) (stereo/stereo.cpp:388-404) */
+int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, float C,
+                                       int iterations, int warps);
+/* Stereo::getOutput() (stereo/stereo.cpp:412-417): H x W float disparity. */
+int cnncrf_stereo_get_output(cnncrf_stereo_t s, float *h_out);
+int cnncrf_stereo_get_output_device(cnncrf_stereo_t s, const float **d_out);
+/* Stereo::getIntegerOutput() (stereo/stereo.cpp:439-442) */
+int cnncrf_stereo_get_labels_device(cnncrf_stereo_t s, const int32_t **d_labels);
+/* Stereo::getVolume() (stereo/stereo.cpp:419-423) */
+int cnncrf_stereo_get_volume_device(cnncrf_stereo_t s, const float **d_volume);
+/* Stereo::getWx / getWy (stereo/stereo.cpp:425-437): lambda-scaled weights. */
+int cnncrf_stereo_get_weights_device(cnncrf_stereo_t s, const float **d_wx, const float **d_wy);
+/* Stereo::getDepth() (stereo/stereo.cpp:444-447) */
+int cnncrf_stereo_get_depth(cnncrf_stereo_t s, int *depth);
+/* The solver's LB() after the last computeSlackPropagation. */
+int cnncrf_stereo_lower_bound(cnncrf_stereo_t s, double *lb);
+/* Device time of the stages of the last run (CUDA events, ms): cnn, corr,
+ * crf, refine; any may be NULL. */
+int cnncrf_stereo_stage_times(cnncrf_stereo_t s, float *cnn_ms, float *corr_ms, float *crf_ms,
+                              float *refine_ms);
+
+/* ---------------------------------------------------------------- instrumentation
+ * (no counterpart in the reference, which timed whole stages with
+ * iu::IuCudaTimer when verbose, stereo/stereonet.cpp:258-315) */
+
+/* Number of kernels this library has launched in the process. */
+int cnncrf_kernel_launches(uint64_t *count);
+/* While enabled, every launch is bracketed by CUDA events on its stream. */
+int cnncrf_profile_enable(int enable);
+int cnncrf_profile_reset(void);
+/* Launches and summed device time (ms) of one kernel since the last reset;
+ * synchronises on the recorded events. */
+int cnncrf_profile_query(const char *kernel, int *launches, double *total_ms);
+/* Newline-separated names of the kernels timed since the last reset. */
+int cnncrf_profile_kernels(char *buf, size_t len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CNNCRF_H */
