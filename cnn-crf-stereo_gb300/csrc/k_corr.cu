@@ -80,8 +80,10 @@ __global__ void __launch_bounds__(256)
                     int xb = (int)(w2 + 1.0f);
                     float num = w2 - (float)xa;
                     float den = (float)xb - (float)xa;
-                    const float *b0 = sr + (min(xa, W - 1) - xlo) * CS;
-                    const float *b1 = sr + (min(xb, W - 1) - xlo) * CS;
+                    // taps stay inside the staged band [xlo, xhi] (float rounding of
+                    // w2 + 1 cannot step past it); xhi <= W - 1 also clamps the right edge
+                    const float *b0 = sr + (min(max(xa, xlo), xhi) - xlo) * CS;
+                    const float *b1 = sr + (min(max(xb, xlo), xhi) - xlo) * CS;
                     for (int c = 0; c < C; ++c) {
                         float y0 = b0[c], y1 = b1[c];
                         float it = y0 + ((y1 - y0) * num) / den;

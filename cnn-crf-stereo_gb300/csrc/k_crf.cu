@@ -168,7 +168,12 @@ __global__ void __launch_bounds__(64)
     for (int x = W - 1; x >= 0; --x) {
         const long pix = row + x;
         load_vec<P>(theta + pix * D, lane, D, th);
-        if (!first) load_vec<P>(phi + pix * D, lane, D, ph);
+        if (!first) {
+            load_vec<P>(phi + pix * D, lane, D, ph);
+        } else {
+#pragma unroll
+            for (int r = 0; r < P; ++r) ph[r] = 0.0f; // phi starts at zero
+        }
         load_vec<P>(Lbuf + pix * D, lane, D, Lx);
 #pragma unroll
         for (int r = 0; r < P; ++r) {
@@ -352,6 +357,7 @@ int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H,
     Layout l = layout(W, H, D);
     if (ws_bytes < l.total) return fail(CNNCRF_EINVAL, "crf: workspace %zu < %zu bytes", ws_bytes, l.total);
     if (((uintptr_t)ws & 255) != 0) return fail(CNNCRF_EINVAL, "crf: workspace not 256-byte aligned");
+    if (((uintptr_t)cost & 15) != 0) return fail(CNNCRF_EINVAL, "crf: cost volume not 16-byte aligned");
     char *w = (char *)ws;
     if (iters <= 0) {
         {
