@@ -42,19 +42,25 @@ WORKLOAD = dict(name="kitti1242x375_d128", W=1242, H=375, D=128, layers=7, topol
 
 
 def conv_flops(W, H, layers=7, feat=100, ic=3, pw=64, k=3):
-    """Algorithmic FLOPs of the convs of one pair: 2 x output pixels x Cout x
-    (kh kw Cin), summed over the layers of both sides + the pairwise net."""
+    """Algorithmic FLOPs of the convolutions of one pair, 2 x output pixels x
+    Cout x (kh kw Cin) per layer, both sides.  Returns (tensor-core layers:
+    feature layers 2..L and the pairwise 64->64 conv; SIMT layers: feature
+    layer 1, pairwise 3->64 conv and the 1x1 head)."""
     p = layers  # all-3x3: padding = number of layers
     h, w = H + 2 * p, W + 2 * p
-    f = 0
+    tc = simt = 0
     cin = ic
-    for _ in range(layers):
+    for l in range(layers):
         h, w = h - (k - 1), w - (k - 1)
-        f += 2 * h * w * feat * k * k * cin
+        f = 2 * 2 * h * w * feat * k * k * cin
+        if l == 0:
+            simt += f
+        else:
+            tc += f
         cin = feat
-    feat_flops = 2 * f
-    pw_flops = 2 * (H + 2) * (W + 2) * pw * 9 * 3 + 2 * H * W * pw * 9 * pw + 2 * H * W * 2 * pw
-    return feat_flops, pw_flops
+    simt += 2 * (H + 2) * (W + 2) * pw * 9 * 3 + 2 * H * W * 2 * pw
+    tc += 2 * H * W * pw * 9 * pw
+    return tc, simt
 
 
 def crf_bytes_per_pass(W, H, D):
@@ -319,7 +325,7 @@ def main():
         return 0
 
     peaks, peak_src = measured_peaks()
-    feat_f, pw_f = conv_flops(W, H, wl["layers"], wl["feat"], 3, wl["pw"])
+    tc_f, simt_f = conv_flops(W, H, wl["layers"], wl["feat"], 3, wl["pw"])
     conv_name = "conv_tc" if "conv_tc" in prof else "conv_simt"
     kernels = {k: {"launches": n, "total_ms": round(t, 4), "share": None} for k, (n, t) in prof.items()}
     tot = sum(t for _, t in prof.values()) or 1.0
@@ -328,7 +334,8 @@ def main():
     roof = None
     if conv_name in prof:
         n, t = prof[conv_name]
-        achieved = (feat_f + pw_f) * args.steps / (t / 1000.0) / 1e12
+        flops = tc_f if conv_name == "conv_tc" else tc_f + simt_f
+        achieved = flops * args.steps / (t / 1000.0) / 1e12
         if conv_name == "conv_tc":
             roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved,
                     "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],

@@ -9,6 +9,8 @@
 //
 // Tiling: CTA = 128 pixels of one output row x 128 output channels, k-slices
 // of 8 double-buffered in shared memory, 256 threads with 8x8 register tiles.
+#include <cuda_bf16.h>
+
 #include "../../include/cnncrf_fmath.h"
 #include "common.h"
 #include "kernels.h"
@@ -109,14 +111,17 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
         int p = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
         int ox = ox0 + p;
         if (ox >= Wo) continue;
-        float *dst = a.out + ((long)oy * Wo + ox) * a.Cout;
+        float *dst = a.out16 ? nullptr : a.out + ((long)oy * Wo + ox) * a.Cout;
+        __nv_bfloat16 *dst16 = a.out16 ? (__nv_bfloat16 *)a.out16 + ((long)oy * Wo + ox) * a.out_cs : nullptr;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             int co = (j < 4) ? tx * 4 + j : 64 + tx * 4 + (j - 4);
             if (co < a.Cout) {
                 float v = acc[i][j];
                 if (a.bias) v = __fadd_rn(v, a.bias[co]);
-                dst[co] = act_fn(v, a.act);
+                v = act_fn(v, a.act);
+                if (dst16) dst16[co] = __float2bfloat16_rn(v);
+                else dst[co] = v;
             }
         }
     }

@@ -1,0 +1,364 @@
+// k_conv_tc.cu -- BF16 implicit-GEMM convolution on the 5th-generation tensor
+// cores (tcgen05), the BF16 path's replacement for cudnnConvolutionForward +
+// cudnnAddTensor + tanh (stereo/operators/convolution.cpp:141-152,
+// bias.cpp:58-67, activation.cpp:33-41).
+//
+// GEMM view: D[pixel][n] = sum_{tap, c} act[y+ky][x+kx][c] * W[n][tap][c]
+// (kernel pre-flipped on the host: CUDNN_CONVOLUTION).  A tile is 128
+// consecutive output pixels of one row (M = 128) times all NP output channels;
+// K runs over taps x 64-channel chunks of the NHWC input.
+//
+// Persistent, warp-specialised CTA (192 threads, one per SM):
+//   warp 0      TMA producer: per k-block one 4-D box (64 ch x 128 px) of the
+//               activation at the tap's offset (zero fill past the row end)
+//               and one 2-D box (64 ch x NP) of the weights, 128-byte swizzle
+//   warp 1      TMEM allocation + single-thread tcgen05.mma issue (M=128,
+//               N=NP, K=16 steps), commits free smem stages and hand
+//               finished accumulators to the epilogue
+//   warps 2..5  epilogue: tcgen05.ld of the tile (one pixel per thread),
+//               bias + tanh, then store BF16 NHWC / L2-normalise / apply
+//               the pairwise net's 1x1 head
+// Two TMEM accumulators (128 columns each) let the epilogue of tile i overlap
+// the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout the role
+// raises the CTA abort flag and the global error flag, in-flight copies and
+// MMAs are drained (again bounded) and TMEM is freed before exit.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "common.h"
+#include "kernels.h"
+#include "tc_util.cuh"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+constexpr int BM = 128;
+constexpr int TILE_A = BM * 128; // 128 rows x 64 bf16
+constexpr int NUM_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 256;
+constexpr uint32_t ACC_STRIDE = 128;
+
+struct TcParams {
+    int n_img, Hin, Win, Ho, Wo, kh, kw, cp_in, kchunks, kk_last, cout, cp_out, tiles_x, num_tiles, mode,
+        stages;
+    const float *bias; // [NP], zero padded
+    const float *head; // [2][NP] (mode 2)
+    void *out;
+    int *err;
+};
+
+template <int NP> __host__ __device__ constexpr int stage_bytes() { return TILE_A + NP * 128; }
+
+template <int NP>
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
+{
+    constexpr int STAGE = stage_bytes<NP>();
+    constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int S = p.stages;
+    uint64_t *full = (uint64_t *)(smem + S * STAGE);
+    uint64_t *empty = full + S;
+    uint64_t *tfull = empty + S;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *drain = tempty + 2;
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    volatile int *zero_flag = abort_flag + 1;
+    float *sbias = (float *)(tmem_slot + 4);
+    float *shead = sbias + NP;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 128);
+        }
+        tc::mbar_init(drain, 1);
+        *abort_flag = 0;
+        *zero_flag = 0;
+        tc::mbar_fence_init();
+        tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmB);
+    }
+    for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias[i];
+    if (p.mode == 2)
+        for (int i = threadIdx.x; i < 2 * NP; i += NUM_THREADS) shead[i] = p.head[i];
+    if (warp == 1) {
+        tc::tmem_alloc(tmem_slot, TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const int kblocks = p.kh * p.kw * p.kchunks;
+    const int tiles_per_img = p.Ho * p.tiles_x;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int stage = 0, issued = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
+                const int img = t / tiles_per_img, r = t - img * tiles_per_img;
+                const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * BM;
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    const int tap = kb / p.kchunks, ch = kb - tap * p.kchunks;
+                    const int ky = tap / p.kw, kx = tap - ky * p.kw;
+                    if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *sa = smem + stage * STAGE;
+                    tc::mbar_expect_tx(&full[stage], STAGE);
+                    tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x0 + kx, y + ky, img);
+                    tc::tma_load_2d(sa + TILE_A, &tmB, &full[stage], tap * p.cp_in + ch * 64, 0);
+                    ++issued;
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+                // let the copies already issued land before shared memory is released
+                int st = stage;
+                uint32_t ph = phase;
+                for (int i = 0; i < S && i < issued; ++i) {
+                    if (--st < 0) {
+                        st = S - 1;
+                        ph ^= 1;
+                    }
+                    tc::mbar_wait(&full[st], ph, zero_flag, 1u << 20);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0, lt = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x, ++lt) {
+                const int buf = lt & 1;
+                const uint32_t use = (uint32_t)lt >> 1;
+                if (!tc::mbar_wait(&tempty[buf], (use & 1) ^ 1, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t d = tmem + buf * ACC_STRIDE;
+                for (int kb = 0; kb < kblocks; ++kb) {
+                    if (!tc::mbar_wait(&full[stage], phase, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const int ch = kb % p.kchunks;
+                    const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
+                    const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
+                    const uint64_t da = tc::sdesc_sw128(sa), db = tc::sdesc_sw128(sa + TILE_A);
+                    for (int kk = 0; kk < nk; ++kk)
+                        tc::umma_bf16(d, da + 2 * kk, db + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
+                    tc::umma_commit(&empty[stage]);
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+                if (ok) tc::umma_commit(&tfull[buf]);
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+            }
+            // every MMA of this thread completes before TMEM is released
+            tc::umma_commit(drain);
+            tc::mbar_wait(drain, 0, zero_flag, 1u << 22);
+        }
+    } else {
+        const int q = warp & 3; // the TMEM lane quarter this warp may read
+        const int row = q * 32 + lane;
+        int lt = 0;
+        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
+            const int buf = lt & 1;
+            const uint32_t use = (uint32_t)lt >> 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&tfull[buf], use & 1, abort_flag) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            __syncwarp();
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+                break;
+            }
+            tc::fence_after_sync();
+            const int img = t / tiles_per_img, r = t - img * tiles_per_img;
+            const int y = r / p.tiles_x, x = (r - y * p.tiles_x) * BM + row;
+            const bool valid = x < p.Wo;
+            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE;
+            float v[16];
+            // the TMEM reads are warp-collective: every lane runs them
+            float sc = 1.0f;
+            if (p.mode == 1) { // pass 1: squared norm of tanh(acc + bias)
+                float s2 = 0.0f;
+#pragma unroll 1
+                for (int c = 0; c < NP / 16; ++c) {
+                    tc::tmem_ld16(ta + c * 16, v);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const float f = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                        s2 = fmaf(f, f, s2);
+                    }
+                }
+                sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
+            }
+            const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
+            __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
+            float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll 1
+            for (int c = 0; c < NP / 16; ++c) {
+                tc::tmem_ld16(ta + c * 16, v);
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                if (p.mode == 2) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        a0 = fmaf(v[j], shead[c * 16 + j], a0);
+                        a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
+                    }
+                } else if (valid) {
+                    uint32_t u[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        __nv_bfloat162 hv = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
+                        u[j] = *(uint32_t *)&hv;
+                    }
+                    uint4 *dst = (uint4 *)(o16 + c * 16);
+                    dst[0] = make_uint4(u[0], u[1], u[2], u[3]);
+                    dst[1] = make_uint4(u[4], u[5], u[6], u[7]);
+                }
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&tempty[buf]);
+            if (p.mode == 2 && valid) {
+                float *o = (float *)p.out;
+                const size_t plane = (size_t)p.Ho * p.Wo;
+                o[(size_t)y * p.Wo + x] = fabsf(a0);
+                o[plane + (size_t)y * p.Wo + x] = fabsf(a1);
+            }
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
+    }
+    return fn;
+}
+
+template <int NP> size_t smem_bytes(int stages)
+{
+    return 1024 + (size_t)stages * stage_bytes<NP>() + (2 * stages + 5) * 8 + 16 + 3 * NP * 4 + 64;
+}
+
+template <int NP> int launch(const TcConvArgs &a, const TcParams &p, cudaStream_t st)
+{
+    auto enc = encode_fn();
+    if (!enc) return fail(CNNCRF_ECUDA, "conv_tc: cuTensorMapEncodeTiled unavailable");
+    CUtensorMap ma, mb;
+    cuuint64_t gA[4] = {(cuuint64_t)a.cp_in, (cuuint64_t)a.Win, (cuuint64_t)a.Hin, (cuuint64_t)a.n_img};
+    cuuint64_t sA[3] = {(cuuint64_t)a.cp_in * 2, (cuuint64_t)a.Win * a.cp_in * 2,
+                        (cuuint64_t)a.Hin * a.Win * a.cp_in * 2};
+    cuuint32_t bA[4] = {64, BM, 1, 1};
+    cuuint32_t eA[4] = {1, 1, 1, 1};
+    CUresult r = enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.in, gA, sA, bA, eA,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation tensor map (%d)", (int)r);
+    const int taps = a.kh * a.kw;
+    cuuint64_t gB[2] = {(cuuint64_t)taps * a.cp_in, (cuuint64_t)NP};
+    cuuint64_t sB[1] = {(cuuint64_t)taps * a.cp_in * 2};
+    cuuint32_t bB[2] = {64, (cuuint32_t)NP};
+    cuuint32_t eB[2] = {1, 1};
+    r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)a.wt, gB, sB, bB, eB, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: weight tensor map (%d)", (int)r);
+    size_t smem = smem_bytes<NP>(p.stages);
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    int grid = std::min(p.num_tiles, sms);
+    {
+        CNNCRF_PROF("conv_tc", st);
+        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, mb, p);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace
+
+int conv_tc(const TcConvArgs &a, cudaStream_t st)
+{
+    if (a.cp_in % 64 != 0 || a.cp_in < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_in %d not a multiple of 64", a.cp_in);
+    if (a.cin < 1 || a.cin > a.cp_in) return fail(CNNCRF_EINVAL, "conv_tc: cin %d", a.cin);
+    if (((uintptr_t)a.in & 15) || ((uintptr_t)a.wt & 15) || ((uintptr_t)a.out & 15))
+        return fail(CNNCRF_EINVAL, "conv_tc: operands must be 16-byte aligned");
+    TcParams p{};
+    p.n_img = a.n_img, p.Hin = a.Hin, p.Win = a.Win;
+    p.Ho = a.Hin - a.kh + 1, p.Wo = a.Win - a.kw + 1;
+    if (p.Ho < 1 || p.Wo < 1) return fail(CNNCRF_ESHAPE, "conv_tc: empty output");
+    p.kh = a.kh, p.kw = a.kw, p.cp_in = a.cp_in, p.kchunks = a.cp_in / 64;
+    int rem = a.cin - 64 * (p.kchunks - 1);
+    p.kk_last = rem <= 0 ? 1 : std::min(4, (rem + 15) / 16);
+    p.cout = a.cout, p.cp_out = a.cp_out;
+    p.tiles_x = ceil_div(p.Wo, BM);
+    p.num_tiles = a.n_img * p.Ho * p.tiles_x;
+    p.mode = a.mode;
+    p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
+    if (a.mode != 2 && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);
+    switch (a.np) {
+    case 64:
+        p.stages = 8;
+        if (a.mode != 2 && a.cp_out < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        return launch<64>(a, p, st);
+    case 112:
+        p.stages = 6;
+        if (a.mode != 2 && a.cp_out < 112) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        return launch<112>(a, p, st);
+    case 128:
+        p.stages = 6;
+        if (a.mode != 2 && a.cp_out < 128) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        return launch<128>(a, p, st);
+    default:
+        return fail(CNNCRF_EUNSUPPORTED, "conv_tc: N = %d (64, 112, 128 built)", a.np);
+    }
+}
+
+} // namespace k
+} // namespace cnncrf

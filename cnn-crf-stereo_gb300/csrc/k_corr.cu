@@ -14,6 +14,8 @@
 // lane j owns disparity indices k = j + 32 r.
 #include <cfloat>
 
+#include <cuda_bf16.h>
+
 #include "../../include/cnncrf_fmath.h"
 #include "common.h"
 #include "kernels.h"
@@ -26,8 +28,14 @@ namespace {
 constexpr int PIX = 32;
 constexpr int MAXP = 16; // D <= 512
 
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__nv_bfloat16 v) { return __bfloat162float(v); }
+
+// TIN: feature element type (float: the bit-exact path; bf16: the tensor-core
+// path's features); cs = channel stride of a pixel (>= C)
+template <typename TIN>
 __global__ void __launch_bounds__(256)
-    k_corr(const float *__restrict__ fl, const float *__restrict__ fr, int H, int W, int C,
+    k_corr(const TIN *__restrict__ fl, const TIN *__restrict__ fr, int H, int W, int C, int cs,
            const float *__restrict__ list, int D, int omin, int omax, int interp, int unary,
            float *__restrict__ out)
 {
@@ -44,11 +52,11 @@ __global__ void __launch_bounds__(256)
     float *sd = sr + (size_t)R * CS;    // [D]
     for (int i = threadIdx.x; i < npx * C; i += blockDim.x) {
         int p = i / C, c = i - p * C;
-        sl[p * CS + c] = fl[((long)y * W + x0 + p) * C + c];
+        sl[p * CS + c] = to_f(fl[((long)y * W + x0 + p) * cs + c]);
     }
     for (int i = threadIdx.x; i < R * C; i += blockDim.x) {
         int p = i / C, c = i - p * C;
-        sr[p * CS + c] = fr[((long)y * W + xlo + p) * C + c];
+        sr[p * CS + c] = to_f(fr[((long)y * W + xlo + p) * cs + c]);
     }
     for (int i = threadIdx.x; i < D; i += blockDim.x) sd[i] = list[i];
     __syncthreads();
@@ -130,22 +138,36 @@ __global__ void __launch_bounds__(256)
 
 } // namespace
 
-int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list, int D,
-                int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
+template <typename TIN>
+static int corr_launch(const TIN *fl, const TIN *fr, int H, int W, int C, int cs, const float *d_list, int D,
+                       int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
 {
     if (D < 1 || D > 32 * MAXP) return fail(CNNCRF_EINVAL, "correlation: D=%d outside [1,%d]", D, 32 * MAXP);
     int R = PIX + omax - omin + 1;
     size_t smem = sizeof(float) * ((size_t)(PIX + R) * (C + 1) + D);
     if (smem > 227 * 1024)
         return fail(CNNCRF_EINVAL, "correlation: disparity band too wide (%zu bytes of shared memory)", smem);
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr<TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid(ceil_div(W, PIX), H);
     {
         CNNCRF_PROF("corr", st);
-        k_corr<<<grid, 256, smem, st>>>(fl, fr, H, W, C, d_list, D, omin, omax, interp ? 1 : 0, unary, out);
+        k_corr<TIN><<<grid, 256, smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, interp ? 1 : 0, unary, out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
+}
+
+int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list, int D, int omin,
+                int omax, bool interp, int unary, float *out, cudaStream_t st)
+{
+    return corr_launch<float>(fl, fr, H, W, C, C, d_list, D, omin, omax, interp, unary, out, st);
+}
+
+int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs, const float *d_list, int D,
+                     int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
+{
+    return corr_launch<__nv_bfloat16>((const __nv_bfloat16 *)fl, (const __nv_bfloat16 *)fr, H, W, C, cs, d_list,
+                                      D, omin, omax, interp, unary, out, st);
 }
 
 } // namespace k

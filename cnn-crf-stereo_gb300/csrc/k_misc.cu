@@ -3,6 +3,8 @@
 // so the results equal the CPU oracle bit for bit.
 #include <cfloat>
 
+#include <cuda_bf16.h>
+
 #include "common.h"
 #include "kernels.h"
 
@@ -50,6 +52,15 @@ __global__ void k_nchw_to_nhwc(const float *__restrict__ in, float *__restrict__
     long p = i / C;
     int c = (int)(i - p * C);
     out[i] = in[(long)c * npx + p];
+}
+
+__global__ void k_bf16_to_f32(const __nv_bfloat16 *__restrict__ in, int cs, int C, long npx, float *__restrict__ out)
+{
+    long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npx * C) return;
+    long p = i / C;
+    int c = (int)(i - p * C);
+    out[i] = __bfloat162float(in[p * cs + c]);
 }
 
 // warp_image_kernel on a point-sampled, clamp-addressed C4 texture
@@ -174,6 +185,16 @@ int nchw_to_nhwc(const float *in, float *out, int C, long npx, cudaStream_t st)
     {
         CNNCRF_PROF("nchw_to_nhwc", st);
         k_nchw_to_nhwc<<<ceil_div(npx * C, 256), 256, 0, st>>>(in, out, C, npx);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int bf16_to_f32(const void *in, int cs, int C, long npx, float *out, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("bf16_to_f32", st);
+        k_bf16_to_f32<<<ceil_div(npx * C, 256), 256, 0, st>>>((const __nv_bfloat16 *)in, cs, C, npx, out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

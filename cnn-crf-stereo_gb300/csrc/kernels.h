@@ -28,6 +28,8 @@ struct ConvArgs {
     const float *bias;    // [128] or nullptr
     int Cout, kh, kw, act; // act: 0 none, 1 tanh, 2 abs
     float *out;           // NHWC dense [Ho][Wo][Cout]
+    void *out16 = nullptr; // if set: BF16 NHWC output [Ho][Wo][out_cs] instead of `out`
+    int out_cs = 0;
 };
 int conv_simt(const ConvArgs &a, cudaStream_t st);
 // 1x1 conv Cin -> 2, no bias, |.| (stereo/stereonet.cpp:167,401): planar [2][H][W]
@@ -36,11 +38,29 @@ int conv_head2(const float *in, int npx, int Cin, const float *w /*[2][Cin]*/, f
 // per-pixel L2 normalisation of NHWC features
 int l2norm(float *f, long npx, int C, cudaStream_t st);
 
+// ------------------------------------------------------------ BF16 tensor-core conv
+struct TcConvArgs {
+    const void *in; // BF16 NHWC [n_img][Hin][Win][cp_in], channels >= cin zero
+    int n_img, Hin, Win, cp_in, cin;
+    const void *wt; // BF16 [np][kh*kw][cp_in], kernel flipped
+    int np, cout, kh, kw;
+    const float *bias; // [np] zero padded
+    const float *head; // [2][np] (mode 2)
+    int mode;          // 0 tanh -> BF16, 1 tanh + L2 norm -> BF16, 2 tanh + 1x1 head + abs -> FP32 [2][Ho][Wo]
+    void *out;
+    int cp_out;
+    int *err; // set to 1 if a bounded wait gave up
+};
+int conv_tc(const TcConvArgs &a, cudaStream_t st);
+
 // ------------------------------------------------------------ correlation
 // raw correlation (+ unary: -1 none, 0 -softmax, 1 one-minus) of NHWC FP32
 // features; list = the reference's stored (negated) disparities.
 int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list,
                 int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st);
+// same on BF16 features with channel stride cs (FP32 accumulation)
+int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs, const float *d_list,
+                     int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st);
 
 // ------------------------------------------------------------ CRF
 struct CrfParams {
@@ -63,6 +83,8 @@ int argmin(float *out, const float *vol, long npx, int D, float dmin, float dste
            cudaStream_t st);
 int scale(float *x, long n, float s, cudaStream_t st);
 int nchw_to_nhwc(const float *in, float *out, int C, long npx, cudaStream_t st);
+// BF16 [npx][cs] -> FP32 [npx][C]
+int bf16_to_f32(const void *in, int cs, int C, long npx, float *out, cudaStream_t st);
 int warp_rgba(float *out, const float *in, const float *u, int W, int H, cudaStream_t st);
 int tv_fit(const float *vol3, float *qf, int W, int H, float step, float lam, cudaStream_t st);
 int tv_iterate(float *u, float *u_, const float *u0, const float *qf, float *p, float *q,

@@ -19,6 +19,21 @@ namespace {
 
 constexpr int NPAD = 128; // output-channel padding of the FP32 weight layout
 
+// float -> bfloat16, round to nearest even
+uint16_t f2bf(float f)
+{
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return 0x7fc0;
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+int pad_to(int c, int m) { return (c + m - 1) / m * m; }
+
+// UMMA N for a layer width: 64, 112 or 128
+int umma_n(int cout) { return cout <= 64 ? 64 : (cout <= 112 ? 112 : 128); }
+
 void build_layers(cnncrf_net *n)
 {
     const cnncrf_net_desc &d = n->d;
@@ -93,6 +108,14 @@ int cnncrf_net::upload(int slot)
             for (int ci = 0; ci < L->cin; ++ci) w[co * L->cin + ci] = src[co * L->cin + ci];
         CNNCRF_TRY(L->wt.reserve(w.size() * sizeof(float)));
         CNNCRF_CUDA(cudaMemcpy(L->wt.get(), w.data(), w.size() * sizeof(float), cudaMemcpyHostToDevice));
+        if (d.precision == CNNCRF_BF16) { // [2][np] for the fused head of the tensor-core conv
+            int np = umma_n(L->cin);
+            std::vector<float> h((size_t)2 * np, 0.0f);
+            for (int co = 0; co < 2; ++co)
+                for (int ci = 0; ci < L->cin; ++ci) h[(size_t)co * np + ci] = src[co * L->cin + ci];
+            CNNCRF_TRY(head16.reserve(h.size() * sizeof(float)));
+            CNNCRF_CUDA(cudaMemcpy(head16.get(), h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
         return CNNCRF_OK;
     }
     // CUDNN_CONVOLUTION flips the kernel: wt[(ky*kw+kx)*Cin+ci][co] = w[co][ci][kh-1-ky][kw-1-kx]
@@ -108,6 +131,19 @@ int cnncrf_net::upload(int slot)
                 }
     CNNCRF_TRY(L->wt.reserve(wt.size() * sizeof(float)));
     CNNCRF_CUDA(cudaMemcpy(L->wt.get(), wt.data(), wt.size() * sizeof(float), cudaMemcpyHostToDevice));
+    if (d.precision == CNNCRF_BF16 && L->cin >= 16) {
+        // tensor-core layout: [np][tap][cp] BF16, K-major per output channel
+        int np = umma_n(L->cout), cp = pad_to(L->cin, 64), taps = L->kh * L->kw;
+        std::vector<uint16_t> w16((size_t)np * taps * cp, 0);
+        for (int co = 0; co < L->cout; ++co)
+            for (int ky = 0; ky < L->kh; ++ky)
+                for (int kx = 0; kx < L->kw; ++kx)
+                    for (int ci = 0; ci < L->cin; ++ci)
+                        w16[((size_t)co * taps + ky * L->kw + kx) * cp + ci] = f2bf(
+                            src[(((size_t)co * L->cin + ci) * L->kh + (L->kh - 1 - ky)) * L->kw + (L->kw - 1 - kx)]);
+        CNNCRF_TRY(L->wt16.reserve(w16.size() * 2));
+        CNNCRF_CUDA(cudaMemcpy(L->wt16.get(), w16.data(), w16.size() * 2, cudaMemcpyHostToDevice));
+    }
     return CNNCRF_OK;
 }
 
@@ -293,9 +329,7 @@ int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step
             net->pwout = net->pw_own.as<float>();
         }
     }
-    if (net->d.precision == CNNCRF_BF16) {
-        // tensor-core path buffers are sized on first use
-    }
+    if (net->d.precision == CNNCRF_BF16) CNNCRF_TRY(net->alloc_bf16());
     CNNCRF_TRY(net->set_disparities(min_disp, max_disp, step, d_unary_out));
     net->inited = true;
     return CNNCRF_OK;
@@ -404,6 +438,12 @@ int cnncrf_net_pairwise(cnncrf_net_t net, float **d_pairwise)
 int cnncrf_net_features(cnncrf_net_t net, int side, float *d_out)
 {
     if (!net || !d_out || side < 0 || side > 1) return fail(CNNCRF_EINVAL, "features: bad argument");
+    if (net->d.precision == CNNCRF_BF16) {
+        if (!net->feat16) return fail(CNNCRF_ESTATE, "features: no prediction yet");
+        size_t npx = (size_t)net->H * net->W;
+        const uint16_t *f = (const uint16_t *)net->feat16 + side * npx * net->cp_feat;
+        return k::bf16_to_f32(f, net->cp_feat, net->d.feat_channels, (long)npx, d_out, net->st);
+    }
     if (!net->feats[side]) return fail(CNNCRF_ESTATE, "features: no prediction yet");
     CNNCRF_CUDA(cudaMemcpyAsync(d_out, net->feats[side], sizeof(float) * (size_t)net->H * net->W * net->d.feat_channels,
                                 cudaMemcpyDeviceToDevice, net->st));

@@ -33,9 +33,16 @@ struct cnncrf_net {
 
     // activations
     cnncrf::DevBuf norm[2], act[2][2], pwa, pwb, scratch;
-    cnncrf::DevBuf act16[2][2], feat32[2];
     float *feats[2] = {nullptr, nullptr};
     bool inited = false;
+
+    // tensor-core path: BF16 NHWC activations of both images, channel
+    // padded to cp_feat (feature net) / cp_pw (pairwise net)
+    int np_feat = 0, cp_feat = 0, np_pw = 0, cp_pw = 0;
+    cnncrf::DevBuf a16[2], pw16, head16, err;
+    const void *feat16 = nullptr; // [2][H][W][cp_feat] after predict
+    int alloc_bf16();
+    int check_error();
 
     int num_params() const { return (int)host.size(); }
     int expected_shape(int i, int64_t s[4], int *nd) const;

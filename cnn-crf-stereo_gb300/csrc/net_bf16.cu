@@ -1,10 +1,119 @@
-// net_bf16.cu -- the BF16 tensor-core predict path (placeholder until the
-// tcgen05 kernels land).
+// net_bf16.cu -- ColorStereoNet::predict on the tensor cores: the BF16 path.
+//
+//   normalise (FP32, as the exact path)
+//   layer 1          SIMT conv (Cin = 1/3/5 is too thin for the tensor
+//                    cores), FP32 math, BF16 NHWC output padded to cp_feat
+//   layers 2..L      tcgen05 implicit GEMM over both images at once; the last
+//                    layer L2-normalises in its epilogue for the 1-<fL,fR> unary
+//   correlation      BF16 features, FP32 accumulation, unary fused
+//   pairwise net     SIMT 3x3 (3 -> 64) into BF16, then tcgen05 3x3 (64 -> 64)
+//                    whose epilogue applies the 1x1 head and |.| and writes wx, wy
+// Reference: stereo/stereonet.cpp:250-421, stereo/colorstereonet.cpp:38-77.
+#include "kernels.h"
 #include "net.h"
 
 using namespace cnncrf;
 
-int cnncrf_net::predict_bf16(const float *, const float *)
+namespace {
+int pad_to(int c, int m) { return (c + m - 1) / m * m; }
+int umma_n(int cout) { return cout <= 64 ? 64 : (cout <= 112 ? 112 : 128); }
+} // namespace
+
+int cnncrf_net::alloc_bf16()
 {
-    return fail(CNNCRF_EUNSUPPORTED, "BF16 path not built yet");
+    cp_feat = pad_to(d.feat_channels, 64);
+    np_feat = umma_n(d.feat_channels);
+    size_t h1 = h - 2, w1 = w - 2; // layer-1 output, the largest activation
+    size_t bytes = 2 * h1 * w1 * cp_feat * 2;
+    for (int i = 0; i < 2; ++i) {
+        CNNCRF_TRY(a16[i].reserve(bytes));
+        // channels past feat_channels are never written and must read as zero
+        CNNCRF_CUDA(cudaMemset(a16[i].get(), 0, bytes));
+    }
+    if (d.with_pairwise) {
+        cp_pw = pad_to(d.pw_channels, 64);
+        np_pw = umma_n(d.pw_channels);
+        size_t pb = (size_t)(H + 2) * (W + 2) * cp_pw * 2;
+        CNNCRF_TRY(pw16.reserve(pb));
+        CNNCRF_CUDA(cudaMemset(pw16.get(), 0, pb));
+    }
+    CNNCRF_TRY(err.reserve(sizeof(int)));
+    CNNCRF_CUDA(cudaMemset(err.get(), 0, sizeof(int)));
+    return CNNCRF_OK;
+}
+
+int cnncrf_net::check_error()
+{
+    if (d.precision != CNNCRF_BF16 || !err.get()) return CNNCRF_OK;
+    int e = 0;
+    CNNCRF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    CNNCRF_CUDA(cudaStreamSynchronize(st));
+    if (e) {
+        CNNCRF_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(int), st));
+        return fail(CNNCRF_ETIMEOUT, "a tensor-core kernel gave up on a bounded wait");
+    }
+    return CNNCRF_OK;
+}
+
+int cnncrf_net::predict_bf16(const float *left, const float *right)
+{
+    if (d.num_layers < 2) return fail(CNNCRF_EUNSUPPORTED, "BF16 path needs >= 2 feature layers");
+    const float *img[2] = {left, right};
+    const int ic = d.in_channels, F = d.feat_channels, cp = cp_feat;
+    const size_t h1 = h - 2, w1 = w - 2;
+    for (int s = 0; s < 2; ++s) {
+        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st));
+        Layer &L0 = feat[0];
+        k::ConvArgs a{norm[s].as<float>(), h, w, ic, (long)ic, (long)w * ic, L0.wt.as<float>(), L0.bias.as<float>(),
+                      F, 3, 3, 1, nullptr};
+        a.out16 = (uint16_t *)a16[0].get() + s * h1 * w1 * cp;
+        a.out_cs = cp;
+        CNNCRF_TRY(k::conv_simt(a, st));
+    }
+    int hin = (int)h1, win = (int)w1;
+    int cur = 0;
+    for (size_t l = 1; l < feat.size(); ++l) {
+        Layer &L = feat[l];
+        k::TcConvArgs t{};
+        t.in = a16[cur].get();
+        t.n_img = 2, t.Hin = hin, t.Win = win, t.cp_in = cp, t.cin = F;
+        t.wt = L.wt16.get();
+        t.np = np_feat, t.cout = F, t.kh = L.kh, t.kw = L.kw;
+        t.bias = L.bias.as<float>();
+        t.head = nullptr;
+        t.mode = (l + 1 == feat.size() && d.unary == CNNCRF_UNARY_ONE_MINUS_DOT) ? 1 : 0;
+        t.out = a16[cur ^ 1].get();
+        t.cp_out = cp;
+        t.err = err.as<int>();
+        CNNCRF_TRY(k::conv_tc(t, st));
+        hin -= L.kh - 1, win -= L.kw - 1;
+        cur ^= 1;
+    }
+    if (hin != H || win != W) return fail(CNNCRF_ESHAPE, "BF16 feature map %dx%d != %dx%d", win, hin, W, H);
+    const uint16_t *f = (const uint16_t *)a16[cur].get();
+    feat16 = f;
+    CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)H * W * cp, H, W, F, cp, d_list.as<float>(), D, omin, omax,
+                                   interp || force_interp, d.unary, vol, st));
+    if (d.with_pairwise) {
+        int cr = pad - 2;
+        const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+        k::ConvArgs a1{in, H + 4, W + 4, pw[0].cin, (long)ic, (long)w * ic, pw[0].wt.as<float>(), pw[0].bias.as<float>(),
+                       pw[0].cout, 3, 3, 1, nullptr};
+        a1.out16 = pw16.get();
+        a1.out_cs = cp_pw;
+        CNNCRF_TRY(k::conv_simt(a1, st));
+        k::TcConvArgs t{};
+        t.in = pw16.get();
+        t.n_img = 1, t.Hin = H + 2, t.Win = W + 2, t.cp_in = cp_pw, t.cin = pw[1].cin;
+        t.wt = pw[1].wt16.get();
+        t.np = np_pw, t.cout = pw[1].cout, t.kh = 3, t.kw = 3;
+        t.bias = pw[1].bias.as<float>();
+        t.head = head16.as<float>();
+        t.mode = 2;
+        t.out = pwout;
+        t.cp_out = 0;
+        t.err = err.as<int>();
+        CNNCRF_TRY(k::conv_tc(t, st));
+    }
+    return CNNCRF_OK;
 }
