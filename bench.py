@@ -208,6 +208,27 @@ def build_stereo(cnncrf, wl, precision, stream):
     return st
 
 
+def run_profile(args):
+    """The device step alone, for ncu: no timing, FP32 comparison or CPU leg."""
+    import torch
+    import cnncrf
+    from cnncrf import scenes
+    wl = WORKLOAD
+    precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
+    stream = torch.cuda.Stream()
+    scene = scenes.kitti_scene(wl["W"], wl["H"], wl["D"], seed=0)
+    with torch.cuda.stream(stream):
+        st = build_stereo(cnncrf, wl, precision, stream)
+        dl = torch.from_numpy(scene["left"]).cuda()
+        dr = torch.from_numpy(scene["right"]).cuda()
+        for _ in range(args.warmup + args.steps):
+            st.set_color_images(dl, dr)
+            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+        torch.cuda.synchronize()
+    print("profile run done")
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -216,9 +237,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
+                    help="profile: only warm-up + `steps` device steps of the path (for ncu captures)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.mode == "profile":
+        return run_profile(args)
 
     import numpy as np
     import torch

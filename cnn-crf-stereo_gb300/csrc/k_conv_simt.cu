@@ -127,6 +127,64 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
     }
 }
 
+// First layers (Cin <= 5): one thread per output pixel holds all COUT
+// accumulators; its 3x3xCin patch sits in registers and the weights are read
+// from shared memory as broadcast float4.  Same per-output order as above:
+// k = (ky, kx, ci) ascending, one fmaf per term, then + bias, activation.
+template <int COUT>
+__global__ void __launch_bounds__(128) k_conv_first(ConvArgs a, int Ho, int Wo, int K)
+{
+    constexpr int CP = (COUT + 3) & ~3;
+    extern __shared__ float4 wsm4[];
+    float *wsm = (float *)wsm4; // [K][CP]
+    for (int i = threadIdx.x; i < K * CP; i += blockDim.x) {
+        int k = i / CP, co = i - k * CP;
+        wsm[i] = a.wt[(long)k * BN + co];
+    }
+    __syncthreads();
+    const int oy = blockIdx.y, ox = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ox >= Wo) return;
+    float acc[CP];
+#pragma unroll
+    for (int co = 0; co < CP; ++co) acc[co] = 0.0f;
+    for (int ky = 0; ky < a.kh; ++ky)
+        for (int kx = 0; kx < a.kw; ++kx) {
+            const float *src = a.in + (long)(oy + ky) * a.in_row + (long)(ox + kx) * a.in_pix;
+            const int kb = (ky * a.kw + kx) * a.Cin;
+            for (int ci = 0; ci < a.Cin; ++ci) {
+                const float xv = __ldg(src + ci);
+                const float4 *w = (const float4 *)(wsm + (kb + ci) * CP);
+#pragma unroll
+                for (int q = 0; q < CP / 4; ++q) {
+                    const float4 wv = w[q];
+                    acc[4 * q + 0] = __fmaf_rn(wv.x, xv, acc[4 * q + 0]);
+                    acc[4 * q + 1] = __fmaf_rn(wv.y, xv, acc[4 * q + 1]);
+                    acc[4 * q + 2] = __fmaf_rn(wv.z, xv, acc[4 * q + 2]);
+                    acc[4 * q + 3] = __fmaf_rn(wv.w, xv, acc[4 * q + 3]);
+                }
+            }
+        }
+#pragma unroll
+    for (int co = 0; co < CP; ++co) {
+        float v = acc[co];
+        if (a.bias) v = __fadd_rn(v, a.bias[co]);
+        acc[co] = act_fn(v, a.act);
+    }
+    const long pix = (long)oy * Wo + ox;
+    if (a.out16) {
+        __nv_bfloat16 *d16 = (__nv_bfloat16 *)a.out16 + pix * a.out_cs;
+#pragma unroll
+        for (int co = 0; co < COUT; co += 2) {
+            const float v1 = co + 1 < COUT ? acc[co + 1] : 0.0f;
+            *(__nv_bfloat162 *)(d16 + co) = __floats2bfloat162_rn(acc[co], v1);
+        }
+    } else {
+        float *d = a.out + pix * a.Cout;
+#pragma unroll
+        for (int co = 0; co < COUT; ++co) d[co] = acc[co];
+    }
+}
+
 __global__ void k_head2(const float *__restrict__ in, int npx, int Cin, const float *__restrict__ w,
                         float *__restrict__ out)
 {
@@ -162,6 +220,19 @@ int conv_simt(const ConvArgs &a, cudaStream_t st)
     int Ho = a.H - a.kh + 1, Wo = a.W - a.kw + 1;
     if (Ho <= 0 || Wo <= 0) return fail(CNNCRF_ESHAPE, "conv_simt: empty output");
     int K = a.kh * a.kw * a.Cin;
+    if (K <= 45 && (a.Cout == 100 || a.Cout == 64) && a.Cout == (a.Cout & ~1)) {
+        dim3 g(ceil_div(Wo, 128), Ho);
+        size_t smem = sizeof(float) * (size_t)K * ((a.Cout + 3) & ~3);
+        if (a.Cout == 100) {
+            CNNCRF_PROF("conv_first", st);
+            k_conv_first<100><<<g, 128, smem, st>>>(a, Ho, Wo, K);
+        } else {
+            CNNCRF_PROF("conv_first", st);
+            k_conv_first<64><<<g, 128, smem, st>>>(a, Ho, Wo, K);
+        }
+        CNNCRF_CHECK_LAUNCH();
+        return CNNCRF_OK;
+    }
     dim3 grid(ceil_div(Wo, BM), Ho);
     {
         CNNCRF_PROF("conv_simt", st);

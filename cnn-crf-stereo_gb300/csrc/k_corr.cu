@@ -12,6 +12,7 @@
 // pixels those pixels can see are staged in shared memory (odd row stride:
 // lanes read consecutive rows without bank conflicts).  One warp per pixel;
 // lane j owns disparity indices k = j + 32 r.
+#include <algorithm>
 #include <cfloat>
 
 #include <cuda_bf16.h>
@@ -136,6 +137,126 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Integer disparities as a banded GEMM: for the 32 pixels x0.. of row y and
+// every right pixel j of their band, T[p][j] = sum_c fL[c][p] * fR[c][j]
+// (ascending c, one fmaf per term from 0: the same value as the per-pixel
+// loop above), register-blocked 4 pixels x NJ band columns per thread; then
+// one warp per pixel picks its D taps out of T and applies the unary.
+constexpr int MAXNJ = 16;
+
+template <typename TIN>
+__global__ void __launch_bounds__(256)
+    k_corr_band(const TIN *__restrict__ fl, const TIN *__restrict__ fr, int H, int W, int C, int cs,
+                const float *__restrict__ list, int D, int omin, int omax, int NJ, int unary,
+                float *__restrict__ out)
+{
+    extern __shared__ float sm[];
+    const int y = blockIdx.y;
+    const int x0 = blockIdx.x * PIX;
+    const int RB = NJ * 32;                  // band columns computed (>= PIX + omax - omin)
+    const int xlo = x0 + omin;               // band column 0 (may be < 0: zero filled)
+    const int LS = PIX + 1, RS = RB + 1;     // odd row strides
+    float *sl = sm;                          // [C][LS]
+    float *sr = sl + (size_t)C * LS;         // [C][RS]
+    float *sd = sr + (size_t)C * RS;         // [D]
+    const int npx = min(PIX, W - x0);
+    for (int i = threadIdx.x; i < PIX * C; i += blockDim.x) {
+        int p = i / C, c = i - p * C;
+        sl[c * LS + p] = p < npx ? to_f(fl[((long)y * W + x0 + p) * cs + c]) : 0.0f;
+    }
+    for (int i = threadIdx.x; i < RB * C; i += blockDim.x) {
+        int j = i / C, c = i - j * C;
+        int xr = xlo + j;
+        sr[c * RS + j] = (xr >= 0 && xr < W) ? to_f(fr[((long)y * W + xr) * cs + c]) : 0.0f;
+    }
+    for (int i = threadIdx.x; i < D; i += blockDim.x) sd[i] = list[i];
+    __syncthreads();
+
+    const int tp = threadIdx.x & 7, tj = threadIdx.x >> 3;
+    float acc[4][MAXNJ];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < MAXNJ; ++j) acc[i][j] = 0.0f;
+    for (int c = 0; c < C; ++c) {
+        const float *a = sl + c * LS + tp * 4;
+        const float a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3];
+        const float *b = sr + c * RS + tj * NJ;
+#pragma unroll
+        for (int j = 0; j < MAXNJ; ++j) {
+            if (j < NJ) {
+                const float bv = b[j];
+                acc[0][j] = __fmaf_rn(a0, bv, acc[0][j]);
+                acc[1][j] = __fmaf_rn(a1, bv, acc[1][j]);
+                acc[2][j] = __fmaf_rn(a2, bv, acc[2][j]);
+                acc[3][j] = __fmaf_rn(a3, bv, acc[3][j]);
+            }
+        }
+    }
+    __syncthreads(); // the tiles are dead: T reuses their storage
+    float *T = sm;   // [PIX][RS]
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < MAXNJ; ++j)
+            if (j < NJ) T[(tp * 4 + i) * RS + tj * NJ + j] = acc[i][j];
+    float *sd2 = T + (size_t)PIX * RS;
+    for (int i = threadIdx.x; i < D; i += blockDim.x) sd2[i] = list[i];
+    __syncthreads();
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int P = (D + 31) >> 5;
+    for (int pi = warp; pi < npx; pi += 8) {
+        const int x = x0 + pi;
+        float cv[MAXP];
+#pragma unroll
+        for (int r = 0; r < MAXP; ++r) {
+            cv[r] = 0.0f;
+            int kk = lane + 32 * r;
+            if (r < P && kk < D) {
+                float s = sd2[kk];
+                float w2 = (float)x + s;
+                if (w2 >= 0.0f) {
+                    int xs = x + (int)s;
+                    if (xs <= W - 1) cv[r] = T[pi * RS + (xs - xlo)];
+                }
+            }
+        }
+        float *o = out + ((long)y * W + x) * D;
+        if (unary == 0) {
+            float m = -FLT_MAX;
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r)
+                if (r < P && lane + 32 * r < D) m = fmaxf(m, cv[r]);
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, off));
+            float sum = 0.0f;
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                if (r < P) {
+                    int kk = lane + 32 * r;
+                    float e = kk < D ? cnncrf_expf(cv[r] - m) : 0.0f;
+                    cv[r] = e;
+                    sum = (r == 0) ? e : sum + e;
+                }
+            }
+#pragma unroll
+            for (int off = 16; off >= 1; off >>= 1) sum = sum + __shfl_xor_sync(0xffffffffu, sum, off);
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                int kk = lane + 32 * r;
+                if (r < P && kk < D) o[kk] = -(cv[r] / sum);
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                int kk = lane + 32 * r;
+                if (r < P && kk < D) o[kk] = unary == 1 ? 1.0f - cv[r] : cv[r];
+            }
+        }
+    }
+}
+
 } // namespace
 
 template <typename TIN>
@@ -143,12 +264,27 @@ static int corr_launch(const TIN *fl, const TIN *fr, int H, int W, int C, int cs
                        int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
 {
     if (D < 1 || D > 32 * MAXP) return fail(CNNCRF_EINVAL, "correlation: D=%d outside [1,%d]", D, 32 * MAXP);
+    dim3 grid(ceil_div(W, PIX), H);
+    const int NJ = ceil_div(PIX + omax - omin, 32);
+    // phase 1 holds the two feature tiles, phase 2 the result tile T in the
+    // same storage: allocate the larger of the two
+    const size_t tiles = (size_t)C * (PIX + 1) + (size_t)C * (NJ * 32 + 1) + D;
+    const size_t tres = (size_t)PIX * (NJ * 32 + 1) + D;
+    const size_t band_smem = sizeof(float) * std::max(tiles, tres);
+    if (!interp && NJ <= MAXNJ && band_smem <= 227 * 1024) {
+        CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_band<TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem));
+        {
+            CNNCRF_PROF("corr", st);
+            k_corr_band<TIN><<<grid, 256, band_smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, NJ, unary, out);
+        }
+        CNNCRF_CHECK_LAUNCH();
+        return CNNCRF_OK;
+    }
     int R = PIX + omax - omin + 1;
     size_t smem = sizeof(float) * ((size_t)(PIX + R) * (C + 1) + D);
     if (smem > 227 * 1024)
         return fail(CNNCRF_EINVAL, "correlation: disparity band too wide (%zu bytes of shared memory)", smem);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_corr<TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid(ceil_div(W, PIX), H);
     {
         CNNCRF_PROF("corr", st);
         k_corr<TIN><<<grid, 256, smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, interp ? 1 : 0, unary, out);

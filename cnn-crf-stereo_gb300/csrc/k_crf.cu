@@ -39,14 +39,21 @@ struct Rho {
 
 #define INF CUDART_INF_F
 
+// Order-preserving map of (non-NaN) floats to signed ints, and back: the
+// warp minimum is then one redux.sync.min.s32, exact like a float min.
+__device__ __forceinline__ int f2ord(float f)
+{
+    const int b = __float_as_int(f);
+    return b ^ ((b >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7fffffff)); }
+
 template <int P> __device__ __forceinline__ float warp_min(const float (&v)[P])
 {
     float m = v[0];
 #pragma unroll
     for (int r = 1; r < P; ++r) m = fminf(m, v[r]);
-#pragma unroll
-    for (int off = 16; off >= 1; off >>= 1) m = fminf(m, __shfl_xor_sync(0xffffffffu, m, off));
-    return m;
+    return ord2f(__reduce_min_sync(0xffffffffu, f2ord(m)));
 }
 
 template <int P> __device__ __forceinline__ void load_vec(const float *p, int lane, int D, float (&v)[P])
@@ -131,132 +138,174 @@ __device__ __forceinline__ void minconv(const float (&v)[P], float g, float w, c
     }
 }
 
-// Horizontal pass: one warp per row y, chain over x, weights wx[y][x] on the
-// edge x -> x+1; unary theta - phi; the handed-over slack is added to phi.
-template <int P, int DELTA>
-__global__ void __launch_bounds__(64)
-    k_crf_h(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wx,
-            float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, double *__restrict__ cH)
+// ---------------------------------------------------------------- cp.async ring
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
 {
-    const int lane = threadIdx.x & 31;
-    const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (y >= H) return;
-    const long row = (long)y * W;
-    float L[P], v[P], th[P], ph[P];
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, int bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// copy this lane's P labels of one pixel vector into its ring slot
+template <int P> __device__ __forceinline__ void lane_copy(float *dst, const float *src, int lane, int D)
+{
+    const int k0 = lane * P;
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + k0);
+    if (D == 32 * P) {
+        if constexpr (P % 4 == 0) {
 #pragma unroll
-    for (int r = 0; r < P; ++r) L[r] = 0.0f, ph[r] = 0.0f;
-    double acc = 0.0, cmin = 0.0;
-    for (int x = 0; x < W; ++x) {
-        const long pix = row + x;
-        load_vec<P>(theta + pix * D, lane, D, th);
-        if (!first) load_vec<P>(phi + pix * D, lane, D, ph);
-        store_vec<P>(Lbuf + pix * D, lane, D, L);
+            for (int i = 0; i < P / 4; ++i) cp_async16(d + 16 * i, src + k0 + 4 * i);
+        } else if constexpr (P % 2 == 0) {
 #pragma unroll
-        for (int r = 0; r < P; ++r)
-            v[r] = (lane * P + r < D) ? __fadd_rn(L[r], __fsub_rn(th[r], ph[r])) : INF;
-        float g = warp_min<P>(v);
-        if (x < W - 1) {
-            acc += (double)g;
-            minconv<P, DELTA>(v, g, wx[pix], rp, lane, D, L);
+            for (int i = 0; i < P / 2; ++i) cp_async8(d + 8 * i, src + k0 + 2 * i);
         } else {
-            cmin = acc + (double)g;
+#pragma unroll
+            for (int i = 0; i < P; ++i) cp_async4(d + 4 * i, src + k0 + i, 4);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const bool ok = k0 + i < D;
+            cp_async4(d + 4 * i, ok ? src + k0 + i : src, ok ? 4 : 0);
         }
     }
+}
+
+template <int P> __device__ __forceinline__ void lane_read(const float *slot, int lane, float (&v)[P])
+{
+#pragma unroll
+    for (int r = 0; r < P; ++r) v[r] = slot[lane * P + r];
+}
+
+constexpr int RING = 8; // prefetch depth in chain steps
+
+__host__ __device__ constexpr int ring_floats(int P) { return RING * 3 * 32 * P; }
+
+// One pass over the chains of one direction; one warp per chain.
+//   HPASS: chain = row y over x (weights wx[y][x] on edge x -> x+1), unary
+//          theta - phi, the handed-over slack is added to phi.
+//   !HPASS: chain = column x over y (weights wy[y][x] on edge y -> y+1),
+//          unary phi, the handed-over slack is subtracted from phi; labels
+//          (if given) = first argmin of the min-marginals.
+// Per step the pixel vectors come from a per-warp shared-memory ring filled
+// RING steps ahead with cp.async (each lane copies and reads only its own
+// labels), so the chain's dependent arithmetic does not wait on DRAM.
+template <int P, int DELTA, bool HPASS>
+__global__ void __launch_bounds__(64)
+    k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
+                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
+                int32_t *__restrict__ labels, double *__restrict__ cmin_out)
+{
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int chain = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int n = HPASS ? W : H;
+    if (chain >= (HPASS ? H : W)) return;
+    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P));
+    float *ring = wsm + nmax;
+    auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
+    for (int i = lane; i < n; i += 32) wsm[i] = wgt[pix(i)];
+    __syncwarp();
+    const bool use_phi = !(HPASS && first);
+    auto slot = [&](int i, int a) { return ring + ((i % RING) * 3 + a) * (32 * P); };
+
+    // ---- forward: messages into each node, stored for the backward sweep
+    auto issue_f = [&](int i) {
+        if (i < n) {
+            if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
+            if (use_phi) lane_copy<P>(slot(i, 1), phi + pix(i) * D, lane, D);
+        }
+        cp_commit();
+    };
+    float L[P], v[P], th[P], ph[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
+    for (int i = 0; i < RING - 1; ++i) issue_f(i);
+    double acc = 0.0, cmin = 0.0;
+    for (int i = 0; i < n; ++i) {
+        issue_f(i + RING - 1);
+        cp_wait<RING - 1>();
+        if (HPASS) lane_read<P>(slot(i, 0), lane, th);
+        if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
+        store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            const float un = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
+            v[r] = (lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
+        }
+        const float g = warp_min<P>(v);
+        if (lane == 0) { // the FP64 bound lives in lane 0 only (off the message chain)
+            if (i < n - 1) acc += (double)g;
+            else cmin = acc + (double)g;
+        }
+        if (i < n - 1) minconv<P, DELTA>(v, g, wsm[i], rp, lane, D, L);
+    }
+    cp_wait<0>();
+
+    // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
+    auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j
+        const int i = n - 1 - j;
+        if (i >= 0) {
+            if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
+            if (use_phi) lane_copy<P>(slot(j, 1), phi + pix(i) * D, lane, D);
+            lane_copy<P>(slot(j, 2), Lbuf + pix(i) * D, lane, D);
+        }
+        cp_commit();
+    };
     float R[P], Lx[P], m[P], A[P];
 #pragma unroll
     for (int r = 0; r < P; ++r) R[r] = 0.0f;
-    for (int x = W - 1; x >= 0; --x) {
-        const long pix = row + x;
-        load_vec<P>(theta + pix * D, lane, D, th);
-        if (!first) {
-            load_vec<P>(phi + pix * D, lane, D, ph);
+    for (int j = 0; j < RING - 1; ++j) issue_b(j);
+    for (int j = 0; j < n; ++j) {
+        const int i = n - 1 - j;
+        issue_b(j + RING - 1);
+        cp_wait<RING - 1>();
+        if (HPASS) lane_read<P>(slot(j, 0), lane, th);
+        if (use_phi) {
+            lane_read<P>(slot(j, 1), lane, ph);
         } else {
 #pragma unroll
             for (int r = 0; r < P; ++r) ph[r] = 0.0f; // phi starts at zero
         }
-        load_vec<P>(Lbuf + pix * D, lane, D, Lx);
+        lane_read<P>(slot(j, 2), lane, Lx);
 #pragma unroll
         for (int r = 0; r < P; ++r) {
-            A[r] = __fsub_rn(th[r], ph[r]);
+            A[r] = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
             m[r] = (lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], A[r]), R[r]) : INF;
         }
         const float mu = warp_min<P>(m);
-#pragma unroll
-        for (int r = 0; r < P; ++r) {
-            float h = __fmul_rn(rp.slack, __fsub_rn(m[r], mu));
-            A[r] = __fsub_rn(A[r], h);
-            ph[r] = __fadd_rn(ph[r], h);
-        }
-        store_vec<P>(phi + pix * D, lane, D, ph);
-        if (x > 0) {
-#pragma unroll
-            for (int r = 0; r < P; ++r) v[r] = (lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
-            float g = warp_min<P>(v);
-            minconv<P, DELTA>(v, g, wx[pix - 1], rp, lane, D, R);
-        }
-    }
-    if (lane == 0) cH[y] = cmin;
-}
-
-// Vertical pass: one warp per column x, chain over y, weights wy[y][x] on the
-// edge y -> y+1; unary phi; the handed-over slack is subtracted from phi.
-template <int P, int DELTA>
-__global__ void __launch_bounds__(64)
-    k_crf_v(float *__restrict__ phi, const float *__restrict__ wy, float *__restrict__ Lbuf, int W,
-            int H, int D, Rho rp, int32_t *__restrict__ labels, double *__restrict__ cV)
-{
-    const int lane = threadIdx.x & 31;
-    const int x = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (x >= W) return;
-    float L[P], v[P], B[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) L[r] = 0.0f;
-    double acc = 0.0, cmin = 0.0;
-    for (int y = 0; y < H; ++y) {
-        const long pix = (long)y * W + x;
-        load_vec<P>(phi + pix * D, lane, D, B);
-        store_vec<P>(Lbuf + pix * D, lane, D, L);
-#pragma unroll
-        for (int r = 0; r < P; ++r) v[r] = (lane * P + r < D) ? __fadd_rn(L[r], B[r]) : INF;
-        float g = warp_min<P>(v);
-        if (y < H - 1) {
-            acc += (double)g;
-            minconv<P, DELTA>(v, g, wy[pix], rp, lane, D, L);
-        } else {
-            cmin = acc + (double)g;
-        }
-    }
-    float R[P], Lx[P], m[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) R[r] = 0.0f;
-    for (int y = H - 1; y >= 0; --y) {
-        const long pix = (long)y * W + x;
-        load_vec<P>(phi + pix * D, lane, D, B);
-        load_vec<P>(Lbuf + pix * D, lane, D, Lx);
-#pragma unroll
-        for (int r = 0; r < P; ++r)
-            m[r] = (lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], B[r]), R[r]) : INF;
-        const float mu = warp_min<P>(m);
-        if (labels) {
+        if (!HPASS && labels) {
             int best = 0x7fffffff;
 #pragma unroll
             for (int r = P - 1; r >= 0; --r)
                 if (m[r] == mu && lane * P + r < D) best = lane * P + r;
-#pragma unroll
-            for (int off = 16; off >= 1; off >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, off));
-            if (lane == 0) labels[pix] = best;
+            best = __reduce_min_sync(0xffffffffu, best);
+            if (lane == 0) labels[pix(i)] = best;
         }
 #pragma unroll
-        for (int r = 0; r < P; ++r) B[r] = __fsub_rn(B[r], __fmul_rn(rp.slack, __fsub_rn(m[r], mu)));
-        store_vec<P>(phi + pix * D, lane, D, B);
-        if (y > 0) {
+        for (int r = 0; r < P; ++r) {
+            const float h = __fmul_rn(rp.slack, __fsub_rn(m[r], mu));
+            A[r] = __fsub_rn(A[r], h);
+            ph[r] = HPASS ? __fadd_rn(ph[r], h) : A[r];
+        }
+        store_vec<P>(phi + pix(i) * D, lane, D, ph);
+        if (i > 0) {
 #pragma unroll
-            for (int r = 0; r < P; ++r) v[r] = (lane * P + r < D) ? __fadd_rn(B[r], R[r]) : INF;
-            float g = warp_min<P>(v);
-            minconv<P, DELTA>(v, g, wy[pix - W], rp, lane, D, R);
+            for (int r = 0; r < P; ++r) v[r] = (lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
+            const float g = warp_min<P>(v);
+            minconv<P, DELTA>(v, g, wsm[i - 1], rp, lane, D, R);
         }
     }
-    if (lane == 0) cV[x] = cmin;
+    cp_wait<0>();
+    if (lane == 0) cmin_out[chain] = cmin;
 }
 
 __global__ void k_lb(const double *__restrict__ cH, int H, const double *__restrict__ cV, int W,
@@ -311,16 +360,23 @@ int run_passes(const float *cost, const float *wx, const float *wy, int W, int H
     float *phi = (float *)(ws + l.phi), *lbuf = (float *)(ws + l.lbuf);
     double *cH = (double *)(ws + l.ch), *cV = (double *)(ws + l.cv), *lb = (double *)(ws + l.lb);
     const int wpb = 2;
+    const int nh = (W + 3) & ~3, nv = (H + 3) & ~3;
+    const size_t smh = sizeof(float) * wpb * (size_t)(nh + ring_floats(P));
+    const size_t smv = sizeof(float) * wpb * (size_t)(nv + ring_floats(P));
+    if (smh > 227 * 1024 || smv > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
+    auto kh = k_crf_chain<P, DELTA, true>;
+    auto kv = k_crf_chain<P, DELTA, false>;
+    CNNCRF_CUDA(cudaFuncSetAttribute(kh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smh));
+    CNNCRF_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smv));
     for (int it = 0; it < iters; ++it) {
         {
             CNNCRF_PROF("crf_h", st);
-            k_crf_h<P, DELTA><<<ceil_div(H, wpb), 32 * wpb, 0, st>>>(cost, phi, wx, lbuf, W, H, D, rp,
-                                                                 it == 0, cH);
+            kh<<<ceil_div(H, wpb), 32 * wpb, smh, st>>>(cost, phi, wx, lbuf, W, H, D, rp, it == 0, nh, nullptr, cH);
         }
         {
             CNNCRF_PROF("crf_v", st);
-            k_crf_v<P, DELTA><<<ceil_div(W, wpb), 32 * wpb, 0, st>>>(
-            phi, wy, lbuf, W, H, D, rp, it == iters - 1 ? labels : nullptr, cV);
+            kv<<<ceil_div(W, wpb), 32 * wpb, smv, st>>>(cost, phi, wy, lbuf, W, H, D, rp, 0, nv,
+                                                       it == iters - 1 ? labels : nullptr, cV);
         }
     }
     {

@@ -37,38 +37,52 @@ __device__ __forceinline__ float plane_val(const float *rgba, long i, int c, int
     return px[c];
 }
 
-// One thread per (plane, row): FP64 row sums in x order.  pass 0 sums values,
-// pass 1 sums squares of (v - mean_c) rounded to float, as the oracle does.
+// FP64 sums in a fixed order shared with the CPU oracle: lane j of a warp sums
+// the elements j, j+32, j+64, ... in ascending order, then the 32 partial sums
+// are combined by an xor butterfly (offsets 16, 8, 4, 2, 1).
+__device__ __forceinline__ double warp_tree_sum(double s)
+{
+#pragma unroll
+    for (int off = 16; off >= 1; off >>= 1) s = s + __shfl_xor_sync(0xffffffffu, s, off);
+    return s;
+}
+
+// One warp per (plane, row).  pass 0 sums the values, pass 1 the squares of
+// (v - mean_c) rounded to float.
 __global__ void k_rowsums(const float *__restrict__ rgba, int Wp, int Hp, int planes, int gray,
                           int pass, const float *__restrict__ stats, double *__restrict__ rows)
 {
-    int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= planes * Hp) return;
-    int c = t / Hp, y = t - c * Hp;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= planes * Hp) return;
+    const int c = w / Hp, y = w - c * Hp;
+    const long base = (long)y * Wp;
     double s = 0.0;
-    long base = (long)y * Wp;
     if (pass == 0) {
-        for (int x = 0; x < Wp; ++x) s += (double)plane_val(rgba, base + x, c, gray);
+        for (int x = lane; x < Wp; x += 32) s += (double)plane_val(rgba, base + x, c, gray);
     } else {
-        float mean = stats[c];
-        for (int x = 0; x < Wp; ++x) {
-            float v = __fsub_rn(plane_val(rgba, base + x, c, gray), mean);
+        const float mean = stats[c];
+        for (int x = lane; x < Wp; x += 32) {
+            const float v = __fsub_rn(plane_val(rgba, base + x, c, gray), mean);
             s += (double)__fmul_rn(v, v);
         }
     }
-    rows[t] = s;
+    s = warp_tree_sum(s);
+    if (lane == 0) rows[w] = s;
 }
 
-// One thread per plane: the row partials in y order -> mean (pass 0) or std.
+// One warp per plane: the row sums in the same lane / butterfly order -> mean
+// (pass 0) or population std (pass 1).
 __global__ void k_finalize(const double *__restrict__ rows, int Hp, int planes, long N, int pass,
                            float *__restrict__ stats)
 {
-    int c = threadIdx.x;
-    if (c >= planes) return;
-    double tot = 0.0;
-    for (int y = 0; y < Hp; ++y) tot += rows[c * Hp + y];
-    if (pass == 0) stats[c] = (float)(tot / (double)N);
-    else stats[4 + c] = (float)sqrt(tot / (double)N);
+    const int c = blockIdx.x, lane = threadIdx.x;
+    double s = 0.0;
+    for (int y = lane; y < Hp; y += 32) s += rows[c * Hp + y];
+    s = warp_tree_sum(s);
+    if (lane == 0) {
+        if (pass == 0) stats[c] = (float)(s / (double)N);
+        else stats[4 + c] = (float)sqrt(s / (double)N);
+    }
 }
 
 __global__ void k_norm_write(const float *__restrict__ rgba, int Wp, int Hp, int ic,
@@ -111,22 +125,22 @@ int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scrat
     double *rows = (double *)scratch;
     float *stats = (float *)((char *)scratch + sizeof(double) * 3 * (size_t)Hp);
     long N = (long)Wp * Hp;
-    int nt = planes * Hp;
+    const long nthreads = 32L * planes * Hp;
     {
         CNNCRF_PROF("rowsums", st);
-        k_rowsums<<<ceil_div(nt, 128), 128, 0, st>>>(rgba, Wp, Hp, planes, gray, 0, stats, rows);
+        k_rowsums<<<ceil_div(nthreads, 256), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 0, stats, rows);
     }
     {
         CNNCRF_PROF("finalize", st);
-        k_finalize<<<1, 32, 0, st>>>(rows, Hp, planes, N, 0, stats);
+        k_finalize<<<planes, 32, 0, st>>>(rows, Hp, planes, N, 0, stats);
     }
     {
         CNNCRF_PROF("rowsums", st);
-        k_rowsums<<<ceil_div(nt, 128), 128, 0, st>>>(rgba, Wp, Hp, planes, gray, 1, stats, rows);
+        k_rowsums<<<ceil_div(nthreads, 256), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 1, stats, rows);
     }
     {
         CNNCRF_PROF("finalize", st);
-        k_finalize<<<1, 32, 0, st>>>(rows, Hp, planes, N, 1, stats);
+        k_finalize<<<planes, 32, 0, st>>>(rows, Hp, planes, N, 1, stats);
     }
     {
         CNNCRF_PROF("norm_write", st);

@@ -73,8 +73,21 @@ void set_threads(int t)
 
 // ---------------------------------------------------------------- normalise
 // stereo/colorstereonet.cpp:53-64 (+ xy 102-121), stereo/utils.cu:169-237.
-// Sums are FP64 in a fixed order (rows sequentially, then row partials
-// sequentially); the reference's thrust reduction order is unspecified.
+// Sums are FP64 in a fixed order (the reference's thrust reduction order is
+// unspecified): 32 partial sums, partial j taking elements j, j+32, ... in
+// ascending order, combined by an xor butterfly 16, 8, 4, 2, 1 -- first per
+// row, then over the row sums.
+double tree_sum_strided(const double *v, long n)
+{
+    double s[32] = {0}, t[32];
+    for (long i = 0; i < n; ++i) s[i % 32] += v[i];
+    for (int off = 16; off >= 1; off >>= 1) {
+        for (int j = 0; j < 32; ++j) t[j] = s[j] + s[j ^ off];
+        std::memcpy(s, t, sizeof s);
+    }
+    return s[0];
+}
+
 template <class T>
 void normalize_T(const float *rgba, int Wp, int Hp, int ic, T *out)
 {
@@ -91,26 +104,23 @@ void normalize_T(const float *rgba, int Wp, int Hp, int ic, T *out)
             else
                 pl[i] = (T)px[c];
         }
+        std::vector<double> row((size_t)Wp);
         for (int y = 0; y < Hp; ++y) {
-            double s = 0.0;
-            for (int x = 0; x < Wp; ++x) s += (double)pl[(long)y * Wp + x];
-            rs[y] = s;
+            for (int x = 0; x < Wp; ++x) row[x] = (double)pl[(long)y * Wp + x];
+            rs[y] = tree_sum_strided(row.data(), Wp);
         }
-        double tot = 0.0;
-        for (int y = 0; y < Hp; ++y) tot += rs[y];
+        double tot = tree_sum_strided(rs.data(), Hp);
         T mean = (T)(tot / (double)N);
         for (long i = 0; i < N; ++i) pl[i] = pl[i] - mean;
         for (int y = 0; y < Hp; ++y) {
-            double s = 0.0;
             for (int x = 0; x < Wp; ++x) {
                 T v = pl[(long)y * Wp + x];
                 T sq = v * v;
-                s += (double)sq;
+                row[x] = (double)sq;
             }
-            rs[y] = s;
+            rs[y] = tree_sum_strided(row.data(), Wp);
         }
-        tot = 0.0;
-        for (int y = 0; y < Hp; ++y) tot += rs[y];
+        tot = tree_sum_strided(rs.data(), Hp);
         T sd = (T)std::sqrt(tot / (double)N);
         for (long i = 0; i < N; ++i) out[i * ic + c] = sd > (T)0 ? pl[i] / sd : (T)0;
     }

@@ -102,4 +102,4 @@ def test_bf16_pipeline_label_change(cuda, oracle):
         labs.append(st.labels_device().cpu().numpy())
     changed = float((labs[0] != labs[1]).mean())
     print("BF16 vs FP32 label change: %.4f" % changed)
-    assert changed <= 0.05
+    assert changed <= 0.01
