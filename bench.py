@@ -229,11 +229,25 @@ def run_profile(args):
     return 0
 
 
+def make_batch(cnncrf, wl, B, precision, graph, stream, seed0):
+    from cnncrf import scenes
+    from cnncrf.api import StereoBatch
+    b = StereoBatch(precision=precision, unary=cnncrf.UNARY_ONE_MINUS_DOT, topology=cnncrf.TOPO_ALL3X3,
+                    feat_channels=wl["feat"], pw_channels=wl["pw"], crf_shape=cnncrf.RHO_LINEAR,
+                    num_layers=wl["layers"], seed=wl["seed"], graph=graph, stream=stream)
+    sc = [scenes.kitti_scene(wl["W"], wl["H"], wl["D"], seed=seed0 + i) for i in range(B)]
+    for _ in range(B):
+        b.add_pair(wl["W"], wl["H"], 0.0, 1.0, float(wl["D"] - 1))
+    return b, sc
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=8, help="KITTI pairs per step (the batched form)")
+    ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -253,133 +267,143 @@ def main():
     rank, world, local = dist_setup()
     torch.cuda.set_device(local)
     wl = WORKLOAD
-    W, H, D = wl["W"], wl["H"], wl["D"]
+    W, H, D, B = wl["W"], wl["H"], wl["D"], args.batch
     precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
+    crf = (wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], wl["lam"])
     stream = torch.cuda.Stream()
-    scene = scenes.kitti_scene(W, H, D, seed=rank)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     with torch.cuda.stream(stream):
-        st = build_stereo(cnncrf, wl, precision, stream)
-        dl = torch.from_numpy(scene["left"]).cuda()
-        dr = torch.from_numpy(scene["right"]).cuda()
-        hl = torch.from_numpy(scene["left"]).pin_memory()
-        hr = torch.from_numpy(scene["right"]).pin_memory()
-        hout = torch.empty((H, W), dtype=torch.float32).pin_memory()
-        flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+        b, sc = make_batch(cnncrf, wl, B, precision, not args.no_graph, stream, seed0=1000 * rank)
+        dl = [torch.from_numpy(x["left"]).cuda() for x in sc]
+        dr = [torch.from_numpy(x["right"]).cuda() for x in sc]
+        hl = [torch.from_numpy(x["left"]).pin_memory() for x in sc]
+        hr = [torch.from_numpy(x["right"]).pin_memory() for x in sc]
+        hout = [torch.empty((H, W), dtype=torch.float32).pin_memory() for _ in range(B)]
 
         def step_device():
-            st.set_color_images(dl, dr)
-            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+            for i in range(B):
+                b.set_images(i, dl[i], dr[i])
+            b.run(*crf)
 
         def step_e2e():
-            st.set_color_images(hl, hr)
-            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
-            st.get_output_into(hout)
+            for i in range(B):
+                b.set_images(i, hl[i], hr[i])
+            b.run(*crf)
+            for i in range(B):
+                b.get_output(i, hout[i])
 
         for _ in range(max(args.warmup, 3)):
             step_device()
         step_e2e()
+        b.check()
         torch.cuda.synchronize()
 
-        # ---- timed region (device-resident inputs)
+        def timed(fn, steps):
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(steps)]
+            barrier(world)
+            torch.cuda.synchronize()
+            for a, e in evs:
+                flush.zero_()
+                a.record(stream)
+                fn()
+                e.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            return allmax(sum(a.elapsed_time(e) for a, e in evs), world)
+
+        # ---- timed region: device-resident inputs (graph replay of the batch step)
         clocks = ClockSampler(local)
-        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        barrier(world)
-        torch.cuda.synchronize()
         clocks.start()
+        l0 = _lib.kernel_launches()
+        t_ms = timed(step_device, args.steps)
+        launches = _lib.kernel_launches() - l0
+        clk = clocks.stop()
+        value = args.steps * B * world / (t_ms / 1000.0)
+        # ---- end to end through the public API from pinned host buffers
+        e_ms = timed(step_e2e, args.steps)
+        e2e = args.steps * B * world / (e_ms / 1000.0)
+        b.check()
+        labels0 = b.labels_device(0).cpu().numpy()
+        disp0 = b.get_output(0)
+
+        # ---- per-kernel device time: the same batch step run eagerly with
+        # CUDA events around every launch on its stream
+        bp, _ = make_batch(cnncrf, wl, B, precision, False, stream, seed0=1000 * rank)
+        for i in range(B):
+            bp.set_images(i, dl[i], dr[i])
+        bp.run(*crf)
+        torch.cuda.synchronize()
         _lib.profile_reset()
         _lib.profile_enable(True)
-        l0 = _lib.kernel_launches()
-        for a, b in evs:
-            flush.zero_()
-            a.record(stream)
-            step_device()
-            b.record(stream)
-        torch.cuda.synchronize()
-        launches = _lib.kernel_launches() - l0
+        nprof = max(3, args.steps // 4)
+        p_ms = timed(lambda: bp.run(*crf), nprof)
         _lib.profile_enable(False)
-        barrier(world)
-        clk = clocks.stop()
-        t_ms = sum(a.elapsed_time(b) for a, b in evs)
-        t_ms = allmax(t_ms, world)
-        value = args.steps * world / (t_ms / 1000.0)
-
-        prof = {}
-        for kname in _lib.profile_kernels():
-            n, tot = _lib.profile_query(kname)
-            prof[kname] = (n, tot)
+        prof = {k: _lib.profile_query(k) for k in _lib.profile_kernels()}
         _lib.profile_reset()
+        del bp
+        if args.no_graph:
+            launches_per_step = launches / args.steps
+        else:
+            launches_per_step = sum(n for n, _ in prof.values()) / nprof
 
-        # ---- end to end through the public API, host buffers
-        evs2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        barrier(world)
-        torch.cuda.synchronize()
-        for a, b in evs2:
-            flush.zero_()
-            a.record(stream)
-            step_e2e()
-            b.record(stream)
-        torch.cuda.synchronize()
-        e_ms = allmax(sum(a.elapsed_time(b) for a, b in evs2), world)
-        e2e = args.steps * world / (e_ms / 1000.0)
-
-        labels = st.labels_device().cpu().numpy()
-        disp = st.get_output()
-
-    # ---- BF16 vs FP32: disparity change on the same pair, FP32 pairs/s
+    # ---- BF16 vs FP32: label change on the same pair, single-pair FP32 pairs/s
     cmp = {}
     if precision == cnncrf.BF16:
         with torch.cuda.stream(stream):
             st32 = build_stereo(cnncrf, wl, cnncrf.FP32, stream)
-            st32.set_color_images(dl, dr)
+            st32.set_color_images(dl[0], dr[0])
             st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
             torch.cuda.synchronize()
-            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
             n32 = 3
-            ev[0].record(stream)
-            for _ in range(n32):
-                st32.set_color_images(dl, dr)
-                st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
-            ev[1].record(stream)
-            torch.cuda.synchronize()
+
+            def step32():
+                st32.set_color_images(dl[0], dr[0])
+                st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0,
+                                               wl["lam"])
+            t32 = timed(step32, n32)
             lab32 = st32.labels_device().cpu().numpy()
-            cmp = {"fp32_pairs_per_s": n32 / (ev[0].elapsed_time(ev[1]) / 1000.0),
-                   "disparity_change_vs_fp32": float((lab32 != labels).mean())}
-            cmp["speedup_vs_fp32"] = value / world / cmp["fp32_pairs_per_s"]
+            st1 = build_stereo(cnncrf, wl, cnncrf.BF16, stream)
+            step1 = lambda: (st1.set_color_images(dl[0], dr[0]),
+                             st1.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"],
+                                                           0.0, 0.0, wl["lam"]))
+            step1()
+            t1 = timed(step1, n32)
+            cmp = {"fp32_single_pair_pairs_per_s": n32 / (t32 / 1000.0),
+                   "bf16_single_pair_pairs_per_s": n32 / (t1 / 1000.0),
+                   "disparity_change_vs_fp32": float((lab32 != labels0).mean())}
+            cmp["speedup_vs_fp32"] = value / world / cmp["fp32_single_pair_pairs_per_s"]
 
     if rank != 0:
         return 0
 
     peaks, peak_src = measured_peaks()
     tc_f, simt_f = conv_flops(W, H, wl["layers"], wl["feat"], 3, wl["pw"])
-    conv_name = "conv_tc" if "conv_tc" in prof else "conv_simt"
-    kernels = {k: {"launches": n, "total_ms": round(t, 4), "share": None} for k, (n, t) in prof.items()}
+    kernels = {k: {"launches": n, "total_ms": round(t, 4)} for k, (n, t) in prof.items()}
     tot = sum(t for _, t in prof.values()) or 1.0
     for k in kernels:
         kernels[k]["share"] = round(prof[k][1] / tot, 4)
     roof = None
+    conv_name = "conv_tc" if "conv_tc" in prof else "conv_simt"
     if conv_name in prof:
         n, t = prof[conv_name]
-        flops = tc_f if conv_name == "conv_tc" else tc_f + simt_f
-        achieved = flops * args.steps / (t / 1000.0) / 1e12
-        if conv_name == "conv_tc":
-            roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved,
-                    "peak": peaks["bf16_tflops"], "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
-                    "traffic": None, "peak_source": peak_src + " (bf16 dense burst)"}
-        else:
-            roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
-                    "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-                    "peak_source": peak_src + " (bf16 dense burst; this FP32 SIMT kernel cannot reach it)"}
-    crf = None
+        flops = (tc_f if conv_name == "conv_tc" else tc_f + simt_f) * B * nprof
+        achieved = flops / (t / 1000.0) / 1e12
+        roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                "peak_source": peak_src + " (bf16 dense burst)",
+                "per_launch": "FLOPs of the tensor-core layers of %d pairs / their summed launch time" % B}
+    crf_roof = None
     if "crf_h" in prof and "crf_v" in prof:
         n = prof["crf_h"][0] + prof["crf_v"][0]
         t = prof["crf_h"][1] + prof["crf_v"][1]
-        gbs = crf_bytes_per_pass(W, H, D) * n / (t / 1000.0) / 1e9
-        crf = {"kernel": "crf_h+crf_v", "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-               "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src}
+        gbs = crf_bytes_per_pass(W, H, D) * B * n / (t / 1000.0) / 1e9
+        crf_roof = {"kernel": "crf_h+crf_v", "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src}
 
     cpu = None
     if not args.no_cpu_baseline:
-        v, dt = cpu_pairs_per_s(wl, scene, 1)
+        v, dt = cpu_pairs_per_s(wl, sc[0], 1)
         cpu = {"value": v, "unit": "pairs/s", "cores": os.cpu_count(), "kind": "port",
                "sample": "one full 1242x375 D=128 pair (CNN, correlation, CRF, remap), %.1f s" % dt}
 
@@ -387,18 +411,20 @@ def main():
         "metric": METRIC, "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16" if precision == cnncrf.BF16 else "f32",
-        "data": "synthetic (seeded KITTI-shaped scene: ground plane + 15 boxes)",
+        "data": "synthetic (seeded KITTI-shaped scenes: ground plane + 15 boxes)",
         "config": {"workload": wl["name"], "W": W, "H": H, "D": D, "crf_iters": wl["crf_iters"],
+                   "pairs_per_step": B, "graph": not args.no_graph,
                    "net": "7x3x3 conv 100ch + L2 norm, 1-dot unary, pairwise CNN 3x3-3x3-1x1",
                    "crf": "truncated linear L1=0.5 T=3", "l2": "flushed (256 MiB write) between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": 2 * W * H * 4 * 4,
-                "d2h_bytes_per_step": W * H * 4},
-        "gpu_launches": launches,
-        "roofline": roof, "crf_roofline": crf, "kernels": kernels, "clocks": clk,
+        "e2e": {"value": e2e, "unit": "pairs/s", "h2d_bytes_per_step": B * 2 * W * H * 4 * 4,
+                "d2h_bytes_per_step": B * W * H * 4},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "roofline": roof, "crf_roofline": crf_roof,
+        "kernels": kernels, "kernel_profile_ms_per_step": p_ms / nprof, "clocks": clk,
         "cpu_baseline": cpu,
         "precision_check": cmp,
-        "disparity_stats": {"mean": float(np.mean(disp)), "bad3px_vs_gt": scenes.bad_pixels(disp, scene["disp"])},
+        "disparity_stats": {"bad3px_vs_gt_pair0": scenes.bad_pixels(disp0, sc[0]["disp"])},
     }
     print(json.dumps(line))
     return 0

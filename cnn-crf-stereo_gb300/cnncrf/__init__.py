@@ -17,7 +17,7 @@ __all__ = ["lib", "LIB_PATH", "CnnCrfError", "FP32", "BF16", "TOPO_REF", "TOPO_A
 def __getattr__(name):
     # the torch-backed API is imported lazily so that the pure-C parts
     # (symbol checks, config parsing) work without touching CUDA
-    if name in ("StereoNet", "SlackProp", "Stereo", "crf_solve", "correlation_forward",
+    if name in ("StereoNet", "SlackProp", "Stereo", "StereoBatch", "crf_solve", "correlation_forward",
                 "remap_solution", "warp_image", "tv_fit", "tv_iterate", "as_device_tensor"):
         from . import api
         return getattr(api, name)

@@ -110,6 +110,22 @@ PROTOS = {
     "cnncrf_stereo_get_depth": ([vp, C.POINTER(i32)], i32),
     "cnncrf_stereo_lower_bound": ([vp, C.POINTER(C.c_double)], i32),
     "cnncrf_stereo_stage_times": ([vp, C.POINTER(f32), C.POINTER(f32), C.POINTER(f32), C.POINTER(f32)], i32),
+    "cnncrf_batch_create": ([C.POINTER(vp), C.POINTER(StereoOptions)], i32),
+    "cnncrf_batch_destroy": ([vp], i32),
+    "cnncrf_batch_set_stream": ([vp, vp], i32),
+    "cnncrf_batch_set_network": ([vp, i32, i32, i32, C.c_char_p, C.c_uint64], i32),
+    "cnncrf_batch_add_pair": ([vp, i32, i32, f32, f32, f32, C.POINTER(i32)], i32),
+    "cnncrf_batch_num_pairs": ([vp, C.POINTER(i32)], i32),
+    "cnncrf_batch_set_images": ([vp, i32, vp, vp], i32),
+    "cnncrf_batch_set_images_device": ([vp, i32, vp, vp], i32),
+    "cnncrf_batch_use_graph": ([vp, i32], i32),
+    "cnncrf_batch_run": ([vp, f32, f32, f32, i32, f32], i32),
+    "cnncrf_batch_get_output": ([vp, i32, vp], i32),
+    "cnncrf_batch_get_output_device": ([vp, i32, C.POINTER(vp)], i32),
+    "cnncrf_batch_get_labels_device": ([vp, i32, C.POINTER(vp)], i32),
+    "cnncrf_batch_get_volume_device": ([vp, i32, C.POINTER(vp), C.POINTER(i32)], i32),
+    "cnncrf_batch_lower_bound": ([vp, i32, C.POINTER(C.c_double)], i32),
+    "cnncrf_batch_check": ([vp], i32),
     "cnncrf_kernel_launches": ([C.POINTER(C.c_uint64)], i32),
     "cnncrf_profile_enable": ([i32], i32),
     "cnncrf_profile_reset": ([], i32),

@@ -21,7 +21,7 @@ import torch
 from . import _lib as L
 from ._lib import CnnCrfError, CrfOptions, NetDesc, StereoOptions, call
 
-__all__ = ["StereoNet", "SlackProp", "Stereo", "crf_solve", "correlation_forward", "remap_solution",
+__all__ = ["StereoNet", "SlackProp", "Stereo", "StereoBatch", "crf_solve", "correlation_forward", "remap_solution",
            "warp_image", "tv_fit", "tv_iterate", "CnnCrfError", "as_device_tensor"]
 
 
@@ -373,3 +373,81 @@ class Stereo:
         a, b, c, d = C.c_float(), C.c_float(), C.c_float(), C.c_float()
         call("cnncrf_stereo_stage_times", self._h, C.byref(a), C.byref(b), C.byref(c), C.byref(d))
         return dict(cnn=a.value, corr=b.value, crf=c.value, refine=d.value)
+
+
+class StereoBatch:
+    """Many pairs through computeSlackPropagation at once (cnncrf_batch_*)."""
+
+    def __init__(self, precision=L.BF16, unary=L.UNARY_ONE_MINUS_DOT, topology=L.TOPO_ALL3X3,
+                 feat_channels=100, pw_channels=64, ref_depth_rounding=False, crf_shape=L.RHO_LINEAR,
+                 crf_slack=0.5, matching=L.MATCH_COLORCNN_PAIRWISE, num_layers=7, with_xy=False,
+                 param_base=None, seed=0, graph=False, stream=None):
+        o = StereoOptions()
+        call("cnncrf_stereo_default_options", C.byref(o))
+        o.precision, o.unary, o.topology = precision, unary, topology
+        o.feat_channels, o.pw_channels = feat_channels, pw_channels
+        o.ref_depth_rounding = 1 if ref_depth_rounding else 0
+        o.crf_shape, o.crf_slack = crf_shape, crf_slack
+        self._h = C.c_void_p()
+        call("cnncrf_batch_create", C.byref(self._h), C.byref(o))
+        call("cnncrf_batch_set_stream", self._h, _stream_ptr(stream))
+        call("cnncrf_batch_set_network", self._h, matching, num_layers, 1 if with_xy else 0,
+             None if param_base is None else str(param_base).encode(), seed)
+        call("cnncrf_batch_use_graph", self._h, 1 if graph else 0)
+        self.shapes = []
+
+    def __del__(self):
+        if getattr(self, "_h", None) and L._lib is not None:
+            L.lib().cnncrf_batch_destroy(self._h)
+            self._h = None
+
+    def add_pair(self, width, height, disp_min, disp_step, disp_max):
+        i = C.c_int()
+        call("cnncrf_batch_add_pair", self._h, width, height, disp_min, disp_step, disp_max, C.byref(i))
+        self.shapes.append((height, width))
+        return i.value
+
+    def set_images(self, pair, left, right):
+        if isinstance(left, torch.Tensor) and left.is_cuda:
+            call("cnncrf_batch_set_images_device", self._h, pair, _ptr(left), _ptr(right))
+            return
+        if isinstance(left, torch.Tensor):
+            call("cnncrf_batch_set_images", self._h, pair, C.c_void_p(left.data_ptr()), C.c_void_p(right.data_ptr()))
+            return
+        l = np.ascontiguousarray(left, np.float32)
+        r = np.ascontiguousarray(right, np.float32)
+        call("cnncrf_batch_set_images", self._h, pair, l.ctypes.data_as(C.c_void_p), r.ctypes.data_as(C.c_void_p))
+
+    def run(self, L1, L2, delta, iterations, lambda_reg=1.0):
+        call("cnncrf_batch_run", self._h, L1, L2, float(delta), iterations, lambda_reg)
+
+    def check(self):
+        call("cnncrf_batch_check", self._h)
+
+    def get_output(self, pair, out=None):
+        H, W = self.shapes[pair]
+        if out is None:
+            out = np.empty((H, W), np.float32)
+        ptr = C.c_void_p(out.data_ptr()) if isinstance(out, torch.Tensor) else out.ctypes.data_as(C.c_void_p)
+        call("cnncrf_batch_get_output", self._h, pair, ptr)
+        return out
+
+    def labels_device(self, pair):
+        p = C.c_void_p()
+        call("cnncrf_batch_get_labels_device", self._h, pair, C.byref(p))
+        return as_device_tensor(p.value, self.shapes[pair], torch.int32)
+
+    def output_device(self, pair):
+        p = C.c_void_p()
+        call("cnncrf_batch_get_output_device", self._h, pair, C.byref(p))
+        return as_device_tensor(p.value, self.shapes[pair])
+
+    def volume_device(self, pair):
+        p, d = C.c_void_p(), C.c_int()
+        call("cnncrf_batch_get_volume_device", self._h, pair, C.byref(p), C.byref(d))
+        return as_device_tensor(p.value, self.shapes[pair] + (d.value,))
+
+    def lower_bound(self, pair):
+        v = C.c_double()
+        call("cnncrf_batch_lower_bound", self._h, pair, C.byref(v))
+        return v.value

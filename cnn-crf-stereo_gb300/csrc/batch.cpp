@@ -1,0 +1,409 @@
+// batch.cpp -- the batched form of Stereo::computeSlackPropagation for many
+// pairs at once (cnncrf_batch_*; no counterpart in the reference, whose
+// Stereo object holds one pair).
+//
+// Pairs with the same size and disparity range form a group.  A group runs as
+// one batch: one net over all its images (the tensor-core convolutions see
+// 2n images per launch), one correlation launch, one CRF launch per pass
+// over all n x H row chains / n x W column chains.  Each group has its own
+// stream, forked from and joined back into the caller's stream, so groups
+// of different sizes overlap on the GPU.  With graph capture on, the whole
+// fork / groups / join sequence is captured once into a CUDA graph and
+// replayed by later runs with the same parameters.
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "common.h"
+#include "kernels.h"
+#include "net.h"
+
+using namespace cnncrf;
+
+namespace {
+
+struct Group {
+    int W = 0, H = 0, depth = 0;
+    float dmin = 0, dstep = 1, dmax = 0;
+    std::vector<int> members; // global pair indices, in batch order
+    DevBuf img[2], padded[2], vol, pw, out, labels, ws;
+    cnncrf_net_t net = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+    size_t ws_bytes = 0;
+    ~Group()
+    {
+        if (net) cnncrf_net_destroy(net);
+        if (done) cudaEventDestroy(done);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+int log2i(int num)
+{
+    int r = 0;
+    while (num >>= 1) ++r;
+    return r;
+}
+
+} // namespace
+
+struct cnncrf_batch {
+    cnncrf_stereo_options o{};
+    int matching = CNNCRF_MATCH_COLORCNN_PAIRWISE, num_layers = 7, with_xy = 0;
+    std::string param_base;
+    bool xavier = true;
+    uint64_t seed = 0;
+    cudaStream_t st = nullptr;   // the caller's stream
+    cudaStream_t work = nullptr; // the batch's own stream (capturable even when `st` is the legacy stream)
+    cudaEvent_t in_ev = nullptr, out_ev = nullptr;
+    std::vector<std::unique_ptr<Group>> groups;
+    std::vector<std::pair<int, int>> loc; // pair -> (group, slot)
+    bool built = false;
+    // graph
+    bool use_graph = false;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t fork = nullptr;
+    float gL1 = 0, gL2 = 0, gdelta = 0, glambda = 0;
+    int giters = -1;
+    bool ran_eager = false;
+
+    ~cnncrf_batch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (fork) cudaEventDestroy(fork);
+        if (in_ev) cudaEventDestroy(in_ev);
+        if (out_ev) cudaEventDestroy(out_ev);
+        groups.clear();
+        if (work) cudaStreamDestroy(work);
+    }
+    void invalidate()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        giters = -1;
+        ran_eager = false;
+    }
+    int build();
+    int enqueue(float L1, float L2, float delta, int iters, float lambda);
+};
+
+int cnncrf_batch::build()
+{
+    if (matching != CNNCRF_MATCH_COLORCNN_PAIRWISE && matching != CNNCRF_MATCH_GRAYCNN_PAIRWISE)
+        return fail(CNNCRF_EUNSUPPORTED, "batch: only the pairwise (COLORPAIR) matching is batched");
+    bool gray = matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
+    for (auto &gp : groups) {
+        Group &g = *gp;
+        const int n = (int)g.members.size();
+        const size_t N = (size_t)g.W * g.H;
+        cnncrf_net_desc d{};
+        d.num_layers = num_layers;
+        d.topology = o.topology;
+        d.in_channels = gray ? 1 : (with_xy ? 5 : 3);
+        d.feat_channels = o.feat_channels;
+        d.unary = o.unary;
+        d.precision = o.precision;
+        d.with_pairwise = 1;
+        d.pw_channels = o.pw_channels;
+        int loss = 2 + (num_layers - 1) * (o.topology == CNNCRF_TOPO_REF ? 1 : 2);
+        int pad = loss / 2;
+        if (g.net) cnncrf_net_destroy(g.net);
+        g.net = nullptr;
+        CNNCRF_TRY(cnncrf_net_create(&g.net, &d, n, g.H + 2 * pad, g.W + 2 * pad));
+        if (!g.stream) CNNCRF_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+        if (!g.done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+        CNNCRF_TRY(cnncrf_net_set_stream(g.net, (cnncrf_stream_t)g.stream));
+        for (int s = 0; s < 2; ++s) {
+            CNNCRF_TRY(g.img[s].reserve(sizeof(float) * 4 * N * n));
+            CNNCRF_TRY(g.padded[s].reserve(sizeof(float) * 4 * (size_t)(g.W + 2 * pad) * (g.H + 2 * pad) * n));
+        }
+        CNNCRF_TRY(g.vol.reserve(sizeof(float) * N * g.depth * n));
+        CNNCRF_TRY(g.pw.reserve(sizeof(float) * 2 * N * n));
+        CNNCRF_TRY(g.out.reserve(sizeof(float) * N * n));
+        CNNCRF_TRY(g.labels.reserve(sizeof(int32_t) * N * n));
+        g.ws_bytes = k::crf_workspace_bytes(g.W, g.H, g.depth, n);
+        CNNCRF_TRY(g.ws.reserve(g.ws_bytes));
+        CNNCRF_TRY(cnncrf_net_init(g.net, g.dmin, g.dmax, g.dstep, 0, g.vol.as<float>(), g.pw.as<float>()));
+        if (g.net->D != g.depth)
+            return fail(CNNCRF_ESHAPE, "batch: disparity list has %d entries, volume depth %d", g.net->D, g.depth);
+        if (xavier) CNNCRF_TRY(cnncrf_net_init_xavier(g.net, seed));
+        else CNNCRF_TRY(cnncrf_net_set_all_params(g.net, (param_base + ".npz").c_str()));
+    }
+    if (!fork) CNNCRF_CUDA(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming));
+    if (!in_ev) CNNCRF_CUDA(cudaEventCreateWithFlags(&in_ev, cudaEventDisableTiming));
+    if (!out_ev) CNNCRF_CUDA(cudaEventCreateWithFlags(&out_ev, cudaEventDisableTiming));
+    if (!work) CNNCRF_CUDA(cudaStreamCreateWithFlags(&work, cudaStreamNonBlocking));
+    CNNCRF_CUDA(cudaDeviceSynchronize()); // parameter uploads done before any stream work
+    built = true;
+    return CNNCRF_OK;
+}
+
+// fork -> every group on its stream -> join, all enqueued on `work`
+int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lambda)
+{
+    k::CrfParams p;
+    int di = (int)delta;
+    if ((float)di != delta || di < 1 || di > 4) return fail(CNNCRF_EUNSUPPORTED, "batch: delta %g", delta);
+    p.L1 = L1, p.L2 = L2, p.delta = di, p.shape = o.crf_shape, p.slack = o.crf_slack;
+    CNNCRF_CUDA(cudaEventRecord(fork, work));
+    for (auto &gp : groups) {
+        Group &g = *gp;
+        const int n = (int)g.members.size();
+        const long N = (long)g.W * g.H;
+        cudaStream_t gs = g.stream;
+        CNNCRF_CUDA(cudaStreamWaitEvent(gs, fork, 0));
+        const int pad = g.net->pad;
+        CNNCRF_TRY(k::pad_rgba(g.img[0].as<float>(), g.W, g.H, pad, g.padded[0].as<float>(), gs, n));
+        CNNCRF_TRY(k::pad_rgba(g.img[1].as<float>(), g.W, g.H, pad, g.padded[1].as<float>(), gs, n));
+        CNNCRF_TRY(g.net->predict(g.padded[0].as<float>(), g.padded[1].as<float>()));
+        CNNCRF_TRY(k::scale(g.pw.as<float>(), 2 * N * n, lambda, gs)); // stereo/stereo.cpp:136-137
+        CNNCRF_TRY(k::crf_solve_batch(g.vol.as<float>(), g.pw.as<float>(), g.W, g.H, g.depth, n, p, iters,
+                                      g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, gs));
+        CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, gs));
+        CNNCRF_CUDA(cudaEventRecord(g.done, gs));
+        CNNCRF_CUDA(cudaStreamWaitEvent(work, g.done, 0));
+    }
+    return CNNCRF_OK;
+}
+
+extern "C" {
+
+int cnncrf_batch_create(cnncrf_batch_t *b, const cnncrf_stereo_options *opt)
+{
+    clear_error();
+    if (!b) return fail(CNNCRF_EINVAL, "null argument");
+    auto *bt = new cnncrf_batch;
+    if (opt) bt->o = *opt;
+    else cnncrf_stereo_default_options(&bt->o);
+    *b = bt;
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_destroy(cnncrf_batch_t b)
+{
+    if (b) cudaDeviceSynchronize();
+    delete b;
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_set_stream(cnncrf_batch_t b, cnncrf_stream_t stream)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    b->st = (cudaStream_t)stream;
+    b->invalidate();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_set_network(cnncrf_batch_t b, int matching, int num_layers, int with_xy, const char *param_base,
+                             uint64_t seed)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    b->matching = matching;
+    b->num_layers = num_layers;
+    b->with_xy = with_xy ? 1 : 0;
+    b->xavier = param_base == nullptr;
+    if (param_base) b->param_base = param_base;
+    b->seed = seed;
+    b->built = false;
+    b->invalidate();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_add_pair(cnncrf_batch_t b, int width, int height, float disp_min, float disp_step, float disp_max,
+                          int *pair_index)
+{
+    clear_error();
+    if (!b || !pair_index) return fail(CNNCRF_EINVAL, "null argument");
+    if (width < 1 || height < 1 || !(disp_step > 0.0f)) return fail(CNNCRF_EINVAL, "add_pair: bad size / step");
+    int depth = (int)((disp_max - disp_min) / disp_step + 1);
+    if (depth < 1) return fail(CNNCRF_EINVAL, "add_pair: empty disparity range");
+    if (b->o.ref_depth_rounding) depth = std::min(256, 1 << (log2i(depth - 1) + 1));
+    float dmax = disp_min + (depth - 1) * disp_step;
+    int gi = -1;
+    for (size_t i = 0; i < b->groups.size(); ++i) {
+        Group &g = *b->groups[i];
+        if (g.W == width && g.H == height && g.dmin == disp_min && g.dstep == disp_step && g.depth == depth) {
+            gi = (int)i;
+            break;
+        }
+    }
+    if (gi < 0) {
+        b->groups.emplace_back(new Group);
+        Group &g = *b->groups.back();
+        g.W = width, g.H = height, g.depth = depth, g.dmin = disp_min, g.dstep = disp_step, g.dmax = dmax;
+        gi = (int)b->groups.size() - 1;
+    }
+    Group &g = *b->groups[gi];
+    *pair_index = (int)b->loc.size();
+    b->loc.push_back({gi, (int)g.members.size()});
+    g.members.push_back(*pair_index);
+    b->built = false;
+    b->invalidate();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_num_pairs(cnncrf_batch_t b, int *n)
+{
+    if (!b || !n) return fail(CNNCRF_EINVAL, "null argument");
+    *n = (int)b->loc.size();
+    return CNNCRF_OK;
+}
+
+static int stage(cnncrf_batch_t b, int pair, const float *l, const float *r, cudaMemcpyKind kind)
+{
+    if (!b || !l || !r) return fail(CNNCRF_EINVAL, "set_images: null argument");
+    if (pair < 0 || pair >= (int)b->loc.size()) return fail(CNNCRF_EINVAL, "set_images: pair %d", pair);
+    if (!b->built) CNNCRF_TRY(b->build());
+    Group &g = *b->groups[b->loc[pair].first];
+    const size_t bytes = sizeof(float) * 4 * (size_t)g.W * g.H;
+    const size_t off = bytes * b->loc[pair].second;
+    CNNCRF_CUDA(cudaMemcpyAsync((char *)g.img[0].get() + off, l, bytes, kind, b->st));
+    CNNCRF_CUDA(cudaMemcpyAsync((char *)g.img[1].get() + off, r, bytes, kind, b->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_set_images(cnncrf_batch_t b, int pair, const float *h_left, const float *h_right)
+{
+    clear_error();
+    return stage(b, pair, h_left, h_right, cudaMemcpyHostToDevice);
+}
+
+int cnncrf_batch_set_images_device(cnncrf_batch_t b, int pair, const float *d_left, const float *d_right)
+{
+    clear_error();
+    return stage(b, pair, d_left, d_right, cudaMemcpyDeviceToDevice);
+}
+
+int cnncrf_batch_use_graph(cnncrf_batch_t b, int enable)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    b->use_graph = enable != 0;
+    b->invalidate();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
+{
+    clear_error();
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    if (b->loc.empty()) return fail(CNNCRF_ESTATE, "batch: no pairs");
+    if (!b->built) CNNCRF_TRY(b->build());
+    // hand over from the caller's stream (image copies) to the batch's stream
+    CNNCRF_CUDA(cudaEventRecord(b->in_ev, b->st));
+    CNNCRF_CUDA(cudaStreamWaitEvent(b->work, b->in_ev, 0));
+    int rc = CNNCRF_OK;
+    const bool same = b->giters == iterations && b->gL1 == L1 && b->gL2 == L2 && b->gdelta == delta &&
+                      b->glambda == lambda_reg;
+    if (b->use_graph && b->exec && same) {
+        cudaError_t e = cudaGraphLaunch(b->exec, b->work);
+        if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
+    } else if (!b->use_graph || !b->ran_eager || !same) {
+        // eager (it also sets every kernel attribute); with graphs on, the
+        // next run with the same parameters captures
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        rc = b->enqueue(L1, L2, delta, iterations, lambda_reg);
+        b->ran_eager = rc == CNNCRF_OK;
+        b->giters = iterations, b->gL1 = L1, b->gL2 = L2, b->gdelta = delta, b->glambda = lambda_reg;
+    } else {
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(b->work, cudaStreamCaptureModeRelaxed);
+        if (e != cudaSuccess) {
+            rc = fail(CNNCRF_ECUDA, "batch: begin capture: %s", cudaGetErrorString(e));
+        } else {
+            rc = b->enqueue(L1, L2, delta, iterations, lambda_reg);
+            e = cudaStreamEndCapture(b->work, &graph);
+            if (rc == CNNCRF_OK && e != cudaSuccess)
+                rc = fail(CNNCRF_ECUDA, "batch: graph capture failed: %s", cudaGetErrorString(e));
+            if (rc == CNNCRF_OK) {
+                e = cudaGraphInstantiate(&b->exec, graph, 0);
+                if (e != cudaSuccess) {
+                    b->exec = nullptr;
+                    rc = fail(CNNCRF_ECUDA, "batch: graph instantiation failed: %s", cudaGetErrorString(e));
+                }
+            }
+            if (graph) cudaGraphDestroy(graph);
+            if (rc == CNNCRF_OK) {
+                e = cudaGraphLaunch(b->exec, b->work);
+                if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
+            }
+        }
+    }
+    // hand back: the caller's stream sees the results after this point
+    CNNCRF_CUDA(cudaEventRecord(b->out_ev, b->work));
+    CNNCRF_CUDA(cudaStreamWaitEvent(b->st, b->out_ev, 0));
+    return rc;
+}
+
+static Group *group_of(cnncrf_batch_t b, int pair, size_t *off_px)
+{
+    if (!b || pair < 0 || pair >= (int)b->loc.size() || !b->built) return nullptr;
+    Group *g = b->groups[b->loc[pair].first].get();
+    *off_px = (size_t)g->W * g->H * b->loc[pair].second;
+    return g;
+}
+
+int cnncrf_batch_get_output(cnncrf_batch_t b, int pair, float *h_out)
+{
+    size_t off;
+    Group *g = group_of(b, pair, &off);
+    if (!g || !h_out) return fail(CNNCRF_EINVAL, "get_output: bad pair / null output");
+    CNNCRF_CUDA(cudaMemcpyAsync(h_out, g->out.as<float>() + off, sizeof(float) * g->W * g->H,
+                                cudaMemcpyDeviceToHost, b->st));
+    CNNCRF_CUDA(cudaStreamSynchronize(b->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_get_output_device(cnncrf_batch_t b, int pair, const float **d_out)
+{
+    size_t off;
+    Group *g = group_of(b, pair, &off);
+    if (!g || !d_out) return fail(CNNCRF_EINVAL, "get_output_device: bad pair");
+    *d_out = g->out.as<float>() + off;
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_get_labels_device(cnncrf_batch_t b, int pair, const int32_t **d_labels)
+{
+    size_t off;
+    Group *g = group_of(b, pair, &off);
+    if (!g || !d_labels) return fail(CNNCRF_EINVAL, "get_labels_device: bad pair");
+    *d_labels = g->labels.as<int32_t>() + off;
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_get_volume_device(cnncrf_batch_t b, int pair, const float **d_vol, int *depth)
+{
+    size_t off;
+    Group *g = group_of(b, pair, &off);
+    if (!g || !d_vol) return fail(CNNCRF_EINVAL, "get_volume_device: bad pair");
+    *d_vol = g->vol.as<float>() + off * g->depth;
+    if (depth) *depth = g->depth;
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_lower_bound(cnncrf_batch_t b, int pair, double *lb)
+{
+    size_t off;
+    Group *g = group_of(b, pair, &off);
+    if (!g || !lb) return fail(CNNCRF_EINVAL, "lower_bound: bad pair");
+    const double *d = k::crf_lb_device(g->ws.get(), g->W, g->H, g->depth, (int)g->members.size());
+    CNNCRF_CUDA(cudaMemcpyAsync(lb, d + b->loc[pair].second, sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    CNNCRF_CUDA(cudaStreamSynchronize(b->st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_check(cnncrf_batch_t b)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    CNNCRF_CUDA(cudaStreamSynchronize(b->st));
+    for (auto &g : b->groups)
+        if (g->net) CNNCRF_TRY(g->net->check_error());
+    return CNNCRF_OK;
+}
+
+} // extern "C"

@@ -36,6 +36,9 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
     const int tid = threadIdx.x;
     const int oy = blockIdx.y;
     const int ox0 = blockIdx.x * BM;
+    a.in += (long)blockIdx.z * a.in_img; // image of the batch
+    if (a.out16) a.out16 = (char *)a.out16 + (long)blockIdx.z * a.out_img * 2;
+    else a.out += (long)blockIdx.z * a.out_img;
     const int a_kk = tid & 7, a_p = tid >> 3;
     const int b_kk = tid >> 5, b_n = (tid & 31) * 4;
     const int tx = tid & 15, ty = tid >> 4;
@@ -144,6 +147,9 @@ __global__ void __launch_bounds__(128) k_conv_first(ConvArgs a, int Ho, int Wo, 
     __syncthreads();
     const int oy = blockIdx.y, ox = blockIdx.x * blockDim.x + threadIdx.x;
     if (ox >= Wo) return;
+    a.in += (long)blockIdx.z * a.in_img; // image of the batch
+    if (a.out16) a.out16 = (char *)a.out16 + (long)blockIdx.z * a.out_img * 2;
+    else a.out += (long)blockIdx.z * a.out_img;
     float acc[CP];
 #pragma unroll
     for (int co = 0; co < CP; ++co) acc[co] = 0.0f;
@@ -190,6 +196,8 @@ __global__ void k_head2(const float *__restrict__ in, int npx, int Cin, const fl
 {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npx) return;
+    in += (long)blockIdx.y * npx * Cin; // image of the batch
+    out += (long)blockIdx.y * 2 * npx;
     const float *x = in + (long)p * Cin;
     float a0 = 0.0f, a1 = 0.0f;
     for (int ci = 0; ci < Cin; ++ci) {
@@ -221,7 +229,7 @@ int conv_simt(const ConvArgs &a, cudaStream_t st)
     if (Ho <= 0 || Wo <= 0) return fail(CNNCRF_ESHAPE, "conv_simt: empty output");
     int K = a.kh * a.kw * a.Cin;
     if (K <= 45 && (a.Cout == 100 || a.Cout == 64) && a.Cout == (a.Cout & ~1)) {
-        dim3 g(ceil_div(Wo, 128), Ho);
+        dim3 g(ceil_div(Wo, 128), Ho, a.n_img);
         size_t smem = sizeof(float) * (size_t)K * ((a.Cout + 3) & ~3);
         if (a.Cout == 100) {
             CNNCRF_PROF("conv_first", st);
@@ -233,7 +241,7 @@ int conv_simt(const ConvArgs &a, cudaStream_t st)
         CNNCRF_CHECK_LAUNCH();
         return CNNCRF_OK;
     }
-    dim3 grid(ceil_div(Wo, BM), Ho);
+    dim3 grid(ceil_div(Wo, BM), Ho, a.n_img);
     {
         CNNCRF_PROF("conv_simt", st);
         k_conv_simt<<<grid, 256, 0, st>>>(a, Ho, Wo, K);
@@ -242,11 +250,11 @@ int conv_simt(const ConvArgs &a, cudaStream_t st)
     return CNNCRF_OK;
 }
 
-int conv_head2(const float *in, int npx, int Cin, const float *w, float *out, cudaStream_t st)
+int conv_head2(const float *in, int npx, int Cin, const float *w, float *out, cudaStream_t st, int n_img)
 {
     {
         CNNCRF_PROF("head2", st);
-        k_head2<<<ceil_div(npx, 256), 256, 0, st>>>(in, npx, Cin, w, out);
+        k_head2<<<dim3(ceil_div(npx, 256), n_img), 256, 0, st>>>(in, npx, Cin, w, out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

@@ -252,8 +252,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::fence_before_sync();
             tc::mbar_arrive(&tempty[buf]);
             if (p.mode == 2 && valid) {
-                float *o = (float *)p.out;
                 const size_t plane = (size_t)p.Ho * p.Wo;
+                float *o = (float *)p.out + (size_t)img * 2 * plane; // [img][2][Ho][Wo]
                 o[(size_t)y * p.Wo + x] = fabsf(a0);
                 o[plane + (size_t)y * p.Wo + x] = fabsf(a1);
             }

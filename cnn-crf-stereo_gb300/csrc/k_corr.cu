@@ -38,9 +38,12 @@ template <typename TIN>
 __global__ void __launch_bounds__(256)
     k_corr(const TIN *__restrict__ fl, const TIN *__restrict__ fr, int H, int W, int C, int cs,
            const float *__restrict__ list, int D, int omin, int omax, int interp, int unary,
-           float *__restrict__ out)
+           float *__restrict__ out, long fps)
 {
     extern __shared__ float sm[];
+    fl += blockIdx.z * fps; // pair of the batch
+    fr += blockIdx.z * fps;
+    out += (long)blockIdx.z * H * W * D;
     const int y = blockIdx.y;
     const int x0 = blockIdx.x * PIX;
     const int CS = C + 1;
@@ -148,9 +151,12 @@ template <typename TIN>
 __global__ void __launch_bounds__(256)
     k_corr_band(const TIN *__restrict__ fl, const TIN *__restrict__ fr, int H, int W, int C, int cs,
                 const float *__restrict__ list, int D, int omin, int omax, int NJ, int unary,
-                float *__restrict__ out)
+                float *__restrict__ out, long fps)
 {
     extern __shared__ float sm[];
+    fl += blockIdx.z * fps; // pair of the batch
+    fr += blockIdx.z * fps;
+    out += (long)blockIdx.z * H * W * D;
     const int y = blockIdx.y;
     const int x0 = blockIdx.x * PIX;
     const int RB = NJ * 32;                  // band columns computed (>= PIX + omax - omin)
@@ -261,10 +267,11 @@ __global__ void __launch_bounds__(256)
 
 template <typename TIN>
 static int corr_launch(const TIN *fl, const TIN *fr, int H, int W, int C, int cs, const float *d_list, int D,
-                       int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
+                       int omin, int omax, bool interp, int unary, float *out, cudaStream_t st, int npairs,
+                       long fps)
 {
     if (D < 1 || D > 32 * MAXP) return fail(CNNCRF_EINVAL, "correlation: D=%d outside [1,%d]", D, 32 * MAXP);
-    dim3 grid(ceil_div(W, PIX), H);
+    dim3 grid(ceil_div(W, PIX), H, npairs);
     const int NJ = ceil_div(PIX + omax - omin, 32);
     // phase 1 holds the two feature tiles, phase 2 the result tile T in the
     // same storage: allocate the larger of the two
@@ -275,7 +282,8 @@ static int corr_launch(const TIN *fl, const TIN *fr, int H, int W, int C, int cs
         CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_band<TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)band_smem));
         {
             CNNCRF_PROF("corr", st);
-            k_corr_band<TIN><<<grid, 256, band_smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, NJ, unary, out);
+            k_corr_band<TIN><<<grid, 256, band_smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, NJ, unary, out,
+                                                             fps);
         }
         CNNCRF_CHECK_LAUNCH();
         return CNNCRF_OK;
@@ -287,23 +295,24 @@ static int corr_launch(const TIN *fl, const TIN *fr, int H, int W, int C, int cs
     CNNCRF_CUDA(cudaFuncSetAttribute(k_corr<TIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     {
         CNNCRF_PROF("corr", st);
-        k_corr<TIN><<<grid, 256, smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, interp ? 1 : 0, unary, out);
+        k_corr<TIN><<<grid, 256, smem, st>>>(fl, fr, H, W, C, cs, d_list, D, omin, omax, interp ? 1 : 0, unary, out,
+                                              fps);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
 int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list, int D, int omin,
-                int omax, bool interp, int unary, float *out, cudaStream_t st)
+                int omax, bool interp, int unary, float *out, cudaStream_t st, int npairs, long fps)
 {
-    return corr_launch<float>(fl, fr, H, W, C, C, d_list, D, omin, omax, interp, unary, out, st);
+    return corr_launch<float>(fl, fr, H, W, C, C, d_list, D, omin, omax, interp, unary, out, st, npairs, fps);
 }
 
 int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs, const float *d_list, int D,
-                     int omin, int omax, bool interp, int unary, float *out, cudaStream_t st)
+                     int omin, int omax, bool interp, int unary, float *out, cudaStream_t st, int npairs, long fps)
 {
     return corr_launch<__nv_bfloat16>((const __nv_bfloat16 *)fl, (const __nv_bfloat16 *)fr, H, W, C, cs, d_list,
-                                      D, omin, omax, interp, unary, out, st);
+                                      D, omin, omax, interp, unary, out, st, npairs, fps);
 }
 
 } // namespace k

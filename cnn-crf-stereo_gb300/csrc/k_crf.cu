@@ -202,13 +202,23 @@ template <int P, int DELTA, bool HPASS>
 __global__ void __launch_bounds__(64)
     k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
                 float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
-                int32_t *__restrict__ labels, double *__restrict__ cmin_out)
+                int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
 {
     extern __shared__ float4 smem4[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int chain = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int gchain = blockIdx.x * (blockDim.x >> 5) + wib;
     const int n = HPASS ? W : H;
-    if (chain >= (HPASS ? H : W)) return;
+    const int nch = HPASS ? H : W;
+    if (gchain >= nch * npairs) return;
+    // pair of the batch and chain within it
+    const int pair = gchain / nch, chain = gchain - pair * nch;
+    const long pnd = (long)W * H * D * pair;
+    theta += pnd;
+    phi += pnd;
+    Lbuf += pnd;
+    wgt += wps * pair;
+    if (labels) labels += (long)W * H * pair;
+    cmin_out += (long)nch * pair;
     float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P));
     float *ring = wsm + nmax;
     auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
@@ -308,13 +318,16 @@ __global__ void __launch_bounds__(64)
     if (lane == 0) cmin_out[chain] = cmin;
 }
 
+// one thread per pair: sum of chain minima in y then x order
 __global__ void k_lb(const double *__restrict__ cH, int H, const double *__restrict__ cV, int W,
-                     double *__restrict__ lb)
+                     double *__restrict__ lb, int npairs)
 {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npairs) return;
     double sh = 0.0, sv = 0.0;
-    for (int y = 0; y < H; ++y) sh += cH[y];
-    for (int x = 0; x < W; ++x) sv += cV[x];
-    *lb = sh + sv;
+    for (int y = 0; y < H; ++y) sh += cH[(long)p * H + y];
+    for (int x = 0; x < W; ++x) sv += cV[(long)p * W + x];
+    lb[p] = sh + sv;
 }
 
 __global__ void k_wta(const float *__restrict__ cost, long npx, int D, int32_t *__restrict__ labels)
@@ -339,23 +352,23 @@ struct Layout {
     size_t phi, lbuf, ch, cv, lb, total;
 };
 
-Layout layout(int W, int H, int D)
+Layout layout(int W, int H, int D, int np = 1)
 {
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     Layout l;
-    size_t n = (size_t)W * H * D;
+    size_t n = (size_t)W * H * D * np;
     l.phi = 0;
     l.lbuf = al(l.phi + n * sizeof(float));
     l.ch = al(l.lbuf + n * sizeof(float));
-    l.cv = al(l.ch + (size_t)H * sizeof(double));
-    l.lb = al(l.cv + (size_t)W * sizeof(double));
-    l.total = al(l.lb + sizeof(double));
+    l.cv = al(l.ch + (size_t)H * np * sizeof(double));
+    l.lb = al(l.cv + (size_t)W * np * sizeof(double));
+    l.total = al(l.lb + np * sizeof(double));
     return l;
 }
 
 template <int P, int DELTA>
-int run_passes(const float *cost, const float *wx, const float *wy, int W, int H, int D, const Rho &rp,
-               int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+int run_passes(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
+               const Rho &rp, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
 {
     float *phi = (float *)(ws + l.phi), *lbuf = (float *)(ws + l.lbuf);
     double *cH = (double *)(ws + l.ch), *cV = (double *)(ws + l.cv), *lb = (double *)(ws + l.lb);
@@ -371,46 +384,43 @@ int run_passes(const float *cost, const float *wx, const float *wy, int W, int H
     for (int it = 0; it < iters; ++it) {
         {
             CNNCRF_PROF("crf_h", st);
-            kh<<<ceil_div(H, wpb), 32 * wpb, smh, st>>>(cost, phi, wx, lbuf, W, H, D, rp, it == 0, nh, nullptr, cH);
+            kh<<<ceil_div((long)H * np, wpb), 32 * wpb, smh, st>>>(cost, phi, wx, lbuf, W, H, D, rp, it == 0, nh,
+                                                                  nullptr, cH, np, wps);
         }
         {
             CNNCRF_PROF("crf_v", st);
-            kv<<<ceil_div(W, wpb), 32 * wpb, smv, st>>>(cost, phi, wy, lbuf, W, H, D, rp, 0, nv,
-                                                       it == iters - 1 ? labels : nullptr, cV);
+            kv<<<ceil_div((long)W * np, wpb), 32 * wpb, smv, st>>>(cost, phi, wy, lbuf, W, H, D, rp, 0, nv,
+                                                                  it == iters - 1 ? labels : nullptr, cV, np, wps);
         }
     }
     {
         CNNCRF_PROF("lb", st);
-        k_lb<<<1, 1, 0, st>>>(cH, H, cV, W, lb);
+        k_lb<<<ceil_div(np, 64), 64, 0, st>>>(cH, H, cV, W, lb, np);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
 template <int P>
-int dispatch_delta(int delta, const float *cost, const float *wx, const float *wy, int W, int H, int D,
-                   const Rho &rp, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+int dispatch_delta(int delta, const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D,
+                   int np, const Rho &rp, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
 {
     switch (delta) {
-    case 1: return run_passes<P, 1>(cost, wx, wy, W, H, D, rp, iters, labels, ws, l, st);
-    case 2: return run_passes<P, 2>(cost, wx, wy, W, H, D, rp, iters, labels, ws, l, st);
-    case 3: return run_passes<P, 3>(cost, wx, wy, W, H, D, rp, iters, labels, ws, l, st);
-    case 4: return run_passes<P, 4>(cost, wx, wy, W, H, D, rp, iters, labels, ws, l, st);
+    case 1: return run_passes<P, 1>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
+    case 2: return run_passes<P, 2>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
+    case 3: return run_passes<P, 3>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
+    case 4: return run_passes<P, 4>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
     default: return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
     }
 }
 
-} // namespace
-
-size_t crf_workspace_bytes(int W, int H, int D) { return layout(W, H, D).total; }
-
-int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D, const CrfParams &p,
-              int iters, int32_t *labels, void *ws, size_t ws_bytes, double *h_lb, cudaStream_t st)
+int solve_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
+               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st)
 {
-    if (W < 1 || H < 1 || D < 1 || D > 256) return fail(CNNCRF_EINVAL, "crf: bad size %dx%dx%d", W, H, D);
+    if (W < 1 || H < 1 || D < 1 || D > 256 || np < 1) return fail(CNNCRF_EINVAL, "crf: bad size %dx%dx%d x%d", W, H, D, np);
     if (!cost || !wx || !wy || !labels || !ws) return fail(CNNCRF_EINVAL, "crf: null pointer");
     if (p.slack <= 0.0f || p.slack > 1.0f) return fail(CNNCRF_EINVAL, "crf: slack %g outside (0,1]", p.slack);
-    Layout l = layout(W, H, D);
+    Layout l = layout(W, H, D, np);
     if (ws_bytes < l.total) return fail(CNNCRF_EINVAL, "crf: workspace %zu < %zu bytes", ws_bytes, l.total);
     if (((uintptr_t)ws & 255) != 0) return fail(CNNCRF_EINVAL, "crf: workspace not 256-byte aligned");
     if (((uintptr_t)cost & 15) != 0) return fail(CNNCRF_EINVAL, "crf: cost volume not 16-byte aligned");
@@ -418,32 +428,52 @@ int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H,
     if (iters <= 0) {
         {
             CNNCRF_PROF("wta", st);
-            k_wta<<<ceil_div((long)W * H, 256), 256, 0, st>>>(cost, (long)W * H, D, labels);
+            k_wta<<<ceil_div((long)W * H * np, 256), 256, 0, st>>>(cost, (long)W * H * np, D, labels);
         }
-        CNNCRF_CUDA(cudaMemsetAsync(w + l.lb, 0, sizeof(double), st));
+        CNNCRF_CUDA(cudaMemsetAsync(w + l.lb, 0, sizeof(double) * np, st));
         CNNCRF_CHECK_LAUNCH();
-    } else {
-        Rho rp;
-        rp.L2 = p.L2;
-        rp.slack = p.slack;
-        rp.rho[0] = 0.0f;
-        for (int t = 1; t <= 8; ++t)
-            rp.rho[t] = p.shape == 0 ? fminf(p.L1, p.L2) : fminf(p.L1 * (float)t, p.L2);
-        int P = (D + 31) / 32;
-        int rc;
-        if (P <= 1) rc = dispatch_delta<1>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        else if (P <= 2) rc = dispatch_delta<2>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        else if (P <= 3) rc = dispatch_delta<3>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        else if (P <= 4) rc = dispatch_delta<4>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        else if (P <= 6) rc = dispatch_delta<6>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        else rc = dispatch_delta<8>(p.delta, cost, wx, wy, W, H, D, rp, iters, labels, w, l, st);
-        if (rc != CNNCRF_OK) return rc;
+        return CNNCRF_OK;
     }
+    Rho rp;
+    rp.L2 = p.L2;
+    rp.slack = p.slack;
+    rp.rho[0] = 0.0f;
+    for (int t = 1; t <= 8; ++t) rp.rho[t] = p.shape == 0 ? fminf(p.L1, p.L2) : fminf(p.L1 * (float)t, p.L2);
+    int P = (D + 31) / 32;
+    if (P <= 1) return dispatch_delta<1>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    if (P <= 2) return dispatch_delta<2>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    if (P <= 3) return dispatch_delta<3>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    if (P <= 4) return dispatch_delta<4>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    if (P <= 6) return dispatch_delta<6>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    return dispatch_delta<8>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+}
+
+} // namespace
+
+size_t crf_workspace_bytes(int W, int H, int D, int npairs) { return layout(W, H, D, npairs).total; }
+
+int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D, const CrfParams &p,
+              int iters, int32_t *labels, void *ws, size_t ws_bytes, double *h_lb, cudaStream_t st)
+{
+    CNNCRF_TRY(solve_impl(cost, wx, wy, 0, W, H, D, 1, p, iters, labels, ws, ws_bytes, st));
     if (h_lb) {
-        CNNCRF_CUDA(cudaMemcpyAsync(h_lb, w + l.lb, sizeof(double), cudaMemcpyDeviceToHost, st));
+        Layout l = layout(W, H, D, 1);
+        CNNCRF_CUDA(cudaMemcpyAsync(h_lb, (char *)ws + l.lb, sizeof(double), cudaMemcpyDeviceToHost, st));
         CNNCRF_CUDA(cudaStreamSynchronize(st));
     }
     return CNNCRF_OK;
+}
+
+int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs, const CrfParams &p,
+                    int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st)
+{
+    const long N = (long)W * H;
+    return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st);
+}
+
+const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs)
+{
+    return (const double *)((const char *)ws + layout(W, H, D, npairs).lb);
 }
 
 int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st)

@@ -23,6 +23,8 @@ __global__ void k_pad(const float4 *__restrict__ in, int W, int H, int p, float4
     int Wp = W + 2 * p, Hp = H + 2 * p;
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)Wp * Hp) return;
+    in += (long)blockIdx.y * W * H; // image of the batch
+    out += (long)blockIdx.y * Wp * Hp;
     int y = (int)(i / Wp), x = (int)(i - (long)y * Wp);
     out[i] = in[(long)mirror_idx(y - p, H) * W + mirror_idx(x - p, W)];
 }
@@ -54,6 +56,9 @@ __global__ void k_rowsums(const float *__restrict__ rgba, int Wp, int Hp, int pl
 {
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (w >= planes * Hp) return;
+    rgba += (long)blockIdx.y * Wp * Hp * 4; // image of the batch
+    rows += (long)blockIdx.y * 3 * Hp;
+    stats += blockIdx.y * 8;
     const int c = w / Hp, y = w - c * Hp;
     const long base = (long)y * Wp;
     double s = 0.0;
@@ -76,6 +81,8 @@ __global__ void k_finalize(const double *__restrict__ rows, int Hp, int planes, 
                            float *__restrict__ stats)
 {
     const int c = blockIdx.x, lane = threadIdx.x;
+    rows += (long)blockIdx.y * 3 * Hp;
+    stats += blockIdx.y * 8;
     double s = 0.0;
     for (int y = lane; y < Hp; y += 32) s += rows[c * Hp + y];
     s = warp_tree_sum(s);
@@ -90,6 +97,9 @@ __global__ void k_norm_write(const float *__restrict__ rgba, int Wp, int Hp, int
 {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (long)Wp * Hp) return;
+    rgba += (long)blockIdx.y * Wp * Hp * 4;
+    stats += blockIdx.y * 8;
+    out += (long)blockIdx.y * Wp * Hp * ic;
     int gray = ic == 1;
     int planes = gray ? 1 : 3;
     for (int c = 0; c < planes; ++c) {
@@ -106,45 +116,45 @@ __global__ void k_norm_write(const float *__restrict__ rgba, int Wp, int Hp, int
 
 } // namespace
 
-int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st)
+int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st, int nimg)
 {
     long n = (long)(W + 2 * p) * (H + 2 * p);
     {
         CNNCRF_PROF("pad", st);
-        k_pad<<<ceil_div(n, 256), 256, 0, st>>>((const float4 *)in, W, H, p, (float4 *)out);
+        k_pad<<<dim3(ceil_div(n, 256), nimg), 256, 0, st>>>((const float4 *)in, W, H, p, (float4 *)out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
-size_t normalize_scratch_bytes(int Hp) { return sizeof(double) * 3 * (size_t)Hp + 64; }
+size_t normalize_scratch_bytes(int Hp, int nimg) { return (sizeof(double) * 3 * (size_t)Hp + 32) * nimg + 64; }
 
-int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scratch, cudaStream_t st)
+int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scratch, cudaStream_t st, int nimg)
 {
     int gray = ic == 1, planes = gray ? 1 : 3;
     double *rows = (double *)scratch;
-    float *stats = (float *)((char *)scratch + sizeof(double) * 3 * (size_t)Hp);
+    float *stats = (float *)((char *)scratch + sizeof(double) * 3 * (size_t)Hp * nimg);
     long N = (long)Wp * Hp;
     const long nthreads = 32L * planes * Hp;
     {
         CNNCRF_PROF("rowsums", st);
-        k_rowsums<<<ceil_div(nthreads, 256), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 0, stats, rows);
+        k_rowsums<<<dim3(ceil_div(nthreads, 256), nimg), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 0, stats, rows);
     }
     {
         CNNCRF_PROF("finalize", st);
-        k_finalize<<<planes, 32, 0, st>>>(rows, Hp, planes, N, 0, stats);
+        k_finalize<<<dim3(planes, nimg), 32, 0, st>>>(rows, Hp, planes, N, 0, stats);
     }
     {
         CNNCRF_PROF("rowsums", st);
-        k_rowsums<<<ceil_div(nthreads, 256), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 1, stats, rows);
+        k_rowsums<<<dim3(ceil_div(nthreads, 256), nimg), 256, 0, st>>>(rgba, Wp, Hp, planes, gray, 1, stats, rows);
     }
     {
         CNNCRF_PROF("finalize", st);
-        k_finalize<<<planes, 32, 0, st>>>(rows, Hp, planes, N, 1, stats);
+        k_finalize<<<dim3(planes, nimg), 32, 0, st>>>(rows, Hp, planes, N, 1, stats);
     }
     {
         CNNCRF_PROF("norm_write", st);
-        k_norm_write<<<ceil_div(N, 256), 256, 0, st>>>(rgba, Wp, Hp, ic, stats, out);
+        k_norm_write<<<dim3(ceil_div(N, 256), nimg), 256, 0, st>>>(rgba, Wp, Hp, ic, stats, out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

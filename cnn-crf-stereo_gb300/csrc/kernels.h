@@ -11,13 +11,14 @@ namespace k {
 
 // ------------------------------------------------------------ front end
 // mirror pad of an RGBA image (stereo/stereo.cu:879-911)
-int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st);
+int pad_rgba(const float *in, int W, int H, int p, float *out, cudaStream_t st, int nimg = 1);
 // zero-mean / unit-std planes of a padded RGBA image -> NHWC [Hp][Wp][ic]
 // (stereo/colorstereonet.cpp:53-64,102-121; stereo/utils.cu:169-237).
 // scratch: >= 6*Hp doubles + 8 floats.
+// images of a batch are contiguous ([nimg][Hp][Wp][4] in, [nimg][Hp][Wp][ic] out)
 int normalize(const float *rgba, int Wp, int Hp, int ic, float *out, void *scratch,
-              cudaStream_t st);
-size_t normalize_scratch_bytes(int Hp);
+              cudaStream_t st, int nimg = 1);
+size_t normalize_scratch_bytes(int Hp, int nimg = 1);
 
 // ------------------------------------------------------------ FP32 conv
 struct ConvArgs {
@@ -30,11 +31,13 @@ struct ConvArgs {
     float *out;           // NHWC dense [Ho][Wo][Cout]
     void *out16 = nullptr; // if set: BF16 NHWC output [Ho][Wo][out_cs] instead of `out`
     int out_cs = 0;
+    int n_img = 1;         // images of a batch: input / output element strides
+    long in_img = 0, out_img = 0;
 };
 int conv_simt(const ConvArgs &a, cudaStream_t st);
 // 1x1 conv Cin -> 2, no bias, |.| (stereo/stereonet.cpp:167,401): planar [2][H][W]
 int conv_head2(const float *in, int npx, int Cin, const float *w /*[2][Cin]*/, float *out,
-               cudaStream_t st);
+               cudaStream_t st, int n_img = 1);
 // per-pixel L2 normalisation of NHWC features
 int l2norm(float *f, long npx, int C, cudaStream_t st);
 
@@ -56,11 +59,14 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st);
 // ------------------------------------------------------------ correlation
 // raw correlation (+ unary: -1 none, 0 -softmax, 1 one-minus) of NHWC FP32
 // features; list = the reference's stored (negated) disparities.
+// npairs pairs: features of pair p at fl + p*fps, fr + p*fps; volume at out + p*H*W*D
 int correlation(const float *fl, const float *fr, int H, int W, int C, const float *d_list,
-                int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st);
+                int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st,
+                int npairs = 1, long fps = 0);
 // same on BF16 features with channel stride cs (FP32 accumulation)
 int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs, const float *d_list,
-                     int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st);
+                     int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st,
+                     int npairs = 1, long fps = 0);
 
 // ------------------------------------------------------------ CRF
 struct CrfParams {
@@ -70,7 +76,13 @@ struct CrfParams {
     float slack;
 };
 // workspace layout helpers
-size_t crf_workspace_bytes(int W, int H, int D);
+size_t crf_workspace_bytes(int W, int H, int D, int npairs = 1);
+// npairs pairs at once: cost [n][H][W][D], weights [n][2][H][W] (wx, wy),
+// labels [n][H][W]; bounds stay in the workspace (crf_lb_device)
+int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs,
+                    const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
+                    cudaStream_t st);
+const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs);
 int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D,
               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
               double *h_lb, cudaStream_t st);

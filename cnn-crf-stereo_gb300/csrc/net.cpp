@@ -179,7 +179,7 @@ int cnncrf_net::set_disparities(float mn, float mx, float step, float *d_out)
     if (d_out) {
         vol = d_out;
     } else {
-        CNNCRF_TRY(vol_own.reserve(sizeof(float) * (size_t)H * W * D));
+        CNNCRF_TRY(vol_own.reserve(sizeof(float) * (size_t)H * W * D * n));
         vol = vol_own.as<float>();
     }
     return CNNCRF_OK;
@@ -188,15 +188,17 @@ int cnncrf_net::set_disparities(float mn, float mx, float step, float *d_out)
 int cnncrf_net::pairwise_fp32()
 {
     // crop by pad-2 of the normalised left image (stereo/colorstereonet.cpp:69-73)
-    int cr = pad - 2, ic = d.in_channels;
+    int cr = pad - 2, ic = d.in_channels, P = d.pw_channels;
     const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
     k::ConvArgs a1{in, H + 4, W + 4, pw[0].cin, (long)ic, (long)w * ic, pw[0].wt.as<float>(),
                    pw[0].bias.as<float>(), pw[0].cout, 3, 3, 1, pwa.as<float>()};
+    a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * P;
     CNNCRF_TRY(k::conv_simt(a1, st));
     k::ConvArgs a2{pwa.as<float>(), H + 2, W + 2, pw[1].cin, (long)pw[1].cin, (long)(W + 2) * pw[1].cin,
                    pw[1].wt.as<float>(), pw[1].bias.as<float>(), pw[1].cout, 3, 3, 1, pwb.as<float>()};
+    a2.n_img = n, a2.in_img = (long)(H + 2) * (W + 2) * P, a2.out_img = (long)H * W * P;
     CNNCRF_TRY(k::conv_simt(a2, st));
-    return k::conv_head2(pwb.as<float>(), H * W, pw[2].cin, pw[2].wt.as<float>(), pwout, st);
+    return k::conv_head2(pwb.as<float>(), H * W, pw[2].cin, pw[2].wt.as<float>(), pwout, st, n);
 }
 
 int cnncrf_net::predict_fp32(const float *left, const float *right)
@@ -204,7 +206,7 @@ int cnncrf_net::predict_fp32(const float *left, const float *right)
     const float *img[2] = {left, right};
     int ic = d.in_channels;
     for (int s = 0; s < 2; ++s) {
-        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st));
+        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
         const float *cur = norm[s].as<float>();
         int ch = h, cw = w, cc = ic;
         for (size_t l = 0; l < feat.size(); ++l) {
@@ -212,17 +214,18 @@ int cnncrf_net::predict_fp32(const float *left, const float *right)
             float *out = act[s][l & 1].as<float>();
             k::ConvArgs a{cur, ch, cw, cc, (long)cc, (long)cw * cc, L.wt.as<float>(), L.bias.as<float>(),
                           L.cout, L.kh, L.kw, L.act, out};
+            int oh = ch - (L.kh - 1), ow = cw - (L.kw - 1);
+            a.n_img = n, a.in_img = (long)ch * cw * cc, a.out_img = (long)oh * ow * L.cout;
             CNNCRF_TRY(k::conv_simt(a, st));
-            ch -= L.kh - 1;
-            cw -= L.kw - 1;
-            cc = L.cout;
+            ch = oh, cw = ow, cc = L.cout;
             cur = out;
         }
         feats[s] = const_cast<float *>(cur);
-        if (d.unary == CNNCRF_UNARY_ONE_MINUS_DOT) CNNCRF_TRY(k::l2norm(feats[s], (long)H * W, d.feat_channels, st));
+        if (d.unary == CNNCRF_UNARY_ONE_MINUS_DOT)
+            CNNCRF_TRY(k::l2norm(feats[s], (long)H * W * n, d.feat_channels, st));
     }
     CNNCRF_TRY(k::correlation(feats[0], feats[1], H, W, d.feat_channels, d_list.as<float>(), D, omin, omax,
-                              interp || force_interp, d.unary, vol, st));
+                              interp || force_interp, d.unary, vol, st, n, (long)H * W * d.feat_channels));
     if (d.with_pairwise) CNNCRF_TRY(pairwise_fp32());
     return CNNCRF_OK;
 }
@@ -247,7 +250,7 @@ int cnncrf_net_create(cnncrf_net_t *out, const cnncrf_net_desc *desc, int n, int
     if (!out || !desc) return fail(CNNCRF_EINVAL, "net_create: null argument");
     *out = nullptr;
     const cnncrf_net_desc &d = *desc;
-    if (n != 1) return fail(CNNCRF_EUNSUPPORTED, "net_create: only n = 1 (got %d)", n);
+    if (n < 1 || n > 256) return fail(CNNCRF_EINVAL, "net_create: batch n = %d outside 1..256", n);
     if (d.num_layers < 1 || d.num_layers > 16) return fail(CNNCRF_EINVAL, "net_create: num_layers %d", d.num_layers);
     if (d.topology != CNNCRF_TOPO_REF && d.topology != CNNCRF_TOPO_ALL3X3)
         return fail(CNNCRF_EINVAL, "net_create: topology %d", d.topology);
@@ -304,8 +307,8 @@ int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step
     clear_error();
     if (!net) return fail(CNNCRF_EINVAL, "null net");
     if (rect_corr != 0) return fail(CNNCRF_EUNSUPPORTED, "rect_corr != 0 is not built");
-    int ic = net->d.in_channels, h = net->h, w = net->w, H = net->H, W = net->W;
-    size_t np = (size_t)h * w;
+    int ic = net->d.in_channels, h = net->h, w = net->w, H = net->H, W = net->W, nb = net->n;
+    size_t np = (size_t)h * w * nb;
     for (int s = 0; s < 2; ++s) CNNCRF_TRY(net->norm[s].reserve(np * ic * sizeof(float)));
     size_t amax = 0;
     {
@@ -315,17 +318,21 @@ int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step
             amax = std::max(amax, (size_t)ch * cw * L.cout);
         }
     }
+    const bool fp32 = net->d.precision == CNNCRF_FP32;
     for (int s = 0; s < 2; ++s)
-        for (int b = 0; b < 2; ++b) CNNCRF_TRY(net->act[s][b].reserve(amax * sizeof(float)));
-    CNNCRF_TRY(net->scratch.reserve(k::normalize_scratch_bytes(h)));
+        for (int b = 0; b < 2; ++b)
+            if (fp32) CNNCRF_TRY(net->act[s][b].reserve(amax * nb * sizeof(float)));
+    CNNCRF_TRY(net->scratch.reserve(k::normalize_scratch_bytes(h, nb)));
     if (net->d.with_pairwise) {
         int P = net->d.pw_channels;
-        CNNCRF_TRY(net->pwa.reserve((size_t)(H + 2) * (W + 2) * P * sizeof(float)));
-        CNNCRF_TRY(net->pwb.reserve((size_t)H * W * P * sizeof(float)));
+        if (fp32) {
+            CNNCRF_TRY(net->pwa.reserve((size_t)(H + 2) * (W + 2) * P * nb * sizeof(float)));
+            CNNCRF_TRY(net->pwb.reserve((size_t)H * W * P * nb * sizeof(float)));
+        }
         if (d_pairwise_out) {
             net->pwout = d_pairwise_out;
         } else {
-            CNNCRF_TRY(net->pw_own.reserve((size_t)2 * H * W * sizeof(float)));
+            CNNCRF_TRY(net->pw_own.reserve((size_t)2 * H * W * nb * sizeof(float)));
             net->pwout = net->pw_own.as<float>();
         }
     }
@@ -441,7 +448,7 @@ int cnncrf_net_features(cnncrf_net_t net, int side, float *d_out)
     if (net->d.precision == CNNCRF_BF16) {
         if (!net->feat16) return fail(CNNCRF_ESTATE, "features: no prediction yet");
         size_t npx = (size_t)net->H * net->W;
-        const uint16_t *f = (const uint16_t *)net->feat16 + side * npx * net->cp_feat;
+        const uint16_t *f = (const uint16_t *)net->feat16 + (size_t)side * net->n * npx * net->cp_feat;
         return k::bf16_to_f32(f, net->cp_feat, net->d.feat_channels, (long)npx, d_out, net->st);
     }
     if (!net->feats[side]) return fail(CNNCRF_ESTATE, "features: no prediction yet");

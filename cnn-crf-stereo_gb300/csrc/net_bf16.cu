@@ -24,7 +24,7 @@ int cnncrf_net::alloc_bf16()
     cp_feat = pad_to(d.feat_channels, 64);
     np_feat = umma_n(d.feat_channels);
     size_t h1 = h - 2, w1 = w - 2; // layer-1 output, the largest activation
-    size_t bytes = 2 * h1 * w1 * cp_feat * 2;
+    size_t bytes = 2 * (size_t)n * h1 * w1 * cp_feat * 2; // [side][pair][h][w][cp] BF16
     for (int i = 0; i < 2; ++i) {
         CNNCRF_TRY(a16[i].reserve(bytes));
         // channels past feat_channels are never written and must read as zero
@@ -33,7 +33,7 @@ int cnncrf_net::alloc_bf16()
     if (d.with_pairwise) {
         cp_pw = pad_to(d.pw_channels, 64);
         np_pw = umma_n(d.pw_channels);
-        size_t pb = (size_t)(H + 2) * (W + 2) * cp_pw * 2;
+        size_t pb = (size_t)n * (H + 2) * (W + 2) * cp_pw * 2;
         CNNCRF_TRY(pw16.reserve(pb));
         CNNCRF_CUDA(cudaMemset(pw16.get(), 0, pb));
     }
@@ -62,12 +62,13 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
     const int ic = d.in_channels, F = d.feat_channels, cp = cp_feat;
     const size_t h1 = h - 2, w1 = w - 2;
     for (int s = 0; s < 2; ++s) {
-        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st));
+        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
         Layer &L0 = feat[0];
         k::ConvArgs a{norm[s].as<float>(), h, w, ic, (long)ic, (long)w * ic, L0.wt.as<float>(), L0.bias.as<float>(),
                       F, 3, 3, 1, nullptr};
-        a.out16 = (uint16_t *)a16[0].get() + s * h1 * w1 * cp;
+        a.out16 = (uint16_t *)a16[0].get() + (size_t)s * n * h1 * w1 * cp;
         a.out_cs = cp;
+        a.n_img = n, a.in_img = (long)h * w * ic, a.out_img = (long)(h1 * w1 * cp);
         CNNCRF_TRY(k::conv_simt(a, st));
     }
     int hin = (int)h1, win = (int)w1;
@@ -76,7 +77,7 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
         Layer &L = feat[l];
         k::TcConvArgs t{};
         t.in = a16[cur].get();
-        t.n_img = 2, t.Hin = hin, t.Win = win, t.cp_in = cp, t.cin = F;
+        t.n_img = 2 * n, t.Hin = hin, t.Win = win, t.cp_in = cp, t.cin = F; // left images, then right images
         t.wt = L.wt16.get();
         t.np = np_feat, t.cout = F, t.kh = L.kh, t.kw = L.kw;
         t.bias = L.bias.as<float>();
@@ -91,9 +92,10 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
     }
     if (hin != H || win != W) return fail(CNNCRF_ESHAPE, "BF16 feature map %dx%d != %dx%d", win, hin, W, H);
     const uint16_t *f = (const uint16_t *)a16[cur].get();
+    const size_t fimg = (size_t)H * W * cp;
     feat16 = f;
-    CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)H * W * cp, H, W, F, cp, d_list.as<float>(), D, omin, omax,
-                                   interp || force_interp, d.unary, vol, st));
+    CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)n * fimg, H, W, F, cp, d_list.as<float>(), D, omin, omax,
+                                   interp || force_interp, d.unary, vol, st, n, (long)fimg));
     if (d.with_pairwise) {
         int cr = pad - 2;
         const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
@@ -101,10 +103,11 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
                        pw[0].cout, 3, 3, 1, nullptr};
         a1.out16 = pw16.get();
         a1.out_cs = cp_pw;
+        a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * cp_pw;
         CNNCRF_TRY(k::conv_simt(a1, st));
         k::TcConvArgs t{};
         t.in = pw16.get();
-        t.n_img = 1, t.Hin = H + 2, t.Win = W + 2, t.cp_in = cp_pw, t.cin = pw[1].cin;
+        t.n_img = n, t.Hin = H + 2, t.Win = W + 2, t.cp_in = cp_pw, t.cin = pw[1].cin;
         t.wt = pw[1].wt16.get();
         t.np = np_pw, t.cout = pw[1].cout, t.kh = 3, t.kw = 3;
         t.bias = pw[1].bias.as<float>();

@@ -305,6 +305,44 @@ int cnncrf_stereo_lower_bound(cnncrf_stereo_t s, double *lb);
 int cnncrf_stereo_stage_times(cnncrf_stereo_t s, float *cnn_ms, float *corr_ms, float *crf_ms,
                               float *refine_ms);
 
+/* ---------------------------------------------------------------- batched Stereo
+ * Many pairs through computeSlackPropagation at once (no counterpart in the
+ * reference: its Stereo object holds one pair, stereo/stereo.h:40-133).
+ * Pairs of equal size and disparity range form a group that runs as one
+ * batch (tensor-core convolutions over all its images, one correlation and
+ * one CRF launch per pass over all its chains); groups run on their own
+ * streams, forked from and joined into the batch's stream.  With graph
+ * capture on, the first run executes eagerly, the second captures the whole
+ * step into a CUDA graph, later runs with the same CRF parameters replay it. */
+typedef struct cnncrf_batch *cnncrf_batch_t;
+int cnncrf_batch_create(cnncrf_batch_t *b, const cnncrf_stereo_options *opt);
+int cnncrf_batch_destroy(cnncrf_batch_t b);
+int cnncrf_batch_set_stream(cnncrf_batch_t b, cnncrf_stream_t stream);
+/* matching (COLORPAIR / GRAYPAIR), layers, xy channels, weights: npz base
+ * name (".npz" appended) or NULL for Xavier weights from `seed`. */
+int cnncrf_batch_set_network(cnncrf_batch_t b, int matching, int num_layers, int with_xy,
+                             const char *param_base, uint64_t seed);
+/* Stereo::initialize for one more pair; returns its index. */
+int cnncrf_batch_add_pair(cnncrf_batch_t b, int width, int height, float disp_min, float disp_step,
+                          float disp_max, int *pair_index);
+int cnncrf_batch_num_pairs(cnncrf_batch_t b, int *n);
+/* Stereo::setColorImages for one pair (host RGBA / device RGBA). */
+int cnncrf_batch_set_images(cnncrf_batch_t b, int pair, const float *h_left, const float *h_right);
+int cnncrf_batch_set_images_device(cnncrf_batch_t b, int pair, const float *d_left,
+                                   const float *d_right);
+int cnncrf_batch_use_graph(cnncrf_batch_t b, int enable);
+/* computeSlackPropagation(L1, L2, delta, iterations, -, -, lambda, lr = 1)
+ * for every pair; asynchronous on the batch's stream. */
+int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations,
+                     float lambda_reg);
+int cnncrf_batch_get_output(cnncrf_batch_t b, int pair, float *h_out);
+int cnncrf_batch_get_output_device(cnncrf_batch_t b, int pair, const float **d_out);
+int cnncrf_batch_get_labels_device(cnncrf_batch_t b, int pair, const int32_t **d_labels);
+int cnncrf_batch_get_volume_device(cnncrf_batch_t b, int pair, const float **d_volume, int *depth);
+int cnncrf_batch_lower_bound(cnncrf_batch_t b, int pair, double *lb);
+/* Synchronise and report a kernel that gave up on a bounded wait (ETIMEOUT). */
+int cnncrf_batch_check(cnncrf_batch_t b);
+
 /* ---------------------------------------------------------------- instrumentation
  * (no counterpart in the reference, which timed whole stages with
  * iu::IuCudaTimer when verbose, stereo/stereonet.cpp:258-315) */

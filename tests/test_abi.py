@@ -46,7 +46,7 @@ def test_net_create_rejects_bad_descriptions(lib):
         assert rc == L.EINVAL, (rc, lib.cnncrf_last_error())
         assert lib.cnncrf_last_error()
     d = L.NetDesc(7, 0, 3, 100, 0, 0, 0, 64)
-    assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 2, 64, 64) == L.EUNSUPPORTED
+    assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 0, 64, 64) == L.EINVAL
     assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 1, 6, 6) == L.ESHAPE
 
 
@@ -84,6 +84,23 @@ def test_stereo_host_checks(lib):
     assert lib.cnncrf_stereo_initialize(s, 10, 10, 0.0, 0.0, 10.0) == L.EINVAL
     assert lib.cnncrf_stereo_set_matching_function(s, 42) == L.EINVAL
     lib.cnncrf_stereo_destroy(s)
+
+
+def test_batch_host_checks(lib):
+    import cnncrf._lib as L
+    b = C.c_void_p()
+    assert lib.cnncrf_batch_create(C.byref(b), None) == L.OK
+    assert lib.cnncrf_batch_run(b, 1.0, 5.0, 2.0, 3, 1.0) == L.ESTATE  # no pairs
+    i = C.c_int()
+    assert lib.cnncrf_batch_add_pair(b, 0, 10, 0.0, 1.0, 7.0, C.byref(i)) == L.EINVAL
+    assert lib.cnncrf_batch_add_pair(b, 20, 10, 0.0, 1.0, 7.0, C.byref(i)) == L.OK and i.value == 0
+    assert lib.cnncrf_batch_add_pair(b, 20, 10, 0.0, 1.0, 7.0, C.byref(i)) == L.OK and i.value == 1
+    n = C.c_int()
+    lib.cnncrf_batch_num_pairs(b, C.byref(n))
+    assert n.value == 2
+    out = C.c_void_p()
+    assert lib.cnncrf_batch_get_output_device(b, 5, C.byref(out)) == L.EINVAL
+    lib.cnncrf_batch_destroy(b)
 
 
 def test_crf_option_checks(lib):

@@ -1,0 +1,92 @@
+"""GPU tests of the batched form: pairs grouped by shape, each group one
+batch per launch, groups on their own streams, optional CUDA-graph replay.
+Batching must not change a single bit of any pair's result."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def single_run(L, scene, prec, dmax, layers, iters, crf):
+    from cnncrf.api import Stereo
+    H, W = scene["disp"].shape
+    st = Stereo(precision=prec, unary=L.UNARY_ONE_MINUS_DOT, topology=L.TOPO_ALL3X3, ref_depth_rounding=False,
+                crf_shape=L.RHO_LINEAR)
+    st.initialize(W, H, 0.0, 1.0, dmax)
+    st.set_matching_function(L.MATCH_COLORCNN_PAIRWISE)
+    st.set_num_layers(layers)
+    st.set_xavier_seed(0)
+    st.set_color_images(scene["left"], scene["right"])
+    st.compute_slack_propagation(crf[0], crf[1], crf[2], iters, 0.0, 0.0, 1.0)
+    return st.labels_device().cpu().numpy(), st.get_output(), st.lower_bound()
+
+
+@pytest.mark.parametrize("prec_name", ["FP32", "BF16"])
+def test_batch_equals_single(cuda, prec_name):
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import StereoBatch
+    prec = getattr(L, prec_name)
+    layers, iters, crf = 3, 3, (0.5, 1.5, 3)
+    shapes = [(64, 40, 16), (64, 40, 16), (96, 24, 32), (64, 40, 16)]  # two groups, interleaved
+    sc = [scenes.voronoi_scene(W, H, D, seed=10 + i, cells=4, off_range=(1, D - 2), slope=0.05)
+          for i, (W, H, D) in enumerate(shapes)]
+    b = StereoBatch(precision=prec, num_layers=layers, seed=0)
+    for (W, H, D) in shapes:
+        b.add_pair(W, H, 0.0, 1.0, float(D - 1))
+    for i, s in enumerate(sc):
+        b.set_images(i, s["left"], s["right"])
+    b.run(*crf, iters)
+    b.check()
+    for i, (W, H, D) in enumerate(shapes):
+        lab, disp, lb = single_run(L, sc[i], prec, float(D - 1), layers, iters, crf)
+        assert np.array_equal(b.labels_device(i).cpu().numpy(), lab), i
+        assert np.array_equal(b.get_output(i), disp), i
+        assert b.lower_bound(i) == lb, i
+
+
+def test_batch_graph_replay(cuda):
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import StereoBatch
+    torch = cuda
+    shapes = [(80, 32, 32)] * 3 + [(48, 24, 16)]
+    b = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=True)
+    eager = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=False)
+    for (W, H, D) in shapes:
+        b.add_pair(W, H, 0.0, 1.0, float(D - 1))
+        eager.add_pair(W, H, 0.0, 1.0, float(D - 1))
+    for rnd in range(4):  # eager run, capture, two replays with new images
+        sc = [scenes.voronoi_scene(W, H, D, seed=100 * rnd + i, cells=4, off_range=(1, D - 2))
+              for i, (W, H, D) in enumerate(shapes)]
+        for i, s in enumerate(sc):
+            b.set_images(i, torch.from_numpy(s["left"]).cuda(), torch.from_numpy(s["right"]).cuda())
+            eager.set_images(i, s["left"], s["right"])
+        b.run(0.5, 1.5, 3, 4)
+        eager.run(0.5, 1.5, 3, 4)
+        torch.cuda.synchronize()
+        for i in range(len(shapes)):
+            assert np.array_equal(b.get_output(i), eager.get_output(i)), (rnd, i)
+
+
+def test_net_batch_of_two(cuda, oracle):
+    """StereoNet with n = 2: each pair's volume equals the oracle's."""
+    torch = cuda
+    from cnncrf import scenes
+    from cnncrf.api import StereoNet
+    W, H, D = 40, 20, 12
+    cfg = oracle.make_cfg(num_layers=3, topology=0, disp_max=float(D - 1))
+    p = oracle.padding(cfg)
+    params = oracle.xavier_params(cfg, seed=4)
+    sc = [scenes.voronoi_scene(W, H, D, seed=s, cells=3, off_range=(1, D - 2)) for s in (1, 2)]
+    lp = np.stack([np.pad(s["left"], ((p, p), (p, p), (0, 0)), mode="symmetric") for s in sc])
+    rp = np.stack([np.pad(s["right"], ((p, p), (p, p), (0, 0)), mode="symmetric") for s in sc])
+    net = StereoNet(3, 2, 3, H + 2 * p, W + 2 * p, with_pairwise=True)
+    vol = torch.empty((2, H, W, D), device="cuda")
+    pw = torch.zeros((2, 2, H, W), device="cuda")
+    net.init_net(0.0, float(D - 1), 1.0, unary_out=vol, pairwise_out=pw)
+    net.init_xavier(4)
+    net.predict(torch.from_numpy(lp).cuda(), torch.from_numpy(rp).cuda())
+    lst = oracle.disparity_list(0.0, float(D - 1), 1.0)
+    for i in range(2):
+        ovol, opw = oracle.predict(cfg, params, lp[i], rp[i], lst)
+        assert np.array_equal(vol[i].cpu().numpy(), ovol)
+        assert np.array_equal(pw[i].cpu().numpy(), opw)
