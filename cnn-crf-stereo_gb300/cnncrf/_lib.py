@@ -73,6 +73,8 @@ PROTOS = {
     "cnncrf_crf_workspace_size": ([i32, i32, i32, C.POINTER(C.c_size_t)], i32),
     "cnncrf_crf_solve": ([vp, vp, vp, i32, i32, i32, C.POINTER(CrfOptions), vp, C.POINTER(C.c_double), vp,
                           C.c_size_t, vp], i32),
+    "cnncrf_crf_solve_static": ([vp, vp, vp, i32, i32, i32, C.POINTER(CrfOptions), vp, C.POINTER(C.c_double),
+                                 vp], i32),
     "cnncrf_slackprop_create": ([C.POINTER(vp)], i32),
     "cnncrf_slackprop_destroy": ([vp], i32),
     "cnncrf_slackprop_set_stream": ([vp, vp], i32),

@@ -192,6 +192,23 @@ int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, 
                      double *lower_bound, void *d_workspace, size_t workspace_bytes,
                      cnncrf_stream_t stream);
 
+/* No counterpart in the reference.  The same solve as cnncrf_crf_solve
+ * (same arguments, results and errors) with no workspace argument: the
+ * scratch lives in a 64 MiB array compiled into this library, and no call
+ * allocates device memory.  For callers that may not call cudaMalloc: a
+ * plug-in whose host framework owns every device allocation, or a real-time
+ * loop that cannot afford a device-wide allocation stall.
+ * Limit: cnncrf_crf_workspace_size(width, height, depth) <= 64 MiB (about
+ * 8 million labels W*H*D); larger problems return CNNCRF_EINVAL.
+ * The first call on each device looks up the array's address and caches it;
+ * make that first call before any stream capture.
+ * Nothing in the array has to start at zero.  All calls on a device share the
+ * one array: calls that overlap on the GPU (other streams, other threads)
+ * race and must be serialised by the caller. */
+int cnncrf_crf_solve_static(const float *d_cost, const float *d_wx, const float *d_wy, int width,
+                            int height, int depth, const cnncrf_crf_options *opt, int32_t *d_labels,
+                            double *lower_bound, cnncrf_stream_t stream);
+
 /* Object form of the same solver, mirroring slack_prop_2D_alg's members. */
 typedef struct cnncrf_slackprop *cnncrf_slackprop_t;
 int cnncrf_slackprop_create(cnncrf_slackprop_t *sp);
