@@ -266,20 +266,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
 }
 
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void *ptr = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)ptr;
-    }
-    return fn;
-}
-
 template <int NP> size_t smem_bytes(int stages)
 {
     return 1024 + (size_t)stages * stage_bytes<NP>() + (2 * stages + 5) * 8 + 16 + 3 * NP * 4 + 64;
@@ -287,7 +273,7 @@ template <int NP> size_t smem_bytes(int stages)
 
 template <int NP> int launch(const TcConvArgs &a, const TcParams &p, cudaStream_t st)
 {
-    auto enc = encode_fn();
+    auto enc = tc::tensor_map_encoder();
     if (!enc) return fail(CNNCRF_ECUDA, "conv_tc: cuTensorMapEncodeTiled unavailable");
     CUtensorMap ma, mb;
     cuuint64_t gA[4] = {(cuuint64_t)a.cp_in, (cuuint64_t)a.Win, (cuuint64_t)a.Hin, (cuuint64_t)a.n_img};

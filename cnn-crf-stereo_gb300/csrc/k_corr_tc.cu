@@ -1,0 +1,343 @@
+// k_corr_tc.cu -- the BF16 path's correlation cost volume on the tcgen05
+// tensor cores, with the unary fused into the epilogue.
+//
+// Replaces kCorrelation_NHWC (stereo/operators/stereocorrelation.cu:111-142,
+// integer disparities, rectCorr = 0) followed by the channel softmax and the
+// negation (stereo/operators/softmax.cpp:30-38, stereo/utils.cu:289-292), or
+// by 1 - <fL,fR> on L2-normalised features.
+//
+// Banded GEMM per image row: a tile is 128 consecutive left pixels x0.. of
+// row y (UMMA M = 128) against the 256 right pixels starting at x0 + omin
+// (UMMA N = 256), K = the feature channels.  Left pixel m and disparity index
+// k meet in band column n = m + s_k - omin (s_k = the stored, negated
+// disparity), so the tile holds every product the 128 pixels need as long as
+// omax - omin <= 128.  Right pixels outside [0, W) arrive as zeros through
+// TMA's out-of-bounds fill: exactly the reference's 0 for w - d < 0.
+//
+// Persistent, warp-specialised CTA (192 threads, one per SM):
+//   warp 0      TMA: per 64-channel block, a 4-D box (64 ch x 128 px) of the
+//               left features and one (64 ch x 256 px) of the right
+//               features, 128-byte swizzle; a ring of `stages` blocks
+//   warp 1      TMEM allocation + single-thread tcgen05.mma (M=128, N=256,
+//               K=16 steps) into one of two 256-column accumulators
+//   warps 2..5  epilogue: warp q owns TMEM lanes (pixels) 32q..32q+31 and
+//               reads the 32 + omax - omin columns they touch into shared
+//               memory (one row per pixel); then per pixel the whole warp
+//               gathers the D taps along the band (lane j: k = j + 32 r),
+//               applies the unary and stores the pixel's D costs with
+//               coalesced 128-byte writes
+// Every mbarrier wait is bounded; on timeout the role raises the CTA abort
+// flag and the global error flag, drains what it issued and TMEM is freed.
+#include <cfloat>
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include "../../include/cnncrf_fmath.h"
+#include "common.h"
+#include "kernels.h"
+#include "tc_util.cuh"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+constexpr int BM = 128;                    // left pixels per tile (UMMA M)
+constexpr int BN = 256;                    // band columns per tile (UMMA N)
+constexpr int A_BYTES = BM * 128;          // 128 px x 64 bf16
+constexpr int B_BYTES = BN * 128;          // 256 px x 64 bf16
+constexpr int STAGE = A_BYTES + B_BYTES;   // one 64-channel block of a tile
+constexpr int NUM_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
+constexpr int SROW = 161;                  // staged row stride in floats (odd: no bank conflicts)
+constexpr int SCOLS = 160;                 // columns staged per warp: 32 + max band spread
+constexpr int MAXP = 8;                    // D <= 256
+constexpr int STG_BYTES = 4 * 32 * SROW * 4;
+constexpr uint32_t IDESC = tc::idesc_bf16(BM, BN);
+
+struct CorrTcParams {
+    int H, W, npairs, D, omin, nkb, kk_last, nchunks, tiles_x, num_tiles, unary, stages;
+    const float *list;
+    float *out;
+    int *err;
+};
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    k_corr_tc(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR, const CorrTcParams p)
+{
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    const int S = p.stages;
+    float *stg = (float *)(smem + S * STAGE);
+    uint64_t *full = (uint64_t *)((uint8_t *)stg + STG_BYTES);
+    uint64_t *empty = full + S;
+    uint64_t *tfull = empty + S;
+    uint64_t *tempty = tfull + 2;
+    uint64_t *drain = tempty + 2;
+    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    volatile int *zero_flag = abort_flag + 1;
+    int *coff = (int *)(tmem_slot + 4); // [D] band column offset of disparity k
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) {
+            tc::mbar_init(&full[s], 1);
+            tc::mbar_init(&empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tempty[b], 128);
+        }
+        tc::mbar_init(drain, 1);
+        *abort_flag = 0;
+        *zero_flag = 0;
+        tc::mbar_fence_init();
+        tc::prefetch_tmap(&tmL);
+        tc::prefetch_tmap(&tmR);
+    }
+    for (int i = threadIdx.x; i < p.D; i += NUM_THREADS) coff[i] = (int)p.list[i] - p.omin;
+    if (warp == 1) {
+        tc::tmem_alloc(tmem_slot, TMEM_COLS);
+        tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const int tiles_per_pair = p.H * p.tiles_x;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int stage = 0, issued = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
+                const int pair = t / tiles_per_pair, r = t - pair * tiles_per_pair;
+                const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * BM;
+                for (int kb = 0; kb < p.nkb; ++kb) {
+                    if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    uint8_t *sa = smem + stage * STAGE;
+                    tc::mbar_expect_tx(&full[stage], STAGE);
+                    tc::tma_load_4d(sa, &tmL, &full[stage], kb * 64, x0, y, pair);
+                    tc::tma_load_4d(sa + A_BYTES, &tmR, &full[stage], kb * 64, x0 + p.omin, y, p.npairs + pair);
+                    ++issued;
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+                // let the copies already issued land before shared memory is released
+                int st = stage;
+                uint32_t ph = phase;
+                for (int i = 0; i < S && i < issued; ++i) {
+                    if (--st < 0) {
+                        st = S - 1;
+                        ph ^= 1;
+                    }
+                    tc::mbar_wait(&full[st], ph, zero_flag, 1u << 20);
+                }
+            }
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            int stage = 0, lt = 0;
+            uint32_t phase = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x, ++lt) {
+                const int buf = lt & 1;
+                const uint32_t use = (uint32_t)lt >> 1;
+                if (!tc::mbar_wait(&tempty[buf], (use & 1) ^ 1, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc::fence_after_sync();
+                const uint32_t d = tmem + buf * BN;
+                for (int kb = 0; kb < p.nkb; ++kb) {
+                    if (!tc::mbar_wait(&full[stage], phase, abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    tc::fence_after_sync();
+                    const int nk = (kb == p.nkb - 1) ? p.kk_last : 4;
+                    const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
+                    const uint64_t da = tc::sdesc_sw128(sa), db = tc::sdesc_sw128(sa + A_BYTES);
+                    for (int kk = 0; kk < nk; ++kk)
+                        tc::umma_bf16(d, da + 2 * kk, db + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
+                    tc::umma_commit(&empty[stage]);
+                    if (++stage == S) {
+                        stage = 0;
+                        phase ^= 1;
+                    }
+                }
+                if (ok) tc::umma_commit(&tfull[buf]);
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+            }
+            // every MMA of this thread completes before TMEM is released
+            tc::umma_commit(drain);
+            tc::mbar_wait(drain, 0, zero_flag, 1u << 22);
+        }
+    } else {
+        const int q = warp & 3; // the TMEM lane quarter this warp may read
+        float *sw = stg + q * 32 * SROW;
+        const int P = (p.D + 31) >> 5;
+        int off[MAXP];
+#pragma unroll
+        for (int r = 0; r < MAXP; ++r) {
+            const int kk = lane + 32 * r;
+            off[r] = (r < P && kk < p.D) ? coff[kk] : 0;
+        }
+        int lt = 0;
+        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
+            const int buf = lt & 1;
+            const uint32_t use = (uint32_t)lt >> 1;
+            int ok = 1;
+            if (lane == 0) ok = tc::mbar_wait(&tfull[buf], use & 1, abort_flag) ? 1 : 0;
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+                break;
+            }
+            tc::fence_after_sync();
+            // rows 32q.. of the accumulator, columns 32q .. 32q + 32*nchunks
+            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * BN + q * 32;
+            float v[32];
+#pragma unroll 1
+            for (int c = 0; c < p.nchunks; ++c) {
+                tc::tmem_ld32(ta + c * 32, v); // warp-collective: every lane runs it
+#pragma unroll
+                for (int j = 0; j < 32; ++j) sw[lane * SROW + c * 32 + j] = v[j];
+            }
+            tc::fence_before_sync();
+            tc::mbar_arrive(&tempty[buf]);
+            __syncwarp();
+
+            const int pair = t / tiles_per_pair, r = t - pair * tiles_per_pair;
+            const int y = r / p.tiles_x, xq = (r - y * p.tiles_x) * BM + q * 32;
+            const int npx = min(32, p.W - xq);
+            float *obase = p.out + (((size_t)pair * p.H + y) * p.W + xq) * p.D;
+#pragma unroll 1
+            for (int i = 0; i < npx; ++i) {
+                const float *row = sw + i * SROW + i;
+                float cv[MAXP];
+#pragma unroll
+                for (int rr = 0; rr < MAXP; ++rr) cv[rr] = (rr < P && lane + 32 * rr < p.D) ? row[off[rr]] : 0.0f;
+                float *o = obase + (size_t)i * p.D;
+                if (p.unary == 0) {
+                    float m = -FLT_MAX;
+#pragma unroll
+                    for (int rr = 0; rr < MAXP; ++rr)
+                        if (rr < P && lane + 32 * rr < p.D) m = fmaxf(m, cv[rr]);
+#pragma unroll
+                    for (int s = 16; s >= 1; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+                    float sum = 0.0f;
+#pragma unroll
+                    for (int rr = 0; rr < MAXP; ++rr) {
+                        if (rr < P) {
+                            const float e = lane + 32 * rr < p.D ? cnncrf_expf(cv[rr] - m) : 0.0f;
+                            cv[rr] = e;
+                            sum = (rr == 0) ? e : sum + e;
+                        }
+                    }
+#pragma unroll
+                    for (int s = 16; s >= 1; s >>= 1) sum = sum + __shfl_xor_sync(0xffffffffu, sum, s);
+#pragma unroll
+                    for (int rr = 0; rr < MAXP; ++rr) {
+                        const int kk = lane + 32 * rr;
+                        if (rr < P && kk < p.D) o[kk] = -(cv[rr] / sum);
+                    }
+                } else {
+#pragma unroll
+                    for (int rr = 0; rr < MAXP; ++rr) {
+                        const int kk = lane + 32 * rr;
+                        if (rr < P && kk < p.D) o[kk] = p.unary == 1 ? 1.0f - cv[rr] : cv[rr];
+                    }
+                }
+            }
+            __syncwarp(); // the staging rows are rewritten by the next tile
+        }
+    }
+    __syncthreads();
+    if (warp == 1) {
+        tc::fence_after_sync();
+        tc::tmem_dealloc(tmem, TMEM_COLS);
+    }
+}
+
+size_t smem_bytes(int stages, int D)
+{
+    return 1024 + (size_t)stages * STAGE + STG_BYTES + (2 * (size_t)stages + 5) * 8 + 16 + (size_t)D * 4;
+}
+
+} // namespace
+
+bool corr_tc_supported(int C, int cp, int D, int omin, int omax)
+{
+    return cp % 64 == 0 && C >= 1 && C <= cp && D >= 1 && D <= 32 * MAXP && omax >= omin &&
+           omax - omin <= BN - BM && 32 + (omax - omin) <= SCOLS;
+}
+
+int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list, int D, int omin,
+                   int omax, int unary, float *out, int *err, cudaStream_t st)
+{
+    if (!corr_tc_supported(C, cp, D, omin, omax))
+        return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: C=%d cp=%d D=%d band [%d,%d]", C, cp, D, omin, omax);
+    if (npairs < 1 || H < 1 || W < 1) return fail(CNNCRF_EINVAL, "correlation_tc: bad size");
+    if (((uintptr_t)feat & 15) || !out || !err || !d_list) return fail(CNNCRF_EINVAL, "correlation_tc: bad pointer");
+    auto enc = tc::tensor_map_encoder();
+    if (!enc) return fail(CNNCRF_ECUDA, "correlation_tc: cuTensorMapEncodeTiled unavailable");
+    // features [2 * npairs][H][W][cp] BF16: left images first, then right images
+    cuuint64_t g[4] = {(cuuint64_t)cp, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)(2 * npairs)};
+    cuuint64_t s[3] = {(cuuint64_t)cp * 2, (cuuint64_t)W * cp * 2, (cuuint64_t)H * W * cp * 2};
+    cuuint32_t e[4] = {1, 1, 1, 1};
+    cuuint32_t bl[4] = {64, BM, 1, 1};
+    cuuint32_t br[4] = {64, BN, 1, 1};
+    CUtensorMap ml, mr;
+    CUresult r = enc(&ml, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)feat, g, s, bl, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "correlation_tc: left tensor map (%d)", (int)r);
+    r = enc(&mr, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)feat, g, s, br, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "correlation_tc: right tensor map (%d)", (int)r);
+
+    CorrTcParams p{};
+    p.H = H, p.W = W, p.npairs = npairs, p.D = D, p.omin = omin;
+    p.nkb = ceil_div(C, 64);
+    p.kk_last = ceil_div(C - 64 * (p.nkb - 1), 16);
+    p.nchunks = ceil_div(32 + (omax - omin), 32);
+    p.tiles_x = ceil_div(W, BM);
+    p.num_tiles = npairs * H * p.tiles_x;
+    p.unary = unary;
+    p.list = d_list, p.out = out, p.err = err;
+
+    int dev = 0, sms = 0, maxsm = 0;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    p.stages = smem_bytes(3, D) <= (size_t)maxsm ? 3 : 2;
+    const size_t smem = smem_bytes(p.stages, D);
+    if (smem > (size_t)maxsm) return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: %zu bytes of shared memory", smem);
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = std::min(p.num_tiles, sms);
+    {
+        CNNCRF_PROF("corr_tc", st);
+        k_corr_tc<<<grid, NUM_THREADS, smem, st>>>(ml, mr, p);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace k
+} // namespace cnncrf

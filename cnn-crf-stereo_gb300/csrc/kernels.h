@@ -68,6 +68,14 @@ int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs
                      int D, int omin, int omax, bool interp, int unary, float *out, cudaStream_t st,
                      int npairs = 1, long fps = 0);
 
+// same on the tensor cores: BF16 features [2 * npairs][H][W][cp] (left
+// images, then right), integer disparity list whose band omax - omin <= 128;
+// corr_tc_supported says whether a shape qualifies.  err: the bounded-wait
+// error flag.
+bool corr_tc_supported(int C, int cp, int D, int omin, int omax);
+int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list, int D,
+                   int omin, int omax, int unary, float *out, int *err, cudaStream_t st);
+
 // ------------------------------------------------------------ CRF
 struct CrfParams {
     float L1, L2;

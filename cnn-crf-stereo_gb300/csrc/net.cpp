@@ -162,6 +162,8 @@ int cnncrf_net::set_disparities(float mn, float mx, float step, float *d_out)
     float v = D >= 2 ? l[1] : l[0]; // stereo/operators/stereocorrelation.cu:364-373
     interp = std::fabs(v - std::round(v)) > 0.001f;
     bool ip = interp || force_interp;
+    int_list = true;
+    for (float s : l) int_list = int_list && s == std::floor(s);
     omin = 1 << 30, omax = -(1 << 30);
     for (float s : l) {
         int a, b;

@@ -25,6 +25,7 @@ struct cnncrf_net {
     cnncrf::DevBuf d_list;
     int D = 0;
     bool interp = false, force_interp = false;
+    bool int_list = false; // every stored disparity an exact integer
     int omin = 0, omax = 0;
     float *vol = nullptr;
     cnncrf::DevBuf vol_own;

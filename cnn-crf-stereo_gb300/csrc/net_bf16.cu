@@ -5,7 +5,9 @@
 //                    cores), FP32 math, BF16 NHWC output padded to cp_feat
 //   layers 2..L      tcgen05 implicit GEMM over both images at once; the last
 //                    layer L2-normalises in its epilogue for the 1-<fL,fR> unary
-//   correlation      BF16 features, FP32 accumulation, unary fused
+//   correlation      BF16 features, FP32 accumulation, unary fused: tcgen05
+//                    banded GEMM for integer lists of band <= 128, SIMT
+//                    banded kernel otherwise (fractional or wide lists)
 //   pairwise net     SIMT 3x3 (3 -> 64) into BF16, then tcgen05 3x3 (64 -> 64)
 //                    whose epilogue applies the 1x1 head and |.| and writes wx, wy
 // Reference: stereo/stereonet.cpp:250-421, stereo/colorstereonet.cpp:38-77.
@@ -94,8 +96,13 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
     const uint16_t *f = (const uint16_t *)a16[cur].get();
     const size_t fimg = (size_t)H * W * cp;
     feat16 = f;
-    CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)n * fimg, H, W, F, cp, d_list.as<float>(), D, omin, omax,
-                                   interp || force_interp, d.unary, vol, st, n, (long)fimg));
+    const bool ip = interp || force_interp;
+    if (!ip && int_list && k::corr_tc_supported(F, cp, D, omin, omax))
+        CNNCRF_TRY(k::correlation_tc(f, n, H, W, F, cp, d_list.as<float>(), D, omin, omax, d.unary, vol, err.as<int>(),
+                                     st));
+    else
+        CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)n * fimg, H, W, F, cp, d_list.as<float>(), D, omin, omax, ip,
+                                       d.unary, vol, st, n, (long)fimg));
     if (d.with_pairwise) {
         int cr = pad - 2;
         const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
