@@ -4,27 +4,34 @@
 // bias.cpp:58-67, activation.cpp:33-41).
 //
 // GEMM view: D[pixel][n] = sum_{tap, c} act[y+ky][x+kx][c] * W[n][tap][c]
-// (kernel pre-flipped on the host: CUDNN_CONVOLUTION).  A tile is 128
-// consecutive output pixels of one row (M = 128) times all NP output channels;
-// K runs over taps x 64-channel chunks of the NHWC input.
+// (kernel pre-flipped on the host: CUDNN_CONVOLUTION).  A tile is 256
+// consecutive output pixels of one row, computed as two M = 128 halves that
+// share every weight load; N = NP output channels; K runs over taps x
+// 64-channel chunks of the NHWC input.
+//
+// Operand reuse: one shared-memory stage holds, for one kernel row ky and one
+// 64-channel chunk, a 136-pixel window of input row y+ky per half and the
+// weights of the kw taps of that row.  The kx taps read the same window
+// shifted by kx pixels (a descriptor that starts kx 128-byte rows into the
+// swizzled tile), so the input is loaded once per kernel row instead of once
+// per tap.
 //
 // Persistent, warp-specialised CTA (192 threads, one per SM):
-//   warp 0      TMA producer: per k-block one 4-D box (64 ch x 128 px) of the
-//               activation at the tap's offset (zero fill past the row end)
-//               and one 2-D box (64 ch x NP) of the weights, 128-byte swizzle
+//   warp 0      TMA producer: per stage two 4-D boxes (64 ch x 136 px, zero
+//               fill past the row end) and kw 2-D weight boxes (64 ch x NP),
+//               128-byte swizzle
 //   warp 1      TMEM allocation + single-thread tcgen05.mma issue (M=128,
-//               N=NP, K=16 steps), commits free smem stages and hand
-//               finished accumulators to the epilogue
-//   warps 2..5  epilogue: tcgen05.ld of the tile (one pixel per thread),
-//               bias + tanh, then store BF16 NHWC / L2-normalise / apply
-//               the pairwise net's 1x1 head
-// Two TMEM accumulators (128 columns each) let the epilogue of tile i overlap
-// the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout the role
-// raises the CTA abort flag and the global error flag, in-flight copies and
-// MMAs are drained (again bounded) and TMEM is freed before exit.
+//               N=NP, K=16 steps) into two accumulators per tile; commits
+//               free smem stages and hand finished tiles to the epilogue
+//   warps 2..5  epilogue: tcgen05.ld of both halves (one pixel per thread
+//               per half), bias + tanh, then store BF16 NHWC / L2-normalise
+//               / apply the pairwise net's 1x1 head
+// TMEM holds two tiles (four 128-column accumulators): the epilogue of tile i
+// overlaps the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout
+// the role raises the CTA abort flag and the global error flag, in-flight
+// copies and MMAs are drained (again bounded) and TMEM is freed before exit.
 #include <cuda.h>
 #include <cuda_bf16.h>
-#include <cudaTypedefs.h>
 
 #include "common.h"
 #include "kernels.h"
@@ -35,32 +42,34 @@ namespace k {
 
 namespace {
 
-constexpr int BM = 128;
-constexpr int TILE_A = BM * 128; // 128 rows x 64 bf16
+constexpr int BM = 128;                 // pixels per half (UMMA M)
+constexpr int TILE_PX = 2 * BM;         // pixels per tile
+constexpr int AROWS = 136;              // input window per half: 128 + up to 3 kx shifts, 8-row multiple
+constexpr int A_BYTES = AROWS * 128;    // 136 rows x 64 bf16 = 17 KB
 constexpr int NUM_THREADS = 192;
-constexpr uint32_t TMEM_COLS = 256;
-constexpr uint32_t ACC_STRIDE = 128;
+constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
+constexpr int MAX_STAGES = 4;
 
 struct TcParams {
     int n_img, Hin, Win, Ho, Wo, kh, kw, cp_in, kchunks, kk_last, cout, cp_out, tiles_x, num_tiles, mode,
-        stages;
+        stages, stage_bytes;
     const float *bias; // [NP], zero padded
     const float *head; // [2][NP] (mode 2)
     void *out;
     int *err;
 };
 
-template <int NP> __host__ __device__ constexpr int stage_bytes() { return TILE_A + NP * 128; }
-
 template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
 {
-    constexpr int STAGE = stage_bytes<NP>();
     constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
+    constexpr int B_BYTES = NP * 128; // one tap's 64-channel weight box
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = p.stages;
+    const int STAGE = p.stage_bytes;
     uint64_t *full = (uint64_t *)(smem + S * STAGE);
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;
@@ -100,7 +109,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     __syncthreads();
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
-    const int kblocks = p.kh * p.kw * p.kchunks;
+    const int kblocks = p.kh * p.kchunks; // stages per tile: (ky, chunk)
     const int tiles_per_img = p.Ho * p.tiles_x;
 
     if (warp == 0) {
@@ -110,18 +119,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             bool ok = true;
             for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
                 const int img = t / tiles_per_img, r = t - img * tiles_per_img;
-                const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * BM;
+                const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * TILE_PX;
                 for (int kb = 0; kb < kblocks; ++kb) {
-                    const int tap = kb / p.kchunks, ch = kb - tap * p.kchunks;
-                    const int ky = tap / p.kw, kx = tap - ky * p.kw;
+                    const int ky = kb / p.kchunks, ch = kb - ky * p.kchunks;
                     if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
                         ok = false;
                         break;
                     }
                     uint8_t *sa = smem + stage * STAGE;
                     tc::mbar_expect_tx(&full[stage], STAGE);
-                    tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x0 + kx, y + ky, img);
-                    tc::tma_load_2d(sa + TILE_A, &tmB, &full[stage], tap * p.cp_in + ch * 64, 0);
+                    tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x0, y + ky, img);
+                    tc::tma_load_4d(sa + A_BYTES, &tmA, &full[stage], ch * 64, x0 + BM, y + ky, img);
+                    for (int kx = 0; kx < p.kw; ++kx)
+                        tc::tma_load_2d(sa + 2 * A_BYTES + kx * B_BYTES, &tmB, &full[stage],
+                                        (ky * p.kw + kx) * p.cp_in + ch * 64, 0);
                     ++issued;
                     if (++stage == S) {
                         stage = 0;
@@ -157,7 +168,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t d = tmem + buf * ACC_STRIDE;
+                const uint32_t d0 = tmem + (2 * buf) * ACC_STRIDE, d1 = d0 + ACC_STRIDE;
                 for (int kb = 0; kb < kblocks; ++kb) {
                     if (!tc::mbar_wait(&full[stage], phase, abort_flag)) {
                         ok = false;
@@ -167,9 +178,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int ch = kb % p.kchunks;
                     const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
                     const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
-                    const uint64_t da = tc::sdesc_sw128(sa), db = tc::sdesc_sw128(sa + TILE_A);
-                    for (int kk = 0; kk < nk; ++kk)
-                        tc::umma_bf16(d, da + 2 * kk, db + 2 * kk, IDESC, (kb | kk) != 0 ? 1u : 0u);
+                    for (int kx = 0; kx < p.kw; ++kx) {
+                        const uint64_t a0 = tc::sdesc_sw128_rows(sa, kx);
+                        const uint64_t a1 = tc::sdesc_sw128_rows(sa + A_BYTES, kx);
+                        const uint64_t db = tc::sdesc_sw128(sa + 2 * A_BYTES + kx * B_BYTES);
+                        for (int kk = 0; kk < nk; ++kk) {
+                            const uint32_t acc = (kb | kx | kk) != 0 ? 1u : 0u;
+                            tc::umma_bf16(d0, a0 + 2 * kk, db + 2 * kk, IDESC, acc);
+                            tc::umma_bf16(d1, a1 + 2 * kk, db + 2 * kk, IDESC, acc);
+                        }
+                    }
                     tc::umma_commit(&empty[stage]);
                     if (++stage == S) {
                         stage = 0;
@@ -204,58 +222,71 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             }
             tc::fence_after_sync();
             const int img = t / tiles_per_img, r = t - img * tiles_per_img;
-            const int y = r / p.tiles_x, x = (r - y * p.tiles_x) * BM + row;
-            const bool valid = x < p.Wo;
-            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * ACC_STRIDE;
-            float v[16];
-            // the TMEM reads are warp-collective: every lane runs them
-            float sc = 1.0f;
-            if (p.mode == 1) { // pass 1: squared norm of tanh(acc + bias)
-                float s2 = 0.0f;
+            const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * TILE_PX;
+            float hv0[2] = {0.0f, 0.0f}, hv1[2] = {0.0f, 0.0f};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int x = x0 + h * BM + row;
+                const bool valid = x < p.Wo;
+                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf + h) * ACC_STRIDE;
+                float v[16];
+                // the TMEM reads are warp-collective: every lane runs them
+                float sc = 1.0f;
+                if (p.mode == 1) { // pass 1: squared norm of tanh(acc + bias)
+                    float s2 = 0.0f;
+#pragma unroll 1
+                    for (int c = 0; c < NP / 16; ++c) {
+                        tc::tmem_ld16(ta + c * 16, v);
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            const float f = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                            s2 = fmaf(f, f, s2);
+                        }
+                    }
+                    sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
+                }
+                const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
+                __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
+                float a0 = 0.0f, a1 = 0.0f;
 #pragma unroll 1
                 for (int c = 0; c < NP / 16; ++c) {
                     tc::tmem_ld16(ta + c * 16, v);
 #pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        const float f = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
-                        s2 = fmaf(f, f, s2);
+                    for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                    if (p.mode == 2) {
+#pragma unroll
+                        for (int j = 0; j < 16; ++j) {
+                            a0 = fmaf(v[j], shead[c * 16 + j], a0);
+                            a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
+                        }
+                    } else if (valid) {
+                        uint32_t u[8];
+#pragma unroll
+                        for (int j = 0; j < 8; ++j) {
+                            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
+                            u[j] = *(uint32_t *)&b2;
+                        }
+                        uint4 *dst = (uint4 *)(o16 + c * 16);
+                        dst[0] = make_uint4(u[0], u[1], u[2], u[3]);
+                        dst[1] = make_uint4(u[4], u[5], u[6], u[7]);
                     }
                 }
-                sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
-            }
-            const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
-            __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
-            float a0 = 0.0f, a1 = 0.0f;
-#pragma unroll 1
-            for (int c = 0; c < NP / 16; ++c) {
-                tc::tmem_ld16(ta + c * 16, v);
-#pragma unroll
-                for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
-                if (p.mode == 2) {
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) {
-                        a0 = fmaf(v[j], shead[c * 16 + j], a0);
-                        a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
-                    }
-                } else if (valid) {
-                    uint32_t u[8];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) {
-                        __nv_bfloat162 hv = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
-                        u[j] = *(uint32_t *)&hv;
-                    }
-                    uint4 *dst = (uint4 *)(o16 + c * 16);
-                    dst[0] = make_uint4(u[0], u[1], u[2], u[3]);
-                    dst[1] = make_uint4(u[4], u[5], u[6], u[7]);
-                }
+                hv0[h] = a0;
+                hv1[h] = a1;
             }
             tc::fence_before_sync();
             tc::mbar_arrive(&tempty[buf]);
-            if (p.mode == 2 && valid) {
+            if (p.mode == 2) {
                 const size_t plane = (size_t)p.Ho * p.Wo;
                 float *o = (float *)p.out + (size_t)img * 2 * plane; // [img][2][Ho][Wo]
-                o[(size_t)y * p.Wo + x] = fabsf(a0);
-                o[plane + (size_t)y * p.Wo + x] = fabsf(a1);
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int x = x0 + h * BM + row;
+                    if (x < p.Wo) {
+                        o[(size_t)y * p.Wo + x] = fabsf(hv0[h]);
+                        o[plane + (size_t)y * p.Wo + x] = fabsf(hv1[h]);
+                    }
+                }
             }
         }
     }
@@ -266,12 +297,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
 }
 
-template <int NP> size_t smem_bytes(int stages)
+template <int NP> int stage_bytes(int kw) { return 2 * A_BYTES + kw * NP * 128; }
+
+template <int NP> size_t smem_bytes(int stages, int kw)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>() + (2 * stages + 5) * 8 + 16 + 3 * NP * 4 + 64;
+    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 5) * 8 + 16 + 3 * NP * 4 + 64;
 }
 
-template <int NP> int launch(const TcConvArgs &a, const TcParams &p, cudaStream_t st)
+template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
 {
     auto enc = tc::tensor_map_encoder();
     if (!enc) return fail(CNNCRF_ECUDA, "conv_tc: cuTensorMapEncodeTiled unavailable");
@@ -279,7 +312,7 @@ template <int NP> int launch(const TcConvArgs &a, const TcParams &p, cudaStream_
     cuuint64_t gA[4] = {(cuuint64_t)a.cp_in, (cuuint64_t)a.Win, (cuuint64_t)a.Hin, (cuuint64_t)a.n_img};
     cuuint64_t sA[3] = {(cuuint64_t)a.cp_in * 2, (cuuint64_t)a.Win * a.cp_in * 2,
                         (cuuint64_t)a.Hin * a.Win * a.cp_in * 2};
-    cuuint32_t bA[4] = {64, BM, 1, 1};
+    cuuint32_t bA[4] = {64, AROWS, 1, 1};
     cuuint32_t eA[4] = {1, 1, 1, 1};
     CUresult r = enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.in, gA, sA, bA, eA,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
@@ -293,11 +326,17 @@ template <int NP> int launch(const TcConvArgs &a, const TcParams &p, cudaStream_
     r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)a.wt, gB, sB, bB, eB, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: weight tensor map (%d)", (int)r);
-    size_t smem = smem_bytes<NP>(p.stages);
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int dev = 0, sms = 0;
+    int dev = 0, sms = 0, maxsm = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    p.stage_bytes = stage_bytes<NP>(a.kw);
+    p.stages = 0;
+    for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
+        if (smem_bytes<NP>(s, a.kw) <= (size_t)maxsm) p.stages = s;
+    if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
+    const size_t smem = smem_bytes<NP>(p.stages, a.kw);
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = std::min(p.num_tiles, sms);
     {
         CNNCRF_PROF("conv_tc", st);
@@ -313,6 +352,7 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
 {
     if (a.cp_in % 64 != 0 || a.cp_in < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_in %d not a multiple of 64", a.cp_in);
     if (a.cin < 1 || a.cin > a.cp_in) return fail(CNNCRF_EINVAL, "conv_tc: cin %d", a.cin);
+    if (a.kw < 1 || a.kw > AROWS - BM + 1 || a.kh < 1) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: kernel %dx%d", a.kh, a.kw);
     if (((uintptr_t)a.in & 15) || ((uintptr_t)a.wt & 15) || ((uintptr_t)a.out & 15))
         return fail(CNNCRF_EINVAL, "conv_tc: operands must be 16-byte aligned");
     TcParams p{};
@@ -323,22 +363,19 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     int rem = a.cin - 64 * (p.kchunks - 1);
     p.kk_last = rem <= 0 ? 1 : std::min(4, (rem + 15) / 16);
     p.cout = a.cout, p.cp_out = a.cp_out;
-    p.tiles_x = ceil_div(p.Wo, BM);
+    p.tiles_x = ceil_div(p.Wo, TILE_PX);
     p.num_tiles = a.n_img * p.Ho * p.tiles_x;
     p.mode = a.mode;
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
     if (a.mode != 2 && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);
     switch (a.np) {
     case 64:
-        p.stages = 8;
         if (a.mode != 2 && a.cp_out < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<64>(a, p, st);
     case 112:
-        p.stages = 6;
         if (a.mode != 2 && a.cp_out < 112) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<112>(a, p, st);
     case 128:
-        p.stages = 6;
         if (a.mode != 2 && a.cp_out < 128) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<128>(a, p, st);
     default:

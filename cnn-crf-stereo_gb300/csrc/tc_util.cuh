@@ -133,6 +133,17 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr)
     return d;
 }
 
+// Same for an operand that starts `rows` 128-byte rows into a 1024-byte
+// aligned swizzled tile (a shifted window of the tile TMA wrote).  The
+// swizzle phase of a row follows its absolute shared-memory address, for TMA
+// and tcgen05.mma alike, so only the start address moves; the matrix base
+// offset field stays 0 (measured on sm_103a: a base offset of
+// (start >> 7) & 7 on top of the moved start gives wrong products).
+__device__ __forceinline__ uint64_t sdesc_sw128_rows(uint32_t tile_saddr, int rows)
+{
+    return sdesc_sw128(tile_saddr + (uint32_t)rows * 128u);
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator ([4,6) = 1), BF16 A
 // ([7,10) = 1) and B ([10,13) = 1), both K-major, N >> 3 at [17,23),
 // M >> 4 at [24,29).
