@@ -99,17 +99,41 @@ template <int P> __device__ __forceinline__ void store_vec(float *p, int lane, i
         if (k0 + r < D) p[k0 + r] = v[r];
 }
 
-// out = minconv(v) - g, pads (k >= D) kept at +inf.
-template <int P, int DELTA>
+// Exact two-lane IEEE add (add.rn.f32x2) and three-input minimum (min.f32
+// with three sources): the same values as two __fadd_rn and two fminf, in
+// fewer instructions.
+__device__ __forceinline__ void add2(float a0, float a1, float b, float &d0, float &d1)
+{
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %4};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d0), "=f"(d1)
+        : "f"(a0), "f"(a1), "f"(b));
+}
+__device__ __forceinline__ float min3(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// out = minconv(v) - g, pads (k >= D) kept at +inf.  FULL: D == 32 * P (no
+// pad labels, only the chain ends of lanes 0 and 31 are masked).
+template <int P, int DELTA, bool FULL>
 __device__ __forceinline__ void minconv(const float (&v)[P], float g, float w, const Rho &rp, int lane,
                                         int D, float (&out)[P])
 {
+    constexpr int NE = P + 2 * DELTA;       // labels lane*P - DELTA .. lane*P + P + DELTA - 1
+    constexpr int NE2 = (NE + 1) / 2 * 2;   // padded to whole pairs
     float c[DELTA + 1];
 #pragma unroll
     for (int t = 1; t <= DELTA; ++t) c[t] = __fmul_rn(w, rp.rho[t]);
     const float base = __fadd_rn(g, __fmul_rn(w, rp.L2));
+    const int DD = FULL ? 32 * P : D;
     // E[DELTA + i] = value at label lane*P + i, i in [-DELTA, P + DELTA)
-    float E[P + 2 * DELTA];
+    float E[NE2];
 #pragma unroll
     for (int i = -DELTA; i < P + DELTA; ++i) {
         float val;
@@ -122,20 +146,23 @@ __device__ __forceinline__ void minconv(const float (&v)[P], float g, float w, c
             int reg = ((i % P) + P) % P;
             val = __shfl_up_sync(0xffffffffu, v[reg], off);
         }
-        int kk = lane * P + i;
-        E[DELTA + i] = (kk >= 0 && kk < D) ? val : INF;
+        const int kk = lane * P + i;
+        E[DELTA + i] = (kk >= 0 && kk < DD) ? val : INF;
+    }
+    if (NE2 > NE) E[NE2 - 1] = INF;
+    float o[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) o[r] = E[DELTA + r];
+#pragma unroll
+    for (int t = 1; t <= DELTA; ++t) {
+        float S[NE2]; // S[j] = E[j] + c[t]
+#pragma unroll
+        for (int q = 0; q < NE2; q += 2) add2(E[q], E[q + 1], c[t], S[q], S[q + 1]);
+#pragma unroll
+        for (int r = 0; r < P; ++r) o[r] = min3(o[r], S[DELTA + r - t], S[DELTA + r + t]);
     }
 #pragma unroll
-    for (int r = 0; r < P; ++r) {
-        float o = E[DELTA + r];
-#pragma unroll
-        for (int t = 1; t <= DELTA; ++t) {
-            o = fminf(o, __fadd_rn(E[DELTA + r - t], c[t]));
-            o = fminf(o, __fadd_rn(E[DELTA + r + t], c[t]));
-        }
-        o = fminf(o, base);
-        out[r] = (lane * P + r < D) ? __fsub_rn(o, g) : INF;
-    }
+    for (int r = 0; r < P; ++r) out[r] = (FULL || lane * P + r < D) ? __fsub_rn(fminf(o[r], base), g) : INF;
 }
 
 // ---------------------------------------------------------------- cp.async ring
@@ -181,8 +208,20 @@ template <int P> __device__ __forceinline__ void lane_copy(float *dst, const flo
 
 template <int P> __device__ __forceinline__ void lane_read(const float *slot, int lane, float (&v)[P])
 {
+    const float *q = slot + lane * P; // 16-byte aligned for P % 4 == 0, 8-byte for P == 2
+    if constexpr (P % 4 == 0) {
 #pragma unroll
-    for (int r = 0; r < P; ++r) v[r] = slot[lane * P + r];
+        for (int i = 0; i < P / 4; ++i) {
+            const float4 t = *(const float4 *)(q + 4 * i);
+            v[4 * i] = t.x, v[4 * i + 1] = t.y, v[4 * i + 2] = t.z, v[4 * i + 3] = t.w;
+        }
+    } else if constexpr (P == 2) {
+        const float2 t = *(const float2 *)q;
+        v[0] = t.x, v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int r = 0; r < P; ++r) v[r] = q[r];
+    }
 }
 
 constexpr int RING = 8; // prefetch depth in chain steps
@@ -198,7 +237,7 @@ __host__ __device__ constexpr int ring_floats(int P) { return RING * 3 * 32 * P;
 // Per step the pixel vectors come from a per-warp shared-memory ring filled
 // RING steps ahead with cp.async (each lane copies and reads only its own
 // labels), so the chain's dependent arithmetic does not wait on DRAM.
-template <int P, int DELTA, bool HPASS>
+template <int P, int DELTA, bool HPASS, bool FULL>
 __global__ void __launch_bounds__(64)
     k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
                 float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
@@ -249,14 +288,14 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
         for (int r = 0; r < P; ++r) {
             const float un = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
-            v[r] = (lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
+            v[r] = (FULL || lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
         }
         const float g = warp_min<P>(v);
         if (lane == 0) { // the FP64 bound lives in lane 0 only (off the message chain)
             if (i < n - 1) acc += (double)g;
             else cmin = acc + (double)g;
         }
-        if (i < n - 1) minconv<P, DELTA>(v, g, wsm[i], rp, lane, D, L);
+        if (i < n - 1) minconv<P, DELTA, FULL>(v, g, wsm[i], rp, lane, D, L);
     }
     cp_wait<0>();
 
@@ -289,14 +328,14 @@ __global__ void __launch_bounds__(64)
 #pragma unroll
         for (int r = 0; r < P; ++r) {
             A[r] = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
-            m[r] = (lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], A[r]), R[r]) : INF;
+            m[r] = (FULL || lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], A[r]), R[r]) : INF;
         }
         const float mu = warp_min<P>(m);
         if (!HPASS && labels) {
             int best = 0x7fffffff;
 #pragma unroll
             for (int r = P - 1; r >= 0; --r)
-                if (m[r] == mu && lane * P + r < D) best = lane * P + r;
+                if (m[r] == mu && (FULL || lane * P + r < D)) best = lane * P + r;
             best = __reduce_min_sync(0xffffffffu, best);
             if (lane == 0) labels[pix(i)] = best;
         }
@@ -309,9 +348,9 @@ __global__ void __launch_bounds__(64)
         store_vec<P>(phi + pix(i) * D, lane, D, ph);
         if (i > 0) {
 #pragma unroll
-            for (int r = 0; r < P; ++r) v[r] = (lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
+            for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
             const float g = warp_min<P>(v);
-            minconv<P, DELTA>(v, g, wsm[i - 1], rp, lane, D, R);
+            minconv<P, DELTA, FULL>(v, g, wsm[i - 1], rp, lane, D, R);
         }
     }
     cp_wait<0>();
@@ -377,8 +416,9 @@ int run_passes(const float *cost, const float *wx, const float *wy, long wps, in
     const size_t smh = sizeof(float) * wpb * (size_t)(nh + ring_floats(P));
     const size_t smv = sizeof(float) * wpb * (size_t)(nv + ring_floats(P));
     if (smh > 227 * 1024 || smv > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
-    auto kh = k_crf_chain<P, DELTA, true>;
-    auto kv = k_crf_chain<P, DELTA, false>;
+    const bool full = D == 32 * P;
+    auto kh = full ? k_crf_chain<P, DELTA, true, true> : k_crf_chain<P, DELTA, true, false>;
+    auto kv = full ? k_crf_chain<P, DELTA, false, true> : k_crf_chain<P, DELTA, false, false>;
     CNNCRF_CUDA(cudaFuncSetAttribute(kh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smh));
     CNNCRF_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smv));
     for (int it = 0; it < iters; ++it) {
