@@ -35,6 +35,10 @@ struct ConvArgs {
     long in_img = 0, out_img = 0;
 };
 int conv_simt(const ConvArgs &a, cudaStream_t st);
+// BF16 path: a thin first layer (kh*kw*Cin <= 64, Cout 100 or 64, tanh, BF16
+// output) on the tensor cores; err: the bounded-wait error flag
+bool conv_first_tc_supported(const ConvArgs &a);
+int conv_first_tc(const ConvArgs &a, int *err, cudaStream_t st);
 // 1x1 conv Cin -> 2, no bias, |.| (stereo/stereonet.cpp:167,401): planar [2][H][W]
 int conv_head2(const float *in, int npx, int Cin, const float *w /*[2][Cin]*/, float *out,
                cudaStream_t st, int n_img = 1);

@@ -1,14 +1,15 @@
 // net_bf16.cu -- ColorStereoNet::predict on the tensor cores: the BF16 path.
 //
 //   normalise (FP32, as the exact path)
-//   layer 1          SIMT conv (Cin = 1/3/5 is too thin for the tensor
-//                    cores), FP32 math, BF16 NHWC output padded to cp_feat
+//   layer 1          tcgen05 conv with the patch gathered per pixel (K =
+//                    9 * Cin <= 45 is too thin for TMA k-blocks), BF16
+//                    inputs and weights, BF16 NHWC output padded to cp_feat
 //   layers 2..L      tcgen05 implicit GEMM over both images at once; the last
 //                    layer L2-normalises in its epilogue for the 1-<fL,fR> unary
 //   correlation      BF16 features, FP32 accumulation, unary fused: tcgen05
 //                    banded GEMM for integer lists of band <= 128, SIMT
 //                    banded kernel otherwise (fractional or wide lists)
-//   pairwise net     SIMT 3x3 (3 -> 64) into BF16, then tcgen05 3x3 (64 -> 64)
+//   pairwise net     tcgen05 3x3 (3 -> 64, gathered patch) into BF16, then tcgen05 3x3 (64 -> 64)
 //                    whose epilogue applies the 1x1 head and |.| and writes wx, wy
 // Reference: stereo/stereonet.cpp:250-421, stereo/colorstereonet.cpp:38-77.
 #include "kernels.h"
@@ -71,7 +72,8 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
         a.out16 = (uint16_t *)a16[0].get() + (size_t)s * n * h1 * w1 * cp;
         a.out_cs = cp;
         a.n_img = n, a.in_img = (long)h * w * ic, a.out_img = (long)(h1 * w1 * cp);
-        CNNCRF_TRY(k::conv_simt(a, st));
+        if (k::conv_first_tc_supported(a)) CNNCRF_TRY(k::conv_first_tc(a, err.as<int>(), st));
+        else CNNCRF_TRY(k::conv_simt(a, st));
     }
     int hin = (int)h1, win = (int)w1;
     int cur = 0;
@@ -111,7 +113,8 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
         a1.out16 = pw16.get();
         a1.out_cs = cp_pw;
         a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * cp_pw;
-        CNNCRF_TRY(k::conv_simt(a1, st));
+        if (k::conv_first_tc_supported(a1)) CNNCRF_TRY(k::conv_first_tc(a1, err.as<int>(), st));
+        else CNNCRF_TRY(k::conv_simt(a1, st));
         k::TcConvArgs t{};
         t.in = pw16.get();
         t.n_img = n, t.Hin = H + 2, t.Win = W + 2, t.cp_in = cp_pw, t.cin = pw[1].cin;

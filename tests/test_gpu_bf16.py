@@ -16,16 +16,16 @@ def bf16(x, torch):
 
 
 def emulate_features(torch, oracle, cfg, params, img_pad):
-    """The BF16 path in torch: layer 1 in FP32 rounded to BF16, later layers
-    with BF16 weights / activations and FP32 accumulation, tanh, BF16 output;
-    the last layer L2-normalised (unary 1)."""
+    """The BF16 path in torch: every layer with BF16 inputs and weights, FP32
+    accumulation, tanh, BF16 output (layer 1 takes the normalised FP32 image
+    rounded to BF16); the last layer L2-normalised (unary 1)."""
     x = torch.from_numpy(oracle.normalize(img_pad, cfg.in_channels, 32)).permute(2, 0, 1)[None].double()
+    x = bf16(x.float(), torch).double()
     L = cfg.num_layers
     for l in range(L):
         w = torch.from_numpy(params[2 * l]).flip(2, 3)
         b = torch.from_numpy(params[2 * l + 1])
-        if l > 0:
-            w = bf16(w, torch)
+        w = bf16(w, torch)
         y = torch.tanh(torch.nn.functional.conv2d(x.float(), w.float(), b.float()).double())
         if l == L - 1 and cfg.unary == 1:
             y = y / y.norm(dim=1, keepdim=True)
