@@ -229,12 +229,12 @@ def run_profile(args):
     return 0
 
 
-def make_batch(cnncrf, wl, B, precision, graph, stream, seed0):
+def make_batch(cnncrf, wl, B, precision, graph, stream, seed0, group_size=0):
     from cnncrf import scenes
     from cnncrf.api import StereoBatch
     b = StereoBatch(precision=precision, unary=cnncrf.UNARY_ONE_MINUS_DOT, topology=cnncrf.TOPO_ALL3X3,
                     feat_channels=wl["feat"], pw_channels=wl["pw"], crf_shape=cnncrf.RHO_LINEAR,
-                    num_layers=wl["layers"], seed=wl["seed"], graph=graph, stream=stream)
+                    num_layers=wl["layers"], seed=wl["seed"], graph=graph, stream=stream, group_size=group_size)
     sc = [scenes.kitti_scene(wl["W"], wl["H"], wl["D"], seed=seed0 + i) for i in range(B)]
     for _ in range(B):
         b.add_pair(wl["W"], wl["H"], 0.0, 1.0, float(wl["D"] - 1))
@@ -248,6 +248,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=8, help="KITTI pairs per step (the batched form)")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--group-size", type=int, default=-1,
+                    help="pairs per pipelined group of the batch (0: one group of --batch pairs; "
+                         "default: half the batch)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -268,12 +271,15 @@ def main():
     torch.cuda.set_device(local)
     wl = WORKLOAD
     W, H, D, B = wl["W"], wl["H"], wl["D"], args.batch
+    if args.group_size < 0:
+        args.group_size = max(1, B // 2) if B >= 4 else 0
     precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
     crf = (wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], wl["lam"])
     stream = torch.cuda.Stream()
     flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
     with torch.cuda.stream(stream):
-        b, sc = make_batch(cnncrf, wl, B, precision, not args.no_graph, stream, seed0=1000 * rank)
+        b, sc = make_batch(cnncrf, wl, B, precision, not args.no_graph, stream, seed0=1000 * rank,
+                           group_size=args.group_size)
         dl = [torch.from_numpy(x["left"]).cuda() for x in sc]
         dr = [torch.from_numpy(x["right"]).cuda() for x in sc]
         hl = [torch.from_numpy(x["left"]).pin_memory() for x in sc]
@@ -327,8 +333,9 @@ def main():
         labels0 = b.labels_device(0).cpu().numpy()
         disp0 = b.get_output(0)
 
-        # ---- per-kernel device time: the same batch step run eagerly with
-        # CUDA events around every launch on its stream
+        # ---- per-kernel device time: the same batch step run eagerly as one
+        # group (no overlap between kernels) with CUDA events around every
+        # launch on its stream
         bp, _ = make_batch(cnncrf, wl, B, precision, False, stream, seed0=1000 * rank)
         for i in range(B):
             bp.set_images(i, dl[i], dr[i])
@@ -413,7 +420,7 @@ def main():
         "vs_baseline": None, "dtype": "bf16" if precision == cnncrf.BF16 else "f32",
         "data": "synthetic (seeded KITTI-shaped scenes: ground plane + 15 boxes)",
         "config": {"workload": wl["name"], "W": W, "H": H, "D": D, "crf_iters": wl["crf_iters"],
-                   "pairs_per_step": B, "graph": not args.no_graph,
+                   "pairs_per_step": B, "pairs_per_group": args.group_size or B, "graph": not args.no_graph,
                    "net": "7x3x3 conv 100ch + L2 norm, 1-dot unary, pairwise CNN 3x3-3x3-1x1",
                    "crf": "truncated linear L1=0.5 T=3", "l2": "flushed (256 MiB write) between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},

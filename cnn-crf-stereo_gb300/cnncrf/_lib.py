@@ -116,6 +116,7 @@ PROTOS = {
     "cnncrf_batch_destroy": ([vp], i32),
     "cnncrf_batch_set_stream": ([vp, vp], i32),
     "cnncrf_batch_set_network": ([vp, i32, i32, i32, C.c_char_p, C.c_uint64], i32),
+    "cnncrf_batch_set_group_size": ([vp, i32], i32),
     "cnncrf_batch_add_pair": ([vp, i32, i32, f32, f32, f32, C.POINTER(i32)], i32),
     "cnncrf_batch_num_pairs": ([vp, C.POINTER(i32)], i32),
     "cnncrf_batch_set_images": ([vp, i32, vp, vp], i32),

@@ -2,14 +2,21 @@
 // pairs at once (cnncrf_batch_*; no counterpart in the reference, whose
 // Stereo object holds one pair).
 //
-// Pairs with the same size and disparity range form a group.  A group runs as
-// one batch: one net over all its images (the tensor-core convolutions see
-// 2n images per launch), one correlation launch, one CRF launch per pass
-// over all n x H row chains / n x W column chains.  Each group has its own
-// stream, forked from and joined back into the caller's stream, so groups
-// of different sizes overlap on the GPU.  With graph capture on, the whole
-// fork / groups / join sequence is captured once into a CUDA graph and
-// replayed by later runs with the same parameters.
+// Pairs with the same size and disparity range form a group (at most
+// group_cap pairs each when a cap is set).  A group runs as one batch: one
+// net over all its images (the tensor-core convolutions see 2n images per
+// launch), one correlation launch, one CRF launch per pass over all n x H row
+// chains / n x W column chains.
+//
+// The groups form a pipeline: the CNN part of a group (padding, both nets,
+// correlation) runs on a high-priority stream after the CNN part of the
+// previous group, and its CRF on a low-priority stream of its own.  The CNN
+// kernels are bound by the tensor cores, the CRF by HBM, and a CRF CTA fits
+// on an SM beside a convolution CTA, so the CNN of group i+1 runs while the
+// CRF of group i streams its volume.  Everything is forked from and joined
+// back into the batch's stream; with graph capture on, the whole sequence is
+// captured once into a CUDA graph (node priorities kept) and replayed by
+// later runs with the same parameters.
 #include <cmath>
 #include <memory>
 #include <string>
@@ -29,14 +36,17 @@ struct Group {
     std::vector<int> members; // global pair indices, in batch order
     DevBuf img[2], padded[2], vol, pw, out, labels, ws;
     cnncrf_net_t net = nullptr;
-    cudaStream_t stream = nullptr;
-    cudaEvent_t done = nullptr;
+    cudaStream_t stream = nullptr;     // CNN part (high priority)
+    cudaStream_t crf_stream = nullptr; // CRF part (low priority)
+    cudaEvent_t cnn_done = nullptr, done = nullptr;
     size_t ws_bytes = 0;
     ~Group()
     {
         if (net) cnncrf_net_destroy(net);
         if (done) cudaEventDestroy(done);
+        if (cnn_done) cudaEventDestroy(cnn_done);
         if (stream) cudaStreamDestroy(stream);
+        if (crf_stream) cudaStreamDestroy(crf_stream);
     }
 };
 
@@ -60,6 +70,7 @@ struct cnncrf_batch {
     cudaEvent_t in_ev = nullptr, out_ev = nullptr;
     std::vector<std::unique_ptr<Group>> groups;
     std::vector<std::pair<int, int>> loc; // pair -> (group, slot)
+    int group_cap = 0;                    // most pairs per group (0: no cap)
     bool built = false;
     // graph
     bool use_graph = false;
@@ -112,8 +123,12 @@ int cnncrf_batch::build()
         if (g.net) cnncrf_net_destroy(g.net);
         g.net = nullptr;
         CNNCRF_TRY(cnncrf_net_create(&g.net, &d, n, g.H + 2 * pad, g.W + 2 * pad));
-        if (!g.stream) CNNCRF_CUDA(cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking));
+        int prio_low = 0, prio_high = 0;
+        CNNCRF_CUDA(cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high));
+        if (!g.stream) CNNCRF_CUDA(cudaStreamCreateWithPriority(&g.stream, cudaStreamNonBlocking, prio_high));
+        if (!g.crf_stream) CNNCRF_CUDA(cudaStreamCreateWithPriority(&g.crf_stream, cudaStreamNonBlocking, prio_low));
         if (!g.done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+        if (!g.cnn_done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.cnn_done, cudaEventDisableTiming));
         CNNCRF_TRY(cnncrf_net_set_stream(g.net, (cnncrf_stream_t)g.stream));
         for (int s = 0; s < 2; ++s) {
             CNNCRF_TRY(g.img[s].reserve(sizeof(float) * 4 * N * n));
@@ -140,7 +155,8 @@ int cnncrf_batch::build()
     return CNNCRF_OK;
 }
 
-// fork -> every group on its stream -> join, all enqueued on `work`
+// fork -> the groups' CNN parts one after another, each group's CRF after
+// its CNN -> join, all enqueued from `work`
 int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lambda)
 {
     k::CrfParams p;
@@ -148,21 +164,25 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
     if ((float)di != delta || di < 1 || di > 4) return fail(CNNCRF_EUNSUPPORTED, "batch: delta %g", delta);
     p.L1 = L1, p.L2 = L2, p.delta = di, p.shape = o.crf_shape, p.slack = o.crf_slack;
     CNNCRF_CUDA(cudaEventRecord(fork, work));
+    cudaEvent_t prev = fork;
     for (auto &gp : groups) {
         Group &g = *gp;
         const int n = (int)g.members.size();
         const long N = (long)g.W * g.H;
-        cudaStream_t gs = g.stream;
-        CNNCRF_CUDA(cudaStreamWaitEvent(gs, fork, 0));
+        cudaStream_t gs = g.stream, cs = g.crf_stream;
+        CNNCRF_CUDA(cudaStreamWaitEvent(gs, prev, 0));
         const int pad = g.net->pad;
         CNNCRF_TRY(k::pad_rgba(g.img[0].as<float>(), g.W, g.H, pad, g.padded[0].as<float>(), gs, n));
         CNNCRF_TRY(k::pad_rgba(g.img[1].as<float>(), g.W, g.H, pad, g.padded[1].as<float>(), gs, n));
         CNNCRF_TRY(g.net->predict(g.padded[0].as<float>(), g.padded[1].as<float>()));
         CNNCRF_TRY(k::scale(g.pw.as<float>(), 2 * N * n, lambda, gs)); // stereo/stereo.cpp:136-137
+        CNNCRF_CUDA(cudaEventRecord(g.cnn_done, gs));
+        prev = g.cnn_done;
+        CNNCRF_CUDA(cudaStreamWaitEvent(cs, g.cnn_done, 0));
         CNNCRF_TRY(k::crf_solve_batch(g.vol.as<float>(), g.pw.as<float>(), g.W, g.H, g.depth, n, p, iters,
-                                      g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, gs));
-        CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, gs));
-        CNNCRF_CUDA(cudaEventRecord(g.done, gs));
+                                      g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, cs));
+        CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, cs));
+        CNNCRF_CUDA(cudaEventRecord(g.done, cs));
         CNNCRF_CUDA(cudaStreamWaitEvent(work, g.done, 0));
     }
     return CNNCRF_OK;
@@ -224,7 +244,8 @@ int cnncrf_batch_add_pair(cnncrf_batch_t b, int width, int height, float disp_mi
     int gi = -1;
     for (size_t i = 0; i < b->groups.size(); ++i) {
         Group &g = *b->groups[i];
-        if (g.W == width && g.H == height && g.dmin == disp_min && g.dstep == disp_step && g.depth == depth) {
+        if (g.W == width && g.H == height && g.dmin == disp_min && g.dstep == disp_step && g.depth == depth &&
+            (b->group_cap <= 0 || (int)g.members.size() < b->group_cap)) {
             gi = (int)i;
             break;
         }
@@ -241,6 +262,15 @@ int cnncrf_batch_add_pair(cnncrf_batch_t b, int width, int height, float disp_mi
     g.members.push_back(*pair_index);
     b->built = false;
     b->invalidate();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_set_group_size(cnncrf_batch_t b, int max_pairs)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    if (max_pairs < 0) return fail(CNNCRF_EINVAL, "set_group_size: %d", max_pairs);
+    if (!b->loc.empty()) return fail(CNNCRF_ESTATE, "set_group_size: call it before the first add_pair");
+    b->group_cap = max_pairs;
     return CNNCRF_OK;
 }
 
@@ -320,7 +350,7 @@ int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iter
             if (rc == CNNCRF_OK && e != cudaSuccess)
                 rc = fail(CNNCRF_ECUDA, "batch: graph capture failed: %s", cudaGetErrorString(e));
             if (rc == CNNCRF_OK) {
-                e = cudaGraphInstantiate(&b->exec, graph, 0);
+                e = cudaGraphInstantiateWithFlags(&b->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
                 if (e != cudaSuccess) {
                     b->exec = nullptr;
                     rc = fail(CNNCRF_ECUDA, "batch: graph instantiation failed: %s", cudaGetErrorString(e));

@@ -339,6 +339,11 @@ int cnncrf_batch_set_stream(cnncrf_batch_t b, cnncrf_stream_t stream);
  * name (".npz" appended) or NULL for Xavier weights from `seed`. */
 int cnncrf_batch_set_network(cnncrf_batch_t b, int matching, int num_layers, int with_xy,
                              const char *param_base, uint64_t seed);
+/* Most pairs per group (0, the default: every pair of one size and range in
+ * one group).  Smaller groups pipeline: the CNN of one group runs while the
+ * CRF of the previous one streams its volume.  Call before the first
+ * add_pair (ESTATE after). */
+int cnncrf_batch_set_group_size(cnncrf_batch_t b, int max_pairs);
 /* Stereo::initialize for one more pair; returns its index. */
 int cnncrf_batch_add_pair(cnncrf_batch_t b, int width, int height, float disp_min, float disp_step,
                           float disp_max, int *pair_index);

@@ -91,6 +91,8 @@ def test_batch_host_checks(lib):
     b = C.c_void_p()
     assert lib.cnncrf_batch_create(C.byref(b), None) == L.OK
     assert lib.cnncrf_batch_run(b, 1.0, 5.0, 2.0, 3, 1.0) == L.ESTATE  # no pairs
+    assert lib.cnncrf_batch_set_group_size(b, -1) == L.EINVAL
+    assert lib.cnncrf_batch_set_group_size(b, 2) == L.OK
     i = C.c_int()
     assert lib.cnncrf_batch_add_pair(b, 0, 10, 0.0, 1.0, 7.0, C.byref(i)) == L.EINVAL
     assert lib.cnncrf_batch_add_pair(b, 20, 10, 0.0, 1.0, 7.0, C.byref(i)) == L.OK and i.value == 0
@@ -98,6 +100,7 @@ def test_batch_host_checks(lib):
     n = C.c_int()
     lib.cnncrf_batch_num_pairs(b, C.byref(n))
     assert n.value == 2
+    assert lib.cnncrf_batch_set_group_size(b, 4) == L.ESTATE  # grouping is fixed once pairs exist
     out = C.c_void_p()
     assert lib.cnncrf_batch_get_output_device(b, 5, C.byref(out)) == L.EINVAL
     lib.cnncrf_batch_destroy(b)

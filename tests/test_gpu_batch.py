@@ -21,16 +21,18 @@ def single_run(L, scene, prec, dmax, layers, iters, crf):
     return st.labels_device().cpu().numpy(), st.get_output(), st.lower_bound()
 
 
-@pytest.mark.parametrize("prec_name", ["FP32", "BF16"])
-def test_batch_equals_single(cuda, prec_name):
+@pytest.mark.parametrize("prec_name,group_size", [("FP32", 0), ("BF16", 0), ("BF16", 2)])
+def test_batch_equals_single(cuda, prec_name, group_size):
+    """group_size 2 splits the three same-shape pairs into a pipelined group of
+    two and a group of one."""
     from cnncrf import scenes, _lib as L
     from cnncrf.api import StereoBatch
     prec = getattr(L, prec_name)
     layers, iters, crf = 3, 3, (0.5, 1.5, 3)
-    shapes = [(64, 40, 16), (64, 40, 16), (96, 24, 32), (64, 40, 16)]  # two groups, interleaved
+    shapes = [(64, 40, 16), (64, 40, 16), (96, 24, 32), (64, 40, 16)]  # two shapes, interleaved
     sc = [scenes.voronoi_scene(W, H, D, seed=10 + i, cells=4, off_range=(1, D - 2), slope=0.05)
           for i, (W, H, D) in enumerate(shapes)]
-    b = StereoBatch(precision=prec, num_layers=layers, seed=0)
+    b = StereoBatch(precision=prec, num_layers=layers, seed=0, group_size=group_size)
     for (W, H, D) in shapes:
         b.add_pair(W, H, 0.0, 1.0, float(D - 1))
     for i, s in enumerate(sc):
@@ -44,12 +46,13 @@ def test_batch_equals_single(cuda, prec_name):
         assert b.lower_bound(i) == lb, i
 
 
-def test_batch_graph_replay(cuda):
+@pytest.mark.parametrize("group_size", [0, 1])
+def test_batch_graph_replay(cuda, group_size):
     from cnncrf import scenes, _lib as L
     from cnncrf.api import StereoBatch
     torch = cuda
     shapes = [(80, 32, 32)] * 3 + [(48, 24, 16)]
-    b = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=True)
+    b = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=True, group_size=group_size)
     eager = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=False)
     for (W, H, D) in shapes:
         b.add_pair(W, H, 0.0, 1.0, float(D - 1))
