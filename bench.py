@@ -209,21 +209,22 @@ def build_stereo(cnncrf, wl, precision, stream):
 
 
 def run_profile(args):
-    """The device step alone, for ncu: no timing, FP32 comparison or CPU leg."""
+    """The batched device step alone, for ncu: eager launches of one group of
+    --batch pairs, no timing, FP32 comparison or CPU leg."""
     import torch
     import cnncrf
-    from cnncrf import scenes
     wl = WORKLOAD
     precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
     stream = torch.cuda.Stream()
-    scene = scenes.kitti_scene(wl["W"], wl["H"], wl["D"], seed=0)
     with torch.cuda.stream(stream):
-        st = build_stereo(cnncrf, wl, precision, stream)
-        dl = torch.from_numpy(scene["left"]).cuda()
-        dr = torch.from_numpy(scene["right"]).cuda()
+        b, sc = make_batch(cnncrf, wl, args.batch, precision, False, stream, seed0=0, group_size=0)
+        dl = [torch.from_numpy(x["left"]).cuda() for x in sc]
+        dr = [torch.from_numpy(x["right"]).cuda() for x in sc]
         for _ in range(args.warmup + args.steps):
-            st.set_color_images(dl, dr)
-            st.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
+            for i in range(args.batch):
+                b.set_images(i, dl[i], dr[i])
+            b.run(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], wl["lam"])
+        b.check()
         torch.cuda.synchronize()
     print("profile run done")
     return 0

@@ -60,6 +60,38 @@ struct TcParams {
     int *err;
 };
 
+// One stage's MMAs, fully unrolled: kw taps x nk K-steps x two halves, the
+// halves alternating (their accumulators are independent, so the tensor core
+// overlaps them).  Descriptor arithmetic is in 16-byte units: +8 moves the A
+// window one pixel row, +2 one 16-element K step, +NP*8 to the next tap's
+// weight box.  `first` = 0 only for the tile's first stage (overwrite).
+template <int NP, int KW, int NK>
+__device__ __forceinline__ void issue_stage(uint32_t d0, uint32_t d1, uint64_t a0, uint64_t a1, uint64_t db,
+                                            uint32_t first)
+{
+    constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
+#pragma unroll
+    for (int kx = 0; kx < KW; ++kx)
+#pragma unroll
+        for (int kk = 0; kk < NK; ++kk) {
+            const uint32_t acc = (kx | kk) ? 1u : first;
+            tc::umma_bf16(d0, a0 + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, acc);
+            tc::umma_bf16(d1, a1 + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, acc);
+        }
+}
+
+template <int NP, int KW>
+__device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d0, uint32_t d1, uint64_t a0, uint64_t a1,
+                                               uint64_t db, uint32_t first)
+{
+    switch (nk) {
+    case 1: issue_stage<NP, KW, 1>(d0, d1, a0, a1, db, first); break;
+    case 2: issue_stage<NP, KW, 2>(d0, d1, a0, a1, db, first); break;
+    case 3: issue_stage<NP, KW, 3>(d0, d1, a0, a1, db, first); break;
+    default: issue_stage<NP, KW, 4>(d0, d1, a0, a1, db, first); break;
+    }
+}
+
 template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
@@ -178,16 +210,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int ch = kb % p.kchunks;
                     const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
                     const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
-                    for (int kx = 0; kx < p.kw; ++kx) {
-                        const uint64_t a0 = tc::sdesc_sw128_rows(sa, kx);
-                        const uint64_t a1 = tc::sdesc_sw128_rows(sa + A_BYTES, kx);
-                        const uint64_t db = tc::sdesc_sw128(sa + 2 * A_BYTES + kx * B_BYTES);
-                        for (int kk = 0; kk < nk; ++kk) {
-                            const uint32_t acc = (kb | kx | kk) != 0 ? 1u : 0u;
-                            tc::umma_bf16(d0, a0 + 2 * kk, db + 2 * kk, IDESC, acc);
-                            tc::umma_bf16(d1, a1 + 2 * kk, db + 2 * kk, IDESC, acc);
-                        }
-                    }
+                    const uint64_t a0 = tc::sdesc_sw128(sa), a1 = tc::sdesc_sw128(sa + A_BYTES);
+                    const uint64_t db = tc::sdesc_sw128(sa + 2 * A_BYTES);
+                    const uint32_t first = kb == 0 ? 0u : 1u;
+                    // the issue loop is on the tensor core's critical path: unrolled per (kw, nk)
+                    if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d0, d1, a0, a1, db, first);
+                    else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d0, d1, a0, a1, db, first);
+                    else issue_stage_nk<NP, 1>(nk, d0, d1, a0, a1, db, first);
                     tc::umma_commit(&empty[stage]);
                     if (++stage == S) {
                         stage = 0;
@@ -352,7 +381,7 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
 {
     if (a.cp_in % 64 != 0 || a.cp_in < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_in %d not a multiple of 64", a.cp_in);
     if (a.cin < 1 || a.cin > a.cp_in) return fail(CNNCRF_EINVAL, "conv_tc: cin %d", a.cin);
-    if (a.kw < 1 || a.kw > AROWS - BM + 1 || a.kh < 1) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: kernel %dx%d", a.kh, a.kw);
+    if (a.kw < 1 || a.kw > 3 || a.kh < 1) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: kernel %dx%d", a.kh, a.kw);
     if (((uintptr_t)a.in & 15) || ((uintptr_t)a.wt & 15) || ((uintptr_t)a.out & 15))
         return fail(CNNCRF_EINVAL, "conv_tc: operands must be 16-byte aligned");
     TcParams p{};
