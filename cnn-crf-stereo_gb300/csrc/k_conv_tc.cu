@@ -16,13 +16,15 @@
 // swizzled tile), so the input is loaded once per kernel row instead of once
 // per tap.
 //
-// Persistent, warp-specialised CTA (192 threads, one per SM):
+// Persistent, warp-specialised CTA (224 threads, one per SM):
 //   warp 0      TMA producer: per stage two 4-D boxes (64 ch x 136 px, zero
 //               fill past the row end) and kw 2-D weight boxes (64 ch x NP),
 //               128-byte swizzle
-//   warp 1      TMEM allocation + single-thread tcgen05.mma issue (M=128,
-//               N=NP, K=16 steps) into two accumulators per tile; commits
-//               free smem stages and hand finished tiles to the epilogue
+//   warps 1, 6  TMEM allocation (warp 1) and tcgen05.mma issue (M=128,
+//               N=NP, K=16 steps), one thread per half / accumulator: two
+//               issuers keep the tensor core fed with these short MMAs;
+//               their commits free smem stages and hand finished tiles to
+//               the epilogue
 //   warps 2..5  epilogue: tcgen05.ld of both halves (one pixel per thread
 //               per half), bias + tanh, then store BF16 NHWC / L2-normalise
 //               / apply the pairwise net's 1x1 head
@@ -46,7 +48,7 @@ constexpr int BM = 128;                 // pixels per half (UMMA M)
 constexpr int TILE_PX = 2 * BM;         // pixels per tile
 constexpr int AROWS = 136;              // input window per half: 128 + up to 3 kx shifts, 8-row multiple
 constexpr int A_BYTES = AROWS * 128;    // 136 rows x 64 bf16 = 17 KB
-constexpr int NUM_THREADS = 192;
+constexpr int NUM_THREADS = 224;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
 constexpr int MAX_STAGES = 4;
@@ -60,35 +62,29 @@ struct TcParams {
     int *err;
 };
 
-// One stage's MMAs, fully unrolled: kw taps x nk K-steps x two halves, the
-// halves alternating (their accumulators are independent, so the tensor core
-// overlaps them).  Descriptor arithmetic is in 16-byte units: +8 moves the A
-// window one pixel row, +2 one 16-element K step, +NP*8 to the next tap's
-// weight box.  `first` = 0 only for the tile's first stage (overwrite).
+// One stage's MMAs of one half, fully unrolled: kw taps x nk K-steps.
+// Descriptor arithmetic is in 16-byte units: +8 moves the A window one pixel
+// row, +2 one 16-element K step, +NP*8 to the next tap's weight box.
+// `first` = 0 only for the tile's first stage (overwrite the accumulator).
 template <int NP, int KW, int NK>
-__device__ __forceinline__ void issue_stage(uint32_t d0, uint32_t d1, uint64_t a0, uint64_t a1, uint64_t db,
-                                            uint32_t first)
+__device__ __forceinline__ void issue_stage(uint32_t d, uint64_t a, uint64_t db, uint32_t first)
 {
     constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
 #pragma unroll
     for (int kx = 0; kx < KW; ++kx)
 #pragma unroll
-        for (int kk = 0; kk < NK; ++kk) {
-            const uint32_t acc = (kx | kk) ? 1u : first;
-            tc::umma_bf16(d0, a0 + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, acc);
-            tc::umma_bf16(d1, a1 + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, acc);
-        }
+        for (int kk = 0; kk < NK; ++kk)
+            tc::umma_bf16(d, a + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, (kx | kk) ? 1u : first);
 }
 
 template <int NP, int KW>
-__device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d0, uint32_t d1, uint64_t a0, uint64_t a1,
-                                               uint64_t db, uint32_t first)
+__device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d, uint64_t a, uint64_t db, uint32_t first)
 {
     switch (nk) {
-    case 1: issue_stage<NP, KW, 1>(d0, d1, a0, a1, db, first); break;
-    case 2: issue_stage<NP, KW, 2>(d0, d1, a0, a1, db, first); break;
-    case 3: issue_stage<NP, KW, 3>(d0, d1, a0, a1, db, first); break;
-    default: issue_stage<NP, KW, 4>(d0, d1, a0, a1, db, first); break;
+    case 1: issue_stage<NP, KW, 1>(d, a, db, first); break;
+    case 2: issue_stage<NP, KW, 2>(d, a, db, first); break;
+    case 3: issue_stage<NP, KW, 3>(d, a, db, first); break;
+    default: issue_stage<NP, KW, 4>(d, a, db, first); break;
     }
 }
 
@@ -96,7 +92,6 @@ template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
 {
-    constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
     constexpr int B_BYTES = NP * 128; // one tap's 64-channel weight box
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -106,8 +101,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;
     uint64_t *tempty = tfull + 2;
-    uint64_t *drain = tempty + 2;
-    uint32_t *tmem_slot = (uint32_t *)(drain + 1);
+    uint64_t *drain = tempty + 2; // one per issuer
+    uint32_t *tmem_slot = (uint32_t *)(drain + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
     volatile int *zero_flag = abort_flag + 1;
     float *sbias = (float *)(tmem_slot + 4);
@@ -117,13 +112,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
             tc::mbar_init(&full[s], 1);
-            tc::mbar_init(&empty[s], 1);
+            tc::mbar_init(&empty[s], 2); // a commit from each issuer
         }
         for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&tfull[b], 1);
+            tc::mbar_init(&tfull[b], 2);
             tc::mbar_init(&tempty[b], 128);
         }
-        tc::mbar_init(drain, 1);
+        tc::mbar_init(&drain[0], 1);
+        tc::mbar_init(&drain[1], 1);
         *abort_flag = 0;
         *zero_flag = 0;
         tc::mbar_fence_init();
@@ -187,8 +183,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
             }
         }
-    } else if (warp == 1) {
+    } else if (warp == 1 || warp == 6) {
+        // two MMA issuers, one per half: a single thread cannot issue this
+        // tile's short MMAs as fast as the tensor core retires them
         if (lane == 0) {
+            const int h = warp == 6 ? 1 : 0;
             int stage = 0, lt = 0;
             uint32_t phase = 0;
             bool ok = true;
@@ -200,7 +199,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t d0 = tmem + (2 * buf) * ACC_STRIDE, d1 = d0 + ACC_STRIDE;
+                const uint32_t d = tmem + (2 * buf + h) * ACC_STRIDE;
                 for (int kb = 0; kb < kblocks; ++kb) {
                     if (!tc::mbar_wait(&full[stage], phase, abort_flag)) {
                         ok = false;
@@ -210,13 +209,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int ch = kb % p.kchunks;
                     const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
                     const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
-                    const uint64_t a0 = tc::sdesc_sw128(sa), a1 = tc::sdesc_sw128(sa + A_BYTES);
+                    const uint64_t a = tc::sdesc_sw128(sa + h * A_BYTES);
                     const uint64_t db = tc::sdesc_sw128(sa + 2 * A_BYTES);
                     const uint32_t first = kb == 0 ? 0u : 1u;
-                    // the issue loop is on the tensor core's critical path: unrolled per (kw, nk)
-                    if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d0, d1, a0, a1, db, first);
-                    else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d0, d1, a0, a1, db, first);
-                    else issue_stage_nk<NP, 1>(nk, d0, d1, a0, a1, db, first);
+                    if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d, a, db, first);
+                    else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d, a, db, first);
+                    else issue_stage_nk<NP, 1>(nk, d, a, db, first);
                     tc::umma_commit(&empty[stage]);
                     if (++stage == S) {
                         stage = 0;
@@ -230,8 +228,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 atomicExch(p.err, 1);
             }
             // every MMA of this thread completes before TMEM is released
-            tc::umma_commit(drain);
-            tc::mbar_wait(drain, 0, zero_flag, 1u << 22);
+            tc::umma_commit(&drain[h]);
+            tc::mbar_wait(&drain[h], 0, zero_flag, 1u << 22);
         }
     } else {
         const int q = warp & 3; // the TMEM lane quarter this warp may read
@@ -330,7 +328,7 @@ template <int NP> int stage_bytes(int kw) { return 2 * A_BYTES + kw * NP * 128; 
 
 template <int NP> size_t smem_bytes(int stages, int kw)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 5) * 8 + 16 + 3 * NP * 4 + 64;
+    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 6) * 8 + 16 + 3 * NP * 4 + 64;
 }
 
 template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
