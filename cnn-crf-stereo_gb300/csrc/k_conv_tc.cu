@@ -10,15 +10,16 @@
 // 64-channel chunks of the NHWC input.
 //
 // Operand reuse: one shared-memory stage holds, for one kernel row ky and one
-// 64-channel chunk, a 136-pixel window of input row y+ky per half and the
-// weights of the kw taps of that row.  The kx taps read the same window
+// 64-channel chunk, the 264-pixel window of input row y+ky that both halves
+// read (a 128-row and a 136-row box, one after the other) and the weights of
+// the kw taps of that row.  The kx taps read the same window
 // shifted by kx pixels (a descriptor that starts kx 128-byte rows into the
 // swizzled tile), so the input is loaded once per kernel row instead of once
 // per tap.
 //
 // Persistent, warp-specialised CTA (224 threads, one per SM):
-//   warp 0      TMA producer: per stage two 4-D boxes (64 ch x 136 px, zero
-//               fill past the row end) and kw 2-D weight boxes (64 ch x NP),
+//   warp 0      TMA producer: per stage two 4-D boxes (64 ch x 128 / 136 px,
+//               zero fill past the row end) and kw 2-D weight boxes (64 ch x NP),
 //               128-byte swizzle
 //   warps 1, 6  TMEM allocation (warp 1) and tcgen05.mma issue (M=128,
 //               N=NP, K=16 steps), one thread per half / accumulator: two
@@ -46,8 +47,8 @@ namespace {
 
 constexpr int BM = 128;                 // pixels per half (UMMA M)
 constexpr int TILE_PX = 2 * BM;         // pixels per tile
-constexpr int AROWS = 136;              // input window per half: 128 + up to 3 kx shifts, 8-row multiple
-constexpr int A_BYTES = AROWS * 128;    // 136 rows x 64 bf16 = 17 KB
+constexpr int AROWS = 2 * BM + 8;       // input window of both halves: 256 px + up to 8 more for the kx taps
+constexpr int A_BYTES = AROWS * 128;    // 264 rows x 64 bf16 = 33 KB (loaded as 128 + 136 rows)
 constexpr int NUM_THREADS = 224;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
@@ -90,7 +91,8 @@ __device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d, uint64_t a, u
 
 template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
-    k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const TcParams p)
+    k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
+              const __grid_constant__ CUtensorMap tmB, const TcParams p)
 {
     constexpr int B_BYTES = NP * 128; // one tap's 64-channel weight box
     extern __shared__ uint8_t smem_raw[];
@@ -124,6 +126,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         *zero_flag = 0;
         tc::mbar_fence_init();
         tc::prefetch_tmap(&tmA);
+        tc::prefetch_tmap(&tmA2);
         tc::prefetch_tmap(&tmB);
     }
     for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias[i];
@@ -156,10 +159,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                     uint8_t *sa = smem + stage * STAGE;
                     tc::mbar_expect_tx(&full[stage], STAGE);
+                    // input pixels x0 .. x0 + 263 as rows 0 .. 263 (a 128-row and a 136-row box)
                     tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x0, y + ky, img);
-                    tc::tma_load_4d(sa + A_BYTES, &tmA, &full[stage], ch * 64, x0 + BM, y + ky, img);
+                    tc::tma_load_4d(sa + BM * 128, &tmA2, &full[stage], ch * 64, x0 + BM, y + ky, img);
                     for (int kx = 0; kx < p.kw; ++kx)
-                        tc::tma_load_2d(sa + 2 * A_BYTES + kx * B_BYTES, &tmB, &full[stage],
+                        tc::tma_load_2d(sa + A_BYTES + kx * B_BYTES, &tmB, &full[stage],
                                         (ky * p.kw + kx) * p.cp_in + ch * 64, 0);
                     ++issued;
                     if (++stage == S) {
@@ -209,8 +213,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int ch = kb % p.kchunks;
                     const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
                     const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
-                    const uint64_t a = tc::sdesc_sw128(sa + h * A_BYTES);
-                    const uint64_t db = tc::sdesc_sw128(sa + 2 * A_BYTES);
+                    const uint64_t a = tc::sdesc_sw128(sa + h * BM * 128);
+                    const uint64_t db = tc::sdesc_sw128(sa + A_BYTES);
                     const uint32_t first = kb == 0 ? 0u : 1u;
                     if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d, a, db, first);
                     else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d, a, db, first);
@@ -324,11 +328,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
 }
 
-template <int NP> int stage_bytes(int kw) { return 2 * A_BYTES + kw * NP * 128; }
+template <int NP> int stage_bytes(int kw) { return A_BYTES + kw * NP * 128; }
 
-template <int NP> size_t smem_bytes(int stages, int kw)
+template <int NP> size_t smem_bytes(int stages, int kw, int mode)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 6) * 8 + 16 + 3 * NP * 4 + 64;
+    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 6) * 8 + 16 + (mode == 2 ? 3 : 1) * NP * 4;
 }
 
 template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
@@ -339,11 +343,15 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     cuuint64_t gA[4] = {(cuuint64_t)a.cp_in, (cuuint64_t)a.Win, (cuuint64_t)a.Hin, (cuuint64_t)a.n_img};
     cuuint64_t sA[3] = {(cuuint64_t)a.cp_in * 2, (cuuint64_t)a.Win * a.cp_in * 2,
                         (cuuint64_t)a.Hin * a.Win * a.cp_in * 2};
-    cuuint32_t bA[4] = {64, AROWS, 1, 1};
+    cuuint32_t bA[4] = {64, BM, 1, 1}, bA2[4] = {64, AROWS - BM, 1, 1};
     cuuint32_t eA[4] = {1, 1, 1, 1};
+    CUtensorMap ma2;
     CUresult r = enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.in, gA, sA, bA, eA,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation tensor map (%d)", (int)r);
+    r = enc(&ma2, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.in, gA, sA, bA2, eA, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation tensor map (%d)", (int)r);
     const int taps = a.kh * a.kw;
     cuuint64_t gB[2] = {(cuuint64_t)taps * a.cp_in, (cuuint64_t)NP};
@@ -360,14 +368,14 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     p.stage_bytes = stage_bytes<NP>(a.kw);
     p.stages = 0;
     for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
-        if (smem_bytes<NP>(s, a.kw) <= (size_t)maxsm) p.stages = s;
+        if (smem_bytes<NP>(s, a.kw, a.mode) <= (size_t)maxsm) p.stages = s;
     if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
-    const size_t smem = smem_bytes<NP>(p.stages, a.kw);
+    const size_t smem = smem_bytes<NP>(p.stages, a.kw, a.mode);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = std::min(p.num_tiles, sms);
     {
         CNNCRF_PROF("conv_tc", st);
-        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, mb, p);
+        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, p);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
@@ -380,6 +388,7 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     if (a.cp_in % 64 != 0 || a.cp_in < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_in %d not a multiple of 64", a.cp_in);
     if (a.cin < 1 || a.cin > a.cp_in) return fail(CNNCRF_EINVAL, "conv_tc: cin %d", a.cin);
     if (a.kw < 1 || a.kw > 3 || a.kh < 1) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: kernel %dx%d", a.kh, a.kw);
+    static_assert(AROWS - 2 * BM + 1 >= 3, "the input window covers kx shifts up to 2 for the second half");
     if (((uintptr_t)a.in & 15) || ((uintptr_t)a.wt & 15) || ((uintptr_t)a.out & 15))
         return fail(CNNCRF_EINVAL, "conv_tc: operands must be 16-byte aligned");
     TcParams p{};
