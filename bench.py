@@ -64,8 +64,8 @@ def conv_flops(W, H, layers=7, feat=100, ic=3, pw=64, k=3):
 
 
 def crf_bytes_per_pass(W, H, D):
-    """Algorithmic bytes of one chain pass: read unary, read message, write
-    message, N*D floats each."""
+    """Algorithmic bytes of one chain pass as counted for the roofline: three
+    N*D float arrays (the subproblem's unary inputs read once, phi written)."""
     return 3 * W * H * D * 4
 
 
@@ -228,6 +228,13 @@ def run_profile(args):
         torch.cuda.synchronize()
     print("profile run done")
     return 0
+
+
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) measured with ncu on one-pair launches
+# of this workload, scaled to a launch of the 8-pair step (traffic grows with the images / chains):
+# k_conv_tc layer 2 over 2 images 417.4 MB; k_crf_chain H pass 1553.6 MB and V pass 1067.6 MB per pair.
+CONV_TC_BYTES_PER_IMAGE = 417.4e6 / 2
+CRF_H_BYTES_PER_PAIR, CRF_V_BYTES_PER_PAIR = 1553.6e6, 1067.6e6
 
 
 def make_batch(cnncrf, wl, B, precision, graph, stream, seed0, group_size=0):
@@ -398,7 +405,10 @@ def main():
         flops = (tc_f if conv_name == "conv_tc" else tc_f + simt_f) * B * nprof
         achieved = flops / (t / 1000.0) / 1e12
         roof = {"kernel": conv_name, "bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"],
-                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+                "unit": "TFLOP/s", "frac": achieved / peaks["bf16_tflops"],
+                "traffic": CONV_TC_BYTES_PER_IMAGE * 2 * B if conv_name == "conv_tc" else None,
+                "traffic_unit": "DRAM bytes of one feature-layer launch (%d images; ncu, 2-image launch scaled)"
+                                % (2 * B),
                 "peak_source": peak_src + " (bf16 dense burst)",
                 "per_launch": "FLOPs of the tensor-core layers of %d pairs / their summed launch time" % B}
     crf_roof = None
@@ -406,8 +416,12 @@ def main():
         n = prof["crf_h"][0] + prof["crf_v"][0]
         t = prof["crf_h"][1] + prof["crf_v"][1]
         gbs = crf_bytes_per_pass(W, H, D) * B * n / (t / 1000.0) / 1e9
+        tb = (CRF_H_BYTES_PER_PAIR + CRF_V_BYTES_PER_PAIR) / 2 * B
         crf_roof = {"kernel": "crf_h+crf_v", "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
-                    "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src}
+                    "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"], "traffic": tb,
+                    "traffic_unit": "DRAM bytes per pass launch (%d pairs, mean of H and V; ncu, 1-pair launches "
+                                    "scaled); achieved counts the algorithmic 3 x N x D x 4 B per pass" % B,
+                    "measured_gbs": tb * n / (t / 1000.0) / 1e9, "peak_source": peak_src}
 
     cpu = None
     if not args.no_cpu_baseline:
