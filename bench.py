@@ -1,20 +1,21 @@
 """Benchmark of the CNN-CRF stereo hot path (one JSON line on rank 0).
 
-Workload (the reference's metric "stereo pairs/s at 1242x375 D=128"): one
-KITTI-shaped RGB pair per step, 1242x375, D = 128 (disparities 0..127), the
-7-layer all-3x3 100-channel feature CNN with L2-normalised features and the
+Workload (the reference's metric "stereo pairs/s at 1242x375 D=128"):
+KITTI-shaped RGB pairs, 1242x375, D = 128 (disparities 0..127), the 7-layer
+all-3x3 100-channel feature CNN with L2-normalised features and the
 1 - <fL,fR> unary, the 2-layer 3x3 (+1x1) pairwise CNN, a 4-connected CRF
 with truncated-linear pairwise (L1 = 0.5, truncation 3) solved with 8
-iterations, Xavier weights from seed 0, seeded synthetic scene (ground plane
-+ 15 boxes; the KITTI images are not available).
+iterations, Xavier weights from seed 0, seeded synthetic scenes (ground plane
++ 15 boxes; the KITTI images are not available).  A step is one batched run
+of --batch pairs (default 8) through the BF16 path.
 
-  value   pairs/s with the input pair already in HBM (device-to-device
+  value   pairs/s with the input pairs already in HBM (device-to-device
           staging + CNN + correlation + CRF + remap per step), CUDA events on
           the library's stream, L2 flushed (256 MiB write) between steps
-  e2e     same through the public API from pinned HOST buffers: H2D of both
-          RGBA images, the whole path, D2H of the disparity map per step
+  e2e     same through the public API from pinned HOST buffers: H2D of the
+          RGBA images, the whole path, D2H of the disparity maps per step
   --impl reference   the CPU restatement of the reference path (OpenMP, all
-          host threads) on the same workload; see the design doc.
+          host threads) on the same workload, one pair per step.
 
 Multi-GPU: pairs are independent, so N ranks run N replicas (no
 collective on the data path); value = pairs of all ranks / max rank time.
@@ -130,6 +131,12 @@ def dist_setup():
     return rank, world, local
 
 
+def replica_value(steps, pairs_per_step, world, t_ms):
+    """Whole-job pairs/s: every rank runs `steps` steps of its own pairs; the
+    time is the slowest rank's (max over ranks)."""
+    return steps * pairs_per_step * world / (t_ms / 1000.0)
+
+
 def barrier(world):
     if world > 1:
         import torch.distributed as dist
@@ -168,8 +175,9 @@ def cpu_pairs_per_s(wl, scene, pairs=1):
 
 
 def run_reference(args):
-    rank, world, _ = dist_setup()
-    if rank != 0:
+    # rank 0 alone times the CPU path; it needs no process group, so the other
+    # ranks of a torchrun launch exit at once
+    if int(os.environ.get("RANK", "0")) != 0:
         return 0
     from cnncrf import scenes
     wl = WORKLOAD
@@ -333,10 +341,10 @@ def main():
         t_ms = timed(step_device, args.steps)
         launches = _lib.kernel_launches() - l0
         clk = clocks.stop()
-        value = args.steps * B * world / (t_ms / 1000.0)
+        value = replica_value(args.steps, B, world, t_ms)
         # ---- end to end through the public API from pinned host buffers
         e_ms = timed(step_e2e, args.steps)
-        e2e = args.steps * B * world / (e_ms / 1000.0)
+        e2e = replica_value(args.steps, B, world, e_ms)
         b.check()
         labels0 = b.labels_device(0).cpu().numpy()
         disp0 = b.get_output(0)
