@@ -88,6 +88,11 @@ PROTOS = {
     "cnncrf_warp_image": ([vp, vp, vp, i32, i32, vp], i32),
     "cnncrf_tv_fit": ([vp, vp, i32, i32, f32, f32, vp], i32),
     "cnncrf_tv_iterate": ([vp, vp, vp, vp, vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp], i32),
+    "cnncrf_rgb_to_gray": ([vp, vp, i32, i32, vp], i32),
+    "cnncrf_census_volume": ([vp, vp, i32, i32, i32, f32, f32, i32, f32, vp, vp], i32),
+    "cnncrf_edge_weights": ([vp, i32, i32, f32, f32, f32, vp, vp, vp], i32),
+    "cnncrf_quad_fit_direct": ([vp, vp, i32, i32, i32, f32, f32, vp], i32),
+    "cnncrf_left_right_check": ([vp, vp, i32, i32, f32, vp, vp], i32),
     "cnncrf_stereo_default_options": ([C.POINTER(StereoOptions)], i32),
     "cnncrf_stereo_create": ([C.POINTER(vp), C.POINTER(StereoOptions)], i32),
     "cnncrf_stereo_destroy": ([vp], i32),
@@ -102,6 +107,9 @@ PROTOS = {
     "cnncrf_stereo_set_color_images_device": ([vp, vp, vp], i32),
     "cnncrf_stereo_compute_volume": ([vp, i32], i32),
     "cnncrf_stereo_compute_slack_propagation": ([vp, f32, f32, f32, i32, f32, f32, f32, i32], i32),
+    "cnncrf_stereo_set_filter_size": ([vp, i32], i32),
+    "cnncrf_stereo_compute_weights": ([vp, f32, f32, f32, i32], i32),
+    "cnncrf_stereo_fuse_quad_fit_direct": ([vp], i32),
     "cnncrf_stereo_compute_argmax": ([vp, i32], i32),
     "cnncrf_stereo_fuse_thuber_quad_fit": ([vp, f32, f32, i32, i32], i32),
     "cnncrf_stereo_get_output": ([vp, vp], i32),

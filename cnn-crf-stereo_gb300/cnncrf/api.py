@@ -261,6 +261,48 @@ def tv_iterate(u, u0, qf, wx, wy, C_, huber_eps, disp_step, iterations, stream=N
     return u, u_, p, q
 
 
+def rgb_to_gray(img_rgba, stream=None):
+    """(H, W, 4) RGBA -> (H, W) grey, .2989 R + .5870 G + .1140 B."""
+    H, W, _ = img_rgba.shape
+    out = torch.empty((H, W), device="cuda", dtype=torch.float32)
+    call("cnncrf_rgb_to_gray", _ptr(img_rgba), _ptr(out), W, H, _stream_ptr(stream))
+    return out
+
+
+def census_volume(gray_ref, gray_other, filter_size, disp_min, disp_step, depth, lambda_census=1.0, stream=None):
+    """Census cost volume (H, W, depth) of gray_ref against gray_other shifted by -disparity."""
+    H, W = gray_ref.shape
+    out = torch.empty((H, W, depth), device="cuda", dtype=torch.float32)
+    call("cnncrf_census_volume", _ptr(gray_ref), _ptr(gray_other), W, H, filter_size, disp_min, disp_step, depth,
+         lambda_census, _ptr(out), _stream_ptr(stream))
+    return out
+
+
+def edge_weights(gray, alpha, beta, lambda_reg, stream=None):
+    """Image-gradient pairwise weights (wx, wy), each (H, W)."""
+    H, W = gray.shape
+    wx = torch.empty((H, W), device="cuda", dtype=torch.float32)
+    wy = torch.empty_like(wx)
+    call("cnncrf_edge_weights", _ptr(gray), W, H, alpha, beta, lambda_reg, _ptr(wx), _ptr(wy), _stream_ptr(stream))
+    return wx, wy
+
+
+def quad_fit_direct(u, c1, disp_min, disp_step, stream=None):
+    """Sub-label refinement of the disparity map u (H, W) on the costs c1 (H, W, D); returns a new map."""
+    H, W, D = c1.shape
+    u = u.clone()
+    call("cnncrf_quad_fit_direct", _ptr(u), _ptr(c1), W, H, D, disp_min, disp_step, _stream_ptr(stream))
+    return u
+
+
+def left_right_check(left, right, threshold, stream=None):
+    """Left disparities where the right map agrees within threshold, else -1."""
+    H, W = left.shape
+    out = torch.empty_like(left)
+    call("cnncrf_left_right_check", _ptr(left), _ptr(right), W, H, threshold, _ptr(out), _stream_ptr(stream))
+    return out
+
+
 class Stereo:
     """Stereo (stereo/stereo.h:40-133) over cnncrf_stereo_*."""
 
@@ -303,6 +345,9 @@ class Stereo:
     def set_with_xy(self, v):
         call("cnncrf_stereo_set_with_xy", self._h, 1 if v else 0)
 
+    def set_filter_size(self, fs):
+        call("cnncrf_stereo_set_filter_size", self._h, fs)
+
     def set_color_images(self, left, right):
         """Host RGBA float arrays (H, W, 4), or CUDA tensors."""
         if isinstance(left, torch.Tensor) and left.is_cuda:
@@ -327,8 +372,14 @@ class Stereo:
     def compute_argmax(self, lr=True):
         call("cnncrf_stereo_compute_argmax", self._h, 1 if lr else 0)
 
+    def compute_weights(self, alpha, beta, lambda_reg, lr=True):
+        call("cnncrf_stereo_compute_weights", self._h, alpha, beta, lambda_reg, 1 if lr else 0)
+
     def fuse_thuber_quad_fit(self, lambda_reg, C_, iterations=10, warps=2):
         call("cnncrf_stereo_fuse_thuber_quad_fit", self._h, lambda_reg, C_, iterations, warps)
+
+    def fuse_quad_fit_direct(self):
+        call("cnncrf_stereo_fuse_quad_fit_direct", self._h)
 
     def get_output(self, out=None):
         out = np.empty((self.H, self.W), np.float32) if out is None else out

@@ -113,7 +113,7 @@ def workload(name, seed=0):
 
 
 def bad_pixels(disp, gt, thresh=3.0, rel=0.05):
-    """KITTI-style error rate: |d - gt| > thresh and > rel * gt."""
-    err = np.abs(disp - gt)
-    bad = (err > thresh) & (err > rel * np.abs(gt))
-    return float(bad.mean())
+    """KITTI error rate of a disparity map against a synthetic ground truth,
+    both read as 16-bit PNGs would be (eval/compute_numbers_kitti.py:6-17)."""
+    from .evaluation import kitti_error, quantize_png16
+    return kitti_error(quantize_png16(disp), quantize_png16(gt), (thresh, rel))

@@ -80,6 +80,19 @@ bool corr_tc_supported(int C, int cp, int D, int omin, int omax);
 int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list, int D,
                    int omin, int omax, int unary, float *out, int *err, cudaStream_t st);
 
+// ------------------------------------------------------------ census, edge weights, QuadDirect, LR check
+constexpr int GAUSS_R = 3;           // Gaussian of the edge image: radius 3 >= 3 sigma
+constexpr float GAUSS_SIGMA = 0.7f;  // stereo/stereo.cu:1092
+int rgb_to_gray(const float *rgba, long n, float *gray, cudaStream_t st);
+// d_list[z] = the z-th disparity (positive = left pixel x matches right x - d)
+int census_volume(const float *g1, const float *g2, int W, int H, int fs, const float *d_list, int D, float lambda,
+                  float *vol, cudaStream_t st);
+void gauss_weights(float sigma, int R, float *w); // host: 2R+1 normalised weights
+int edge_weights(const float *gray, int W, int H, float alpha, float beta, float lambda, float *tmp, float *tmp2,
+                 const float *d_gw, float *wx, float *wy, cudaStream_t st);
+int quadfit_direct(float *u, const float *c1, long npx, int D, float dmin, float dstep, cudaStream_t st);
+int lr_check(const float *left, const float *right, int W, int H, float th, float *out, cudaStream_t st);
+
 // ------------------------------------------------------------ CRF
 struct CrfParams {
     float L1, L2;

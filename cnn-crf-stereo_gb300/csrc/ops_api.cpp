@@ -4,6 +4,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <vector>
 
 #include "common.h"
 #include "kernels.h"
@@ -222,6 +223,73 @@ int cnncrf_tv_iterate(float *d_u, float *d_u_, const float *d_u0, const float *d
     CNNCRF_CUDA(cudaMemsetAsync(d_q, 0, sizeof(float) * 2 * (size_t)width * height, st));
     return k::tv_iterate(d_u, d_u_, d_u0, d_qf, d_p, d_q, d_wx, d_wy, width, height, C, huber_eps, disp_step,
                          iterations, st);
+}
+
+// ---------------------------------------------------------------- census, edge weights, QuadDirect, LR check
+
+int cnncrf_rgb_to_gray(const float *d_rgba, float *d_gray, int width, int height, cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!d_rgba || !d_gray || width < 1 || height < 1) return fail(CNNCRF_EINVAL, "rgb_to_gray: bad argument");
+    return k::rgb_to_gray(d_rgba, (long)width * height, d_gray, (cudaStream_t)stream);
+}
+
+int cnncrf_census_volume(const float *d_gray_ref, const float *d_gray_other, int width, int height, int filter_size,
+                         float disp_min, float disp_step, int depth, float lambda, float *d_volume,
+                         cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!d_gray_ref || !d_gray_other || !d_volume || width < 1 || height < 1 || depth < 1)
+        return fail(CNNCRF_EINVAL, "census_volume: bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    std::vector<float> l((size_t)depth);
+    float d = disp_min;
+    for (int z = 0; z < depth; ++z, d += disp_step) l[z] = d;
+    DevBuf dl;
+    CNNCRF_TRY(dl.reserve(sizeof(float) * depth));
+    CNNCRF_CUDA(cudaMemcpyAsync(dl.get(), l.data(), sizeof(float) * depth, cudaMemcpyHostToDevice, st));
+    CNNCRF_TRY(k::census_volume(d_gray_ref, d_gray_other, width, height, filter_size, dl.as<float>(), depth, lambda,
+                                d_volume, st));
+    CNNCRF_CUDA(cudaStreamSynchronize(st)); // the list buffer is freed on return
+    return CNNCRF_OK;
+}
+
+int cnncrf_edge_weights(const float *d_gray, int width, int height, float alpha, float beta, float lambda,
+                        float *d_wx, float *d_wy, cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!d_gray || !d_wx || !d_wy || width < 1 || height < 1) return fail(CNNCRF_EINVAL, "edge_weights: bad argument");
+    cudaStream_t st = (cudaStream_t)stream;
+    const size_t n = (size_t)width * height;
+    float w[2 * k::GAUSS_R + 1];
+    k::gauss_weights(k::GAUSS_SIGMA, k::GAUSS_R, w);
+    DevBuf t1, t2, gw;
+    CNNCRF_TRY(t1.reserve(n * sizeof(float)));
+    CNNCRF_TRY(t2.reserve(n * sizeof(float)));
+    CNNCRF_TRY(gw.reserve(sizeof w));
+    CNNCRF_CUDA(cudaMemcpyAsync(gw.get(), w, sizeof w, cudaMemcpyHostToDevice, st));
+    CNNCRF_TRY(k::edge_weights(d_gray, width, height, alpha, beta, lambda, t1.as<float>(), t2.as<float>(),
+                               gw.as<float>(), d_wx, d_wy, st));
+    CNNCRF_CUDA(cudaStreamSynchronize(st)); // the scratch buffers are freed on return
+    return CNNCRF_OK;
+}
+
+int cnncrf_quad_fit_direct(float *d_u, const float *d_c1, int width, int height, int depth, float disp_min,
+                           float disp_step, cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!d_u || !d_c1 || width < 1 || height < 1 || depth < 1 || !(disp_step > 0.0f))
+        return fail(CNNCRF_EINVAL, "quad_fit_direct: bad argument");
+    return k::quadfit_direct(d_u, d_c1, (long)width * height, depth, disp_min, disp_step, (cudaStream_t)stream);
+}
+
+int cnncrf_left_right_check(const float *d_left, const float *d_right, int width, int height, float threshold,
+                            float *d_out, cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!d_left || !d_right || !d_out || width < 1 || height < 1)
+        return fail(CNNCRF_EINVAL, "left_right_check: bad argument");
+    return k::lr_check(d_left, d_right, width, height, threshold, d_out, (cudaStream_t)stream);
 }
 
 } // extern "C"

@@ -8,6 +8,7 @@
 // (stereo/stereo.cu:1113-1170).
 #include <cmath>
 #include <string>
+#include <vector>
 
 #include "common.h"
 #include "kernels.h"
@@ -28,6 +29,9 @@ struct cnncrf_stereo {
     uint64_t seed = 0;
     int with_xy = 0;
     DevBuf img[2], padded[2], warped, warped_pad, vol, pw, out, labels, out_, out0, qf, p, q, vol3;
+    DevBuf gray[2], gtmp, gtmp2, gw, dlist; // census and edge weights
+    std::vector<float> dlist_host;          // host copy of the census disparity list
+    int filter_size = 7;                    // stereo/stereo_img.cpp:73
     cnncrf_net_t net = nullptr;
     cnncrf_slackprop_t solver = nullptr;
     double lb = 0.0;
@@ -59,6 +63,8 @@ struct cnncrf_stereo {
     }
     int build_net();
     int compute_volume(int lr);
+    int census(int lr);
+    int compute_weights(float alpha, float beta, float lambda, int lr);
 };
 
 static int log2i(int num) // stereo/stereo.cpp:56-62
@@ -100,10 +106,35 @@ int cnncrf_stereo::build_net()
     return CNNCRF_OK;
 }
 
+// calccostvolumecensus on the grey images, lambda 1 (stereo/stereo.cpp:264-268, 290-294)
+int cnncrf_stereo::census(int lr)
+{
+    const size_t n = (size_t)W * H;
+    for (int i = 0; i < 2; ++i) CNNCRF_TRY(k::rgb_to_gray(img[i].as<float>(), (long)n, gray[i].as<float>(), st));
+    dlist_host.resize((size_t)depth);
+    float d = lr ? dmin : -dmax; // disp += disp_step, as the census kernel steps
+    for (int z = 0; z < depth; ++z, d += dstep) dlist_host[z] = d;
+    CNNCRF_CUDA(cudaMemcpyAsync(dlist.get(), dlist_host.data(), sizeof(float) * depth, cudaMemcpyHostToDevice, st));
+    const int a = lr ? 0 : 1;
+    return k::census_volume(gray[a].as<float>(), gray[1 - a].as<float>(), W, H, filter_size, dlist.as<float>(), depth,
+                            1.0f, vol.as<float>(), st);
+}
+
+// computeWeights: calcEdgeImage of the reference side's grey image
+// (stereo/stereo.cpp:320-326) into wx, wy
+int cnncrf_stereo::compute_weights(float alpha, float beta, float lambda, int lr)
+{
+    const size_t n = (size_t)W * H;
+    CNNCRF_TRY(k::rgb_to_gray(img[lr ? 0 : 1].as<float>(), (long)n, gray[0].as<float>(), st));
+    return k::edge_weights(gray[0].as<float>(), W, H, alpha, beta, lambda, gtmp.as<float>(), gtmp2.as<float>(),
+                           gw.as<float>(), pw.as<float>(), pw.as<float>() + n, st);
+}
+
 int cnncrf_stereo::compute_volume(int lr)
 {
     if (!inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
     if (matching == CNNCRF_MATCH_LOAD) return CNNCRF_OK;
+    if (matching == CNNCRF_MATCH_CENSUS) return census(lr);
     if (!net) {
         int rc = build_net();
         if (rc != CNNCRF_OK) {
@@ -193,6 +224,16 @@ int cnncrf_stereo_initialize(cnncrf_stereo_t s, int width, int height, float dis
     CNNCRF_TRY(s->p.reserve(2 * n * sizeof(float)));
     CNNCRF_TRY(s->q.reserve(2 * n * sizeof(float)));
     CNNCRF_TRY(s->vol3.reserve(3 * n * sizeof(float)));
+    for (int i = 0; i < 2; ++i) CNNCRF_TRY(s->gray[i].reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->gtmp.reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->gtmp2.reserve(n * sizeof(float)));
+    CNNCRF_TRY(s->dlist.reserve(depth * sizeof(float)));
+    if (!s->gw.get()) { // the Gaussian of calcEdgeImage never changes
+        float w[2 * k::GAUSS_R + 1];
+        k::gauss_weights(k::GAUSS_SIGMA, k::GAUSS_R, w);
+        CNNCRF_TRY(s->gw.reserve(sizeof w));
+        CNNCRF_CUDA(cudaMemcpy(s->gw.get(), w, sizeof w, cudaMemcpyHostToDevice));
+    }
     CNNCRF_CUDA(cudaMemsetAsync(s->pw.get(), 0, 2 * n * sizeof(float), s->st));
     s->destroy_net();
     if (s->solver) {
@@ -284,17 +325,16 @@ int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C
                                             float alpha, float beta, float lambda_reg, int lr)
 {
     clear_error();
-    (void)alpha, (void)beta;
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->inited) return fail(CNNCRF_ESTATE, "computeSlackPropagation before initialize");
-    if (!s->pairwise() && s->matching != CNNCRF_MATCH_LOAD)
-        return fail(CNNCRF_EUNSUPPORTED,
-                    "CRF with image-gradient edge weights (non-pairwise matching) is not built");
     CNNCRF_TRY(s->record(0));
     CNNCRF_TRY(s->compute_volume(lr));
     CNNCRF_TRY(s->record(1));
     size_t n = (size_t)s->W * s->H;
-    CNNCRF_TRY(k::scale(s->pw.as<float>(), (long)(2 * n), lambda_reg, s->st)); // stereo/stereo.cpp:136-137
+    if (s->pairwise()) // the pairwise CNN's weights, times lambda (stereo/stereo.cpp:136-137)
+        CNNCRF_TRY(k::scale(s->pw.as<float>(), (long)(2 * n), lambda_reg, s->st));
+    else // image-gradient edge weights (stereo/stereo.cpp:132-133)
+        CNNCRF_TRY(s->compute_weights(alpha, beta, lambda_reg, lr));
     if (!s->solver) {
         CNNCRF_TRY(cnncrf_slackprop_create(&s->solver));
         CNNCRF_TRY(cnncrf_slackprop_init(s->solver, s->vol.as<float>(), s->W, s->H, s->depth, s->labels.as<int32_t>()));
@@ -312,6 +352,32 @@ int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C
     if (lr) CNNCRF_TRY(k::remap(s->out.as<float>(), s->labels.as<int32_t>(), (long)n, s->dmin, s->dstep, s->st));
     else CNNCRF_TRY(k::remap(s->out.as<float>(), s->labels.as<int32_t>(), (long)n, -s->dmax, s->dstep, s->st));
     return s->record(2);
+}
+
+int cnncrf_stereo_set_filter_size(cnncrf_stereo_t s, int filter_size)
+{
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (filter_size < 1 || filter_size > 16) return fail(CNNCRF_EINVAL, "filter size %d outside 1..16", filter_size);
+    s->filter_size = filter_size;
+    return CNNCRF_OK;
+}
+
+int cnncrf_stereo_compute_weights(cnncrf_stereo_t s, float alpha, float beta, float lambda_reg, int lr)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->inited) return fail(CNNCRF_ESTATE, "computeWeights before initialize");
+    return s->compute_weights(alpha, beta, lambda_reg, lr);
+}
+
+int cnncrf_stereo_fuse_quad_fit_direct(cnncrf_stereo_t s)
+{
+    clear_error();
+    if (!s) return fail(CNNCRF_EINVAL, "null stereo");
+    if (!s->solver) return fail(CNNCRF_ESTATE, "fuseQuadFitDirect needs a computeSlackPropagation first");
+    float *c1 = nullptr;
+    CNNCRF_TRY(cnncrf_slackprop_get_c1(s->solver, &c1)); // solver->get_C1() (stereo/stereo.cpp:408)
+    return k::quadfit_direct(s->out.as<float>(), c1, (long)s->W * s->H, s->depth, s->dmin, s->dstep, s->st);
 }
 
 int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr)

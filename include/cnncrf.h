@@ -55,7 +55,7 @@ typedef enum cnncrf_matching {
     CNNCRF_MATCH_GRAYCNN_PAIRWISE = 3,
     CNNCRF_MATCH_COLORCNN_PAIRWISE = 4,  /* "COLORPAIR" on the command line */
     CNNCRF_MATCH_CONCATCNN_PAIRWISE = 5, /* EUNSUPPORTED */
-    CNNCRF_MATCH_CENSUS = 6,             /* EUNSUPPORTED (not on the CNN path) */
+    CNNCRF_MATCH_CENSUS = 6,             /* census cost + image-gradient edge weights */
     CNNCRF_MATCH_LOAD = 7                /* volume supplied by the caller */
 } cnncrf_matching;
 
@@ -252,6 +252,36 @@ int cnncrf_tv_iterate(float *d_u, float *d_u_, const float *d_u0, const float *d
                       float C, float huber_eps, float disp_step, int iterations,
                       cnncrf_stream_t stream);
 
+/* ---------------------------------------------------------------- census, edges, QuadDirect, LR */
+
+/* rgb_to_gray_kernel (stereo/stereo.cu:853-863): .2989 R + .5870 G + .1140 B. */
+int cnncrf_rgb_to_gray(const float *d_rgba, float *d_gray, int width, int height, cnncrf_stream_t stream);
+/* cost_vol_census_kernel (stereo/stereo.cu:306-346): H x W x depth volume;
+ * disparity z = disp_min + z*disp_step (float accumulation), the census window
+ * (2 filter_size + 1)^2 without its centre, value = lambda * mismatches /
+ * (4 filter_size^2).  Grey images are read clamp-addressed; at fractional
+ * disparities linearly interpolated in FP32.  Synchronises the stream. */
+int cnncrf_census_volume(const float *d_gray_ref, const float *d_gray_other, int width, int height,
+                         int filter_size, float disp_min, float disp_step, int depth, float lambda,
+                         float *d_volume, cnncrf_stream_t stream);
+/* calcEdgeImage (stereo/stereo.cu:1090-1095, 471-520): Gaussian (sigma 0.7,
+ * radius 3, clamp-to-edge) of the grey image, forward differences, then
+ * w = alpha > 0 ? max(lambda exp(-alpha |d|^beta), 1e-6) : lambda |d|.
+ * Synchronises the stream. */
+int cnncrf_edge_weights(const float *d_gray, int width, int height, float alpha, float beta, float lambda,
+                        float *d_wx, float *d_wy, cnncrf_stream_t stream);
+/* fuseQuadFitDirect (stereo/stereo.cu:913-942, 1172-1194): per pixel the
+ * parabola through the costs of labels z-1, z, z+1 of d_c1 (H x W x depth)
+ * around z = (int)((u - disp_min) / disp_step); u += (c0 - c2) / (2 h) /
+ * max(1e-3, (c0 + c2 - 2 c1) / h^2).  Pixels at z <= 0 or z >= depth - 1 are
+ * left unchanged. */
+int cnncrf_quad_fit_direct(float *d_u, const float *d_c1, int width, int height, int depth,
+                           float disp_min, float disp_step, cnncrf_stream_t stream);
+/* leftrightcheck_kernel (stereo/stereo.cu:803-817): out = d if |d - (-right(x - d))| <= th,
+ * else -1 (right read clamp-addressed, linear in x). */
+int cnncrf_left_right_check(const float *d_left, const float *d_right, int width, int height,
+                            float threshold, float *d_out, cnncrf_stream_t stream);
+
 /* ---------------------------------------------------------------- Stereo */
 
 typedef struct cnncrf_stereo *cnncrf_stereo_t;
@@ -294,11 +324,20 @@ int cnncrf_stereo_set_color_images_device(cnncrf_stereo_t s, const float *d_left
 /* Stereo::computeVolume(lr) (stereo/stereo.cpp:179-318) */
 int cnncrf_stereo_compute_volume(cnncrf_stereo_t s, int lr);
 /* Stereo::computeSlackPropagation(C1, C2, delta, iterations, alpha, beta,
- * lambda, lr) (stereo/stereo.cpp:129-162).  alpha/beta only matter for the
- * CENSUS edge weights, which are not built (they are ignored). */
+ * lambda, lr) (stereo/stereo.cpp:129-162).  Pairwise (COLORPAIR) matching
+ * uses the pairwise CNN's weights times lambda; every other matching the
+ * image-gradient edge weights of (alpha, beta, lambda). */
 int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C2, float delta,
                                             int iterations, float alpha, float beta,
                                             float lambda_reg, int lr);
+/* Stereo::setFilterSize (census window half-size, stereo/stereo_img.cpp:73, default 7). */
+int cnncrf_stereo_set_filter_size(cnncrf_stereo_t s, int filter_size);
+/* Stereo::computeWeights(alpha, beta, lambda, lr) (stereo/stereo.cpp:320-326):
+ * edge weights of the reference side's grey image into the wx / wy buffers. */
+int cnncrf_stereo_compute_weights(cnncrf_stereo_t s, float alpha, float beta, float lambda_reg, int lr);
+/* Stereo::fuseQuadFitDirect() (stereo/stereo.cpp:406-409): QuadDirect on the
+ * solver's get_C1() volume after computeSlackPropagation. */
+int cnncrf_stereo_fuse_quad_fit_direct(cnncrf_stereo_t s);
 /* Stereo::computeArgMax(lr) (stereo/stereo.cpp:164-177; arg_min_kernel stereo/stereo.cu:348-370) */
 int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr);
 /* Stereo::fuseTHuberQuadFit(lambda, C, iterations, warps) (stereo/stereo.cpp:388-404) */

@@ -179,4 +179,62 @@ CNNCRF_HD float cnncrf_tanhf(float x)
     return x < 0.0f ? -t : t;
 }
 
+/* log(x) for finite x > 0 (0 -> -inf, x < 0 -> NaN).  Method (published,
+ * e.g. Muller, "Elementary Functions", ch. 6): x = 2^e * m with m in
+ * [sqrt(1/2), sqrt(2)), s = (m - 1) / (m + 1), log(m) = 2 atanh(s) =
+ * 2 (s + s^3/3 + s^5/5 + ... + s^11/11) with |s| <= 0.1716 (truncation
+ * below 1e-11 relative), log(x) = e ln2 + log(m) with ln2 split hi / lo as
+ * above.  The coefficients are 1/(2k+1) rounded to the nearest float. */
+CNNCRF_HD float cnncrf_logf(float x)
+{
+    if (!(x > 0.0f)) return x == 0.0f ? -1.0f / 0.0f : 0.0f / 0.0f;
+    if (x == 1.0f / 0.0f) return x;
+    int32_t bits;
+#if defined(__CUDA_ARCH__)
+    bits = __float_as_int(x);
+#else
+    memcpy(&bits, &x, sizeof bits);
+#endif
+    int e = 0;
+    if (((bits >> 23) & 0xff) == 0) { /* subnormal: scale by 2^23 (exact) */
+        x = cnncrf_mul(x, 8388608.0f);
+#if defined(__CUDA_ARCH__)
+        bits = __float_as_int(x);
+#else
+        memcpy(&bits, &x, sizeof bits);
+#endif
+        e = -23;
+    }
+    e += ((bits >> 23) & 0xff) - 127;
+    int32_t mb = (bits & 0x7fffff) | 0x3f800000; /* m in [1, 2) */
+    float m;
+#if defined(__CUDA_ARCH__)
+    m = __int_as_float(mb);
+#else
+    memcpy(&m, &mb, sizeof m);
+#endif
+    if (m > 1.41421356f) { /* m in [sqrt(1/2), sqrt(2)) */
+        m = cnncrf_mul(m, 0.5f);
+        e += 1;
+    }
+    const float s = cnncrf_div(cnncrf_add(m, -1.0f), cnncrf_add(m, 1.0f));
+    const float s2 = cnncrf_mul(s, s);
+    float p = 0.09090909090909091f;          /* 1/11 */
+    p = cnncrf_fma(p, s2, 0.1111111111111111f); /* 1/9 */
+    p = cnncrf_fma(p, s2, 0.14285714285714285f); /* 1/7 */
+    p = cnncrf_fma(p, s2, 0.2f);                /* 1/5 */
+    p = cnncrf_fma(p, s2, 0.3333333432674408f);  /* 1/3 */
+    const float s2x = cnncrf_add(s, s);
+    const float lm = cnncrf_fma(s2x, cnncrf_mul(s2, p), s2x); /* 2s + 2s * s^2 p */
+    const float ef = (float)e;
+    return cnncrf_fma(ef, CNNCRF_LN2_HI, cnncrf_fma(ef, CNNCRF_LN2_LO, lm));
+}
+
+/* x^y for x >= 0 as exp(y log x); 0^y = 0 for y > 0, 1 for y == 0. */
+CNNCRF_HD float cnncrf_powf(float x, float y)
+{
+    if (x == 0.0f) return y > 0.0f ? 0.0f : (y == 0.0f ? 1.0f : 1.0f / 0.0f);
+    return cnncrf_expf(cnncrf_mul(y, cnncrf_logf(x)));
+}
+
 #endif /* CNNCRF_FMATH_H */

@@ -907,4 +907,132 @@ int oracle_run_pair(const oracle_cfg *cfg, const float *const *params, const flo
     return 0;
 }
 
+// ---------------------------------------------------------------- census, edges, QuadDirect, LR check
+// (the reference reads these images through CUDA textures: clamp-addressed
+// reads at integer positions, FP32 linear interpolation at fractional ones)
+
+static inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+static inline float lerp_row(const float *r, int W, float u)
+{
+    const float t = u - 0.5f;
+    const float f = std::floor(t);
+    const int i = (int)f;
+    const float a = t - f;
+    const float v0 = r[clampi(i, 0, W - 1)];
+    if (a == 0.0f) return v0;
+    const float v1 = r[clampi(i + 1, 0, W - 1)];
+    return v0 + a * (v1 - v0);
+}
+
+// rgb_to_gray_kernel (stereo/stereo.cu:853-863), weights in double, rounded once
+void oracle_gray(const float *rgba, long n, float *gray)
+{
+    for (long i = 0; i < n; ++i) {
+        const float *px = rgba + 4 * i;
+        gray[i] = (float)(0.2989 * (double)px[0] + 0.5870 * (double)px[1] + 0.1140 * (double)px[2]);
+    }
+}
+
+// cost_vol_census_kernel (stereo/stereo.cu:306-346)
+void oracle_census(const float *g1, const float *g2, int W, int H, int fs, const float *list, int D, float lambda,
+                   float *vol)
+{
+    const float norm = (float)(fs * fs * 4);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float c1 = g1[(long)y * W + x];
+            const float xx = (float)x + 0.5f;
+            for (int z = 0; z < D; ++z) {
+                const float d = list[z];
+                const float c2 = lerp_row(g2 + (long)y * W, W, xx - d);
+                float cnt = 0.0f;
+                for (int dy = -fs; dy <= fs; ++dy) {
+                    const int yy = clampi(y + dy, 0, H - 1);
+                    const float *r1 = g1 + (long)yy * W, *r2 = g2 + (long)yy * W;
+                    for (int dx = -fs; dx <= fs; ++dx) {
+                        if (dx == 0 && dy == 0) continue;
+                        const float i1 = r1[clampi(x + dx, 0, W - 1)];
+                        const float i2 = lerp_row(r2, W, ((float)(x + dx) + 0.5f) - d);
+                        if ((c1 > i1) != (c2 > i2)) cnt += 1.0f;
+                    }
+                }
+                vol[((long)y * W + x) * D + z] = lambda * (cnt / norm);
+            }
+        }
+}
+
+// Gaussian weights exp(-i^2 / (2 sigma^2)) / sum, double, rounded once
+void oracle_gauss_weights(float sigma, int R, float *w)
+{
+    double s = 0.0, v[64];
+    for (int i = -R; i <= R; ++i) s += (v[i + R] = std::exp(-(double)(i * i) / (2.0 * sigma * sigma)));
+    for (int i = 0; i <= 2 * R; ++i) w[i] = (float)(v[i] / s);
+}
+
+static inline float edge_weight(float diff, float alpha, float beta, float lambda)
+{
+    if (alpha > 0.0f)
+        return std::max(cnncrf_mul(lambda, cnncrf_expf(cnncrf_mul(-alpha, cnncrf_powf(diff, beta)))), 1.0e-6f);
+    return lambda * diff;
+}
+
+// calcEdgeImage (stereo/stereo.cu:1090-1095): Gaussian sigma 0.7 (radius 3,
+// clamp-to-edge, horizontal then vertical), forward differences (the last
+// column / row differs from itself: 0), edge weight of each difference
+void oracle_edge_weights(const float *gray, int W, int H, float alpha, float beta, float lambda, float *wx,
+                         float *wy)
+{
+    const int R = 3;
+    float w[2 * R + 1];
+    oracle_gauss_weights(0.7f, R, w);
+    const long n = (long)W * H;
+    std::vector<float> t1((size_t)n), t2((size_t)n);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            float s = 0.0f;
+            for (int i = -R; i <= R; ++i) s = fmaf(w[i + R], gray[(long)y * W + clampi(x + i, 0, W - 1)], s);
+            t1[(long)y * W + x] = s;
+        }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            float s = 0.0f;
+            for (int i = -R; i <= R; ++i) s = fmaf(w[i + R], t1[(long)clampi(y + i, 0, H - 1) * W + x], s);
+            t2[(long)y * W + x] = s;
+        }
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const long i = (long)y * W + x;
+            const float c = t2[i];
+            wx[i] = edge_weight(std::fabs(t2[(long)y * W + std::min(x + 1, W - 1)] - c), alpha, beta, lambda);
+            wy[i] = edge_weight(std::fabs(t2[(long)std::min(y + 1, H - 1) * W + x] - c), alpha, beta, lambda);
+        }
+}
+
+// do_fitting_kernel_volume + do_argmin_kernel_volume (stereo/stereo.cu:913-942)
+void oracle_quadfit_direct(float *u, const float *c1, long npx, int D, float dmin, float dstep)
+{
+    for (long i = 0; i < npx; ++i) {
+        const int z = (int)((u[i] - dmin) / dstep);
+        if (z <= 0 || z >= D - 1) continue;
+        const float *c = c1 + i * D;
+        const float a = (c[z - 1] - c[z + 1]) / (dstep * 2.0f);
+        const float b = std::max(1.0e-3f, ((c[z - 1] + c[z + 1]) - 2.0f * c[z]) / (dstep * dstep));
+        u[i] = u[i] + a / b;
+    }
+}
+
+// leftrightcheck_kernel (stereo/stereo.cu:803-817)
+void oracle_lr_check(const float *left, const float *right, int W, int H, float th, float *out)
+{
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const long i = (long)y * W + x;
+            const float d = left[i];
+            const float dr = -lerp_row(right + (long)y * W, W, ((float)x + 0.5f) - d);
+            out[i] = std::fabs(d - dr) <= th ? d : -1.0f;
+        }
+}
+
 } // extern "C"

@@ -105,6 +105,16 @@ double oracle_chain_bruteforce(const float *cost, const float *w, int n, int D, 
 
 /* remap label -> disparity (stereo/stereo.cu:848) */
 void oracle_remap(const int32_t *labels, long n, float dmin, float dstep, float *out);
+/* grey image, census volume, edge weights, QuadDirect, left-right check
+ * (stereo/stereo.cu:853-863, 306-346, 1090-1095, 913-942, 803-817) */
+void oracle_gray(const float *rgba, long n, float *gray);
+void oracle_census(const float *g1, const float *g2, int W, int H, int fs, const float *list, int D,
+                   float lambda, float *vol);
+void oracle_gauss_weights(float sigma, int R, float *w);
+void oracle_edge_weights(const float *gray, int W, int H, float alpha, float beta, float lambda, float *wx,
+                         float *wy);
+void oracle_quadfit_direct(float *u, const float *c1, long npx, int D, float dmin, float dstep);
+void oracle_lr_check(const float *left, const float *right, int W, int H, float th, float *out);
 /* WTA (stereo/stereo.cu:348-370) */
 void oracle_argmin(const float *vol, long npx, int D, float dmin, float dstep, float *out);
 /* nearest warp (stereo/stereo.cu:830-839) */

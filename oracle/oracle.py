@@ -88,6 +88,16 @@ def lib():
         L.oracle_remap.restype = None
         L.oracle_argmin.argtypes = [f32p, C.c_long, C.c_int, C.c_float, C.c_float, f32p]
         L.oracle_argmin.restype = None
+        L.oracle_gray.argtypes = [f32p, C.c_long, f32p]
+        L.oracle_gray.restype = None
+        L.oracle_census.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_int, f32p, C.c_int, C.c_float, f32p]
+        L.oracle_census.restype = None
+        L.oracle_edge_weights.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, f32p, f32p]
+        L.oracle_edge_weights.restype = None
+        L.oracle_quadfit_direct.argtypes = [f32p, f32p, C.c_long, C.c_int, C.c_float, C.c_float]
+        L.oracle_quadfit_direct.restype = None
+        L.oracle_lr_check.argtypes = [f32p, f32p, C.c_int, C.c_int, C.c_float, f32p]
+        L.oracle_lr_check.restype = None
         L.oracle_warp.argtypes = [f32p, f32p, C.c_int, C.c_int, f32p]
         L.oracle_warp.restype = None
         L.oracle_tv_fit.argtypes = [f32p, C.c_int, C.c_int, C.c_float, C.c_float, f32p]
@@ -260,6 +270,57 @@ def argmin(vol, dmin, dstep):
     vol = np.ascontiguousarray(vol, np.float32)
     out = np.empty(vol.shape[:-1], np.float32)
     lib().oracle_argmin(vol.reshape(-1), out.size, vol.shape[-1], dmin, dstep, out.reshape(-1))
+    return out
+
+
+def gray(rgba):
+    rgba = np.ascontiguousarray(rgba, np.float32)
+    out = np.empty(rgba.shape[:-1], np.float32)
+    lib().oracle_gray(rgba.reshape(-1), out.size, out.reshape(-1))
+    return out
+
+
+def census(g1, g2, fs, disparities, lam=1.0):
+    """H x W x D census volume; disparities[z] = the z-th (positive) disparity."""
+    g1 = np.ascontiguousarray(g1, np.float32)
+    H, W = g1.shape
+    d = np.ascontiguousarray(disparities, np.float32)
+    out = np.empty((H, W, len(d)), np.float32)
+    lib().oracle_census(g1.reshape(-1), np.ascontiguousarray(g2, np.float32).reshape(-1), W, H, fs, d, len(d), lam,
+                        out.reshape(-1))
+    return out
+
+
+def census_list(dmin, dstep, depth):
+    """The census kernel's float loop: d = dmin; d += dstep."""
+    out, d = [], np.float32(dmin)
+    for _ in range(depth):
+        out.append(d)
+        d = np.float32(d + np.float32(dstep))
+    return np.array(out, np.float32)
+
+
+def edge_weights(g, alpha, beta, lam):
+    g = np.ascontiguousarray(g, np.float32)
+    H, W = g.shape
+    wx, wy = np.empty_like(g), np.empty_like(g)
+    lib().oracle_edge_weights(g.reshape(-1), W, H, alpha, beta, lam, wx.reshape(-1), wy.reshape(-1))
+    return wx, wy
+
+
+def quadfit_direct(u, c1, dmin, dstep):
+    u = np.array(u, np.float32, copy=True)
+    c1 = np.ascontiguousarray(c1, np.float32)
+    lib().oracle_quadfit_direct(u.reshape(-1), c1.reshape(-1), u.size, c1.shape[-1], dmin, dstep)
+    return u
+
+
+def lr_check(left, right, th):
+    left = np.ascontiguousarray(left, np.float32)
+    H, W = left.shape
+    out = np.empty_like(left)
+    lib().oracle_lr_check(left.reshape(-1), np.ascontiguousarray(right, np.float32).reshape(-1), W, H, th,
+                          out.reshape(-1))
     return out
 
 

@@ -223,7 +223,7 @@ def test_stereo_argmax_and_errors(cuda, oracle):
     s = scenes.voronoi_scene(W, H, 8, seed=9, cells=3, off_range=(1, 6), slope=0.0)
     st = Stereo()
     st.initialize(W, H, 0.0, 1.0, 7.0)
-    st.set_matching_function(L.MATCH_CENSUS)
+    st.set_matching_function(L.MATCH_CONCATCNN)  # not compiled in the reference either
     st.set_color_images(s["left"], s["right"])
     with pytest.raises(CnnCrfError) as e:
         st.compute_argmax()
