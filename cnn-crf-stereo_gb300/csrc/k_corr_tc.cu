@@ -14,6 +14,14 @@
 // omax - omin <= 128.  Right pixels outside [0, W) arrive as zeros through
 // TMA's out-of-bounds fill: exactly the reference's 0 for w - d < 0.
 //
+// Wider lists (D = 192 at 1440 x 960, up to D = 516) are cut into up to four
+// contiguous parts whose bands are each <= 128 wide; a tile is then (pixel
+// block, part), the part's band origin moves the right-feature box, and the
+// epilogue writes the part's slice of every pixel's D costs.  The parts of
+// one pixel block are consecutive tiles, so the second read of its left
+// features comes from L2.  The channel softmax needs all D taps of a pixel in
+// one warp and so takes single-part lists only; 1 - <fL,fR> takes any.
+//
 // Persistent, warp-specialised CTA (192 threads, one per SM):
 //   warp 0      TMA: per 64-channel block, a 4-D box (64 ch x 128 px) of the
 //               left features and one (64 ch x 256 px) of the right
@@ -28,7 +36,9 @@
 //               coalesced 128-byte writes
 // Every mbarrier wait is bounded; on timeout the role raises the CTA abort
 // flag and the global error flag, drains what it issued and TMEM is freed.
+#include <algorithm>
 #include <cfloat>
+#include <cmath>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -52,12 +62,14 @@ constexpr int NUM_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int SROW = 161;                  // staged row stride in floats (odd: no bank conflicts)
 constexpr int SCOLS = 160;                 // columns staged per warp: 32 + max band spread
-constexpr int MAXP = 8;                    // D <= 256
+constexpr int MAXP = 8;                    // taps per lane: <= 256 disparities per part
+constexpr int MAXPARTS = 4;                // disparity parts of a wide list
 constexpr int STG_BYTES = 4 * 32 * SROW * 4;
 constexpr uint32_t IDESC = tc::idesc_bf16(BM, BN);
 
 struct CorrTcParams {
-    int H, W, npairs, D, omin, nkb, kk_last, nchunks, tiles_x, num_tiles, unary, stages;
+    int H, W, npairs, D, nkb, kk_last, tiles_x, num_tiles, unary, stages, nparts;
+    int pk0[MAXPARTS], pD[MAXPARTS], pomin[MAXPARTS], pnch[MAXPARTS]; // per part: first k, count, band origin, chunks
     const float *list;
     float *out;
     int *err;
@@ -97,7 +109,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tc::prefetch_tmap(&tmL);
         tc::prefetch_tmap(&tmR);
     }
-    for (int i = threadIdx.x; i < p.D; i += NUM_THREADS) coff[i] = (int)p.list[i] - p.omin;
+    for (int pp = 0; pp < p.nparts; ++pp) // band column of disparity k within its part's tile
+        for (int i = threadIdx.x; i < p.pD[pp]; i += NUM_THREADS)
+            coff[p.pk0[pp] + i] = (int)p.list[p.pk0[pp] + i] - p.pomin[pp];
     if (warp == 1) {
         tc::tmem_alloc(tmem_slot, TMEM_COLS);
         tc::tmem_relinquish();
@@ -114,7 +128,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             uint32_t phase = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
-                const int pair = t / tiles_per_pair, r = t - pair * tiles_per_pair;
+                const int part = t % p.nparts, tt = t / p.nparts;
+                const int pair = tt / tiles_per_pair, r = tt - pair * tiles_per_pair;
                 const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * BM;
                 for (int kb = 0; kb < p.nkb; ++kb) {
                     if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
@@ -124,7 +139,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     uint8_t *sa = smem + stage * STAGE;
                     tc::mbar_expect_tx(&full[stage], STAGE);
                     tc::tma_load_4d(sa, &tmL, &full[stage], kb * 64, x0, y, pair);
-                    tc::tma_load_4d(sa + A_BYTES, &tmR, &full[stage], kb * 64, x0 + p.omin, y, p.npairs + pair);
+                    tc::tma_load_4d(sa + A_BYTES, &tmR, &full[stage], kb * 64, x0 + p.pomin[part], y,
+                                    p.npairs + pair);
                     ++issued;
                     if (++stage == S) {
                         stage = 0;
@@ -191,15 +207,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else {
         const int q = warp & 3; // the TMEM lane quarter this warp may read
         float *sw = stg + q * 32 * SROW;
-        const int P = (p.D + 31) >> 5;
-        int off[MAXP];
-#pragma unroll
-        for (int r = 0; r < MAXP; ++r) {
-            const int kk = lane + 32 * r;
-            off[r] = (r < P && kk < p.D) ? coff[kk] : 0;
-        }
         int lt = 0;
         for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
+            const int part = t % p.nparts, tt = t / p.nparts;
+            const int Dp = p.pD[part], k0 = p.pk0[part];
+            const int P = (Dp + 31) >> 5;
+            int off[MAXP];
+#pragma unroll
+            for (int r = 0; r < MAXP; ++r) {
+                const int kk = lane + 32 * r;
+                off[r] = (r < P && kk < Dp) ? coff[k0 + kk] : 0;
+            }
             const int buf = lt & 1;
             const uint32_t use = (uint32_t)lt >> 1;
             int ok = 1;
@@ -215,7 +233,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * BN + q * 32;
             float v[32];
 #pragma unroll 1
-            for (int c = 0; c < p.nchunks; ++c) {
+            for (int c = 0; c < p.pnch[part]; ++c) {
                 tc::tmem_ld32(ta + c * 32, v); // warp-collective: every lane runs it
 #pragma unroll
                 for (int j = 0; j < 32; ++j) sw[lane * SROW + c * 32 + j] = v[j];
@@ -224,29 +242,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::mbar_arrive(&tempty[buf]);
             __syncwarp();
 
-            const int pair = t / tiles_per_pair, r = t - pair * tiles_per_pair;
+            const int pair = tt / tiles_per_pair, r = tt - pair * tiles_per_pair;
             const int y = r / p.tiles_x, xq = (r - y * p.tiles_x) * BM + q * 32;
             const int npx = min(32, p.W - xq);
-            float *obase = p.out + (((size_t)pair * p.H + y) * p.W + xq) * p.D;
+            float *obase = p.out + (((size_t)pair * p.H + y) * p.W + xq) * p.D + k0;
 #pragma unroll 1
             for (int i = 0; i < npx; ++i) {
                 const float *row = sw + i * SROW + i;
                 float cv[MAXP];
 #pragma unroll
-                for (int rr = 0; rr < MAXP; ++rr) cv[rr] = (rr < P && lane + 32 * rr < p.D) ? row[off[rr]] : 0.0f;
+                for (int rr = 0; rr < MAXP; ++rr) cv[rr] = (rr < P && lane + 32 * rr < Dp) ? row[off[rr]] : 0.0f;
                 float *o = obase + (size_t)i * p.D;
                 if (p.unary == 0) {
                     float m = -FLT_MAX;
 #pragma unroll
                     for (int rr = 0; rr < MAXP; ++rr)
-                        if (rr < P && lane + 32 * rr < p.D) m = fmaxf(m, cv[rr]);
+                        if (rr < P && lane + 32 * rr < Dp) m = fmaxf(m, cv[rr]);
 #pragma unroll
                     for (int s = 16; s >= 1; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
                     float sum = 0.0f;
 #pragma unroll
                     for (int rr = 0; rr < MAXP; ++rr) {
                         if (rr < P) {
-                            const float e = lane + 32 * rr < p.D ? cnncrf_expf(cv[rr] - m) : 0.0f;
+                            const float e = lane + 32 * rr < Dp ? cnncrf_expf(cv[rr] - m) : 0.0f;
                             cv[rr] = e;
                             sum = (rr == 0) ? e : sum + e;
                         }
@@ -256,13 +274,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
                     for (int rr = 0; rr < MAXP; ++rr) {
                         const int kk = lane + 32 * rr;
-                        if (rr < P && kk < p.D) o[kk] = -(cv[rr] / sum);
+                        if (rr < P && kk < Dp) o[kk] = -(cv[rr] / sum);
                     }
                 } else {
 #pragma unroll
                     for (int rr = 0; rr < MAXP; ++rr) {
                         const int kk = lane + 32 * rr;
-                        if (rr < P && kk < p.D) o[kk] = p.unary == 1 ? 1.0f - cv[rr] : cv[rr];
+                        if (rr < P && kk < Dp) o[kk] = p.unary == 1 ? 1.0f - cv[rr] : cv[rr];
                     }
                 }
             }
@@ -281,19 +299,56 @@ size_t smem_bytes(int stages, int D)
     return 1024 + (size_t)stages * STAGE + STG_BYTES + (2 * (size_t)stages + 5) * 8 + 16 + (size_t)D * 4;
 }
 
-} // namespace
+struct CorrTcPlan {
+    int nparts = 0;
+    int k0[MAXPARTS], D[MAXPARTS], omin[MAXPARTS], omax[MAXPARTS];
+};
 
-bool corr_tc_supported(int C, int cp, int D, int omin, int omax)
+// The fewest near-equal contiguous parts of the stored list whose bands each
+// fit a tile (band spread <= BN - BM); false if the list has a fractional
+// entry, needs more than MAXPARTS parts, or needs several under the softmax.
+bool corr_tc_plan(const float *h_list, int D, int unary, CorrTcPlan &pl)
 {
-    return cp % 64 == 0 && C >= 1 && C <= cp && D >= 1 && D <= 32 * MAXP && omax >= omin &&
-           omax - omin <= BN - BM && 32 + (omax - omin) <= SCOLS;
+    if (!h_list || D < 1 || D > MAXPARTS * (BN - BM + 1)) return false;
+    for (int i = 0; i < D; ++i)
+        if (h_list[i] != std::floor(h_list[i]) || std::fabs(h_list[i]) > (float)(1 << 20)) return false;
+    for (int np = 1; np <= MAXPARTS && (np == 1 || unary != 0); ++np) {
+        if (np > D) break;
+        bool ok = D / np + 1 <= 32 * MAXP; // a part's taps fit the epilogue's registers
+        int k0 = 0;
+        for (int pp = 0; pp < np && ok; ++pp) {
+            const int n = D / np + (pp < D % np ? 1 : 0);
+            int lo = 1 << 30, hi = -(1 << 30);
+            for (int i = k0; i < k0 + n; ++i) {
+                lo = std::min(lo, (int)h_list[i]);
+                hi = std::max(hi, (int)h_list[i]);
+            }
+            ok = hi - lo <= BN - BM && 32 + (hi - lo) <= SCOLS;
+            pl.k0[pp] = k0, pl.D[pp] = n, pl.omin[pp] = lo, pl.omax[pp] = hi;
+            k0 += n;
+        }
+        if (ok) {
+            pl.nparts = np;
+            return true;
+        }
+    }
+    return false;
 }
 
-int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list, int D, int omin,
-                   int omax, int unary, float *out, int *err, cudaStream_t st)
+} // namespace
+
+bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary)
 {
-    if (!corr_tc_supported(C, cp, D, omin, omax))
-        return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: C=%d cp=%d D=%d band [%d,%d]", C, cp, D, omin, omax);
+    CorrTcPlan pl;
+    return cp % 64 == 0 && C >= 1 && C <= cp && corr_tc_plan(h_list, D, unary, pl);
+}
+
+int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list,
+                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st)
+{
+    CorrTcPlan pl;
+    if (!(cp % 64 == 0 && C >= 1 && C <= cp) || !corr_tc_plan(h_list, D, unary, pl))
+        return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: C=%d cp=%d D=%d unary %d", C, cp, D, unary);
     if (npairs < 1 || H < 1 || W < 1) return fail(CNNCRF_EINVAL, "correlation_tc: bad size");
     if (((uintptr_t)feat & 15) || !out || !err || !d_list) return fail(CNNCRF_EINVAL, "correlation_tc: bad pointer");
     auto enc = tc::tensor_map_encoder();
@@ -313,12 +368,16 @@ int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, co
     if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "correlation_tc: right tensor map (%d)", (int)r);
 
     CorrTcParams p{};
-    p.H = H, p.W = W, p.npairs = npairs, p.D = D, p.omin = omin;
+    p.H = H, p.W = W, p.npairs = npairs, p.D = D;
     p.nkb = ceil_div(C, 64);
     p.kk_last = ceil_div(C - 64 * (p.nkb - 1), 16);
-    p.nchunks = ceil_div(32 + (omax - omin), 32);
+    p.nparts = pl.nparts;
+    for (int pp = 0; pp < pl.nparts; ++pp) {
+        p.pk0[pp] = pl.k0[pp], p.pD[pp] = pl.D[pp], p.pomin[pp] = pl.omin[pp];
+        p.pnch[pp] = ceil_div(32 + (pl.omax[pp] - pl.omin[pp]), 32);
+    }
     p.tiles_x = ceil_div(W, BM);
-    p.num_tiles = npairs * H * p.tiles_x;
+    p.num_tiles = npairs * H * p.tiles_x * pl.nparts;
     p.unary = unary;
     p.list = d_list, p.out = out, p.err = err;
 

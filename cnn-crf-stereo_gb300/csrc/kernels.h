@@ -73,12 +73,13 @@ int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs
                      int npairs = 1, long fps = 0);
 
 // same on the tensor cores: BF16 features [2 * npairs][H][W][cp] (left
-// images, then right), integer disparity list whose band omax - omin <= 128;
-// corr_tc_supported says whether a shape qualifies.  err: the bounded-wait
-// error flag.
-bool corr_tc_supported(int C, int cp, int D, int omin, int omax);
-int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list, int D,
-                   int omin, int omax, int unary, float *out, int *err, cudaStream_t st);
+// images, then right), an integer disparity list (h_list on the host, d_list
+// its device copy) cut into at most 4 parts whose bands are <= 128 wide (one
+// part under the softmax unary); corr_tc_supported says whether a list
+// qualifies.  err: the bounded-wait error flag.
+bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary);
+int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list,
+                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st);
 
 // ------------------------------------------------------------ census, edge weights, QuadDirect, LR check
 constexpr int GAUSS_R = 3;           // Gaussian of the edge image: radius 3 >= 3 sigma

@@ -99,9 +99,9 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
     const size_t fimg = (size_t)H * W * cp;
     feat16 = f;
     const bool ip = interp || force_interp;
-    if (!ip && int_list && k::corr_tc_supported(F, cp, D, omin, omax))
-        CNNCRF_TRY(k::correlation_tc(f, n, H, W, F, cp, d_list.as<float>(), D, omin, omax, d.unary, vol, err.as<int>(),
-                                     st));
+    if (!ip && int_list && k::corr_tc_supported(F, cp, list.data(), D, d.unary))
+        CNNCRF_TRY(k::correlation_tc(f, n, H, W, F, cp, d_list.as<float>(), list.data(), D, d.unary, vol,
+                                     err.as<int>(), st));
     else
         CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)n * fimg, H, W, F, cp, d_list.as<float>(), D, omin, omax, ip,
                                        d.unary, vol, st, n, (long)fimg));
