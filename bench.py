@@ -257,6 +257,169 @@ def make_batch(cnncrf, wl, B, precision, graph, stream, seed0, group_size=0):
     return b, sc
 
 
+def run_uneven(args):
+    """The uneven batch: --per-shape pairs of each of 480x320/D64, 720x480/D96,
+    1242x375/D128 and 1440x960/D192 (32 by default) through one StereoBatch,
+    replayed as one CUDA graph per step; pairs/s of the whole batch, the CRF's
+    HBM GB/s and the tensor-core convolutions' TFLOP/s."""
+    import numpy as np
+    import torch
+    import cnncrf
+    from cnncrf import scenes, _lib
+    from cnncrf.api import StereoBatch
+
+    rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    wl = WORKLOAD
+    shapes, per = scenes.UNEVEN_SHAPES, args.per_shape
+    gs = args.group_size if args.group_size >= 0 else max(1, per // 2)
+    crf = (wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], wl["lam"])
+    stream = torch.cuda.Stream()
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device="cuda")  # 256 MiB > L2
+
+    def batch(scs, graph, group_size):
+        b = StereoBatch(precision=cnncrf.BF16, unary=cnncrf.UNARY_ONE_MINUS_DOT, topology=cnncrf.TOPO_ALL3X3,
+                        feat_channels=wl["feat"], pw_channels=wl["pw"], crf_shape=cnncrf.RHO_LINEAR,
+                        num_layers=wl["layers"], seed=wl["seed"], graph=graph, stream=stream,
+                        group_size=group_size)
+        for x in scs:
+            b.add_pair(x["W"], x["H"], 0.0, 1.0, float(x["D"] - 1))
+        return b
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        barrier(world)
+        torch.cuda.synchronize()
+        for a, e in evs:
+            flush.zero_()
+            a.record(stream)
+            fn()
+            e.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return allmax(sum(a.elapsed_time(e) for a, e in evs), world)
+
+    sc = scenes.uneven_scenes(per, seed0=1000 * rank)
+    B = len(sc)
+    with torch.cuda.stream(stream):
+        b = batch(sc, not args.no_graph, gs)
+        dl = [torch.from_numpy(x["left"]).cuda() for x in sc]
+        dr = [torch.from_numpy(x["right"]).cuda() for x in sc]
+        hl = [torch.from_numpy(x["left"]).pin_memory() for x in sc]
+        hr = [torch.from_numpy(x["right"]).pin_memory() for x in sc]
+        hout = [torch.empty((x["H"], x["W"]), dtype=torch.float32).pin_memory() for x in sc]
+
+        def step_device():
+            for i in range(B):
+                b.set_images(i, dl[i], dr[i])
+            b.run(*crf)
+
+        def step_e2e():
+            for i in range(B):
+                b.set_images(i, hl[i], hr[i])
+            b.run(*crf)
+            for i in range(B):
+                b.get_output(i, hout[i])
+
+        for i in range(B):
+            b.set_images(i, dl[i], dr[i])
+        tiles = b.autotune(*crf) if not args.no_autotune else []
+        for _ in range(max(args.warmup, 3)):
+            step_device()
+        step_e2e()
+        b.check()
+        torch.cuda.synchronize()
+        clocks = ClockSampler(local)
+        clocks.start()
+        l0 = _lib.kernel_launches()
+        t_ms = timed(step_device, args.steps)
+        launches = _lib.kernel_launches() - l0
+        clk = clocks.stop()
+        e_ms = timed(step_e2e, args.steps)
+        b.check()
+        bad = float(np.mean([scenes.bad_pixels(hout[i].numpy(), sc[i]["disp"]) for i in range(B)]))
+        del b
+        torch.cuda.synchronize()
+
+        # per-kernel device time, one shape at a time (one group, eager), so
+        # no kernel of another group overlaps the events around a launch
+        nprof = 2
+        prof, per_shape = {}, {}
+        for j, (W, H, D) in enumerate(shapes):
+            part = sc[j * per:(j + 1) * per]
+            bp = batch(part, False, 0)
+            for i in range(per):
+                bp.set_images(i, dl[j * per + i], dr[j * per + i])
+            if not args.no_autotune:
+                bp.autotune(*crf)
+            bp.run(*crf)
+            torch.cuda.synchronize()
+            _lib.profile_reset()
+            _lib.profile_enable(True)
+            p_ms = timed(lambda: bp.run(*crf), nprof)
+            _lib.profile_enable(False)
+            kp = {k: _lib.profile_query(k) for k in _lib.profile_kernels()}
+            _lib.profile_reset()
+            bp.check()
+            del bp
+            per_shape["%dx%d_d%d" % (W, H, D)] = {
+                "pairs": per, "ms_per_pair_eager": p_ms / nprof / per,
+                "kernels_ms_per_pair": {k: round(t / nprof / per, 4) for k, (n, t) in kp.items()}}
+            for k, (n, t) in kp.items():
+                a = prof.setdefault(k, [0, 0.0])
+                a[0] += n
+                a[1] += t
+    if not args.no_graph:
+        launches_per_step = sum(n for n, _ in prof.values()) / nprof
+    else:
+        launches_per_step = launches / args.steps
+    if rank != 0:
+        return 0
+    peaks, peak_src = measured_peaks()
+    tc_f = sum(conv_flops(W, H, wl["layers"], wl["feat"], 3, wl["pw"])[0] for (W, H, D) in shapes) * per
+    crf_b = sum(crf_bytes_per_pass(W, H, D) for (W, H, D) in shapes) * per * 2 * wl["crf_iters"]
+    roof = crf_roof = None
+    if "conv_tc" in prof:
+        ach = tc_f * nprof / (prof["conv_tc"][1] / 1000.0) / 1e12
+        roof = {"kernel": "conv_tc", "bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"],
+                "unit": "TFLOP/s", "frac": ach / peaks["bf16_tflops"], "traffic": None,
+                "peak_source": peak_src + " (bf16 dense burst)",
+                "per_launch": "FLOPs of the tensor-core layers of all pairs / their summed launch time"}
+    if "crf_h" in prof and "crf_v" in prof:
+        t = prof["crf_h"][1] + prof["crf_v"][1]
+        gbs = crf_b * nprof / (t / 1000.0) / 1e9
+        crf_roof = {"kernel": "crf_h+crf_v", "bound": "hbm", "achieved": gbs, "peak": peaks["hbm_gbs"],
+                    "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peak_src,
+                    "per_launch": "algorithmic 3 x N x D x 4 B per pass of all pairs / summed pass time"}
+    tot = sum(t for _, t in prof.values()) or 1.0
+    kernels = {k: {"launches": n, "total_ms": round(t, 4), "share": round(t / tot, 4)} for k, (n, t) in prof.items()}
+    value = replica_value(args.steps, B, world, t_ms)
+    line = {
+        "metric": "stereo pairs/s, uneven batch (480x320/D64, 720x480/D96, 1242x375/D128, 1440x960/D192)",
+        "value": value, "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16", "data": "synthetic (seeded Voronoi plane scenes, 30 cells, per pair seed)",
+        "config": {"workload": "uneven%d" % B, "shapes": ["%dx%d_d%d" % x for x in shapes], "pairs_per_shape": per,
+                   "pairs_per_group": gs, "graph": not args.no_graph, "crf_iters": wl["crf_iters"],
+                   "net": "7x3x3 conv 100ch + L2 norm, 1-dot unary, pairwise CNN 3x3-3x3-1x1",
+                   "crf": "truncated linear L1=0.5 T=3", "l2": "flushed (256 MiB write) between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": replica_value(args.steps, B, world, e_ms), "unit": "pairs/s",
+                "h2d_bytes_per_step": sum(2 * x["W"] * x["H"] * 16 for x in sc),
+                "d2h_bytes_per_step": sum(x["W"] * x["H"] * 4 for x in sc)},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "roofline": roof, "crf_roofline": crf_roof, "kernels": kernels, "per_shape": per_shape, "clocks": clk,
+        "crf_tiles": [dict(shape="%dx%d_d%d x%d" % (t["W"], t["H"], t["D"], t["npairs"]), **t["tile"])
+                      for t in tiles],
+        "cpu_baseline": None,
+        "disparity_stats": {"kitti_bad3px_5pct_mean": bad,
+                            "definition": "eval/compute_numbers_kitti.py computeError on PNG16-quantised maps, "
+                                          "mean over the batch, synthetic ground truth"},
+    }
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -270,6 +433,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="kitti", choices=["kitti", "uneven"],
+                    help="uneven: --per-shape pairs of each of four sizes / ranges in one batch")
+    ap.add_argument("--per-shape", type=int, default=8)
+    ap.add_argument("--no-autotune", action="store_true", help="run the default CRF tile (no tile tuning)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: only warm-up + `steps` device steps of the path (for ncu captures)")
     args = ap.parse_args()
@@ -277,6 +444,8 @@ def main():
         return run_reference(args)
     if args.mode == "profile":
         return run_profile(args)
+    if args.workload == "uneven":
+        return run_uneven(args)
 
     import numpy as np
     import torch
@@ -314,6 +483,9 @@ def main():
             for i in range(B):
                 b.get_output(i, hout[i])
 
+        for i in range(B):
+            b.set_images(i, dl[i], dr[i])
+        tiles = b.autotune(*crf) if not args.no_autotune else []
         for _ in range(max(args.warmup, 3)):
             step_device()
         step_e2e()
@@ -354,6 +526,8 @@ def main():
         bp, _ = make_batch(cnncrf, wl, B, precision, False, stream, seed0=1000 * rank)
         for i in range(B):
             bp.set_images(i, dl[i], dr[i])
+        if not args.no_autotune:
+            bp.autotune(*crf)
         bp.run(*crf)
         torch.cuda.synchronize()
         _lib.profile_reset()
@@ -377,6 +551,11 @@ def main():
             st32.set_color_images(dl[0], dr[0])
             st32.compute_slack_propagation(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], 0.0, 0.0, wl["lam"])
             torch.cuda.synchronize()
+            if not args.no_autotune:  # the single-pair shape both single-pair paths run
+                from cnncrf.api import crf_autotune
+                wx32, wy32 = st32.weights_device()
+                crf_autotune(st32.volume_device(), wx32, wy32, wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"],
+                             cnncrf.RHO_LINEAR, stream=stream)
             n32 = 3
 
             def step32():
@@ -450,6 +629,8 @@ def main():
                 "d2h_bytes_per_step": B * W * H * 4},
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "roofline": roof, "crf_roofline": crf_roof,
+        "crf_tiles": [dict(shape="%dx%d_d%d x%d" % (t["W"], t["H"], t["D"], t["npairs"]), **t["tile"])
+                      for t in tiles],
         "kernels": kernels, "kernel_profile_ms_per_step": p_ms / nprof, "clocks": clk,
         "cpu_baseline": cpu,
         "precision_check": cmp,

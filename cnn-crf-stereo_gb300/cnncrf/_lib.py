@@ -40,6 +40,11 @@ class CrfOptions(C.Structure):
                 ("shape", C.c_int), ("slack", C.c_float)]
 
 
+class CrfTile(C.Structure):
+    _fields_ = [("ring_h", C.c_int), ("chains_per_cta_h", C.c_int), ("ring_v", C.c_int),
+                ("chains_per_cta_v", C.c_int)]
+
+
 class StereoOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("unary", C.c_int), ("topology", C.c_int),
                 ("feat_channels", C.c_int), ("pw_channels", C.c_int),
@@ -75,6 +80,14 @@ PROTOS = {
                           C.c_size_t, vp], i32),
     "cnncrf_crf_solve_static": ([vp, vp, vp, i32, i32, i32, C.POINTER(CrfOptions), vp, C.POINTER(C.c_double),
                                  vp], i32),
+    "cnncrf_crf_tuning_set": ([i32, i32, i32, i32, i32, C.POINTER(CrfTile)], i32),
+    "cnncrf_crf_tuning_get": ([i32, i32, i32, i32, i32, C.POINTER(CrfTile), C.POINTER(i32), C.POINTER(f32),
+                               C.POINTER(f32)], i32),
+    "cnncrf_crf_tuning_clear": ([], i32),
+    "cnncrf_crf_tuning_count": ([C.POINTER(i32)], i32),
+    "cnncrf_crf_tuning_save": ([C.c_char_p], i32),
+    "cnncrf_crf_tuning_load": ([C.c_char_p], i32),
+    "cnncrf_crf_autotune": ([vp, vp, vp, i32, i32, i32, C.POINTER(CrfOptions), vp, C.c_size_t, vp], i32),
     "cnncrf_slackprop_create": ([C.POINTER(vp)], i32),
     "cnncrf_slackprop_destroy": ([vp], i32),
     "cnncrf_slackprop_set_stream": ([vp, vp], i32),
@@ -137,6 +150,9 @@ PROTOS = {
     "cnncrf_batch_get_volume_device": ([vp, i32, C.POINTER(vp), C.POINTER(i32)], i32),
     "cnncrf_batch_lower_bound": ([vp, i32, C.POINTER(C.c_double)], i32),
     "cnncrf_batch_check": ([vp], i32),
+    "cnncrf_batch_autotune": ([vp, f32, f32, f32, i32, f32], i32),
+    "cnncrf_batch_num_groups": ([vp, C.POINTER(i32)], i32),
+    "cnncrf_batch_group_shape": ([vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
     "cnncrf_kernel_launches": ([C.POINTER(C.c_uint64)], i32),
     "cnncrf_profile_enable": ([i32], i32),
     "cnncrf_profile_reset": ([], i32),

@@ -181,6 +181,20 @@ def crf_solve(cost, wx, wy, L1=1.0, L2=12.0, delta=2, total_it=4, shape=L.RHO_ST
     return labels, lb.value
 
 
+def crf_autotune(cost, wx, wy, L1=1.0, L2=12.0, delta=2, total_it=4, shape=L.RHO_STEP, slack=0.5, stream=None,
+                 workspace=None):
+    """Measure every CRF tile on this single-pair problem and enter the fastest
+    in the tile table (cnncrf.tuning); synchronises."""
+    H, W, D = cost.shape
+    opt = crf_options(L1, L2, delta, total_it, shape, slack)
+    nb = C.c_size_t()
+    call("cnncrf_crf_workspace_size", W, H, D, C.byref(nb))
+    if workspace is None:
+        workspace = torch.empty(nb.value, device="cuda", dtype=torch.uint8)
+    call("cnncrf_crf_autotune", _ptr(cost), _ptr(wx), _ptr(wy), W, H, D, C.byref(opt), _ptr(workspace), nb.value,
+         _stream_ptr(stream))
+
+
 class SlackProp:
     """slack_prop_2D_alg: init(C{K,W,H}, sols); ops[...]; update_W; execute; LB; get_C1."""
 
@@ -472,6 +486,22 @@ class StereoBatch:
 
     def run(self, L1, L2, delta, iterations, lambda_reg=1.0):
         call("cnncrf_batch_run", self._h, L1, L2, float(delta), iterations, lambda_reg)
+
+    def autotune(self, L1, L2, delta, iterations, lambda_reg=1.0):
+        """Run once, tune every group's CRF tile (see cnncrf.tuning); returns
+        one dict per group: shape, pairs, tile and the measured pass times."""
+        from . import tuning
+        call("cnncrf_batch_autotune", self._h, L1, L2, delta, iterations, lambda_reg)
+        n = C.c_int()
+        call("cnncrf_batch_num_groups", self._h, C.byref(n))
+        out = []
+        for g in range(n.value):
+            W, H, D, np_ = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+            call("cnncrf_batch_group_shape", self._h, g, C.byref(W), C.byref(H), C.byref(D), C.byref(np_))
+            tile, found, mh, mv = tuning.get_tile(W.value, H.value, D.value, np_.value, int(delta))
+            out.append(dict(W=W.value, H=H.value, D=D.value, npairs=np_.value, delta=int(delta), tile=tile,
+                            found=found, ms_h=mh, ms_v=mv))
+        return out
 
     def check(self):
         call("cnncrf_batch_check", self._h)

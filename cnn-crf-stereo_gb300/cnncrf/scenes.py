@@ -112,6 +112,20 @@ def workload(name, seed=0):
     raise KeyError(name)
 
 
+# the uneven batch: 8 pairs of each (W, H, D), each from the Middlebury-shaped
+# generator (30 planar cells, offsets in [4, 90] clipped to D - 1, slopes
+# +-0.2) with its own seed
+UNEVEN_SHAPES = [(480, 320, 64), (720, 480, 96), (1242, 375, 128), (1440, 960, 192)]
+
+
+def uneven_scenes(per_shape=8, seed0=0, shapes=None):
+    out = []
+    for j, (W, H, D) in enumerate(shapes or UNEVEN_SHAPES):
+        for i in range(per_shape):
+            out.append(voronoi_scene(W, H, D, seed0 + 100 * j + i, cells=30, off_range=(4, 90), slope=0.2))
+    return out
+
+
 def bad_pixels(disp, gt, thresh=3.0, rel=0.05):
     """KITTI error rate of a disparity map against a synthetic ground truth,
     both read as 16-bit PNGs would be (eval/compute_numbers_kitti.py:6-17)."""

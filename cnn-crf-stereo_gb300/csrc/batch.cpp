@@ -314,6 +314,41 @@ int cnncrf_batch_use_graph(cnncrf_batch_t b, int enable)
     return CNNCRF_OK;
 }
 
+int cnncrf_batch_autotune(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
+{
+    clear_error();
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    CNNCRF_TRY(cnncrf_batch_run(b, L1, L2, delta, iterations, lambda_reg)); // every group's volume and weights
+    CNNCRF_CUDA(cudaStreamSynchronize(b->st));
+    CNNCRF_TRY(cnncrf_batch_check(b));
+    k::CrfParams p;
+    p.L1 = L1, p.L2 = L2, p.delta = (int)delta, p.shape = b->o.crf_shape, p.slack = b->o.crf_slack;
+    for (auto &gp : b->groups) {
+        Group &g = *gp;
+        const long N = (long)g.W * g.H;
+        CNNCRF_TRY(k::crf_autotune(g.vol.as<float>(), g.pw.as<float>(), g.pw.as<float>() + N, 2 * N, g.W, g.H,
+                                   g.depth, (int)g.members.size(), p, g.ws.get(), g.ws_bytes, b->work));
+    }
+    b->invalidate(); // the captured launches carry the old tiles
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_num_groups(cnncrf_batch_t b, int *n)
+{
+    if (!b || !n) return fail(CNNCRF_EINVAL, "null argument");
+    *n = (int)b->groups.size();
+    return CNNCRF_OK;
+}
+
+int cnncrf_batch_group_shape(cnncrf_batch_t b, int group, int *width, int *height, int *depth, int *npairs)
+{
+    if (!b || !width || !height || !depth || !npairs) return fail(CNNCRF_EINVAL, "null argument");
+    if (group < 0 || group >= (int)b->groups.size()) return fail(CNNCRF_EINVAL, "group %d", group);
+    const Group &g = *b->groups[group];
+    *width = g.W, *height = g.H, *depth = g.depth, *npairs = (int)g.members.size();
+    return CNNCRF_OK;
+}
+
 int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
 {
     clear_error();

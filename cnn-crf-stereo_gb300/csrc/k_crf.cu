@@ -20,342 +20,26 @@
 // warp shuffles, the minimum over labels from an xor-shuffle butterfly.  All
 // operations are exact (min) or single IEEE ops in the oracle's order, so the
 // labels equal the oracle's bit for bit.  Compiled with --fmad=false.
-#include <cfloat>
-#include <math_constants.h>
+#include <algorithm>
+#include <vector>
 
-#include "common.h"
-#include "kernels.h"
+#include "k_crf_chain.cuh"
 
 namespace cnncrf {
 namespace k {
 
+int crf_pass_ring8(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStream_t st)
+{
+    return launch_pass_any<8>(a, hpass, delta, wpb, st);
+}
+
+size_t crf_pass_smem(int P, int RING, int W, int H, bool hpass, int wpb)
+{
+    const int n = hpass ? W : H;
+    return sizeof(float) * wpb * (size_t)(((n + 3) & ~3) + ring_floats(P, RING));
+}
+
 namespace {
-
-struct Rho {
-    float rho[9];
-    float L2;
-    float slack;
-};
-
-#define INF CUDART_INF_F
-
-// Order-preserving map of (non-NaN) floats to signed ints, and back: the
-// warp minimum is then one redux.sync.min.s32, exact like a float min.
-__device__ __forceinline__ int f2ord(float f)
-{
-    const int b = __float_as_int(f);
-    return b ^ ((b >> 31) & 0x7fffffff);
-}
-__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7fffffff)); }
-
-template <int P> __device__ __forceinline__ float warp_min(const float (&v)[P])
-{
-    float m = v[0];
-#pragma unroll
-    for (int r = 1; r < P; ++r) m = fminf(m, v[r]);
-    return ord2f(__reduce_min_sync(0xffffffffu, f2ord(m)));
-}
-
-template <int P> __device__ __forceinline__ void load_vec(const float *p, int lane, int D, float (&v)[P])
-{
-    const int k0 = lane * P;
-    if (D == 32 * P && (P == 1 || P == 2 || P == 4 || P == 8)) {
-        if constexpr (P == 1) {
-            v[0] = p[k0];
-        } else if constexpr (P == 2) {
-            float2 t = *(const float2 *)(p + k0);
-            v[0] = t.x, v[1] = t.y;
-        } else if constexpr (P == 4) {
-            float4 t = *(const float4 *)(p + k0);
-            v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
-        } else if constexpr (P == 8) {
-            float4 t = *(const float4 *)(p + k0), u = *(const float4 *)(p + k0 + 4);
-            v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w, v[4] = u.x, v[5] = u.y, v[6] = u.z, v[7] = u.w;
-        }
-        return;
-    }
-#pragma unroll
-    for (int r = 0; r < P; ++r) v[r] = (k0 + r < D) ? p[k0 + r] : 0.0f;
-}
-
-template <int P> __device__ __forceinline__ void store_vec(float *p, int lane, int D, const float (&v)[P])
-{
-    const int k0 = lane * P;
-    if (D == 32 * P && (P == 1 || P == 2 || P == 4 || P == 8)) {
-        if constexpr (P == 1) {
-            p[k0] = v[0];
-        } else if constexpr (P == 2) {
-            *(float2 *)(p + k0) = make_float2(v[0], v[1]);
-        } else if constexpr (P == 4) {
-            *(float4 *)(p + k0) = make_float4(v[0], v[1], v[2], v[3]);
-        } else if constexpr (P == 8) {
-            *(float4 *)(p + k0) = make_float4(v[0], v[1], v[2], v[3]);
-            *(float4 *)(p + k0 + 4) = make_float4(v[4], v[5], v[6], v[7]);
-        }
-        return;
-    }
-#pragma unroll
-    for (int r = 0; r < P; ++r)
-        if (k0 + r < D) p[k0 + r] = v[r];
-}
-
-// Exact two-lane IEEE add (add.rn.f32x2) and three-input minimum (min.f32
-// with three sources): the same values as two __fadd_rn and two fminf, in
-// fewer instructions.
-__device__ __forceinline__ void add2(float a0, float a1, float b, float &d0, float &d1)
-{
-    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
-        "mov.b64 ra, {%2, %3};\n\t"
-        "mov.b64 rb, {%4, %4};\n\t"
-        "add.rn.f32x2 rd, ra, rb;\n\t"
-        "mov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(d0), "=f"(d1)
-        : "f"(a0), "f"(a1), "f"(b));
-}
-__device__ __forceinline__ float min3(float a, float b, float c)
-{
-    float d;
-    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
-    return d;
-}
-
-// out = minconv(v) - g, pads (k >= D) kept at +inf.  FULL: D == 32 * P (no
-// pad labels, only the chain ends of lanes 0 and 31 are masked).
-template <int P, int DELTA, bool FULL>
-__device__ __forceinline__ void minconv(const float (&v)[P], float g, float w, const Rho &rp, int lane,
-                                        int D, float (&out)[P])
-{
-    constexpr int NE = P + 2 * DELTA;       // labels lane*P - DELTA .. lane*P + P + DELTA - 1
-    constexpr int NE2 = (NE + 1) / 2 * 2;   // padded to whole pairs
-    float c[DELTA + 1];
-#pragma unroll
-    for (int t = 1; t <= DELTA; ++t) c[t] = __fmul_rn(w, rp.rho[t]);
-    const float base = __fadd_rn(g, __fmul_rn(w, rp.L2));
-    const int DD = FULL ? 32 * P : D;
-    // E[DELTA + i] = value at label lane*P + i, i in [-DELTA, P + DELTA)
-    float E[NE2];
-#pragma unroll
-    for (int i = -DELTA; i < P + DELTA; ++i) {
-        float val;
-        if (i >= 0 && i < P) {
-            val = v[i];
-        } else if (i >= P) {
-            val = __shfl_down_sync(0xffffffffu, v[i % P], i / P);
-        } else {
-            int off = (-i + P - 1) / P;
-            int reg = ((i % P) + P) % P;
-            val = __shfl_up_sync(0xffffffffu, v[reg], off);
-        }
-        const int kk = lane * P + i;
-        E[DELTA + i] = (kk >= 0 && kk < DD) ? val : INF;
-    }
-    if (NE2 > NE) E[NE2 - 1] = INF;
-    float o[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) o[r] = E[DELTA + r];
-#pragma unroll
-    for (int t = 1; t <= DELTA; ++t) {
-        float S[NE2]; // S[j] = E[j] + c[t]
-#pragma unroll
-        for (int q = 0; q < NE2; q += 2) add2(E[q], E[q + 1], c[t], S[q], S[q + 1]);
-#pragma unroll
-        for (int r = 0; r < P; ++r) o[r] = min3(o[r], S[DELTA + r - t], S[DELTA + r + t]);
-    }
-#pragma unroll
-    for (int r = 0; r < P; ++r) out[r] = (FULL || lane * P + r < D) ? __fsub_rn(fminf(o[r], base), g) : INF;
-}
-
-// ---------------------------------------------------------------- cp.async ring
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, int bytes)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// copy this lane's P labels of one pixel vector into its ring slot
-template <int P> __device__ __forceinline__ void lane_copy(float *dst, const float *src, int lane, int D)
-{
-    const int k0 = lane * P;
-    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + k0);
-    if (D == 32 * P) {
-        if constexpr (P % 4 == 0) {
-#pragma unroll
-            for (int i = 0; i < P / 4; ++i) cp_async16(d + 16 * i, src + k0 + 4 * i);
-        } else if constexpr (P % 2 == 0) {
-#pragma unroll
-            for (int i = 0; i < P / 2; ++i) cp_async8(d + 8 * i, src + k0 + 2 * i);
-        } else {
-#pragma unroll
-            for (int i = 0; i < P; ++i) cp_async4(d + 4 * i, src + k0 + i, 4);
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < P; ++i) {
-            const bool ok = k0 + i < D;
-            cp_async4(d + 4 * i, ok ? src + k0 + i : src, ok ? 4 : 0);
-        }
-    }
-}
-
-template <int P> __device__ __forceinline__ void lane_read(const float *slot, int lane, float (&v)[P])
-{
-    const float *q = slot + lane * P; // 16-byte aligned for P % 4 == 0, 8-byte for P == 2
-    if constexpr (P % 4 == 0) {
-#pragma unroll
-        for (int i = 0; i < P / 4; ++i) {
-            const float4 t = *(const float4 *)(q + 4 * i);
-            v[4 * i] = t.x, v[4 * i + 1] = t.y, v[4 * i + 2] = t.z, v[4 * i + 3] = t.w;
-        }
-    } else if constexpr (P == 2) {
-        const float2 t = *(const float2 *)q;
-        v[0] = t.x, v[1] = t.y;
-    } else {
-#pragma unroll
-        for (int r = 0; r < P; ++r) v[r] = q[r];
-    }
-}
-
-constexpr int RING = 8; // prefetch depth in chain steps
-
-__host__ __device__ constexpr int ring_floats(int P) { return RING * 3 * 32 * P; }
-
-// One pass over the chains of one direction; one warp per chain.
-//   HPASS: chain = row y over x (weights wx[y][x] on edge x -> x+1), unary
-//          theta - phi, the handed-over slack is added to phi.
-//   !HPASS: chain = column x over y (weights wy[y][x] on edge y -> y+1),
-//          unary phi, the handed-over slack is subtracted from phi; labels
-//          (if given) = first argmin of the min-marginals.
-// Per step the pixel vectors come from a per-warp shared-memory ring filled
-// RING steps ahead with cp.async (each lane copies and reads only its own
-// labels), so the chain's dependent arithmetic does not wait on DRAM.
-template <int P, int DELTA, bool HPASS, bool FULL>
-__global__ void __launch_bounds__(64)
-    k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
-                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
-                int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
-{
-    extern __shared__ float4 smem4[];
-    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-    const int gchain = blockIdx.x * (blockDim.x >> 5) + wib;
-    const int n = HPASS ? W : H;
-    const int nch = HPASS ? H : W;
-    if (gchain >= nch * npairs) return;
-    // pair of the batch and chain within it
-    const int pair = gchain / nch, chain = gchain - pair * nch;
-    const long pnd = (long)W * H * D * pair;
-    theta += pnd;
-    phi += pnd;
-    Lbuf += pnd;
-    wgt += wps * pair;
-    if (labels) labels += (long)W * H * pair;
-    cmin_out += (long)nch * pair;
-    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P));
-    float *ring = wsm + nmax;
-    auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
-    for (int i = lane; i < n; i += 32) wsm[i] = wgt[pix(i)];
-    __syncwarp();
-    const bool use_phi = !(HPASS && first);
-    auto slot = [&](int i, int a) { return ring + ((i % RING) * 3 + a) * (32 * P); };
-
-    // ---- forward: messages into each node, stored for the backward sweep
-    auto issue_f = [&](int i) {
-        if (i < n) {
-            if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
-            if (use_phi) lane_copy<P>(slot(i, 1), phi + pix(i) * D, lane, D);
-        }
-        cp_commit();
-    };
-    float L[P], v[P], th[P], ph[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
-    for (int i = 0; i < RING - 1; ++i) issue_f(i);
-    double acc = 0.0, cmin = 0.0;
-    for (int i = 0; i < n; ++i) {
-        issue_f(i + RING - 1);
-        cp_wait<RING - 1>();
-        if (HPASS) lane_read<P>(slot(i, 0), lane, th);
-        if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
-        store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
-#pragma unroll
-        for (int r = 0; r < P; ++r) {
-            const float un = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
-            v[r] = (FULL || lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
-        }
-        const float g = warp_min<P>(v);
-        if (lane == 0) { // the FP64 bound lives in lane 0 only (off the message chain)
-            if (i < n - 1) acc += (double)g;
-            else cmin = acc + (double)g;
-        }
-        if (i < n - 1) minconv<P, DELTA, FULL>(v, g, wsm[i], rp, lane, D, L);
-    }
-    cp_wait<0>();
-
-    // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
-    auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j
-        const int i = n - 1 - j;
-        if (i >= 0) {
-            if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
-            if (use_phi) lane_copy<P>(slot(j, 1), phi + pix(i) * D, lane, D);
-            lane_copy<P>(slot(j, 2), Lbuf + pix(i) * D, lane, D);
-        }
-        cp_commit();
-    };
-    float R[P], Lx[P], m[P], A[P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) R[r] = 0.0f;
-    for (int j = 0; j < RING - 1; ++j) issue_b(j);
-    for (int j = 0; j < n; ++j) {
-        const int i = n - 1 - j;
-        issue_b(j + RING - 1);
-        cp_wait<RING - 1>();
-        if (HPASS) lane_read<P>(slot(j, 0), lane, th);
-        if (use_phi) {
-            lane_read<P>(slot(j, 1), lane, ph);
-        } else {
-#pragma unroll
-            for (int r = 0; r < P; ++r) ph[r] = 0.0f; // phi starts at zero
-        }
-        lane_read<P>(slot(j, 2), lane, Lx);
-#pragma unroll
-        for (int r = 0; r < P; ++r) {
-            A[r] = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
-            m[r] = (FULL || lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], A[r]), R[r]) : INF;
-        }
-        const float mu = warp_min<P>(m);
-        if (!HPASS && labels) {
-            int best = 0x7fffffff;
-#pragma unroll
-            for (int r = P - 1; r >= 0; --r)
-                if (m[r] == mu && (FULL || lane * P + r < D)) best = lane * P + r;
-            best = __reduce_min_sync(0xffffffffu, best);
-            if (lane == 0) labels[pix(i)] = best;
-        }
-#pragma unroll
-        for (int r = 0; r < P; ++r) {
-            const float h = __fmul_rn(rp.slack, __fsub_rn(m[r], mu));
-            A[r] = __fsub_rn(A[r], h);
-            ph[r] = HPASS ? __fadd_rn(ph[r], h) : A[r];
-        }
-        store_vec<P>(phi + pix(i) * D, lane, D, ph);
-        if (i > 0) {
-#pragma unroll
-            for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
-            const float g = warp_min<P>(v);
-            minconv<P, DELTA, FULL>(v, g, wsm[i - 1], rp, lane, D, R);
-        }
-    }
-    cp_wait<0>();
-    if (lane == 0) cmin_out[chain] = cmin;
-}
 
 // one thread per pair: sum of chain minima in y then x order
 __global__ void k_lb(const double *__restrict__ cH, int H, const double *__restrict__ cV, int W,
@@ -405,33 +89,59 @@ Layout layout(int W, int H, int D, int np = 1)
     return l;
 }
 
-template <int P, int DELTA>
-int run_passes(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
-               const Rho &rp, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+int pass(const CrfPassArgs &a, bool hpass, int delta, int ring, int wpb, cudaStream_t st)
 {
-    float *phi = (float *)(ws + l.phi), *lbuf = (float *)(ws + l.lbuf);
+    return ring == 4 ? crf_pass_ring4(a, hpass, delta, wpb, st) : crf_pass_ring8(a, hpass, delta, wpb, st);
+}
+
+// labels per lane of the instantiated kernel (launch_pass_any's choice)
+int lane_labels(int D)
+{
+    const int P = (D + 31) / 32;
+    return P <= 4 ? P : (P <= 6 ? 6 : 8);
+}
+
+bool fits(int D, int W, int H, bool hpass, int ring, int wpb)
+{
+    return crf_pass_smem(lane_labels(D), ring, W, H, hpass, wpb) <= 227 * 1024;
+}
+
+// the tile of the tuning table for this shape, each pass falling back to the
+// default when the tuned one does not fit the shared memory
+CrfTile effective_tile(int W, int H, int D, int np, int delta)
+{
+    CrfTile t = crf_tile_lookup(W, H, D, np, delta), d;
+    if (!fits(D, W, H, true, t.ring_h, t.wpb_h)) t.ring_h = d.ring_h, t.wpb_h = d.wpb_h;
+    if (!fits(D, W, H, false, t.ring_v, t.wpb_v)) t.ring_v = d.ring_v, t.wpb_v = d.wpb_v;
+    return t;
+}
+
+CrfPassArgs pass_args(const float *cost, long wps, int W, int H, int D, int np, const Rho &rp, char *ws,
+                      const Layout &l)
+{
+    CrfPassArgs a{};
+    a.theta = cost;
+    a.phi = (float *)(ws + l.phi);
+    a.lbuf = (float *)(ws + l.lbuf);
+    a.W = W, a.H = H, a.D = D, a.np = np, a.wps = wps;
+    a.rp = rp;
+    return a;
+}
+
+int run_passes(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
+               const Rho &rp, int delta, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+{
+    if (delta < 1 || delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
+    const CrfTile t = effective_tile(W, H, D, np, delta);
+    if (!fits(D, W, H, true, t.ring_h, t.wpb_h) || !fits(D, W, H, false, t.ring_v, t.wpb_v))
+        return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
     double *cH = (double *)(ws + l.ch), *cV = (double *)(ws + l.cv), *lb = (double *)(ws + l.lb);
-    const int wpb = 2;
-    const int nh = (W + 3) & ~3, nv = (H + 3) & ~3;
-    const size_t smh = sizeof(float) * wpb * (size_t)(nh + ring_floats(P));
-    const size_t smv = sizeof(float) * wpb * (size_t)(nv + ring_floats(P));
-    if (smh > 227 * 1024 || smv > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
-    const bool full = D == 32 * P;
-    auto kh = full ? k_crf_chain<P, DELTA, true, true> : k_crf_chain<P, DELTA, true, false>;
-    auto kv = full ? k_crf_chain<P, DELTA, false, true> : k_crf_chain<P, DELTA, false, false>;
-    CNNCRF_CUDA(cudaFuncSetAttribute(kh, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smh));
-    CNNCRF_CUDA(cudaFuncSetAttribute(kv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smv));
+    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, rp, ws, l);
     for (int it = 0; it < iters; ++it) {
-        {
-            CNNCRF_PROF("crf_h", st);
-            kh<<<ceil_div((long)H * np, wpb), 32 * wpb, smh, st>>>(cost, phi, wx, lbuf, W, H, D, rp, it == 0, nh,
-                                                                  nullptr, cH, np, wps);
-        }
-        {
-            CNNCRF_PROF("crf_v", st);
-            kv<<<ceil_div((long)W * np, wpb), 32 * wpb, smv, st>>>(cost, phi, wy, lbuf, W, H, D, rp, 0, nv,
-                                                                  it == iters - 1 ? labels : nullptr, cV, np, wps);
-        }
+        a.wgt = wx, a.first = it == 0, a.labels = nullptr, a.cmin = cH;
+        CNNCRF_TRY(pass(a, true, delta, t.ring_h, t.wpb_h, st));
+        a.wgt = wy, a.first = 0, a.labels = it == iters - 1 ? labels : nullptr, a.cmin = cV;
+        CNNCRF_TRY(pass(a, false, delta, t.ring_v, t.wpb_v, st));
     }
     {
         CNNCRF_PROF("lb", st);
@@ -441,29 +151,35 @@ int run_passes(const float *cost, const float *wx, const float *wy, long wps, in
     return CNNCRF_OK;
 }
 
-template <int P>
-int dispatch_delta(int delta, const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D,
-                   int np, const Rho &rp, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+Rho make_rho(const CrfParams &p)
 {
-    switch (delta) {
-    case 1: return run_passes<P, 1>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
-    case 2: return run_passes<P, 2>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
-    case 3: return run_passes<P, 3>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
-    case 4: return run_passes<P, 4>(cost, wx, wy, wps, W, H, D, np, rp, iters, labels, ws, l, st);
-    default: return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
-    }
+    Rho rp;
+    rp.L2 = p.L2;
+    rp.slack = p.slack;
+    rp.rho[0] = 0.0f;
+    for (int t = 1; t <= 8; ++t) rp.rho[t] = p.shape == 0 ? fminf(p.L1, p.L2) : fminf(p.L1 * (float)t, p.L2);
+    return rp;
+}
+
+int check_args(const float *cost, const float *wx, const float *wy, int W, int H, int D, int np, const CrfParams &p,
+               const void *ws, size_t ws_bytes)
+{
+    if (W < 1 || H < 1 || D < 1 || D > 256 || np < 1) return fail(CNNCRF_EINVAL, "crf: bad size %dx%dx%d x%d", W, H, D, np);
+    if (!cost || !wx || !wy || !ws) return fail(CNNCRF_EINVAL, "crf: null pointer");
+    if (p.slack <= 0.0f || p.slack > 1.0f) return fail(CNNCRF_EINVAL, "crf: slack %g outside (0,1]", p.slack);
+    const Layout l = layout(W, H, D, np);
+    if (ws_bytes < l.total) return fail(CNNCRF_EINVAL, "crf: workspace %zu < %zu bytes", ws_bytes, l.total);
+    if (((uintptr_t)ws & 255) != 0) return fail(CNNCRF_EINVAL, "crf: workspace not 256-byte aligned");
+    if (((uintptr_t)cost & 15) != 0) return fail(CNNCRF_EINVAL, "crf: cost volume not 16-byte aligned");
+    return CNNCRF_OK;
 }
 
 int solve_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
                const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st)
 {
-    if (W < 1 || H < 1 || D < 1 || D > 256 || np < 1) return fail(CNNCRF_EINVAL, "crf: bad size %dx%dx%d x%d", W, H, D, np);
-    if (!cost || !wx || !wy || !labels || !ws) return fail(CNNCRF_EINVAL, "crf: null pointer");
-    if (p.slack <= 0.0f || p.slack > 1.0f) return fail(CNNCRF_EINVAL, "crf: slack %g outside (0,1]", p.slack);
-    Layout l = layout(W, H, D, np);
-    if (ws_bytes < l.total) return fail(CNNCRF_EINVAL, "crf: workspace %zu < %zu bytes", ws_bytes, l.total);
-    if (((uintptr_t)ws & 255) != 0) return fail(CNNCRF_EINVAL, "crf: workspace not 256-byte aligned");
-    if (((uintptr_t)cost & 15) != 0) return fail(CNNCRF_EINVAL, "crf: cost volume not 16-byte aligned");
+    CNNCRF_TRY(check_args(cost, wx, wy, W, H, D, np, p, ws, ws_bytes));
+    if (!labels) return fail(CNNCRF_EINVAL, "crf: null pointer");
+    const Layout l = layout(W, H, D, np);
     char *w = (char *)ws;
     if (iters <= 0) {
         {
@@ -474,18 +190,73 @@ int solve_impl(const float *cost, const float *wx, const float *wy, long wps, in
         CNNCRF_CHECK_LAUNCH();
         return CNNCRF_OK;
     }
-    Rho rp;
-    rp.L2 = p.L2;
-    rp.slack = p.slack;
-    rp.rho[0] = 0.0f;
-    for (int t = 1; t <= 8; ++t) rp.rho[t] = p.shape == 0 ? fminf(p.L1, p.L2) : fminf(p.L1 * (float)t, p.L2);
-    int P = (D + 31) / 32;
-    if (P <= 1) return dispatch_delta<1>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
-    if (P <= 2) return dispatch_delta<2>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
-    if (P <= 3) return dispatch_delta<3>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
-    if (P <= 4) return dispatch_delta<4>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
-    if (P <= 6) return dispatch_delta<6>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
-    return dispatch_delta<8>(p.delta, cost, wx, wy, wps, W, H, D, np, rp, iters, labels, w, l, st);
+    return run_passes(cost, wx, wy, wps, W, H, D, np, make_rho(p), p.delta, iters, labels, w, l, st);
+}
+
+// time one H and one V pass of every candidate tile (events on `st`, best of
+// `reps`); the workspace's messages are overwritten, the next solve starts
+// afresh (its first H pass does not read them)
+int autotune_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
+                  const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, CrfTile *best, float *ms_h,
+                  float *ms_v)
+{
+    CNNCRF_TRY(check_args(cost, wx, wy, W, H, D, np, p, ws, ws_bytes));
+    if (p.delta < 1 || p.delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", p.delta);
+    const Layout l = layout(W, H, D, np);
+    char *w = (char *)ws;
+    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, make_rho(p), w, l);
+    const int rings[2] = {8, 4}, wpbs[3] = {2, 1, 4}; // the default first: it wins ties
+    const int reps = 3;
+    struct Cand {
+        int ring, wpb;
+        bool h, v;
+        cudaEvent_t e[3 * 3];
+    };
+    std::vector<Cand> cands;
+    for (int r : rings)
+        for (int b : wpbs) {
+            Cand c{r, b, fits(D, W, H, true, r, b), fits(D, W, H, false, r, b), {}};
+            if (c.h || c.v) cands.push_back(c);
+        }
+    int rc = CNNCRF_OK;
+    for (auto &c : cands)
+        for (auto &e : c.e)
+            if (rc == CNNCRF_OK && cudaEventCreate(&e) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "crf tune: event");
+    for (int rep = 0; rep < reps && rc == CNNCRF_OK; ++rep)
+        for (auto &c : cands) {
+            cudaEvent_t *e = c.e + 3 * rep;
+            if (cudaEventRecord(e[0], st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "crf tune: record");
+            a.wgt = wx, a.first = 1, a.labels = nullptr, a.cmin = (double *)(w + l.ch);
+            if (rc == CNNCRF_OK && c.h) rc = pass(a, true, p.delta, c.ring, c.wpb, st);
+            if (rc == CNNCRF_OK && cudaEventRecord(e[1], st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "crf tune: record");
+            a.wgt = wy, a.first = 0, a.cmin = (double *)(w + l.cv);
+            if (rc == CNNCRF_OK && c.v) rc = pass(a, false, p.delta, c.ring, c.wpb, st);
+            if (rc == CNNCRF_OK && cudaEventRecord(e[2], st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "crf tune: record");
+            if (rc != CNNCRF_OK) break;
+        }
+    if (rc == CNNCRF_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "crf tune: sync");
+    CrfTile t;
+    float bh = 1e30f, bv = 1e30f;
+    for (auto &c : cands) {
+        float mh = 1e30f, mv = 1e30f;
+        for (int rep = 0; rep < reps && rc == CNNCRF_OK; ++rep) {
+            float x = 0, y = 0;
+            cudaEventElapsedTime(&x, c.e[3 * rep], c.e[3 * rep + 1]);
+            cudaEventElapsedTime(&y, c.e[3 * rep + 1], c.e[3 * rep + 2]);
+            mh = std::min(mh, x), mv = std::min(mv, y);
+        }
+        if (c.h && mh < bh) bh = mh, t.ring_h = c.ring, t.wpb_h = c.wpb;
+        if (c.v && mv < bv) bv = mv, t.ring_v = c.ring, t.wpb_v = c.wpb;
+    }
+    for (auto &c : cands)
+        for (auto &e : c.e)
+            if (e) cudaEventDestroy(e);
+    if (rc != CNNCRF_OK) return rc;
+    if (bh >= 1e30f || bv >= 1e30f) return fail(CNNCRF_EUNSUPPORTED, "crf tune: no tile fits %dx%dx%d", W, H, D);
+    *best = t;
+    if (ms_h) *ms_h = bh;
+    if (ms_v) *ms_v = bv;
+    return CNNCRF_OK;
 }
 
 } // namespace
@@ -509,6 +280,16 @@ int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int
 {
     const long N = (long)W * H;
     return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st);
+}
+
+int crf_autotune(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int npairs,
+                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store)
+{
+    CrfTile t;
+    float mh = 0, mv = 0;
+    CNNCRF_TRY(autotune_impl(cost, wx, wy, wps, W, H, D, npairs, p, ws, ws_bytes, st, &t, &mh, &mv));
+    if (store) crf_tile_store(W, H, D, npairs, p.delta, t, mh, mv);
+    return CNNCRF_OK;
 }
 
 const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs)

@@ -1,0 +1,417 @@
+// k_crf_chain.cuh -- the chain pass of the CRF solve (k_crf.cu), shared by
+// the translation units that instantiate it for one prefetch depth each
+// (k_crf.cu: 8 chain steps, k_crf_r4.cu: 4), so the variants the tile tuner
+// chooses between compile in parallel.  Everything device-side has internal
+// linkage; each unit exports one launcher, crf_pass_ring<RING>.
+#ifndef CNNCRF_K_CRF_CHAIN_CUH
+#define CNNCRF_K_CRF_CHAIN_CUH
+
+#include <cfloat>
+#include <math_constants.h>
+
+#include "common.h"
+#include "kernels.h"
+
+namespace cnncrf {
+namespace k {
+
+// pairwise term: rho[t] for |t| = 0..8 (t > delta: L2), slack fraction
+struct Rho {
+    float rho[9];
+    float L2;
+    float slack;
+};
+
+// one pass over all chains of one direction (see k_crf_chain)
+struct CrfPassArgs {
+    const float *theta; // the cost volume [np][H][W][D]
+    float *phi;         // H/V split of the unary, same layout
+    const float *wgt;   // wx (H pass) or wy (V pass), pair stride wps
+    float *lbuf;        // forward messages, same layout as phi
+    int W, H, D, np;
+    long wps;
+    Rho rp;
+    int first;           // H pass of the first iteration: phi = 0, not read
+    int32_t *labels;     // V pass of the last iteration: argmin labels, else null
+    double *cmin;        // per chain minimum [np][chains]
+};
+
+// launch one pass with prefetch depth RING (4 or 8) and `wpb` warps (chains)
+// per CTA; EUNSUPPORTED when the CTA's shared memory would exceed the limit
+int crf_pass_ring8(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStream_t st);
+int crf_pass_ring4(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStream_t st);
+size_t crf_pass_smem(int P, int RING, int W, int H, bool hpass, int wpb);
+
+namespace {
+
+#define INF CUDART_INF_F
+
+// Order-preserving map of (non-NaN) floats to signed ints, and back: the
+// warp minimum is then one redux.sync.min.s32, exact like a float min.
+__device__ __forceinline__ int f2ord(float f)
+{
+    const int b = __float_as_int(f);
+    return b ^ ((b >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7fffffff)); }
+
+template <int P> __device__ __forceinline__ float warp_min(const float (&v)[P])
+{
+    float m = v[0];
+#pragma unroll
+    for (int r = 1; r < P; ++r) m = fminf(m, v[r]);
+    return ord2f(__reduce_min_sync(0xffffffffu, f2ord(m)));
+}
+
+template <int P> __device__ __forceinline__ void load_vec(const float *p, int lane, int D, float (&v)[P])
+{
+    const int k0 = lane * P;
+    if (D == 32 * P && (P == 1 || P == 2 || P == 4 || P == 8)) {
+        if constexpr (P == 1) {
+            v[0] = p[k0];
+        } else if constexpr (P == 2) {
+            float2 t = *(const float2 *)(p + k0);
+            v[0] = t.x, v[1] = t.y;
+        } else if constexpr (P == 4) {
+            float4 t = *(const float4 *)(p + k0);
+            v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+        } else if constexpr (P == 8) {
+            float4 t = *(const float4 *)(p + k0), u = *(const float4 *)(p + k0 + 4);
+            v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w, v[4] = u.x, v[5] = u.y, v[6] = u.z, v[7] = u.w;
+        }
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r) v[r] = (k0 + r < D) ? p[k0 + r] : 0.0f;
+}
+
+template <int P> __device__ __forceinline__ void store_vec(float *p, int lane, int D, const float (&v)[P])
+{
+    const int k0 = lane * P;
+    if (D == 32 * P && (P == 1 || P == 2 || P == 4 || P == 8)) {
+        if constexpr (P == 1) {
+            p[k0] = v[0];
+        } else if constexpr (P == 2) {
+            *(float2 *)(p + k0) = make_float2(v[0], v[1]);
+        } else if constexpr (P == 4) {
+            *(float4 *)(p + k0) = make_float4(v[0], v[1], v[2], v[3]);
+        } else if constexpr (P == 8) {
+            *(float4 *)(p + k0) = make_float4(v[0], v[1], v[2], v[3]);
+            *(float4 *)(p + k0 + 4) = make_float4(v[4], v[5], v[6], v[7]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r)
+        if (k0 + r < D) p[k0 + r] = v[r];
+}
+
+// Exact two-lane IEEE add (add.rn.f32x2) and three-input minimum (min.f32
+// with three sources): the same values as two __fadd_rn and two fminf, in
+// fewer instructions.
+__device__ __forceinline__ void add2(float a0, float a1, float b, float &d0, float &d1)
+{
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %4};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d0), "=f"(d1)
+        : "f"(a0), "f"(a1), "f"(b));
+}
+__device__ __forceinline__ float min3(float a, float b, float c)
+{
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
+// out = minconv(v) - g, pads (k >= D) kept at +inf.  FULL: D == 32 * P (no
+// pad labels, only the chain ends of lanes 0 and 31 are masked).
+template <int P, int DELTA, bool FULL>
+__device__ __forceinline__ void minconv(const float (&v)[P], float g, float w, const Rho &rp, int lane,
+                                        int D, float (&out)[P])
+{
+    constexpr int NE = P + 2 * DELTA;       // labels lane*P - DELTA .. lane*P + P + DELTA - 1
+    constexpr int NE2 = (NE + 1) / 2 * 2;   // padded to whole pairs
+    float c[DELTA + 1];
+#pragma unroll
+    for (int t = 1; t <= DELTA; ++t) c[t] = __fmul_rn(w, rp.rho[t]);
+    const float base = __fadd_rn(g, __fmul_rn(w, rp.L2));
+    const int DD = FULL ? 32 * P : D;
+    // E[DELTA + i] = value at label lane*P + i, i in [-DELTA, P + DELTA)
+    float E[NE2];
+#pragma unroll
+    for (int i = -DELTA; i < P + DELTA; ++i) {
+        float val;
+        if (i >= 0 && i < P) {
+            val = v[i];
+        } else if (i >= P) {
+            val = __shfl_down_sync(0xffffffffu, v[i % P], i / P);
+        } else {
+            int off = (-i + P - 1) / P;
+            int reg = ((i % P) + P) % P;
+            val = __shfl_up_sync(0xffffffffu, v[reg], off);
+        }
+        const int kk = lane * P + i;
+        E[DELTA + i] = (kk >= 0 && kk < DD) ? val : INF;
+    }
+    if (NE2 > NE) E[NE2 - 1] = INF;
+    float o[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) o[r] = E[DELTA + r];
+#pragma unroll
+    for (int t = 1; t <= DELTA; ++t) {
+        float S[NE2]; // S[j] = E[j] + c[t]
+#pragma unroll
+        for (int q = 0; q < NE2; q += 2) add2(E[q], E[q + 1], c[t], S[q], S[q + 1]);
+#pragma unroll
+        for (int r = 0; r < P; ++r) o[r] = min3(o[r], S[DELTA + r - t], S[DELTA + r + t]);
+    }
+#pragma unroll
+    for (int r = 0; r < P; ++r) out[r] = (FULL || lane * P + r < D) ? __fsub_rn(fminf(o[r], base), g) : INF;
+}
+
+// ---------------------------------------------------------------- cp.async ring
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void *src, int bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> __device__ __forceinline__ void cp_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// copy this lane's P labels of one pixel vector into its ring slot
+template <int P> __device__ __forceinline__ void lane_copy(float *dst, const float *src, int lane, int D)
+{
+    const int k0 = lane * P;
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst + k0);
+    if (D == 32 * P) {
+        if constexpr (P % 4 == 0) {
+#pragma unroll
+            for (int i = 0; i < P / 4; ++i) cp_async16(d + 16 * i, src + k0 + 4 * i);
+        } else if constexpr (P % 2 == 0) {
+#pragma unroll
+            for (int i = 0; i < P / 2; ++i) cp_async8(d + 8 * i, src + k0 + 2 * i);
+        } else {
+#pragma unroll
+            for (int i = 0; i < P; ++i) cp_async4(d + 4 * i, src + k0 + i, 4);
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < P; ++i) {
+            const bool ok = k0 + i < D;
+            cp_async4(d + 4 * i, ok ? src + k0 + i : src, ok ? 4 : 0);
+        }
+    }
+}
+
+template <int P> __device__ __forceinline__ void lane_read(const float *slot, int lane, float (&v)[P])
+{
+    const float *q = slot + lane * P; // 16-byte aligned for P % 4 == 0, 8-byte for P == 2
+    if constexpr (P % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < P / 4; ++i) {
+            const float4 t = *(const float4 *)(q + 4 * i);
+            v[4 * i] = t.x, v[4 * i + 1] = t.y, v[4 * i + 2] = t.z, v[4 * i + 3] = t.w;
+        }
+    } else if constexpr (P == 2) {
+        const float2 t = *(const float2 *)q;
+        v[0] = t.x, v[1] = t.y;
+    } else {
+#pragma unroll
+        for (int r = 0; r < P; ++r) v[r] = q[r];
+    }
+}
+
+__host__ __device__ constexpr int ring_floats(int P, int RING) { return RING * 3 * 32 * P; }
+
+// One pass over the chains of one direction; one warp per chain.
+//   HPASS: chain = row y over x (weights wx[y][x] on edge x -> x+1), unary
+//          theta - phi, the handed-over slack is added to phi.
+//   !HPASS: chain = column x over y (weights wy[y][x] on edge y -> y+1),
+//          unary phi, the handed-over slack is subtracted from phi; labels
+//          (if given) = first argmin of the min-marginals.
+// Per step the pixel vectors come from a per-warp shared-memory ring filled
+// RING steps ahead with cp.async (each lane copies and reads only its own
+// labels), so the chain's dependent arithmetic does not wait on DRAM.
+template <int P, int DELTA, bool HPASS, bool FULL, int RING>
+__global__ void __launch_bounds__(128)
+    k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
+                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
+                int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
+{
+    extern __shared__ float4 smem4[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int gchain = blockIdx.x * (blockDim.x >> 5) + wib;
+    const int n = HPASS ? W : H;
+    const int nch = HPASS ? H : W;
+    if (gchain >= nch * npairs) return;
+    // pair of the batch and chain within it
+    const int pair = gchain / nch, chain = gchain - pair * nch;
+    const long pnd = (long)W * H * D * pair;
+    theta += pnd;
+    phi += pnd;
+    Lbuf += pnd;
+    wgt += wps * pair;
+    if (labels) labels += (long)W * H * pair;
+    cmin_out += (long)nch * pair;
+    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P, RING));
+    float *ring = wsm + nmax;
+    auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
+    for (int i = lane; i < n; i += 32) wsm[i] = wgt[pix(i)];
+    __syncwarp();
+    const bool use_phi = !(HPASS && first);
+    auto slot = [&](int i, int a) { return ring + ((i % RING) * 3 + a) * (32 * P); };
+
+    // ---- forward: messages into each node, stored for the backward sweep
+    auto issue_f = [&](int i) {
+        if (i < n) {
+            if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
+            if (use_phi) lane_copy<P>(slot(i, 1), phi + pix(i) * D, lane, D);
+        }
+        cp_commit();
+    };
+    float L[P], v[P], th[P], ph[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
+    for (int i = 0; i < RING - 1; ++i) issue_f(i);
+    double acc = 0.0, cmin = 0.0;
+    for (int i = 0; i < n; ++i) {
+        issue_f(i + RING - 1);
+        cp_wait<RING - 1>();
+        if (HPASS) lane_read<P>(slot(i, 0), lane, th);
+        if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
+        store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            const float un = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
+            v[r] = (FULL || lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
+        }
+        const float g = warp_min<P>(v);
+        if (lane == 0) { // the FP64 bound lives in lane 0 only (off the message chain)
+            if (i < n - 1) acc += (double)g;
+            else cmin = acc + (double)g;
+        }
+        if (i < n - 1) minconv<P, DELTA, FULL>(v, g, wsm[i], rp, lane, D, L);
+    }
+    cp_wait<0>();
+
+    // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
+    auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j
+        const int i = n - 1 - j;
+        if (i >= 0) {
+            if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
+            if (use_phi) lane_copy<P>(slot(j, 1), phi + pix(i) * D, lane, D);
+            lane_copy<P>(slot(j, 2), Lbuf + pix(i) * D, lane, D);
+        }
+        cp_commit();
+    };
+    float R[P], Lx[P], m[P], A[P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) R[r] = 0.0f;
+    for (int j = 0; j < RING - 1; ++j) issue_b(j);
+    for (int j = 0; j < n; ++j) {
+        const int i = n - 1 - j;
+        issue_b(j + RING - 1);
+        cp_wait<RING - 1>();
+        if (HPASS) lane_read<P>(slot(j, 0), lane, th);
+        if (use_phi) {
+            lane_read<P>(slot(j, 1), lane, ph);
+        } else {
+#pragma unroll
+            for (int r = 0; r < P; ++r) ph[r] = 0.0f; // phi starts at zero
+        }
+        lane_read<P>(slot(j, 2), lane, Lx);
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            A[r] = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
+            m[r] = (FULL || lane * P + r < D) ? __fadd_rn(__fadd_rn(Lx[r], A[r]), R[r]) : INF;
+        }
+        const float mu = warp_min<P>(m);
+        if (!HPASS && labels) {
+            int best = 0x7fffffff;
+#pragma unroll
+            for (int r = P - 1; r >= 0; --r)
+                if (m[r] == mu && (FULL || lane * P + r < D)) best = lane * P + r;
+            best = __reduce_min_sync(0xffffffffu, best);
+            if (lane == 0) labels[pix(i)] = best;
+        }
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+            const float h = __fmul_rn(rp.slack, __fsub_rn(m[r], mu));
+            A[r] = __fsub_rn(A[r], h);
+            ph[r] = HPASS ? __fadd_rn(ph[r], h) : A[r];
+        }
+        store_vec<P>(phi + pix(i) * D, lane, D, ph);
+        if (i > 0) {
+#pragma unroll
+            for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
+            const float g = warp_min<P>(v);
+            minconv<P, DELTA, FULL>(v, g, wsm[i - 1], rp, lane, D, R);
+        }
+    }
+    cp_wait<0>();
+    if (lane == 0) cmin_out[chain] = cmin;
+}
+
+template <int P, int DELTA, int RING>
+int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
+{
+    const int n = hpass ? a.W : a.H;
+    const int nmax = (n + 3) & ~3;
+    const size_t sm = sizeof(float) * wpb * (size_t)(nmax + ring_floats(P, RING));
+    if (sm > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
+    const bool full = a.D == 32 * P;
+    auto kern = hpass ? (full ? k_crf_chain<P, DELTA, true, true, RING> : k_crf_chain<P, DELTA, true, false, RING>)
+                      : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
+    CNNCRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const long chains = (long)(hpass ? a.H : a.W) * a.np;
+    {
+        CNNCRF_PROF(hpass ? "crf_h" : "crf_v", st);
+        kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.phi, a.wgt, a.lbuf, a.W, a.H, a.D, a.rp,
+                                                           a.first, nmax, a.labels, a.cmin, a.np, a.wps);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+template <int P, int RING>
+int launch_pass_delta(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStream_t st)
+{
+    switch (delta) {
+    case 1: return launch_pass<P, 1, RING>(a, hpass, wpb, st);
+    case 2: return launch_pass<P, 2, RING>(a, hpass, wpb, st);
+    case 3: return launch_pass<P, 3, RING>(a, hpass, wpb, st);
+    case 4: return launch_pass<P, 4, RING>(a, hpass, wpb, st);
+    default: return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
+    }
+}
+
+// labels per lane P = ceil(D / 32) rounded up to 1, 2, 3, 4, 6 or 8
+template <int RING>
+int launch_pass_any(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStream_t st)
+{
+    if (wpb < 1 || wpb > 4) return fail(CNNCRF_EINVAL, "crf: %d chains per CTA outside 1..4", wpb);
+    const int P = (a.D + 31) / 32;
+    if (P <= 1) return launch_pass_delta<1, RING>(a, hpass, delta, wpb, st);
+    if (P <= 2) return launch_pass_delta<2, RING>(a, hpass, delta, wpb, st);
+    if (P <= 3) return launch_pass_delta<3, RING>(a, hpass, delta, wpb, st);
+    if (P <= 4) return launch_pass_delta<4, RING>(a, hpass, delta, wpb, st);
+    if (P <= 6) return launch_pass_delta<6, RING>(a, hpass, delta, wpb, st);
+    return launch_pass_delta<8, RING>(a, hpass, delta, wpb, st);
+}
+
+} // namespace
+
+} // namespace k
+} // namespace cnncrf
+
+#endif

@@ -115,6 +115,21 @@ int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H,
 // theta - phi of the last solve (get_C1)
 int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st);
 
+// CRF tile: prefetch ring depth (4 or 8 chain steps) and chains (warps) per
+// CTA (1, 2 or 4) of the H and the V pass.  Every tile gives the same bits;
+// only the speed differs.  The solver takes the tile of the process-wide
+// tuning table for (W, H, D, npairs, delta), the default if there is none.
+struct CrfTile {
+    int ring_h = 8, wpb_h = 2, ring_v = 8, wpb_v = 2;
+};
+bool crf_tile_valid(const CrfTile &t);
+CrfTile crf_tile_lookup(int W, int H, int D, int npairs, int delta);
+void crf_tile_store(int W, int H, int D, int npairs, int delta, const CrfTile &t, float ms_h, float ms_v);
+// time every tile on this problem (one H and one V pass each, best of 3)
+// and, with store, enter the fastest per pass in the table; synchronises st
+int crf_autotune(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int npairs,
+                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store = true);
+
 // ------------------------------------------------------------ small ops
 int remap(float *out, const int32_t *labels, long n, float dmin, float dstep, cudaStream_t st);
 int argmin(float *out, const float *vol, long npx, int D, float dmin, float dstep,

@@ -104,6 +104,18 @@ int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, 
                         workspace_bytes, lower_bound, (cudaStream_t)stream);
 }
 
+int cnncrf_crf_autotune(const float *d_cost, const float *d_wx, const float *d_wy, int width, int height, int depth,
+                        const cnncrf_crf_options *opt, void *d_workspace, size_t workspace_bytes,
+                        cnncrf_stream_t stream)
+{
+    clear_error();
+    if (!opt) return fail(CNNCRF_EINVAL, "crf: null options");
+    k::CrfParams p;
+    CNNCRF_TRY(crf_params(opt, &p));
+    return k::crf_autotune(d_cost, d_wx, d_wy, 0, width, height, depth, 1, p, d_workspace, workspace_bytes,
+                           (cudaStream_t)stream);
+}
+
 int cnncrf_slackprop_create(cnncrf_slackprop_t *sp)
 {
     if (!sp) return fail(CNNCRF_EINVAL, "null argument");

@@ -209,6 +209,43 @@ int cnncrf_crf_solve_static(const float *d_cost, const float *d_wx, const float 
                             int height, int depth, const cnncrf_crf_options *opt, int32_t *d_labels,
                             double *lower_bound, cnncrf_stream_t stream);
 
+/* CRF tiles.  No counterpart in the reference, whose solver has one launch
+ * shape.  A tile is the chain kernel's prefetch ring depth (4 or 8 chain
+ * steps) and chains per CTA (1, 2 or 4) for the horizontal and the vertical
+ * pass.  Every tile gives the same labels and bound bit for bit; the fastest
+ * depends on the label count, the chain lengths and the pairs per launch, so
+ * the library keeps a process-wide table from (width, height, depth, npairs,
+ * delta) to a tile.  Every solve (cnncrf_crf_solve, SlackProp, Stereo, the
+ * batch) looks its shape up and runs the default tile (ring 8, 2 chains per
+ * CTA, both passes) when the table has none.  The table is filled by the two
+ * autotune calls below or set by hand, and can be saved to a text file and
+ * merged back, so a deployment measures once.  Thread-safe. */
+typedef struct cnncrf_crf_tile {
+    int ring_h, chains_per_cta_h; /* horizontal pass */
+    int ring_v, chains_per_cta_v; /* vertical pass */
+} cnncrf_crf_tile;
+int cnncrf_crf_tuning_set(int width, int height, int depth, int npairs, int delta, const cnncrf_crf_tile *tile);
+/* *found = 0 and the default tile when the table has no entry; ms_h / ms_v
+ * (may be NULL): the pass times the autotuner measured, 0 for a set tile. */
+int cnncrf_crf_tuning_get(int width, int height, int depth, int npairs, int delta, cnncrf_crf_tile *tile,
+                          int *found, float *ms_h, float *ms_v);
+int cnncrf_crf_tuning_clear(void);
+int cnncrf_crf_tuning_count(int *n);
+/* Text file: the line "cnncrf-crf-tiles 1", then one line per entry
+ * "W H D npairs delta ring_h chains_h ring_v chains_v ms_h ms_v"; '#' starts
+ * a comment line.  Load merges into the table; a malformed file returns
+ * CNNCRF_EINVAL naming the line and changes nothing. */
+int cnncrf_crf_tuning_save(const char *path);
+int cnncrf_crf_tuning_load(const char *path);
+/* Measures every tile on this problem (one horizontal and one vertical pass
+ * each, best of three, CUDA events on `stream`) and enters the fastest per
+ * pass for (width, height, depth, 1, opt->delta).  Arguments as
+ * cnncrf_crf_solve; the workspace's contents are overwritten (the next solve
+ * does not depend on them).  Synchronises the stream: not during a capture. */
+int cnncrf_crf_autotune(const float *d_cost, const float *d_wx, const float *d_wy, int width, int height,
+                        int depth, const cnncrf_crf_options *opt, void *d_workspace, size_t workspace_bytes,
+                        cnncrf_stream_t stream);
+
 /* Object form of the same solver, mirroring slack_prop_2D_alg's members. */
 typedef struct cnncrf_slackprop *cnncrf_slackprop_t;
 int cnncrf_slackprop_create(cnncrf_slackprop_t *sp);
@@ -403,6 +440,16 @@ int cnncrf_batch_get_volume_device(cnncrf_batch_t b, int pair, const float **d_v
 int cnncrf_batch_lower_bound(cnncrf_batch_t b, int pair, double *lb);
 /* Synchronise and report a kernel that gave up on a bounded wait (ETIMEOUT). */
 int cnncrf_batch_check(cnncrf_batch_t b);
+/* No counterpart in the reference.  Runs the batch once (the staged images
+ * through the whole path), then tunes the CRF tile of every group on its
+ * volume (cnncrf_crf_autotune per group, npairs = the group's pairs) and
+ * drops the captured graph so the next run captures the tuned launches.  The
+ * outputs of that run stay readable.  Synchronises: not during a capture. */
+int cnncrf_batch_autotune(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg);
+/* The groups the pairs fall into (same size and range, at most the group
+ * size set by cnncrf_batch_set_group_size), in pipeline order. */
+int cnncrf_batch_num_groups(cnncrf_batch_t b, int *n);
+int cnncrf_batch_group_shape(cnncrf_batch_t b, int group, int *width, int *height, int *depth, int *npairs);
 
 /* ---------------------------------------------------------------- instrumentation
  * (no counterpart in the reference, which timed whole stages with

@@ -93,3 +93,27 @@ def test_net_batch_of_two(cuda, oracle):
         ovol, opw = oracle.predict(cfg, params, lp[i], rp[i], lst)
         assert np.array_equal(vol[i].cpu().numpy(), ovol)
         assert np.array_equal(pw[i].cpu().numpy(), opw)
+
+
+def test_uneven_batch_full_size_equals_single(cuda):
+    """The uneven batch's four sizes and ranges at full size (480x320/D64,
+    720x480/D96, 1242x375/D128, 1440x960/D192), two pairs each, replayed as
+    one CUDA graph: every pair's labels, disparities and bound equal those of
+    a single-pair run."""
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import StereoBatch
+    layers, iters, crf = 7, 8, (0.5, 1.5, 3)
+    sc = scenes.uneven_scenes(2, seed0=7)
+    b = StereoBatch(precision=L.BF16, num_layers=layers, seed=0, graph=True, group_size=0)
+    for s in sc:
+        b.add_pair(s["W"], s["H"], 0.0, 1.0, float(s["D"] - 1))
+    for rnd in range(2):  # eager run, then the captured graph
+        for i, s in enumerate(sc):
+            b.set_images(i, s["left"], s["right"])
+        b.run(*crf, iters)
+    b.check()
+    for i, s in enumerate(sc):
+        lab, disp, lb = single_run(L, s, L.BF16, float(s["D"] - 1), layers, iters, crf)
+        assert np.array_equal(b.labels_device(i).cpu().numpy(), lab), i
+        assert np.array_equal(b.get_output(i), disp), i
+        assert b.lower_bound(i) == lb, i
