@@ -1036,3 +1036,205 @@ void oracle_lr_check(const float *left, const float *right, int W, int H, float 
 }
 
 } // extern "C"
+
+// ================================================================ adjoints (training step), FP64
+// The backward of oracle_predict for the one-minus-dot unary and integer
+// disparity lists: given dL/dvol and dL/dpw, the gradient of every parameter
+// in its npz layout.  The reference has no gradient code for the nets; the
+// correlation adjoint follows the reference's backward kernels
+// (stereo/operators/stereocorrelation.cu:210-350: dL/dfL and dL/dfR of the
+// integer-disparity correlation, zero where x + s_k leaves the row).
+namespace {
+
+// Forward: out[oy][ox][co] = b[co] + sum_{ky,kx,ci} w[co][ci][kh-1-ky][kw-1-kx] in[oy+ky][ox+kx][ci].
+// dz = dL/d(pre-activation output) [Ho][Wo][Cout].  Adds to dw (npz layout)
+// and db (may be null); writes din [H][W][Cin] when non-null.
+void conv_backward_d(const double *in, int H, int W, int Cin, const float *w, int Cout, int kh, int kw,
+                     const double *dz, double *dw, double *db, double *din)
+{
+    const int Ho = H - kh + 1, Wo = W - kw + 1;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int co = 0; co < Cout; ++co) {
+        for (int ci = 0; ci < Cin; ++ci)
+            for (int ky = 0; ky < kh; ++ky)
+                for (int kx = 0; kx < kw; ++kx) {
+                    double acc = 0;
+                    for (int oy = 0; oy < Ho; ++oy)
+                        for (int ox = 0; ox < Wo; ++ox)
+                            acc += dz[((size_t)oy * Wo + ox) * Cout + co] *
+                                   in[((size_t)(oy + ky) * W + ox + kx) * Cin + ci];
+                    dw[(((size_t)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += acc;
+                }
+        if (db) {
+            double acc = 0;
+            for (long i = 0; i < (long)Ho * Wo; ++i) acc += dz[(size_t)i * Cout + co];
+            db[co] += acc;
+        }
+    }
+    if (!din) return;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int iy = 0; iy < H; ++iy)
+        for (int ix = 0; ix < W; ++ix) {
+            double *d = din + ((size_t)iy * W + ix) * Cin;
+            for (int ci = 0; ci < Cin; ++ci) d[ci] = 0;
+            for (int ky = 0; ky < kh; ++ky) {
+                const int oy = iy - ky;
+                if (oy < 0 || oy >= Ho) continue;
+                for (int kx = 0; kx < kw; ++kx) {
+                    const int ox = ix - kx;
+                    if (ox < 0 || ox >= Wo) continue;
+                    const double *g = dz + ((size_t)oy * Wo + ox) * Cout;
+                    for (int co = 0; co < Cout; ++co)
+                        for (int ci = 0; ci < Cin; ++ci)
+                            d[ci] += g[co] * (double)w[(((size_t)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)];
+                }
+            }
+        }
+}
+
+// dz = dy * (1 - y^2), the tanh adjoint
+void tanh_backward(const std::vector<double> &y, std::vector<double> &dy)
+{
+    for (size_t i = 0; i < y.size(); ++i) dy[i] *= 1.0 - y[i] * y[i];
+}
+
+size_t slot_size(const oracle_cfg *cfg, int i)
+{
+    int64_t s[4];
+    int nd = 0;
+    oracle_param_shape(cfg, i, s, &nd);
+    size_t n = 1;
+    for (int k = 0; k < nd; ++k) n *= (size_t)s[k];
+    return n;
+}
+
+} // namespace
+
+extern "C" {
+
+/* grads[i]: slot i's gradient, slot_size doubles each, overwritten.
+ * Returns 0, or 3 (unary is not one-minus-dot), 4 (fractional list), 1/2 (shape). */
+int oracle_predict_backward(const oracle_cfg *cfg, const float *const *params, const float *lp, const float *rp,
+                            int w, int h, const float *list, int D, const double *gvol, const double *gpw,
+                            double *const *grads)
+{
+    if (cfg->unary != 1) return 3;
+    if (oracle_disp_is_float(list, D)) return 4;
+    const int p = oracle_padding(cfg);
+    if (p < 0) return 1;
+    const int H = h - 2 * p, W = w - 2 * p, ic = cfg->in_channels, C = cfg->feat_channels;
+    const int np = oracle_num_params(cfg);
+    for (int i = 0; i < np; ++i) std::fill(grads[i], grads[i] + slot_size(cfg, i), 0.0);
+    auto layers = feature_layers(cfg);
+    const int L = (int)layers.size();
+    // forward, keeping every layer's output
+    std::vector<double> norm[2];
+    std::vector<std::vector<double>> acts[2];
+    std::vector<int> hs(L + 1), ws(L + 1);
+    const float *img[2] = {lp, rp};
+    for (int s = 0; s < 2; ++s) {
+        norm[s].resize((size_t)w * h * ic);
+        normalize_T<double>(img[s], w, h, ic, norm[s].data());
+        acts[s].assign(L + 1, {});
+        acts[s][0] = norm[s];
+        int ch = h, cw = w;
+        hs[0] = h, ws[0] = w;
+        for (int l = 0; l < L; ++l) {
+            const Layer &Ly = layers[l];
+            const int oh = ch - Ly.kh + 1, ow = cw - Ly.kw + 1;
+            acts[s][l + 1].assign((size_t)oh * ow * Ly.cout, 0.0);
+            conv_T<double>(acts[s][l].data(), ch, cw, Ly.cin, params[Ly.wslot], params[Ly.bslot], Ly.cout, Ly.kh,
+                           Ly.kw, 1, acts[s][l + 1].data());
+            ch = oh, cw = ow;
+            hs[l + 1] = ch, ws[l + 1] = cw;
+        }
+        if (ch != H || cw != W) return 2;
+    }
+    // L2 normalisation (kept: f and the norms)
+    std::vector<double> f[2], nrm[2];
+    for (int s = 0; s < 2; ++s) {
+        f[s] = acts[s][L];
+        nrm[s].assign((size_t)H * W, 0.0);
+        for (long i = 0; i < (long)H * W; ++i) {
+            double *q = f[s].data() + i * C;
+            double ss = 0;
+            for (int c = 0; c < C; ++c) ss = std::fma(q[c], q[c], ss);
+            const double n = std::sqrt(ss);
+            nrm[s][i] = n;
+            for (int c = 0; c < C; ++c) q[c] = n > 0 ? q[c] / n : 0.0;
+        }
+    }
+    // correlation adjoint: vol = 1 - C, so dC = -gvol
+    std::vector<double> df[2];
+    df[0].assign((size_t)H * W * C, 0.0);
+    df[1].assign((size_t)H * W * C, 0.0);
+#pragma omp parallel for
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x)
+            for (int k = 0; k < D; ++k) {
+                const int xs = x + (int)list[k];
+                if (xs < 0 || xs > W - 1) continue;
+                const double g = -gvol[((size_t)y * W + x) * D + k];
+                const double *a = f[0].data() + ((size_t)y * W + x) * C;
+                const double *b = f[1].data() + ((size_t)y * W + xs) * C;
+                double *da = df[0].data() + ((size_t)y * W + x) * C;
+                double *dbb = df[1].data() + ((size_t)y * W + xs) * C;
+                for (int c = 0; c < C; ++c) {
+                    da[c] += g * b[c];
+                    dbb[c] += g * a[c];
+                }
+            }
+    // through the normalisation, the tanh layers and the convolutions of both images
+    for (int s = 0; s < 2; ++s) {
+        std::vector<double> dy((size_t)H * W * C);
+        for (long i = 0; i < (long)H * W; ++i) {
+            const double *q = f[s].data() + i * C, *g = df[s].data() + i * C;
+            double dot = 0;
+            for (int c = 0; c < C; ++c) dot += q[c] * g[c];
+            const double n = nrm[s][i];
+            for (int c = 0; c < C; ++c) dy[(size_t)i * C + c] = n > 0 ? (g[c] - q[c] * dot) / n : 0.0;
+        }
+        for (int l = L - 1; l >= 0; --l) {
+            const Layer &Ly = layers[l];
+            tanh_backward(acts[s][l + 1], dy);
+            std::vector<double> din;
+            if (l > 0) din.assign((size_t)hs[l] * ws[l] * Ly.cin, 0.0);
+            conv_backward_d(acts[s][l].data(), hs[l], ws[l], Ly.cin, params[Ly.wslot], Ly.cout, Ly.kh, Ly.kw,
+                            dy.data(), grads[Ly.wslot], grads[Ly.bslot], l > 0 ? din.data() : nullptr);
+            dy.swap(din);
+        }
+    }
+    if (cfg->with_pairwise && gpw) {
+        const int cr = p - 2, pc = ic == 1 ? 1 : 3, ph = H + 4, pww = W + 4;
+        std::vector<double> pin((size_t)ph * pww * pc);
+        for (int y = 0; y < ph; ++y)
+            for (int x = 0; x < pww; ++x)
+                for (int c = 0; c < pc; ++c)
+                    pin[((size_t)y * pww + x) * pc + c] = norm[0][((size_t)(y + cr) * w + x + cr) * ic + c];
+        auto pl = pairwise_layers(cfg);
+        const Layer &A = pl[0], &B = pl[1], &Hd = pl[2];
+        std::vector<double> y1((size_t)(H + 2) * (W + 2) * A.cout), y2((size_t)H * W * B.cout), hh((size_t)H * W * 2);
+        conv_T<double>(pin.data(), ph, pww, A.cin, params[A.wslot], params[A.bslot], A.cout, 3, 3, 1, y1.data());
+        conv_T<double>(y1.data(), H + 2, W + 2, B.cin, params[B.wslot], params[B.bslot], B.cout, 3, 3, 1, y2.data());
+        conv_T<double>(y2.data(), H, W, Hd.cin, params[Hd.wslot], nullptr, 2, 1, 1, 0, hh.data());
+        std::vector<double> gh((size_t)H * W * 2);
+        for (long i = 0; i < (long)H * W; ++i)
+            for (int o = 0; o < 2; ++o) {
+                const double v = hh[(size_t)i * 2 + o];
+                const double sg = v > 0 ? 1.0 : (v < 0 ? -1.0 : 0.0); // d|v|/dv
+                gh[(size_t)i * 2 + o] = gpw[(size_t)o * H * W + i] * sg;
+            }
+        std::vector<double> dy2((size_t)H * W * B.cout), dy1((size_t)(H + 2) * (W + 2) * A.cout);
+        conv_backward_d(y2.data(), H, W, Hd.cin, params[Hd.wslot], 2, 1, 1, gh.data(), grads[Hd.wslot], nullptr,
+                        dy2.data());
+        tanh_backward(y2, dy2);
+        conv_backward_d(y1.data(), H + 2, W + 2, B.cin, params[B.wslot], B.cout, 3, 3, dy2.data(), grads[B.wslot],
+                        grads[B.bslot], dy1.data());
+        tanh_backward(y1, dy1);
+        conv_backward_d(pin.data(), ph, pww, A.cin, params[A.wslot], A.cout, 3, 3, dy1.data(), grads[A.wslot],
+                        grads[A.bslot], nullptr);
+    }
+    return 0;
+}
+
+} // extern "C"

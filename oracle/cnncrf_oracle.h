@@ -134,6 +134,14 @@ int oracle_run_pair(const oracle_cfg *cfg, const float *const *params, const flo
                     const float *right, int W, int H, float *disp, int32_t *labels, float *vol,
                     float *wx, float *wy, double *lb);
 
+/* Backward of oracle_predict in FP64 (one-minus-dot unary, integer lists):
+ * gvol = dL/dvol (H x W x D), gpw = dL/dpw ([2][H][W], may be NULL) -> grads[i],
+ * slot i's gradient in its npz layout (doubles, overwritten).  Returns 0, or
+ * 3 (unary not one-minus-dot), 4 (fractional list), 1 / 2 (shape). */
+int oracle_predict_backward(const oracle_cfg *cfg, const float *const *params, const float *left_pad,
+                            const float *right_pad, int w, int h, const float *list, int D,
+                            const double *gvol, const double *gpw, double *const *grads);
+
 #ifdef __cplusplus
 }
 #endif

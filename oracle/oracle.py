@@ -72,6 +72,8 @@ def lib():
         L.oracle_unary.restype = None
         L.oracle_disparity_list.argtypes = [C.c_float, C.c_float, C.c_float, C.c_void_p, C.c_int]
         L.oracle_disp_is_float.argtypes = [f32p, C.c_int]
+        L.oracle_predict_backward.argtypes = [cp, C.c_void_p, f32p, f32p, C.c_int, C.c_int, f32p, C.c_int, f64p,
+                                              C.c_void_p, C.c_void_p]
         L.oracle_predict.argtypes = [cp, C.c_void_p, f32p, f32p, C.c_int, C.c_int, f32p, C.c_int,
                                      C.c_void_p, C.c_void_p]
         L.oracle_crf.argtypes = [f32p, f32p, f32p, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
@@ -227,6 +229,65 @@ def predict(cfg, params, left_pad, right_pad, lst):
     if rc:
         raise RuntimeError("oracle_predict failed: %d" % rc)
     return vol, pw
+
+
+def predict_backward(cfg, params, left_pad, right_pad, lst, gvol, gpw=None):
+    """FP64 parameter gradients (npz layouts) of sum(gvol * vol) + sum(gpw * pw)."""
+    h, w = left_pad.shape[:2]
+    grads = [np.zeros(np.shape(p), np.float64) for p in params]
+    gptr = (C.c_void_p * len(grads))(*[g.ctypes.data for g in grads])
+    ptrs, keep = _param_array(params)
+    gp = None if gpw is None else np.ascontiguousarray(gpw, np.float64)
+    rc = lib().oracle_predict_backward(C.byref(cfg), ptrs, np.ascontiguousarray(left_pad, np.float32).reshape(-1),
+                                       np.ascontiguousarray(right_pad, np.float32).reshape(-1), w, h,
+                                       np.ascontiguousarray(lst, np.float32), len(lst),
+                                       np.ascontiguousarray(gvol, np.float64).reshape(-1),
+                                       None if gp is None else gp.ctypes.data_as(C.c_void_p), gptr)
+    if rc:
+        raise RuntimeError("oracle_predict_backward failed: %d" % rc)
+    return grads
+
+
+def rho_table(L1, L2, delta, shape):
+    """rho(|t|) of the CRF spec: 0 at 0, min(L1, L2) (step) or min(L1 t, L2)
+    (linear) up to delta, L2 beyond; float32 like the solver."""
+    r = np.full(257, np.float32(L2), np.float32)
+    r[0] = 0.0
+    for t in range(1, int(delta) + 1):
+        r[t] = min(np.float32(L1), np.float32(L2)) if shape == 0 else min(np.float32(L1) * np.float32(t),
+                                                                           np.float32(L2))
+    return r
+
+
+def hinge(vol, pw, gt, lam, L1, L2, delta, iters, shape=1, slack=0.5):
+    """Structured hinge with margin 1 per mislabelled pixel for one pair.
+
+    E(y) = sum_i vol[i, y_i] + sum_edges lam * pw * rho(|y_i - y_j|);
+    y_hat = the CRF's labelling of the loss-augmented energy, whose unary is
+    vol + 1 at the ground-truth label (the same minimiser as vol - [k != gt]);
+    loss = E(gt) - E(y_hat) + #(y_hat != gt).  Returns loss, y_hat, dL/dvol
+    (+1 at gt, -1 at y_hat) and dL/dpw = lam * (rho at gt - rho at y_hat) per
+    edge (wx on x -> x+1, wy on y -> y+1)."""
+    vol = np.ascontiguousarray(vol, np.float32)
+    H, W, D = vol.shape
+    gt = np.ascontiguousarray(gt, np.int32)
+    aug = vol.copy()
+    aug[np.arange(H)[:, None], np.arange(W)[None, :], gt] += np.float32(1.0)
+    wx = (np.float32(lam) * pw[0]).astype(np.float32)
+    wy = (np.float32(lam) * pw[1]).astype(np.float32)
+    yh, _, _, _ = crf(aug, wx, wy, L1, L2, delta, iters, shape=shape, slack=slack)
+    e_gt = energy(vol, wx, wy, gt, L1, L2, delta, shape)
+    e_hat = energy(vol, wx, wy, yh, L1, L2, delta, shape)
+    loss = e_gt - e_hat + float((yh != gt).sum())
+    gvol = np.zeros((H, W, D), np.float64)
+    ii, jj = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    gvol[ii, jj, gt] += 1.0
+    gvol[ii, jj, yh] -= 1.0
+    r = rho_table(L1, L2, delta, shape).astype(np.float64)
+    gpw = np.zeros((2, H, W), np.float64)
+    gpw[0, :, :-1] = lam * (r[np.abs(gt[:, 1:] - gt[:, :-1])] - r[np.abs(yh[:, 1:] - yh[:, :-1])])
+    gpw[1, :-1, :] = lam * (r[np.abs(gt[1:, :] - gt[:-1, :])] - r[np.abs(yh[1:, :] - yh[:-1, :])])
+    return loss, yh, gvol, gpw
 
 
 def crf(cost, wx, wy, L1, L2, delta, iters, shape=0, slack=0.5, threads=0, want_c1=False):
