@@ -45,6 +45,13 @@ class CrfTile(C.Structure):
                 ("chains_per_cta_v", C.c_int)]
 
 
+class TrainDesc(C.Structure):
+    _fields_ = [("num_layers", C.c_int), ("topology", C.c_int), ("feat_channels", C.c_int), ("pw_channels", C.c_int),
+                ("disp_min", C.c_float), ("disp_step", C.c_float), ("disp_max", C.c_float), ("lam", C.c_float),
+                ("L1", C.c_float), ("L2", C.c_float), ("delta", C.c_int), ("crf_shape", C.c_int),
+                ("crf_slack", C.c_float), ("crf_iters", C.c_int)]
+
+
 class StereoOptions(C.Structure):
     _fields_ = [("precision", C.c_int), ("unary", C.c_int), ("topology", C.c_int),
                 ("feat_channels", C.c_int), ("pw_channels", C.c_int),
@@ -153,6 +160,23 @@ PROTOS = {
     "cnncrf_batch_autotune": ([vp, f32, f32, f32, i32, f32], i32),
     "cnncrf_batch_num_groups": ([vp, C.POINTER(i32)], i32),
     "cnncrf_batch_group_shape": ([vp, i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(i32)], i32),
+    "cnncrf_train_default_desc": ([C.POINTER(TrainDesc)], i32),
+    "cnncrf_train_create": ([C.POINTER(vp), C.POINTER(TrainDesc), i32, i32, i32], i32),
+    "cnncrf_train_destroy": ([vp], i32),
+    "cnncrf_train_set_stream": ([vp, vp], i32),
+    "cnncrf_train_num_params": ([vp, C.POINTER(i32)], i32),
+    "cnncrf_train_param_shape": ([vp, i32, C.POINTER(C.c_int64), C.POINTER(i32)], i32),
+    "cnncrf_train_init_xavier": ([vp, C.c_uint64], i32),
+    "cnncrf_train_set_param": ([vp, i32, vp, C.c_size_t], i32),
+    "cnncrf_train_get_param": ([vp, i32, vp, C.c_size_t], i32),
+    "cnncrf_train_get_grad": ([vp, i32, vp, C.c_size_t], i32),
+    "cnncrf_train_forward": ([vp, vp, vp], i32),
+    "cnncrf_train_outputs": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32)], i32),
+    "cnncrf_train_hinge": ([vp, vp, C.POINTER(C.c_double), vp], i32),
+    "cnncrf_train_hinge_grads": ([vp, C.POINTER(vp), C.POINTER(vp)], i32),
+    "cnncrf_train_backward": ([vp, vp, vp], i32),
+    "cnncrf_train_sgd": ([vp, f32, f32], i32),
+    "cnncrf_train_step": ([vp, vp, vp, vp, f32, f32, C.POINTER(C.c_double)], i32),
     "cnncrf_kernel_launches": ([C.POINTER(C.c_uint64)], i32),
     "cnncrf_profile_enable": ([i32], i32),
     "cnncrf_profile_reset": ([], i32),

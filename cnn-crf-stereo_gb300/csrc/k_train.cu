@@ -1,0 +1,499 @@
+// k_train.cu -- the kernels of the training step: weight layouts from the
+// npz layout, the adjoints of tanh, the L2 normalisation, the correlation,
+// the convolutions (weight gradient here, input gradient through conv_simt on
+// the zero-padded output gradient) and the pairwise head, the structured
+// hinge's subgradient and the SGD-with-momentum update.
+//
+// The reference ships no training code; its only gradient code is the
+// correlation's backward (stereo/operators/stereocorrelation.cu:210-350),
+// whose integer-disparity form the correlation adjoint here follows: dL/dfL
+// and dL/dfR of C[y][x][k] = <fL(y, x), fR(y, x + s_k)>, zero where x + s_k
+// leaves the row.  Everything is FP32 with fixed reduction orders (weight and
+// bias gradients sum fixed pixel chunks, then the chunks in order), so a step
+// is deterministic run to run.
+#include <algorithm>
+#include <cfloat>
+
+#include "common.h"
+#include "kernels.h"
+
+namespace cnncrf {
+namespace k {
+
+namespace {
+
+// ------------------------------------------------------------ weight layouts
+// forward (conv_simt): wt[(ky*kw + kx)*Cin + ci][co] = w[co][ci][kh-1-ky][kw-1-kx], [K][128]
+__global__ void k_w_fwd(const float *__restrict__ w, int Cout, int Cin, int kh, int kw, float *__restrict__ wt)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x, K = (long)kh * kw * Cin;
+    if (i >= K * 128) return;
+    const int k = (int)(i / 128), co = (int)(i % 128);
+    const int ci = k % Cin, t = k / Cin, kx = t % kw, ky = t / kw;
+    wt[i] = co < Cout ? w[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] : 0.0f;
+}
+
+// input gradient as conv_simt on the output gradient padded by (kh-1, kw-1):
+// wd[(ky*kw + kx)*Cout + co][ci] = w[co][ci][ky][kx], [kh*kw*Cout][128]
+__global__ void k_w_dgrad(const float *__restrict__ w, int Cout, int Cin, int kh, int kw, float *__restrict__ wd)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x, K = (long)kh * kw * Cout;
+    if (i >= K * 128) return;
+    const int k = (int)(i / 128), ci = (int)(i % 128);
+    const int co = k % Cout, t = k / Cout, kx = t % kw, ky = t / kw;
+    wd[i] = ci < Cin ? w[(((long)co * Cin + ci) * kh + ky) * kw + kx] : 0.0f;
+}
+
+__global__ void k_pad128(const float *__restrict__ b, int n, float *__restrict__ out)
+{
+    const int i = threadIdx.x;
+    if (i < 128) out[i] = i < n ? b[i] : 0.0f;
+}
+
+// ------------------------------------------------------------ elementwise
+__global__ void k_tanh_bwd(float *__restrict__ dy, const float *__restrict__ y, long n)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float v = y[i];
+        dy[i] = dy[i] * (1.0f - v * v);
+    }
+}
+
+// out [n][H + 2p][W + 2q][C] = in [n][H][W][C] with a zero border
+__global__ void k_pad_zero(const float *__restrict__ in, int H, int W, int C, int p, int q, float *__restrict__ out)
+{
+    const int Hp = H + 2 * p, Wp = W + 2 * q;
+    const long per = (long)Hp * Wp * C;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int img = blockIdx.y;
+    if (i >= per) return;
+    const int c = (int)(i % C);
+    const long px = i / C;
+    const int x = (int)(px % Wp) - q, y = (int)(px / Wp) - p;
+    out[(long)img * per + i] =
+        (x >= 0 && x < W && y >= 0 && y < H) ? in[(((long)img * H + y) * W + x) * C + c] : 0.0f;
+}
+
+// f = y / |y| per pixel; dy = (df - y <y, df> / |y|^2) / |y|, zero where |y| = 0.  A warp per pixel.
+__global__ void k_l2norm_bwd(const float *__restrict__ y, const float *__restrict__ df, long npx, int C,
+                             float *__restrict__ dy)
+{
+    const long px = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (px >= npx) return;
+    const float *yp = y + px * C, *gp = df + px * C;
+    float ss = 0.0f, dot = 0.0f;
+    for (int c = lane; c < C; c += 32) {
+        ss = fmaf(yp[c], yp[c], ss);
+        dot = fmaf(yp[c], gp[c], dot);
+    }
+    for (int o = 16; o; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        dot += __shfl_xor_sync(0xffffffffu, dot, o);
+    }
+    const float n = sqrtf(ss);
+    for (int c = lane; c < C; c += 32)
+        dy[px * C + c] = n > 0.0f ? (gp[c] - yp[c] * (dot / ss)) / n : 0.0f;
+}
+
+// ------------------------------------------------------------ correlation adjoint
+// Left: dfl[x][c] = -sum_k gvol[x][k] fr[x + s_k][c].  A CTA per (32-pixel
+// tile, row, pair); thread c; the right features of the tile's band in shared memory.
+__global__ void k_corr_bwd_left(const float *__restrict__ fr, const float *__restrict__ gvol,
+                                const float *__restrict__ list, int H, int W, int C, int D, int omin, int span,
+                                float *__restrict__ dfl)
+{
+    extern __shared__ float win[]; // [span][C], column j = pixel x0 + omin + j
+    int *s = (int *)(win + (size_t)span * C);
+    const int x0 = blockIdx.x * 32, y = blockIdx.y, pair = blockIdx.z;
+    const long row = ((long)pair * H + y) * W;
+    for (int i = threadIdx.x; i < D; i += blockDim.x) s[i] = (int)list[i];
+    for (int i = threadIdx.x; i < span * C; i += blockDim.x) {
+        const int xs = x0 + omin + i / C, c = i % C;
+        win[i] = (xs >= 0 && xs < W) ? fr[(row + xs) * C + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    for (int i = 0; i < 32 && x0 + i < W; ++i) {
+        const int x = x0 + i;
+        const float *g = gvol + (row + x) * D;
+        float acc = 0.0f;
+        for (int k = 0; k < D; ++k) {
+            const int xs = x + s[k];
+            if (xs >= 0 && xs < W) acc = fmaf(g[k], win[(size_t)(xs - x0 - omin) * C + c], acc);
+        }
+        dfl[(row + x) * C + c] = -acc;
+    }
+}
+
+// Right: dfr[x'][c] = -sum_k gvol[x' - s_k][k] fl[x' - s_k][c] over x' - s_k in
+// [0, W); the left features x' - omax .. x' + 31 - omin in shared memory.
+__global__ void k_corr_bwd_right(const float *__restrict__ fl, const float *__restrict__ gvol,
+                                 const float *__restrict__ list, int H, int W, int C, int D, int omax, int span,
+                                 float *__restrict__ dfr)
+{
+    extern __shared__ float win[]; // [span][C], column j = pixel x0 - omax + j
+    int *s = (int *)(win + (size_t)span * C);
+    const int x0 = blockIdx.x * 32, y = blockIdx.y, pair = blockIdx.z;
+    const long row = ((long)pair * H + y) * W;
+    for (int i = threadIdx.x; i < D; i += blockDim.x) s[i] = (int)list[i];
+    for (int i = threadIdx.x; i < span * C; i += blockDim.x) {
+        const int x = x0 - omax + i / C, c = i % C;
+        win[i] = (x >= 0 && x < W) ? fl[(row + x) * C + c] : 0.0f;
+    }
+    __syncthreads();
+    const int c = threadIdx.x;
+    if (c >= C) return;
+    for (int i = 0; i < 32 && x0 + i < W; ++i) {
+        const int xr = x0 + i;
+        float acc = 0.0f;
+        for (int k = 0; k < D; ++k) {
+            const int x = xr - s[k];
+            if (x >= 0 && x < W) acc = fmaf(gvol[(row + x) * D + k], win[(size_t)(x - x0 + omax) * C + c], acc);
+        }
+        dfr[(row + xr) * C + c] = -acc;
+    }
+}
+
+// ------------------------------------------------------------ weight gradient
+// part[split][co][k] = sum over the split's pixels p of dz[p][co] * A[p][k],
+// A[p][(ky*kw + kx)*Cin + ci] = in(img, oy + ky, ox + kx, ci).  A CTA per
+// (64-wide k tile, split); 256 threads, 8 co x 4 k each; 32 pixels staged per step.
+struct WgradArgs {
+    const float *dz;
+    int Cout;
+    const float *in;
+    long in_pix, in_row, in_img;
+    int Cin, kh, kw, Ho, Wo;
+    long P, chunk;
+    float *part;
+};
+
+constexpr int WG_PX = 32, WG_KT = 64;
+
+__global__ void __launch_bounds__(256) k_wgrad(const WgradArgs a)
+{
+    __shared__ float As[WG_PX][128];
+    __shared__ float Bs[WG_PX][WG_KT];
+    const int K = a.kh * a.kw * a.Cin;
+    const int kt0 = blockIdx.x * WG_KT, split = blockIdx.y;
+    const long p0 = (long)split * a.chunk, p1 = min(a.P, p0 + a.chunk);
+    const int t = threadIdx.x, cb = (t & 15) * 8, kb = (t >> 4) * 4;
+    float acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+    for (long pb = p0; pb < p1; pb += WG_PX) {
+        for (int i = t; i < WG_PX * 128; i += 256) {
+            const int pp = i / 128, co = i % 128;
+            const long p = pb + pp;
+            As[pp][co] = (p < p1 && co < a.Cout) ? a.dz[p * a.Cout + co] : 0.0f;
+        }
+        for (int i = t; i < WG_PX * WG_KT; i += 256) {
+            const int pp = i / WG_KT, kk = kt0 + i % WG_KT;
+            const long p = pb + pp;
+            float v = 0.0f;
+            if (p < p1 && kk < K) {
+                const int ci = kk % a.Cin, tt = kk / a.Cin, kx = tt % a.kw, ky = tt / a.kw;
+                const long img = p / ((long)a.Ho * a.Wo), r = p - img * a.Ho * a.Wo;
+                const int oy = (int)(r / a.Wo), ox = (int)(r % a.Wo);
+                v = a.in[img * a.in_img + (long)(oy + ky) * a.in_row + (long)(ox + kx) * a.in_pix + ci];
+            }
+            Bs[pp][i % WG_KT] = v;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int pp = 0; pp < WG_PX; ++pp) {
+            float av[8], bv[4];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) av[i] = As[pp][cb + i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) bv[j] = Bs[pp][kb + j];
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int co = cb + i, kk = kt0 + kb + j;
+            if (co < a.Cout && kk < K) a.part[((long)split * a.Cout + co) * K + kk] = acc[i][j];
+        }
+}
+
+// dw[co][ci][kh-1-ky][kw-1-kx] += sum_split part[split][co][k], splits in order
+__global__ void k_wgrad_reduce(const float *__restrict__ part, int nsplit, int Cout, int Cin, int kh, int kw,
+                               float *__restrict__ dw)
+{
+    const int K = kh * kw * Cin;
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)Cout * K) return;
+    const int co = (int)(i / K), k = (int)(i % K);
+    float s = 0.0f;
+    for (int sp = 0; sp < nsplit; ++sp) s += part[((long)sp * Cout + co) * K + k];
+    const int ci = k % Cin, t = k / Cin, kx = t % kw, ky = t / kw;
+    dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += s;
+}
+
+// db[co] += sum_p dz[p][co]: per split a partial, then the splits in order
+__global__ void k_bias_part(const float *__restrict__ dz, int Cout, long P, long chunk, float *__restrict__ part)
+{
+    const int co = threadIdx.x, split = blockIdx.x;
+    if (co >= Cout) return;
+    const long p0 = (long)split * chunk, p1 = min(P, p0 + chunk);
+    float s = 0.0f;
+    for (long p = p0; p < p1; ++p) s += dz[p * Cout + co];
+    part[(long)split * Cout + co] = s;
+}
+
+__global__ void k_bias_reduce(const float *__restrict__ part, int nsplit, int Cout, float *__restrict__ db)
+{
+    const int co = threadIdx.x;
+    if (co >= Cout) return;
+    float s = 0.0f;
+    for (int sp = 0; sp < nsplit; ++sp) s += part[(long)sp * Cout + co];
+    db[co] += s;
+}
+
+// ------------------------------------------------------------ pairwise head adjoint
+// pw = |h|, h[o] = sum_c wh[o][c] y2[c]: gh[o] = gpw[o] sign(h[o]); dy2[c] = sum_o wh[o][c] gh[o]
+__global__ void k_head_bwd(const float *__restrict__ y2, const float *__restrict__ wh, const float *__restrict__ gpw,
+                           int npx, int P, float *__restrict__ gh, float *__restrict__ dy2)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, img = blockIdx.y;
+    if (p >= npx) return;
+    const long q = (long)img * npx + p;
+    const float *v = y2 + q * P;
+    float h0 = 0.0f, h1 = 0.0f;
+    for (int c = 0; c < P; ++c) {
+        h0 = fmaf(wh[c], v[c], h0);
+        h1 = fmaf(wh[P + c], v[c], h1);
+    }
+    const float a0 = gpw[(long)img * 2 * npx + p], a1 = gpw[((long)img * 2 + 1) * npx + p];
+    const float g0 = h0 > 0.0f ? a0 : (h0 < 0.0f ? -a0 : 0.0f);
+    const float g1 = h1 > 0.0f ? a1 : (h1 < 0.0f ? -a1 : 0.0f);
+    gh[q * 2] = g0;
+    gh[q * 2 + 1] = g1;
+    for (int c = 0; c < P; ++c) dy2[q * P + c] = fmaf(wh[c], g0, wh[P + c] * g1);
+}
+
+// ------------------------------------------------------------ structured hinge
+// aug = vol, + 1 at the ground-truth label (invalid labels: counted in err, left out)
+__global__ void k_augment(const float *__restrict__ vol, const int32_t *__restrict__ gt, long npx, int D,
+                          float *__restrict__ aug, int *__restrict__ err)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= npx * D) return;
+    const long px = i / D;
+    const int k = (int)(i % D), g = gt[px];
+    if (k == 0 && (g < 0 || g >= D)) atomicAdd(err, 1);
+    aug[i] = k == g ? vol[i] + 1.0f : vol[i];
+}
+
+__device__ __forceinline__ float rho_of(const float *rho, int delta, float L2, int t)
+{
+    t = t < 0 ? -t : t;
+    return t == 0 ? 0.0f : (t <= delta ? rho[t] : L2);
+}
+
+struct HingeArgs {
+    const float *vol, *w; // unary volume, lambda * pw ([n][2][H][W])
+    const int32_t *gt, *yh;
+    int W, H, D;
+    float lam, L2;
+    int delta;
+    float rho[9];
+    float *gvol, *gpw; // gvol zeroed by the caller
+    double *contrib;   // per pixel: its unary, margin and right / down edge terms of E(gt) - E(yh) + margin
+};
+
+__global__ void k_hinge(const HingeArgs a)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, img = blockIdx.z;
+    if (x >= a.W) return;
+    const long N = (long)a.W * a.H, i = (long)y * a.W + x, q = (long)img * N + i;
+    const int g = a.gt[q], h = a.yh[q];
+    float gx = 0.0f, gy = 0.0f;
+    double c = 0.0;
+    if (g >= 0 && g < a.D && h >= 0 && h < a.D) { // invalid labels are reported by k_augment
+        float *gv = a.gvol + q * a.D;
+        gv[g] += 1.0f;
+        gv[h] -= 1.0f;
+        c = (double)a.vol[q * a.D + g] - (double)a.vol[q * a.D + h] + (g != h ? 1.0 : 0.0);
+        const float *wx = a.w + (long)img * 2 * N, *wy = wx + N;
+        if (x + 1 < a.W) {
+            const int g2 = a.gt[q + 1], h2 = a.yh[q + 1];
+            if (g2 >= 0 && g2 < a.D && h2 >= 0 && h2 < a.D) {
+                const float rg = rho_of(a.rho, a.delta, a.L2, g - g2), rh = rho_of(a.rho, a.delta, a.L2, h - h2);
+                gx = a.lam * (rg - rh);
+                c += (double)wx[i] * (double)rg - (double)wx[i] * (double)rh;
+            }
+        }
+        if (y + 1 < a.H) {
+            const int g2 = a.gt[q + a.W], h2 = a.yh[q + a.W];
+            if (g2 >= 0 && g2 < a.D && h2 >= 0 && h2 < a.D) {
+                const float rg = rho_of(a.rho, a.delta, a.L2, g - g2), rh = rho_of(a.rho, a.delta, a.L2, h - h2);
+                gy = a.lam * (rg - rh);
+                c += (double)wy[i] * (double)rg - (double)wy[i] * (double)rh;
+            }
+        }
+    }
+    a.gpw[(long)img * 2 * N + i] = gx;
+    a.gpw[((long)img * 2 + 1) * N + i] = gy;
+    a.contrib[q] = c;
+}
+
+// rows[r] = sum of row r's W contributions, left to right
+__global__ void k_row_sums_d(const double *__restrict__ c, long rows, int W, double *__restrict__ out)
+{
+    const long r = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    double s = 0.0;
+    for (int x = 0; x < W; ++x) s += c[r * W + x];
+    out[r] = s;
+}
+
+// ------------------------------------------------------------ SGD with momentum
+// v = mu v + g; theta -= lr v (the torch.optim.SGD convention, no dampening)
+__global__ void k_sgd(float *__restrict__ theta, const float *__restrict__ g, float *__restrict__ v, long n,
+                      float lr, float mu)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float nv = fmaf(mu, v[i], g[i]);
+    v[i] = nv;
+    theta[i] = fmaf(-lr, nv, theta[i]);
+}
+
+} // namespace
+
+int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int kh, int kw, float *wt, float *wd,
+                         float *b128, cudaStream_t st)
+{
+    const long K = (long)kh * kw * Cin, Kd = (long)kh * kw * Cout;
+    if (wt) k_w_fwd<<<ceil_div(K * 128, 256), 256, 0, st>>>(w, Cout, Cin, kh, kw, wt);
+    if (wd) k_w_dgrad<<<ceil_div(Kd * 128, 256), 256, 0, st>>>(w, Cout, Cin, kh, kw, wd);
+    if (b && b128) k_pad128<<<1, 128, 0, st>>>(b, Cout, b128);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_tanh_bwd(float *dy, const float *y, long n, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("tanh_bwd", st);
+        k_tanh_bwd<<<ceil_div(n, 256), 256, 0, st>>>(dy, y, n);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_pad_zero(const float *in, int nimg, int H, int W, int C, int p, int q, float *out, cudaStream_t st)
+{
+    const long per = (long)(H + 2 * p) * (W + 2 * q) * C;
+    k_pad_zero<<<dim3(ceil_div(per, 256), nimg), 256, 0, st>>>(in, H, W, C, p, q, out);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_l2norm_bwd(const float *y, const float *df, long npx, int C, float *dy, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("l2norm_bwd", st);
+        k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>(y, df, npx, C, dy);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_corr_bwd(const float *fl, const float *fr, const float *gvol, const float *d_list, int npairs, int H, int W,
+                   int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st)
+{
+    if (C > 128) return fail(CNNCRF_EINVAL, "corr_bwd: %d channels > 128", C);
+    const int span = 32 + omax - omin;
+    const size_t smem = sizeof(float) * (size_t)span * C + sizeof(int) * (size_t)D;
+    if (smem > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "corr_bwd: band %d too wide", omax - omin);
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_left, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_right, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const dim3 g(ceil_div(W, 32), H, npairs);
+    {
+        CNNCRF_PROF("corr_bwd", st);
+        k_corr_bwd_left<<<g, 128, smem, st>>>(fr, gvol, d_list, H, W, C, D, omin, span, dfl);
+        k_corr_bwd_right<<<g, 128, smem, st>>>(fl, gvol, d_list, H, W, C, D, omax, span, dfr);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_wgrad_splits(long P) { return (int)std::max(1L, std::min(64L, P / 2048)); }
+
+int train_wgrad(const float *dz, int Cout, const float *in, long in_pix, long in_row, long in_img, int Cin, int kh,
+                int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st)
+{
+    if (Cout > 128) return fail(CNNCRF_EINVAL, "wgrad: %d output channels > 128", Cout);
+    WgradArgs a;
+    a.dz = dz, a.Cout = Cout, a.in = in, a.in_pix = in_pix, a.in_row = in_row, a.in_img = in_img;
+    a.Cin = Cin, a.kh = kh, a.kw = kw, a.Ho = Ho, a.Wo = Wo;
+    a.P = (long)nimg * Ho * Wo;
+    const int ns = train_wgrad_splits(a.P);
+    a.chunk = (a.P + ns - 1) / ns;
+    a.part = part;
+    const int K = kh * kw * Cin;
+    {
+        CNNCRF_PROF("wgrad", st);
+        k_wgrad<<<dim3(ceil_div(K, WG_KT), ns), 256, 0, st>>>(a);
+        k_wgrad_reduce<<<ceil_div((long)Cout * K, 256), 256, 0, st>>>(part, ns, Cout, Cin, kh, kw, dw);
+        if (db) {
+            k_bias_part<<<ns, 128, 0, st>>>(dz, Cout, a.P, a.chunk, partb);
+            k_bias_reduce<<<1, 128, 0, st>>>(partb, ns, Cout, db);
+        }
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_head_bwd(const float *y2, const float *wh, const float *gpw, int nimg, int npx, int P, float *gh,
+                   float *dy2, cudaStream_t st)
+{
+    k_head_bwd<<<dim3(ceil_div(npx, 128), nimg), 128, 0, st>>>(y2, wh, gpw, npx, P, gh, dy2);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st)
+{
+    k_augment<<<ceil_div(npx * D, 256), 256, 0, st>>>(vol, gt, npx, D, aug, err);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,
+                int D, float lam, const float rho[9], float L2, int delta, float *gvol, float *gpw, double *contrib,
+                double *rows, cudaStream_t st)
+{
+    HingeArgs a;
+    a.vol = vol, a.w = w, a.gt = gt, a.yh = yh, a.W = W, a.H = H, a.D = D, a.lam = lam, a.L2 = L2, a.delta = delta;
+    for (int t = 0; t < 9; ++t) a.rho[t] = rho[t];
+    a.gvol = gvol, a.gpw = gpw, a.contrib = contrib;
+    k_hinge<<<dim3(ceil_div(W, 128), H, npairs), 128, 0, st>>>(a);
+    k_row_sums_d<<<ceil_div((long)npairs * H, 128), 128, 0, st>>>(contrib, (long)npairs * H, W, rows);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_sgd(float *theta, const float *g, float *v, long n, float lr, float mu, cudaStream_t st)
+{
+    k_sgd<<<ceil_div(n, 256), 256, 0, st>>>(theta, g, v, n, lr, mu);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+} // namespace k
+} // namespace cnncrf

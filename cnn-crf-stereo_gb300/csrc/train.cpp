@@ -1,0 +1,540 @@
+// train.cpp -- the training step (cnncrf_train_*): forward through both
+// nets and the correlation keeping every layer's activations, the structured
+// hinge loss on the CRF's loss-augmented labelling, the backward through the
+// hand-written adjoints (k_train.cu) into every parameter, SGD with momentum
+// on FP32 master weights.
+//
+// No counterpart in the reference, which ships inference only (its weights
+// were trained elsewhere).  The forward is StereoNet::performPrediction
+// (stereo/stereonet.cpp:250-421) on the FP32 kernels of the inference path,
+// so the volume and the pairwise output equal the inference net's bit for
+// bit; padding and normalisation are those of ColorStereoNet::predict
+// (stereo/colorstereonet.cpp:38-77).  One-minus-dot unary, integer disparity
+// list, RGB input.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "../../include/cnncrf.h"
+#include "../../include/cnncrf_xavier.h"
+#include "common.h"
+#include "kernels.h"
+
+using namespace cnncrf;
+
+namespace {
+
+struct TLayer {
+    int cin, cout, kh, kw, act, wslot, bslot;
+    int hin, win;        // input extent
+    DevBuf wt, wd, b128; // conv_simt layout, input-gradient layout, padded bias
+    int hout() const { return hin - kh + 1; }
+    int wout() const { return win - kw + 1; }
+};
+
+size_t al64(size_t x) { return (x + 63) & ~(size_t)63; }
+
+} // namespace
+
+struct cnncrf_train {
+    cnncrf_train_desc d{};
+    int n = 0, H = 0, W = 0, p = 0, h = 0, w = 0, D = 0;
+    const int ic = 3;
+    cudaStream_t st = nullptr;
+    std::vector<TLayer> feat, pw; // pw: conv 3x3, conv 3x3, 1x1 head
+    std::vector<size_t> off, cnt; // slot offset / count in the flat parameter buffers
+    size_t total = 0;
+    DevBuf theta, grad, vel;
+    std::vector<float> list;
+    int omin = 0, omax = 0;
+    DevBuf dlist;
+    // forward state
+    DevBuf padded[2], norm[2], scratch;
+    std::vector<DevBuf> act[2];
+    DevBuf f[2], vol, y1, y2, pwout;
+    bool forwarded = false, hinged = false;
+    // backward and hinge scratch
+    DevBuf gvol, gpw, df[2], dy, dyb, padb, part, partb, gh;
+    DevBuf aug, wts, labels, crfws, contrib, rows, err;
+    size_t crfws_bytes = 0;
+
+    int build();
+    int refresh();
+    int forward(const float *l, const float *r);
+    int hinge(const int32_t *gt, double *loss, int32_t *yh_out);
+    int backward(const float *gv, const float *gp);
+    int layer_back(TLayer &L, const float *in, long in_pix, long in_row, long in_img, const float *y, float *dz,
+                   float *dprev);
+    float *param(int slot) { return theta.as<float>() + off[slot]; }
+    float *gradp(int slot) { return grad.as<float>() + off[slot]; }
+};
+
+int cnncrf_train::build()
+{
+    const int L = d.num_layers, F = d.feat_channels, P = d.pw_channels;
+    const int k = d.topology == CNNCRF_TOPO_REF ? 2 : 3;
+    feat.clear();
+    pw.clear();
+    feat.push_back({ic, F, 3, 3, 1, 0, 1, 0, 0}); // stereo/stereonet.cpp:69-79
+    for (int l = 1; l < L; ++l) feat.push_back({F, F, k, k, 1, 2 * l, 2 * l + 1, 0, 0});
+    int loss = 0;
+    for (auto &Ly : feat) loss += Ly.kh - 1;
+    if (loss % 2) return fail(CNNCRF_EINVAL, "train: receptive-field loss %d is odd", loss);
+    p = loss / 2;
+    if (p < 2) return fail(CNNCRF_EINVAL, "train: the pairwise net needs padding >= 2");
+    h = H + 2 * p, w = W + 2 * p;
+    int ch = h, cw = w;
+    for (auto &Ly : feat) {
+        Ly.hin = ch, Ly.win = cw;
+        ch -= Ly.kh - 1, cw -= Ly.kw - 1;
+    }
+    const int base = 2 * L; // stereo/stereonet.cpp:159-167
+    pw.push_back({3, P, 3, 3, 1, base, base + 1, H + 4, W + 4});
+    pw.push_back({P, P, 3, 3, 1, base + 2, base + 3, H + 2, W + 2});
+    pw.push_back({P, 2, 1, 1, 2, base + 4, -1, H, W});
+    const int np = 2 * L + 5;
+    off.assign(np, 0);
+    cnt.assign(np, 0);
+    for (auto *v : {&feat, &pw})
+        for (auto &Ly : *v) {
+            cnt[Ly.wslot] = (size_t)Ly.cout * Ly.cin * Ly.kh * Ly.kw;
+            if (Ly.bslot >= 0) cnt[Ly.bslot] = Ly.cout;
+        }
+    total = 0;
+    for (int i = 0; i < np; ++i) {
+        off[i] = total;
+        total += al64(cnt[i]);
+    }
+    for (auto *b : {&theta, &grad, &vel}) {
+        CNNCRF_TRY(b->reserve(total * sizeof(float)));
+        CNNCRF_CUDA(cudaMemset(b->get(), 0, total * sizeof(float)));
+    }
+    for (auto *v : {&feat, &pw})
+        for (auto &Ly : *v)
+            if (Ly.act == 1) {
+                CNNCRF_TRY(Ly.wt.reserve(sizeof(float) * (size_t)Ly.kh * Ly.kw * Ly.cin * 128));
+                CNNCRF_TRY(Ly.wd.reserve(sizeof(float) * (size_t)Ly.kh * Ly.kw * Ly.cout * 128));
+                CNNCRF_TRY(Ly.b128.reserve(sizeof(float) * 128));
+            }
+    // the stored list -d (stereo/operators/stereocorrelation.cpp:83-85); integers only
+    list.clear();
+    for (float dd = d.disp_min; dd <= d.disp_max; dd += d.disp_step) {
+        list.push_back(-dd);
+        if (list.size() > 256) return fail(CNNCRF_EINVAL, "train: more than 256 disparities");
+    }
+    if (list.empty()) return fail(CNNCRF_EINVAL, "train: empty disparity range");
+    D = (int)list.size();
+    omin = 1 << 30, omax = -(1 << 30);
+    for (float s : list) {
+        if (s != std::floor(s)) return fail(CNNCRF_EUNSUPPORTED, "train: fractional disparity %g", -s);
+        omin = std::min(omin, (int)s), omax = std::max(omax, (int)s);
+    }
+    CNNCRF_TRY(dlist.reserve(sizeof(float) * D));
+    CNNCRF_CUDA(cudaMemcpy(dlist.get(), list.data(), sizeof(float) * D, cudaMemcpyHostToDevice));
+    // activations
+    const size_t N = (size_t)n * H * W;
+    size_t amax = (size_t)n * h * w * 4;
+    for (int s = 0; s < 2; ++s) {
+        CNNCRF_TRY(padded[s].reserve(sizeof(float) * n * h * w * 4));
+        CNNCRF_TRY(norm[s].reserve(sizeof(float) * n * h * w * ic));
+        act[s].clear();
+        act[s].resize(feat.size());
+        for (size_t l = 0; l < feat.size(); ++l) {
+            const size_t e = (size_t)n * feat[l].hout() * feat[l].wout() * feat[l].cout;
+            CNNCRF_TRY(act[s][l].reserve(sizeof(float) * e));
+            amax = std::max(amax, e);
+        }
+        CNNCRF_TRY(f[s].reserve(sizeof(float) * N * F));
+        CNNCRF_TRY(df[s].reserve(sizeof(float) * N * F));
+    }
+    CNNCRF_TRY(scratch.reserve(k::normalize_scratch_bytes(h, n)));
+    CNNCRF_TRY(vol.reserve(sizeof(float) * N * D));
+    CNNCRF_TRY(y1.reserve(sizeof(float) * n * (H + 2) * (W + 2) * P));
+    CNNCRF_TRY(y2.reserve(sizeof(float) * N * P));
+    CNNCRF_TRY(pwout.reserve(sizeof(float) * N * 2));
+    amax = std::max(amax, (size_t)n * (H + 4) * (W + 4) * P);
+    // backward: dy / dyb hold any layer's output or input gradient, padb a padded output gradient
+    CNNCRF_TRY(dy.reserve(sizeof(float) * amax));
+    CNNCRF_TRY(dyb.reserve(sizeof(float) * amax));
+    CNNCRF_TRY(padb.reserve(sizeof(float) * (size_t)n * (h + 4) * (w + 4) * std::max(F, P)));
+    CNNCRF_TRY(gvol.reserve(sizeof(float) * N * D));
+    CNNCRF_TRY(gpw.reserve(sizeof(float) * N * 2));
+    CNNCRF_TRY(gh.reserve(sizeof(float) * N * 2));
+    long Pmax = 0;
+    int Kmax = 0;
+    for (auto *v : {&feat, &pw})
+        for (auto &Ly : *v) {
+            Pmax = std::max(Pmax, (long)n * Ly.hout() * Ly.wout());
+            Kmax = std::max(Kmax, Ly.kh * Ly.kw * Ly.cin);
+        }
+    const int ns = k::train_wgrad_splits(Pmax); // the most splits any layer uses
+    CNNCRF_TRY(part.reserve(sizeof(float) * (size_t)ns * 128 * Kmax));
+    CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
+    // hinge
+    CNNCRF_TRY(aug.reserve(sizeof(float) * N * D));
+    CNNCRF_TRY(wts.reserve(sizeof(float) * N * 2));
+    CNNCRF_TRY(labels.reserve(sizeof(int32_t) * N));
+    crfws_bytes = k::crf_workspace_bytes(W, H, D, n);
+    CNNCRF_TRY(crfws.reserve(crfws_bytes));
+    CNNCRF_TRY(contrib.reserve(sizeof(double) * N));
+    CNNCRF_TRY(rows.reserve(sizeof(double) * n * H));
+    CNNCRF_TRY(err.reserve(sizeof(int)));
+    return CNNCRF_OK;
+}
+
+// the kernel layouts of every weight from the master copy
+int cnncrf_train::refresh()
+{
+    for (auto *v : {&feat, &pw})
+        for (auto &Ly : *v)
+            if (Ly.act == 1)
+                CNNCRF_TRY(k::train_weight_layouts(param(Ly.wslot), param(Ly.bslot), Ly.cout, Ly.cin, Ly.kh, Ly.kw,
+                                                   Ly.wt.as<float>(), Ly.wd.as<float>(), Ly.b128.as<float>(), st));
+    return CNNCRF_OK;
+}
+
+int cnncrf_train::forward(const float *l, const float *r)
+{
+    const float *img[2] = {l, r};
+    for (int s = 0; s < 2; ++s) {
+        CNNCRF_TRY(k::pad_rgba(img[s], W, H, p, padded[s].as<float>(), st, n));
+        CNNCRF_TRY(k::normalize(padded[s].as<float>(), w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
+        const float *cur = norm[s].as<float>();
+        int cc = ic;
+        for (size_t li = 0; li < feat.size(); ++li) {
+            TLayer &Ly = feat[li];
+            k::ConvArgs a{cur, Ly.hin, Ly.win, cc, (long)cc, (long)Ly.win * cc, Ly.wt.as<float>(), Ly.b128.as<float>(),
+                          Ly.cout, Ly.kh, Ly.kw, 1, act[s][li].as<float>()};
+            a.n_img = n, a.in_img = (long)Ly.hin * Ly.win * cc, a.out_img = (long)Ly.hout() * Ly.wout() * Ly.cout;
+            CNNCRF_TRY(k::conv_simt(a, st));
+            cur = act[s][li].as<float>();
+            cc = Ly.cout;
+        }
+        const size_t fb = sizeof(float) * (size_t)n * H * W * d.feat_channels;
+        CNNCRF_CUDA(cudaMemcpyAsync(f[s].get(), cur, fb, cudaMemcpyDeviceToDevice, st));
+        CNNCRF_TRY(k::l2norm(f[s].as<float>(), (long)n * H * W, d.feat_channels, st));
+    }
+    CNNCRF_TRY(k::correlation(f[0].as<float>(), f[1].as<float>(), H, W, d.feat_channels, dlist.as<float>(), D, omin,
+                              omax, false, CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), st, n,
+                              (long)H * W * d.feat_channels));
+    // pairwise net on the left image's normalisation cropped by p - 2 (stereo/colorstereonet.cpp:69-73)
+    const int cr = p - 2, P = d.pw_channels;
+    const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+    k::ConvArgs a1{in, H + 4, W + 4, 3, (long)ic, (long)w * ic, pw[0].wt.as<float>(), pw[0].b128.as<float>(), P, 3, 3,
+                   1, y1.as<float>()};
+    a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * P;
+    CNNCRF_TRY(k::conv_simt(a1, st));
+    k::ConvArgs a2{y1.as<float>(), H + 2, W + 2, P, (long)P, (long)(W + 2) * P, pw[1].wt.as<float>(),
+                   pw[1].b128.as<float>(), P, 3, 3, 1, y2.as<float>()};
+    a2.n_img = n, a2.in_img = (long)(H + 2) * (W + 2) * P, a2.out_img = (long)H * W * P;
+    CNNCRF_TRY(k::conv_simt(a2, st));
+    CNNCRF_TRY(k::conv_head2(y2.as<float>(), H * W, P, param(pw[2].wslot), pwout.as<float>(), st, n));
+    forwarded = true;
+    hinged = false;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
+{
+    if (!forwarded) return fail(CNNCRF_ESTATE, "train: hinge before forward");
+    const long N = (long)n * H * W;
+    CNNCRF_CUDA(cudaMemsetAsync(err.get(), 0, sizeof(int), st));
+    CNNCRF_TRY(k::train_augment(vol.as<float>(), gt, N, D, aug.as<float>(), err.as<int>(), st));
+    CNNCRF_CUDA(cudaMemcpyAsync(wts.get(), pwout.get(), sizeof(float) * N * 2, cudaMemcpyDeviceToDevice, st));
+    CNNCRF_TRY(k::scale(wts.as<float>(), N * 2, d.lambda, st)); // stereo/stereo.cpp:136-137
+    k::CrfParams cp;
+    cp.L1 = d.L1, cp.L2 = d.L2, cp.delta = d.delta, cp.shape = d.crf_shape, cp.slack = d.crf_slack;
+    CNNCRF_TRY(k::crf_solve_batch(aug.as<float>(), wts.as<float>(), W, H, D, n, cp, d.crf_iters, labels.as<int32_t>(),
+                                  crfws.get(), crfws_bytes, st));
+    float rho[9];
+    rho[0] = 0.0f;
+    for (int t = 1; t <= 8; ++t) rho[t] = d.crf_shape == 0 ? fminf(d.L1, d.L2) : fminf(d.L1 * (float)t, d.L2);
+    CNNCRF_CUDA(cudaMemsetAsync(gvol.get(), 0, sizeof(float) * N * D, st));
+    CNNCRF_TRY(k::train_hinge(vol.as<float>(), wts.as<float>(), gt, labels.as<int32_t>(), n, W, H, D, d.lambda, rho,
+                              d.L2, d.delta, gvol.as<float>(), gpw.as<float>(), contrib.as<double>(),
+                              rows.as<double>(), st));
+    std::vector<double> r((size_t)n * H);
+    int e = 0;
+    CNNCRF_CUDA(cudaMemcpyAsync(r.data(), rows.get(), sizeof(double) * r.size(), cudaMemcpyDeviceToHost, st));
+    CNNCRF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    CNNCRF_CUDA(cudaStreamSynchronize(st));
+    if (e) return fail(CNNCRF_EINVAL, "train: %d ground-truth labels outside 0..%d", e, D - 1);
+    if (loss)
+        for (int i = 0; i < n; ++i) {
+            double s = 0.0;
+            for (int y = 0; y < H; ++y) s += r[(size_t)i * H + y];
+            loss[i] = s;
+        }
+    if (yh_out)
+        CNNCRF_CUDA(cudaMemcpyAsync(yh_out, labels.get(), sizeof(int32_t) * N, cudaMemcpyDeviceToDevice, st));
+    hinged = true;
+    return CNNCRF_OK;
+}
+
+// dz: the layer's output gradient, turned into the pre-activation gradient in
+// place; dprev (if set): the input gradient
+int cnncrf_train::layer_back(TLayer &L, const float *in, long in_pix, long in_row, long in_img, const float *y,
+                             float *dz, float *dprev)
+{
+    const int Ho = L.hout(), Wo = L.wout();
+    CNNCRF_TRY(k::train_tanh_bwd(dz, y, (long)n * Ho * Wo * L.cout, st));
+    CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo, part.as<float>(),
+                              gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr, partb.as<float>(), st));
+    if (!dprev) return CNNCRF_OK;
+    const int ph = L.kh - 1, pwd = L.kw - 1;
+    CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
+    const int Hp = Ho + 2 * ph, Wp = Wo + 2 * pwd;
+    k::ConvArgs a{padb.as<float>(), Hp, Wp, L.cout, (long)L.cout, (long)Wp * L.cout, L.wd.as<float>(), nullptr,
+                  L.cin, L.kh, L.kw, 0, dprev};
+    a.n_img = n, a.in_img = (long)Hp * Wp * L.cout, a.out_img = (long)L.hin * L.win * L.cin;
+    return k::conv_simt(a, st);
+}
+
+int cnncrf_train::backward(const float *gv, const float *gp)
+{
+    if (!forwarded) return fail(CNNCRF_ESTATE, "train: backward before forward");
+    if (!gv && !hinged) return fail(CNNCRF_ESTATE, "train: backward from the hinge before hinge");
+    if (!gv) gv = gvol.as<float>(), gp = gpw.as<float>();
+    const int F = d.feat_channels, P = d.pw_channels;
+    const long N = (long)n * H * W;
+    CNNCRF_CUDA(cudaMemsetAsync(grad.get(), 0, total * sizeof(float), st));
+    CNNCRF_TRY(k::train_corr_bwd(f[0].as<float>(), f[1].as<float>(), gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
+                                 df[0].as<float>(), df[1].as<float>(), st));
+    for (int s = 0; s < 2; ++s) {
+        const int L = (int)feat.size();
+        CNNCRF_TRY(k::train_l2norm_bwd(act[s][L - 1].as<float>(), df[s].as<float>(), N, F, dy.as<float>(), st));
+        float *cur = dy.as<float>(), *nxt = dyb.as<float>();
+        for (int l = L - 1; l >= 0; --l) {
+            TLayer &Ly = feat[l];
+            const float *in = l > 0 ? act[s][l - 1].as<float>() : norm[s].as<float>();
+            const int cin = Ly.cin;
+            CNNCRF_TRY(layer_back(Ly, in, cin, (long)Ly.win * cin, (long)Ly.hin * Ly.win * cin, act[s][l].as<float>(),
+                                  cur, l > 0 ? nxt : nullptr));
+            std::swap(cur, nxt);
+        }
+    }
+    if (gp) {
+        // head: gh = gpw sign(h), dy2 = W^T gh; its weight gradient is a 1x1 wgrad on y2
+        CNNCRF_TRY(k::train_head_bwd(y2.as<float>(), param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
+                                     dy.as<float>(), st));
+        CNNCRF_TRY(k::train_wgrad(gh.as<float>(), 2, y2.as<float>(), P, (long)W * P, (long)H * W * P, P, 1, 1, n, H, W,
+                                  part.as<float>(), gradp(pw[2].wslot), nullptr, partb.as<float>(), st));
+        CNNCRF_TRY(layer_back(pw[1], y1.as<float>(), P, (long)(W + 2) * P, (long)(H + 2) * (W + 2) * P, y2.as<float>(),
+                              dy.as<float>(), dyb.as<float>()));
+        const int cr = p - 2;
+        const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+        CNNCRF_TRY(layer_back(pw[0], in, ic, (long)w * ic, (long)h * w * ic, y1.as<float>(), dyb.as<float>(), nullptr));
+    }
+    return CNNCRF_OK;
+}
+
+// ---------------------------------------------------------------- C ABI
+
+extern "C" {
+
+int cnncrf_train_default_desc(cnncrf_train_desc *d)
+{
+    if (!d) return fail(CNNCRF_EINVAL, "null argument");
+    std::memset(d, 0, sizeof *d);
+    d->num_layers = 7;
+    d->topology = CNNCRF_TOPO_ALL3X3;
+    d->feat_channels = 100;
+    d->pw_channels = 64;
+    d->disp_min = 0.0f, d->disp_step = 1.0f, d->disp_max = 127.0f;
+    d->lambda = 1.0f;
+    d->L1 = 0.5f, d->L2 = 1.5f, d->delta = 3;
+    d->crf_shape = CNNCRF_RHO_LINEAR;
+    d->crf_slack = 0.5f;
+    d->crf_iters = 8;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_create(cnncrf_train_t *out, const cnncrf_train_desc *desc, int npairs, int width, int height)
+{
+    clear_error();
+    if (!out || !desc) return fail(CNNCRF_EINVAL, "null argument");
+    *out = nullptr;
+    const cnncrf_train_desc &d = *desc;
+    if (npairs < 1 || width < 1 || height < 1) return fail(CNNCRF_EINVAL, "train: bad size");
+    if (d.num_layers < 1 || d.num_layers > 16) return fail(CNNCRF_EINVAL, "train: num_layers %d", d.num_layers);
+    if (d.topology != CNNCRF_TOPO_REF && d.topology != CNNCRF_TOPO_ALL3X3)
+        return fail(CNNCRF_EINVAL, "train: topology %d", d.topology);
+    if (d.feat_channels < 1 || d.feat_channels > 128 || d.pw_channels < 1 || d.pw_channels > 128)
+        return fail(CNNCRF_EINVAL, "train: channels %d / %d outside 1..128", d.feat_channels, d.pw_channels);
+    if (!(d.disp_step > 0.0f) || d.delta < 1 || d.delta > 4 || d.crf_iters < 1 || !(d.crf_slack > 0.0f) ||
+        d.crf_slack > 1.0f)
+        return fail(CNNCRF_EINVAL, "train: bad disparity step or CRF options");
+    auto *t = new cnncrf_train;
+    t->d = d;
+    t->n = npairs, t->W = width, t->H = height;
+    int rc = t->build();
+    if (rc != CNNCRF_OK) {
+        delete t;
+        return rc;
+    }
+    *out = t;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_destroy(cnncrf_train_t t)
+{
+    if (t) cudaDeviceSynchronize();
+    delete t;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_set_stream(cnncrf_train_t t, cnncrf_stream_t stream)
+{
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    t->st = (cudaStream_t)stream;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_num_params(cnncrf_train_t t, int *n)
+{
+    if (!t || !n) return fail(CNNCRF_EINVAL, "null argument");
+    *n = (int)t->off.size();
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_param_shape(cnncrf_train_t t, int i, int64_t shape[4], int *ndim)
+{
+    if (!t || !shape || !ndim) return fail(CNNCRF_EINVAL, "null argument");
+    for (auto *v : {&t->feat, &t->pw})
+        for (auto &L : *v) {
+            if (L.wslot == i) {
+                shape[0] = L.cout, shape[1] = L.cin, shape[2] = L.kh, shape[3] = L.kw;
+                *ndim = 4;
+                return CNNCRF_OK;
+            }
+            if (L.bslot == i) {
+                shape[0] = L.cout;
+                *ndim = 1;
+                return CNNCRF_OK;
+            }
+        }
+    return fail(CNNCRF_EINVAL, "train: parameter %d outside 0..%zu", i, t->off.size() - 1);
+}
+
+int cnncrf_train_init_xavier(cnncrf_train_t t, uint64_t seed)
+{
+    clear_error();
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    std::vector<float> all(t->total, 0.0f);
+    for (size_t i = 0; i < t->off.size(); ++i) {
+        int64_t s[4];
+        int nd;
+        CNNCRF_TRY(cnncrf_train_param_shape(t, (int)i, s, &nd));
+        if (nd == 4) cnncrf_xavier_fill(all.data() + t->off[i], (int)s[0], (int)s[1], (int)s[2], (int)s[3], seed, (int)i);
+    }
+    CNNCRF_CUDA(cudaMemcpy(t->theta.get(), all.data(), t->total * sizeof(float), cudaMemcpyHostToDevice));
+    CNNCRF_CUDA(cudaMemset(t->vel.get(), 0, t->total * sizeof(float)));
+    CNNCRF_TRY(t->refresh());
+    t->forwarded = t->hinged = false;
+    return CNNCRF_OK;
+}
+
+static int slot_check(cnncrf_train_t t, int i, const void *data, size_t count)
+{
+    if (!t || !data) return fail(CNNCRF_EINVAL, "null argument");
+    if (i < 0 || i >= (int)t->off.size()) return fail(CNNCRF_EINVAL, "train: parameter %d", i);
+    if (count != t->cnt[i]) return fail(CNNCRF_ESHAPE, "train: parameter %d has %zu values, not %zu", i, t->cnt[i], count);
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_set_param(cnncrf_train_t t, int i, const float *data, size_t count)
+{
+    clear_error();
+    CNNCRF_TRY(slot_check(t, i, data, count));
+    CNNCRF_CUDA(cudaStreamSynchronize(t->st));
+    CNNCRF_CUDA(cudaMemcpy(t->param(i), data, count * sizeof(float), cudaMemcpyDefault));
+    CNNCRF_TRY(t->refresh());
+    t->forwarded = t->hinged = false;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_get_param(cnncrf_train_t t, int i, float *data, size_t count)
+{
+    clear_error();
+    CNNCRF_TRY(slot_check(t, i, data, count));
+    CNNCRF_CUDA(cudaStreamSynchronize(t->st));
+    CNNCRF_CUDA(cudaMemcpy(data, t->param(i), count * sizeof(float), cudaMemcpyDefault));
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_get_grad(cnncrf_train_t t, int i, float *data, size_t count)
+{
+    clear_error();
+    CNNCRF_TRY(slot_check(t, i, data, count));
+    CNNCRF_CUDA(cudaStreamSynchronize(t->st));
+    CNNCRF_CUDA(cudaMemcpy(data, t->gradp(i), count * sizeof(float), cudaMemcpyDefault));
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_forward(cnncrf_train_t t, const float *d_left, const float *d_right)
+{
+    clear_error();
+    if (!t || !d_left || !d_right) return fail(CNNCRF_EINVAL, "null argument");
+    return t->forward(d_left, d_right);
+}
+
+int cnncrf_train_outputs(cnncrf_train_t t, const float **d_volume, const float **d_pairwise, int *depth)
+{
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    if (!t->forwarded) return fail(CNNCRF_ESTATE, "train: outputs before forward");
+    if (d_volume) *d_volume = t->vol.as<float>();
+    if (d_pairwise) *d_pairwise = t->pwout.as<float>();
+    if (depth) *depth = t->D;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_hinge(cnncrf_train_t t, const int32_t *d_gt, double *h_loss, int32_t *d_labels)
+{
+    clear_error();
+    if (!t || !d_gt) return fail(CNNCRF_EINVAL, "null argument");
+    return t->hinge(d_gt, h_loss, d_labels);
+}
+
+int cnncrf_train_hinge_grads(cnncrf_train_t t, const float **d_gvol, const float **d_gpw)
+{
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    if (!t->hinged) return fail(CNNCRF_ESTATE, "train: hinge gradients before hinge");
+    if (d_gvol) *d_gvol = t->gvol.as<float>();
+    if (d_gpw) *d_gpw = t->gpw.as<float>();
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_backward(cnncrf_train_t t, const float *d_gvol, const float *d_gpw)
+{
+    clear_error();
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    if (!d_gvol && d_gpw) return fail(CNNCRF_EINVAL, "train: pairwise gradient without a volume gradient");
+    return t->backward(d_gvol, d_gpw);
+}
+
+int cnncrf_train_sgd(cnncrf_train_t t, float lr, float momentum)
+{
+    clear_error();
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    if (!(lr >= 0.0f) || !(momentum >= 0.0f) || momentum >= 1.0f)
+        return fail(CNNCRF_EINVAL, "train: lr %g, momentum %g", lr, momentum);
+    CNNCRF_TRY(k::train_sgd(t->theta.as<float>(), t->grad.as<float>(), t->vel.as<float>(), (long)t->total, lr,
+                            momentum, t->st));
+    CNNCRF_TRY(t->refresh());
+    t->forwarded = t->hinged = false;
+    return CNNCRF_OK;
+}
+
+int cnncrf_train_step(cnncrf_train_t t, const float *d_left, const float *d_right, const int32_t *d_gt, float lr,
+                      float momentum, double *h_loss)
+{
+    clear_error();
+    if (!t || !d_left || !d_right || !d_gt) return fail(CNNCRF_EINVAL, "null argument");
+    CNNCRF_TRY(t->forward(d_left, d_right));
+    CNNCRF_TRY(t->hinge(d_gt, h_loss, nullptr));
+    CNNCRF_TRY(t->backward(nullptr, nullptr));
+    return cnncrf_train_sgd(t, lr, momentum);
+}
+
+} // extern "C"

@@ -319,6 +319,71 @@ int cnncrf_quad_fit_direct(float *d_u, const float *d_c1, int width, int height,
 int cnncrf_left_right_check(const float *d_left, const float *d_right, int width, int height,
                             float threshold, float *d_out, cnncrf_stream_t stream);
 
+/* ---------------------------------------------------------------- training step */
+
+/* No counterpart in the reference, which ships inference only.  One step of
+ * end-to-end training of the feature net and the pairwise net through the
+ * CRF: the forward keeps every layer's activations (FP32); the structured
+ * hinge with margin 1 per mislabelled pixel takes the CRF's labelling y^ of
+ * the loss-augmented energy (the unary plus 1 at each ground-truth label):
+ *   loss = E(gt) - E(y^) + #(y^ != gt),
+ *   E(y) = sum_i vol[i][y_i] + sum_edges lambda pw rho(|y_i - y_j|);
+ * its subgradient (+1 at gt, -1 at y^ in the volume; lambda (rho(gt) -
+ * rho(y^)) per edge) goes back through the hand-written adjoints of the
+ * correlation, the L2 normalisation, the tanh convolutions and the |1x1|
+ * head into every parameter; SGD with momentum (v = mu v + g, theta -= lr v)
+ * updates FP32 master weights in the npz layout (stereo/stereonet.cpp:191-223).
+ * Nets: num_layers 3x3 (or reference-topology) tanh layers, one-minus-dot
+ * unary, integer disparity list, RGB; images [npairs][height][width][4] RGBA
+ * on the device, mirror-padded and normalised inside as in predict. */
+typedef struct cnncrf_train *cnncrf_train_t;
+
+typedef struct cnncrf_train_desc {
+    int num_layers;     /* 7 */
+    int topology;       /* CNNCRF_TOPO_ALL3X3 (default) or CNNCRF_TOPO_REF */
+    int feat_channels;  /* 100 */
+    int pw_channels;    /* 64 */
+    float disp_min, disp_step, disp_max; /* integer disparities disp_min + k step <= disp_max: 0, 1, 127 */
+    float lambda;       /* w = lambda * |pairwise net|: 1 */
+    float L1, L2;       /* rho: 0.5, 1.5 */
+    int delta;          /* 3 */
+    int crf_shape;      /* CNNCRF_RHO_LINEAR */
+    float crf_slack;    /* 0.5 */
+    int crf_iters;      /* 8 */
+} cnncrf_train_desc;
+
+int cnncrf_train_default_desc(cnncrf_train_desc *d);
+int cnncrf_train_create(cnncrf_train_t *t, const cnncrf_train_desc *d, int npairs, int width, int height);
+int cnncrf_train_destroy(cnncrf_train_t t);
+int cnncrf_train_set_stream(cnncrf_train_t t, cnncrf_stream_t stream);
+/* parameters in the npz slot order of cnncrf_net_set_param, npz shapes */
+int cnncrf_train_num_params(cnncrf_train_t t, int *n);
+int cnncrf_train_param_shape(cnncrf_train_t t, int i, int64_t shape[4], int *ndim);
+int cnncrf_train_init_xavier(cnncrf_train_t t, uint64_t seed); /* the nets' seeded Xavier init; momentum zeroed */
+/* host or device pointers; count = the slot's element count (else CNNCRF_ESHAPE) */
+int cnncrf_train_set_param(cnncrf_train_t t, int i, const float *data, size_t count);
+int cnncrf_train_get_param(cnncrf_train_t t, int i, float *data, size_t count);
+int cnncrf_train_get_grad(cnncrf_train_t t, int i, float *data, size_t count);
+/* forward: the unary volume [npairs][H][W][D] and the pairwise output |h|
+ * (before lambda) [npairs][2][H][W] stay on the device (cnncrf_train_outputs) */
+int cnncrf_train_forward(cnncrf_train_t t, const float *d_left, const float *d_right);
+int cnncrf_train_outputs(cnncrf_train_t t, const float **d_volume, const float **d_pairwise, int *depth);
+/* after forward: the loss-augmented CRF solve, the loss of every pair
+ * (h_loss[npairs], may be NULL) and the subgradient; d_gt [npairs][H][W]
+ * labels in 0..D-1 (CNNCRF_EINVAL otherwise); d_labels (may be NULL): y^.
+ * Synchronises the stream. */
+int cnncrf_train_hinge(cnncrf_train_t t, const int32_t *d_gt, double *h_loss, int32_t *d_labels);
+/* the hinge's subgradient buffers ([npairs][H][W][D] and [npairs][2][H][W])
+ * of the last cnncrf_train_hinge, valid until the next forward */
+int cnncrf_train_hinge_grads(cnncrf_train_t t, const float **d_gvol, const float **d_gpw);
+/* parameter gradients of sum(gvol * vol) + sum(gpw * pw) (gpw may be NULL:
+ * the pairwise net gets none), or of the hinge loss when both are NULL */
+int cnncrf_train_backward(cnncrf_train_t t, const float *d_gvol, const float *d_gpw);
+int cnncrf_train_sgd(cnncrf_train_t t, float lr, float momentum);
+/* forward + hinge + backward + sgd */
+int cnncrf_train_step(cnncrf_train_t t, const float *d_left, const float *d_right, const int32_t *d_gt, float lr,
+                      float momentum, double *h_loss);
+
 /* ---------------------------------------------------------------- Stereo */
 
 typedef struct cnncrf_stereo *cnncrf_stereo_t;
