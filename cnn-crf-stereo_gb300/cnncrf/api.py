@@ -62,7 +62,7 @@ class StereoNet:
         self._h = C.c_void_p()
         call("cnncrf_net_create", C.byref(self._h), C.byref(d), n, h, w)
         self.desc = d
-        self.h, self.w = h, w
+        self.n, self.h, self.w = n, h, w
         self.pad = self.padding()
         self.H, self.W = h - 2 * self.pad, w - 2 * self.pad
         self.volume = None
@@ -83,11 +83,15 @@ class StereoNet:
     def init_net(self, min_disp=0.0, max_disp=0.0, step=0.0, rect_corr=0, unary_out=None,
                  pairwise_out=None):
         D = _count_disparities(min_disp, max_disp, step)
+        lead = () if self.n == 1 else (self.n,)  # the library writes every pair of the batch
         self.volume = unary_out if unary_out is not None else torch.empty(
-            (self.H, self.W, D), device="cuda", dtype=torch.float32)
+            lead + (self.H, self.W, D), device="cuda", dtype=torch.float32)
         if self.desc.with_pairwise:
             self.pairwise_out = pairwise_out if pairwise_out is not None else torch.zeros(
-                (2, self.H, self.W), device="cuda", dtype=torch.float32)
+                lead + (2, self.H, self.W), device="cuda", dtype=torch.float32)
+        need = self.n * self.H * self.W * D
+        if self.volume.numel() < need or (self.desc.with_pairwise and self.pairwise_out.numel() < 2 * need // D):
+            raise ValueError("init_net: output buffers smaller than %d pairs" % self.n)
         call("cnncrf_net_init", self._h, min_disp, max_disp, step, rect_corr, _ptr(self.volume),
              _ptr(self.pairwise_out))
 

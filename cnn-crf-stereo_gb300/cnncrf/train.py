@@ -36,18 +36,20 @@ def _count(dmin, dstep, dmax):
 class Trainer:
     def __init__(self, npairs, width, height, num_layers=7, topology=L.TOPO_ALL3X3, feat_channels=100,
                  pw_channels=64, disp_min=0.0, disp_step=1.0, disp_max=127.0, lam=1.0, L1=0.5, L2=1.5, delta=3,
-                 crf_shape=L.RHO_LINEAR, crf_slack=0.5, crf_iters=8, stream=None):
+                 crf_shape=L.RHO_LINEAR, crf_slack=0.5, crf_iters=8, mean_loss=True, stream=None):
         d = TrainDesc()
         call("cnncrf_train_default_desc", C.byref(d))
         d.num_layers, d.topology, d.feat_channels, d.pw_channels = num_layers, topology, feat_channels, pw_channels
         d.disp_min, d.disp_step, d.disp_max, d.lam = disp_min, disp_step, disp_max, lam
         d.L1, d.L2, d.delta, d.crf_shape, d.crf_slack, d.crf_iters = L1, L2, delta, crf_shape, crf_slack, crf_iters
+        d.mean_loss = 1 if mean_loss else 0
         self._h = C.c_void_p()
         call("cnncrf_train_create", C.byref(self._h), C.byref(d), npairs, width, height)
         self.stream = stream
         call("cnncrf_train_set_stream", self._h, _stream_ptr(stream))
         self.n, self.W, self.H = npairs, width, height
         self.D = _count(disp_min, disp_step, disp_max)
+        self.mean_loss = bool(mean_loss)
 
     def __del__(self):
         if getattr(self, "_h", None) and L._lib is not None:
@@ -158,14 +160,16 @@ class StereoNetsFunction(torch.autograd.Function):
 
 
 class HingeLossFunction(torch.autograd.Function):
-    """Sum over the batch of the structured hinge.  vol and pw must be the
+    """The structured hinge of the batch: the mean of the pairs' per-pixel
+    losses (mean_loss) or the sum of their losses.  vol and pw must be the
     trainer's last forward outputs: the CRF runs on its own copies of them."""
 
     @staticmethod
     def forward(ctx, trainer, vol, pw, gt):
         losses, _ = trainer.hinge(gt)
         ctx.trainer = trainer
-        return torch.tensor(float(losses.sum()), dtype=torch.float64, device=vol.device)
+        total = losses.mean() if trainer.mean_loss else losses.sum()
+        return torch.tensor(float(total), dtype=torch.float64, device=vol.device)
 
     @staticmethod
     def backward(ctx, g):

@@ -310,6 +310,7 @@ struct HingeArgs {
     float lam, L2;
     int delta;
     float rho[9];
+    float gscale;      // scale of the subgradient (1, or 1 / pixels of the batch for the mean loss)
     float *gvol, *gpw; // gvol zeroed by the caller
     double *contrib;   // per pixel: its unary, margin and right / down edge terms of E(gt) - E(yh) + margin
 };
@@ -324,15 +325,15 @@ __global__ void k_hinge(const HingeArgs a)
     double c = 0.0;
     if (g >= 0 && g < a.D && h >= 0 && h < a.D) { // invalid labels are reported by k_augment
         float *gv = a.gvol + q * a.D;
-        gv[g] += 1.0f;
-        gv[h] -= 1.0f;
+        gv[g] += a.gscale;
+        gv[h] -= a.gscale;
         c = (double)a.vol[q * a.D + g] - (double)a.vol[q * a.D + h] + (g != h ? 1.0 : 0.0);
         const float *wx = a.w + (long)img * 2 * N, *wy = wx + N;
         if (x + 1 < a.W) {
             const int g2 = a.gt[q + 1], h2 = a.yh[q + 1];
             if (g2 >= 0 && g2 < a.D && h2 >= 0 && h2 < a.D) {
                 const float rg = rho_of(a.rho, a.delta, a.L2, g - g2), rh = rho_of(a.rho, a.delta, a.L2, h - h2);
-                gx = a.lam * (rg - rh);
+                gx = a.lam * (rg - rh) * a.gscale;
                 c += (double)wx[i] * (double)rg - (double)wx[i] * (double)rh;
             }
         }
@@ -340,7 +341,7 @@ __global__ void k_hinge(const HingeArgs a)
             const int g2 = a.gt[q + a.W], h2 = a.yh[q + a.W];
             if (g2 >= 0 && g2 < a.D && h2 >= 0 && h2 < a.D) {
                 const float rg = rho_of(a.rho, a.delta, a.L2, g - g2), rh = rho_of(a.rho, a.delta, a.L2, h - h2);
-                gy = a.lam * (rg - rh);
+                gy = a.lam * (rg - rh) * a.gscale;
                 c += (double)wy[i] * (double)rg - (double)wy[i] * (double)rh;
             }
         }
@@ -475,10 +476,11 @@ int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *a
 }
 
 int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,
-                int D, float lam, const float rho[9], float L2, int delta, float *gvol, float *gpw, double *contrib,
-                double *rows, cudaStream_t st)
+                int D, float lam, const float rho[9], float L2, int delta, float gscale, float *gvol, float *gpw,
+                double *contrib, double *rows, cudaStream_t st)
 {
     HingeArgs a;
+    a.gscale = gscale;
     a.vol = vol, a.w = w, a.gt = gt, a.yh = yh, a.W = W, a.H = H, a.D = D, a.lam = lam, a.L2 = L2, a.delta = delta;
     for (int t = 0; t < 9; ++t) a.rho[t] = rho[t];
     a.gvol = gvol, a.gpw = gpw, a.contrib = contrib;

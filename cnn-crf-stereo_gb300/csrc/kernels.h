@@ -102,8 +102,8 @@ int train_head_bwd(const float *y2, const float *wh, const float *gpw, int nimg,
                    float *dy2, cudaStream_t st);
 int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st);
 int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,
-                int D, float lam, const float rho[9], float L2, int delta, float *gvol, float *gpw, double *contrib,
-                double *rows, cudaStream_t st);
+                int D, float lam, const float rho[9], float L2, int delta, float gscale, float *gvol, float *gpw,
+                double *contrib, double *rows, cudaStream_t st);
 int train_sgd(float *theta, const float *g, float *v, long n, float lr, float mu, cudaStream_t st);
 
 // ------------------------------------------------------------ census, edge weights, QuadDirect, LR check

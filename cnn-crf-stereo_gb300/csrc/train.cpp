@@ -251,8 +251,10 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
     rho[0] = 0.0f;
     for (int t = 1; t <= 8; ++t) rho[t] = d.crf_shape == 0 ? fminf(d.L1, d.L2) : fminf(d.L1 * (float)t, d.L2);
     CNNCRF_CUDA(cudaMemsetAsync(gvol.get(), 0, sizeof(float) * N * D, st));
+    // mean loss: every pair's loss per pixel, the subgradient of their mean over the batch
+    const float gscale = d.mean_loss ? (float)(1.0 / (double)N) : 1.0f;
     CNNCRF_TRY(k::train_hinge(vol.as<float>(), wts.as<float>(), gt, labels.as<int32_t>(), n, W, H, D, d.lambda, rho,
-                              d.L2, d.delta, gvol.as<float>(), gpw.as<float>(), contrib.as<double>(),
+                              d.L2, d.delta, gscale, gvol.as<float>(), gpw.as<float>(), contrib.as<double>(),
                               rows.as<double>(), st));
     std::vector<double> r((size_t)n * H);
     int e = 0;
@@ -264,7 +266,7 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
         for (int i = 0; i < n; ++i) {
             double s = 0.0;
             for (int y = 0; y < H; ++y) s += r[(size_t)i * H + y];
-            loss[i] = s;
+            loss[i] = d.mean_loss ? s / ((double)H * W) : s;
         }
     if (yh_out)
         CNNCRF_CUDA(cudaMemcpyAsync(yh_out, labels.get(), sizeof(int32_t) * N, cudaMemcpyDeviceToDevice, st));
@@ -347,6 +349,7 @@ int cnncrf_train_default_desc(cnncrf_train_desc *d)
     d->crf_shape = CNNCRF_RHO_LINEAR;
     d->crf_slack = 0.5f;
     d->crf_iters = 8;
+    d->mean_loss = 1;
     return CNNCRF_OK;
 }
 

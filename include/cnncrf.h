@@ -350,6 +350,8 @@ typedef struct cnncrf_train_desc {
     int crf_shape;      /* CNNCRF_RHO_LINEAR */
     float crf_slack;    /* 0.5 */
     int crf_iters;      /* 8 */
+    int mean_loss;      /* 1: per-pair losses per pixel, the gradient of their mean over the batch
+                           (the scale at which lr 1e-3 is a sane step); 0: plain sums */
 } cnncrf_train_desc;
 
 int cnncrf_train_default_desc(cnncrf_train_desc *d);

@@ -95,6 +95,18 @@ def test_net_batch_of_two(cuda, oracle):
         assert np.array_equal(pw[i].cpu().numpy(), opw)
 
 
+def test_net_batch_output_buffers(cuda):
+    """StereoNet with n = 3 sizes its own outputs for every pair, and refuses
+    caller buffers that hold fewer pairs than the library would write."""
+    torch = cuda
+    from cnncrf.api import StereoNet
+    net = StereoNet(3, 3, 3, 26, 46, with_pairwise=True)
+    net.init_net(0.0, 7.0, 1.0)
+    assert tuple(net.volume.shape) == (3, 22, 42, 8) and tuple(net.pairwise_out.shape) == (3, 2, 22, 42)
+    with pytest.raises(ValueError):
+        StereoNet(3, 3, 3, 26, 46).init_net(0.0, 7.0, 1.0, unary_out=torch.empty((22, 42, 8), device="cuda"))
+
+
 def test_uneven_batch_full_size_equals_single(cuda):
     """The uneven batch's four sizes and ranges at full size (480x320/D64,
     720x480/D96, 1242x375/D128, 1440x960/D192), two pairs each, replayed as

@@ -1,0 +1,232 @@
+"""GPU tests of the training step (cnncrf_train_*) against the oracle: the
+forward equals the oracle's FP32 forward bit for bit; the adjoints equal the
+FP64 oracle's gradient (itself pinned by central differences in
+test_oracle_train.py) within FP32 accumulation error; the hinge finds the
+oracle's loss-augmented labelling, loss and subgradient; SGD with momentum
+follows v = mu v + g, theta -= lr v; the autograd form gives the fused step's
+gradients; the full-size training step of 4 crops of 512 x 256, D = 128 runs."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# |g - g64| <= TOL * max|g64| per parameter slot: FP32 activations and sums against FP64
+TOL = 2e-4
+
+
+def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3, mean_loss=False):
+    import torch
+    from cnncrf import scenes
+    from cnncrf.train import Trainer
+    cfg = oracle.make_cfg(num_layers=layers, topology=topology, in_channels=3, feat_channels=F, unary=1,
+                          with_pairwise=1, pw_channels=P, precision=32, disp_min=0.0, disp_max=float(D - 1))
+    params = oracle.xavier_params(cfg, seed=seed)
+    sc = [scenes.voronoi_scene(W, H, D, seed=seed + 10 * i, cells=4, off_range=(1, D - 2), slope=0.05)
+          for i in range(n)]
+    t = Trainer(n, W, H, num_layers=layers, topology=topology, feat_channels=F, pw_channels=P, disp_max=float(D - 1),
+                mean_loss=mean_loss)
+    t.init_xavier(seed)
+    left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
+    right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
+    p = oracle.padding(cfg)
+    pads = [(oracle.pad_rgba(s["left"], p), oracle.pad_rgba(s["right"], p)) for s in sc]
+    gt = np.stack([np.clip(np.rint(s["disp"]), 0, D - 1).astype(np.int32) for s in sc])
+    lst = oracle.disparity_list(0.0, float(D - 1), 1.0)
+    return cfg, params, t, left, right, pads, gt, lst
+
+
+def close(g, g64, what):
+    scale = max(np.abs(g64).max(), 1e-12)
+    err = np.abs(g - g64).max() / scale
+    assert err <= TOL, (what, err)
+
+
+@pytest.mark.parametrize("layers,topology", [(3, 1), (3, 0)])
+def test_forward_bitexact(cuda, oracle, layers, topology):
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, layers, topology)
+    for i, prm in enumerate(params):
+        assert np.array_equal(t.get_param(i), prm), i  # the same seeded Xavier init
+    vol, pw = t.forward(left, right)
+    for i, (lp, rp) in enumerate(pads):
+        ovol, opw = oracle.predict(cfg, params, lp, rp, lst)
+        assert np.array_equal(vol[i].cpu().numpy(), ovol)
+        assert np.array_equal(pw[i].cpu().numpy(), opw)
+
+
+@pytest.mark.parametrize("layers,topology", [(3, 1), (3, 0)])
+def test_backward_matches_fp64_oracle(cuda, oracle, layers, topology):
+    torch = cuda
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, layers, topology)
+    vol, pw = t.forward(left, right)
+    rng = np.random.default_rng(7)
+    gvol = rng.standard_normal(tuple(vol.shape)).astype(np.float32)
+    gpw = rng.standard_normal(tuple(pw.shape)).astype(np.float32)
+    t.backward(torch.from_numpy(gvol).cuda(), torch.from_numpy(gpw).cuda())
+    g64 = None
+    cfg64 = oracle.make_cfg(**{k: getattr(cfg, k) for k, _ in cfg._fields_})
+    cfg64.precision = 64
+    for i, (lp, rp) in enumerate(pads):
+        g = oracle.predict_backward(cfg64, params, lp, rp, lst, gvol[i], gpw[i])
+        g64 = g if g64 is None else [a + b for a, b in zip(g64, g)]
+    for i in range(len(params)):
+        close(t.get_grad(i), g64[i], i)
+
+
+def test_volume_only_gradient_leaves_the_pairwise_net_at_zero(cuda, oracle):
+    torch = cuda
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle)
+    vol, pw = t.forward(left, right)
+    t.backward(torch.ones_like(vol), None)
+    npw = 2 * cfg.num_layers
+    assert all(not t.get_grad(i).any() for i in range(npw, len(params)))
+    assert any(t.get_grad(i).any() for i in range(npw))
+
+
+def test_hinge_matches_oracle(cuda, oracle):
+    torch = cuda
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle)
+    t.forward(left, right)
+    losses, yh = t.hinge(torch.from_numpy(gt).cuda())
+    gv, gp = t.hinge_grads()
+    cfg64 = oracle.make_cfg(**{k: getattr(cfg, k) for k, _ in cfg._fields_})
+    cfg64.precision = 64
+    g64 = None
+    for i, (lp, rp) in enumerate(pads):
+        vol32, pw32 = oracle.predict(cfg, params, lp, rp, lst)
+        loss, yho, gvo, gpo = oracle.hinge(vol32, pw32, gt[i], 1.0, 0.5, 1.5, 3, 8, shape=1)
+        assert np.array_equal(yh[i].cpu().numpy(), yho), i
+        assert losses[i] == pytest.approx(loss, rel=1e-12, abs=1e-9), i
+        assert np.array_equal(gv[i].cpu().numpy(), gvo.astype(np.float32)), i
+        assert np.array_equal(gp[i].cpu().numpy(), gpo.astype(np.float32)), i
+        g = oracle.predict_backward(cfg64, params, lp, rp, lst, gvo, gpo)
+        g64 = g if g64 is None else [a + b for a, b in zip(g64, g)]
+    t.backward()  # from the hinge's own subgradient
+    for i in range(len(params)):
+        close(t.get_grad(i), g64[i], i)
+
+
+def test_sgd_momentum_and_training_progress(cuda, oracle):
+    torch = cuda
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, n=1)
+    g_t = torch.from_numpy(gt).cuda()
+    th0 = [t.get_param(i) for i in range(len(params))]
+    first = t.step(left, right, g_t, lr=0.01, momentum=0.9)
+    g1 = [t.get_grad(i) for i in range(len(params))]
+    th1 = [t.get_param(i) for i in range(len(params))]
+    # the update is one fused multiply-add per element: allow an ulp of the larger operand
+    for a, g, b in zip(th0, g1, th1):  # v = g after the first step
+        np.testing.assert_allclose(b, a - np.float32(0.01) * g, rtol=1e-6, atol=2e-7)
+    t.step(left, right, g_t, lr=0.01, momentum=0.9)
+    g2 = [t.get_grad(i) for i in range(len(params))]
+    th2 = [t.get_param(i) for i in range(len(params))]
+    for a, ga, gb, b in zip(th1, g1, g2, th2):  # v = 0.9 g1 + g2
+        np.testing.assert_allclose(b, a - np.float32(0.01) * (np.float32(0.9) * ga + gb), rtol=1e-5, atol=2e-7)
+    hist = [first.sum()]
+    for _ in range(25):
+        hist.append(t.step(left, right, g_t, lr=0.01, momentum=0.9).sum())
+    assert np.mean(hist[-3:]) < hist[0], hist
+
+
+def test_autograd_equals_fused_step(cuda, oracle):
+    torch = cuda
+    from cnncrf.train import HingeLossFunction, StereoNetsFunction
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle)
+    g_t = torch.from_numpy(gt).cuda()
+    t.forward(left, right)
+    fused_loss, _ = t.hinge(g_t)
+    t.backward()
+    fused = [t.get_grad(i) for i in range(len(params))]
+    ps = [torch.from_numpy(np.ascontiguousarray(p, np.float32)).cuda().requires_grad_() for p in params]
+    vol, pw = StereoNetsFunction.apply(t, left, right, *ps)
+    loss = HingeLossFunction.apply(t, vol, pw, g_t)
+    assert loss.item() == pytest.approx(fused_loss.sum(), rel=1e-12)  # mean_loss off: sums
+    loss.backward()
+    for i, p in enumerate(ps):
+        assert np.array_equal(p.grad.cpu().numpy(), fused[i]), i
+    # torch's SGD on the autograd gradients and the library's update agree
+    opt = torch.optim.SGD(ps, lr=0.01, momentum=0.9)
+    opt.step()
+    t.sgd(0.01, 0.9)
+    for i, p in enumerate(ps):
+        np.testing.assert_allclose(p.detach().cpu().numpy(), t.get_param(i), rtol=1e-6, atol=2e-7)
+
+
+def test_errors(cuda, oracle):
+    torch = cuda
+    from cnncrf import _lib as L
+    from cnncrf.api import CnnCrfError
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle)
+    with pytest.raises(CnnCrfError) as e:
+        t.backward()
+    assert e.value.status == L.ESTATE
+    t.forward(left, right)
+    bad = gt.copy()
+    bad[0, 0, 0] = 10  # D = 10: labels 0..9
+    with pytest.raises(CnnCrfError) as e:
+        t.hinge(torch.from_numpy(bad).cuda())
+    assert e.value.status == L.EINVAL
+    with pytest.raises(CnnCrfError) as e:
+        t.set_param(0, np.zeros(3, np.float32))
+    assert e.value.status == L.ESHAPE
+
+
+def test_full_size_training_step(cuda, oracle):
+    """4 crops of 512 x 256 from the KITTI-shaped generator, D = 128, the
+    7-layer 100-channel nets: two steps, finite losses and gradients, and the
+    forward of the first equals the FP32 inference net's."""
+    torch = cuda
+    import time
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import StereoNet
+    from cnncrf.train import Trainer
+    n, W, H, D = 4, 512, 256, 128
+    sc = [scenes.kitti_scene(W, H, D, seed=40 + i) for i in range(n)]
+    left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
+    right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
+    gt = torch.from_numpy(np.stack([np.clip(np.rint(s["disp"]), 0, D - 1).astype(np.int32) for s in sc])).cuda()
+    t = Trainer(n, W, H)  # mean loss: lr 1e-3 and momentum 0.9 of the task
+    t.init_xavier(0)
+    vol, pw = t.forward(left, right)
+    net = StereoNet(7, n, 3, H + 14, W + 14, topology=L.TOPO_ALL3X3, unary=L.UNARY_ONE_MINUS_DOT,
+                    with_pairwise=True)
+    net.init_net(0.0, float(D - 1), 1.0)
+    net.init_xavier(0)
+    lp = np.stack([oracle.pad_rgba(s["left"], 7) for s in sc])
+    rp = np.stack([oracle.pad_rgba(s["right"], 7) for s in sc])
+    ivol = net.predict(torch.from_numpy(lp).cuda(), torch.from_numpy(rp).cuda())
+    assert torch.equal(vol.reshape(ivol.shape), ivol)
+    assert torch.equal(pw.reshape(net.pairwise_out.shape), net.pairwise_out)
+    del net, ivol
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    l1 = t.step(left, right, gt, lr=1e-3, momentum=0.9)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    l2 = t.step(left, right, gt, lr=1e-3, momentum=0.9)
+    assert np.isfinite(l1).all() and np.isfinite(l2).all() and (l1 > 0).all()
+    assert (np.abs(l2 - l1) < 0.5 * l1).all()  # a sane step: the per-pixel loss moves, it does not explode
+    for i in range(t.num_params()):
+        g = t.get_grad(i)
+        assert np.isfinite(g).all(), i
+    assert any(t.get_grad(i).any() for i in range(t.num_params()))
+    print("training step 4 x 512x256 D128: %.1f ms, losses %s -> %s" % (dt * 1e3, l1, l2))
+
+
+def test_mean_loss_scaling(cuda, oracle):
+    """mean_loss: every pair's loss per pixel, the subgradient and the
+    gradients of their mean over the batch (sums / pixels)."""
+    torch = cuda
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, mean_loss=False)
+    cfg2, params2, tm, left2, right2, _, _, _ = setup(oracle, mean_loss=True)
+    g_t = torch.from_numpy(gt).cuda()
+    t.forward(left, right)
+    tm.forward(left, right)
+    ls, _ = t.hinge(g_t)
+    lm, _ = tm.hinge(g_t)
+    npx = t.H * t.W
+    np.testing.assert_allclose(lm, ls / npx, rtol=1e-12)
+    t.backward()
+    tm.backward()
+    for i in range(len(params)):
+        np.testing.assert_allclose(tm.get_grad(i), t.get_grad(i) / (t.n * npx), rtol=2e-5,
+                                   atol=1e-7 * np.abs(t.get_grad(i)).max() / (t.n * npx))
