@@ -228,5 +228,6 @@ def test_mean_loss_scaling(cuda, oracle):
     t.backward()
     tm.backward()
     for i in range(len(params)):
-        np.testing.assert_allclose(tm.get_grad(i), t.get_grad(i) / (t.n * npx), rtol=2e-5,
-                                   atol=1e-7 * np.abs(t.get_grad(i)).max() / (t.n * npx))
+        # the scale 1 / pixels is no power of two: the FP32 sums round differently
+        ref = t.get_grad(i) / (t.n * npx)
+        np.testing.assert_allclose(tm.get_grad(i), ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
