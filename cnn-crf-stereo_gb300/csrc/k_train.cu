@@ -14,6 +14,8 @@
 #include <algorithm>
 #include <cfloat>
 
+#include <cuda_bf16.h>
+
 #include "common.h"
 #include "kernels.h"
 
@@ -21,6 +23,10 @@ namespace cnncrf {
 namespace k {
 
 namespace {
+
+// activations are FP32 or BF16 (the BF16 training mode), read at a channel stride
+__device__ __forceinline__ float ld(const float *p) { return *p; }
+__device__ __forceinline__ float ld(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
 
 // ------------------------------------------------------------ weight layouts
 // forward (conv_simt): wt[(ky*kw + kx)*Cin + ci][co] = w[co][ci][kh-1-ky][kw-1-kx], [K][128]
@@ -44,6 +50,52 @@ __global__ void k_w_dgrad(const float *__restrict__ w, int Cout, int Cin, int kh
     wd[i] = ci < Cin ? w[(((long)co * Cin + ci) * kh + ky) * kw + kx] : 0.0f;
 }
 
+// tensor-core conv (conv_tc): w16[(co*kh*kw + ky*kw + kx)*cp + ci] = bf16(w[co][ci][kh-1-ky][kw-1-kx]),
+// [np][kh*kw][cp], zero past Cout / Cin
+__global__ void k_w16(const float *__restrict__ w, int Cout, int Cin, int kh, int kw, int np, int cp,
+                      __nv_bfloat16 *__restrict__ w16)
+{
+    const long taps = (long)kh * kw, i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)np * taps * cp) return;
+    const int ci = (int)(i % cp);
+    const long r = i / cp;
+    const int t = (int)(r % taps), co = (int)(r / taps), ky = t / kw, kx = t % kw;
+    const float v = (co < Cout && ci < Cin) ? w[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] : 0.0f;
+    w16[i] = __float2bfloat16_rn(v);
+}
+
+// BF16 L2 normalisation: f = y / |y| per pixel in FP32, rounded once; a warp per pixel
+__global__ void k_l2norm_bf16(const __nv_bfloat16 *__restrict__ y, long npx, int C, int cs,
+                              __nv_bfloat16 *__restrict__ f)
+{
+    const long px = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (px >= npx) return;
+    const __nv_bfloat16 *yp = y + px * cs;
+    float ss = 0.0f;
+    for (int c = lane; c < C; c += 32) ss = fmaf(ld(yp + c), ld(yp + c), ss);
+    for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    const float n = sqrtf(ss);
+    for (int c = lane; c < C; c += 32) f[px * cs + c] = __float2bfloat16_rn(n > 0.0f ? ld(yp + c) / n : 0.0f);
+}
+
+// pw = |h|, h[o] = sum_c wh[o][c] y2[c] on BF16 y2 (channel stride cs): [img][2][npx]
+__global__ void k_head2_bf16(const __nv_bfloat16 *__restrict__ y2, int npx, int P, int cs, const float *__restrict__ wh,
+                             float *__restrict__ out)
+{
+    const int p = blockIdx.x * blockDim.x + threadIdx.x, img = blockIdx.y;
+    if (p >= npx) return;
+    const __nv_bfloat16 *v = y2 + ((long)img * npx + p) * cs;
+    float h0 = 0.0f, h1 = 0.0f;
+    for (int c = 0; c < P; ++c) {
+        const float x = ld(v + c);
+        h0 = fmaf(wh[c], x, h0);
+        h1 = fmaf(wh[P + c], x, h1);
+    }
+    out[(long)img * 2 * npx + p] = fabsf(h0);
+    out[((long)img * 2 + 1) * npx + p] = fabsf(h1);
+}
+
 __global__ void k_pad128(const float *__restrict__ b, int n, float *__restrict__ out)
 {
     const int i = threadIdx.x;
@@ -51,11 +103,12 @@ __global__ void k_pad128(const float *__restrict__ b, int n, float *__restrict__
 }
 
 // ------------------------------------------------------------ elementwise
-__global__ void k_tanh_bwd(float *__restrict__ dy, const float *__restrict__ y, long n)
+template <class T>
+__global__ void k_tanh_bwd(float *__restrict__ dy, const T *__restrict__ y, long npx, int C, int ys)
 {
     const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) {
-        const float v = y[i];
+    if (i < npx * C) {
+        const float v = ld(y + (i / C) * ys + i % C);
         dy[i] = dy[i] * (1.0f - v * v);
     }
 }
@@ -76,17 +129,19 @@ __global__ void k_pad_zero(const float *__restrict__ in, int H, int W, int C, in
 }
 
 // f = y / |y| per pixel; dy = (df - y <y, df> / |y|^2) / |y|, zero where |y| = 0.  A warp per pixel.
-__global__ void k_l2norm_bwd(const float *__restrict__ y, const float *__restrict__ df, long npx, int C,
+template <class T>
+__global__ void k_l2norm_bwd(const T *__restrict__ y, int ys, const float *__restrict__ df, long npx, int C,
                              float *__restrict__ dy)
 {
     const long px = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (px >= npx) return;
-    const float *yp = y + px * C, *gp = df + px * C;
+    const T *yp = y + px * ys;
+    const float *gp = df + px * C;
     float ss = 0.0f, dot = 0.0f;
     for (int c = lane; c < C; c += 32) {
-        ss = fmaf(yp[c], yp[c], ss);
-        dot = fmaf(yp[c], gp[c], dot);
+        ss = fmaf(ld(yp + c), ld(yp + c), ss);
+        dot = fmaf(ld(yp + c), gp[c], dot);
     }
     for (int o = 16; o; o >>= 1) {
         ss += __shfl_xor_sync(0xffffffffu, ss, o);
@@ -94,13 +149,14 @@ __global__ void k_l2norm_bwd(const float *__restrict__ y, const float *__restric
     }
     const float n = sqrtf(ss);
     for (int c = lane; c < C; c += 32)
-        dy[px * C + c] = n > 0.0f ? (gp[c] - yp[c] * (dot / ss)) / n : 0.0f;
+        dy[px * C + c] = n > 0.0f ? (gp[c] - ld(yp + c) * (dot / ss)) / n : 0.0f;
 }
 
 // ------------------------------------------------------------ correlation adjoint
 // Left: dfl[x][c] = -sum_k gvol[x][k] fr[x + s_k][c].  A CTA per (32-pixel
 // tile, row, pair); thread c; the right features of the tile's band in shared memory.
-__global__ void k_corr_bwd_left(const float *__restrict__ fr, const float *__restrict__ gvol,
+template <class T>
+__global__ void k_corr_bwd_left(const T *__restrict__ fr, int fs, const float *__restrict__ gvol,
                                 const float *__restrict__ list, int H, int W, int C, int D, int omin, int span,
                                 float *__restrict__ dfl)
 {
@@ -111,7 +167,7 @@ __global__ void k_corr_bwd_left(const float *__restrict__ fr, const float *__res
     for (int i = threadIdx.x; i < D; i += blockDim.x) s[i] = (int)list[i];
     for (int i = threadIdx.x; i < span * C; i += blockDim.x) {
         const int xs = x0 + omin + i / C, c = i % C;
-        win[i] = (xs >= 0 && xs < W) ? fr[(row + xs) * C + c] : 0.0f;
+        win[i] = (xs >= 0 && xs < W) ? ld(fr + (row + xs) * fs + c) : 0.0f;
     }
     __syncthreads();
     const int c = threadIdx.x;
@@ -130,7 +186,8 @@ __global__ void k_corr_bwd_left(const float *__restrict__ fr, const float *__res
 
 // Right: dfr[x'][c] = -sum_k gvol[x' - s_k][k] fl[x' - s_k][c] over x' - s_k in
 // [0, W); the left features x' - omax .. x' + 31 - omin in shared memory.
-__global__ void k_corr_bwd_right(const float *__restrict__ fl, const float *__restrict__ gvol,
+template <class T>
+__global__ void k_corr_bwd_right(const T *__restrict__ fl, int fs, const float *__restrict__ gvol,
                                  const float *__restrict__ list, int H, int W, int C, int D, int omax, int span,
                                  float *__restrict__ dfr)
 {
@@ -141,7 +198,7 @@ __global__ void k_corr_bwd_right(const float *__restrict__ fl, const float *__re
     for (int i = threadIdx.x; i < D; i += blockDim.x) s[i] = (int)list[i];
     for (int i = threadIdx.x; i < span * C; i += blockDim.x) {
         const int x = x0 - omax + i / C, c = i % C;
-        win[i] = (x >= 0 && x < W) ? fl[(row + x) * C + c] : 0.0f;
+        win[i] = (x >= 0 && x < W) ? ld(fl + (row + x) * fs + c) : 0.0f;
     }
     __syncthreads();
     const int c = threadIdx.x;
@@ -161,10 +218,10 @@ __global__ void k_corr_bwd_right(const float *__restrict__ fl, const float *__re
 // part[split][co][k] = sum over the split's pixels p of dz[p][co] * A[p][k],
 // A[p][(ky*kw + kx)*Cin + ci] = in(img, oy + ky, ox + kx, ci).  A CTA per
 // (64-wide k tile, split); 256 threads, 8 co x 4 k each; 32 pixels staged per step.
-struct WgradArgs {
+template <class T> struct WgradArgs {
     const float *dz;
     int Cout;
-    const float *in;
+    const T *in;
     long in_pix, in_row, in_img;
     int Cin, kh, kw, Ho, Wo;
     long P, chunk;
@@ -173,7 +230,7 @@ struct WgradArgs {
 
 constexpr int WG_PX = 32, WG_KT = 64;
 
-__global__ void __launch_bounds__(256) k_wgrad(const WgradArgs a)
+template <class T> __global__ void __launch_bounds__(256) k_wgrad(const WgradArgs<T> a)
 {
     __shared__ float As[WG_PX][128];
     __shared__ float Bs[WG_PX][WG_KT];
@@ -200,7 +257,7 @@ __global__ void __launch_bounds__(256) k_wgrad(const WgradArgs a)
                 const int ci = kk % a.Cin, tt = kk / a.Cin, kx = tt % a.kw, ky = tt / a.kw;
                 const long img = p / ((long)a.Ho * a.Wo), r = p - img * a.Ho * a.Wo;
                 const int oy = (int)(r / a.Wo), ox = (int)(r % a.Wo);
-                v = a.in[img * a.in_img + (long)(oy + ky) * a.in_row + (long)(ox + kx) * a.in_pix + ci];
+                v = ld(a.in + img * a.in_img + (long)(oy + ky) * a.in_row + (long)(ox + kx) * a.in_pix + ci);
             }
             Bs[pp][i % WG_KT] = v;
         }
@@ -264,17 +321,18 @@ __global__ void k_bias_reduce(const float *__restrict__ part, int nsplit, int Co
 
 // ------------------------------------------------------------ pairwise head adjoint
 // pw = |h|, h[o] = sum_c wh[o][c] y2[c]: gh[o] = gpw[o] sign(h[o]); dy2[c] = sum_o wh[o][c] gh[o]
-__global__ void k_head_bwd(const float *__restrict__ y2, const float *__restrict__ wh, const float *__restrict__ gpw,
+template <class T>
+__global__ void k_head_bwd(const T *__restrict__ y2, int ys, const float *__restrict__ wh, const float *__restrict__ gpw,
                            int npx, int P, float *__restrict__ gh, float *__restrict__ dy2)
 {
     const int p = blockIdx.x * blockDim.x + threadIdx.x, img = blockIdx.y;
     if (p >= npx) return;
     const long q = (long)img * npx + p;
-    const float *v = y2 + q * P;
+    const T *v = y2 + q * ys;
     float h0 = 0.0f, h1 = 0.0f;
     for (int c = 0; c < P; ++c) {
-        h0 = fmaf(wh[c], v[c], h0);
-        h1 = fmaf(wh[P + c], v[c], h1);
+        h0 = fmaf(wh[c], ld(v + c), h0);
+        h1 = fmaf(wh[P + c], ld(v + c), h1);
     }
     const float a0 = gpw[(long)img * 2 * npx + p], a1 = gpw[((long)img * 2 + 1) * npx + p];
     const float g0 = h0 > 0.0f ? a0 : (h0 < 0.0f ? -a0 : 0.0f);
@@ -386,11 +444,43 @@ int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int 
     return CNNCRF_OK;
 }
 
-int train_tanh_bwd(float *dy, const float *y, long n, cudaStream_t st)
+int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16, cudaStream_t st)
+{
+    const long n = (long)np * kh * kw * cp;
+    k_w16<<<ceil_div(n, 256), 256, 0, st>>>(w, Cout, Cin, kh, kw, np, cp, (__nv_bfloat16 *)w16);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_l2norm_bf16(const void *y, long npx, int C, int cs, void *f, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("l2norm", st);
+        k_l2norm_bf16<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const __nv_bfloat16 *)y, npx, C, cs,
+                                                                (__nv_bfloat16 *)f);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_head2_bf16(const void *y2, int nimg, int npx, int P, int cs, const float *wh, float *out, cudaStream_t st)
+{
+    {
+        CNNCRF_PROF("head2", st);
+        k_head2_bf16<<<dim3(ceil_div(npx, 128), nimg), 128, 0, st>>>((const __nv_bfloat16 *)y2, npx, P, cs, wh, out);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_tanh_bwd(float *dy, const void *y, bool bf16, long npx, int C, int ys, cudaStream_t st)
 {
     {
         CNNCRF_PROF("tanh_bwd", st);
-        k_tanh_bwd<<<ceil_div(n, 256), 256, 0, st>>>(dy, y, n);
+        if (bf16)
+            k_tanh_bwd<<<ceil_div(npx * C, 256), 256, 0, st>>>(dy, (const __nv_bfloat16 *)y, npx, C, ys);
+        else
+            k_tanh_bwd<<<ceil_div(npx * C, 256), 256, 0, st>>>(dy, (const float *)y, npx, C, ys);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
@@ -404,42 +494,57 @@ int train_pad_zero(const float *in, int nimg, int H, int W, int C, int p, int q,
     return CNNCRF_OK;
 }
 
-int train_l2norm_bwd(const float *y, const float *df, long npx, int C, float *dy, cudaStream_t st)
+int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx, int C, float *dy, cudaStream_t st)
 {
     {
         CNNCRF_PROF("l2norm_bwd", st);
-        k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>(y, df, npx, C, dy);
+        if (bf16)
+            k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const __nv_bfloat16 *)y, ys, df, npx, C, dy);
+        else
+            k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const float *)y, ys, df, npx, C, dy);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
-int train_corr_bwd(const float *fl, const float *fr, const float *gvol, const float *d_list, int npairs, int H, int W,
-                   int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st)
+template <class T>
+static int corr_bwd_t(const T *fl, const T *fr, int fs, const float *gvol, const float *d_list, int npairs, int H,
+                      int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st)
 {
     if (C > 128) return fail(CNNCRF_EINVAL, "corr_bwd: %d channels > 128", C);
     const int span = 32 + omax - omin;
     const size_t smem = sizeof(float) * (size_t)span * C + sizeof(int) * (size_t)D;
     if (smem > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "corr_bwd: band %d too wide", omax - omin);
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_left, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_right, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_left<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_right<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const dim3 g(ceil_div(W, 32), H, npairs);
     {
         CNNCRF_PROF("corr_bwd", st);
-        k_corr_bwd_left<<<g, 128, smem, st>>>(fr, gvol, d_list, H, W, C, D, omin, span, dfl);
-        k_corr_bwd_right<<<g, 128, smem, st>>>(fl, gvol, d_list, H, W, C, D, omax, span, dfr);
+        k_corr_bwd_left<T><<<g, 128, smem, st>>>(fr, fs, gvol, d_list, H, W, C, D, omin, span, dfl);
+        k_corr_bwd_right<T><<<g, 128, smem, st>>>(fl, fs, gvol, d_list, H, W, C, D, omax, span, dfr);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
+int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,
+                   int npairs, int H, int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st)
+{
+    if (bf16)
+        return corr_bwd_t((const __nv_bfloat16 *)fl, (const __nv_bfloat16 *)fr, fs, gvol, d_list, npairs, H, W, C, D,
+                          omin, omax, dfl, dfr, st);
+    return corr_bwd_t((const float *)fl, (const float *)fr, fs, gvol, d_list, npairs, H, W, C, D, omin, omax, dfl, dfr,
+                      st);
+}
+
 int train_wgrad_splits(long P) { return (int)std::max(1L, std::min(64L, P / 2048)); }
 
-int train_wgrad(const float *dz, int Cout, const float *in, long in_pix, long in_row, long in_img, int Cin, int kh,
-                int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st)
+template <class T>
+static int wgrad_t(const float *dz, int Cout, const T *in, long in_pix, long in_row, long in_img, int Cin, int kh,
+                   int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st)
 {
     if (Cout > 128) return fail(CNNCRF_EINVAL, "wgrad: %d output channels > 128", Cout);
-    WgradArgs a;
+    WgradArgs<T> a;
     a.dz = dz, a.Cout = Cout, a.in = in, a.in_pix = in_pix, a.in_row = in_row, a.in_img = in_img;
     a.Cin = Cin, a.kh = kh, a.kw = kw, a.Ho = Ho, a.Wo = Wo;
     a.P = (long)nimg * Ho * Wo;
@@ -449,7 +554,7 @@ int train_wgrad(const float *dz, int Cout, const float *in, long in_pix, long in
     const int K = kh * kw * Cin;
     {
         CNNCRF_PROF("wgrad", st);
-        k_wgrad<<<dim3(ceil_div(K, WG_KT), ns), 256, 0, st>>>(a);
+        k_wgrad<T><<<dim3(ceil_div(K, WG_KT), ns), 256, 0, st>>>(a);
         k_wgrad_reduce<<<ceil_div((long)Cout * K, 256), 256, 0, st>>>(part, ns, Cout, Cin, kh, kw, dw);
         if (db) {
             k_bias_part<<<ns, 128, 0, st>>>(dz, Cout, a.P, a.chunk, partb);
@@ -460,10 +565,24 @@ int train_wgrad(const float *dz, int Cout, const float *in, long in_pix, long in
     return CNNCRF_OK;
 }
 
-int train_head_bwd(const float *y2, const float *wh, const float *gpw, int nimg, int npx, int P, float *gh,
-                   float *dy2, cudaStream_t st)
+int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pix, long in_row, long in_img, int Cin,
+                int kh, int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st)
 {
-    k_head_bwd<<<dim3(ceil_div(npx, 128), nimg), 128, 0, st>>>(y2, wh, gpw, npx, P, gh, dy2);
+    if (bf16)
+        return wgrad_t(dz, Cout, (const __nv_bfloat16 *)in, in_pix, in_row, in_img, Cin, kh, kw, nimg, Ho, Wo, part,
+                       dw, db, partb, st);
+    return wgrad_t(dz, Cout, (const float *)in, in_pix, in_row, in_img, Cin, kh, kw, nimg, Ho, Wo, part, dw, db, partb,
+                   st);
+}
+
+int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
+                   float *gh, float *dy2, cudaStream_t st)
+{
+    const dim3 g(ceil_div(npx, 128), nimg);
+    if (bf16)
+        k_head_bwd<<<g, 128, 0, st>>>((const __nv_bfloat16 *)y2, ys, wh, gpw, npx, P, gh, dy2);
+    else
+        k_head_bwd<<<g, 128, 0, st>>>((const float *)y2, ys, wh, gpw, npx, P, gh, dy2);
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

@@ -86,20 +86,26 @@ int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, co
 // gradient's wd [kh*kw*Cout][128] (if wd), bias padded to 128 (if b and b128)
 int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int kh, int kw, float *wt, float *wd,
                          float *b128, cudaStream_t st);
-int train_tanh_bwd(float *dy, const float *y, long n, cudaStream_t st); // dy *= 1 - y^2
+// the BF16 mode's tensor-core weight layout [np][kh*kw][cp], its L2 normalisation and |1x1| head
+int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16, cudaStream_t st);
+int train_l2norm_bf16(const void *y, long npx, int C, int cs, void *f, cudaStream_t st);
+int train_head2_bf16(const void *y2, int nimg, int npx, int P, int cs, const float *wh, float *out, cudaStream_t st);
+// Activations y are FP32 or BF16 (bf16) at channel stride ys; gradients are dense FP32 [px][C].
+int train_tanh_bwd(float *dy, const void *y, bool bf16, long npx, int C, int ys, cudaStream_t st); // dy *= 1 - y^2
 int train_pad_zero(const float *in, int nimg, int H, int W, int C, int p, int q, float *out, cudaStream_t st);
-int train_l2norm_bwd(const float *y, const float *df, long npx, int C, float *dy, cudaStream_t st);
-// one-minus-dot unary over an integer stored list (band [omin, omax]): dfl, dfr from dL/dvol
-int train_corr_bwd(const float *fl, const float *fr, const float *gvol, const float *d_list, int npairs, int H, int W,
-                   int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st);
+int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx, int C, float *dy, cudaStream_t st);
+// one-minus-dot unary over an integer stored list (band [omin, omax]): dfl, dfr (dense) from dL/dvol;
+// features at channel stride fs
+int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,
+                   int npairs, int H, int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st);
 // pixel splits (at most 64) of the weight gradient's fixed-order reduction for P output pixels
 int train_wgrad_splits(long P);
 // dw (npz layout) += weight gradient, db += bias gradient (if db); part:
 // splits x Cout x kh*kw*Cin floats, partb: splits x Cout floats of scratch
-int train_wgrad(const float *dz, int Cout, const float *in, long in_pix, long in_row, long in_img, int Cin, int kh,
-                int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st);
-int train_head_bwd(const float *y2, const float *wh, const float *gpw, int nimg, int npx, int P, float *gh,
-                   float *dy2, cudaStream_t st);
+int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pix, long in_row, long in_img, int Cin,
+                int kh, int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st);
+int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
+                   float *gh, float *dy2, cudaStream_t st);
 int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st);
 int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,
                 int D, float lam, const float rho[9], float L2, int delta, float gscale, float *gvol, float *gpw,

@@ -29,6 +29,7 @@ struct TLayer {
     int cin, cout, kh, kw, act, wslot, bslot;
     int hin, win;        // input extent
     DevBuf wt, wd, b128; // conv_simt layout, input-gradient layout, padded bias
+    DevBuf w16;          // the BF16 mode's tensor-core layout
     int hout() const { return hin - kh + 1; }
     int wout() const { return win - kw + 1; }
 };
@@ -41,6 +42,8 @@ struct cnncrf_train {
     cnncrf_train_desc d{};
     int n = 0, H = 0, W = 0, p = 0, h = 0, w = 0, D = 0;
     const int ic = 3;
+    bool bf16 = false;
+    int cp_feat = 0, np_feat = 0, cp_pw = 0, np_pw = 0;
     cudaStream_t st = nullptr;
     std::vector<TLayer> feat, pw; // pw: conv 3x3, conv 3x3, 1x1 head
     std::vector<size_t> off, cnt; // slot offset / count in the flat parameter buffers
@@ -49,14 +52,15 @@ struct cnncrf_train {
     std::vector<float> list;
     int omin = 0, omax = 0;
     DevBuf dlist;
-    // forward state
+    // forward state; feature-layer outputs: checkpoints in their own buffers, the rest in a shared pool
     DevBuf padded[2], norm[2], scratch;
-    std::vector<DevBuf> act[2];
-    DevBuf f[2], vol, y1, y2, pwout;
+    std::vector<char> keep;
+    std::vector<DevBuf> act[2], pool;
+    DevBuf fbuf, vol, y1, y2, pwout; // fbuf: both sides' normalised features
     bool forwarded = false, hinged = false;
     // backward and hinge scratch
     DevBuf gvol, gpw, df[2], dy, dyb, padb, part, partb, gh;
-    DevBuf aug, wts, labels, crfws, contrib, rows, err;
+    DevBuf aug, wts, labels, crfws, contrib, rows, err, tcerr;
     size_t crfws_bytes = 0;
 
     int build();
@@ -64,16 +68,38 @@ struct cnncrf_train {
     int forward(const float *l, const float *r);
     int hinge(const int32_t *gt, double *loss, int32_t *yh_out);
     int backward(const float *gv, const float *gp);
-    int layer_back(TLayer &L, const float *in, long in_pix, long in_row, long in_img, const float *y, float *dz,
-                   float *dprev);
+    int run_layer(int s, int l);
+    int layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img, const void *y,
+                   int ys, float *dz, float *dprev);
     float *param(int slot) { return theta.as<float>() + off[slot]; }
     float *gradp(int slot) { return grad.as<float>() + off[slot]; }
+    size_t es() const { return bf16 ? 2 : 4; }
+    int fstride() const { return bf16 ? cp_feat : d.feat_channels; } // channel stride of feature activations
+    int pstride() const { return bf16 ? cp_pw : d.pw_channels; }
+    void *actp(int s, int l)
+    {
+        if (keep[l]) return act[s][l].get();
+        int c = l;
+        while (c > 0 && !keep[c - 1]) --c; // first layer of l's segment
+        return pool[l - c].get();
+    }
+    void *fside(int s) { return (char *)fbuf.get() + (size_t)s * n * H * W * fstride() * es(); }
 };
+
+namespace {
+int pad_to(int c, int m) { return (c + m - 1) / m * m; }
+int umma_n(int cout) { return cout <= 64 ? 64 : (cout <= 112 ? 112 : 128); }
+} // namespace
 
 int cnncrf_train::build()
 {
     const int L = d.num_layers, F = d.feat_channels, P = d.pw_channels;
     const int k = d.topology == CNNCRF_TOPO_REF ? 2 : 3;
+    bf16 = d.precision == CNNCRF_BF16;
+    if (bf16 && (L < 2 || F < 16 || P < 16))
+        return fail(CNNCRF_EUNSUPPORTED, "train: the BF16 mode needs >= 2 layers and >= 16 channels per net");
+    cp_feat = bf16 ? pad_to(F, 64) : F, np_feat = umma_n(F);
+    cp_pw = bf16 ? pad_to(P, 64) : P, np_pw = umma_n(P);
     feat.clear();
     pw.clear();
     feat.push_back({ic, F, 3, 3, 1, 0, 1, 0, 0}); // stereo/stereonet.cpp:69-79
@@ -116,6 +142,11 @@ int cnncrf_train::build()
                 CNNCRF_TRY(Ly.wt.reserve(sizeof(float) * (size_t)Ly.kh * Ly.kw * Ly.cin * 128));
                 CNNCRF_TRY(Ly.wd.reserve(sizeof(float) * (size_t)Ly.kh * Ly.kw * Ly.cout * 128));
                 CNNCRF_TRY(Ly.b128.reserve(sizeof(float) * 128));
+                CNNCRF_CUDA(cudaMemset(Ly.b128.get(), 0, sizeof(float) * 128));
+                if (bf16 && Ly.cin >= 16) { // the tensor-core layers
+                    const int npd = v == &feat ? np_feat : np_pw, cpi = v == &feat ? cp_feat : cp_pw;
+                    CNNCRF_TRY(Ly.w16.reserve(2 * (size_t)npd * Ly.kh * Ly.kw * cpi));
+                }
             }
     // the stored list -d (stereo/operators/stereocorrelation.cpp:83-85); integers only
     list.clear();
@@ -132,26 +163,45 @@ int cnncrf_train::build()
     }
     CNNCRF_TRY(dlist.reserve(sizeof(float) * D));
     CNNCRF_CUDA(cudaMemcpy(dlist.get(), list.data(), sizeof(float) * D, cudaMemcpyHostToDevice));
-    // activations
+    // checkpoints: every r-th feature layer's output and the last one; the rest is recomputed in backward
+    const int r = d.checkpoint_every;
+    keep.assign(L, 1);
+    if (r > 0)
+        for (int l = 0; l < L; ++l) keep[l] = (l + 1) % r == 0 || l == L - 1;
+    int run = 0, poolsz = 0;
+    for (int l = 0; l < L; ++l) {
+        run = keep[l] ? 0 : run + 1;
+        poolsz = std::max(poolsz, run);
+    }
+    // activations (zeroed: the BF16 mode's padding channels must read as zero)
     const size_t N = (size_t)n * H * W;
-    size_t amax = (size_t)n * h * w * 4;
+    size_t amax = (size_t)n * h * w * 4, lmax = 0;
+    for (auto &Ly : feat) lmax = std::max(lmax, (size_t)n * Ly.hout() * Ly.wout() * fstride() * es());
+    auto zalloc = [&](DevBuf &b, size_t bytes) -> int {
+        CNNCRF_TRY(b.reserve(bytes));
+        CNNCRF_CUDA(cudaMemset(b.get(), 0, bytes));
+        return CNNCRF_OK;
+    };
     for (int s = 0; s < 2; ++s) {
         CNNCRF_TRY(padded[s].reserve(sizeof(float) * n * h * w * 4));
         CNNCRF_TRY(norm[s].reserve(sizeof(float) * n * h * w * ic));
         act[s].clear();
         act[s].resize(feat.size());
         for (size_t l = 0; l < feat.size(); ++l) {
-            const size_t e = (size_t)n * feat[l].hout() * feat[l].wout() * feat[l].cout;
-            CNNCRF_TRY(act[s][l].reserve(sizeof(float) * e));
+            const size_t e = (size_t)n * feat[l].hout() * feat[l].wout() * F;
             amax = std::max(amax, e);
+            if (keep[l]) CNNCRF_TRY(zalloc(act[s][l], (size_t)n * feat[l].hout() * feat[l].wout() * fstride() * es()));
         }
-        CNNCRF_TRY(f[s].reserve(sizeof(float) * N * F));
         CNNCRF_TRY(df[s].reserve(sizeof(float) * N * F));
     }
+    pool.clear();
+    pool.resize(poolsz);
+    for (auto &b : pool) CNNCRF_TRY(zalloc(b, lmax));
+    CNNCRF_TRY(zalloc(fbuf, 2 * N * fstride() * es()));
     CNNCRF_TRY(scratch.reserve(k::normalize_scratch_bytes(h, n)));
     CNNCRF_TRY(vol.reserve(sizeof(float) * N * D));
-    CNNCRF_TRY(y1.reserve(sizeof(float) * n * (H + 2) * (W + 2) * P));
-    CNNCRF_TRY(y2.reserve(sizeof(float) * N * P));
+    CNNCRF_TRY(zalloc(y1, (size_t)n * (H + 2) * (W + 2) * pstride() * es()));
+    CNNCRF_TRY(zalloc(y2, N * pstride() * es()));
     CNNCRF_TRY(pwout.reserve(sizeof(float) * N * 2));
     amax = std::max(amax, (size_t)n * (H + 4) * (W + 4) * P);
     // backward: dy / dyb hold any layer's output or input gradient, padb a padded output gradient
@@ -179,7 +229,8 @@ int cnncrf_train::build()
     CNNCRF_TRY(crfws.reserve(crfws_bytes));
     CNNCRF_TRY(contrib.reserve(sizeof(double) * N));
     CNNCRF_TRY(rows.reserve(sizeof(double) * n * H));
-    CNNCRF_TRY(err.reserve(sizeof(int)));
+    CNNCRF_TRY(zalloc(err, sizeof(int)));
+    CNNCRF_TRY(zalloc(tcerr, sizeof(int)));
     return CNNCRF_OK;
 }
 
@@ -188,48 +239,100 @@ int cnncrf_train::refresh()
 {
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v)
-            if (Ly.act == 1)
+            if (Ly.act == 1) {
                 CNNCRF_TRY(k::train_weight_layouts(param(Ly.wslot), param(Ly.bslot), Ly.cout, Ly.cin, Ly.kh, Ly.kw,
                                                    Ly.wt.as<float>(), Ly.wd.as<float>(), Ly.b128.as<float>(), st));
+                if (Ly.w16.get())
+                    CNNCRF_TRY(k::train_w16(param(Ly.wslot), Ly.cout, Ly.cin, Ly.kh, Ly.kw,
+                                            v == &feat ? np_feat : np_pw, v == &feat ? cp_feat : cp_pw, Ly.w16.get(),
+                                            st));
+            }
     return CNNCRF_OK;
+}
+
+// feature layer l of side s into actp(s, l)
+int cnncrf_train::run_layer(int s, int l)
+{
+    TLayer &Ly = feat[l];
+    void *out = actp(s, l);
+    if (l == 0 || !bf16) {
+        const float *in = l == 0 ? norm[s].as<float>() : (const float *)actp(s, l - 1);
+        const int cs = l == 0 ? ic : d.feat_channels;
+        k::ConvArgs a{in, Ly.hin, Ly.win, Ly.cin, (long)cs, (long)Ly.win * cs, Ly.wt.as<float>(), Ly.b128.as<float>(),
+                      Ly.cout, Ly.kh, Ly.kw, 1, bf16 ? nullptr : (float *)out};
+        a.n_img = n, a.in_img = (long)Ly.hin * Ly.win * cs, a.out_img = (long)Ly.hout() * Ly.wout() * fstride();
+        if (!bf16) return k::conv_simt(a, st);
+        a.out16 = out, a.out_cs = cp_feat; // BF16 NHWC output padded to cp_feat
+        return k::conv_first_tc_supported(a) ? k::conv_first_tc(a, tcerr.as<int>(), st) : k::conv_simt(a, st);
+    }
+    k::TcConvArgs t{};
+    t.in = actp(s, l - 1);
+    t.n_img = n, t.Hin = Ly.hin, t.Win = Ly.win, t.cp_in = cp_feat, t.cin = Ly.cin;
+    t.wt = Ly.w16.get();
+    t.np = np_feat, t.cout = Ly.cout, t.kh = Ly.kh, t.kw = Ly.kw;
+    t.bias = Ly.b128.as<float>();
+    t.head = nullptr;
+    t.mode = 0; // tanh -> BF16: the pre-normalisation features stay for the backward
+    t.out = out;
+    t.cp_out = cp_feat;
+    t.err = tcerr.as<int>();
+    return k::conv_tc(t, st);
 }
 
 int cnncrf_train::forward(const float *l, const float *r)
 {
     const float *img[2] = {l, r};
+    const int F = d.feat_channels, L = (int)feat.size();
     for (int s = 0; s < 2; ++s) {
         CNNCRF_TRY(k::pad_rgba(img[s], W, H, p, padded[s].as<float>(), st, n));
         CNNCRF_TRY(k::normalize(padded[s].as<float>(), w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
-        const float *cur = norm[s].as<float>();
-        int cc = ic;
-        for (size_t li = 0; li < feat.size(); ++li) {
-            TLayer &Ly = feat[li];
-            k::ConvArgs a{cur, Ly.hin, Ly.win, cc, (long)cc, (long)Ly.win * cc, Ly.wt.as<float>(), Ly.b128.as<float>(),
-                          Ly.cout, Ly.kh, Ly.kw, 1, act[s][li].as<float>()};
-            a.n_img = n, a.in_img = (long)Ly.hin * Ly.win * cc, a.out_img = (long)Ly.hout() * Ly.wout() * Ly.cout;
-            CNNCRF_TRY(k::conv_simt(a, st));
-            cur = act[s][li].as<float>();
-            cc = Ly.cout;
+        for (int li = 0; li < L; ++li) CNNCRF_TRY(run_layer(s, li));
+        if (bf16) {
+            CNNCRF_TRY(k::train_l2norm_bf16(actp(s, L - 1), (long)n * H * W, F, cp_feat, fside(s), st));
+        } else {
+            const size_t fb = sizeof(float) * (size_t)n * H * W * F;
+            CNNCRF_CUDA(cudaMemcpyAsync(fside(s), actp(s, L - 1), fb, cudaMemcpyDeviceToDevice, st));
+            CNNCRF_TRY(k::l2norm((float *)fside(s), (long)n * H * W, F, st));
         }
-        const size_t fb = sizeof(float) * (size_t)n * H * W * d.feat_channels;
-        CNNCRF_CUDA(cudaMemcpyAsync(f[s].get(), cur, fb, cudaMemcpyDeviceToDevice, st));
-        CNNCRF_TRY(k::l2norm(f[s].as<float>(), (long)n * H * W, d.feat_channels, st));
     }
-    CNNCRF_TRY(k::correlation(f[0].as<float>(), f[1].as<float>(), H, W, d.feat_channels, dlist.as<float>(), D, omin,
-                              omax, false, CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), st, n,
-                              (long)H * W * d.feat_channels));
+    if (!bf16)
+        CNNCRF_TRY(k::correlation((const float *)fside(0), (const float *)fside(1), H, W, F, dlist.as<float>(), D, omin,
+                                  omax, false, CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), st, n, (long)H * W * F));
+    else if (k::corr_tc_supported(F, cp_feat, list.data(), D, CNNCRF_UNARY_ONE_MINUS_DOT))
+        CNNCRF_TRY(k::correlation_tc(fbuf.get(), n, H, W, F, cp_feat, dlist.as<float>(), list.data(), D,
+                                     CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), tcerr.as<int>(), st));
+    else
+        CNNCRF_TRY(k::correlation_bf16(fside(0), fside(1), H, W, F, cp_feat, dlist.as<float>(), D, omin, omax, false,
+                                       CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), st, n, (long)H * W * cp_feat));
     // pairwise net on the left image's normalisation cropped by p - 2 (stereo/colorstereonet.cpp:69-73)
     const int cr = p - 2, P = d.pw_channels;
     const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
     k::ConvArgs a1{in, H + 4, W + 4, 3, (long)ic, (long)w * ic, pw[0].wt.as<float>(), pw[0].b128.as<float>(), P, 3, 3,
-                   1, y1.as<float>()};
-    a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * P;
-    CNNCRF_TRY(k::conv_simt(a1, st));
-    k::ConvArgs a2{y1.as<float>(), H + 2, W + 2, P, (long)P, (long)(W + 2) * P, pw[1].wt.as<float>(),
-                   pw[1].b128.as<float>(), P, 3, 3, 1, y2.as<float>()};
-    a2.n_img = n, a2.in_img = (long)(H + 2) * (W + 2) * P, a2.out_img = (long)H * W * P;
-    CNNCRF_TRY(k::conv_simt(a2, st));
-    CNNCRF_TRY(k::conv_head2(y2.as<float>(), H * W, P, param(pw[2].wslot), pwout.as<float>(), st, n));
+                   1, bf16 ? nullptr : y1.as<float>()};
+    a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * pstride();
+    if (!bf16) {
+        CNNCRF_TRY(k::conv_simt(a1, st));
+        k::ConvArgs a2{y1.as<float>(), H + 2, W + 2, P, (long)P, (long)(W + 2) * P, pw[1].wt.as<float>(),
+                       pw[1].b128.as<float>(), P, 3, 3, 1, y2.as<float>()};
+        a2.n_img = n, a2.in_img = (long)(H + 2) * (W + 2) * P, a2.out_img = (long)H * W * P;
+        CNNCRF_TRY(k::conv_simt(a2, st));
+        CNNCRF_TRY(k::conv_head2(y2.as<float>(), H * W, P, param(pw[2].wslot), pwout.as<float>(), st, n));
+    } else {
+        a1.out16 = y1.get(), a1.out_cs = cp_pw;
+        CNNCRF_TRY(k::conv_first_tc_supported(a1) ? k::conv_first_tc(a1, tcerr.as<int>(), st) : k::conv_simt(a1, st));
+        k::TcConvArgs t{};
+        t.in = y1.get();
+        t.n_img = n, t.Hin = H + 2, t.Win = W + 2, t.cp_in = cp_pw, t.cin = P;
+        t.wt = pw[1].w16.get();
+        t.np = np_pw, t.cout = P, t.kh = 3, t.kw = 3;
+        t.bias = pw[1].b128.as<float>();
+        t.mode = 0;
+        t.out = y2.get();
+        t.cp_out = cp_pw;
+        t.err = tcerr.as<int>();
+        CNNCRF_TRY(k::conv_tc(t, st));
+        CNNCRF_TRY(k::train_head2_bf16(y2.get(), n, H * W, P, cp_pw, param(pw[2].wslot), pwout.as<float>(), st));
+    }
     forwarded = true;
     hinged = false;
     return CNNCRF_OK;
@@ -257,10 +360,15 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
                               d.L2, d.delta, gscale, gvol.as<float>(), gpw.as<float>(), contrib.as<double>(),
                               rows.as<double>(), st));
     std::vector<double> r((size_t)n * H);
-    int e = 0;
+    int e = 0, te = 0;
     CNNCRF_CUDA(cudaMemcpyAsync(r.data(), rows.get(), sizeof(double) * r.size(), cudaMemcpyDeviceToHost, st));
     CNNCRF_CUDA(cudaMemcpyAsync(&e, err.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
+    CNNCRF_CUDA(cudaMemcpyAsync(&te, tcerr.get(), sizeof(int), cudaMemcpyDeviceToHost, st));
     CNNCRF_CUDA(cudaStreamSynchronize(st));
+    if (te) {
+        CNNCRF_CUDA(cudaMemset(tcerr.get(), 0, sizeof(int)));
+        return fail(CNNCRF_ETIMEOUT, "train: a tensor-core kernel gave up on a bounded wait");
+    }
     if (e) return fail(CNNCRF_EINVAL, "train: %d ground-truth labels outside 0..%d", e, D - 1);
     if (loss)
         for (int i = 0; i < n; ++i) {
@@ -274,15 +382,17 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
     return CNNCRF_OK;
 }
 
-// dz: the layer's output gradient, turned into the pre-activation gradient in
-// place; dprev (if set): the input gradient
-int cnncrf_train::layer_back(TLayer &L, const float *in, long in_pix, long in_row, long in_img, const float *y,
-                             float *dz, float *dprev)
+// dz: the layer's output gradient (dense FP32), turned into the pre-activation
+// gradient in place; y: the layer's output at channel stride ys; dprev (if
+// set): the input gradient (dense FP32)
+int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img,
+                             const void *y, int ys, float *dz, float *dprev)
 {
     const int Ho = L.hout(), Wo = L.wout();
-    CNNCRF_TRY(k::train_tanh_bwd(dz, y, (long)n * Ho * Wo * L.cout, st));
-    CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo, part.as<float>(),
-                              gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr, partb.as<float>(), st));
+    CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
+    CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo,
+                              part.as<float>(), gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr,
+                              partb.as<float>(), st));
     if (!dprev) return CNNCRF_OK;
     const int ph = L.kh - 1, pwd = L.kw - 1;
     CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
@@ -298,35 +408,43 @@ int cnncrf_train::backward(const float *gv, const float *gp)
     if (!forwarded) return fail(CNNCRF_ESTATE, "train: backward before forward");
     if (!gv && !hinged) return fail(CNNCRF_ESTATE, "train: backward from the hinge before hinge");
     if (!gv) gv = gvol.as<float>(), gp = gpw.as<float>();
-    const int F = d.feat_channels, P = d.pw_channels;
+    const int F = d.feat_channels, P = d.pw_channels, L = (int)feat.size(), fs = fstride(), ps = pstride();
     const long N = (long)n * H * W;
     CNNCRF_CUDA(cudaMemsetAsync(grad.get(), 0, total * sizeof(float), st));
-    CNNCRF_TRY(k::train_corr_bwd(f[0].as<float>(), f[1].as<float>(), gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
+    CNNCRF_TRY(k::train_corr_bwd(fside(0), fside(1), bf16, fs, gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
                                  df[0].as<float>(), df[1].as<float>(), st));
     for (int s = 0; s < 2; ++s) {
-        const int L = (int)feat.size();
-        CNNCRF_TRY(k::train_l2norm_bwd(act[s][L - 1].as<float>(), df[s].as<float>(), N, F, dy.as<float>(), st));
+        CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
         float *cur = dy.as<float>(), *nxt = dyb.as<float>();
-        for (int l = L - 1; l >= 0; --l) {
-            TLayer &Ly = feat[l];
-            const float *in = l > 0 ? act[s][l - 1].as<float>() : norm[s].as<float>();
-            const int cin = Ly.cin;
-            CNNCRF_TRY(layer_back(Ly, in, cin, (long)Ly.win * cin, (long)Ly.hin * Ly.win * cin, act[s][l].as<float>(),
-                                  cur, l > 0 ? nxt : nullptr));
-            std::swap(cur, nxt);
+        int top = L - 1;
+        while (top >= 0) {
+            int c = top - 1; // the checkpoint under this segment (-1: the normalised input)
+            while (c >= 0 && !keep[c]) --c;
+            for (int j = c + 1; j < top; ++j) CNNCRF_TRY(run_layer(s, j)); // recompute the segment
+            for (int j = top; j > c; --j) {
+                TLayer &Ly = feat[j];
+                const void *in = j > 0 ? actp(s, j - 1) : (const void *)norm[s].get();
+                const bool ib = j > 0 && bf16;
+                const int cs = j > 0 ? fs : ic;
+                CNNCRF_TRY(layer_back(Ly, in, ib, cs, (long)Ly.win * cs, (long)Ly.hin * Ly.win * cs, actp(s, j), fs,
+                                      cur, j > 0 ? nxt : nullptr));
+                std::swap(cur, nxt);
+            }
+            top = c;
         }
     }
     if (gp) {
         // head: gh = gpw sign(h), dy2 = W^T gh; its weight gradient is a 1x1 wgrad on y2
-        CNNCRF_TRY(k::train_head_bwd(y2.as<float>(), param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
+        CNNCRF_TRY(k::train_head_bwd(y2.get(), bf16, ps, param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
                                      dy.as<float>(), st));
-        CNNCRF_TRY(k::train_wgrad(gh.as<float>(), 2, y2.as<float>(), P, (long)W * P, (long)H * W * P, P, 1, 1, n, H, W,
-                                  part.as<float>(), gradp(pw[2].wslot), nullptr, partb.as<float>(), st));
-        CNNCRF_TRY(layer_back(pw[1], y1.as<float>(), P, (long)(W + 2) * P, (long)(H + 2) * (W + 2) * P, y2.as<float>(),
-                              dy.as<float>(), dyb.as<float>()));
+        CNNCRF_TRY(k::train_wgrad(gh.as<float>(), 2, y2.get(), bf16, ps, (long)W * ps, (long)H * W * ps, P, 1, 1, n, H,
+                                  W, part.as<float>(), gradp(pw[2].wslot), nullptr, partb.as<float>(), st));
+        CNNCRF_TRY(layer_back(pw[1], y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
+                              ps, dy.as<float>(), dyb.as<float>()));
         const int cr = p - 2;
         const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
-        CNNCRF_TRY(layer_back(pw[0], in, ic, (long)w * ic, (long)h * w * ic, y1.as<float>(), dyb.as<float>(), nullptr));
+        CNNCRF_TRY(layer_back(pw[0], in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps, dyb.as<float>(),
+                              nullptr));
     }
     return CNNCRF_OK;
 }
@@ -350,6 +468,8 @@ int cnncrf_train_default_desc(cnncrf_train_desc *d)
     d->crf_slack = 0.5f;
     d->crf_iters = 8;
     d->mean_loss = 1;
+    d->precision = CNNCRF_BF16;
+    d->checkpoint_every = 3;
     return CNNCRF_OK;
 }
 
@@ -365,6 +485,8 @@ int cnncrf_train_create(cnncrf_train_t *out, const cnncrf_train_desc *desc, int 
         return fail(CNNCRF_EINVAL, "train: topology %d", d.topology);
     if (d.feat_channels < 1 || d.feat_channels > 128 || d.pw_channels < 1 || d.pw_channels > 128)
         return fail(CNNCRF_EINVAL, "train: channels %d / %d outside 1..128", d.feat_channels, d.pw_channels);
+    if (d.precision != CNNCRF_FP32 && d.precision != CNNCRF_BF16) return fail(CNNCRF_EINVAL, "train: precision");
+    if (d.checkpoint_every < 0) return fail(CNNCRF_EINVAL, "train: checkpoint_every %d", d.checkpoint_every);
     if (!(d.disp_step > 0.0f) || d.delta < 1 || d.delta > 4 || d.crf_iters < 1 || !(d.crf_slack > 0.0f) ||
         d.crf_slack > 1.0f)
         return fail(CNNCRF_EINVAL, "train: bad disparity step or CRF options");

@@ -335,7 +335,9 @@ int cnncrf_left_right_check(const float *d_left, const float *d_right, int width
  * updates FP32 master weights in the npz layout (stereo/stereonet.cpp:191-223).
  * Nets: num_layers 3x3 (or reference-topology) tanh layers, one-minus-dot
  * unary, integer disparity list, RGB; images [npairs][height][width][4] RGBA
- * on the device, mirror-padded and normalised inside as in predict. */
+ * on the device, mirror-padded and normalised inside as in predict.
+ * Recomputation changes no result bit: a checkpointed step equals the
+ * keep-all step exactly. */
 typedef struct cnncrf_train *cnncrf_train_t;
 
 typedef struct cnncrf_train_desc {
@@ -352,6 +354,10 @@ typedef struct cnncrf_train_desc {
     int crf_iters;      /* 8 */
     int mean_loss;      /* 1: per-pair losses per pixel, the gradient of their mean over the batch
                            (the scale at which lr 1e-3 is a sane step); 0: plain sums */
+    int precision;      /* CNNCRF_BF16 (default): tensor-core forward, BF16 activations, FP32 gradients
+                           and master weights; CNNCRF_FP32: the exact path (forward equals the oracle's) */
+    int checkpoint_every; /* r > 0 (default 3): keep every r-th feature layer's output and the last,
+                             recompute the others during backward; 0: keep all */
 } cnncrf_train_desc;
 
 int cnncrf_train_default_desc(cnncrf_train_desc *d);

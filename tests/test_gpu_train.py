@@ -14,17 +14,20 @@ pytestmark = pytest.mark.gpu
 TOL = 2e-4
 
 
-def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3, mean_loss=False):
+def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3, mean_loss=False, precision=None,
+          checkpoint_every=0):
     import torch
     from cnncrf import scenes
+    from cnncrf import _lib as L
     from cnncrf.train import Trainer
+    precision = L.FP32 if precision is None else precision
     cfg = oracle.make_cfg(num_layers=layers, topology=topology, in_channels=3, feat_channels=F, unary=1,
                           with_pairwise=1, pw_channels=P, precision=32, disp_min=0.0, disp_max=float(D - 1))
     params = oracle.xavier_params(cfg, seed=seed)
     sc = [scenes.voronoi_scene(W, H, D, seed=seed + 10 * i, cells=4, off_range=(1, D - 2), slope=0.05)
           for i in range(n)]
     t = Trainer(n, W, H, num_layers=layers, topology=topology, feat_channels=F, pw_channels=P, disp_max=float(D - 1),
-                mean_loss=mean_loss)
+                mean_loss=mean_loss, precision=precision, checkpoint_every=checkpoint_every)
     t.init_xavier(seed)
     left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
     right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
@@ -184,7 +187,7 @@ def test_full_size_training_step(cuda, oracle):
     left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
     right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
     gt = torch.from_numpy(np.stack([np.clip(np.rint(s["disp"]), 0, D - 1).astype(np.int32) for s in sc])).cuda()
-    t = Trainer(n, W, H)  # mean loss: lr 1e-3 and momentum 0.9 of the task
+    t = Trainer(n, W, H, precision=L.FP32, checkpoint_every=0)  # the exact mode: equals the inference net
     t.init_xavier(0)
     vol, pw = t.forward(left, right)
     net = StereoNet(7, n, 3, H + 14, W + 14, topology=L.TOPO_ALL3X3, unary=L.UNARY_ONE_MINUS_DOT,
@@ -196,7 +199,11 @@ def test_full_size_training_step(cuda, oracle):
     ivol = net.predict(torch.from_numpy(lp).cuda(), torch.from_numpy(rp).cuda())
     assert torch.equal(vol.reshape(ivol.shape), ivol)
     assert torch.equal(pw.reshape(net.pairwise_out.shape), net.pairwise_out)
-    del net, ivol
+    del net, ivol, t
+    # the task's step: BF16 activations, checkpoints, mean loss, lr 1e-3, momentum 0.9
+    t = Trainer(n, W, H)
+    t.init_xavier(0)
+    t.step(left, right, gt, lr=0.0, momentum=0.9)  # warm up, no update
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     l1 = t.step(left, right, gt, lr=1e-3, momentum=0.9)
@@ -231,3 +238,63 @@ def test_mean_loss_scaling(cuda, oracle):
         # the scale 1 / pixels is no power of two: the FP32 sums round differently
         ref = t.get_grad(i) / (t.n * npx)
         np.testing.assert_allclose(tm.get_grad(i), ref, rtol=2e-5, atol=2e-5 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("prec,r", [("FP32", 2), ("FP32", 3), ("BF16", 2), ("BF16", 3)])
+def test_checkpointing_changes_no_bit(cuda, oracle, prec, r):
+    """Recomputing the layers between checkpoints during backward gives the
+    keep-all step's losses and gradients exactly."""
+    torch = cuda
+    from cnncrf import _lib as L
+    kw = dict(layers=5, F=100, P=64, precision=getattr(L, prec))
+    _, params, t0, left, right, _, gt, _ = setup(oracle, checkpoint_every=0, **kw)
+    _, _, tr, _, _, _, _, _ = setup(oracle, checkpoint_every=r, **kw)
+    g_t = torch.from_numpy(gt).cuda()
+    for t in (t0, tr):
+        t.forward(left, right)
+    l0, y0 = t0.hinge(g_t)
+    lr_, yr = tr.hinge(g_t)
+    assert np.array_equal(l0, lr_) and torch.equal(y0, yr)
+    t0.backward()
+    tr.backward()
+    for i in range(len(params)):
+        assert np.array_equal(t0.get_grad(i), tr.get_grad(i)), i
+
+
+def test_bf16_mode_against_fp64_oracle(cuda, oracle):
+    """The BF16 mode (tensor-core forward, BF16 activations, FP32 gradients):
+    the volume and every slot's gradient against the FP64 oracle, errors
+    relative to the largest value, stated per output."""
+    torch = cuda
+    from cnncrf import _lib as L
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, layers=3, F=100, P=64, precision=L.BF16,
+                                                       checkpoint_every=2)
+    cfg64 = oracle.make_cfg(**{k: getattr(cfg, k) for k, _ in cfg._fields_})
+    cfg64.precision = 64
+    vol, pw = t.forward(left, right)
+    rng = np.random.default_rng(11)
+    gvol = rng.standard_normal(tuple(vol.shape)).astype(np.float32)
+    gpw = rng.standard_normal(tuple(pw.shape)).astype(np.float32)
+    t.backward(torch.from_numpy(gvol).cuda(), torch.from_numpy(gpw).cuda())
+    errs = {}
+    g64 = None
+    for i, (lp, rp) in enumerate(pads):
+        v64, p64 = oracle.predict(cfg64, params, lp, rp, lst)
+        errs.setdefault("volume", []).append(np.abs(vol[i].cpu().numpy() - v64).max())
+        errs.setdefault("pairwise", []).append(np.abs(pw[i].cpu().numpy() - p64).max() / np.abs(p64).max())
+        g = oracle.predict_backward(cfg64, params, lp, rp, lst, gvol[i], gpw[i])
+        g64 = g if g64 is None else [a + b for a, b in zip(g64, g)]
+    for i in range(len(params)):
+        errs["grad%d" % i] = [np.abs(t.get_grad(i) - g64[i]).max() / max(np.abs(g64[i]).max(), 1e-12)]
+    print("BF16 mode vs FP64:", {k: float("%.2e" % max(v)) for k, v in errs.items()})
+    assert max(errs["volume"]) < 2e-2  # 1 - <fL, fR> on BF16 features (measured 3e-3)
+    assert max(errs["pairwise"]) < 5e-2  # measured 4e-3
+    npf = 2 * cfg.num_layers
+    for i in range(npf):  # feature net (measured 5e-3 .. 7e-3)
+        assert errs["grad%d" % i][0] < 2e-2, (i, errs["grad%d" % i])
+    # pairwise net (measured up to 8.5e-2): d|h|/dh = sign(h), and where h is
+    # near 0 BF16 and FP64 can fall on opposite sides of the kink; a few such
+    # pixels out of ~1800 give errors of this size
+    for i in range(npf, len(params)):
+        assert errs["grad%d" % i][0] < 0.15, (i, errs["grad%d" % i])
+
