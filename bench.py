@@ -216,12 +216,101 @@ def build_stereo(cnncrf, wl, precision, stream):
     return st
 
 
+def train_setup(n=4, W=512, H=256, D=128, fp32=False):
+    """The training step of 4 crops of 512 x 256 from the KITTI-shaped
+    generator with its ground truth, D = 128, the 7-layer 100-channel nets."""
+    import numpy as np
+    import torch
+    import cnncrf
+    from cnncrf import scenes
+    from cnncrf.train import Trainer
+    sc = [scenes.kitti_scene(W, H, D, seed=40 + i) for i in range(n)]
+    left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
+    right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
+    gt = torch.from_numpy(np.stack([np.clip(np.rint(s["disp"]), 0, D - 1).astype(np.int32) for s in sc])).cuda()
+    kw = dict(precision=cnncrf.FP32, checkpoint_every=0) if fp32 else {}
+    t = Trainer(n, W, H, disp_max=float(D - 1), **kw)
+    t.init_xavier(0)
+    return t, left, right, gt
+
+
+def run_train(args):
+    """Training steps per second: forward, hinge on the loss-augmented CRF,
+    the adjoints, SGD with momentum (lr 1e-3, momentum 0.9)."""
+    import torch
+    from cnncrf import _lib
+    t, left, right, gt = train_setup(n=args.train_pairs, fp32=args.precision == "fp32")
+    for _ in range(max(args.warmup, 3)):
+        t.step(left, right, gt, lr=1e-3, momentum=0.9)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(args.steps):
+        losses = t.step(left, right, gt, lr=1e-3, momentum=0.9)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    _lib.profile_reset()
+    _lib.profile_enable(True)
+    for _ in range(3):
+        t.step(left, right, gt, lr=1e-3, momentum=0.9)
+    torch.cuda.synchronize()
+    _lib.profile_enable(False)
+    prof = {k: _lib.profile_query(k) for k in _lib.profile_kernels()}
+    tot = sum(v for _, v in prof.values()) or 1.0
+    line = {"metric": "training steps/s, %d crops 512x256 D=128 (7x3x3 100ch + pairwise nets, CRF hinge, SGD)"
+                      % args.train_pairs,
+            "value": 1000.0 / ms, "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16" if args.precision == "bf16" else "f32", "data": "synthetic (KITTI-shaped crops)",
+            "config": {"workload": "train%dx512x256_d128" % args.train_pairs,
+                       "checkpoint_every": 0 if args.precision == "fp32" else 3,
+                       "lr": 1e-3, "momentum": 0.9, "loss": "mean structured hinge"},
+            "loss_per_pixel": [float(x) for x in losses], "clocks": clk,
+            "kernels": {k: {"launches": n // 3, "ms_per_step": round(v / 3, 3), "share": round(v / tot, 4)}
+                        for k, (n, v) in sorted(prof.items(), key=lambda kv: -kv[1][1])}}
+    print(json.dumps(line))
+    return 0
+
+
 def run_profile(args):
-    """The batched device step alone, for ncu: eager launches of one group of
-    --batch pairs, no timing, FP32 comparison or CPU leg."""
+    """The device work alone, for ncu: eager launches, no timing, FP32
+    comparison or CPU leg.  kitti: one group of --batch pairs; uneven: the
+    uneven batch; train: training steps."""
     import torch
     import cnncrf
     wl = WORKLOAD
+    if args.workload == "train":
+        t, left, right, gt = train_setup(n=args.train_pairs, fp32=args.precision == "fp32")
+        for _ in range(args.warmup + args.steps):
+            t.step(left, right, gt, lr=1e-3, momentum=0.9)
+        torch.cuda.synchronize()
+        print("profile run done")
+        return 0
+    if args.workload == "uneven":
+        from cnncrf import scenes
+        from cnncrf.api import StereoBatch
+        stream = torch.cuda.Stream()
+        with torch.cuda.stream(stream):
+            sc = scenes.uneven_scenes(args.per_shape)
+            b = StereoBatch(precision=cnncrf.BF16, unary=cnncrf.UNARY_ONE_MINUS_DOT, topology=cnncrf.TOPO_ALL3X3,
+                            crf_shape=cnncrf.RHO_LINEAR, num_layers=wl["layers"], seed=wl["seed"], graph=False,
+                            stream=stream, group_size=max(1, args.per_shape // 2))
+            for x in sc:
+                b.add_pair(x["W"], x["H"], 0.0, 1.0, float(x["D"] - 1))
+            dl = [torch.from_numpy(x["left"]).cuda() for x in sc]
+            dr = [torch.from_numpy(x["right"]).cuda() for x in sc]
+            for _ in range(args.warmup + args.steps):
+                for i in range(len(sc)):
+                    b.set_images(i, dl[i], dr[i])
+                b.run(wl["L1"], wl["L2"], wl["delta"], wl["crf_iters"], wl["lam"])
+            b.check()
+            torch.cuda.synchronize()
+        print("profile run done")
+        return 0
     precision = cnncrf.BF16 if args.precision == "bf16" else cnncrf.FP32
     stream = torch.cuda.Stream()
     with torch.cuda.stream(stream):
@@ -433,9 +522,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="kitti", choices=["kitti", "uneven"],
-                    help="uneven: --per-shape pairs of each of four sizes / ranges in one batch")
+    ap.add_argument("--workload", default="kitti", choices=["kitti", "uneven", "train"],
+                    help="uneven: --per-shape pairs of each of four sizes / ranges in one batch; "
+                         "train: the training step of 4 crops of 512 x 256, D = 128")
     ap.add_argument("--per-shape", type=int, default=8)
+    ap.add_argument("--train-pairs", type=int, default=4, help="crops per training step (train workload)")
     ap.add_argument("--no-autotune", action="store_true", help="run the default CRF tile (no tile tuning)")
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"],
                     help="profile: only warm-up + `steps` device steps of the path (for ncu captures)")
@@ -446,6 +537,8 @@ def main():
         return run_profile(args)
     if args.workload == "uneven":
         return run_uneven(args)
+    if args.workload == "train":
+        return run_train(args)
 
     import numpy as np
     import torch

@@ -575,6 +575,16 @@ int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pi
                    st);
 }
 
+int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st)
+{
+    const int ns = train_wgrad_splits(P);
+    const long chunk = (P + ns - 1) / ns;
+    k_bias_part<<<ns, 128, 0, st>>>(dz, Cout, P, chunk, partb);
+    k_bias_reduce<<<1, 128, 0, st>>>(partb, ns, Cout, db);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st)
 {

@@ -106,6 +106,16 @@ int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pi
                 int kh, int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st);
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st);
+int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st); // db += sum dz
+// the weight gradient on the tensor cores (k_wgrad_tc.cu): dz dense FP32 [nimg][Ho][Wo][Cout], the
+// layer input BF16 at the given element strides; dw (npz layout) += dW.  scratch: wgrad_tc_scratch_bytes,
+// 1024-byte aligned; err: the bounded-wait error flag
+bool wgrad_tc_supported(int Cout, int Cin, int kh, int kw);
+int wgrad_tc_splits(int kh, long steps);
+size_t wgrad_tc_scratch_bytes(int nimg, int Ho, int Wo, int Hin, int Cout, int Cin, int kh, int kw, int splits);
+int wgrad_tc(const float *dz, int Cout, const void *in, long in_pix, long in_row, long in_img, int Cin, int kh,
+             int kw, int nimg, int Ho, int Wo, void *scratch, size_t scratch_bytes, float *dw, int *err,
+             cudaStream_t st);
 int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st);
 int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,
                 int D, float lam, const float rho[9], float L2, int delta, float gscale, float *gvol, float *gpw,

@@ -62,6 +62,8 @@ struct cnncrf_train {
     DevBuf gvol, gpw, df[2], dy, dyb, padb, part, partb, gh;
     DevBuf aug, wts, labels, crfws, contrib, rows, err, tcerr;
     size_t crfws_bytes = 0;
+    DevBuf wgs; // the tensor-core weight gradient's planar copies and partial sums
+    size_t wgs_bytes = 0;
 
     int build();
     int refresh();
@@ -218,6 +220,17 @@ int cnncrf_train::build()
             Pmax = std::max(Pmax, (long)n * Ly.hout() * Ly.wout());
             Kmax = std::max(Kmax, Ly.kh * Ly.kw * Ly.cin);
         }
+    // the BF16 mode's tensor-core weight gradients: scratch for the largest layer
+    if (bf16 && d.tc_wgrad)
+        for (auto *v : {&feat, &pw})
+            for (auto &Ly : *v)
+                if (Ly.act == 1 && Ly.cin >= 16 && k::wgrad_tc_supported(Ly.cout, Ly.cin, Ly.kh, Ly.kw)) {
+                    const long steps = (long)n * Ly.hout() * ((Ly.wout() + 63) / 64);
+                    wgs_bytes = std::max(wgs_bytes, k::wgrad_tc_scratch_bytes(n, Ly.hout(), Ly.wout(), Ly.hin,
+                                                                              Ly.cout, Ly.cin, Ly.kh, Ly.kw,
+                                                                              k::wgrad_tc_splits(Ly.kh, steps)));
+                }
+    if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
     const int ns = k::train_wgrad_splits(Pmax); // the most splits any layer uses
     CNNCRF_TRY(part.reserve(sizeof(float) * (size_t)ns * 128 * Kmax));
     CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
@@ -390,9 +403,16 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
 {
     const int Ho = L.hout(), Wo = L.wout();
     CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
-    CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo,
-                              part.as<float>(), gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr,
-                              partb.as<float>(), st));
+    if (in_bf16 && wgs_bytes && k::wgrad_tc_supported(L.cout, L.cin, L.kh, L.kw)) { // BF16 mode, tensor cores
+        CNNCRF_TRY(k::wgrad_tc(dz, L.cout, in, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo, wgs.get(),
+                               wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
+        if (L.bslot >= 0)
+            CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
+    } else {
+        CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo,
+                                  part.as<float>(), gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr,
+                                  partb.as<float>(), st));
+    }
     if (!dprev) return CNNCRF_OK;
     const int ph = L.kh - 1, pwd = L.kw - 1;
     CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
@@ -470,6 +490,7 @@ int cnncrf_train_default_desc(cnncrf_train_desc *d)
     d->mean_loss = 1;
     d->precision = CNNCRF_BF16;
     d->checkpoint_every = 3;
+    d->tc_wgrad = 1;
     return CNNCRF_OK;
 }
 

@@ -358,6 +358,8 @@ typedef struct cnncrf_train_desc {
                            and master weights; CNNCRF_FP32: the exact path (forward equals the oracle's) */
     int checkpoint_every; /* r > 0 (default 3): keep every r-th feature layer's output and the last,
                              recompute the others during backward; 0: keep all */
+    int tc_wgrad;       /* BF16 mode: 1 (default) the weight gradients of layers with 16..128 input
+                           channels on the tensor cores (dz rounded to BF16); 0: on the CUDA cores (FP32 dz) */
 } cnncrf_train_desc;
 
 int cnncrf_train_default_desc(cnncrf_train_desc *d);

@@ -15,7 +15,7 @@ TOL = 2e-4
 
 
 def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3, mean_loss=False, precision=None,
-          checkpoint_every=0):
+          checkpoint_every=0, tc_wgrad=True):
     import torch
     from cnncrf import scenes
     from cnncrf import _lib as L
@@ -27,7 +27,7 @@ def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3
     sc = [scenes.voronoi_scene(W, H, D, seed=seed + 10 * i, cells=4, off_range=(1, D - 2), slope=0.05)
           for i in range(n)]
     t = Trainer(n, W, H, num_layers=layers, topology=topology, feat_channels=F, pw_channels=P, disp_max=float(D - 1),
-                mean_loss=mean_loss, precision=precision, checkpoint_every=checkpoint_every)
+                mean_loss=mean_loss, precision=precision, checkpoint_every=checkpoint_every, tc_wgrad=tc_wgrad)
     t.init_xavier(seed)
     left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
     right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
@@ -298,3 +298,38 @@ def test_bf16_mode_against_fp64_oracle(cuda, oracle):
     for i in range(npf, len(params)):
         assert errs["grad%d" % i][0] < 0.15, (i, errs["grad%d" % i])
 
+
+
+@pytest.mark.parametrize("layers,topology,n,W,H", [(3, 1, 2, 40, 22), (4, 1, 1, 150, 37), (3, 0, 3, 97, 19)])
+def test_tensor_core_weight_gradient_matches_cuda_cores(cuda, oracle, layers, topology, n, W, H):
+    """The BF16 mode's weight gradients of the layers with >= 16 input
+    channels on the tensor cores (dz rounded to BF16, FP32 accumulation)
+    against the CUDA-core path (FP32 dz) of the same forward and output
+    gradients.  Every other slot (biases, the first layers, the pairwise head)
+    comes from the same kernels and must match bit for bit; the tensor-core
+    slots within 1e-2 of their largest value (BF16 dz: a relative rounding
+    of 2^-9 per term).  Widths 40, 150 and 97 leave ragged 64-pixel chunks;
+    topology 0 has 2 x 2 kernels."""
+    torch = cuda
+    from cnncrf import _lib as L
+    kw = dict(layers=layers, topology=topology, n=n, W=W, H=H, F=100, P=64, precision=L.BF16, checkpoint_every=2)
+    _, params, t_tc, left, right, _, _, _ = setup(oracle, tc_wgrad=True, **kw)
+    t_cc = setup(oracle, tc_wgrad=False, **kw)[2]
+    vol, pw = t_tc.forward(left, right)
+    vol2, pw2 = t_cc.forward(left, right)
+    assert torch.equal(vol, vol2) and torch.equal(pw, pw2)
+    rng = np.random.default_rng(5)
+    gvol = torch.from_numpy(rng.standard_normal(tuple(vol.shape)).astype(np.float32)).cuda()
+    gpw = torch.from_numpy(rng.standard_normal(tuple(pw.shape)).astype(np.float32)).cuda()
+    t_tc.backward(gvol, gpw)
+    t_cc.backward(gvol, gpw)
+    tc_slots = {2 * l for l in range(1, layers)} | {2 * layers + 2}
+    errs = {}
+    for i in range(len(params)):
+        a, b = t_tc.get_grad(i), t_cc.get_grad(i)
+        if i in tc_slots:
+            errs[i] = np.abs(a - b).max() / max(np.abs(b).max(), 1e-12)
+        else:
+            assert np.array_equal(a, b), i
+    print("tensor-core vs CUDA-core weight gradients:", {k: float("%.2e" % v) for k, v in errs.items()})
+    assert max(errs.values()) < 1e-2, errs
