@@ -50,7 +50,7 @@ class TrainDesc(C.Structure):
                 ("disp_min", C.c_float), ("disp_step", C.c_float), ("disp_max", C.c_float), ("lam", C.c_float),
                 ("L1", C.c_float), ("L2", C.c_float), ("delta", C.c_int), ("crf_shape", C.c_int),
                 ("crf_slack", C.c_float), ("crf_iters", C.c_int), ("mean_loss", C.c_int), ("precision", C.c_int),
-                ("checkpoint_every", C.c_int), ("tc_wgrad", C.c_int)]
+                ("checkpoint_every", C.c_int), ("tc_wgrad", C.c_int), ("tc_dgrad", C.c_int)]
 
 
 class StereoOptions(C.Structure):

@@ -37,7 +37,7 @@ class Trainer:
     def __init__(self, npairs, width, height, num_layers=7, topology=L.TOPO_ALL3X3, feat_channels=100,
                  pw_channels=64, disp_min=0.0, disp_step=1.0, disp_max=127.0, lam=1.0, L1=0.5, L2=1.5, delta=3,
                  crf_shape=L.RHO_LINEAR, crf_slack=0.5, crf_iters=8, mean_loss=True, precision=L.BF16,
-                 checkpoint_every=3, tc_wgrad=True, stream=None):
+                 checkpoint_every=3, tc_wgrad=True, tc_dgrad=True, stream=None):
         d = TrainDesc()
         call("cnncrf_train_default_desc", C.byref(d))
         d.num_layers, d.topology, d.feat_channels, d.pw_channels = num_layers, topology, feat_channels, pw_channels
@@ -46,6 +46,7 @@ class Trainer:
         d.mean_loss = 1 if mean_loss else 0
         d.precision, d.checkpoint_every = precision, checkpoint_every
         d.tc_wgrad = 1 if tc_wgrad else 0
+        d.tc_dgrad = 1 if tc_dgrad else 0
         self._h = C.c_void_p()
         call("cnncrf_train_create", C.byref(self._h), C.byref(d), npairs, width, height)
         self.stream = stream

@@ -28,7 +28,8 @@
 //               the epilogue
 //   warps 2..5  epilogue: tcgen05.ld of both halves (one pixel per thread
 //               per half), bias + tanh, then store BF16 NHWC / L2-normalise
-//               / apply the pairwise net's 1x1 head
+//               / apply the pairwise net's 1x1 head; or (mode 3, a training
+//               step's input gradient) store the sums as FP32 NHWC
 // TMEM holds two tiles (four 128-column accumulators): the epilogue of tile i
 // overlaps the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout
 // the role raises the CTA abort flag and the global error flag, in-flight
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tc::prefetch_tmap(&tmA2);
         tc::prefetch_tmap(&tmB);
     }
-    for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias[i];
+    for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
     if (p.mode == 2)
         for (int i = threadIdx.x; i < 2 * NP; i += NUM_THREADS) shead[i] = p.head[i];
     if (warp == 1) {
@@ -282,6 +283,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll 1
                 for (int c = 0; c < NP / 16; ++c) {
                     tc::tmem_ld16(ta + c * 16, v);
+                    if (p.mode == 3) {
+                        if (valid) {
+                            float *o = (float *)p.out + pix * p.cp_out + c * 16;
+#pragma unroll
+                            for (int g = 0; g < 4; ++g) {
+                                if (c * 16 + 4 * g + 3 < p.cout)
+                                    *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2],
+                                                                         v[4 * g + 3]);
+                                else
+#pragma unroll
+                                    for (int j = 0; j < 4; ++j)
+                                        if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
+                            }
+                        }
+                        continue;
+                    }
 #pragma unroll
                     for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
                     if (p.mode == 2) {
@@ -403,16 +420,22 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     p.num_tiles = a.n_img * p.Ho * p.tiles_x;
     p.mode = a.mode;
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
-    if (a.mode != 2 && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);
+    if (a.mode < 0 || a.mode > 3) return fail(CNNCRF_EINVAL, "conv_tc: mode %d", a.mode);
+    // BF16 outputs store whole 16-channel groups; FP32 input gradients float4 groups below cout
+    const bool bf16_out = a.mode == 0 || a.mode == 1;
+    if (bf16_out && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);
+    if (a.mode == 3 && (a.cp_out % 4 != 0 || a.cp_out < a.cout || a.cout > a.np))
+        return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d / cout %d", a.cp_out, a.cout);
+    if (a.mode != 3 && !a.bias) return fail(CNNCRF_EINVAL, "conv_tc: bias");
     switch (a.np) {
     case 64:
-        if (a.mode != 2 && a.cp_out < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        if (bf16_out && a.cp_out < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<64>(a, p, st);
     case 112:
-        if (a.mode != 2 && a.cp_out < 112) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        if (bf16_out && a.cp_out < 112) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<112>(a, p, st);
     case 128:
-        if (a.mode != 2 && a.cp_out < 128) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
+        if (bf16_out && a.cp_out < 128) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");
         return launch<128>(a, p, st);
     default:
         return fail(CNNCRF_EUNSUPPORTED, "conv_tc: N = %d (64, 112, 128 built)", a.np);

@@ -64,6 +64,22 @@ __global__ void k_w16(const float *__restrict__ w, int Cout, int Cin, int kh, in
     w16[i] = __float2bfloat16_rn(v);
 }
 
+// the input gradient's tensor-core layout: w16d[ci][ky][kx][co] = w[co][ci][ky][kx]
+// (transposed, not flipped: the gradient is the valid convolution of the
+// (kh-1, kw-1)-padded output gradient with the unflipped kernel), zero padded
+// to [np][kh*kw][cp]
+__global__ void k_w16_dgrad(const float *__restrict__ w, int Cout, int Cin, int kh, int kw, int np, int cp,
+                            __nv_bfloat16 *__restrict__ w16d)
+{
+    const long taps = (long)kh * kw, i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (long)np * taps * cp) return;
+    const int co = (int)(i % cp);
+    const long r = i / cp;
+    const int t = (int)(r % taps), ci = (int)(r / taps), ky = t / kw, kx = t % kw;
+    const float v = (ci < Cin && co < Cout) ? w[(((long)co * Cin + ci) * kh + ky) * kw + kx] : 0.0f;
+    w16d[i] = __float2bfloat16_rn(v);
+}
+
 // BF16 L2 normalisation: f = y / |y| per pixel in FP32, rounded once; a warp per pixel
 __global__ void k_l2norm_bf16(const __nv_bfloat16 *__restrict__ y, long npx, int C, int cs,
                               __nv_bfloat16 *__restrict__ f)
@@ -111,6 +127,45 @@ __global__ void k_tanh_bwd(float *__restrict__ dy, const T *__restrict__ y, long
         const float v = ld(y + (i / C) * ys + i % C);
         dy[i] = dy[i] * (1.0f - v * v);
     }
+}
+
+// dz = dy * (1 - y^2) in place (dense FP32 [n][H][W][C], y BF16 at channel
+// stride ys), and its BF16 copy with a zero border of p rows and q columns and
+// channels zero padded to cp: [n][H + 2p][W + 2q][cp].  A thread per padded
+// pixel and 8-channel group (one 16-byte store).
+__global__ void k_tanh_bwd_pad(float *__restrict__ dy, const __nv_bfloat16 *__restrict__ y, int H, int W, int C,
+                               int ys, int p, int q, int cp, long total, __nv_bfloat16 *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int groups = cp >> 3, g = (int)(i % groups);
+    const long px = i / groups;
+    const int Wp = W + 2 * q, Hp = H + 2 * p;
+    const int xp = (int)(px % Wp);
+    const long r = px / Wp;
+    const int yp = (int)(r % Hp), img = (int)(r / Hp);
+    const int x = xp - q, yy = yp - p;
+    uint32_t u[4] = {0u, 0u, 0u, 0u};
+    if (x >= 0 && x < W && yy >= 0 && yy < H) {
+        const long pix = ((long)img * H + yy) * W + x;
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = g * 8 + j;
+            v[j] = 0.0f;
+            if (c < C) {
+                const float a = __bfloat162float(y[pix * ys + c]);
+                v[j] = dy[pix * C + c] * (1.0f - a * a);
+                dy[pix * C + c] = v[j];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+            u[j] = *(uint32_t *)&b2;
+        }
+    }
+    *(uint4 *)(out + px * cp + g * 8) = make_uint4(u[0], u[1], u[2], u[3]);
 }
 
 // out [n][H + 2p][W + 2q][C] = in [n][H][W][C] with a zero border
@@ -448,6 +503,28 @@ int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp,
 {
     const long n = (long)np * kh * kw * cp;
     k_w16<<<ceil_div(n, 256), 256, 0, st>>>(w, Cout, Cin, kh, kw, np, cp, (__nv_bfloat16 *)w16);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_w16_dgrad(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16d, cudaStream_t st)
+{
+    const long n = (long)np * kh * kw * cp;
+    k_w16_dgrad<<<ceil_div(n, 256), 256, 0, st>>>(w, Cout, Cin, kh, kw, np, cp, (__nv_bfloat16 *)w16d);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_tanh_bwd_pad(float *dy, const void *y, int nimg, int H, int W, int C, int ys, int p, int q, int cp,
+                       void *out, cudaStream_t st)
+{
+    if (cp % 8 || cp < C || ((uintptr_t)out & 15)) return fail(CNNCRF_EINVAL, "tanh_bwd_pad: channel padding");
+    const long total = (long)nimg * (H + 2 * p) * (W + 2 * q) * (cp / 8);
+    {
+        CNNCRF_PROF("tanh_bwd", st);
+        k_tanh_bwd_pad<<<ceil_div(total, 256), 256, 0, st>>>(dy, (const __nv_bfloat16 *)y, H, W, C, ys, p, q, cp,
+                                                             total, (__nv_bfloat16 *)out);
+    }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

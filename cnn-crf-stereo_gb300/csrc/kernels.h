@@ -53,7 +53,8 @@ struct TcConvArgs {
     int np, cout, kh, kw;
     const float *bias; // [np] zero padded
     const float *head; // [2][np] (mode 2)
-    int mode;          // 0 tanh -> BF16, 1 tanh + L2 norm -> BF16, 2 tanh + 1x1 head + abs -> FP32 [2][Ho][Wo]
+    int mode;          // 0 tanh -> BF16, 1 tanh + L2 norm -> BF16, 2 tanh + 1x1 head + abs -> FP32 [2][Ho][Wo],
+                       // 3 the plain sums -> FP32 [n_img][Ho][Wo][cp_out], channels < cout (input gradients)
     void *out;
     int cp_out;
     int *err; // set to 1 if a bounded wait gave up
@@ -88,6 +89,11 @@ int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int 
                          float *b128, cudaStream_t st);
 // the BF16 mode's tensor-core weight layout [np][kh*kw][cp], its L2 normalisation and |1x1| head
 int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16, cudaStream_t st);
+// the input gradient's tensor-core layout [np][kh*kw][cp]: w16d[ci][tap][co] = w[co][ci][ky][kx], unflipped
+int train_w16_dgrad(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16d, cudaStream_t st);
+// dy *= 1 - y^2 (y BF16) and a BF16 copy with a (p, q) zero border and channels padded to cp (conv_tc's input)
+int train_tanh_bwd_pad(float *dy, const void *y, int nimg, int H, int W, int C, int ys, int p, int q, int cp,
+                       void *out, cudaStream_t st);
 int train_l2norm_bf16(const void *y, long npx, int C, int cs, void *f, cudaStream_t st);
 int train_head2_bf16(const void *y2, int nimg, int npx, int P, int cs, const float *wh, float *out, cudaStream_t st);
 // Activations y are FP32 or BF16 (bf16) at channel stride ys; gradients are dense FP32 [px][C].

@@ -30,6 +30,7 @@ struct TLayer {
     int hin, win;        // input extent
     DevBuf wt, wd, b128; // conv_simt layout, input-gradient layout, padded bias
     DevBuf w16;          // the BF16 mode's tensor-core layout
+    DevBuf w16d;         // its input-gradient layout (tensor-core input gradients)
     int hout() const { return hin - kh + 1; }
     int wout() const { return win - kw + 1; }
 };
@@ -64,6 +65,7 @@ struct cnncrf_train {
     size_t crfws_bytes = 0;
     DevBuf wgs; // the tensor-core weight gradient's planar copies and partial sums
     size_t wgs_bytes = 0;
+    DevBuf dpad; // the tensor-core input gradient's BF16 padded output gradient
 
     int build();
     int refresh();
@@ -148,6 +150,8 @@ int cnncrf_train::build()
                 if (bf16 && Ly.cin >= 16) { // the tensor-core layers
                     const int npd = v == &feat ? np_feat : np_pw, cpi = v == &feat ? cp_feat : cp_pw;
                     CNNCRF_TRY(Ly.w16.reserve(2 * (size_t)npd * Ly.kh * Ly.kw * cpi));
+                    if (d.tc_dgrad && Ly.cout <= 128 && Ly.kw <= 3)
+                        CNNCRF_TRY(Ly.w16d.reserve(2 * (size_t)umma_n(Ly.cin) * Ly.kh * Ly.kw * pad_to(Ly.cout, 64)));
                 }
             }
     // the stored list -d (stereo/operators/stereocorrelation.cpp:83-85); integers only
@@ -231,6 +235,13 @@ int cnncrf_train::build()
                                                                               k::wgrad_tc_splits(Ly.kh, steps)));
                 }
     if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
+    size_t dpad_bytes = 0;
+    for (auto *v : {&feat, &pw})
+        for (auto &Ly : *v)
+            if (Ly.w16d.get())
+                dpad_bytes = std::max(dpad_bytes, 2 * (size_t)n * (Ly.hout() + 2 * (Ly.kh - 1)) *
+                                                      (Ly.wout() + 2 * (Ly.kw - 1)) * pad_to(Ly.cout, 64));
+    if (dpad_bytes) CNNCRF_TRY(dpad.reserve(dpad_bytes));
     const int ns = k::train_wgrad_splits(Pmax); // the most splits any layer uses
     CNNCRF_TRY(part.reserve(sizeof(float) * (size_t)ns * 128 * Kmax));
     CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
@@ -259,6 +270,9 @@ int cnncrf_train::refresh()
                     CNNCRF_TRY(k::train_w16(param(Ly.wslot), Ly.cout, Ly.cin, Ly.kh, Ly.kw,
                                             v == &feat ? np_feat : np_pw, v == &feat ? cp_feat : cp_pw, Ly.w16.get(),
                                             st));
+                if (Ly.w16d.get())
+                    CNNCRF_TRY(k::train_w16_dgrad(param(Ly.wslot), Ly.cout, Ly.cin, Ly.kh, Ly.kw, umma_n(Ly.cin),
+                                                  pad_to(Ly.cout, 64), Ly.w16d.get(), st));
             }
     return CNNCRF_OK;
 }
@@ -402,7 +416,12 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
                              const void *y, int ys, float *dz, float *dprev)
 {
     const int Ho = L.hout(), Wo = L.wout();
-    CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
+    const int ph = L.kh - 1, pwd = L.kw - 1;
+    const bool tcd = dprev && L.w16d.get(); // the input gradient on the tensor cores (BF16 mode)
+    if (tcd)
+        CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, n, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64), dpad.get(), st));
+    else
+        CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
     if (in_bf16 && wgs_bytes && k::wgrad_tc_supported(L.cout, L.cin, L.kh, L.kw)) { // BF16 mode, tensor cores
         CNNCRF_TRY(k::wgrad_tc(dz, L.cout, in, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo, wgs.get(),
                                wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
@@ -414,7 +433,14 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
                                   partb.as<float>(), st));
     }
     if (!dprev) return CNNCRF_OK;
-    const int ph = L.kh - 1, pwd = L.kw - 1;
+    if (tcd) { // dprev = the valid convolution of the padded dz with the unflipped, transposed kernel
+        k::TcConvArgs t{};
+        t.in = dpad.get(), t.n_img = n, t.Hin = Ho + 2 * ph, t.Win = Wo + 2 * pwd;
+        t.cp_in = pad_to(L.cout, 64), t.cin = L.cout;
+        t.wt = L.w16d.get(), t.np = umma_n(L.cin), t.cout = L.cin, t.kh = L.kh, t.kw = L.kw;
+        t.mode = 3, t.out = dprev, t.cp_out = L.cin, t.err = tcerr.as<int>();
+        return k::conv_tc(t, st);
+    }
     CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
     const int Hp = Ho + 2 * ph, Wp = Wo + 2 * pwd;
     k::ConvArgs a{padb.as<float>(), Hp, Wp, L.cout, (long)L.cout, (long)Wp * L.cout, L.wd.as<float>(), nullptr,
@@ -491,6 +517,7 @@ int cnncrf_train_default_desc(cnncrf_train_desc *d)
     d->precision = CNNCRF_BF16;
     d->checkpoint_every = 3;
     d->tc_wgrad = 1;
+    d->tc_dgrad = 1;
     return CNNCRF_OK;
 }
 

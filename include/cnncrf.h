@@ -360,6 +360,8 @@ typedef struct cnncrf_train_desc {
                              recompute the others during backward; 0: keep all */
     int tc_wgrad;       /* BF16 mode: 1 (default) the weight gradients of layers with 16..128 input
                            channels on the tensor cores (dz rounded to BF16); 0: on the CUDA cores (FP32 dz) */
+    int tc_dgrad;       /* BF16 mode: 1 (default) the input gradients of those layers on the tensor cores
+                           (dz rounded to BF16, FP32 sums); 0: on the CUDA cores */
 } cnncrf_train_desc;
 
 int cnncrf_train_default_desc(cnncrf_train_desc *d);

@@ -15,7 +15,7 @@ TOL = 2e-4
 
 
 def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3, mean_loss=False, precision=None,
-          checkpoint_every=0, tc_wgrad=True):
+          checkpoint_every=0, tc_wgrad=True, tc_dgrad=True):
     import torch
     from cnncrf import scenes
     from cnncrf import _lib as L
@@ -27,7 +27,8 @@ def setup(oracle, layers=3, topology=1, n=2, W=40, H=22, D=10, F=16, P=8, seed=3
     sc = [scenes.voronoi_scene(W, H, D, seed=seed + 10 * i, cells=4, off_range=(1, D - 2), slope=0.05)
           for i in range(n)]
     t = Trainer(n, W, H, num_layers=layers, topology=topology, feat_channels=F, pw_channels=P, disp_max=float(D - 1),
-                mean_loss=mean_loss, precision=precision, checkpoint_every=checkpoint_every, tc_wgrad=tc_wgrad)
+                mean_loss=mean_loss, precision=precision, checkpoint_every=checkpoint_every, tc_wgrad=tc_wgrad,
+                tc_dgrad=tc_dgrad)
     t.init_xavier(seed)
     left = torch.from_numpy(np.stack([s["left"] for s in sc])).cuda()
     right = torch.from_numpy(np.stack([s["right"] for s in sc])).cuda()
@@ -312,7 +313,8 @@ def test_tensor_core_weight_gradient_matches_cuda_cores(cuda, oracle, layers, to
     topology 0 has 2 x 2 kernels."""
     torch = cuda
     from cnncrf import _lib as L
-    kw = dict(layers=layers, topology=topology, n=n, W=W, H=H, F=100, P=64, precision=L.BF16, checkpoint_every=2)
+    kw = dict(layers=layers, topology=topology, n=n, W=W, H=H, F=100, P=64, precision=L.BF16, checkpoint_every=2,
+              tc_dgrad=False)
     _, params, t_tc, left, right, _, _, _ = setup(oracle, tc_wgrad=True, **kw)
     t_cc = setup(oracle, tc_wgrad=False, **kw)[2]
     vol, pw = t_tc.forward(left, right)
@@ -333,3 +335,40 @@ def test_tensor_core_weight_gradient_matches_cuda_cores(cuda, oracle, layers, to
             assert np.array_equal(a, b), i
     print("tensor-core vs CUDA-core weight gradients:", {k: float("%.2e" % v) for k, v in errs.items()})
     assert max(errs.values()) < 1e-2, errs
+
+
+@pytest.mark.parametrize("layers,topology,n,W,H", [(3, 1, 2, 40, 22), (4, 1, 1, 300, 37), (3, 0, 3, 97, 19)])
+def test_tensor_core_input_gradient_matches_cuda_cores(cuda, oracle, layers, topology, n, W, H):
+    """The BF16 mode's input gradients on the tensor cores (the padded output
+    gradient rounded to BF16, the unflipped transposed kernel in BF16, FP32
+    sums) against the CUDA-core path, weight gradients on the CUDA cores in
+    both.  The slots above the first tensor-core input gradient (the top
+    feature layer, the pairwise net's second layer and head) match bit for
+    bit; every other slot within 2e-2 of its largest value (two BF16
+    roundings per layer, compounded over the layers below).  Width 300 gives
+    two 256-pixel tiles per row, the last one ragged."""
+    torch = cuda
+    from cnncrf import _lib as L
+    kw = dict(layers=layers, topology=topology, n=n, W=W, H=H, F=100, P=64, precision=L.BF16, checkpoint_every=2,
+              tc_wgrad=False)
+    _, params, t_tc, left, right, _, _, _ = setup(oracle, tc_dgrad=True, **kw)
+    t_cc = setup(oracle, tc_dgrad=False, **kw)[2]
+    vol, pw = t_tc.forward(left, right)
+    vol2, pw2 = t_cc.forward(left, right)
+    assert torch.equal(vol, vol2) and torch.equal(pw, pw2)
+    rng = np.random.default_rng(6)
+    gvol = torch.from_numpy(rng.standard_normal(tuple(vol.shape)).astype(np.float32)).cuda()
+    gpw = torch.from_numpy(rng.standard_normal(tuple(pw.shape)).astype(np.float32)).cuda()
+    t_tc.backward(gvol, gpw)
+    t_cc.backward(gvol, gpw)
+    base = 2 * layers
+    same = {base - 2, base - 1, base + 2, base + 3, base + 4}
+    errs = {}
+    for i in range(len(params)):
+        a, b = t_tc.get_grad(i), t_cc.get_grad(i)
+        if i in same:
+            assert np.array_equal(a, b), i
+        else:
+            errs[i] = np.abs(a - b).max() / max(np.abs(b).max(), 1e-12)
+    print("tensor-core vs CUDA-core input gradients:", {k: float("%.2e" % v) for k, v in errs.items()})
+    assert max(errs.values()) < 2e-2, errs
