@@ -269,6 +269,98 @@ __global__ void k_corr_bwd_right(const T *__restrict__ fl, int fs, const float *
     }
 }
 
+// Both sides as one banded product, blocked in registers:
+//   dF[u][c] = -sum_k a(u, k) F[u + o_k][c]
+//   left  (right = 0): o_k =  s_k, a(u, k) = gvol[u][k],         F = fr
+//   right (right = 1): o_k = -s_k, a(u, k) = gvol[u - s_k][k],   F = fl
+// A CTA per (64-pixel tile, row, pair), 256 threads.  Shared memory holds the
+// band matrix As[v][u] = a(u, k) at the partner pixel v = u + o_k (zero where
+// no offset of the list lands; the offsets are distinct) for v in the window
+// x0 + omn .. x0 + 63 + omn + span - 1, and the partner features Fs[v][c]
+// (zero outside the row and past C).  Warp w owns pixels x0 + 8w .. + 7,
+// lane l channels 4l .. 4l + 3: per partner pixel two broadcast loads of As,
+// one load of Fs and 32 FMAs in FP32.
+constexpr int CB_TX = 64, CB_AS = CB_TX + 4;
+
+__device__ __forceinline__ void ld4(const float *p, float *f)
+{
+    const float4 v = *(const float4 *)p;
+    f[0] = v.x, f[1] = v.y, f[2] = v.z, f[3] = v.w;
+}
+__device__ __forceinline__ void ld4(const __nv_bfloat16 *p, float *f)
+{
+    const uint2 v = *(const uint2 *)p;
+    f[0] = __uint_as_float(v.x << 16), f[1] = __uint_as_float(v.x & 0xffff0000u);
+    f[2] = __uint_as_float(v.y << 16), f[3] = __uint_as_float(v.y & 0xffff0000u);
+}
+
+size_t corr_bwd_blk_smem(int span, int Cs, size_t es, int D)
+{
+    const size_t nv = CB_TX - 1 + span;
+    return nv * CB_AS * 4 + ((nv * Cs * es + 15) & ~(size_t)15) + 4 * (size_t)D;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_corr_bwd_blk(const T *__restrict__ F, int fs, const float *__restrict__ gvol,
+                                                      const float *__restrict__ list, int H, int W, int C, int Cs,
+                                                      int D, int right, int omn, int span, float *__restrict__ out)
+{
+    extern __shared__ float4 smem4[];
+    const int NV = CB_TX - 1 + span;
+    float *As = (float *)smem4;
+    T *Fs = (T *)(As + (size_t)NV * CB_AS);
+    int *offs = (int *)((char *)Fs + (((size_t)NV * Cs * sizeof(T) + 15) & ~(size_t)15));
+    const int tid = threadIdx.x, x0 = blockIdx.x * CB_TX, y = blockIdx.y, pair = blockIdx.z;
+    const long row = ((long)pair * H + y) * W;
+    const int vbase = x0 + omn;
+    for (int k = tid; k < D; k += 256) offs[k] = right ? -(int)list[k] : (int)list[k];
+    for (int i = tid; i < NV * CB_AS; i += 256) As[i] = 0.0f;
+    for (int i = tid; i < NV * Cs; i += 256) {
+        const int vr = i / Cs, c = i % Cs, x = vbase + vr;
+        Fs[i] = (x >= 0 && x < W && c < C) ? F[(row + x) * fs + c] : T(0.0f);
+    }
+    __syncthreads();
+    if (!right) {
+        for (int i = tid; i < CB_TX * D; i += 256) {
+            const int r = i / D, k = i % D, u = x0 + r;
+            if (u < W) As[(r + offs[k] - omn) * CB_AS + r] = gvol[(row + u) * D + k];
+        }
+    } else {
+        for (int i = tid; i < NV * D; i += 256) {
+            const int r = i / D, k = i % D, x = vbase + r, ur = x - offs[k] - x0;
+            if (x >= 0 && x < W && ur >= 0 && ur < CB_TX && x0 + ur < W) As[r * CB_AS + ur] = gvol[(row + x) * D + k];
+        }
+    }
+    __syncthreads();
+    const int u0 = (tid >> 5) * 8, c0 = (tid & 31) * 4;
+    if (c0 >= C) return;
+    float acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+    const int v1 = u0 + 7 + span; // partner rows of pixels u0 .. u0 + 7
+#pragma unroll 2
+    for (int vr = u0; vr < v1; ++vr) {
+        float a[8], f[4];
+        ld4(As + vr * CB_AS + u0, a);
+        ld4(As + vr * CB_AS + u0 + 4, a + 4);
+        ld4(Fs + (size_t)vr * Cs + c0, f);
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(a[i], f[j], acc[i][j]);
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int u = x0 + u0 + i;
+        if (u < W)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (c0 + j < C) out[(row + u) * C + c0 + j] = -acc[i][j];
+    }
+}
+
 // ------------------------------------------------------------ weight gradient
 // part[split][co][k] = sum over the split's pixels p of dz[p][co] * A[p][k],
 // A[p][(ky*kw + kx)*Cin + ci] = in(img, oy + ky, ox + kx, ci).  A CTA per
@@ -589,6 +681,25 @@ static int corr_bwd_t(const T *fl, const T *fr, int fs, const float *gvol, const
                       int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st)
 {
     if (C > 128) return fail(CNNCRF_EINVAL, "corr_bwd: %d channels > 128", C);
+    int dev = 0, maxsm = 0;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    {
+        // the blocked kernel (integer lists have distinct offsets: the stored list strictly decreases)
+        const int band = omax - omin + 1, Cs = (C + 3) & ~3;
+        const size_t sm = corr_bwd_blk_smem(band, Cs, sizeof(T), D);
+        if (sm <= (size_t)maxsm) {
+            CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_bwd_blk<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+            const dim3 g(ceil_div(W, CB_TX), H, npairs);
+            {
+                CNNCRF_PROF("corr_bwd", st);
+                k_corr_bwd_blk<T><<<g, 256, sm, st>>>(fr, fs, gvol, d_list, H, W, C, Cs, D, 0, omin, band, dfl);
+                k_corr_bwd_blk<T><<<g, 256, sm, st>>>(fl, fs, gvol, d_list, H, W, C, Cs, D, 1, -omax, band, dfr);
+            }
+            CNNCRF_CHECK_LAUNCH();
+            return CNNCRF_OK;
+        }
+    }
     const int span = 32 + omax - omin;
     const size_t smem = sizeof(float) * (size_t)span * C + sizeof(int) * (size_t)D;
     if (smem > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "corr_bwd: band %d too wide", omax - omin);
