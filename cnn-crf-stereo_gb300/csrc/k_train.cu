@@ -433,17 +433,27 @@ template <class T> __global__ void __launch_bounds__(256) k_wgrad(const WgradArg
 }
 
 // dw[co][ci][kh-1-ky][kw-1-kx] += sum_split part[split][co][k], splits in order
-__global__ void k_wgrad_reduce(const float *__restrict__ part, int nsplit, int Cout, int Cin, int kh, int kw,
-                               float *__restrict__ dw)
+// dw (npz layout) += the sum over splits of part[split][co][k]: 32 outputs
+// per CTA (one per lane), warp w sums splits w, w + 8, ..., then lane sums of
+// the 8 warps in a fixed order (deterministic)
+__global__ void __launch_bounds__(256) k_wgrad_reduce(const float *__restrict__ part, int nsplit, int Cout, int Cin,
+                                                      int kh, int kw, float *__restrict__ dw)
 {
-    const int K = kh * kw * Cin;
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= (long)Cout * K) return;
+    __shared__ float s[8][33];
+    const int K = kh * kw * Cin, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long n = (long)Cout * K, i = (long)blockIdx.x * 32 + lane;
+    float acc = 0.0f;
+    if (i < n)
+        for (int sp = w; sp < nsplit; sp += 8) acc += part[(long)sp * n + i];
+    s[w][lane] = acc;
+    __syncthreads();
+    if (w != 0 || i >= n) return;
+    float t = s[0][lane];
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t += s[j][lane];
     const int co = (int)(i / K), k = (int)(i % K);
-    float s = 0.0f;
-    for (int sp = 0; sp < nsplit; ++sp) s += part[((long)sp * Cout + co) * K + k];
-    const int ci = k % Cin, t = k / Cin, kx = t % kw, ky = t / kw;
-    dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += s;
+    const int ci = k % Cin, tt = k / Cin, kx = tt % kw, ky = tt / kw;
+    dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += t;
 }
 
 // db[co] += sum_p dz[p][co]: per split a partial, then the splits in order
@@ -727,6 +737,18 @@ int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const floa
 
 int train_wgrad_splits(long P) { return (int)std::max(1L, std::min(64L, P / 2048)); }
 
+int train_wgrad_splits_k(long P, int K)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        sms = 148;
+    const long kt = ceil_div(K, WG_KT);
+    long ns = std::max(1L, 4L * sms / kt);
+    ns = std::min(ns, std::max(1L, P / 512));
+    return (int)std::min(ns, 1024L);
+}
+
 template <class T>
 static int wgrad_t(const float *dz, int Cout, const T *in, long in_pix, long in_row, long in_img, int Cin, int kh,
                    int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st)
@@ -736,19 +758,16 @@ static int wgrad_t(const float *dz, int Cout, const T *in, long in_pix, long in_
     a.dz = dz, a.Cout = Cout, a.in = in, a.in_pix = in_pix, a.in_row = in_row, a.in_img = in_img;
     a.Cin = Cin, a.kh = kh, a.kw = kw, a.Ho = Ho, a.Wo = Wo;
     a.P = (long)nimg * Ho * Wo;
-    const int ns = train_wgrad_splits(a.P);
+    const int K = kh * kw * Cin;
+    const int ns = train_wgrad_splits_k(a.P, K);
     a.chunk = (a.P + ns - 1) / ns;
     a.part = part;
-    const int K = kh * kw * Cin;
     {
         CNNCRF_PROF("wgrad", st);
         k_wgrad<T><<<dim3(ceil_div(K, WG_KT), ns), 256, 0, st>>>(a);
-        k_wgrad_reduce<<<ceil_div((long)Cout * K, 256), 256, 0, st>>>(part, ns, Cout, Cin, kh, kw, dw);
-        if (db) {
-            k_bias_part<<<ns, 128, 0, st>>>(dz, Cout, a.P, a.chunk, partb);
-            k_bias_reduce<<<1, 128, 0, st>>>(partb, ns, Cout, db);
-        }
+        k_wgrad_reduce<<<ceil_div((long)Cout * K, 32), 256, 0, st>>>(part, ns, Cout, Cin, kh, kw, dw);
     }
+    if (db) CNNCRF_TRY(train_bias_grad(dz, Cout, a.P, partb, db, st));
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

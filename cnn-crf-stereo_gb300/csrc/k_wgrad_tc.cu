@@ -6,23 +6,27 @@
 //                         dz[p][co] * x[img][oy + ky][ox + kx][ci]
 //
 // is a GEMM per tap with M = output channels, N = input channels and K = the
-// pixels.  Both operands must be K-major (pixels contiguous), so they are
-// first written as planar BF16 copies: dzP[img][co][oy][ox] and, once per kx,
-// xP[kx][img][ci][y][ox] = x[img][y][ox + kx][ci] (the kx shift is baked into
-// the copy: a TMA box must start on a 16-byte boundary in x, and a K-major
-// operand cannot start mid-row).  A K step is 64 consecutive pixels of one
-// output row: one 128-row box of dzP (rows past Cout arrive as zeros) and kw
-// boxes of xP at row oy + ky (rows past Cin and pixels past Wo arrive as
-// zeros, so they add nothing).
+// pixels.  Both operands are read as they lie in memory, channels innermost
+// (NHWC), which makes them MN-major: a TMA box of 64 channels x 64 pixels
+// lands as 64 rows (one per pixel, K) of 128 bytes (64 channels, MN) in the
+// 128-byte swizzle, and a second box holds channels 64..127.
+//   A: the output gradient dz in its BF16 copy with a zero border of kh - 1
+//      rows and kw - 1 columns ([img][Ho + 2(kh-1)][Wo + 2(kw-1)][cpa]), read
+//      at (oy + kh - 1, ox + kw - 1): pixels past the row end read the border
+//      or the box's zero fill, so they add nothing;
+//   B: the layer input at (oy + ky, ox + kx): the kx shift is a pixel offset,
+//      free of TMA's 16-byte rule because channels are the inner dimension.
+// Channels past Cout / Cin give rows / columns of dW' that are not stored.
 //
 // One CTA per (ky, pixel split), 192 threads:
-//   warp 0      TMA: per K step one dzP box and kw xP boxes into a ring of stages
+//   warp 0      TMA: per K step (64 pixels of one output row) the dz boxes
+//               and kw x (input boxes) into a ring of stages
 //   warp 1      TMEM allocation + single-thread tcgen05.mma, M = 128, N = NP,
-//               K = 16 x 4 per box, into kw accumulators of 128 columns
+//               K = 16 x 4 per step, into kw accumulators of 128 columns
 //   warps 2..5  epilogue: warp q reads TMEM lanes (output channels) 32q..32q+31
 //               of every accumulator and writes the split's FP32 partials
-// A reduction kernel adds the splits in order into the npz layout, so the
-// result is deterministic.  Every mbarrier wait is bounded; on timeout the
+// A reduction kernel adds the splits in a fixed order into the npz layout, so
+// the result is deterministic.  Every mbarrier wait is bounded; on timeout the
 // roles raise the abort flag and the error flag, drain and free TMEM.
 #include <algorithm>
 
@@ -38,44 +42,21 @@ namespace k {
 
 namespace {
 
-constexpr int BM = 128;        // output channels per tile (UMMA M)
-constexpr int KT = 64;         // pixels per K step (one 128-byte BF16 row)
-constexpr int A_BYTES = BM * 128;
+constexpr int BM = 128;                // output channels per tile (UMMA M)
+constexpr int KT = 64;                 // pixels per K step
+constexpr int BOX_BYTES = 64 * KT * 2; // one 64-channel x 64-pixel box: 8 KB
+constexpr int A_BYTES = 2 * BOX_BYTES; // M = 128 channels: two boxes
 constexpr int NUM_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 512; // kw <= 3 accumulators of 128 columns
 constexpr int MAX_STAGES = 4;
+constexpr int SLACK = 16384; // shared memory past the barriers that no operand is placed in
 
 struct WgTcParams {
-    int n_img, Ho, Wo, chunks_x, kh, kw, np, cout, cin, stages, stage_bytes, b_bytes;
+    int n_img, Ho, Wo, chunks_x, kh, kw, np, cout, cin, a_boxes, b_boxes, stages, stage_bytes, b_bytes;
     long steps, steps_per_split;
     float *part; // [split][ky][kx][cout][cin]
     int *err;
 };
-
-__device__ __forceinline__ float ldv(const float *p) { return *p; }
-__device__ __forceinline__ float ldv(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
-
-// out[(z * C + c) * H * pitch + y * pitch + x] = in[img][y][x + shift][c] for
-// x < Wout, z = zoff + img; a 32 x 32 (pixel x channel) tile through shared memory
-template <class T>
-__global__ void k_to_planar(const T *__restrict__ in, long in_pix, long in_row, long in_img, int C, int H, int Wout,
-                            int shift, int zoff, int pitch, __nv_bfloat16 *__restrict__ out)
-{
-    __shared__ float t[32][33];
-    const int x0 = blockIdx.x * 32, y = blockIdx.y % H, img = blockIdx.y / H, c0 = blockIdx.z * 32;
-    const int tx = threadIdx.x, ty = threadIdx.y; // 32 x 8
-    for (int i = ty; i < 32; i += 8) {
-        const int x = x0 + i, c = c0 + tx;
-        t[i][tx] = (x < Wout && c < C) ? ldv(in + img * in_img + (long)y * in_row + (long)(x + shift) * in_pix + c)
-                                       : 0.0f;
-    }
-    __syncthreads();
-    for (int i = ty; i < 32; i += 8) {
-        const int c = c0 + i, x = x0 + tx;
-        if (c < C && x < Wout)
-            out[(((long)(zoff + img) * C + c) * H + y) * pitch + x] = __float2bfloat16_rn(t[tx][i]);
-    }
-}
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_wgrad_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const WgTcParams p)
@@ -122,6 +103,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             int stage = 0, issued = 0;
             uint32_t phase = 0;
             bool ok = true;
+            const uint32_t tx = (uint32_t)(p.a_boxes + p.kw * p.b_boxes) * BOX_BYTES;
             for (long st = s0; st < s1 && ok; ++st) {
                 const int img = (int)(st / per_img);
                 const long r = st - (long)img * per_img;
@@ -131,11 +113,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     break;
                 }
                 uint8_t *sa = smem + stage * p.stage_bytes;
-                tc::mbar_expect_tx(&full[stage], p.stage_bytes);
-                tc::tma_load_4d(sa, &tmA, &full[stage], x0, oy, 0, img);
+                tc::mbar_expect_tx(&full[stage], tx);
+                for (int b = 0; b < p.a_boxes; ++b)
+                    tc::tma_load_4d(sa + b * BOX_BYTES, &tmA, &full[stage], b * 64, x0 + p.kw - 1, oy + p.kh - 1,
+                                    img);
                 for (int kx = 0; kx < p.kw; ++kx)
-                    tc::tma_load_4d(sa + A_BYTES + kx * p.b_bytes, &tmB, &full[stage], x0, oy + ky, 0,
-                                    kx * p.n_img + img);
+                    for (int b = 0; b < p.b_boxes; ++b)
+                        tc::tma_load_4d(sa + A_BYTES + kx * p.b_bytes + b * BOX_BYTES, &tmB, &full[stage], b * 64,
+                                        x0 + kx, oy + ky, img);
                 ++issued;
                 if (++stage == S) {
                     stage = 0;
@@ -159,7 +144,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {
-            const uint32_t idesc = tc::idesc_bf16(BM, p.np);
+            const uint32_t idesc = tc::idesc_bf16_mn(BM, p.np);
             int stage = 0;
             uint32_t phase = 0;
             bool ok = true;
@@ -170,12 +155,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
                 tc::fence_after_sync();
                 const uint32_t sa = tc::smem_u32(smem + stage * p.stage_bytes);
-                const uint64_t da = tc::sdesc_sw128(sa);
                 for (int kx = 0; kx < p.kw; ++kx) {
-                    const uint64_t db = tc::sdesc_sw128(sa + A_BYTES + kx * p.b_bytes);
 #pragma unroll
-                    for (int kk = 0; kk < KT / 16; ++kk)
-                        tc::umma_bf16(tmem + kx * BM, da + 2 * kk, db + 2 * kk, idesc, (st > s0 || kk > 0) ? 1u : 0u);
+                    for (int kk = 0; kk < KT / 16; ++kk) {
+                        // a K step of 16 pixels = 16 rows of 128 bytes = two 8-row swizzle atoms
+                        const uint64_t da = tc::sdesc_sw128_mn(sa + kk * 2048, BOX_BYTES);
+                        const uint64_t db = tc::sdesc_sw128_mn(sa + A_BYTES + kx * p.b_bytes + kk * 2048, BOX_BYTES);
+                        tc::umma_bf16(tmem + kx * BM, da, db, idesc, (st > s0 || kk > 0) ? 1u : 0u);
+                    }
                 }
                 tc::umma_commit(&empty[stage]);
                 if (++stage == S) {
@@ -223,23 +210,34 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
 }
 
-// dw[co][ci][kh-1-ky][kw-1-kx] += sum over splits of part[split][ky][kx][co][ci], in split order
-__global__ void k_wgrad_tc_reduce(const float *__restrict__ part, int nsplit, int kh, int kw, int Cout, int Cin,
-                                  float *__restrict__ dw)
+// dw[co][ci][kh-1-ky][kw-1-kx] += sum over splits of part[split][ky][kx][co][ci]:
+// 32 outputs per CTA (one per lane), warp w sums splits w, w + 8, ..., then
+// the 8 warp sums in a fixed order (deterministic)
+__global__ void __launch_bounds__(256) k_wgrad_tc_reduce(const float *__restrict__ part, int nsplit, int kh, int kw,
+                                                         int Cout, int Cin, float *__restrict__ dw)
 {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x, per = (long)kh * kw * Cout * Cin;
-    if (i >= per) return;
+    __shared__ float s[8][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long per = (long)kh * kw * Cout * Cin, i = (long)blockIdx.x * 32 + lane;
+    float acc = 0.0f;
+    if (i < per)
+        for (int sp = w; sp < nsplit; sp += 8) acc += part[(long)sp * per + i];
+    s[w][lane] = acc;
+    __syncthreads();
+    if (w != 0 || i >= per) return;
+    float t = s[0][lane];
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t += s[j][lane];
     const int ci = (int)(i % Cin);
     const long r = i / Cin;
-    const int co = (int)(r % Cout), t = (int)(r / Cout), kx = t % kw, ky = t / kw;
-    float s = 0.0f;
-    for (int sp = 0; sp < nsplit; ++sp) s += part[(long)sp * per + i];
-    dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += s;
+    const int co = (int)(r % Cout), tt = (int)(r / Cout), kx = tt % kw, ky = tt / kw;
+    dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += t;
 }
 
-int planar_pitch(int W) { return (W + 7) & ~7; } // rows of 16-byte multiples, as TMA strides need
-
-size_t smem_bytes(int stages, int stage_bytes) { return 1024 + (size_t)stages * stage_bytes + (2 * stages + 2) * 8 + 16; }
+size_t smem_bytes(int stages, int stage_bytes)
+{
+    return 1024 + (size_t)stages * stage_bytes + (2 * stages + 2) * 8 + 16 + SLACK;
+}
 
 } // namespace
 
@@ -258,68 +256,62 @@ int wgrad_tc_splits(int kh, long steps)
     return (int)std::max(1L, std::min((long)std::max(1, sms / kh), steps));
 }
 
-size_t wgrad_tc_scratch_bytes(int nimg, int Ho, int Wo, int Hin, int Cout, int Cin, int kh, int kw, int splits)
+size_t wgrad_tc_scratch_bytes(int Cout, int Cin, int kh, int kw, int splits)
 {
-    const size_t pitch = planar_pitch(Wo);
-    const size_t a = 2 * (size_t)nimg * Cout * Ho * pitch, b = 2 * (size_t)kw * nimg * Cin * Hin * pitch;
-    const size_t c = 4 * (size_t)splits * kh * kw * Cout * Cin;
-    auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
-    return al(a) + al(b) + al(c);
+    return 4 * (size_t)splits * kh * kw * Cout * Cin;
 }
 
-int wgrad_tc(const float *dz, int Cout, const void *in, long in_pix, long in_row, long in_img, int Cin, int kh,
-             int kw, int nimg, int Ho, int Wo, void *scratch, size_t scratch_bytes, float *dw, int *err,
+int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, long in_row, long in_img, int Cin,
+             int kh, int kw, int nimg, int Ho, int Wo, void *scratch, size_t scratch_bytes, float *dw, int *err,
              cudaStream_t st)
 {
     if (!wgrad_tc_supported(Cout, Cin, kh, kw)) return fail(CNNCRF_EUNSUPPORTED, "wgrad_tc: shape");
-    const int Hin = Ho + kh - 1, chunks_x = ceil_div(Wo, KT), pitch = planar_pitch(Wo);
+    if (cpa % 64 || cpa < Cout || in_pix % 64 || in_pix < Cin)
+        return fail(CNNCRF_EINVAL, "wgrad_tc: channel strides %d / %ld must be multiples of 64", cpa, in_pix);
+    if (((uintptr_t)dzpad & 15) || ((uintptr_t)in & 15) || in_row % in_pix || in_img % in_row)
+        return fail(CNNCRF_EINVAL, "wgrad_tc: operand layout");
+    const int Hin = Ho + kh - 1, Win = Wo + kw - 1, chunks_x = ceil_div(Wo, KT);
+    if (in_row / in_pix < Win || in_img / in_row < Hin) return fail(CNNCRF_EINVAL, "wgrad_tc: input extent");
     const long steps = (long)nimg * Ho * chunks_x;
     const int splits = wgrad_tc_splits(kh, steps);
-    if (scratch_bytes < wgrad_tc_scratch_bytes(nimg, Ho, Wo, Hin, Cout, Cin, kh, kw, splits))
+    if (scratch_bytes < wgrad_tc_scratch_bytes(Cout, Cin, kh, kw, splits))
         return fail(CNNCRF_EINVAL, "wgrad_tc: scratch too small");
-    if (((uintptr_t)scratch & 1023) != 0) return fail(CNNCRF_EINVAL, "wgrad_tc: scratch not 1024-byte aligned");
-    auto al = [](size_t x) { return (x + 1023) & ~(size_t)1023; };
-    __nv_bfloat16 *dzP = (__nv_bfloat16 *)scratch;
-    __nv_bfloat16 *xP = (__nv_bfloat16 *)((char *)scratch + al(2 * (size_t)nimg * Cout * Ho * pitch));
-    float *part = (float *)((char *)xP + al(2 * (size_t)kw * nimg * Cin * Hin * pitch));
-    {
-        CNNCRF_PROF("wgrad_planar", st);
-        k_to_planar<float><<<dim3(ceil_div(Wo, 32), Ho * nimg, ceil_div(Cout, 32)), dim3(32, 8), 0, st>>>(
-            dz, Cout, (long)Wo * Cout, (long)Ho * Wo * Cout, Cout, Ho, Wo, 0, 0, pitch, dzP);
-        for (int kx = 0; kx < kw; ++kx)
-            k_to_planar<__nv_bfloat16><<<dim3(ceil_div(Wo, 32), Hin * nimg, ceil_div(Cin, 32)), dim3(32, 8), 0, st>>>(
-                (const __nv_bfloat16 *)in, in_pix, in_row, in_img, Cin, Hin, Wo, kx, kx * nimg, pitch, xP);
-    }
     auto enc = tc::tensor_map_encoder();
     if (!enc) return fail(CNNCRF_ECUDA, "wgrad_tc: cuTensorMapEncodeTiled unavailable");
     const int np = (Cin + 15) & ~15;
     CUtensorMap ma, mb;
     {
-        cuuint64_t g[4] = {(cuuint64_t)Wo, (cuuint64_t)Ho, (cuuint64_t)Cout, (cuuint64_t)nimg};
-        cuuint64_t s[3] = {(cuuint64_t)pitch * 2, (cuuint64_t)Ho * pitch * 2, (cuuint64_t)Cout * Ho * pitch * 2};
-        cuuint32_t box[4] = {KT, 1, BM, 1}, e[4] = {1, 1, 1, 1};
-        CUresult r = enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, dzP, g, s, box, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        const int Hp = Ho + 2 * (kh - 1), Wp = Wo + 2 * (kw - 1);
+        cuuint64_t g[4] = {(cuuint64_t)cpa, (cuuint64_t)Wp, (cuuint64_t)Hp, (cuuint64_t)nimg};
+        cuuint64_t s[3] = {(cuuint64_t)cpa * 2, (cuuint64_t)Wp * cpa * 2, (cuuint64_t)Hp * Wp * cpa * 2};
+        cuuint32_t box[4] = {64, KT, 1, 1}, e[4] = {1, 1, 1, 1};
+        CUresult r = enc(&ma, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)dzpad, g, s, box, e,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "wgrad_tc: output-gradient tensor map (%d)", (int)r);
     }
     {
-        cuuint64_t g[4] = {(cuuint64_t)Wo, (cuuint64_t)Hin, (cuuint64_t)Cin, (cuuint64_t)kw * nimg};
-        cuuint64_t s[3] = {(cuuint64_t)pitch * 2, (cuuint64_t)Hin * pitch * 2, (cuuint64_t)Cin * Hin * pitch * 2};
-        cuuint32_t box[4] = {KT, 1, (cuuint32_t)np, 1}, e[4] = {1, 1, 1, 1};
-        CUresult r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, xP, g, s, box, e, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                         CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+        const long wrow = in_row / in_pix, hin = in_img / in_row;
+        cuuint64_t g[4] = {(cuuint64_t)in_pix, (cuuint64_t)wrow, (cuuint64_t)hin, (cuuint64_t)nimg};
+        cuuint64_t s[3] = {(cuuint64_t)in_pix * 2, (cuuint64_t)in_row * 2, (cuuint64_t)in_img * 2};
+        cuuint32_t box[4] = {64, KT, 1, 1}, e[4] = {1, 1, 1, 1};
+        CUresult r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)in, g, s, box, e,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "wgrad_tc: input tensor map (%d)", (int)r);
     }
     WgTcParams p{};
     p.n_img = nimg, p.Ho = Ho, p.Wo = Wo, p.chunks_x = chunks_x, p.kh = kh, p.kw = kw, p.np = np;
     p.cout = Cout, p.cin = Cin;
-    p.b_bytes = np * 128; // np rows of 128 bytes: whole 1024-byte swizzle atoms, np being a multiple of 16
+    // M = 128 always reads two channel boxes of dz; the second is loaded only when Cout > 64 (the rows
+    // it would fill are not stored).  N = np reads a second input box when np > 64.
+    p.a_boxes = Cout > 64 ? 2 : 1;
+    p.b_boxes = np > 64 ? 2 : 1;
+    p.b_bytes = 2 * BOX_BYTES; // per tap, whether one or two boxes are loaded
     p.stage_bytes = A_BYTES + kw * p.b_bytes;
     p.steps = steps;
     p.steps_per_split = (steps + splits - 1) / splits;
-    p.part = part;
+    p.part = (float *)scratch;
     p.err = err;
     int dev = 0, maxsm = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
@@ -336,7 +328,7 @@ int wgrad_tc(const float *dz, int Cout, const void *in, long in_pix, long in_row
         CNNCRF_PROF("wgrad_tc", st);
         k_wgrad_tc<<<dim3(used, kh), NUM_THREADS, smem, st>>>(ma, mb, p);
         const long per = (long)kh * kw * Cout * Cin;
-        k_wgrad_tc_reduce<<<ceil_div(per, 256), 256, 0, st>>>(part, used, kh, kw, Cout, Cin, dw);
+        k_wgrad_tc_reduce<<<ceil_div(per, 32), 256, 0, st>>>(p.part, used, kh, kw, Cout, Cin, dw);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

@@ -104,23 +104,27 @@ int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx
 // features at channel stride fs
 int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,
                    int npairs, int H, int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st);
-// pixel splits (at most 64) of the weight gradient's fixed-order reduction for P output pixels
+// pixel splits (at most 64) of the bias gradient's fixed-order reduction for P output pixels
 int train_wgrad_splits(long P);
+// pixel splits of the weight gradient (K = kh*kw*Cin): about four CTAs per SM, >= 512 pixels each
+int train_wgrad_splits_k(long P, int K);
 // dw (npz layout) += weight gradient, db += bias gradient (if db); part:
-// splits x Cout x kh*kw*Cin floats, partb: splits x Cout floats of scratch
+// train_wgrad_splits_k x Cout x kh*kw*Cin floats, partb: train_wgrad_splits x Cout floats of scratch
 int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pix, long in_row, long in_img, int Cin,
                 int kh, int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st);
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st);
 int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st); // db += sum dz
-// the weight gradient on the tensor cores (k_wgrad_tc.cu): dz dense FP32 [nimg][Ho][Wo][Cout], the
-// layer input BF16 at the given element strides; dw (npz layout) += dW.  scratch: wgrad_tc_scratch_bytes,
-// 1024-byte aligned; err: the bounded-wait error flag
+// the weight gradient on the tensor cores (k_wgrad_tc.cu), both operands NHWC BF16: dzpad = the output
+// gradient with a (kh-1, kw-1) zero border, channel stride cpa (train_tanh_bwd_pad's copy); the layer
+// input at the given element strides (pixel stride a multiple of 64).  dw (npz layout) += dW.
+// scratch: wgrad_tc_scratch_bytes for wgrad_tc_splits(kh, nimg * Ho * ceil(Wo / 64)) splits;
+// err: the bounded-wait error flag
 bool wgrad_tc_supported(int Cout, int Cin, int kh, int kw);
 int wgrad_tc_splits(int kh, long steps);
-size_t wgrad_tc_scratch_bytes(int nimg, int Ho, int Wo, int Hin, int Cout, int Cin, int kh, int kw, int splits);
-int wgrad_tc(const float *dz, int Cout, const void *in, long in_pix, long in_row, long in_img, int Cin, int kh,
-             int kw, int nimg, int Ho, int Wo, void *scratch, size_t scratch_bytes, float *dw, int *err,
+size_t wgrad_tc_scratch_bytes(int Cout, int Cin, int kh, int kw, int splits);
+int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, long in_row, long in_img, int Cin,
+             int kh, int kw, int nimg, int Ho, int Wo, void *scratch, size_t scratch_bytes, float *dw, int *err,
              cudaStream_t st);
 int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st);
 int train_hinge(const float *vol, const float *w, const int32_t *gt, const int32_t *yh, int npairs, int W, int H,

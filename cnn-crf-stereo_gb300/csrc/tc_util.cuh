@@ -144,12 +144,34 @@ __device__ __forceinline__ uint64_t sdesc_sw128_rows(uint32_t tile_saddr, int ro
     return sdesc_sw128(tile_saddr + (uint32_t)rows * 128u);
 }
 
+// Shared-memory matrix descriptor, MN-major operand in the 128-byte swizzle
+// layout: 64 MN-contiguous BF16 elements per 128-byte row, one row per K
+// index, 8-row / 1024 B swizzle atoms (what TMA writes for a box whose inner
+// dimension is 64 channels and whose second dimension is K).  Leading offset
+// [16,30) = the byte distance between 64-element atoms along MN; stride
+// offset [32,46) = 1024 B between 8-row groups along K.
+__device__ __forceinline__ uint64_t sdesc_sw128_mn(uint32_t saddr, uint32_t mn_atom_bytes)
+{
+    uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)((mn_atom_bytes >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
 // Instruction descriptor, kind::f16: FP32 accumulator ([4,6) = 1), BF16 A
 // ([7,10) = 1) and B ([10,13) = 1), both K-major, N >> 3 at [17,23),
 // M >> 4 at [24,29).
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N)
 {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Same with both operands MN-major (the transpose bits 15 and 16)
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N)
+{
+    return idesc_bf16(M, N) | (1u << 15) | (1u << 16);
 }
 
 __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,

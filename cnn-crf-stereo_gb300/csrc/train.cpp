@@ -31,6 +31,7 @@ struct TLayer {
     DevBuf wt, wd, b128; // conv_simt layout, input-gradient layout, padded bias
     DevBuf w16;          // the BF16 mode's tensor-core layout
     DevBuf w16d;         // its input-gradient layout (tensor-core input gradients)
+    bool tcw = false;    // the weight gradient on the tensor cores
     int hout() const { return hin - kh + 1; }
     int wout() const { return win - kw + 1; }
 };
@@ -65,7 +66,7 @@ struct cnncrf_train {
     size_t crfws_bytes = 0;
     DevBuf wgs; // the tensor-core weight gradient's planar copies and partial sums
     size_t wgs_bytes = 0;
-    DevBuf dpad; // the tensor-core input gradient's BF16 padded output gradient
+    DevBuf dpad; // the BF16 padded output gradient: the tensor-core weight and input gradients read it
 
     int build();
     int refresh();
@@ -218,11 +219,13 @@ int cnncrf_train::build()
     CNNCRF_TRY(gpw.reserve(sizeof(float) * N * 2));
     CNNCRF_TRY(gh.reserve(sizeof(float) * N * 2));
     long Pmax = 0;
-    int Kmax = 0;
+    size_t part_floats = 0;
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v) {
-            Pmax = std::max(Pmax, (long)n * Ly.hout() * Ly.wout());
-            Kmax = std::max(Kmax, Ly.kh * Ly.kw * Ly.cin);
+            const long P = (long)n * Ly.hout() * Ly.wout();
+            const int K = Ly.kh * Ly.kw * Ly.cin;
+            Pmax = std::max(Pmax, P);
+            part_floats = std::max(part_floats, (size_t)k::train_wgrad_splits_k(P, K) * Ly.cout * K);
         }
     // the BF16 mode's tensor-core weight gradients: scratch for the largest layer
     if (bf16 && d.tc_wgrad)
@@ -230,20 +233,20 @@ int cnncrf_train::build()
             for (auto &Ly : *v)
                 if (Ly.act == 1 && Ly.cin >= 16 && k::wgrad_tc_supported(Ly.cout, Ly.cin, Ly.kh, Ly.kw)) {
                     const long steps = (long)n * Ly.hout() * ((Ly.wout() + 63) / 64);
-                    wgs_bytes = std::max(wgs_bytes, k::wgrad_tc_scratch_bytes(n, Ly.hout(), Ly.wout(), Ly.hin,
-                                                                              Ly.cout, Ly.cin, Ly.kh, Ly.kw,
+                    wgs_bytes = std::max(wgs_bytes, k::wgrad_tc_scratch_bytes(Ly.cout, Ly.cin, Ly.kh, Ly.kw,
                                                                               k::wgrad_tc_splits(Ly.kh, steps)));
+                    Ly.tcw = true;
                 }
     if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
     size_t dpad_bytes = 0;
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v)
-            if (Ly.w16d.get())
+            if (Ly.w16d.get() || Ly.tcw)
                 dpad_bytes = std::max(dpad_bytes, 2 * (size_t)n * (Ly.hout() + 2 * (Ly.kh - 1)) *
                                                       (Ly.wout() + 2 * (Ly.kw - 1)) * pad_to(Ly.cout, 64));
     if (dpad_bytes) CNNCRF_TRY(dpad.reserve(dpad_bytes));
-    const int ns = k::train_wgrad_splits(Pmax); // the most splits any layer uses
-    CNNCRF_TRY(part.reserve(sizeof(float) * (size_t)ns * 128 * Kmax));
+    const int ns = k::train_wgrad_splits(Pmax); // the most bias splits any layer uses
+    CNNCRF_TRY(part.reserve(sizeof(float) * part_floats));
     CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
     // hinge
     CNNCRF_TRY(aug.reserve(sizeof(float) * N * D));
@@ -418,13 +421,13 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
     const int Ho = L.hout(), Wo = L.wout();
     const int ph = L.kh - 1, pwd = L.kw - 1;
     const bool tcd = dprev && L.w16d.get(); // the input gradient on the tensor cores (BF16 mode)
-    if (tcd)
+    if (tcd || L.tcw) // dz and its BF16 padded copy, the tensor-core operand
         CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, n, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64), dpad.get(), st));
     else
         CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
-    if (in_bf16 && wgs_bytes && k::wgrad_tc_supported(L.cout, L.cin, L.kh, L.kw)) { // BF16 mode, tensor cores
-        CNNCRF_TRY(k::wgrad_tc(dz, L.cout, in, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo, wgs.get(),
-                               wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
+    if (L.tcw && in_bf16) { // BF16 mode, tensor cores
+        CNNCRF_TRY(k::wgrad_tc(dpad.get(), L.cout, pad_to(L.cout, 64), in, in_pix, in_row, in_img, L.cin, L.kh, L.kw,
+                               n, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
         if (L.bslot >= 0)
             CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
     } else {
