@@ -457,23 +457,76 @@ __global__ void __launch_bounds__(256) k_wgrad_reduce(const float *__restrict__ 
 }
 
 // db[co] += sum_p dz[p][co]: per split a partial, then the splits in order
-__global__ void k_bias_part(const float *__restrict__ dz, int Cout, long P, long chunk, float *__restrict__ part)
+// A CTA of 128 x 4 threads per split: thread (co, r) sums the split's pixels
+// r, r + 4, ...; the 4 sums are added in order.
+__global__ void __launch_bounds__(512) k_bias_part(const float *__restrict__ dz, int Cout, long P, long chunk,
+                                                   float *__restrict__ part)
 {
-    const int co = threadIdx.x, split = blockIdx.x;
-    if (co >= Cout) return;
+    __shared__ float s4[4][128];
+    const int co = threadIdx.x, r = threadIdx.y, split = blockIdx.x;
     const long p0 = (long)split * chunk, p1 = min(P, p0 + chunk);
     float s = 0.0f;
-    for (long p = p0; p < p1; ++p) s += dz[p * Cout + co];
-    part[(long)split * Cout + co] = s;
+    if (co < Cout)
+#pragma unroll 4
+        for (long p = p0 + r; p < p1; p += 4) s += dz[p * Cout + co];
+    s4[r][co] = s;
+    __syncthreads();
+    if (r == 0 && co < Cout) part[(long)split * Cout + co] = ((s4[0][co] + s4[1][co]) + s4[2][co]) + s4[3][co];
 }
 
-__global__ void k_bias_reduce(const float *__restrict__ part, int nsplit, int Cout, float *__restrict__ db)
+// db[co] += the sum over splits: warp w sums splits w, w + 8, ... of 32
+// channels, then the 8 warp sums in order
+__global__ void __launch_bounds__(256) k_bias_reduce(const float *__restrict__ part, int nsplit, int Cout,
+                                                     float *__restrict__ db)
 {
-    const int co = threadIdx.x;
-    if (co >= Cout) return;
+    __shared__ float s8[8][33];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, co = blockIdx.x * 32 + lane;
     float s = 0.0f;
-    for (int sp = 0; sp < nsplit; ++sp) s += part[(long)sp * Cout + co];
-    db[co] += s;
+    if (co < Cout)
+        for (int sp = w; sp < nsplit; sp += 8) s += part[(long)sp * Cout + co];
+    s8[w][lane] = s;
+    __syncthreads();
+    if (w != 0 || co >= Cout) return;
+    float t = s8[0][lane];
+#pragma unroll
+    for (int j = 1; j < 8; ++j) t += s8[j][lane];
+    db[co] += t;
+}
+
+// BF16 copy of an FP32 [npx][C] image with channels padded to 64: the
+// tensor-core weight gradient's operand for the thin first layers
+__global__ void k_to_bf16_c64(const float *__restrict__ in, long npx, int C, __nv_bfloat16 *__restrict__ out)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x; // one 8-channel group
+    if (i >= npx * 8) return;
+    const long px = i >> 3;
+    const int g = (int)(i & 7);
+    uint32_t u[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const int c0 = g * 8 + 2 * j, c1 = c0 + 1;
+        __nv_bfloat162 b2 = __floats2bfloat162_rn(c0 < C ? in[px * C + c0] : 0.0f, c1 < C ? in[px * C + c1] : 0.0f);
+        u[j] = *(uint32_t *)&b2;
+    }
+    *(uint4 *)(out + px * 64 + g * 8) = make_uint4(u[0], u[1], u[2], u[3]);
+}
+
+// The 1x1 head's weight gradient: part[split][o][c] = sum over the split's
+// pixels of gh[p][o] y[p][c], o < 2; thread (c, o, r) takes pixels r, r + 2, ...
+template <class T>
+__global__ void __launch_bounds__(512) k_wgrad_head(const float *__restrict__ gh, const T *__restrict__ y, int ys,
+                                                    long P, long chunk, int C, float *__restrict__ part)
+{
+    __shared__ float s2[2][2][128];
+    const int c = threadIdx.x, o = threadIdx.y, r = threadIdx.z, split = blockIdx.x;
+    const long p0 = (long)split * chunk, p1 = min(P, p0 + chunk);
+    float s = 0.0f;
+    if (c < C)
+#pragma unroll 4
+        for (long p = p0 + r; p < p1; p += 2) s = fmaf(gh[p * 2 + o], ld(y + p * ys + c), s);
+    s2[r][o][c] = s;
+    __syncthreads();
+    if (r == 0 && c < C) part[((long)split * 2 + o) * C + c] = s2[0][o][c] + s2[1][o][c];
 }
 
 // ------------------------------------------------------------ pairwise head adjoint
@@ -735,7 +788,14 @@ int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const floa
                       st);
 }
 
-int train_wgrad_splits(long P) { return (int)std::max(1L, std::min(64L, P / 2048)); }
+int train_wgrad_splits(long P)
+{
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+        sms = 148;
+    return (int)std::max(1L, std::min((long)4 * sms, P / 256));
+}
 
 int train_wgrad_splits_k(long P, int K)
 {
@@ -786,8 +846,37 @@ int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, 
 {
     const int ns = train_wgrad_splits(P);
     const long chunk = (P + ns - 1) / ns;
-    k_bias_part<<<ns, 128, 0, st>>>(dz, Cout, P, chunk, partb);
-    k_bias_reduce<<<1, 128, 0, st>>>(partb, ns, Cout, db);
+    if (Cout > 128) return fail(CNNCRF_EINVAL, "bias grad: %d channels > 128", Cout);
+    k_bias_part<<<ns, dim3(128, 4), 0, st>>>(dz, Cout, P, chunk, partb);
+    k_bias_reduce<<<ceil_div(Cout, 32), 256, 0, st>>>(partb, ns, Cout, db);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_to_bf16_c64(const float *in, long npx, int C, void *out, cudaStream_t st)
+{
+    if (C > 64 || ((uintptr_t)out & 15)) return fail(CNNCRF_EINVAL, "to_bf16_c64: %d channels", C);
+    k_to_bf16_c64<<<ceil_div(npx * 8, 256), 256, 0, st>>>(in, npx, C, (__nv_bfloat16 *)out);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_wgrad_head(const float *gh, const void *y, bool bf16, int ys, long P, int C, float *part, float *dw,
+                     cudaStream_t st)
+{
+    if (C > 128) return fail(CNNCRF_EINVAL, "head wgrad: %d channels > 128", C);
+    const int ns = train_wgrad_splits(P);
+    const long chunk = (P + ns - 1) / ns;
+    {
+        CNNCRF_PROF("wgrad", st);
+        const dim3 blk(128, 2, 2);
+        if (bf16)
+            k_wgrad_head<<<ns, blk, 0, st>>>(gh, (const __nv_bfloat16 *)y, ys, P, chunk, C, part);
+        else
+            k_wgrad_head<<<ns, blk, 0, st>>>(gh, (const float *)y, ys, P, chunk, C, part);
+        // the 2 x C sums, flat: the npz layout w[o][c][1][1]
+        k_bias_reduce<<<ceil_div(2 * C, 32), 256, 0, st>>>(part, ns, 2 * C, dw);
+    }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

@@ -244,7 +244,7 @@ size_t smem_bytes(int stages, int stage_bytes)
 bool wgrad_tc_supported(int Cout, int Cin, int kh, int kw)
 {
     // N = Cin rounded to 16 must fit one accumulator's 128 TMEM columns
-    return Cout >= 1 && Cout <= BM && Cin >= 16 && Cin <= 128 && kw >= 1 && kw <= 3 && kh >= 1 && kh <= 3;
+    return Cout >= 1 && Cout <= BM && Cin >= 1 && Cin <= 128 && kw >= 1 && kw <= 3 && kh >= 1 && kh <= 3;
 }
 
 int wgrad_tc_splits(int kh, long steps)
@@ -291,8 +291,8 @@ int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, 
         if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "wgrad_tc: output-gradient tensor map (%d)", (int)r);
     }
     {
-        const long wrow = in_row / in_pix, hin = in_img / in_row;
-        cuuint64_t g[4] = {(cuuint64_t)in_pix, (cuuint64_t)wrow, (cuuint64_t)hin, (cuuint64_t)nimg};
+        // the layer's input extent exactly (the rows may be a window of a wider image): nothing past it is read
+        cuuint64_t g[4] = {(cuuint64_t)in_pix, (cuuint64_t)Win, (cuuint64_t)Hin, (cuuint64_t)nimg};
         cuuint64_t s[3] = {(cuuint64_t)in_pix * 2, (cuuint64_t)in_row * 2, (cuuint64_t)in_img * 2};
         cuuint32_t box[4] = {64, KT, 1, 1}, e[4] = {1, 1, 1, 1};
         CUresult r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)in, g, s, box, e,

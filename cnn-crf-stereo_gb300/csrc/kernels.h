@@ -104,7 +104,7 @@ int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx
 // features at channel stride fs
 int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,
                    int npairs, int H, int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st);
-// pixel splits (at most 64) of the bias gradient's fixed-order reduction for P output pixels
+// pixel splits of the bias gradient's fixed-order reduction for P output pixels (about four per SM)
 int train_wgrad_splits(long P);
 // pixel splits of the weight gradient (K = kh*kw*Cin): about four CTAs per SM, >= 512 pixels each
 int train_wgrad_splits_k(long P, int K);
@@ -115,6 +115,11 @@ int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pi
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st);
 int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st); // db += sum dz
+// the 1x1 pairwise head (2 outputs): dw[o][c] += sum_p gh[p][o] y[p][c]; part: train_wgrad_splits(P) x 2C floats
+int train_wgrad_head(const float *gh, const void *y, bool bf16, int ys, long P, int C, float *part, float *dw,
+                     cudaStream_t st);
+// BF16 copy of FP32 [npx][C] (C <= 64) at channel stride 64, zero padded
+int train_to_bf16_c64(const float *in, long npx, int C, void *out, cudaStream_t st);
 // the weight gradient on the tensor cores (k_wgrad_tc.cu), both operands NHWC BF16: dzpad = the output
 // gradient with a (kh-1, kw-1) zero border, channel stride cpa (train_tanh_bwd_pad's copy); the layer
 // input at the given element strides (pixel stride a multiple of 64).  dw (npz layout) += dW.

@@ -56,6 +56,7 @@ struct cnncrf_train {
     DevBuf dlist;
     // forward state; feature-layer outputs: checkpoints in their own buffers, the rest in a shared pool
     DevBuf padded[2], norm[2], scratch;
+    DevBuf norm16[2]; // BF16 copies of norm at channel stride 64 (the first layers' tensor-core weight gradients)
     std::vector<char> keep;
     std::vector<DevBuf> act[2], pool;
     DevBuf fbuf, vol, y1, y2, pwout; // fbuf: both sides' normalised features
@@ -231,13 +232,15 @@ int cnncrf_train::build()
     if (bf16 && d.tc_wgrad)
         for (auto *v : {&feat, &pw})
             for (auto &Ly : *v)
-                if (Ly.act == 1 && Ly.cin >= 16 && k::wgrad_tc_supported(Ly.cout, Ly.cin, Ly.kh, Ly.kw)) {
+                if (Ly.act == 1 && k::wgrad_tc_supported(Ly.cout, Ly.cin, Ly.kh, Ly.kw)) {
                     const long steps = (long)n * Ly.hout() * ((Ly.wout() + 63) / 64);
                     wgs_bytes = std::max(wgs_bytes, k::wgrad_tc_scratch_bytes(Ly.cout, Ly.cin, Ly.kh, Ly.kw,
                                                                               k::wgrad_tc_splits(Ly.kh, steps)));
                     Ly.tcw = true;
                 }
     if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
+    if (feat[0].tcw || pw[0].tcw)
+        for (int s = 0; s < 2; ++s) CNNCRF_TRY(zalloc(norm16[s], 2 * (size_t)n * h * w * 64));
     size_t dpad_bytes = 0;
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v)
@@ -316,6 +319,7 @@ int cnncrf_train::forward(const float *l, const float *r)
     for (int s = 0; s < 2; ++s) {
         CNNCRF_TRY(k::pad_rgba(img[s], W, H, p, padded[s].as<float>(), st, n));
         CNNCRF_TRY(k::normalize(padded[s].as<float>(), w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
+        if (norm16[s].get()) CNNCRF_TRY(k::train_to_bf16_c64(norm[s].as<float>(), (long)n * h * w, ic, norm16[s].get(), st));
         for (int li = 0; li < L; ++li) CNNCRF_TRY(run_layer(s, li));
         if (bf16) {
             CNNCRF_TRY(k::train_l2norm_bf16(actp(s, L - 1), (long)n * H * W, F, cp_feat, fside(s), st));
@@ -472,9 +476,11 @@ int cnncrf_train::backward(const float *gv, const float *gp)
             for (int j = c + 1; j < top; ++j) CNNCRF_TRY(run_layer(s, j)); // recompute the segment
             for (int j = top; j > c; --j) {
                 TLayer &Ly = feat[j];
-                const void *in = j > 0 ? actp(s, j - 1) : (const void *)norm[s].get();
-                const bool ib = j > 0 && bf16;
-                const int cs = j > 0 ? fs : ic;
+                // the first layer reads the normalised input: its BF16 copy for the tensor-core weight gradient
+                const bool n16 = j == 0 && Ly.tcw;
+                const void *in = j > 0 ? actp(s, j - 1) : n16 ? norm16[s].get() : (const void *)norm[s].get();
+                const bool ib = (j > 0 && bf16) || n16;
+                const int cs = j > 0 ? fs : n16 ? 64 : ic;
                 CNNCRF_TRY(layer_back(Ly, in, ib, cs, (long)Ly.win * cs, (long)Ly.hin * Ly.win * cs, actp(s, j), fs,
                                       cur, j > 0 ? nxt : nullptr));
                 std::swap(cur, nxt);
@@ -486,14 +492,20 @@ int cnncrf_train::backward(const float *gv, const float *gp)
         // head: gh = gpw sign(h), dy2 = W^T gh; its weight gradient is a 1x1 wgrad on y2
         CNNCRF_TRY(k::train_head_bwd(y2.get(), bf16, ps, param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
                                      dy.as<float>(), st));
-        CNNCRF_TRY(k::train_wgrad(gh.as<float>(), 2, y2.get(), bf16, ps, (long)W * ps, (long)H * W * ps, P, 1, 1, n, H,
-                                  W, part.as<float>(), gradp(pw[2].wslot), nullptr, partb.as<float>(), st));
+        CNNCRF_TRY(k::train_wgrad_head(gh.as<float>(), y2.get(), bf16, ps, (long)n * H * W, P, partb.as<float>(),
+                                       gradp(pw[2].wslot), st));
         CNNCRF_TRY(layer_back(pw[1], y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
                               ps, dy.as<float>(), dyb.as<float>()));
         const int cr = p - 2;
-        const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
-        CNNCRF_TRY(layer_back(pw[0], in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps, dyb.as<float>(),
-                              nullptr));
+        if (pw[0].tcw) {
+            const void *in = (const char *)norm16[0].get() + 2 * ((size_t)cr * w + cr) * 64;
+            CNNCRF_TRY(layer_back(pw[0], in, true, 64, (long)w * 64, (long)h * w * 64, y1.get(), ps, dyb.as<float>(),
+                                  nullptr));
+        } else {
+            const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+            CNNCRF_TRY(layer_back(pw[0], in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps,
+                                  dyb.as<float>(), nullptr));
+        }
     }
     return CNNCRF_OK;
 }

@@ -303,14 +303,14 @@ def test_bf16_mode_against_fp64_oracle(cuda, oracle):
 
 @pytest.mark.parametrize("layers,topology,n,W,H", [(3, 1, 2, 40, 22), (4, 1, 1, 150, 37), (3, 0, 3, 97, 19)])
 def test_tensor_core_weight_gradient_matches_cuda_cores(cuda, oracle, layers, topology, n, W, H):
-    """The BF16 mode's weight gradients of the layers with >= 16 input
-    channels on the tensor cores (dz rounded to BF16, FP32 accumulation)
-    against the CUDA-core path (FP32 dz) of the same forward and output
-    gradients.  Every other slot (biases, the first layers, the pairwise head)
-    comes from the same kernels and must match bit for bit; the tensor-core
-    slots within 1e-2 of their largest value (BF16 dz: a relative rounding
-    of 2^-9 per term).  Widths 40, 150 and 97 leave ragged 64-pixel chunks;
-    topology 0 has 2 x 2 kernels."""
+    """The BF16 mode's weight gradients of the tanh layers on the tensor
+    cores (dz rounded to BF16, FP32 accumulation; the first layers read a
+    BF16 copy of the normalised image) against the CUDA-core path (FP32 dz
+    and input) of the same forward and output gradients.  Every other slot
+    (biases, the pairwise head) comes from the same kernels and must match
+    bit for bit; the tensor-core slots within 1e-2 of their largest value
+    (BF16 operands: a relative rounding of 2^-9 per term).  Widths 40, 150
+    and 97 leave ragged 64-pixel chunks; topology 0 has 2 x 2 kernels."""
     torch = cuda
     from cnncrf import _lib as L
     kw = dict(layers=layers, topology=topology, n=n, W=W, H=H, F=100, P=64, precision=L.BF16, checkpoint_every=2,
@@ -325,7 +325,7 @@ def test_tensor_core_weight_gradient_matches_cuda_cores(cuda, oracle, layers, to
     gpw = torch.from_numpy(rng.standard_normal(tuple(pw.shape)).astype(np.float32)).cuda()
     t_tc.backward(gvol, gpw)
     t_cc.backward(gvol, gpw)
-    tc_slots = {2 * l for l in range(1, layers)} | {2 * layers + 2}
+    tc_slots = {2 * l for l in range(layers)} | {2 * layers, 2 * layers + 2}
     errs = {}
     for i in range(len(params)):
         a, b = t_tc.get_grad(i), t_cc.get_grad(i)
