@@ -29,7 +29,10 @@
 //   warps 2..5  epilogue: tcgen05.ld of both halves (one pixel per thread
 //               per half), bias + tanh, then store BF16 NHWC / L2-normalise
 //               / apply the pairwise net's 1x1 head; or (mode 3, a training
-//               step's input gradient) store the sums as FP32 NHWC
+//               step's input gradient) store the sums as FP32 NHWC; or (mode
+//               4) multiply them by the layer below's tanh derivative
+//               1 - y^2 and store them as FP32 NHWC and as the BF16 copy
+//               with a zero border that the layer below's gradients read
 // TMEM holds two tiles (four 128-column accumulators): the epilogue of tile i
 // overlaps the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout
 // the role raises the CTA abort flag and the global error flag, in-flight
@@ -62,6 +65,9 @@ struct TcParams {
     const float *head; // [2][NP] (mode 2)
     void *out;
     int *err;
+    const __nv_bfloat16 *aux; // mode 4: y [n_img][Ho][Wo][aux_cs]
+    __nv_bfloat16 *out16;     // mode 4: [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs]
+    int aux_cs, o16_cs, o16_ph, o16_pw;
 };
 
 // One stage's MMAs of one half, fully unrolled: kw taps x nk K-steps.
@@ -283,7 +289,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll 1
                 for (int c = 0; c < NP / 16; ++c) {
                     tc::tmem_ld16(ta + c * 16, v);
-                    if (p.mode == 3) {
+                    if (p.mode >= 3) {
+                        if (valid && p.mode == 4) {
+                            // dz of the layer below: the sums times 1 - y^2, y its BF16 output
+                            const uint4 *yp = (const uint4 *)(p.aux + pix * p.aux_cs + c * 16);
+                            const uint4 y0 = yp[0], y1 = yp[1];
+                            const uint32_t yw[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                const float a = __uint_as_float(yw[j] << 16), b = __uint_as_float(yw[j] & 0xffff0000u);
+                                v[2 * j] = v[2 * j] * (1.0f - a * a);
+                                v[2 * j + 1] = v[2 * j + 1] * (1.0f - b * b);
+                            }
+                            uint32_t u[8];
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                                u[j] = *(uint32_t *)&b2;
+                            }
+                            const size_t q16 = ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) *
+                                                   (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
+                            uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
+                            d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
+                            d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
+                        }
                         if (valid) {
                             float *o = (float *)p.out + pix * p.cp_out + c * 16;
 #pragma unroll
@@ -420,13 +449,19 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     p.num_tiles = a.n_img * p.Ho * p.tiles_x;
     p.mode = a.mode;
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
-    if (a.mode < 0 || a.mode > 3) return fail(CNNCRF_EINVAL, "conv_tc: mode %d", a.mode);
+    p.aux = (const __nv_bfloat16 *)a.aux, p.out16 = (__nv_bfloat16 *)a.out16;
+    p.aux_cs = a.aux_cs, p.o16_cs = a.o16_cs, p.o16_ph = a.o16_ph, p.o16_pw = a.o16_pw;
+    if (a.mode < 0 || a.mode > 4) return fail(CNNCRF_EINVAL, "conv_tc: mode %d", a.mode);
+    if (a.mode == 4 && (!a.aux || !a.out16 || a.aux_cs % 8 || a.aux_cs < a.np || a.o16_cs % 8 ||
+                        a.o16_cs < a.np || a.o16_ph < 0 || a.o16_pw < 0 || ((uintptr_t)a.aux & 15) ||
+                        ((uintptr_t)a.out16 & 15)))
+        return fail(CNNCRF_EINVAL, "conv_tc: mode 4 operands");
     // BF16 outputs store whole 16-channel groups; FP32 input gradients float4 groups below cout
     const bool bf16_out = a.mode == 0 || a.mode == 1;
     if (bf16_out && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);
-    if (a.mode == 3 && (a.cp_out % 4 != 0 || a.cp_out < a.cout || a.cout > a.np))
+    if (a.mode >= 3 && (a.cp_out % 4 != 0 || a.cp_out < a.cout || a.cout > a.np))
         return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d / cout %d", a.cp_out, a.cout);
-    if (a.mode != 3 && !a.bias) return fail(CNNCRF_EINVAL, "conv_tc: bias");
+    if (a.mode < 3 && !a.bias) return fail(CNNCRF_EINVAL, "conv_tc: bias");
     switch (a.np) {
     case 64:
         if (bf16_out && a.cp_out < 64) return fail(CNNCRF_EINVAL, "conv_tc: cp_out < N");

@@ -168,6 +168,31 @@ __global__ void k_tanh_bwd_pad(float *__restrict__ dy, const __nv_bfloat16 *__re
     *(uint4 *)(out + px * cp + g * 8) = make_uint4(u[0], u[1], u[2], u[3]);
 }
 
+// zero the border pixels of [n][H + 2p][W + 2q][cp] BF16: a thread per (border pixel, 8-channel group)
+__global__ void k_zero_border(__nv_bfloat16 *__restrict__ buf, int H, int W, int cp, int p, int q, long per_img,
+                              long total)
+{
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const int groups = cp >> 3, g = (int)(i % groups);
+    const long b = i / groups;
+    const int img = (int)(b / per_img);
+    long r = b - img * per_img; // border pixel index within the image
+    const int Wp = W + 2 * q, Hp = H + 2 * p;
+    int yy, xx;
+    if (r < (long)p * Wp) { // top rows
+        yy = (int)(r / Wp), xx = (int)(r % Wp);
+    } else if ((r -= (long)p * Wp) < (long)p * Wp) { // bottom rows
+        yy = H + p + (int)(r / Wp), xx = (int)(r % Wp);
+    } else { // left and right columns of the middle rows
+        r -= (long)p * Wp;
+        const int side = (int)(r / ((long)H * q));
+        r -= (long)side * H * q;
+        yy = p + (int)(r / q), xx = (int)(r % q) + (side ? W + q : 0);
+    }
+    *(uint4 *)(buf + (((long)img * Hp + yy) * Wp + xx) * cp + g * 8) = make_uint4(0u, 0u, 0u, 0u);
+}
+
 // out [n][H + 2p][W + 2q][C] = in [n][H][W][C] with a zero border
 __global__ void k_pad_zero(const float *__restrict__ in, int H, int W, int C, int p, int q, float *__restrict__ out)
 {
@@ -680,6 +705,17 @@ int train_tanh_bwd_pad(float *dy, const void *y, int nimg, int H, int W, int C, 
         k_tanh_bwd_pad<<<ceil_div(total, 256), 256, 0, st>>>(dy, (const __nv_bfloat16 *)y, H, W, C, ys, p, q, cp,
                                                              total, (__nv_bfloat16 *)out);
     }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_zero_border(void *buf, int nimg, int H, int W, int cp, int p, int q, cudaStream_t st)
+{
+    if (cp % 8 || ((uintptr_t)buf & 15)) return fail(CNNCRF_EINVAL, "zero_border: channel padding");
+    const long per_img = 2L * p * (W + 2 * q) + 2L * H * q;
+    const long total = (long)nimg * per_img * (cp / 8);
+    if (total == 0) return CNNCRF_OK;
+    k_zero_border<<<ceil_div(total, 256), 256, 0, st>>>((__nv_bfloat16 *)buf, H, W, cp, p, q, per_img, total);
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

@@ -14,13 +14,15 @@
 //      rows and kw - 1 columns ([img][Ho + 2(kh-1)][Wo + 2(kw-1)][cpa]), read
 //      at (oy + kh - 1, ox + kw - 1): pixels past the row end read the border
 //      or the box's zero fill, so they add nothing;
-//   B: the layer input at (oy + ky, ox + kx): the kx shift is a pixel offset,
-//      free of TMA's 16-byte rule because channels are the inner dimension.
+//   B: the layer input of row oy + ky, pixels x0 .. x0 + 71 (64 + a halo of
+//      8) in one box per 64 channels; tap kx reads it through a descriptor
+//      that starts kx 128-byte rows (pixels) in, so the input is loaded once
+//      per kernel row, not once per tap.
 // Channels past Cout / Cin give rows / columns of dW' that are not stored.
 //
 // One CTA per (ky, pixel split), 192 threads:
 //   warp 0      TMA: per K step (64 pixels of one output row) the dz boxes
-//               and kw x (input boxes) into a ring of stages
+//               and the input boxes into a ring of stages
 //   warp 1      TMEM allocation + single-thread tcgen05.mma, M = 128, N = NP,
 //               K = 16 x 4 per step, into kw accumulators of 128 columns
 //   warps 2..5  epilogue: warp q reads TMEM lanes (output channels) 32q..32q+31
@@ -42,17 +44,21 @@ namespace k {
 
 namespace {
 
-constexpr int BM = 128;                // output channels per tile (UMMA M)
-constexpr int KT = 64;                 // pixels per K step
-constexpr int BOX_BYTES = 64 * KT * 2; // one 64-channel x 64-pixel box: 8 KB
-constexpr int A_BYTES = 2 * BOX_BYTES; // M = 128 channels: two boxes
+constexpr int BM = 128;                  // output channels per tile (UMMA M)
+constexpr int KT = 64;                   // pixels per K step
+constexpr int BROWS = KT + 8;            // input pixels per step: the kx halo, whole 8-row swizzle atoms
+constexpr int A_BOX = 64 * KT * 2;       // one 64-channel x 64-pixel dz box: 8 KB
+constexpr int B_BOX = 64 * BROWS * 2;    // one 64-channel x 72-pixel input box: 9 KB
+constexpr int A_BYTES = 2 * A_BOX;       // M = 128 channels: two boxes
+constexpr int B_BYTES = 2 * B_BOX;       // N <= 128 channels: two boxes
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int NUM_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 512; // kw <= 3 accumulators of 128 columns
-constexpr int MAX_STAGES = 4;
+constexpr int MAX_STAGES = 6;
 constexpr int SLACK = 16384; // shared memory past the barriers that no operand is placed in
 
 struct WgTcParams {
-    int n_img, Ho, Wo, chunks_x, kh, kw, np, cout, cin, a_boxes, b_boxes, stages, stage_bytes, b_bytes;
+    int n_img, Ho, Wo, chunks_x, kh, kw, np, cout, cin, a_boxes, b_boxes, stages;
     long steps, steps_per_split;
     float *part; // [split][ky][kx][cout][cin]
     int *err;
@@ -64,7 +70,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = p.stages;
-    uint64_t *full = (uint64_t *)(smem + S * p.stage_bytes);
+    uint64_t *full = (uint64_t *)(smem + S * STAGE_BYTES);
     uint64_t *empty = full + S;
     uint64_t *done = empty + S;
     uint64_t *drain = done + 1;
@@ -103,7 +109,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             int stage = 0, issued = 0;
             uint32_t phase = 0;
             bool ok = true;
-            const uint32_t tx = (uint32_t)(p.a_boxes + p.kw * p.b_boxes) * BOX_BYTES;
+            const uint32_t tx = (uint32_t)(p.a_boxes * A_BOX + p.b_boxes * B_BOX);
             for (long st = s0; st < s1 && ok; ++st) {
                 const int img = (int)(st / per_img);
                 const long r = st - (long)img * per_img;
@@ -112,15 +118,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     ok = false;
                     break;
                 }
-                uint8_t *sa = smem + stage * p.stage_bytes;
+                uint8_t *sa = smem + stage * STAGE_BYTES;
                 tc::mbar_expect_tx(&full[stage], tx);
                 for (int b = 0; b < p.a_boxes; ++b)
-                    tc::tma_load_4d(sa + b * BOX_BYTES, &tmA, &full[stage], b * 64, x0 + p.kw - 1, oy + p.kh - 1,
-                                    img);
-                for (int kx = 0; kx < p.kw; ++kx)
-                    for (int b = 0; b < p.b_boxes; ++b)
-                        tc::tma_load_4d(sa + A_BYTES + kx * p.b_bytes + b * BOX_BYTES, &tmB, &full[stage], b * 64,
-                                        x0 + kx, oy + ky, img);
+                    tc::tma_load_4d(sa + b * A_BOX, &tmA, &full[stage], b * 64, x0 + p.kw - 1, oy + p.kh - 1, img);
+                for (int b = 0; b < p.b_boxes; ++b)
+                    tc::tma_load_4d(sa + A_BYTES + b * B_BOX, &tmB, &full[stage], b * 64, x0, oy + ky, img);
                 ++issued;
                 if (++stage == S) {
                     stage = 0;
@@ -154,13 +157,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t sa = tc::smem_u32(smem + stage * p.stage_bytes);
+                const uint32_t sa = tc::smem_u32(smem + stage * STAGE_BYTES);
                 for (int kx = 0; kx < p.kw; ++kx) {
 #pragma unroll
                     for (int kk = 0; kk < KT / 16; ++kk) {
-                        // a K step of 16 pixels = 16 rows of 128 bytes = two 8-row swizzle atoms
-                        const uint64_t da = tc::sdesc_sw128_mn(sa + kk * 2048, BOX_BYTES);
-                        const uint64_t db = tc::sdesc_sw128_mn(sa + A_BYTES + kx * p.b_bytes + kk * 2048, BOX_BYTES);
+                        // a K step of 16 pixels = 16 rows of 128 bytes = two 8-row swizzle atoms; tap kx
+                        // starts kx rows into the input box (the swizzle follows the absolute address)
+                        const uint64_t da = tc::sdesc_sw128_mn(sa + kk * 2048, A_BOX);
+                        const uint64_t db = tc::sdesc_sw128_mn(sa + A_BYTES + kx * 128 + kk * 2048, B_BOX);
                         tc::umma_bf16(tmem + kx * BM, da, db, idesc, (st > s0 || kk > 0) ? 1u : 0u);
                     }
                 }
@@ -234,10 +238,7 @@ __global__ void __launch_bounds__(256) k_wgrad_tc_reduce(const float *__restrict
     dw[(((long)co * Cin + ci) * kh + (kh - 1 - ky)) * kw + (kw - 1 - kx)] += t;
 }
 
-size_t smem_bytes(int stages, int stage_bytes)
-{
-    return 1024 + (size_t)stages * stage_bytes + (2 * stages + 2) * 8 + 16 + SLACK;
-}
+size_t smem_bytes(int stages) { return 1024 + (size_t)stages * STAGE_BYTES + (2 * stages + 2) * 8 + 16 + SLACK; }
 
 } // namespace
 
@@ -294,7 +295,7 @@ int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, 
         // the layer's input extent exactly (the rows may be a window of a wider image): nothing past it is read
         cuuint64_t g[4] = {(cuuint64_t)in_pix, (cuuint64_t)Win, (cuuint64_t)Hin, (cuuint64_t)nimg};
         cuuint64_t s[3] = {(cuuint64_t)in_pix * 2, (cuuint64_t)in_row * 2, (cuuint64_t)in_img * 2};
-        cuuint32_t box[4] = {64, KT, 1, 1}, e[4] = {1, 1, 1, 1};
+        cuuint32_t box[4] = {64, BROWS, 1, 1}, e[4] = {1, 1, 1, 1};
         CUresult r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)in, g, s, box, e,
                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -307,8 +308,6 @@ int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, 
     // it would fill are not stored).  N = np reads a second input box when np > 64.
     p.a_boxes = Cout > 64 ? 2 : 1;
     p.b_boxes = np > 64 ? 2 : 1;
-    p.b_bytes = 2 * BOX_BYTES; // per tap, whether one or two boxes are loaded
-    p.stage_bytes = A_BYTES + kw * p.b_bytes;
     p.steps = steps;
     p.steps_per_split = (steps + splits - 1) / splits;
     p.part = (float *)scratch;
@@ -318,9 +317,9 @@ int wgrad_tc(const void *dzpad, int Cout, int cpa, const void *in, long in_pix, 
     CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     p.stages = 0;
     for (int s = 2; s <= MAX_STAGES; ++s)
-        if (smem_bytes(s, p.stage_bytes) <= (size_t)maxsm) p.stages = s;
+        if (smem_bytes(s) <= (size_t)maxsm) p.stages = s;
     if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "wgrad_tc: shared memory");
-    const size_t smem = smem_bytes(p.stages, p.stage_bytes);
+    const size_t smem = smem_bytes(p.stages);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_wgrad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     // every split has at least one step: splits <= steps and steps_per_split = ceil(steps / splits)
     const int used = (int)((steps + p.steps_per_split - 1) / p.steps_per_split);

@@ -54,10 +54,16 @@ struct TcConvArgs {
     const float *bias; // [np] zero padded
     const float *head; // [2][np] (mode 2)
     int mode;          // 0 tanh -> BF16, 1 tanh + L2 norm -> BF16, 2 tanh + 1x1 head + abs -> FP32 [2][Ho][Wo],
-                       // 3 the plain sums -> FP32 [n_img][Ho][Wo][cp_out], channels < cout (input gradients)
+                       // 3 the plain sums -> FP32 [n_img][Ho][Wo][cp_out], channels < cout (input gradients),
+                       // 4 the sums times 1 - aux^2 -> FP32 as mode 3 and BF16 into out16 (below)
     void *out;
     int cp_out;
     int *err; // set to 1 if a bounded wait gave up
+    // mode 4: aux = BF16 [n_img][Ho][Wo][aux_cs] (the layer below's output); out16 = BF16
+    // [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs], written inside its border (channels < np)
+    const void *aux = nullptr;
+    void *out16 = nullptr;
+    int aux_cs = 0, o16_cs = 0, o16_ph = 0, o16_pw = 0;
 };
 int conv_tc(const TcConvArgs &a, cudaStream_t st);
 
@@ -91,6 +97,8 @@ int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int 
 int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16, cudaStream_t st);
 // the input gradient's tensor-core layout [np][kh*kw][cp]: w16d[ci][tap][co] = w[co][ci][ky][kx], unflipped
 int train_w16_dgrad(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16d, cudaStream_t st);
+// zero the (p, q) border of BF16 [n][H + 2p][W + 2q][cp] (all channels)
+int train_zero_border(void *buf, int nimg, int H, int W, int cp, int p, int q, cudaStream_t st);
 // dy *= 1 - y^2 (y BF16) and a BF16 copy with a (p, q) zero border and channels padded to cp (conv_tc's input)
 int train_tanh_bwd_pad(float *dy, const void *y, int nimg, int H, int W, int C, int ys, int p, int q, int cp,
                        void *out, cudaStream_t st);

@@ -67,7 +67,10 @@ struct cnncrf_train {
     size_t crfws_bytes = 0;
     DevBuf wgs; // the tensor-core weight gradient's planar copies and partial sums
     size_t wgs_bytes = 0;
-    DevBuf dpad; // the BF16 padded output gradient: the tensor-core weight and input gradients read it
+    // the BF16 padded output gradient that the tensor-core weight and input gradients read; two, since a
+    // fused input gradient writes the layer below's copy while reading its own
+    DevBuf dpad[2];
+    int dcur = 0;
 
     int build();
     int refresh();
@@ -76,7 +79,7 @@ struct cnncrf_train {
     int backward(const float *gv, const float *gp);
     int run_layer(int s, int l);
     int layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img, const void *y,
-                   int ys, float *dz, float *dprev);
+                   int ys, float *dz, float *dprev, bool &ready, const TLayer *below);
     float *param(int slot) { return theta.as<float>() + off[slot]; }
     float *gradp(int slot) { return grad.as<float>() + off[slot]; }
     size_t es() const { return bf16 ? 2 : 4; }
@@ -247,7 +250,8 @@ int cnncrf_train::build()
             if (Ly.w16d.get() || Ly.tcw)
                 dpad_bytes = std::max(dpad_bytes, 2 * (size_t)n * (Ly.hout() + 2 * (Ly.kh - 1)) *
                                                       (Ly.wout() + 2 * (Ly.kw - 1)) * pad_to(Ly.cout, 64));
-    if (dpad_bytes) CNNCRF_TRY(dpad.reserve(dpad_bytes));
+    if (dpad_bytes)
+        for (auto &b : dpad) CNNCRF_TRY(zalloc(b, dpad_bytes));
     const int ns = k::train_wgrad_splits(Pmax); // the most bias splits any layer uses
     CNNCRF_TRY(part.reserve(sizeof(float) * part_floats));
     CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
@@ -418,20 +422,27 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
 
 // dz: the layer's output gradient (dense FP32), turned into the pre-activation
 // gradient in place; y: the layer's output at channel stride ys; dprev (if
-// set): the input gradient (dense FP32)
+// set): the input gradient (dense FP32).  ready: on entry, whether dz already
+// holds the output gradient times 1 - y^2 with its BF16 padded copy in
+// dpad[dcur] (the layer above's fused input gradient made them); on exit,
+// whether this call made dprev so for `below`, the layer whose output is `in`.
 int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img,
-                             const void *y, int ys, float *dz, float *dprev)
+                             const void *y, int ys, float *dz, float *dprev, bool &ready, const TLayer *below)
 {
     const int Ho = L.hout(), Wo = L.wout();
     const int ph = L.kh - 1, pwd = L.kw - 1;
     const bool tcd = dprev && L.w16d.get(); // the input gradient on the tensor cores (BF16 mode)
-    if (tcd || L.tcw) // dz and its BF16 padded copy, the tensor-core operand
-        CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, n, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64), dpad.get(), st));
-    else
-        CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
+    if (!ready) {
+        if (tcd || L.tcw) // dz and its BF16 padded copy, the tensor-core operand
+            CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, n, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64),
+                                             dpad[dcur].get(), st));
+        else
+            CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
+    }
+    ready = false;
     if (L.tcw && in_bf16) { // BF16 mode, tensor cores
-        CNNCRF_TRY(k::wgrad_tc(dpad.get(), L.cout, pad_to(L.cout, 64), in, in_pix, in_row, in_img, L.cin, L.kh, L.kw,
-                               n, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
+        CNNCRF_TRY(k::wgrad_tc(dpad[dcur].get(), L.cout, pad_to(L.cout, 64), in, in_pix, in_row, in_img, L.cin, L.kh,
+                               L.kw, n, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
         if (L.bslot >= 0)
             CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
     } else {
@@ -442,11 +453,23 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
     if (!dprev) return CNNCRF_OK;
     if (tcd) { // dprev = the valid convolution of the padded dz with the unflipped, transposed kernel
         k::TcConvArgs t{};
-        t.in = dpad.get(), t.n_img = n, t.Hin = Ho + 2 * ph, t.Win = Wo + 2 * pwd;
+        t.in = dpad[dcur].get(), t.n_img = n, t.Hin = Ho + 2 * ph, t.Win = Wo + 2 * pwd;
         t.cp_in = pad_to(L.cout, 64), t.cin = L.cout;
         t.wt = L.w16d.get(), t.np = umma_n(L.cin), t.cout = L.cin, t.kh = L.kh, t.kw = L.kw;
         t.mode = 3, t.out = dprev, t.cp_out = L.cin, t.err = tcerr.as<int>();
-        return k::conv_tc(t, st);
+        // fused with the layer below's tanh backward when its gradients read the padded copy too
+        const bool fuse = below && in_bf16 && (below->tcw || below->w16d.get()) && below->hout() == L.hin &&
+                          below->wout() == L.win && below->cout == L.cin && in_row == (long)L.win * in_pix &&
+                          in_img == (long)L.hin * in_row;
+        if (fuse) {
+            const int bph = below->kh - 1, bpw = below->kw - 1, bcp = pad_to(below->cout, 64);
+            CNNCRF_TRY(k::train_zero_border(dpad[dcur ^ 1].get(), n, L.hin, L.win, bcp, bph, bpw, st));
+            t.mode = 4, t.aux = in, t.aux_cs = (int)in_pix;
+            t.out16 = dpad[dcur ^ 1].get(), t.o16_cs = bcp, t.o16_ph = bph, t.o16_pw = bpw;
+        }
+        CNNCRF_TRY(k::conv_tc(t, st));
+        if (fuse) dcur ^= 1, ready = true;
+        return CNNCRF_OK;
     }
     CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
     const int Hp = Ho + 2 * ph, Wp = Wo + 2 * pwd;
@@ -469,6 +492,7 @@ int cnncrf_train::backward(const float *gv, const float *gp)
     for (int s = 0; s < 2; ++s) {
         CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
         float *cur = dy.as<float>(), *nxt = dyb.as<float>();
+        bool ready = false;
         int top = L - 1;
         while (top >= 0) {
             int c = top - 1; // the checkpoint under this segment (-1: the normalised input)
@@ -482,7 +506,7 @@ int cnncrf_train::backward(const float *gv, const float *gp)
                 const bool ib = (j > 0 && bf16) || n16;
                 const int cs = j > 0 ? fs : n16 ? 64 : ic;
                 CNNCRF_TRY(layer_back(Ly, in, ib, cs, (long)Ly.win * cs, (long)Ly.hin * Ly.win * cs, actp(s, j), fs,
-                                      cur, j > 0 ? nxt : nullptr));
+                                      cur, j > 0 ? nxt : nullptr, ready, j > 0 ? &feat[j - 1] : nullptr));
                 std::swap(cur, nxt);
             }
             top = c;
@@ -494,17 +518,18 @@ int cnncrf_train::backward(const float *gv, const float *gp)
                                      dy.as<float>(), st));
         CNNCRF_TRY(k::train_wgrad_head(gh.as<float>(), y2.get(), bf16, ps, (long)n * H * W, P, partb.as<float>(),
                                        gradp(pw[2].wslot), st));
+        bool ready = false;
         CNNCRF_TRY(layer_back(pw[1], y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
-                              ps, dy.as<float>(), dyb.as<float>()));
+                              ps, dy.as<float>(), dyb.as<float>(), ready, &pw[0]));
         const int cr = p - 2;
         if (pw[0].tcw) {
             const void *in = (const char *)norm16[0].get() + 2 * ((size_t)cr * w + cr) * 64;
             CNNCRF_TRY(layer_back(pw[0], in, true, 64, (long)w * 64, (long)h * w * 64, y1.get(), ps, dyb.as<float>(),
-                                  nullptr));
+                                  nullptr, ready, nullptr));
         } else {
             const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
             CNNCRF_TRY(layer_back(pw[0], in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps,
-                                  dyb.as<float>(), nullptr));
+                                  dyb.as<float>(), nullptr, ready, nullptr));
         }
     }
     return CNNCRF_OK;
