@@ -4,15 +4,18 @@
 // bias.cpp:58-67, activation.cpp:33-41).
 //
 // GEMM view: D[pixel][n] = sum_{tap, c} act[y+ky][x+kx][c] * W[n][tap][c]
-// (kernel pre-flipped on the host: CUDNN_CONVOLUTION).  A tile is 256
-// consecutive output pixels of one row, computed as two M = 128 halves that
-// share every weight load; N = NP output channels; K runs over taps x
-// 64-channel chunks of the NHWC input.
+// (kernel pre-flipped on the host: CUDNN_CONVOLUTION).  A tile is two M = 128
+// halves of 128 output pixels that share every weight load; N = NP output
+// channels; K runs over taps x 64-channel chunks of the NHWC input.  Paired
+// tiles are 256 consecutive pixels of one row; where a row's width modulo 256
+// lies in (0, 128] (the last paired tile would be mostly empty) the tiles are
+// instead consecutive entries of the list of all rows' 128-pixel halves, so a
+// tile's halves may come from two rows.
 //
 // Operand reuse: one shared-memory stage holds, for one kernel row ky and one
 // 64-channel chunk, the 264-pixel window of input row y+ky that both halves
-// read (a 128-row and a 136-row box, one after the other) and the weights of
-// the kw taps of that row.  The kx taps read the same window
+// read (a 128-row and a 136-row box, one after the other; with independent
+// halves a 136-row window per half) and the weights of the kw taps of that row.  The kx taps read the same window
 // shifted by kx pixels (a descriptor that starts kx 128-byte rows into the
 // swizzled tile), so the input is loaded once per kernel row instead of once
 // per tap.
@@ -50,9 +53,9 @@ namespace k {
 namespace {
 
 constexpr int BM = 128;                 // pixels per half (UMMA M)
-constexpr int TILE_PX = 2 * BM;         // pixels per tile
-constexpr int AROWS = 2 * BM + 8;       // input window of both halves: 256 px + up to 8 more for the kx taps
-constexpr int A_BYTES = AROWS * 128;    // 264 rows x 64 bf16 = 33 KB (loaded as 128 + 136 rows)
+constexpr int TILE_PX = 2 * BM;         // pixels per paired tile
+constexpr int HROWS = BM + 8;           // one half's input window: 128 px + up to 8 more for the kx taps
+constexpr int AROWS = BM + HROWS;       // paired: 264 rows x 64 bf16 = 33 KB (loaded as 128 + 136 rows)
 constexpr int NUM_THREADS = 224;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
@@ -61,6 +64,8 @@ constexpr int MAX_STAGES = 4;
 struct TcParams {
     int n_img, Hin, Win, Ho, Wo, kh, kw, cp_in, kchunks, kk_last, cout, cp_out, tiles_x, num_tiles, mode,
         stages, stage_bytes;
+    int halves;      // 0: paired tiles; else the number of 128-pixel halves (tiles_x = halves per row)
+    int a_bytes;     // the input window of a stage: AROWS or 2 * HROWS rows of 128 bytes
     const float *bias; // [NP], zero padded
     const float *head; // [2][NP] (mode 2)
     void *out;
@@ -69,6 +74,26 @@ struct TcParams {
     __nv_bfloat16 *out16;     // mode 4: [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs]
     int aux_cs, o16_cs, o16_ph, o16_pw;
 };
+
+// Output pixel coordinates of half h of tile t; false if the half is past
+// the end of the half list (the last tile of an odd count)
+__device__ __forceinline__ bool half_coords(const TcParams &p, int t, int h, int &img, int &y, int &x0)
+{
+    if (p.halves == 0) {
+        const int per = p.Ho * p.tiles_x;
+        img = t / per;
+        const int r = t - img * per;
+        y = r / p.tiles_x;
+        x0 = (r - y * p.tiles_x) * TILE_PX + h * BM;
+        return true;
+    }
+    const int hi = 2 * t + h, hc = min(hi, p.halves - 1), per = p.Ho * p.tiles_x;
+    img = hc / per;
+    const int r = hc - img * per;
+    y = r / p.tiles_x;
+    x0 = (r - y * p.tiles_x) * BM;
+    return hi < p.halves;
+}
 
 // One stage's MMAs of one half, fully unrolled: kw taps x nk K-steps.
 // Descriptor arithmetic is in 16-byte units: +8 moves the A window one pixel
@@ -148,7 +173,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     const int kblocks = p.kh * p.kchunks; // stages per tile: (ky, chunk)
-    const int tiles_per_img = p.Ho * p.tiles_x;
 
     if (warp == 0) {
         if (lane == 0) {
@@ -156,8 +180,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             uint32_t phase = 0;
             bool ok = true;
             for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
-                const int img = t / tiles_per_img, r = t - img * tiles_per_img;
-                const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * TILE_PX;
+                int img0, y0, x00, img1, y1, x01;
+                half_coords(p, t, 0, img0, y0, x00);
+                half_coords(p, t, 1, img1, y1, x01);
                 for (int kb = 0; kb < kblocks; ++kb) {
                     const int ky = kb / p.kchunks, ch = kb - ky * p.kchunks;
                     if (!tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag)) {
@@ -166,11 +191,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                     uint8_t *sa = smem + stage * STAGE;
                     tc::mbar_expect_tx(&full[stage], STAGE);
-                    // input pixels x0 .. x0 + 263 as rows 0 .. 263 (a 128-row and a 136-row box)
-                    tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x0, y + ky, img);
-                    tc::tma_load_4d(sa + BM * 128, &tmA2, &full[stage], ch * 64, x0 + BM, y + ky, img);
+                    if (p.halves == 0) {
+                        // input pixels x0 .. x0 + 263 as rows 0 .. 263 (a 128-row and a 136-row box)
+                        tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x00, y0 + ky, img0);
+                        tc::tma_load_4d(sa + BM * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
+                    } else { // a 136-row window per half
+                        tc::tma_load_4d(sa, &tmA2, &full[stage], ch * 64, x00, y0 + ky, img0);
+                        tc::tma_load_4d(sa + HROWS * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
+                    }
                     for (int kx = 0; kx < p.kw; ++kx)
-                        tc::tma_load_2d(sa + A_BYTES + kx * B_BYTES, &tmB, &full[stage],
+                        tc::tma_load_2d(sa + p.a_bytes + kx * B_BYTES, &tmB, &full[stage],
                                         (ky * p.kw + kx) * p.cp_in + ch * 64, 0);
                     ++issued;
                     if (++stage == S) {
@@ -220,8 +250,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int ch = kb % p.kchunks;
                     const int nk = (ch == p.kchunks - 1) ? p.kk_last : 4;
                     const uint32_t sa = tc::smem_u32(smem + stage * STAGE);
-                    const uint64_t a = tc::sdesc_sw128(sa + h * BM * 128);
-                    const uint64_t db = tc::sdesc_sw128(sa + A_BYTES);
+                    const uint64_t a = tc::sdesc_sw128(sa + h * (p.halves ? HROWS : BM) * 128);
+                    const uint64_t db = tc::sdesc_sw128(sa + p.a_bytes);
                     const uint32_t first = kb == 0 ? 0u : 1u;
                     if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d, a, db, first);
                     else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d, a, db, first);
@@ -259,13 +289,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 break;
             }
             tc::fence_after_sync();
-            const int img = t / tiles_per_img, r = t - img * tiles_per_img;
-            const int y = r / p.tiles_x, x0 = (r - y * p.tiles_x) * TILE_PX;
+            int himg[2], hy[2], hx0[2];
+            bool hok[2];
+            hok[0] = half_coords(p, t, 0, himg[0], hy[0], hx0[0]);
+            hok[1] = half_coords(p, t, 1, himg[1], hy[1], hx0[1]);
             float hv0[2] = {0.0f, 0.0f}, hv1[2] = {0.0f, 0.0f};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                const int x = x0 + h * BM + row;
-                const bool valid = x < p.Wo;
+                const int img = himg[h], y = hy[h], x = hx0[h] + row;
+                const bool valid = hok[h] && x < p.Wo;
                 const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf + h) * ACC_STRIDE;
                 float v[16];
                 // the TMEM reads are warp-collective: every lane runs them
@@ -355,13 +387,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::mbar_arrive(&tempty[buf]);
             if (p.mode == 2) {
                 const size_t plane = (size_t)p.Ho * p.Wo;
-                float *o = (float *)p.out + (size_t)img * 2 * plane; // [img][2][Ho][Wo]
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
-                    const int x = x0 + h * BM + row;
-                    if (x < p.Wo) {
-                        o[(size_t)y * p.Wo + x] = fabsf(hv0[h]);
-                        o[plane + (size_t)y * p.Wo + x] = fabsf(hv1[h]);
+                    float *o = (float *)p.out + (size_t)himg[h] * 2 * plane; // [img][2][Ho][Wo]
+                    const int x = hx0[h] + row;
+                    if (hok[h] && x < p.Wo) {
+                        o[(size_t)hy[h] * p.Wo + x] = fabsf(hv0[h]);
+                        o[plane + (size_t)hy[h] * p.Wo + x] = fabsf(hv1[h]);
                     }
                 }
             }
@@ -374,11 +406,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     }
 }
 
-template <int NP> int stage_bytes(int kw) { return A_BYTES + kw * NP * 128; }
+template <int NP> int stage_bytes(int a_bytes, int kw) { return a_bytes + kw * NP * 128; }
 
-template <int NP> size_t smem_bytes(int stages, int kw, int mode)
+template <int NP> size_t smem_bytes(int stages, int a_bytes, int kw, int mode)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>(kw) + (2 * stages + 6) * 8 + 16 + (mode == 2 ? 3 : 1) * NP * 4;
+    return 1024 + (size_t)stages * stage_bytes<NP>(a_bytes, kw) + (2 * stages + 6) * 8 + 16 +
+           (mode == 2 ? 3 : 1) * NP * 4;
 }
 
 template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
@@ -411,12 +444,12 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    p.stage_bytes = stage_bytes<NP>(a.kw);
+    p.stage_bytes = stage_bytes<NP>(p.a_bytes, a.kw);
     p.stages = 0;
     for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
-        if (smem_bytes<NP>(s, a.kw, a.mode) <= (size_t)maxsm) p.stages = s;
+        if (smem_bytes<NP>(s, p.a_bytes, a.kw, a.mode) <= (size_t)maxsm) p.stages = s;
     if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
-    const size_t smem = smem_bytes<NP>(p.stages, a.kw, a.mode);
+    const size_t smem = smem_bytes<NP>(p.stages, p.a_bytes, a.kw, a.mode);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = std::min(p.num_tiles, sms);
     {
@@ -445,8 +478,18 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     int rem = a.cin - 64 * (p.kchunks - 1);
     p.kk_last = rem <= 0 ? 1 : std::min(4, (rem + 15) / 16);
     p.cout = a.cout, p.cp_out = a.cp_out;
-    p.tiles_x = ceil_div(p.Wo, TILE_PX);
-    p.num_tiles = a.n_img * p.Ho * p.tiles_x;
+    const int rem256 = p.Wo % TILE_PX;
+    if (rem256 > 0 && rem256 <= BM) { // independent halves: the last paired tile of a row would be mostly empty
+        p.tiles_x = ceil_div(p.Wo, BM);
+        p.halves = a.n_img * p.Ho * p.tiles_x;
+        p.num_tiles = ceil_div(p.halves, 2);
+        p.a_bytes = 2 * HROWS * 128;
+    } else {
+        p.tiles_x = ceil_div(p.Wo, TILE_PX);
+        p.halves = 0;
+        p.num_tiles = a.n_img * p.Ho * p.tiles_x;
+        p.a_bytes = AROWS * 128;
+    }
     p.mode = a.mode;
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
     p.aux = (const __nv_bfloat16 *)a.aux, p.out16 = (__nv_bfloat16 *)a.out16;
