@@ -112,6 +112,11 @@ int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx
 // features at channel stride fs
 int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,
                    int npairs, int H, int W, int C, int D, int omin, int omax, float *dfl, float *dfr, cudaStream_t st);
+// the same on the tensor cores (k_corr_bwd_tc.cu): BF16 features at channel stride fs (a multiple of
+// 64); the list's offsets must be distinct.  err: the bounded-wait error flag
+bool corr_bwd_tc_supported(int C, int fs, int D, int omin, int omax);
+int corr_bwd_tc(const void *fl, const void *fr, int fs, const float *gvol, const float *d_list, int npairs, int H,
+                int W, int C, int D, int omin, int omax, float *dfl, float *dfr, int *err, cudaStream_t st);
 // pixel splits of the bias gradient's fixed-order reduction for P output pixels (about four per SM)
 int train_wgrad_splits(long P);
 // pixel splits of the weight gradient (K = kh*kw*Cin): about four CTAs per SM, >= 512 pixels each

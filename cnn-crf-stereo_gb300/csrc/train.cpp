@@ -57,6 +57,7 @@ struct cnncrf_train {
     // forward state; feature-layer outputs: checkpoints in their own buffers, the rest in a shared pool
     DevBuf padded[2], norm[2], scratch;
     DevBuf norm16[2]; // BF16 copies of norm at channel stride 64 (the first layers' tensor-core weight gradients)
+    bool tc_corr = false; // the correlation adjoint on the tensor cores
     std::vector<char> keep;
     std::vector<DevBuf> act[2], pool;
     DevBuf fbuf, vol, y1, y2, pwout; // fbuf: both sides' normalised features
@@ -242,6 +243,7 @@ int cnncrf_train::build()
                     Ly.tcw = true;
                 }
     if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
+    tc_corr = bf16 && d.tc_dgrad && k::corr_bwd_tc_supported(F, cp_feat, D, omin, omax);
     if (feat[0].tcw || pw[0].tcw)
         for (int s = 0; s < 2; ++s) CNNCRF_TRY(zalloc(norm16[s], 2 * (size_t)n * h * w * 64));
     size_t dpad_bytes = 0;
@@ -487,8 +489,12 @@ int cnncrf_train::backward(const float *gv, const float *gp)
     const int F = d.feat_channels, P = d.pw_channels, L = (int)feat.size(), fs = fstride(), ps = pstride();
     const long N = (long)n * H * W;
     CNNCRF_CUDA(cudaMemsetAsync(grad.get(), 0, total * sizeof(float), st));
-    CNNCRF_TRY(k::train_corr_bwd(fside(0), fside(1), bf16, fs, gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
-                                 df[0].as<float>(), df[1].as<float>(), st));
+    if (tc_corr)
+        CNNCRF_TRY(k::corr_bwd_tc(fside(0), fside(1), fs, gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
+                                  df[0].as<float>(), df[1].as<float>(), tcerr.as<int>(), st));
+    else
+        CNNCRF_TRY(k::train_corr_bwd(fside(0), fside(1), bf16, fs, gv, dlist.as<float>(), n, H, W, F, D, omin,
+                                     omax, df[0].as<float>(), df[1].as<float>(), st));
     for (int s = 0; s < 2; ++s) {
         CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
         float *cur = dy.as<float>(), *nxt = dyb.as<float>();
