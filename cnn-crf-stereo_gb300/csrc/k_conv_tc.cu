@@ -73,6 +73,7 @@ struct TcParams {
     const __nv_bfloat16 *aux; // mode 4: y [n_img][Ho][Wo][aux_cs]
     __nv_bfloat16 *out16;     // mode 4: [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs]
     int aux_cs, o16_cs, o16_ph, o16_pw;
+    float *bias_part;         // mode 4 (optional): [gridDim.x * 4][cout] channel sums of the output
 };
 
 // Output pixel coordinates of half h of tile t; false if the half is past
@@ -93,6 +94,100 @@ __device__ __forceinline__ bool half_coords(const TcParams &p, int t, int h, int
     y = r / p.tiles_x;
     x0 = (r - y * p.tiles_x) * BM;
     return hi < p.halves;
+}
+
+// Mode 4 epilogue of one half for this thread's pixel: dz of the layer below
+// = the sums times 1 - y^2 as BF16 into the padded copy (and FP32 if p.out),
+// plus the warp's per-channel sums into sacc.  All NP / 16 chunks unrolled;
+// the caller loads y (load_dz_y) for both halves before either is used, so
+// the tile waits on memory once.
+template <int NP>
+__device__ __forceinline__ void load_dz_y(const TcParams &p, bool valid, int img, int y, int x, uint4 (*yv)[2])
+{
+    const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
+#pragma unroll
+    for (int c = 0; c < NP / 16; ++c) {
+        if (valid) {
+            const uint4 *yp = (const uint4 *)(p.aux + pix * p.aux_cs + c * 16);
+            yv[c][0] = yp[0], yv[c][1] = yp[1];
+        } else {
+            yv[c][0] = yv[c][1] = make_uint4(0u, 0u, 0u, 0u);
+        }
+    }
+}
+
+template <int NP>
+__device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta, bool valid, int img, int y, int x,
+                                            int q, int lane, float *sacc, const uint4 (*yv)[2])
+{
+    constexpr int NC = NP / 16;
+    const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
+    const size_t q16 = ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        float v[16];
+        tc::tmem_ld16(ta + c * 16, v); // warp-collective
+        const uint32_t yw[8] = {yv[c][0].x, yv[c][0].y, yv[c][0].z, yv[c][0].w,
+                                yv[c][1].x, yv[c][1].y, yv[c][1].z, yv[c][1].w};
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const float a = __uint_as_float(yw[j] << 16), b = __uint_as_float(yw[j] & 0xffff0000u);
+            v[2 * j] = valid ? v[2 * j] * (1.0f - a * a) : 0.0f; // invalid pixels add nothing to the sums
+            v[2 * j + 1] = valid ? v[2 * j + 1] * (1.0f - b * b) : 0.0f;
+        }
+        if (valid) {
+            uint32_t u[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                u[j] = *(uint32_t *)&b2;
+            }
+            uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
+            d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
+            d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
+            if (p.out) {
+                float *o = (float *)p.out + pix * p.cp_out + c * 16;
+#pragma unroll
+                for (int g = 0; g < 4; ++g) {
+                    if (c * 16 + 4 * g + 3 < p.cout)
+                        *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
+                    else
+#pragma unroll
+                        for (int j = 0; j < 4; ++j)
+                            if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
+                }
+            }
+        }
+        if (p.bias_part) {
+            // the warp's 32 pixels summed per channel: each exchange halves the values a lane keeps;
+            // lane L ends with channel c * 16 + (L >> 1), twice
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const bool up = lane & 16;
+                const float keep = up ? v[i + 8] : v[i], give = up ? v[i] : v[i + 8];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, give, 16);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const bool up = lane & 8;
+                const float keep = up ? v[i + 4] : v[i], give = up ? v[i] : v[i + 4];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, give, 8);
+            }
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                const bool up = lane & 4;
+                const float keep = up ? v[i + 2] : v[i], give = up ? v[i] : v[i + 2];
+                v[i] = keep + __shfl_xor_sync(0xffffffffu, give, 4);
+            }
+            {
+                const bool up = lane & 2;
+                const float keep = up ? v[1] : v[0], give = up ? v[0] : v[1];
+                v[0] = keep + __shfl_xor_sync(0xffffffffu, give, 2);
+            }
+            v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+            if (!(lane & 1)) sacc[q * NP + c * 16 + (lane >> 1)] += v[0];
+        }
+    }
 }
 
 // One stage's MMAs of one half, fully unrolled: kw taps x nk K-steps.
@@ -141,6 +236,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     volatile int *zero_flag = abort_flag + 1;
     float *sbias = (float *)(tmem_slot + 4);
     float *shead = sbias + NP;
+    float *sacc = shead + 2 * NP; // mode 4 bias sums: [4 epilogue warps][NP]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -164,6 +260,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
     if (p.mode == 2)
         for (int i = threadIdx.x; i < 2 * NP; i += NUM_THREADS) shead[i] = p.head[i];
+    if (p.bias_part)
+        for (int i = threadIdx.x; i < 4 * NP; i += NUM_THREADS) sacc[i] = 0.0f;
     if (warp == 1) {
         tc::tmem_alloc(tmem_slot, TMEM_COLS);
         tc::tmem_relinquish();
@@ -293,6 +391,19 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             bool hok[2];
             hok[0] = half_coords(p, t, 0, himg[0], hy[0], hx0[0]);
             hok[1] = half_coords(p, t, 1, himg[1], hy[1], hx0[1]);
+            if (p.mode == 4) {
+                uint4 ya[NP / 16][2], yb[NP / 16][2];
+                load_dz_y<NP>(p, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, ya);
+                load_dz_y<NP>(p, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, yb);
+                const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf) * ACC_STRIDE;
+                epilogue_dz<NP>(p, tq, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, q, lane, sacc,
+                                ya);
+                epilogue_dz<NP>(p, tq + ACC_STRIDE, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, q,
+                                lane, sacc, yb);
+                tc::fence_before_sync();
+                tc::mbar_arrive(&tempty[buf]);
+                continue;
+            }
             float hv0[2] = {0.0f, 0.0f}, hv1[2] = {0.0f, 0.0f};
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
@@ -321,30 +432,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll 1
                 for (int c = 0; c < NP / 16; ++c) {
                     tc::tmem_ld16(ta + c * 16, v);
-                    if (p.mode >= 3) {
-                        if (valid && p.mode == 4) {
-                            // dz of the layer below: the sums times 1 - y^2, y its BF16 output
-                            const uint4 *yp = (const uint4 *)(p.aux + pix * p.aux_cs + c * 16);
-                            const uint4 y0 = yp[0], y1 = yp[1];
-                            const uint32_t yw[8] = {y0.x, y0.y, y0.z, y0.w, y1.x, y1.y, y1.z, y1.w};
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                const float a = __uint_as_float(yw[j] << 16), b = __uint_as_float(yw[j] & 0xffff0000u);
-                                v[2 * j] = v[2 * j] * (1.0f - a * a);
-                                v[2 * j + 1] = v[2 * j + 1] * (1.0f - b * b);
-                            }
-                            uint32_t u[8];
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                                u[j] = *(uint32_t *)&b2;
-                            }
-                            const size_t q16 = ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) *
-                                                   (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
-                            uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
-                            d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
-                            d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
-                        }
+                    if (p.mode == 3) {
                         if (valid) {
                             float *o = (float *)p.out + pix * p.cp_out + c * 16;
 #pragma unroll
@@ -400,6 +488,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
     }
     __syncthreads();
+    if (p.bias_part) // this CTA's four partial sums per channel
+        for (int i = threadIdx.x; i < 4 * p.cout; i += NUM_THREADS)
+            p.bias_part[((size_t)blockIdx.x * 4 + i / p.cout) * p.cout + i % p.cout] =
+                sacc[(i / p.cout) * NP + i % p.cout];
     if (warp == 1) {
         tc::fence_after_sync();
         tc::tmem_dealloc(tmem, TMEM_COLS);
@@ -411,7 +503,7 @@ template <int NP> int stage_bytes(int a_bytes, int kw) { return a_bytes + kw * N
 template <int NP> size_t smem_bytes(int stages, int a_bytes, int kw, int mode)
 {
     return 1024 + (size_t)stages * stage_bytes<NP>(a_bytes, kw) + (2 * stages + 6) * 8 + 16 +
-           (mode == 2 ? 3 : 1) * NP * 4;
+           (mode == 4 ? 7 : (mode == 2 ? 3 : 1)) * NP * 4;
 }
 
 template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
@@ -452,6 +544,7 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     const size_t smem = smem_bytes<NP>(p.stages, p.a_bytes, a.kw, a.mode);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = std::min(p.num_tiles, sms);
+    if (a.bias_splits) *a.bias_splits = 4 * grid;
     {
         CNNCRF_PROF("conv_tc", st);
         k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, p);
@@ -494,6 +587,8 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
     p.aux = (const __nv_bfloat16 *)a.aux, p.out16 = (__nv_bfloat16 *)a.out16;
     p.aux_cs = a.aux_cs, p.o16_cs = a.o16_cs, p.o16_ph = a.o16_ph, p.o16_pw = a.o16_pw;
+    p.bias_part = a.mode == 4 ? a.bias_part : nullptr;
+    if (a.mode != 4 && !a.out) return fail(CNNCRF_EINVAL, "conv_tc: output");
     if (a.mode < 0 || a.mode > 4) return fail(CNNCRF_EINVAL, "conv_tc: mode %d", a.mode);
     if (a.mode == 4 && (!a.aux || !a.out16 || a.aux_cs % 8 || a.aux_cs < a.np || a.o16_cs % 8 ||
                         a.o16_cs < a.np || a.o16_ph < 0 || a.o16_pw < 0 || ((uintptr_t)a.aux & 15) ||

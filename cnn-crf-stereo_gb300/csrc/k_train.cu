@@ -917,6 +917,13 @@ int train_wgrad_head(const float *gh, const void *y, bool bf16, int ys, long P, 
     return CNNCRF_OK;
 }
 
+int train_bias_reduce(const float *part, int nsplit, int Cout, float *db, cudaStream_t st)
+{
+    k_bias_reduce<<<ceil_div(Cout, 32), 256, 0, st>>>(part, nsplit, Cout, db);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st)
 {

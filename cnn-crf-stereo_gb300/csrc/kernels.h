@@ -64,6 +64,10 @@ struct TcConvArgs {
     const void *aux = nullptr;
     void *out16 = nullptr;
     int aux_cs = 0, o16_cs = 0, o16_ph = 0, o16_pw = 0;
+    // mode 4, optional: out (FP32) may be null; bias_part = the per-channel sums of the output, one row
+    // of cout floats per (CTA, epilogue warp), *bias_splits = their number (at most 4 x SMs)
+    float *bias_part = nullptr;
+    int *bias_splits = nullptr;
 };
 int conv_tc(const TcConvArgs &a, cudaStream_t st);
 
@@ -128,6 +132,7 @@ int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pi
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st);
 int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st); // db += sum dz
+int train_bias_reduce(const float *part, int nsplit, int Cout, float *db, cudaStream_t st); // db += sum of rows
 // the 1x1 pairwise head (2 outputs): dw[o][c] += sum_p gh[p][o] y[p][c]; part: train_wgrad_splits(P) x 2C floats
 int train_wgrad_head(const float *gh, const void *y, bool bf16, int ys, long P, int C, float *part, float *dw,
                      cudaStream_t st);

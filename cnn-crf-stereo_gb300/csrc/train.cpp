@@ -32,6 +32,7 @@ struct TLayer {
     DevBuf w16;          // the BF16 mode's tensor-core layout
     DevBuf w16d;         // its input-gradient layout (tensor-core input gradients)
     bool tcw = false;    // the weight gradient on the tensor cores
+    bool dprev = false;  // the backward pass computes this layer's input gradient
     int hout() const { return hin - kh + 1; }
     int wout() const { return win - kw + 1; }
 };
@@ -72,6 +73,10 @@ struct cnncrf_train {
     // fused input gradient writes the layer below's copy while reading its own
     DevBuf dpad[2];
     int dcur = 0;
+    // the per-channel sums of the ready dz (the fused input gradient's epilogue): bsplits rows of scratch
+    DevBuf bpart;
+    int bsplits = 0;
+    bool bias_ready = false;
 
     int build();
     int refresh();
@@ -114,6 +119,7 @@ int cnncrf_train::build()
     pw.clear();
     feat.push_back({ic, F, 3, 3, 1, 0, 1, 0, 0}); // stereo/stereonet.cpp:69-79
     for (int l = 1; l < L; ++l) feat.push_back({F, F, k, k, 1, 2 * l, 2 * l + 1, 0, 0});
+    for (int l = 1; l < L; ++l) feat[l].dprev = true;
     int loss = 0;
     for (auto &Ly : feat) loss += Ly.kh - 1;
     if (loss % 2) return fail(CNNCRF_EINVAL, "train: receptive-field loss %d is odd", loss);
@@ -129,6 +135,7 @@ int cnncrf_train::build()
     pw.push_back({3, P, 3, 3, 1, base, base + 1, H + 4, W + 4});
     pw.push_back({P, P, 3, 3, 1, base + 2, base + 3, H + 2, W + 2});
     pw.push_back({P, 2, 1, 1, 2, base + 4, -1, H, W});
+    pw[1].dprev = true;
     const int np = 2 * L + 5;
     off.assign(np, 0);
     cnt.assign(np, 0);
@@ -252,8 +259,13 @@ int cnncrf_train::build()
             if (Ly.w16d.get() || Ly.tcw)
                 dpad_bytes = std::max(dpad_bytes, 2 * (size_t)n * (Ly.hout() + 2 * (Ly.kh - 1)) *
                                                       (Ly.wout() + 2 * (Ly.kw - 1)) * pad_to(Ly.cout, 64));
-    if (dpad_bytes)
+    if (dpad_bytes) {
         for (auto &b : dpad) CNNCRF_TRY(zalloc(b, dpad_bytes));
+        int dev = 0, sms = 0;
+        CNNCRF_CUDA(cudaGetDevice(&dev));
+        CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CNNCRF_TRY(bpart.reserve(sizeof(float) * 4 * (size_t)sms * 128));
+    }
     const int ns = k::train_wgrad_splits(Pmax); // the most bias splits any layer uses
     CNNCRF_TRY(part.reserve(sizeof(float) * part_floats));
     CNNCRF_TRY(partb.reserve(sizeof(float) * (size_t)ns * 128));
@@ -441,12 +453,17 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
         else
             CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
     }
+    const bool was_ready = ready;
     ready = false;
     if (L.tcw && in_bf16) { // BF16 mode, tensor cores
         CNNCRF_TRY(k::wgrad_tc(dpad[dcur].get(), L.cout, pad_to(L.cout, 64), in, in_pix, in_row, in_img, L.cin, L.kh,
                                L.kw, n, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
-        if (L.bslot >= 0)
-            CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
+        if (L.bslot >= 0) {
+            if (was_ready && bias_ready) // the sums the layer above's fused epilogue left
+                CNNCRF_TRY(k::train_bias_reduce(bpart.as<float>(), bsplits, L.cout, gradp(L.bslot), st));
+            else
+                CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
+        }
     } else {
         CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo,
                                   part.as<float>(), gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr,
@@ -463,14 +480,18 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
         const bool fuse = below && in_bf16 && (below->tcw || below->w16d.get()) && below->hout() == L.hin &&
                           below->wout() == L.win && below->cout == L.cin && in_row == (long)L.win * in_pix &&
                           in_img == (long)L.hin * in_row;
+        bias_ready = false;
         if (fuse) {
             const int bph = below->kh - 1, bpw = below->kw - 1, bcp = pad_to(below->cout, 64);
             CNNCRF_TRY(k::train_zero_border(dpad[dcur ^ 1].get(), n, L.hin, L.win, bcp, bph, bpw, st));
             t.mode = 4, t.aux = in, t.aux_cs = (int)in_pix;
             t.out16 = dpad[dcur ^ 1].get(), t.o16_cs = bcp, t.o16_ph = bph, t.o16_pw = bpw;
+            // the FP32 dz only where a CUDA-core gradient of the layer below reads it
+            if (below->tcw && (!below->dprev || below->w16d.get())) t.out = nullptr;
+            if (below->bslot >= 0 && below->tcw) t.bias_part = bpart.as<float>(), t.bias_splits = &bsplits;
         }
         CNNCRF_TRY(k::conv_tc(t, st));
-        if (fuse) dcur ^= 1, ready = true;
+        if (fuse) dcur ^= 1, ready = true, bias_ready = t.bias_part != nullptr;
         return CNNCRF_OK;
     }
     CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
