@@ -232,6 +232,77 @@ __global__ void k_l2norm_bwd(const T *__restrict__ y, int ys, const float *__res
         dy[px * C + c] = n > 0.0f ? (gp[c] - ld(yp + c) * (dot / ss)) / n : 0.0f;
 }
 
+// The last feature layer's whole output gradient in one pass (BF16 mode):
+//   dy = (df - y <y, df> / |y|^2) / |y|   (the L2 normalisation's adjoint, zero where |y| = 0)
+//   dz = dy (1 - y^2)                     (tanh')
+// written as BF16 into [n][H + 2p][W + 2q][128] inside its border, and the
+// CTA's per-channel sums of dz into part[blockIdx.x][C] (warp sums added in
+// warp order).  A warp per pixel, lane l channels 4l .. 4l + 3, four pixels
+// per warp in flight; C <= 128, C and ys multiples of 4.
+__global__ void __launch_bounds__(256) k_l2norm_tanh_bwd_pad(const __nv_bfloat16 *__restrict__ y, int ys,
+                                                             const float *__restrict__ df, int H, int W, int C,
+                                                             long npx, int p, int q, __nv_bfloat16 *__restrict__ out,
+                                                             float *__restrict__ part)
+{
+    __shared__ float ws[8][128];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c0 = 4 * lane;
+    const long nw = (long)gridDim.x * 8;
+    float bs[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    for (long px0 = (long)blockIdx.x * 8 + w; px0 < npx; px0 += 4 * nw) {
+        float yq[4][4], gq[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { // the loads of four pixels first
+            const long px = px0 + u * nw;
+            uint2 yr = make_uint2(0u, 0u);
+            float4 gr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (px < npx && c0 < C) {
+                yr = *(const uint2 *)(y + px * ys + c0);
+                gr = *(const float4 *)(df + px * C + c0);
+            }
+            yq[u][0] = __uint_as_float(yr.x << 16), yq[u][1] = __uint_as_float(yr.x & 0xffff0000u);
+            yq[u][2] = __uint_as_float(yr.y << 16), yq[u][3] = __uint_as_float(yr.y & 0xffff0000u);
+            gq[u][0] = gr.x, gq[u][1] = gr.y, gq[u][2] = gr.z, gq[u][3] = gr.w;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long px = px0 + u * nw;
+            if (px >= npx) break; // warp-uniform
+            const float *yv = yq[u], *g = gq[u];
+            float ss = 0.0f, dot = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                ss = fmaf(yv[j], yv[j], ss);
+                dot = fmaf(yv[j], g[j], dot);
+            }
+            for (int o = 16; o; o >>= 1) {
+                ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                dot += __shfl_xor_sync(0xffffffffu, dot, o);
+            }
+            const float n = sqrtf(ss);
+            float dz[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const float d = n > 0.0f ? (g[j] - yv[j] * (dot / ss)) / n : 0.0f;
+                dz[j] = d * (1.0f - yv[j] * yv[j]);
+                bs[j] += dz[j];
+            }
+            const long img = px / ((long)H * W), r = px - img * H * W;
+            const int yy = (int)(r / W), x = (int)(r % W);
+            const long o = ((img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 128 + c0;
+            __nv_bfloat162 a = __floats2bfloat162_rn(dz[0], dz[1]), b = __floats2bfloat162_rn(dz[2], dz[3]);
+            *(uint2 *)(out + o) = make_uint2(*(uint32_t *)&a, *(uint32_t *)&b);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) ws[w][c0 + j] = bs[j];
+    __syncthreads();
+    for (int c = threadIdx.x; c < C; c += 256) {
+        float s = ws[0][c];
+        for (int k = 1; k < 8; ++k) s += ws[k][c];
+        part[(long)blockIdx.x * C + c] = s;
+    }
+}
+
 // ------------------------------------------------------------ correlation adjoint
 // Left: dfl[x][c] = -sum_k gvol[x][k] fr[x + s_k][c].  A CTA per (32-pixel
 // tile, row, pair); thread c; the right features of the tile's band in shared memory.
@@ -770,6 +841,29 @@ int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx
             k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const __nv_bfloat16 *)y, ys, df, npx, C, dy);
         else
             k_l2norm_bwd<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const float *)y, ys, df, npx, C, dy);
+    }
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_l2norm_tanh_bwd_pad(const void *y, int ys, const float *df, int nimg, int H, int W, int C, int p, int q,
+                              void *out, float *part, int *nsplit, cudaStream_t st)
+{
+    if (C > 128 || C % 4 || ys % 4 || ((uintptr_t)out & 15) || ((uintptr_t)y & 7) || ((uintptr_t)df & 15))
+        return fail(CNNCRF_EINVAL, "l2norm_tanh_bwd_pad: %d channels / layout", C);
+    int dev = 0, sms = 0;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long npx = (long)nimg * H * W;
+    int per_sm = 1; // one full wave of resident CTAs (at most 4 per SM: the sums' rows)
+    CNNCRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_l2norm_tanh_bwd_pad, 256, 0));
+    const int grid = (int)std::max(1L, std::min((long)std::min(4, std::max(1, per_sm)) * sms, (npx + 7) / 8));
+    *nsplit = grid;
+    CNNCRF_TRY(train_zero_border(out, nimg, H, W, 128, p, q, st));
+    {
+        CNNCRF_PROF("l2norm_bwd", st);
+        k_l2norm_tanh_bwd_pad<<<grid, 256, 0, st>>>((const __nv_bfloat16 *)y, ys, df, H, W, C, npx, p, q,
+                                                    (__nv_bfloat16 *)out, part);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

@@ -112,6 +112,10 @@ int train_head2_bf16(const void *y2, int nimg, int npx, int P, int cs, const flo
 int train_tanh_bwd(float *dy, const void *y, bool bf16, long npx, int C, int ys, cudaStream_t st); // dy *= 1 - y^2
 int train_pad_zero(const float *in, int nimg, int H, int W, int C, int p, int q, float *out, cudaStream_t st);
 int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx, int C, float *dy, cudaStream_t st);
+// BF16 mode, the last feature layer: the L2 normalisation's adjoint times tanh' in one pass, written as BF16
+// [n][H + 2p][W + 2q][128] inside a zeroed border; the per-channel sums in *nsplit rows (at most 4 x SMs) of part
+int train_l2norm_tanh_bwd_pad(const void *y, int ys, const float *df, int nimg, int H, int W, int C, int p, int q,
+                              void *out, float *part, int *nsplit, cudaStream_t st);
 // one-minus-dot unary over an integer stored list (band [omin, omax]): dfl, dfr (dense) from dL/dvol;
 // features at channel stride fs
 int train_corr_bwd(const void *fl, const void *fr, bool bf16, int fs, const float *gvol, const float *d_list,

@@ -517,9 +517,18 @@ int cnncrf_train::backward(const float *gv, const float *gp)
         CNNCRF_TRY(k::train_corr_bwd(fside(0), fside(1), bf16, fs, gv, dlist.as<float>(), n, H, W, F, D, omin,
                                      omax, df[0].as<float>(), df[1].as<float>(), st));
     for (int s = 0; s < 2; ++s) {
-        CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
         float *cur = dy.as<float>(), *nxt = dyb.as<float>();
         bool ready = false;
+        TLayer &top_l = feat[L - 1];
+        if (bf16 && top_l.tcw && top_l.w16d.get() && fs == 128 && top_l.kh == top_l.kw) {
+            // the normalisation's adjoint, tanh', the padded copy and the bias sums in one pass
+            CNNCRF_TRY(k::train_l2norm_tanh_bwd_pad(actp(s, L - 1), fs, df[s].as<float>(), n, H, W, F,
+                                                    top_l.kh - 1, top_l.kw - 1, dpad[dcur].get(), bpart.as<float>(),
+                                                    &bsplits, st));
+            ready = bias_ready = true;
+        } else {
+            CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
+        }
         int top = L - 1;
         while (top >= 0) {
             int c = top - 1; // the checkpoint under this segment (-1: the normalised input)
