@@ -18,8 +18,9 @@
 // while TMA brings
 //   P [64 v][C] BF16 from NHWC: MN-major, a box per 64 channels.
 // Warps: 0 TMA; 1 TMEM allocation + single-thread tcgen05.mma (M = 128,
-// N = NP, K = 16 x 4 per block; A K-major, B MN-major); 2..5 builders (one A
-// row per thread); 6..9 epilogue (TMEM -> -sum -> FP32 NHWC).  Two TMEM
+// N = NP, K = 16 x 4 per block; A K-major, B MN-major); 2..9 builders (two
+// threads per A row, four 16-byte chunks each); 10..13 epilogue (TMEM ->
+// -sum -> FP32 NHWC).  Two TMEM
 // accumulators: the epilogue of tile i overlaps tile i + 1.  Every mbarrier
 // wait is bounded; on timeout the roles raise the abort and error flags,
 // drain and free TMEM.  The offsets of the list must be distinct.
@@ -42,7 +43,8 @@ constexpr int KB = 64;                 // window pixels per K-block
 constexpr int A_BYTES = BM * 128;      // 16 KB
 constexpr int P_BOX = 64 * KB * 2;     // one 64-channel x 64-pixel box: 8 KB
 constexpr int STAGE_BYTES = A_BYTES + 2 * P_BOX;
-constexpr int NUM_THREADS = 320;
+constexpr int NB = 8;                             // builder warps
+constexpr int NUM_THREADS = 32 * (2 + NB + 4);
 constexpr uint32_t TMEM_COLS = 256;    // two accumulators of 128 columns
 constexpr int MAX_STAGES = 6;
 constexpr int MAX_SPAN = 1024;
@@ -87,7 +89,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            tc::mbar_init(&full[s], 1 + 4); // the TMA producer's expect_tx + one arrival per builder warp
+            tc::mbar_init(&full[s], 1 + NB); // the TMA producer's expect_tx + one arrival per builder warp
             tc::mbar_init(&empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -197,9 +199,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::umma_commit(drain);
             tc::mbar_wait(drain, 0, zero_flag, 1u << 22);
         }
-    } else if (warp < 6) {
-        // builders: thread r writes row r (output pixel x0 + r) of every K-block's A
-        const int bw = warp - 2, r = bw * 32 + lane;
+    } else if (warp < 2 + NB) {
+        // builders: threads r and r + 128 write row r (output pixel x0 + r) of every K-block's A,
+        // chunks 0..3 and 4..7
+        const int bw = warp - 2, bt = bw * 32 + lane, r = bt & (BM - 1), jh = (bt >> 7) * 4;
         // A warp whose wait gave up keeps looping without work: the four builder
         // warps pass the named barrier below the same number of times.
         int stage = 0;
@@ -213,15 +216,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             // 1. the gradient rows: left pixels x0 + i, right pixels x0 + omn + i; zero outside the row
             const long rowbase = ((long)pair * p.H + y) * p.W;
             const int g0 = p.right ? x0 + p.omn : x0;
-            asm volatile("bar.sync 1, 128;" ::: "memory"); // the previous tile's reads are done
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * NB) : "memory"); // the previous tile's reads are done
             // 16 rows in flight per warp: lane l holds channels 4l .. 4l + 3 of a 128-wide column chunk
             for (int kc = 0; kc < p.D && ok; kc += 128) {
                 const int k = kc + 4 * lane;
-                for (int i0 = bw; i0 < p.grows; i0 += 64) {
+                for (int i0 = bw; i0 < p.grows; i0 += 16 * NB) {
                     float4 v[16];
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        const int i = i0 + 4 * q, x = g0 + i;
+                        const int i = i0 + NB * q, x = g0 + i;
                         v[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                         if (i < p.grows && x >= 0 && x < p.W && k < p.D) {
                             const float *src = p.g + (rowbase + x) * p.D + k;
@@ -237,14 +240,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
 #pragma unroll
                     for (int q = 0; q < 16; ++q) {
-                        const int i = i0 + 4 * q;
+                        const int i = i0 + NB * q;
                         if (i < p.grows && k < p.D)
                             *(uint2 *)(gs + (long)i * p.gstride + k) =
                                 make_uint2(pack_bf16(v[q].x, v[q].y), pack_bf16(v[q].z, v[q].w));
                     }
                 }
             }
-            asm volatile("bar.sync 1, 128;" ::: "memory");
+            asm volatile("bar.sync 1, %0;" ::"n"(32 * NB) : "memory");
             for (int kb = 0; kb < p.nkb && ok; ++kb) {
                 int got = 1;
                 if (lane == 0) got = tc::mbar_wait(&empty[stage], phase ^ 1, abort_flag) ? 1 : 0;
@@ -255,7 +258,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
                 const uint32_t row = tc::smem_u32(smem + stage * STAGE_BYTES) + r * 128;
 #pragma unroll 1
-                for (int j = 0; j < 8; ++j) {
+                for (int j = jh; j < jh + 4; ++j) {
                     const int i0 = kb * KB + 8 * j - r; // band index of the chunk's first pixel
                     uint32_t w[4] = {0u, 0u, 0u, 0u};
                     if (rowvalid && i0 + 7 >= 0 && i0 < p.span) {
