@@ -648,6 +648,70 @@ __global__ void k_head_bwd(const T *__restrict__ y2, int ys, const float *__rest
     for (int c = 0; c < P; ++c) dy2[q * P + c] = fmaf(wh[c], g0, wh[P + c] * g1);
 }
 
+// The head's adjoint and the second pairwise layer's tanh' in one pass (BF16
+// mode, P <= 64): gh = gpw sign(h), dz = (W^T gh)(1 - y2^2), dz written as
+// BF16 into [n][H + 2p][W + 2q][64] inside its border, gh as FP32 [px][2], and
+// the CTA's per-channel sums of dz into part[blockIdx.x][P].  A warp per pixel,
+// lane l channels 2l, 2l + 1; four pixels per warp in flight.
+__global__ void __launch_bounds__(256) k_head_tanh_bwd_pad(const __nv_bfloat16 *__restrict__ y2, int ys,
+                                                           const float *__restrict__ wh, const float *__restrict__ gpw,
+                                                           int H, int W, int P, long npx, int p, int q,
+                                                           float *__restrict__ gh, __nv_bfloat16 *__restrict__ out,
+                                                           float *__restrict__ part)
+{
+    __shared__ float ws[8][64];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, c0 = 2 * lane;
+    const bool on = c0 < P;
+    const float w00 = on ? wh[c0] : 0.0f, w01 = on && c0 + 1 < P ? wh[c0 + 1] : 0.0f;
+    const float w10 = on ? wh[P + c0] : 0.0f, w11 = on && c0 + 1 < P ? wh[P + c0 + 1] : 0.0f;
+    const long nw = (long)gridDim.x * 8, hw = (long)H * W;
+    float b0 = 0.0f, b1 = 0.0f;
+    for (long px0 = (long)blockIdx.x * 8 + w; px0 < npx; px0 += 4 * nw) {
+        uint32_t yr[4];
+        float a0[4], a1[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) { // the loads of four pixels first
+            const long px = px0 + u * nw;
+            yr[u] = 0u, a0[u] = 0.0f, a1[u] = 0.0f;
+            if (px < npx) {
+                if (on) yr[u] = *(const uint32_t *)(y2 + px * ys + c0);
+                const long img = px / hw, r = px - img * hw;
+                a0[u] = gpw[(img * 2) * hw + r], a1[u] = gpw[(img * 2 + 1) * hw + r];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const long px = px0 + u * nw;
+            if (px >= npx) break; // warp-uniform
+            const float ya = __uint_as_float(yr[u] << 16), yb = __uint_as_float(yr[u] & 0xffff0000u);
+            float h0 = fmaf(w00, ya, w01 * yb), h1 = fmaf(w10, ya, w11 * yb);
+            for (int o = 16; o; o >>= 1) {
+                h0 += __shfl_xor_sync(0xffffffffu, h0, o);
+                h1 += __shfl_xor_sync(0xffffffffu, h1, o);
+            }
+            const float g0 = h0 > 0.0f ? a0[u] : (h0 < 0.0f ? -a0[u] : 0.0f);
+            const float g1 = h1 > 0.0f ? a1[u] : (h1 < 0.0f ? -a1[u] : 0.0f);
+            if (lane == 0) *(float2 *)(gh + px * 2) = make_float2(g0, g1);
+            const float da = fmaf(w00, g0, w10 * g1) * (1.0f - ya * ya);
+            const float db = fmaf(w01, g0, w11 * g1) * (1.0f - yb * yb);
+            b0 += da, b1 += db;
+            const long img = px / hw, r = px - img * hw;
+            const int yy = (int)(r / W), x = (int)(r % W);
+            __nv_bfloat162 d2 = __floats2bfloat162_rn(da, db);
+            if (c0 < 64)
+                *(uint32_t *)(out + ((img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 64 + c0) =
+                    *(uint32_t *)&d2;
+        }
+    }
+    ws[w][c0] = b0, ws[w][c0 + 1] = b1;
+    __syncthreads();
+    for (int c = threadIdx.x; c < P; c += 256) {
+        float s = ws[0][c];
+        for (int k = 1; k < 8; ++k) s += ws[k][c];
+        part[(long)blockIdx.x * P + c] = s;
+    }
+}
+
 // ------------------------------------------------------------ structured hinge
 // aug = vol, + 1 at the ground-truth label (invalid labels: counted in err, left out)
 __global__ void k_augment(const float *__restrict__ vol, const int32_t *__restrict__ gt, long npx, int D,
@@ -1026,6 +1090,25 @@ int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const flo
         k_head_bwd<<<g, 128, 0, st>>>((const __nv_bfloat16 *)y2, ys, wh, gpw, npx, P, gh, dy2);
     else
         k_head_bwd<<<g, 128, 0, st>>>((const float *)y2, ys, wh, gpw, npx, P, gh, dy2);
+    CNNCRF_CHECK_LAUNCH();
+    return CNNCRF_OK;
+}
+
+int train_head_tanh_bwd_pad(const void *y2, int ys, const float *wh, const float *gpw, int nimg, int H, int W, int P,
+                            int p, int q, float *gh, void *out, float *part, int *nsplit, cudaStream_t st)
+{
+    if (P > 64 || P % 2 || ys % 2 || ((uintptr_t)out & 15) || ((uintptr_t)y2 & 3) || ((uintptr_t)gh & 7))
+        return fail(CNNCRF_EINVAL, "head_tanh_bwd_pad: %d channels / layout", P);
+    int dev = 0, sms = 0, per_sm = 1;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    CNNCRF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_head_tanh_bwd_pad, 256, 0));
+    const long npx = (long)nimg * H * W;
+    const int grid = (int)std::max(1L, std::min((long)std::min(4, std::max(1, per_sm)) * sms, (npx + 7) / 8));
+    *nsplit = grid;
+    CNNCRF_TRY(train_zero_border(out, nimg, H, W, 64, p, q, st));
+    k_head_tanh_bwd_pad<<<grid, 256, 0, st>>>((const __nv_bfloat16 *)y2, ys, wh, gpw, H, W, P, npx, p, q, gh,
+                                              (__nv_bfloat16 *)out, part);
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

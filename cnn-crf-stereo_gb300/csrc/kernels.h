@@ -60,7 +60,8 @@ struct TcConvArgs {
     int cp_out;
     int *err; // set to 1 if a bounded wait gave up
     // mode 4: aux = BF16 [n_img][Ho][Wo][aux_cs] (the layer below's output); out16 = BF16
-    // [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs], written inside its border (channels < np)
+    // [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs], written inside its border (channels < np).
+    // mode 1, optional: out16 = the tanh outputs before the normalisation, [n_img][Ho][Wo][o16_cs]
     const void *aux = nullptr;
     void *out16 = nullptr;
     int aux_cs = 0, o16_cs = 0, o16_ph = 0, o16_pw = 0;
@@ -135,6 +136,10 @@ int train_wgrad(const float *dz, int Cout, const void *in, bool bf16, long in_pi
                 int kh, int kw, int nimg, int Ho, int Wo, float *part, float *dw, float *db, float *partb, cudaStream_t st);
 int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const float *gpw, int nimg, int npx, int P,
                    float *gh, float *dy2, cudaStream_t st);
+// BF16 mode, P <= 64: the head's adjoint and the layer below's tanh' in one pass: gh (FP32 [px][2]) and dz as
+// BF16 [n][H + 2p][W + 2q][64] inside a zeroed border; per-channel sums of dz in *nsplit rows of part
+int train_head_tanh_bwd_pad(const void *y2, int ys, const float *wh, const float *gpw, int nimg, int H, int W, int P,
+                            int p, int q, float *gh, void *out, float *part, int *nsplit, cudaStream_t st);
 int train_bias_grad(const float *dz, int Cout, long P, float *partb, float *db, cudaStream_t st); // db += sum dz
 int train_bias_reduce(const float *part, int nsplit, int Cout, float *db, cudaStream_t st); // db += sum of rows
 // the 1x1 pairwise head (2 outputs): dw[o][c] += sum_p gh[p][o] y[p][c]; part: train_wgrad_splits(P) x 2C floats

@@ -326,6 +326,10 @@ int cnncrf_train::run_layer(int s, int l)
     t.mode = 0; // tanh -> BF16: the pre-normalisation features stay for the backward
     t.out = out;
     t.cp_out = cp_feat;
+    if (l == (int)feat.size() - 1) { // the last layer also writes the L2-normalised features
+        t.mode = 1, t.out = fside(s);
+        t.out16 = out, t.o16_cs = cp_feat;
+    }
     t.err = tcerr.as<int>();
     return k::conv_tc(t, st);
 }
@@ -340,7 +344,7 @@ int cnncrf_train::forward(const float *l, const float *r)
         if (norm16[s].get()) CNNCRF_TRY(k::train_to_bf16_c64(norm[s].as<float>(), (long)n * h * w, ic, norm16[s].get(), st));
         for (int li = 0; li < L; ++li) CNNCRF_TRY(run_layer(s, li));
         if (bf16) {
-            CNNCRF_TRY(k::train_l2norm_bf16(actp(s, L - 1), (long)n * H * W, F, cp_feat, fside(s), st));
+            // the last layer's epilogue (run_layer) wrote the normalised features
         } else {
             const size_t fb = sizeof(float) * (size_t)n * H * W * F;
             CNNCRF_CUDA(cudaMemcpyAsync(fside(s), actp(s, L - 1), fb, cudaMemcpyDeviceToDevice, st));
@@ -550,11 +554,19 @@ int cnncrf_train::backward(const float *gv, const float *gp)
     }
     if (gp) {
         // head: gh = gpw sign(h), dy2 = W^T gh; its weight gradient is a 1x1 wgrad on y2
-        CNNCRF_TRY(k::train_head_bwd(y2.get(), bf16, ps, param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
-                                     dy.as<float>(), st));
+        bool ready = false;
+        if (bf16 && pw[1].tcw && pw[1].w16d.get() && ps == 64 && P <= 64) {
+            // with the second pairwise layer's tanh', padded copy and bias sums
+            CNNCRF_TRY(k::train_head_tanh_bwd_pad(y2.get(), ps, param(pw[2].wslot), gp, n, H, W, P, pw[1].kh - 1,
+                                                  pw[1].kw - 1, gh.as<float>(), dpad[dcur].get(), bpart.as<float>(),
+                                                  &bsplits, st));
+            ready = bias_ready = true;
+        } else {
+            CNNCRF_TRY(k::train_head_bwd(y2.get(), bf16, ps, param(pw[2].wslot), gp, n, H * W, P, gh.as<float>(),
+                                         dy.as<float>(), st));
+        }
         CNNCRF_TRY(k::train_wgrad_head(gh.as<float>(), y2.get(), bf16, ps, (long)n * H * W, P, partb.as<float>(),
                                        gradp(pw[2].wslot), st));
-        bool ready = false;
         CNNCRF_TRY(layer_back(pw[1], y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
                               ps, dy.as<float>(), dyb.as<float>(), ready, &pw[0]));
         const int cr = p - 2;
