@@ -175,6 +175,7 @@ PROTOS = {
     "cnncrf_train_outputs": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32)], i32),
     "cnncrf_train_hinge": ([vp, vp, C.POINTER(C.c_double), vp], i32),
     "cnncrf_train_hinge_grads": ([vp, C.POINTER(vp), C.POINTER(vp)], i32),
+    "cnncrf_train_autotune": ([vp], i32),
     "cnncrf_train_backward": ([vp, vp, vp], i32),
     "cnncrf_train_sgd": ([vp, f32, f32], i32),
     "cnncrf_train_step": ([vp, vp, vp, vp, f32, f32, C.POINTER(C.c_double)], i32),

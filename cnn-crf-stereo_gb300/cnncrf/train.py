@@ -121,6 +121,11 @@ class Trainer:
         call("cnncrf_train_hinge", self._h, _ptr(gt), loss, _ptr(yh))
         return np.array(loss[:], np.float64), yh
 
+    def autotune(self):
+        """After a forward: time the CRF tiles on the hinge's problem and enter the fastest in the
+        process-wide tile table (no bit changes; synchronises)."""
+        call("cnncrf_train_autotune", self._h)
+
     def hinge_grads(self):
         """Copies of the last hinge's subgradients (volume, pairwise output)."""
         v, p = C.c_void_p(), C.c_void_p()

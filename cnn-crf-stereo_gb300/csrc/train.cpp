@@ -757,6 +757,21 @@ int cnncrf_train_hinge(cnncrf_train_t t, const int32_t *d_gt, double *h_loss, in
     return t->hinge(d_gt, h_loss, d_labels);
 }
 
+int cnncrf_train_autotune(cnncrf_train_t t)
+{
+    clear_error();
+    if (!t) return fail(CNNCRF_EINVAL, "null train");
+    if (!t->forwarded) return fail(CNNCRF_ESTATE, "train: autotune before forward");
+    const long N = (long)t->n * t->H * t->W, img = (long)t->H * t->W;
+    // the hinge's problem: the unary and lambda times the pairwise output, all crops in one solve
+    CNNCRF_CUDA(cudaMemcpyAsync(t->wts.get(), t->pwout.get(), sizeof(float) * N * 2, cudaMemcpyDeviceToDevice, t->st));
+    CNNCRF_TRY(k::scale(t->wts.as<float>(), N * 2, t->d.lambda, t->st));
+    k::CrfParams cp;
+    cp.L1 = t->d.L1, cp.L2 = t->d.L2, cp.delta = t->d.delta, cp.shape = t->d.crf_shape, cp.slack = t->d.crf_slack;
+    return k::crf_autotune(t->vol.as<float>(), t->wts.as<float>(), t->wts.as<float>() + img, 2 * img, t->W, t->H,
+                           t->D, t->n, cp, t->crfws.get(), t->crfws_bytes, t->st, true);
+}
+
 int cnncrf_train_hinge_grads(cnncrf_train_t t, const float **d_gvol, const float **d_gpw)
 {
     if (!t) return fail(CNNCRF_EINVAL, "null train");

@@ -388,6 +388,10 @@ int cnncrf_train_hinge(cnncrf_train_t t, const int32_t *d_gt, double *h_loss, in
 /* the hinge's subgradient buffers ([npairs][H][W][D] and [npairs][2][H][W])
  * of the last cnncrf_train_hinge, valid until the next forward */
 int cnncrf_train_hinge_grads(cnncrf_train_t t, const float **d_gvol, const float **d_gpw);
+/* After a forward: measures the CRF tiles on the hinge's problem (the unary and the weighted pairwise output,
+ * all npairs crops in one solve) and enters the fastest per pass in the process-wide tile table, where every
+ * later hinge of this shape finds it.  Tiles change no bit.  Synchronises the stream. */
+int cnncrf_train_autotune(cnncrf_train_t t);
 /* parameter gradients of sum(gvol * vol) + sum(gpw * pw) (gpw may be NULL:
  * the pairwise net gets none), or of the hinge loss when both are NULL */
 int cnncrf_train_backward(cnncrf_train_t t, const float *d_gvol, const float *d_gpw);

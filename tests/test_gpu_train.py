@@ -406,3 +406,31 @@ def test_tensor_core_correlation_adjoint(cuda, oracle, dmin, dstep, dmax, W):
         errs[i] = np.abs(a - b).max() / max(np.abs(b).max(), 1e-12)
     print("tensor-core vs CUDA-core correlation adjoint:", {k: float("%.2e" % v) for k, v in errs.items()})
     assert max(errs.values()) < 1e-2, errs
+
+
+def test_autotune_changes_no_bit(cuda, oracle):
+    """cnncrf_train_autotune enters the hinge problem's CRF tile in the
+    process-wide table; a step after it gives the same losses, labelling and
+    gradients as a step of an identical trainer before it."""
+    torch = cuda
+    from cnncrf import _lib as L
+    from cnncrf import tuning
+    tuning.clear()
+    kw = dict(n=2, W=150, H=37, D=24, F=16, P=16, precision=L.BF16, checkpoint_every=2)
+    _, params, t0, left, right, _, gt, _ = setup(oracle, **kw)
+    t1 = setup(oracle, **kw)[2]
+    gt = torch.from_numpy(gt).cuda()
+    t0.forward(left, right)
+    l0, y0 = t0.hinge(gt)
+    t0.backward()
+    assert tuning.count() == 0
+    t1.forward(left, right)
+    t1.autotune()
+    assert tuning.count() == 1
+    t1.forward(left, right)
+    l1, y1 = t1.hinge(gt)
+    t1.backward()
+    assert np.array_equal(l0, l1) and torch.equal(y0, y1)
+    for i in range(len(params)):
+        assert np.array_equal(t0.get_grad(i), t1.get_grad(i)), i
+    tuning.clear()
