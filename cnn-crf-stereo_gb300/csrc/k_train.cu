@@ -80,20 +80,6 @@ __global__ void k_w16_dgrad(const float *__restrict__ w, int Cout, int Cin, int 
     w16d[i] = __float2bfloat16_rn(v);
 }
 
-// BF16 L2 normalisation: f = y / |y| per pixel in FP32, rounded once; a warp per pixel
-__global__ void k_l2norm_bf16(const __nv_bfloat16 *__restrict__ y, long npx, int C, int cs,
-                              __nv_bfloat16 *__restrict__ f)
-{
-    const long px = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (px >= npx) return;
-    const __nv_bfloat16 *yp = y + px * cs;
-    float ss = 0.0f;
-    for (int c = lane; c < C; c += 32) ss = fmaf(ld(yp + c), ld(yp + c), ss);
-    for (int o = 16; o; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
-    const float n = sqrtf(ss);
-    for (int c = lane; c < C; c += 32) f[px * cs + c] = __float2bfloat16_rn(n > 0.0f ? ld(yp + c) / n : 0.0f);
-}
 
 // pw = |h|, h[o] = sum_c wh[o][c] y2[c] on BF16 y2 (channel stride cs): [img][2][npx]
 __global__ void k_head2_bf16(const __nv_bfloat16 *__restrict__ y2, int npx, int P, int cs, const float *__restrict__ wh,
@@ -851,17 +837,6 @@ int train_zero_border(void *buf, int nimg, int H, int W, int cp, int p, int q, c
     const long total = (long)nimg * per_img * (cp / 8);
     if (total == 0) return CNNCRF_OK;
     k_zero_border<<<ceil_div(total, 256), 256, 0, st>>>((__nv_bfloat16 *)buf, H, W, cp, p, q, per_img, total);
-    CNNCRF_CHECK_LAUNCH();
-    return CNNCRF_OK;
-}
-
-int train_l2norm_bf16(const void *y, long npx, int C, int cs, void *f, cudaStream_t st)
-{
-    {
-        CNNCRF_PROF("l2norm", st);
-        k_l2norm_bf16<<<ceil_div(npx * 32, 256), 256, 0, st>>>((const __nv_bfloat16 *)y, npx, C, cs,
-                                                                (__nv_bfloat16 *)f);
-    }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }

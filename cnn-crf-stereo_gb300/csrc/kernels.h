@@ -98,7 +98,7 @@ int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, co
 // gradient's wd [kh*kw*Cout][128] (if wd), bias padded to 128 (if b and b128)
 int train_weight_layouts(const float *w, const float *b, int Cout, int Cin, int kh, int kw, float *wt, float *wd,
                          float *b128, cudaStream_t st);
-// the BF16 mode's tensor-core weight layout [np][kh*kw][cp], its L2 normalisation and |1x1| head
+// the BF16 mode's tensor-core weight layout [np][kh*kw][cp] and its |1x1| head
 int train_w16(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16, cudaStream_t st);
 // the input gradient's tensor-core layout [np][kh*kw][cp]: w16d[ci][tap][co] = w[co][ci][ky][kx], unflipped
 int train_w16_dgrad(const float *w, int Cout, int Cin, int kh, int kw, int np, int cp, void *w16d, cudaStream_t st);
@@ -107,7 +107,6 @@ int train_zero_border(void *buf, int nimg, int H, int W, int cp, int p, int q, c
 // dy *= 1 - y^2 (y BF16) and a BF16 copy with a (p, q) zero border and channels padded to cp (conv_tc's input)
 int train_tanh_bwd_pad(float *dy, const void *y, int nimg, int H, int W, int C, int ys, int p, int q, int cp,
                        void *out, cudaStream_t st);
-int train_l2norm_bf16(const void *y, long npx, int C, int cs, void *f, cudaStream_t st);
 int train_head2_bf16(const void *y2, int nimg, int npx, int P, int cs, const float *wh, float *out, cudaStream_t st);
 // Activations y are FP32 or BF16 (bf16) at channel stride ys; gradients are dense FP32 [px][C].
 int train_tanh_bwd(float *dy, const void *y, bool bf16, long npx, int C, int ys, cudaStream_t st); // dy *= 1 - y^2
