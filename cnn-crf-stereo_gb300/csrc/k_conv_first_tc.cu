@@ -11,10 +11,11 @@
 // layout (16-byte chunk c of row r at chunk c ^ (r & 7)).  The weights are
 // converted once per CTA into a resident B tile of the same layout.  A tile
 // is 128 consecutive output pixels of one row: ceil(K / 16) UMMA K-steps
-// (M = 128, N = NP) into one of two TMEM accumulators, so the epilogue of
-// tile i (tcgen05.ld, bias, tanh, BF16 NHWC store) overlaps the MMA of tile
-// i + 1.  128 threads; every mbarrier wait is bounded and reports through
-// the error flag.
+// (M = 128, N = NP) into the CTA's one 128-column TMEM accumulator, then the
+// epilogue (tcgen05.ld, bias, tanh, BF16 NHWC store).  The steps of a tile
+// run in order; four CTAs per SM (4 x 128 TMEM columns) hide each other's
+// gather and store latency.  128 threads; every mbarrier wait is bounded and
+// reports through the error flag.
 #include <cuda_bf16.h>
 
 #include "common.h"
@@ -30,8 +31,8 @@ constexpr int BM = 128;
 constexpr int ROW = 128;           // bytes per swizzled row (64 bf16)
 constexpr int A_BYTES = BM * ROW;  // 16 KB
 constexpr int NUM_THREADS = 128;
-constexpr uint32_t TMEM_COLS = 256;
-constexpr uint32_t ACC_STRIDE = 128;
+constexpr uint32_t TMEM_COLS = 128; // one accumulator (N <= 128)
+constexpr int CTAS_PER_SM = 4;      // 4 x 128 TMEM columns
 constexpr int WT_LD = 128;         // row stride of the FP32 filter matrix [K][128]
 
 struct FirstParams {
@@ -62,10 +63,10 @@ __global__ void __launch_bounds__(NUM_THREADS)
     constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint8_t *sA = smem;                   // [2][128 rows][128 B]
-    uint8_t *sB = smem + 2 * A_BYTES;     // [NP rows][128 B]
+    uint8_t *sA = smem;                   // [128 rows][128 B]
+    uint8_t *sB = smem + A_BYTES;         // [NP rows][128 B]
     float *sbias = (float *)(sB + NP * ROW);
-    uint64_t *done = (uint64_t *)(sbias + NP);
+    uint64_t *done = (uint64_t *)(sbias + NP); // [1]: the tile's MMAs
     uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
@@ -87,7 +88,6 @@ __global__ void __launch_bounds__(NUM_THREADS)
     for (int i = tid; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
     if (tid == 0) {
         tc::mbar_init(&done[0], 1);
-        tc::mbar_init(&done[1], 1);
         *abort_flag = 0;
         tc::mbar_fence_init();
     }
@@ -102,10 +102,10 @@ __global__ void __launch_bounds__(NUM_THREADS)
     const int tiles_per_img = p.Ho * p.tiles_x;
 
     // epilogue of a finished tile: thread = pixel 32 * warp + lane (its TMEM lane)
-    auto epilogue = [&](int t, int buf) {
+    auto epilogue = [&](int t) {
         const int img = t / tiles_per_img, r = t - img * tiles_per_img;
         const int y = r / p.tiles_x, x = (r - y * p.tiles_x) * BM + tid;
-        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16) + buf * ACC_STRIDE;
+        const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
         __nv_bfloat16 *o16 = p.out + img * p.out_img + ((long)y * p.Wo + x) * p.cp_out;
         float v[16];
 #pragma unroll 1
@@ -124,16 +124,16 @@ __global__ void __launch_bounds__(NUM_THREADS)
         }
     };
 
-    int it = 0, prev = -1;
+    int it = 0;
     bool ok = true;
     for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++it) {
-        const int buf = it & 1;
-        // 1. this thread's A row: the patch of output pixel x0 + tid, BF16
+        // 1. this thread's A row: the patch of output pixel x0 + tid, BF16 (the previous tile's MMA,
+        //    waited for below, has read the tile)
         {
             const int img = t / tiles_per_img, r = t - img * tiles_per_img;
             const int y = r / p.tiles_x, x = (r - y * p.tiles_x) * BM + tid;
             const float *src = p.in + img * p.in_img + (long)y * p.in_row + (long)x * p.in_pix;
-            const uint32_t row = tc::smem_u32(sA + buf * A_BYTES + tid * ROW);
+            const uint32_t row = tc::smem_u32(sA + tid * ROW);
             for (int c = 0; c < nchunk; ++c) {
                 uint32_t w[4];
 #pragma unroll
@@ -154,43 +154,28 @@ __global__ void __launch_bounds__(NUM_THREADS)
                 st_shared_v4(row + ((c ^ (tid & 7)) << 4), w[0], w[1], w[2], w[3]);
             }
         }
-        // 2. the tensor core reads A through the async proxy
+        // 2. the tensor core reads A through the async proxy; the previous epilogue's TMEM reads are done
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc::fence_before_sync();
         __syncthreads();
         // 3. MMAs of this tile
         if (tid == 0) {
             tc::fence_after_sync();
-            const uint64_t da = tc::sdesc_sw128(tc::smem_u32(sA + buf * A_BYTES));
+            const uint64_t da = tc::sdesc_sw128(tc::smem_u32(sA));
             const uint64_t db = tc::sdesc_sw128(tc::smem_u32(sB));
             for (int kk = 0; kk < p.nk; ++kk)
-                tc::umma_bf16(tmem + buf * ACC_STRIDE, da + 2 * kk, db + 2 * kk, IDESC, kk > 0 ? 1u : 0u);
-            tc::umma_commit(&done[buf]);
+                tc::umma_bf16(tmem, da + 2 * kk, db + 2 * kk, IDESC, kk > 0 ? 1u : 0u);
+            tc::umma_commit(&done[0]);
         }
-        // 4. epilogue of the previous tile while this one multiplies; the
-        //    outcome of the bounded wait is made uniform over the CTA
-        if (prev >= 0) {
-            const int pb = buf ^ 1;
-            const int got = tc::mbar_wait(&done[pb], ((uint32_t)(it - 1) >> 1) & 1u, abort_flag) ? 1 : 0;
-            if (!__syncthreads_and(got)) {
-                ok = false;
-                break;
-            }
-            tc::fence_after_sync();
-            epilogue(prev, pb);
-            tc::fence_before_sync();
-        }
-        prev = t;
-    }
-    if (ok && prev >= 0) {
-        const int pb = (it - 1) & 1;
-        const int got = tc::mbar_wait(&done[pb], ((uint32_t)(it - 1) >> 1) & 1u, abort_flag) ? 1 : 0;
-        if (__syncthreads_and(got)) {
-            tc::fence_after_sync();
-            epilogue(prev, pb);
-        } else {
+        // 4. its epilogue; the outcome of the bounded wait is made uniform over the CTA
+        const int got = tc::mbar_wait(&done[0], (uint32_t)it & 1u, abort_flag) ? 1 : 0;
+        if (!__syncthreads_and(got)) {
             ok = false;
+            break;
         }
+        tc::fence_after_sync();
+        epilogue(t);
+        tc::fence_before_sync();
     }
     if (!ok && tid == 0) atomicExch(p.err, 1);
     tc::fence_before_sync();
@@ -201,17 +186,18 @@ __global__ void __launch_bounds__(NUM_THREADS)
     }
 }
 
-template <int NP> size_t smem_bytes() { return 1024 + 2 * A_BYTES + NP * ROW + NP * 4 + 2 * 8 + 16; }
+template <int NP> size_t smem_bytes() { return 1024 + A_BYTES + NP * ROW + NP * 4 + 2 * 8 + 16; }
 
 template <int NP> int launch(const FirstParams &p, cudaStream_t st)
 {
     int dev = 0, sms = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    // at most two CTAs per SM: their accumulators fill the SM's 512 TMEM columns
-    const size_t smem = std::max(smem_bytes<NP>(), (size_t)80 * 1024);
+    // at most CTAS_PER_SM CTAs per SM (through shared memory): their accumulators fill the SM's 512 TMEM
+    // columns, so no CTA waits in its allocation
+    const size_t smem = std::max(smem_bytes<NP>(), (size_t)(200 * 1024 / CTAS_PER_SM));
     CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_first_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = std::min(p.num_tiles, 2 * sms);
+    const int grid = std::min(p.num_tiles, CTAS_PER_SM * sms);
     {
         CNNCRF_PROF("conv_first_tc", st);
         k_conv_first_tc<NP><<<grid, NUM_THREADS, smem, st>>>(p);
