@@ -264,17 +264,18 @@ __global__ void __launch_bounds__(256) k_l2norm_tanh_bwd_pad(const __nv_bfloat16
                 ss += __shfl_xor_sync(0xffffffffu, ss, o);
                 dot += __shfl_xor_sync(0xffffffffu, dot, o);
             }
-            const float n = sqrtf(ss);
+            const float n = sqrtf(ss), s = dot / ss, rn = 1.0f / n;
             float dz[4];
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const float d = n > 0.0f ? (g[j] - yv[j] * (dot / ss)) / n : 0.0f;
+                const float d = n > 0.0f ? (g[j] - yv[j] * s) * rn : 0.0f;
                 dz[j] = d * (1.0f - yv[j] * yv[j]);
                 bs[j] += dz[j];
             }
-            const long img = px / ((long)H * W), r = px - img * H * W;
-            const int yy = (int)(r / W), x = (int)(r % W);
-            const long o = ((img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 128 + c0;
+            // 32-bit index arithmetic (npx < 2^31): 64-bit division is a long software sequence
+            const unsigned pu = (unsigned)px, hw = (unsigned)H * W;
+            const unsigned img = pu / hw, r = pu - img * hw, yy = r / W, x = r - yy * W;
+            const long o = (((long)img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 128 + c0;
             __nv_bfloat162 a = __floats2bfloat162_rn(dz[0], dz[1]), b = __floats2bfloat162_rn(dz[2], dz[3]);
             *(uint2 *)(out + o) = make_uint2(*(uint32_t *)&a, *(uint32_t *)&b);
         }
@@ -661,8 +662,8 @@ __global__ void __launch_bounds__(256) k_head_tanh_bwd_pad(const __nv_bfloat16 *
             yr[u] = 0u, a0[u] = 0.0f, a1[u] = 0.0f;
             if (px < npx) {
                 if (on) yr[u] = *(const uint32_t *)(y2 + px * ys + c0);
-                const long img = px / hw, r = px - img * hw;
-                a0[u] = gpw[(img * 2) * hw + r], a1[u] = gpw[(img * 2 + 1) * hw + r];
+                const unsigned img = (unsigned)px / (unsigned)hw, r = (unsigned)px - img * (unsigned)hw;
+                a0[u] = gpw[(long)(img * 2) * hw + r], a1[u] = gpw[(long)(img * 2 + 1) * hw + r];
             }
         }
 #pragma unroll
@@ -681,11 +682,11 @@ __global__ void __launch_bounds__(256) k_head_tanh_bwd_pad(const __nv_bfloat16 *
             const float da = fmaf(w00, g0, w10 * g1) * (1.0f - ya * ya);
             const float db = fmaf(w01, g0, w11 * g1) * (1.0f - yb * yb);
             b0 += da, b1 += db;
-            const long img = px / hw, r = px - img * hw;
-            const int yy = (int)(r / W), x = (int)(r % W);
+            const unsigned img = (unsigned)px / (unsigned)hw, r = (unsigned)px - img * (unsigned)hw;
+            const unsigned yy = r / W, x = r - yy * W;
             __nv_bfloat162 d2 = __floats2bfloat162_rn(da, db);
             if (c0 < 64)
-                *(uint32_t *)(out + ((img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 64 + c0) =
+                *(uint32_t *)(out + (((long)img * (H + 2 * p) + yy + p) * (W + 2 * q) + x + q) * 64 + c0) =
                     *(uint32_t *)&d2;
         }
     }
@@ -888,7 +889,8 @@ int train_l2norm_bwd(const void *y, bool bf16, int ys, const float *df, long npx
 int train_l2norm_tanh_bwd_pad(const void *y, int ys, const float *df, int nimg, int H, int W, int C, int p, int q,
                               void *out, float *part, int *nsplit, cudaStream_t st)
 {
-    if (C > 128 || C % 4 || ys % 4 || ((uintptr_t)out & 15) || ((uintptr_t)y & 7) || ((uintptr_t)df & 15))
+    if (C > 128 || C % 4 || ys % 4 || ((uintptr_t)out & 15) || ((uintptr_t)y & 7) || ((uintptr_t)df & 15) ||
+        (long)nimg * H * W >= (1L << 31))
         return fail(CNNCRF_EINVAL, "l2norm_tanh_bwd_pad: %d channels / layout", C);
     int dev = 0, sms = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
@@ -1072,7 +1074,8 @@ int train_head_bwd(const void *y2, bool bf16, int ys, const float *wh, const flo
 int train_head_tanh_bwd_pad(const void *y2, int ys, const float *wh, const float *gpw, int nimg, int H, int W, int P,
                             int p, int q, float *gh, void *out, float *part, int *nsplit, cudaStream_t st)
 {
-    if (P > 64 || P % 2 || ys % 2 || ((uintptr_t)out & 15) || ((uintptr_t)y2 & 3) || ((uintptr_t)gh & 7))
+    if (P > 64 || P % 2 || ys % 2 || ((uintptr_t)out & 15) || ((uintptr_t)y2 & 3) || ((uintptr_t)gh & 7) ||
+        (long)nimg * H * W >= (1L << 31))
         return fail(CNNCRF_EINVAL, "head_tanh_bwd_pad: %d channels / layout", P);
     int dev = 0, sms = 0, per_sm = 1;
     CNNCRF_CUDA(cudaGetDevice(&dev));
