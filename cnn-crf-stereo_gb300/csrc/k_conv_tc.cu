@@ -456,6 +456,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                             a0 = fmaf(v[j], shead[c * 16 + j], a0);
                             a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
                         }
+                        if (p.out16 && valid) { // the tanh outputs too (a training step's backward reads them)
+                            uint32_t u[8];
+#pragma unroll
+                            for (int j = 0; j < 8; ++j) {
+                                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                                u[j] = *(uint32_t *)&b2;
+                            }
+                            uint4 *d2 = (uint4 *)(p.out16 + pix * p.o16_cs + c * 16);
+                            d2[0] = make_uint4(u[0], u[1], u[2], u[3]);
+                            d2[1] = make_uint4(u[4], u[5], u[6], u[7]);
+                        }
                     } else if (valid) {
                         uint32_t u[8];
 #pragma unroll
@@ -595,7 +606,7 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
     }
     p.mode = a.mode;
     p.bias = a.bias, p.head = a.head, p.out = a.out, p.err = a.err;
-    p.aux = (const __nv_bfloat16 *)a.aux, p.out16 = (a.mode == 1 || a.mode == 4) ? (__nv_bfloat16 *)a.out16 : nullptr;
+    p.aux = (const __nv_bfloat16 *)a.aux, p.out16 = a.mode >= 1 ? (__nv_bfloat16 *)a.out16 : nullptr;
     p.aux_cs = a.aux_cs, p.o16_cs = a.o16_cs, p.o16_ph = a.o16_ph, p.o16_pw = a.o16_pw;
     p.bias_part = a.mode == 4 ? a.bias_part : nullptr;
     if (a.mode != 4 && !a.out) return fail(CNNCRF_EINVAL, "conv_tc: output");
@@ -604,8 +615,9 @@ int conv_tc(const TcConvArgs &a, cudaStream_t st)
                         a.o16_cs < a.np || a.o16_ph < 0 || a.o16_pw < 0 || ((uintptr_t)a.aux & 15) ||
                         ((uintptr_t)a.out16 & 15)))
         return fail(CNNCRF_EINVAL, "conv_tc: mode 4 operands");
-    if (a.mode == 1 && a.out16 && (a.o16_cs % 8 || a.o16_cs < a.np || a.o16_ph || a.o16_pw || ((uintptr_t)a.out16 & 15)))
-        return fail(CNNCRF_EINVAL, "conv_tc: mode 1 second output");
+    if ((a.mode == 1 || a.mode == 2) && a.out16 &&
+        (a.o16_cs % 8 || a.o16_cs < a.np || a.o16_ph || a.o16_pw || ((uintptr_t)a.out16 & 15)))
+        return fail(CNNCRF_EINVAL, "conv_tc: mode %d second output", a.mode);
     // BF16 outputs store whole 16-channel groups; FP32 input gradients float4 groups below cout
     const bool bf16_out = a.mode == 0 || a.mode == 1;
     if (bf16_out && a.cp_out % 8 != 0) return fail(CNNCRF_EINVAL, "conv_tc: cp_out %d", a.cp_out);

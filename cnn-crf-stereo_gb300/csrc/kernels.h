@@ -61,7 +61,8 @@ struct TcConvArgs {
     int *err; // set to 1 if a bounded wait gave up
     // mode 4: aux = BF16 [n_img][Ho][Wo][aux_cs] (the layer below's output); out16 = BF16
     // [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs], written inside its border (channels < np).
-    // mode 1, optional: out16 = the tanh outputs before the normalisation, [n_img][Ho][Wo][o16_cs]
+    // modes 1 and 2, optional: out16 = the tanh outputs (before the normalisation / the head),
+    // [n_img][Ho][Wo][o16_cs]
     const void *aux = nullptr;
     void *out16 = nullptr;
     int aux_cs = 0, o16_cs = 0, o16_ph = 0, o16_pw = 0;

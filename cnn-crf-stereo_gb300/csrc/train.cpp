@@ -382,12 +382,16 @@ int cnncrf_train::forward(const float *l, const float *r)
         t.wt = pw[1].w16.get();
         t.np = np_pw, t.cout = P, t.kh = 3, t.kw = 3;
         t.bias = pw[1].b128.as<float>();
-        t.mode = 0;
-        t.out = y2.get();
-        t.cp_out = cp_pw;
         t.err = tcerr.as<int>();
-        CNNCRF_TRY(k::conv_tc(t, st));
-        CNNCRF_TRY(k::train_head2_bf16(y2.get(), n, H * W, P, cp_pw, param(pw[2].wslot), pwout.as<float>(), st));
+        if (np_pw == P) { // the head and |.| in the epilogue ([2][P] weights = [2][NP]), y2 beside it
+            t.mode = 2, t.head = param(pw[2].wslot), t.out = pwout.get(), t.cp_out = 0;
+            t.out16 = y2.get(), t.o16_cs = cp_pw;
+            CNNCRF_TRY(k::conv_tc(t, st));
+        } else {
+            t.mode = 0, t.out = y2.get(), t.cp_out = cp_pw;
+            CNNCRF_TRY(k::conv_tc(t, st));
+            CNNCRF_TRY(k::train_head2_bf16(y2.get(), n, H * W, P, cp_pw, param(pw[2].wslot), pwout.as<float>(), st));
+        }
     }
     forwarded = true;
     hinged = false;
