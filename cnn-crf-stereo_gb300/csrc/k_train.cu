@@ -701,15 +701,30 @@ __global__ void __launch_bounds__(256) k_head_tanh_bwd_pad(const __nv_bfloat16 *
 
 // ------------------------------------------------------------ structured hinge
 // aug = vol, + 1 at the ground-truth label (invalid labels: counted in err, left out)
+// a warp per pixel (grid-stride), lane l the labels 4l + 128 j: no index division
 __global__ void k_augment(const float *__restrict__ vol, const int32_t *__restrict__ gt, long npx, int D,
                           float *__restrict__ aug, int *__restrict__ err)
 {
-    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= npx * D) return;
-    const long px = i / D;
-    const int k = (int)(i % D), g = gt[px];
-    if (k == 0 && (g < 0 || g >= D)) atomicAdd(err, 1);
-    aug[i] = k == g ? vol[i] + 1.0f : vol[i];
+    const int lane = threadIdx.x & 31;
+    const long nw = ((long)gridDim.x * blockDim.x) >> 5;
+    for (long px = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; px < npx; px += nw) {
+        const int g = gt[px];
+        if (lane == 0 && (g < 0 || g >= D)) atomicAdd(err, 1);
+        const float *v = vol + px * D;
+        float *a = aug + px * D;
+        if ((D & 3) == 0) {
+            for (int k = 4 * lane; k < D; k += 128) {
+                float4 x = *(const float4 *)(v + k);
+                x.x = g == k ? x.x + 1.0f : x.x;
+                x.y = g == k + 1 ? x.y + 1.0f : x.y;
+                x.z = g == k + 2 ? x.z + 1.0f : x.z;
+                x.w = g == k + 3 ? x.w + 1.0f : x.w;
+                *(float4 *)(a + k) = x;
+            }
+        } else {
+            for (int k = lane; k < D; k += 32) a[k] = k == g ? v[k] + 1.0f : v[k];
+        }
+    }
 }
 
 __device__ __forceinline__ float rho_of(const float *rho, int delta, float L2, int t)
@@ -1093,7 +1108,11 @@ int train_head_tanh_bwd_pad(const void *y2, int ys, const float *wh, const float
 
 int train_augment(const float *vol, const int32_t *gt, long npx, int D, float *aug, int *err, cudaStream_t st)
 {
-    k_augment<<<ceil_div(npx * D, 256), 256, 0, st>>>(vol, gt, npx, D, aug, err);
+    if (((uintptr_t)vol & 15) || ((uintptr_t)aug & 15)) return fail(CNNCRF_EINVAL, "augment: alignment");
+    int dev = 0, sms = 0;
+    CNNCRF_CUDA(cudaGetDevice(&dev));
+    CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    k_augment<<<(int)std::min((npx + 7) / 8, (long)8 * sms), 256, 0, st>>>(vol, gt, npx, D, aug, err);
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
