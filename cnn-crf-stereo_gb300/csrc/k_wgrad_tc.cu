@@ -64,6 +64,20 @@ struct WgTcParams {
     int *err;
 };
 
+// One stage's MMAs, fully unrolled: KW taps x 4 K-steps of 16 pixels.  The
+// descriptors advance by constants in their 16-byte start-address field: +128
+// per K-step (16 rows of 128 B), +8 per tap (the input window starts one
+// 128-byte row later).
+template <int KW>
+__device__ __forceinline__ void issue_stage(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, bool first)
+{
+#pragma unroll
+    for (int kx = 0; kx < KW; ++kx)
+#pragma unroll
+        for (int kk = 0; kk < KT / 16; ++kk)
+            tc::umma_bf16(tmem + kx * BM, da + 128 * kk, db + 8 * kx + 128 * kk, idesc, (first && kk == 0) ? 0u : 1u);
+}
+
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_wgrad_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, const WgTcParams p)
 {
@@ -158,16 +172,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
                 tc::fence_after_sync();
                 const uint32_t sa = tc::smem_u32(smem + stage * STAGE_BYTES);
-                for (int kx = 0; kx < p.kw; ++kx) {
-#pragma unroll
-                    for (int kk = 0; kk < KT / 16; ++kk) {
-                        // a K step of 16 pixels = 16 rows of 128 bytes = two 8-row swizzle atoms; tap kx
-                        // starts kx rows into the input box (the swizzle follows the absolute address)
-                        const uint64_t da = tc::sdesc_sw128_mn(sa + kk * 2048, A_BOX);
-                        const uint64_t db = tc::sdesc_sw128_mn(sa + A_BYTES + kx * 128 + kk * 2048, B_BOX);
-                        tc::umma_bf16(tmem + kx * BM, da, db, idesc, (st > s0 || kk > 0) ? 1u : 0u);
-                    }
-                }
+                // a K step of 16 pixels = 16 rows of 128 bytes = two 8-row swizzle atoms; tap kx starts kx
+                // rows into the input box (the swizzle follows the absolute address)
+                const uint64_t da = tc::sdesc_sw128_mn(sa, A_BOX), db = tc::sdesc_sw128_mn(sa + A_BYTES, B_BOX);
+                const bool first = st == s0;
+                if (p.kw == 3) issue_stage<3>(tmem, da, db, idesc, first);
+                else if (p.kw == 2) issue_stage<2>(tmem, da, db, idesc, first);
+                else issue_stage<1>(tmem, da, db, idesc, first);
                 tc::umma_commit(&empty[stage]);
                 if (++stage == S) {
                     stage = 0;
