@@ -29,6 +29,10 @@
 //               issuers keep the tensor core fed with these short MMAs;
 //               their commits free smem stages and hand finished tiles to
 //               the epilogue
+//   warp 7      mode 4 with ysm: TMA of the tile's layer-below activations
+//               into a shared buffer (4 boxes of 64 channels x 128 pixels)
+//               once the epilogue has released it, so the epilogue reads
+//               them from shared memory instead of waiting on DRAM
 //   warps 2..5  epilogue: tcgen05.ld of both halves (one pixel per thread
 //               per half), bias + tanh, then store BF16 NHWC / L2-normalise
 //               / apply the pairwise net's 1x1 head; or (mode 3, a training
@@ -56,7 +60,8 @@ constexpr int BM = 128;                 // pixels per half (UMMA M)
 constexpr int TILE_PX = 2 * BM;         // pixels per paired tile
 constexpr int HROWS = BM + 8;           // one half's input window: 128 px + up to 8 more for the kx taps
 constexpr int AROWS = BM + HROWS;       // paired: 264 rows x 64 bf16 = 33 KB (loaded as 128 + 136 rows)
-constexpr int NUM_THREADS = 224;
+constexpr int NUM_THREADS = 256;
+constexpr int Y_BOX = 64 * BM * 2;      // one 64-channel x 128-pixel box of the layer-below activations
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
 constexpr int MAX_STAGES = 4;
@@ -74,6 +79,7 @@ struct TcParams {
     __nv_bfloat16 *out16;     // mode 4: [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs]
     int aux_cs, o16_cs, o16_ph, o16_pw;
     float *bias_part;         // mode 4 (optional): [gridDim.x * 4][cout] channel sums of the output
+    int ysm, y_boxes;         // mode 4: aux through the shared buffer (y_boxes per half), else global loads
 };
 
 // Output pixel coordinates of half h of tile t; false if the half is past
@@ -113,6 +119,20 @@ __device__ __forceinline__ void load_dz_y(const TcParams &p, bool valid, int img
         } else {
             yv[c][0] = yv[c][1] = make_uint4(0u, 0u, 0u, 0u);
         }
+    }
+}
+
+// the same from the tile's shared buffer: half h's box b (channels 64 b .. 64 b + 63), pixel row r, in
+// the 128-byte swizzle (16-byte chunk j of row r at chunk j ^ (r & 7))
+template <int NP>
+__device__ __forceinline__ void load_dz_y_smem(const uint8_t *ybuf, int y_boxes, int h, int r, uint4 (*yv)[2])
+{
+#pragma unroll
+    for (int c = 0; c < NP / 16; ++c) {
+        const uint8_t *row = ybuf + (h * y_boxes + c / 4) * Y_BOX + r * 128;
+        const int j0 = 2 * (c % 4);
+        yv[c][0] = *(const uint4 *)(row + ((j0 ^ (r & 7)) << 4));
+        yv[c][1] = *(const uint4 *)(row + (((j0 + 1) ^ (r & 7)) << 4));
     }
 }
 
@@ -219,19 +239,21 @@ __device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d, uint64_t a, u
 template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
-              const __grid_constant__ CUtensorMap tmB, const TcParams p)
+              const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmY, const TcParams p)
 {
     constexpr int B_BYTES = NP * 128; // one tap's 64-channel weight box
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = p.stages;
     const int STAGE = p.stage_bytes;
-    uint64_t *full = (uint64_t *)(smem + S * STAGE);
+    uint8_t *ybuf = smem + S * STAGE; // mode 4 with ysm: [2 halves][y_boxes][Y_BOX]
+    uint64_t *full = (uint64_t *)(ybuf + (p.ysm ? 2 * p.y_boxes * Y_BOX : 0));
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;
     uint64_t *tempty = tfull + 2;
     uint64_t *drain = tempty + 2; // one per issuer
-    uint32_t *tmem_slot = (uint32_t *)(drain + 2);
+    uint64_t *yfull = drain + 2, *yempty = yfull + 1;
+    uint32_t *tmem_slot = (uint32_t *)(yempty + 1);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
     volatile int *zero_flag = abort_flag + 1;
     float *sbias = (float *)(tmem_slot + 4);
@@ -250,12 +272,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         tc::mbar_init(&drain[0], 1);
         tc::mbar_init(&drain[1], 1);
+        tc::mbar_init(yfull, 1);
+        tc::mbar_init(yempty, 128);
         *abort_flag = 0;
         *zero_flag = 0;
         tc::mbar_fence_init();
         tc::prefetch_tmap(&tmA);
         tc::prefetch_tmap(&tmA2);
         tc::prefetch_tmap(&tmB);
+        if (p.ysm) tc::prefetch_tmap(&tmY);
     }
     for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
     if (p.mode == 2)
@@ -320,6 +345,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                     tc::mbar_wait(&full[st], ph, zero_flag, 1u << 20);
                 }
+            }
+        }
+    } else if (warp == 7) {
+        if (p.ysm && lane == 0) {
+            // the tile's layer-below activations, once the epilogue has released the buffer
+            int lt = 0, issued = 0;
+            bool ok = true;
+            for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
+                if (!tc::mbar_wait(yempty, ((uint32_t)lt & 1u) ^ 1u, abort_flag)) {
+                    ok = false;
+                    break;
+                }
+                tc::mbar_expect_tx(yfull, (uint32_t)(2 * p.y_boxes * Y_BOX));
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    int img, y, x0;
+                    half_coords(p, t, h, img, y, x0); // a half past the list loads the last one's pixels
+                    for (int b = 0; b < p.y_boxes; ++b)
+                        tc::tma_load_4d(ybuf + (h * p.y_boxes + b) * Y_BOX, &tmY, yfull, b * 64, x0, y, img);
+                }
+                ++issued;
+            }
+            if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
+                // the copies of the last issue land before shared memory is released
+                if (issued) tc::mbar_wait(yfull, ((uint32_t)issued - 1u) & 1u, zero_flag, 1u << 20);
             }
         }
     } else if (warp == 1 || warp == 6) {
@@ -393,8 +445,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             hok[1] = half_coords(p, t, 1, himg[1], hy[1], hx0[1]);
             if (p.mode == 4) {
                 uint4 ya[NP / 16][2], yb[NP / 16][2];
-                load_dz_y<NP>(p, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, ya);
-                load_dz_y<NP>(p, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, yb);
+                if (p.ysm) {
+                    int got = 1;
+                    if (lane == 0) got = tc::mbar_wait(yfull, (uint32_t)lt & 1u, abort_flag) ? 1 : 0;
+                    got = __shfl_sync(0xffffffffu, got, 0);
+                    if (!got) {
+                        *abort_flag = 1;
+                        atomicExch(p.err, 1);
+                        break;
+                    }
+                    load_dz_y_smem<NP>(ybuf, p.y_boxes, 0, row, ya);
+                    load_dz_y_smem<NP>(ybuf, p.y_boxes, 1, row, yb);
+                    tc::mbar_arrive(yempty); // the buffer may take the next tile's activations
+                } else {
+                    load_dz_y<NP>(p, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, ya);
+                    load_dz_y<NP>(p, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, yb);
+                }
                 const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf) * ACC_STRIDE;
                 epilogue_dz<NP>(p, tq, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, q, lane, sacc,
                                 ya);
@@ -521,9 +587,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
 template <int NP> int stage_bytes(int a_bytes, int kw) { return a_bytes + kw * NP * 128; }
 
-template <int NP> size_t smem_bytes(int stages, int a_bytes, int kw, int mode)
+template <int NP> size_t smem_bytes(int stages, int a_bytes, int kw, int mode, int ybytes = 0)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>(a_bytes, kw) + (2 * stages + 6) * 8 + 16 +
+    return 1024 + (size_t)stages * stage_bytes<NP>(a_bytes, kw) + ybytes + (2 * stages + 8) * 8 + 16 +
            (mode == 4 ? 7 : (mode == 2 ? 3 : 1)) * NP * 4;
 }
 
@@ -558,17 +624,33 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     p.stage_bytes = stage_bytes<NP>(p.a_bytes, a.kw);
+    // mode 4: the layer-below activations through shared memory when the buffer fits beside two stages
+    // (their global loads stalled the epilogue more than a third stage gains)
+    p.y_boxes = (NP + 63) / 64;
+    const int ybytes = 2 * p.y_boxes * Y_BOX;
+    p.ysm = a.mode == 4 && smem_bytes<NP>(2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
+    CUtensorMap my = ma; // unused unless ysm
+    if (p.ysm) {
+        cuuint64_t gY[4] = {(cuuint64_t)a.aux_cs, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)a.n_img};
+        cuuint64_t sY[3] = {(cuuint64_t)a.aux_cs * 2, (cuuint64_t)p.Wo * a.aux_cs * 2,
+                            (cuuint64_t)p.Ho * p.Wo * a.aux_cs * 2};
+        cuuint32_t bY[4] = {64, BM, 1, 1}, eY[4] = {1, 1, 1, 1};
+        r = enc(&my, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.aux, gY, sY, bY, eY, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation (mode 4) tensor map (%d)", (int)r);
+    }
+    const int yb = p.ysm ? ybytes : 0;
     p.stages = 0;
     for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
-        if (smem_bytes<NP>(s, p.a_bytes, a.kw, a.mode) <= (size_t)maxsm) p.stages = s;
+        if (smem_bytes<NP>(s, p.a_bytes, a.kw, a.mode, yb) <= (size_t)maxsm) p.stages = s;
     if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
-    const size_t smem = smem_bytes<NP>(p.stages, p.a_bytes, a.kw, a.mode);
+    const size_t smem = smem_bytes<NP>(p.stages, p.a_bytes, a.kw, a.mode, yb);
     CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int grid = std::min(p.num_tiles, sms);
     if (a.bias_splits) *a.bias_splits = 4 * grid;
     {
         CNNCRF_PROF("conv_tc", st);
-        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, p);
+        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, my, p);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
