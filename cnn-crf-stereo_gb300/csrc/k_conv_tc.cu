@@ -136,50 +136,64 @@ __device__ __forceinline__ void load_dz_y_smem(const uint8_t *ybuf, int y_boxes,
     }
 }
 
+// One half's chunk c of mode 4: the sums times 1 - y^2 into v (zero for an
+// invalid pixel, so it adds nothing to the bias sums), stored as BF16 into the
+// padded copy (and as FP32 if p.out).
 template <int NP>
-__device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta, bool valid, int img, int y, int x,
-                                            int q, int lane, float *sacc, const uint4 (*yv)[2])
+__device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, bool valid, size_t pix, size_t q16,
+                                         const uint4 (&yc)[2], float (&v)[16])
+{
+    tc::tmem_ld16(ta + c * 16, v); // warp-collective
+    const uint32_t yw[8] = {yc[0].x, yc[0].y, yc[0].z, yc[0].w, yc[1].x, yc[1].y, yc[1].z, yc[1].w};
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        const float a = __uint_as_float(yw[j] << 16), b = __uint_as_float(yw[j] & 0xffff0000u);
+        v[2 * j] = valid ? v[2 * j] * (1.0f - a * a) : 0.0f;
+        v[2 * j + 1] = valid ? v[2 * j + 1] * (1.0f - b * b) : 0.0f;
+    }
+    if (!valid) return;
+    uint32_t u[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+        u[j] = *(uint32_t *)&b2;
+    }
+    uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
+    d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
+    d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
+    if (p.out) {
+        float *o = (float *)p.out + pix * p.cp_out + c * 16;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+            if (c * 16 + 4 * g + 3 < p.cout)
+                *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
+            else
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
+        }
+    }
+}
+
+// Mode 4 epilogue of a tile for this thread's pixel row in both halves, chunk
+// by chunk (all NP / 16 chunks unrolled; ya / yb hold the layer-below
+// activations of the two pixels).  The bias sums reduce the two halves'
+// values of a chunk together, once.
+template <int NP>
+__device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta0, const bool (&valid)[2],
+                                            const size_t (&pix)[2], const size_t (&q16)[2], int q, int lane,
+                                            float *sacc, const uint4 (*ya)[2], const uint4 (*yb)[2])
 {
     constexpr int NC = NP / 16;
-    const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
-    const size_t q16 = ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        float v[16];
-        tc::tmem_ld16(ta + c * 16, v); // warp-collective
-        const uint32_t yw[8] = {yv[c][0].x, yv[c][0].y, yv[c][0].z, yv[c][0].w,
-                                yv[c][1].x, yv[c][1].y, yv[c][1].z, yv[c][1].w};
-#pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const float a = __uint_as_float(yw[j] << 16), b = __uint_as_float(yw[j] & 0xffff0000u);
-            v[2 * j] = valid ? v[2 * j] * (1.0f - a * a) : 0.0f; // invalid pixels add nothing to the sums
-            v[2 * j + 1] = valid ? v[2 * j + 1] * (1.0f - b * b) : 0.0f;
-        }
-        if (valid) {
-            uint32_t u[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                u[j] = *(uint32_t *)&b2;
-            }
-            uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
-            d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
-            d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
-            if (p.out) {
-                float *o = (float *)p.out + pix * p.cp_out + c * 16;
-#pragma unroll
-                for (int g = 0; g < 4; ++g) {
-                    if (c * 16 + 4 * g + 3 < p.cout)
-                        *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2], v[4 * g + 3]);
-                    else
-#pragma unroll
-                        for (int j = 0; j < 4; ++j)
-                            if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
-                }
-            }
-        }
+        float v[16], w[16];
+        dz_chunk<NP>(p, ta0, c, valid[0], pix[0], q16[0], ya[c], v);
+        dz_chunk<NP>(p, ta0 + ACC_STRIDE, c, valid[1], pix[1], q16[1], yb[c], w);
         if (p.bias_part) {
-            // the warp's 32 pixels summed per channel: each exchange halves the values a lane keeps;
+#pragma unroll
+            for (int j = 0; j < 16; ++j) v[j] += w[j];
+            // the warp's 2 x 32 pixels summed per channel: each exchange halves the values a lane keeps;
             // lane L ends with channel c * 16 + (L >> 1), twice
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
@@ -462,10 +476,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     load_dz_y<NP>(p, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, yb);
                 }
                 const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf) * ACC_STRIDE;
-                epilogue_dz<NP>(p, tq, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, q, lane, sacc,
-                                ya);
-                epilogue_dz<NP>(p, tq + ACC_STRIDE, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, q,
-                                lane, sacc, yb);
+                bool vh[2];
+                size_t ph[2], qh[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int x = hx0[h] + row;
+                    vh[h] = hok[h] && x < p.Wo;
+                    ph[h] = ((size_t)himg[h] * p.Ho + hy[h]) * p.Wo + x;
+                    qh[h] = ((size_t)himg[h] * (p.Ho + 2 * p.o16_ph) + hy[h] + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x +
+                            p.o16_pw;
+                }
+                epilogue_dz<NP>(p, tq, vh, ph, qh, q, lane, sacc, ya, yb);
                 tc::fence_before_sync();
                 tc::mbar_arrive(&tempty[buf]);
                 continue;
