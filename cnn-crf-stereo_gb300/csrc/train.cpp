@@ -55,16 +55,18 @@ struct cnncrf_train {
     std::vector<float> list;
     int omin = 0, omax = 0;
     DevBuf dlist;
-    // forward state; feature-layer outputs: checkpoints in their own buffers, the rest in a shared pool
-    DevBuf padded[2], norm[2], scratch;
-    DevBuf norm16[2]; // BF16 copies of norm at channel stride 64 (the first layers' tensor-core weight gradients)
+    // forward state.  The feature net runs both sides as one batch of 2n images (left crops, then right):
+    // every feature buffer holds both sides, and its side s is the half at s * n images.
+    // Feature-layer outputs: checkpoints in their own buffers, the rest in a shared pool.
+    DevBuf padded, norm, scratch;
+    DevBuf norm16; // BF16 copy of norm at channel stride 64 (the first layers' tensor-core weight gradients)
     bool tc_corr = false; // the correlation adjoint on the tensor cores
     std::vector<char> keep;
-    std::vector<DevBuf> act[2], pool;
+    std::vector<DevBuf> act, pool;
     DevBuf fbuf, vol, y1, y2, pwout; // fbuf: both sides' normalised features
     bool forwarded = false, hinged = false;
     // backward and hinge scratch
-    DevBuf gvol, gpw, df[2], dy, dyb, padb, part, partb, gh;
+    DevBuf gvol, gpw, df, dy, dyb, padb, part, partb, gh; // df: both sides' feature gradients
     DevBuf aug, wts, labels, crfws, contrib, rows, err, tcerr;
     size_t crfws_bytes = 0;
     DevBuf wgs; // the tensor-core weight gradient's planar copies and partial sums
@@ -83,17 +85,21 @@ struct cnncrf_train {
     int forward(const float *l, const float *r);
     int hinge(const int32_t *gt, double *loss, int32_t *yh_out);
     int backward(const float *gv, const float *gp);
-    int run_layer(int s, int l);
-    int layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img, const void *y,
-                   int ys, float *dz, float *dprev, bool &ready, const TLayer *below);
+    int run_layer(int l);
+    int layer_back(TLayer &L, int nimg, const void *in, bool in_bf16, long in_pix, long in_row, long in_img,
+                   const void *y, int ys, float *dz, float *dprev, bool &ready, const TLayer *below);
+    int nf() const { return 2 * n; } // images of the feature net: both sides
+    float *norm_s(int s) { return norm.as<float>() + (size_t)s * n * h * w * ic; }
+    float *padded_s(int s) { return padded.as<float>() + (size_t)s * n * h * w * 4; }
+    float *df_s(int s) { return df.as<float>() + (size_t)s * n * H * W * d.feat_channels; }
     float *param(int slot) { return theta.as<float>() + off[slot]; }
     float *gradp(int slot) { return grad.as<float>() + off[slot]; }
     size_t es() const { return bf16 ? 2 : 4; }
     int fstride() const { return bf16 ? cp_feat : d.feat_channels; } // channel stride of feature activations
     int pstride() const { return bf16 ? cp_pw : d.pw_channels; }
-    void *actp(int s, int l)
+    void *actp(int l) // layer l's output, both sides
     {
-        if (keep[l]) return act[s][l].get();
+        if (keep[l]) return act[l].get();
         int c = l;
         while (c > 0 && !keep[c - 1]) --c; // first layer of l's segment
         return pool[l - c].get();
@@ -195,24 +201,22 @@ int cnncrf_train::build()
     // activations (zeroed: the BF16 mode's padding channels must read as zero)
     const size_t N = (size_t)n * H * W;
     size_t amax = (size_t)n * h * w * 4, lmax = 0;
-    for (auto &Ly : feat) lmax = std::max(lmax, (size_t)n * Ly.hout() * Ly.wout() * fstride() * es());
+    for (auto &Ly : feat) lmax = std::max(lmax, (size_t)nf() * Ly.hout() * Ly.wout() * fstride() * es());
     auto zalloc = [&](DevBuf &b, size_t bytes) -> int {
         CNNCRF_TRY(b.reserve(bytes));
         CNNCRF_CUDA(cudaMemset(b.get(), 0, bytes));
         return CNNCRF_OK;
     };
-    for (int s = 0; s < 2; ++s) {
-        CNNCRF_TRY(padded[s].reserve(sizeof(float) * n * h * w * 4));
-        CNNCRF_TRY(norm[s].reserve(sizeof(float) * n * h * w * ic));
-        act[s].clear();
-        act[s].resize(feat.size());
-        for (size_t l = 0; l < feat.size(); ++l) {
-            const size_t e = (size_t)n * feat[l].hout() * feat[l].wout() * F;
-            amax = std::max(amax, e);
-            if (keep[l]) CNNCRF_TRY(zalloc(act[s][l], (size_t)n * feat[l].hout() * feat[l].wout() * fstride() * es()));
-        }
-        CNNCRF_TRY(df[s].reserve(sizeof(float) * N * F));
+    CNNCRF_TRY(padded.reserve(sizeof(float) * nf() * h * w * 4));
+    CNNCRF_TRY(norm.reserve(sizeof(float) * nf() * h * w * ic));
+    act.clear();
+    act.resize(feat.size());
+    for (size_t l = 0; l < feat.size(); ++l) {
+        const size_t e = (size_t)nf() * feat[l].hout() * feat[l].wout() * F;
+        amax = std::max(amax, e);
+        if (keep[l]) CNNCRF_TRY(zalloc(act[l], (size_t)nf() * feat[l].hout() * feat[l].wout() * fstride() * es()));
     }
+    CNNCRF_TRY(df.reserve(sizeof(float) * 2 * N * F));
     pool.clear();
     pool.resize(poolsz);
     for (auto &b : pool) CNNCRF_TRY(zalloc(b, lmax));
@@ -226,7 +230,7 @@ int cnncrf_train::build()
     // backward: dy / dyb hold any layer's output or input gradient, padb a padded output gradient
     CNNCRF_TRY(dy.reserve(sizeof(float) * amax));
     CNNCRF_TRY(dyb.reserve(sizeof(float) * amax));
-    CNNCRF_TRY(padb.reserve(sizeof(float) * (size_t)n * (h + 4) * (w + 4) * std::max(F, P)));
+    CNNCRF_TRY(padb.reserve(sizeof(float) * (size_t)nf() * (h + 4) * (w + 4) * std::max(F, P)));
     CNNCRF_TRY(gvol.reserve(sizeof(float) * N * D));
     CNNCRF_TRY(gpw.reserve(sizeof(float) * N * 2));
     CNNCRF_TRY(gh.reserve(sizeof(float) * N * 2));
@@ -234,7 +238,7 @@ int cnncrf_train::build()
     size_t part_floats = 0;
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v) {
-            const long P = (long)n * Ly.hout() * Ly.wout();
+            const long P = (long)(v == &feat ? nf() : n) * Ly.hout() * Ly.wout();
             const int K = Ly.kh * Ly.kw * Ly.cin;
             Pmax = std::max(Pmax, P);
             part_floats = std::max(part_floats, (size_t)k::train_wgrad_splits_k(P, K) * Ly.cout * K);
@@ -244,7 +248,7 @@ int cnncrf_train::build()
         for (auto *v : {&feat, &pw})
             for (auto &Ly : *v)
                 if (Ly.act == 1 && k::wgrad_tc_supported(Ly.cout, Ly.cin, Ly.kh, Ly.kw)) {
-                    const long steps = (long)n * Ly.hout() * ((Ly.wout() + 63) / 64);
+                    const long steps = (long)(v == &feat ? nf() : n) * Ly.hout() * ((Ly.wout() + 63) / 64);
                     wgs_bytes = std::max(wgs_bytes, k::wgrad_tc_scratch_bytes(Ly.cout, Ly.cin, Ly.kh, Ly.kw,
                                                                               k::wgrad_tc_splits(Ly.kh, steps)));
                     Ly.tcw = true;
@@ -252,12 +256,12 @@ int cnncrf_train::build()
     if (wgs_bytes) CNNCRF_TRY(wgs.reserve(wgs_bytes));
     tc_corr = bf16 && d.tc_dgrad && k::corr_bwd_tc_supported(F, cp_feat, D, omin, omax);
     if (feat[0].tcw || pw[0].tcw)
-        for (int s = 0; s < 2; ++s) CNNCRF_TRY(zalloc(norm16[s], 2 * (size_t)n * h * w * 64));
+        CNNCRF_TRY(zalloc(norm16, 2 * (size_t)nf() * h * w * 64));
     size_t dpad_bytes = 0;
     for (auto *v : {&feat, &pw})
         for (auto &Ly : *v)
             if (Ly.w16d.get() || Ly.tcw)
-                dpad_bytes = std::max(dpad_bytes, 2 * (size_t)n * (Ly.hout() + 2 * (Ly.kh - 1)) *
+                dpad_bytes = std::max(dpad_bytes, 2 * (size_t)(v == &feat ? nf() : n) * (Ly.hout() + 2 * (Ly.kh - 1)) *
                                                       (Ly.wout() + 2 * (Ly.kw - 1)) * pad_to(Ly.cout, 64));
     if (dpad_bytes) {
         for (auto &b : dpad) CNNCRF_TRY(zalloc(b, dpad_bytes));
@@ -301,24 +305,24 @@ int cnncrf_train::refresh()
     return CNNCRF_OK;
 }
 
-// feature layer l of side s into actp(s, l)
-int cnncrf_train::run_layer(int s, int l)
+// feature layer l of both sides into actp(l)
+int cnncrf_train::run_layer(int l)
 {
     TLayer &Ly = feat[l];
-    void *out = actp(s, l);
+    void *out = actp(l);
     if (l == 0 || !bf16) {
-        const float *in = l == 0 ? norm[s].as<float>() : (const float *)actp(s, l - 1);
+        const float *in = l == 0 ? norm.as<float>() : (const float *)actp(l - 1);
         const int cs = l == 0 ? ic : d.feat_channels;
         k::ConvArgs a{in, Ly.hin, Ly.win, Ly.cin, (long)cs, (long)Ly.win * cs, Ly.wt.as<float>(), Ly.b128.as<float>(),
                       Ly.cout, Ly.kh, Ly.kw, 1, bf16 ? nullptr : (float *)out};
-        a.n_img = n, a.in_img = (long)Ly.hin * Ly.win * cs, a.out_img = (long)Ly.hout() * Ly.wout() * fstride();
+        a.n_img = nf(), a.in_img = (long)Ly.hin * Ly.win * cs, a.out_img = (long)Ly.hout() * Ly.wout() * fstride();
         if (!bf16) return k::conv_simt(a, st);
         a.out16 = out, a.out_cs = cp_feat; // BF16 NHWC output padded to cp_feat
         return k::conv_first_tc_supported(a) ? k::conv_first_tc(a, tcerr.as<int>(), st) : k::conv_simt(a, st);
     }
     k::TcConvArgs t{};
-    t.in = actp(s, l - 1);
-    t.n_img = n, t.Hin = Ly.hin, t.Win = Ly.win, t.cp_in = cp_feat, t.cin = Ly.cin;
+    t.in = actp(l - 1);
+    t.n_img = nf(), t.Hin = Ly.hin, t.Win = Ly.win, t.cp_in = cp_feat, t.cin = Ly.cin;
     t.wt = Ly.w16.get();
     t.np = np_feat, t.cout = Ly.cout, t.kh = Ly.kh, t.kw = Ly.kw;
     t.bias = Ly.b128.as<float>();
@@ -327,7 +331,7 @@ int cnncrf_train::run_layer(int s, int l)
     t.out = out;
     t.cp_out = cp_feat;
     if (l == (int)feat.size() - 1) { // the last layer also writes the L2-normalised features
-        t.mode = 1, t.out = fside(s);
+        t.mode = 1, t.out = fbuf.get(); // both sides, in the order the correlation reads them
         t.out16 = out, t.o16_cs = cp_feat;
     }
     t.err = tcerr.as<int>();
@@ -339,17 +343,15 @@ int cnncrf_train::forward(const float *l, const float *r)
     const float *img[2] = {l, r};
     const int F = d.feat_channels, L = (int)feat.size();
     for (int s = 0; s < 2; ++s) {
-        CNNCRF_TRY(k::pad_rgba(img[s], W, H, p, padded[s].as<float>(), st, n));
-        CNNCRF_TRY(k::normalize(padded[s].as<float>(), w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
-        if (norm16[s].get()) CNNCRF_TRY(k::train_to_bf16_c64(norm[s].as<float>(), (long)n * h * w, ic, norm16[s].get(), st));
-        for (int li = 0; li < L; ++li) CNNCRF_TRY(run_layer(s, li));
-        if (bf16) {
-            // the last layer's epilogue (run_layer) wrote the normalised features
-        } else {
-            const size_t fb = sizeof(float) * (size_t)n * H * W * F;
-            CNNCRF_CUDA(cudaMemcpyAsync(fside(s), actp(s, L - 1), fb, cudaMemcpyDeviceToDevice, st));
-            CNNCRF_TRY(k::l2norm((float *)fside(s), (long)n * H * W, F, st));
-        }
+        CNNCRF_TRY(k::pad_rgba(img[s], W, H, p, padded_s(s), st, n));
+        CNNCRF_TRY(k::normalize(padded_s(s), w, h, ic, norm_s(s), scratch.get(), st, n));
+    }
+    if (norm16.get()) CNNCRF_TRY(k::train_to_bf16_c64(norm.as<float>(), (long)nf() * h * w, ic, norm16.get(), st));
+    for (int li = 0; li < L; ++li) CNNCRF_TRY(run_layer(li)); // both sides at once
+    if (!bf16) { // (the BF16 last layer's epilogue wrote the normalised features)
+        const size_t fb = sizeof(float) * (size_t)nf() * H * W * F;
+        CNNCRF_CUDA(cudaMemcpyAsync(fbuf.get(), actp(L - 1), fb, cudaMemcpyDeviceToDevice, st));
+        CNNCRF_TRY(k::l2norm(fbuf.as<float>(), (long)nf() * H * W, F, st));
     }
     if (!bf16)
         CNNCRF_TRY(k::correlation((const float *)fside(0), (const float *)fside(1), H, W, F, dlist.as<float>(), D, omin,
@@ -362,7 +364,7 @@ int cnncrf_train::forward(const float *l, const float *r)
                                        CNNCRF_UNARY_ONE_MINUS_DOT, vol.as<float>(), st, n, (long)H * W * cp_feat));
     // pairwise net on the left image's normalisation cropped by p - 2 (stereo/colorstereonet.cpp:69-73)
     const int cr = p - 2, P = d.pw_channels;
-    const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
+    const float *in = norm_s(0) + ((size_t)cr * w + cr) * ic;
     k::ConvArgs a1{in, H + 4, W + 4, 3, (long)ic, (long)w * ic, pw[0].wt.as<float>(), pw[0].b128.as<float>(), P, 3, 3,
                    1, bf16 ? nullptr : y1.as<float>()};
     a1.n_img = n, a1.in_img = (long)h * w * ic, a1.out_img = (long)(H + 2) * (W + 2) * pstride();
@@ -442,45 +444,47 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
     return CNNCRF_OK;
 }
 
+// nimg: the batch's images (both sides' for a feature layer).
 // dz: the layer's output gradient (dense FP32), turned into the pre-activation
 // gradient in place; y: the layer's output at channel stride ys; dprev (if
 // set): the input gradient (dense FP32).  ready: on entry, whether dz already
 // holds the output gradient times 1 - y^2 with its BF16 padded copy in
 // dpad[dcur] (the layer above's fused input gradient made them); on exit,
 // whether this call made dprev so for `below`, the layer whose output is `in`.
-int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pix, long in_row, long in_img,
-                             const void *y, int ys, float *dz, float *dprev, bool &ready, const TLayer *below)
+int cnncrf_train::layer_back(TLayer &L, int nimg, const void *in, bool in_bf16, long in_pix, long in_row,
+                             long in_img, const void *y, int ys, float *dz, float *dprev, bool &ready,
+                             const TLayer *below)
 {
     const int Ho = L.hout(), Wo = L.wout();
     const int ph = L.kh - 1, pwd = L.kw - 1;
     const bool tcd = dprev && L.w16d.get(); // the input gradient on the tensor cores (BF16 mode)
     if (!ready) {
         if (tcd || L.tcw) // dz and its BF16 padded copy, the tensor-core operand
-            CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, n, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64),
+            CNNCRF_TRY(k::train_tanh_bwd_pad(dz, y, nimg, Ho, Wo, L.cout, ys, ph, pwd, pad_to(L.cout, 64),
                                              dpad[dcur].get(), st));
         else
-            CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)n * Ho * Wo, L.cout, ys, st));
+            CNNCRF_TRY(k::train_tanh_bwd(dz, y, bf16, (long)nimg * Ho * Wo, L.cout, ys, st));
     }
     const bool was_ready = ready;
     ready = false;
     if (L.tcw && in_bf16) { // BF16 mode, tensor cores
         CNNCRF_TRY(k::wgrad_tc(dpad[dcur].get(), L.cout, pad_to(L.cout, 64), in, in_pix, in_row, in_img, L.cin, L.kh,
-                               L.kw, n, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
+                               L.kw, nimg, Ho, Wo, wgs.get(), wgs_bytes, gradp(L.wslot), tcerr.as<int>(), st));
         if (L.bslot >= 0) {
             if (was_ready && bias_ready) // the sums the layer above's fused epilogue left
                 CNNCRF_TRY(k::train_bias_reduce(bpart.as<float>(), bsplits, L.cout, gradp(L.bslot), st));
             else
-                CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)n * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
+                CNNCRF_TRY(k::train_bias_grad(dz, L.cout, (long)nimg * Ho * Wo, partb.as<float>(), gradp(L.bslot), st));
         }
     } else {
-        CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, n, Ho, Wo,
+        CNNCRF_TRY(k::train_wgrad(dz, L.cout, in, in_bf16, in_pix, in_row, in_img, L.cin, L.kh, L.kw, nimg, Ho, Wo,
                                   part.as<float>(), gradp(L.wslot), L.bslot >= 0 ? gradp(L.bslot) : nullptr,
                                   partb.as<float>(), st));
     }
     if (!dprev) return CNNCRF_OK;
     if (tcd) { // dprev = the valid convolution of the padded dz with the unflipped, transposed kernel
         k::TcConvArgs t{};
-        t.in = dpad[dcur].get(), t.n_img = n, t.Hin = Ho + 2 * ph, t.Win = Wo + 2 * pwd;
+        t.in = dpad[dcur].get(), t.n_img = nimg, t.Hin = Ho + 2 * ph, t.Win = Wo + 2 * pwd;
         t.cp_in = pad_to(L.cout, 64), t.cin = L.cout;
         t.wt = L.w16d.get(), t.np = umma_n(L.cin), t.cout = L.cin, t.kh = L.kh, t.kw = L.kw;
         t.mode = 3, t.out = dprev, t.cp_out = L.cin, t.err = tcerr.as<int>();
@@ -491,7 +495,7 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
         bias_ready = false;
         if (fuse) {
             const int bph = below->kh - 1, bpw = below->kw - 1, bcp = pad_to(below->cout, 64);
-            CNNCRF_TRY(k::train_zero_border(dpad[dcur ^ 1].get(), n, L.hin, L.win, bcp, bph, bpw, st));
+            CNNCRF_TRY(k::train_zero_border(dpad[dcur ^ 1].get(), nimg, L.hin, L.win, bcp, bph, bpw, st));
             t.mode = 4, t.aux = in, t.aux_cs = (int)in_pix;
             t.out16 = dpad[dcur ^ 1].get(), t.o16_cs = bcp, t.o16_ph = bph, t.o16_pw = bpw;
             // the FP32 dz only where a CUDA-core gradient of the layer below reads it
@@ -502,11 +506,11 @@ int cnncrf_train::layer_back(TLayer &L, const void *in, bool in_bf16, long in_pi
         if (fuse) dcur ^= 1, ready = true, bias_ready = t.bias_part != nullptr;
         return CNNCRF_OK;
     }
-    CNNCRF_TRY(k::train_pad_zero(dz, n, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
+    CNNCRF_TRY(k::train_pad_zero(dz, nimg, Ho, Wo, L.cout, ph, pwd, padb.as<float>(), st));
     const int Hp = Ho + 2 * ph, Wp = Wo + 2 * pwd;
     k::ConvArgs a{padb.as<float>(), Hp, Wp, L.cout, (long)L.cout, (long)Wp * L.cout, L.wd.as<float>(), nullptr,
                   L.cin, L.kh, L.kw, 0, dprev};
-    a.n_img = n, a.in_img = (long)Hp * Wp * L.cout, a.out_img = (long)L.hin * L.win * L.cin;
+    a.n_img = nimg, a.in_img = (long)Hp * Wp * L.cout, a.out_img = (long)L.hin * L.win * L.cin;
     return k::conv_simt(a, st);
 }
 
@@ -519,46 +523,44 @@ int cnncrf_train::backward(const float *gv, const float *gp)
     const long N = (long)n * H * W;
     CNNCRF_CUDA(cudaMemsetAsync(grad.get(), 0, total * sizeof(float), st));
     if (tc_corr)
-        CNNCRF_TRY(k::corr_bwd_tc(fside(0), fside(1), fs, gv, dlist.as<float>(), n, H, W, F, D, omin, omax,
-                                  df[0].as<float>(), df[1].as<float>(), tcerr.as<int>(), st));
+        CNNCRF_TRY(k::corr_bwd_tc(fside(0), fside(1), fs, gv, dlist.as<float>(), n, H, W, F, D, omin, omax, df_s(0),
+                                  df_s(1), tcerr.as<int>(), st));
     else
         CNNCRF_TRY(k::train_corr_bwd(fside(0), fside(1), bf16, fs, gv, dlist.as<float>(), n, H, W, F, D, omin,
-                                     omax, df[0].as<float>(), df[1].as<float>(), st));
-    for (int s = 0; s < 2; ++s) {
-        float *cur = dy.as<float>(), *nxt = dyb.as<float>();
-        bool ready = false;
-        TLayer &top_l = feat[L - 1];
-        if (bf16 && top_l.tcw && top_l.w16d.get() && fs == 128 && top_l.kh == top_l.kw) {
-            // the normalisation's adjoint, tanh', the padded copy and the bias sums in one pass
-            CNNCRF_TRY(k::train_l2norm_tanh_bwd_pad(actp(s, L - 1), fs, df[s].as<float>(), n, H, W, F,
-                                                    top_l.kh - 1, top_l.kw - 1, dpad[dcur].get(), bpart.as<float>(),
-                                                    &bsplits, st));
-            ready = bias_ready = true;
-        } else {
-            CNNCRF_TRY(k::train_l2norm_bwd(actp(s, L - 1), bf16, fs, df[s].as<float>(), N, F, dy.as<float>(), st));
+                                     omax, df_s(0), df_s(1), st));
+    // the feature net, both sides at once: each weight gradient sums the two sides in one launch
+    float *cur = dy.as<float>(), *nxt = dyb.as<float>();
+    bool ready = false;
+    TLayer &top_l = feat[L - 1];
+    if (bf16 && top_l.tcw && top_l.w16d.get() && fs == 128 && top_l.kh == top_l.kw) {
+        // the normalisation's adjoint, tanh', the padded copy and the bias sums in one pass
+        CNNCRF_TRY(k::train_l2norm_tanh_bwd_pad(actp(L - 1), fs, df.as<float>(), nf(), H, W, F, top_l.kh - 1,
+                                                top_l.kw - 1, dpad[dcur].get(), bpart.as<float>(), &bsplits, st));
+        ready = bias_ready = true;
+    } else {
+        CNNCRF_TRY(k::train_l2norm_bwd(actp(L - 1), bf16, fs, df.as<float>(), 2 * N, F, dy.as<float>(), st));
+    }
+    int top = L - 1;
+    while (top >= 0) {
+        int c = top - 1; // the checkpoint under this segment (-1: the normalised input)
+        while (c >= 0 && !keep[c]) --c;
+        for (int j = c + 1; j < top; ++j) CNNCRF_TRY(run_layer(j)); // recompute the segment
+        for (int j = top; j > c; --j) {
+            TLayer &Ly = feat[j];
+            // the first layer reads the normalised input: its BF16 copy for the tensor-core weight gradient
+            const bool n16 = j == 0 && Ly.tcw;
+            const void *in = j > 0 ? actp(j - 1) : n16 ? norm16.get() : (const void *)norm.get();
+            const bool ib = (j > 0 && bf16) || n16;
+            const int cs = j > 0 ? fs : n16 ? 64 : ic;
+            CNNCRF_TRY(layer_back(Ly, nf(), in, ib, cs, (long)Ly.win * cs, (long)Ly.hin * Ly.win * cs, actp(j), fs,
+                                  cur, j > 0 ? nxt : nullptr, ready, j > 0 ? &feat[j - 1] : nullptr));
+            std::swap(cur, nxt);
         }
-        int top = L - 1;
-        while (top >= 0) {
-            int c = top - 1; // the checkpoint under this segment (-1: the normalised input)
-            while (c >= 0 && !keep[c]) --c;
-            for (int j = c + 1; j < top; ++j) CNNCRF_TRY(run_layer(s, j)); // recompute the segment
-            for (int j = top; j > c; --j) {
-                TLayer &Ly = feat[j];
-                // the first layer reads the normalised input: its BF16 copy for the tensor-core weight gradient
-                const bool n16 = j == 0 && Ly.tcw;
-                const void *in = j > 0 ? actp(s, j - 1) : n16 ? norm16[s].get() : (const void *)norm[s].get();
-                const bool ib = (j > 0 && bf16) || n16;
-                const int cs = j > 0 ? fs : n16 ? 64 : ic;
-                CNNCRF_TRY(layer_back(Ly, in, ib, cs, (long)Ly.win * cs, (long)Ly.hin * Ly.win * cs, actp(s, j), fs,
-                                      cur, j > 0 ? nxt : nullptr, ready, j > 0 ? &feat[j - 1] : nullptr));
-                std::swap(cur, nxt);
-            }
-            top = c;
-        }
+        top = c;
     }
     if (gp) {
         // head: gh = gpw sign(h), dy2 = W^T gh; its weight gradient is a 1x1 wgrad on y2
-        bool ready = false;
+        ready = false;
         if (bf16 && pw[1].tcw && pw[1].w16d.get() && ps == 64 && P <= 64) {
             // with the second pairwise layer's tanh', padded copy and bias sums
             CNNCRF_TRY(k::train_head_tanh_bwd_pad(y2.get(), ps, param(pw[2].wslot), gp, n, H, W, P, pw[1].kh - 1,
@@ -571,16 +573,16 @@ int cnncrf_train::backward(const float *gv, const float *gp)
         }
         CNNCRF_TRY(k::train_wgrad_head(gh.as<float>(), y2.get(), bf16, ps, (long)n * H * W, P, partb.as<float>(),
                                        gradp(pw[2].wslot), st));
-        CNNCRF_TRY(layer_back(pw[1], y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
+        CNNCRF_TRY(layer_back(pw[1], n, y1.get(), bf16, ps, (long)(W + 2) * ps, (long)(H + 2) * (W + 2) * ps, y2.get(),
                               ps, dy.as<float>(), dyb.as<float>(), ready, &pw[0]));
         const int cr = p - 2;
         if (pw[0].tcw) {
-            const void *in = (const char *)norm16[0].get() + 2 * ((size_t)cr * w + cr) * 64;
-            CNNCRF_TRY(layer_back(pw[0], in, true, 64, (long)w * 64, (long)h * w * 64, y1.get(), ps, dyb.as<float>(),
+            const void *in = (const char *)norm16.get() + 2 * ((size_t)cr * w + cr) * 64;
+            CNNCRF_TRY(layer_back(pw[0], n, in, true, 64, (long)w * 64, (long)h * w * 64, y1.get(), ps, dyb.as<float>(),
                                   nullptr, ready, nullptr));
         } else {
-            const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;
-            CNNCRF_TRY(layer_back(pw[0], in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps,
+            const float *in = norm_s(0) + ((size_t)cr * w + cr) * ic;
+            CNNCRF_TRY(layer_back(pw[0], n, in, false, ic, (long)w * ic, (long)h * w * ic, y1.get(), ps,
                                   dyb.as<float>(), nullptr, ready, nullptr));
         }
     }
