@@ -66,6 +66,8 @@ f32 = C.c_float
 PROTOS = {
     "cnncrf_last_error": ([], C.c_char_p),
     "cnncrf_abi_version": ([], i32),
+    "cnncrf_set_conv_pairs": ([i32], i32),
+    "cnncrf_get_conv_pairs": ([C.POINTER(i32)], i32),
     "cnncrf_net_create": ([C.POINTER(vp), C.POINTER(NetDesc), i32, i32, i32], i32),
     "cnncrf_net_destroy": ([vp], i32),
     "cnncrf_net_set_stream": ([vp, vp], i32),

@@ -44,6 +44,10 @@
 // overlaps the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout
 // the role raises the CTA abort flag and the global error flag, in-flight
 // copies and MMAs are drained (again bounded) and TMEM is freed before exit.
+#include <atomic>
+#include <map>
+#include <mutex>
+
 #include <cuda.h>
 #include <cuda_bf16.h>
 
@@ -60,7 +64,7 @@ constexpr int BM = 128;                 // pixels per half (UMMA M)
 constexpr int TILE_PX = 2 * BM;         // pixels per paired tile
 constexpr int HROWS = BM + 8;           // one half's input window: 128 px + up to 8 more for the kx taps
 constexpr int AROWS = BM + HROWS;       // paired: 264 rows x 64 bf16 = 33 KB (loaded as 128 + 136 rows)
-constexpr int NUM_THREADS = 256;
+constexpr int NUM_THREADS = 384;
 constexpr int Y_BOX = 64 * BM * 2;      // one 64-channel x 128-pixel box of the layer-below activations
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
@@ -78,7 +82,7 @@ struct TcParams {
     const __nv_bfloat16 *aux; // mode 4: y [n_img][Ho][Wo][aux_cs]
     __nv_bfloat16 *out16;     // mode 4: [n_img][Ho + 2 o16_ph][Wo + 2 o16_pw][o16_cs]
     int aux_cs, o16_cs, o16_ph, o16_pw;
-    float *bias_part;         // mode 4 (optional): [gridDim.x * 4][cout] channel sums of the output
+    float *bias_part;         // mode 4 (optional): [gridDim.x * 8][cout] channel sums of the output
     int ysm, y_boxes;         // mode 4: aux through the shared buffer (y_boxes per half), else global loads
 };
 
@@ -175,25 +179,20 @@ __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, 
     }
 }
 
-// Mode 4 epilogue of a tile for this thread's pixel row in both halves, chunk
-// by chunk (all NP / 16 chunks unrolled; ya / yb hold the layer-below
-// activations of the two pixels).  The bias sums reduce the two halves'
-// values of a chunk together, once.
+// Mode 4 epilogue of one half's accumulator for this thread's pixel, chunk by
+// chunk (all NP / 16 chunks unrolled; ya holds the pixel's layer-below
+// activations), adding the warp's per-channel sums into wacc.
 template <int NP>
-__device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta0, const bool (&valid)[2],
-                                            const size_t (&pix)[2], const size_t (&q16)[2], int q, int lane,
-                                            float *sacc, const uint4 (*ya)[2], const uint4 (*yb)[2])
+__device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta, bool valid, size_t pix, size_t q16,
+                                            int lane, float *wacc, const uint4 (*ya)[2])
 {
     constexpr int NC = NP / 16;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
-        float v[16], w[16];
-        dz_chunk<NP>(p, ta0, c, valid[0], pix[0], q16[0], ya[c], v);
-        dz_chunk<NP>(p, ta0 + ACC_STRIDE, c, valid[1], pix[1], q16[1], yb[c], w);
+        float v[16];
+        dz_chunk<NP>(p, ta, c, valid, pix, q16, ya[c], v);
         if (p.bias_part) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) v[j] += w[j];
-            // the warp's 2 x 32 pixels summed per channel: each exchange halves the values a lane keeps;
+            // the warp's 32 pixels summed per channel: each exchange halves the values a lane keeps;
             // lane L ends with channel c * 16 + (L >> 1), twice
 #pragma unroll
             for (int i = 0; i < 8; ++i) {
@@ -219,43 +218,74 @@ __device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta0, con
                 v[0] = keep + __shfl_xor_sync(0xffffffffu, give, 2);
             }
             v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
-            if (!(lane & 1)) sacc[q * NP + c * 16 + (lane >> 1)] += v[0];
+            if (!(lane & 1)) wacc[c * 16 + (lane >> 1)] += v[0];
         }
     }
 }
 
+// 16 values times s as BF16 into 16-byte aligned dst (two 16-byte stores)
+__device__ __forceinline__ void store_bf16_16(__nv_bfloat16 *dst, const float (&v)[16], float s)
+{
+    uint32_t u[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+        __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] * s, v[2 * j + 1] * s);
+        u[j] = *(uint32_t *)&b2;
+    }
+    uint4 *d = (uint4 *)dst;
+    d[0] = make_uint4(u[0], u[1], u[2], u[3]);
+    d[1] = make_uint4(u[4], u[5], u[6], u[7]);
+}
+
 // One stage's MMAs of one half, fully unrolled: kw taps x nk K-steps.
 // Descriptor arithmetic is in 16-byte units: +8 moves the A window one pixel
-// row, +2 one 16-element K step, +NP*8 to the next tap's weight box.
+// row, +2 one 16-element K step, +NB*8 to the next tap's weight box (NB rows:
+// NP, or NP / 2 per CTA of a pair, whose MMAs are M = 256 over both CTAs).
 // `first` = 0 only for the tile's first stage (overwrite the accumulator).
-template <int NP, int KW, int NK>
+template <int NP, bool PAIR, int KW, int NK>
 __device__ __forceinline__ void issue_stage(uint32_t d, uint64_t a, uint64_t db, uint32_t first)
 {
-    constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
+    constexpr int NB = PAIR ? NP / 2 : NP;
+    constexpr uint32_t IDESC = tc::idesc_bf16(PAIR ? 2 * BM : BM, NP);
 #pragma unroll
     for (int kx = 0; kx < KW; ++kx)
 #pragma unroll
-        for (int kk = 0; kk < NK; ++kk)
-            tc::umma_bf16(d, a + 8 * kx + 2 * kk, db + kx * (NP * 8) + 2 * kk, IDESC, (kx | kk) ? 1u : first);
+        for (int kk = 0; kk < NK; ++kk) {
+            const uint32_t acc = (kx | kk) ? 1u : first;
+            if constexpr (PAIR)
+                tc::umma_bf16_pair(d, a + 8 * kx + 2 * kk, db + kx * (NB * 8) + 2 * kk, IDESC, acc);
+            else
+                tc::umma_bf16(d, a + 8 * kx + 2 * kk, db + kx * (NB * 8) + 2 * kk, IDESC, acc);
+        }
 }
 
-template <int NP, int KW>
+template <int NP, bool PAIR, int KW>
 __device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d, uint64_t a, uint64_t db, uint32_t first)
 {
     switch (nk) {
-    case 1: issue_stage<NP, KW, 1>(d, a, db, first); break;
-    case 2: issue_stage<NP, KW, 2>(d, a, db, first); break;
-    case 3: issue_stage<NP, KW, 3>(d, a, db, first); break;
-    default: issue_stage<NP, KW, 4>(d, a, db, first); break;
+    case 1: issue_stage<NP, PAIR, KW, 1>(d, a, db, first); break;
+    case 2: issue_stage<NP, PAIR, KW, 2>(d, a, db, first); break;
+    case 3: issue_stage<NP, PAIR, KW, 3>(d, a, db, first); break;
+    default: issue_stage<NP, PAIR, KW, 4>(d, a, db, first); break;
     }
 }
 
-template <int NP>
+// PAIR: launched as 2-CTA clusters.  Each CTA runs its own tile (the even CTA
+// tile 2u, the odd one 2u + 1 of the pair's u-th step) with its own input
+// window, but stages only half of each tap's weights (output channels NP/2 *
+// rank ..); the even CTA issues M = 256 MMAs over both CTAs' operands, so a
+// weight byte staged serves twice the pixels and the tensor core reads fewer
+// shared-memory bytes per MMA FLOP.  Both CTAs' copies complete on the even
+// CTA's full barriers, its MMA commits arrive on both CTAs' empty and tfull
+// barriers, and both CTAs' epilogue warps release an accumulator on the even
+// CTA's tempty barrier.
+template <int NP, bool PAIR>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
               const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmY, const TcParams p)
 {
-    constexpr int B_BYTES = NP * 128; // one tap's 64-channel weight box
+    constexpr int NB = PAIR ? NP / 2 : NP; // weight rows (output channels) this CTA stages per tap
+    constexpr int B_BYTES = NB * 128;      // one tap's 64-channel weight box
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     const int S = p.stages;
@@ -263,16 +293,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     uint8_t *ybuf = smem + S * STAGE; // mode 4 with ysm: [2 halves][y_boxes][Y_BOX]
     uint64_t *full = (uint64_t *)(ybuf + (p.ysm ? 2 * p.y_boxes * Y_BOX : 0));
     uint64_t *empty = full + S;
-    uint64_t *tfull = empty + S;
-    uint64_t *tempty = tfull + 2;
-    uint64_t *drain = tempty + 2; // one per issuer
+    uint64_t *tfull = empty + S;  // [buffer][half]
+    uint64_t *tempty = tfull + 4; // [buffer][half]
+    uint64_t *drain = tempty + 4; // one per issuer
     uint64_t *yfull = drain + 2, *yempty = yfull + 1;
     uint32_t *tmem_slot = (uint32_t *)(yempty + 1);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
     volatile int *zero_flag = abort_flag + 1;
     float *sbias = (float *)(tmem_slot + 4);
     float *shead = sbias + NP;
-    float *sacc = shead + 2 * NP; // mode 4 bias sums: [4 epilogue warps][NP]
+    float *sacc = shead + 2 * NP; // mode 4 bias sums: [8 epilogue warps][NP]
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -280,14 +310,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::mbar_init(&full[s], 1);
             tc::mbar_init(&empty[s], 2); // a commit from each issuer
         }
-        for (int b = 0; b < 2; ++b) {
-            tc::mbar_init(&tfull[b], 2);
-            tc::mbar_init(&tempty[b], 128);
+        for (int b = 0; b < 4; ++b) {
+            tc::mbar_init(&tfull[b], 1);               // the half's issuer commits
+            tc::mbar_init(&tempty[b], PAIR ? 8 : 4);   // one arrive per epilogue warp of the half (both CTAs)
         }
         tc::mbar_init(&drain[0], 1);
         tc::mbar_init(&drain[1], 1);
         tc::mbar_init(yfull, 1);
-        tc::mbar_init(yempty, 128);
+        tc::mbar_init(yempty, 8); // one arrive per epilogue warp
         *abort_flag = 0;
         *zero_flag = 0;
         tc::mbar_fence_init();
@@ -300,23 +330,38 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     if (p.mode == 2)
         for (int i = threadIdx.x; i < 2 * NP; i += NUM_THREADS) shead[i] = p.head[i];
     if (p.bias_part)
-        for (int i = threadIdx.x; i < 4 * NP; i += NUM_THREADS) sacc[i] = 0.0f;
+        for (int i = threadIdx.x; i < 8 * NP; i += NUM_THREADS) sacc[i] = 0.0f;
     if (warp == 1) {
-        tc::tmem_alloc(tmem_slot, TMEM_COLS);
-        tc::tmem_relinquish();
+        if constexpr (PAIR) {
+            tc::tmem_alloc_pair(tmem_slot, TMEM_COLS);
+            tc::tmem_relinquish_pair();
+        } else {
+            tc::tmem_alloc(tmem_slot, TMEM_COLS);
+            tc::tmem_relinquish();
+        }
     }
     tc::fence_before_sync();
     __syncthreads();
+    if constexpr (PAIR) tc::cluster_sync(); // the peer's barriers are initialised before any arrive on them
     tc::fence_after_sync();
     const uint32_t tmem = *tmem_slot;
     const int kblocks = p.kh * p.kchunks; // stages per tile: (ky, chunk)
+    // the tile loop: step u of this CTA (or pair) runs tile t = tile_of(u); a pair's odd CTA past the
+    // end (odd tile count) repeats the last tile's loads and stores nothing
+    const uint32_t rank = PAIR ? tc::cluster_ctarank() : 0u;
+    const bool leader = rank == 0;
+    const int u0 = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int ustep = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+    const int nsteps = PAIR ? (p.num_tiles + 1) / 2 : p.num_tiles;
+    auto tile_of = [&](int u) { return PAIR ? 2 * u + (int)rank : u; };
 
     if (warp == 0) {
         if (lane == 0) {
             int stage = 0, issued = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x) {
+            for (int u = u0; u < nsteps && ok; u += ustep) {
+                const int t = min(tile_of(u), p.num_tiles - 1);
                 int img0, y0, x00, img1, y1, x01;
                 half_coords(p, t, 0, img0, y0, x00);
                 half_coords(p, t, 1, img1, y1, x01);
@@ -327,18 +372,35 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         break;
                     }
                     uint8_t *sa = smem + stage * STAGE;
-                    tc::mbar_expect_tx(&full[stage], STAGE);
-                    if (p.halves == 0) {
-                        // input pixels x0 .. x0 + 263 as rows 0 .. 263 (a 128-row and a 136-row box)
-                        tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x00, y0 + ky, img0);
-                        tc::tma_load_4d(sa + BM * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
-                    } else { // a 136-row window per half
-                        tc::tma_load_4d(sa, &tmA2, &full[stage], ch * 64, x00, y0 + ky, img0);
-                        tc::tma_load_4d(sa + HROWS * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
+                    const int wc = (ky * p.kw) * p.cp_in + ch * 64; // the row's first tap, this chunk
+                    if constexpr (PAIR) {
+                        // both CTAs' bytes complete on the even CTA's barrier
+                        const uint32_t fb = tc::mapa(tc::smem_u32(&full[stage]), 0);
+                        if (leader) tc::mbar_expect_tx(&full[stage], 2 * STAGE);
+                        if (p.halves == 0) {
+                            tc::tma_load_4d_pair(sa, &tmA, fb, ch * 64, x00, y0 + ky, img0);
+                            tc::tma_load_4d_pair(sa + BM * 128, &tmA2, fb, ch * 64, x01, y1 + ky, img1);
+                        } else {
+                            tc::tma_load_4d_pair(sa, &tmA2, fb, ch * 64, x00, y0 + ky, img0);
+                            tc::tma_load_4d_pair(sa + HROWS * 128, &tmA2, fb, ch * 64, x01, y1 + ky, img1);
+                        }
+                        for (int kx = 0; kx < p.kw; ++kx)
+                            tc::tma_load_2d_pair(sa + p.a_bytes + kx * B_BYTES, &tmB, fb, wc + kx * p.cp_in,
+                                                 (int)rank * NB);
+                    } else {
+                        tc::mbar_expect_tx(&full[stage], STAGE);
+                        if (p.halves == 0) {
+                            // input pixels x0 .. x0 + 263 as rows 0 .. 263 (a 128-row and a 136-row box)
+                            tc::tma_load_4d(sa, &tmA, &full[stage], ch * 64, x00, y0 + ky, img0);
+                            tc::tma_load_4d(sa + BM * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
+                        } else { // a 136-row window per half
+                            tc::tma_load_4d(sa, &tmA2, &full[stage], ch * 64, x00, y0 + ky, img0);
+                            tc::tma_load_4d(sa + HROWS * 128, &tmA2, &full[stage], ch * 64, x01, y1 + ky, img1);
+                        }
+                        for (int kx = 0; kx < p.kw; ++kx)
+                            tc::tma_load_2d(sa + p.a_bytes + kx * B_BYTES, &tmB, &full[stage], wc + kx * p.cp_in,
+                                            0);
                     }
-                    for (int kx = 0; kx < p.kw; ++kx)
-                        tc::tma_load_2d(sa + p.a_bytes + kx * B_BYTES, &tmB, &full[stage],
-                                        (ky * p.kw + kx) * p.cp_in + ch * 64, 0);
                     ++issued;
                     if (++stage == S) {
                         stage = 0;
@@ -346,10 +408,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                 }
             }
-            if (!ok) {
+            if (!ok && (!PAIR || leader)) {
                 *abort_flag = 1;
                 atomicExch(p.err, 1);
-                // let the copies already issued land before shared memory is released
+                // let the copies already issued land before shared memory is released (a pair's full
+                // barriers, which the odd CTA's copies complete on too, are the even CTA's)
                 int st = stage;
                 uint32_t ph = phase;
                 for (int i = 0; i < S && i < issued; ++i) {
@@ -359,6 +422,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                     tc::mbar_wait(&full[st], ph, zero_flag, 1u << 20);
                 }
+            } else if (!ok) {
+                *abort_flag = 1;
+                atomicExch(p.err, 1);
             }
         }
     } else if (warp == 7) {
@@ -366,7 +432,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             // the tile's layer-below activations, once the epilogue has released the buffer
             int lt = 0, issued = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
+            for (int u = u0; u < nsteps; u += ustep, ++lt) {
+                const int t = min(tile_of(u), p.num_tiles - 1);
                 if (!tc::mbar_wait(yempty, ((uint32_t)lt & 1u) ^ 1u, abort_flag)) {
                     ok = false;
                     break;
@@ -391,20 +458,20 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else if (warp == 1 || warp == 6) {
         // two MMA issuers, one per half: a single thread cannot issue this
         // tile's short MMAs as fast as the tensor core retires them
-        if (lane == 0) {
+        if (lane == 0 && leader) {
             const int h = warp == 6 ? 1 : 0;
             int stage = 0, lt = 0;
             uint32_t phase = 0;
             bool ok = true;
-            for (int t = blockIdx.x; t < p.num_tiles && ok; t += gridDim.x, ++lt) {
-                const int buf = lt & 1;
+            for (int u = u0; u < nsteps && ok; u += ustep, ++lt) {
+                const int acc = 2 * (lt & 1) + h; // accumulator: TMEM buffer lt & 1, half h
                 const uint32_t use = (uint32_t)lt >> 1;
-                if (!tc::mbar_wait(&tempty[buf], (use & 1) ^ 1, abort_flag)) {
+                if (!tc::mbar_wait(&tempty[acc], (use & 1) ^ 1, abort_flag)) {
                     ok = false;
                     break;
                 }
                 tc::fence_after_sync();
-                const uint32_t d = tmem + (2 * buf + h) * ACC_STRIDE;
+                const uint32_t d = tmem + acc * ACC_STRIDE;
                 for (int kb = 0; kb < kblocks; ++kb) {
                     if (!tc::mbar_wait(&full[stage], phase, abort_flag)) {
                         ok = false;
@@ -417,48 +484,71 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const uint64_t a = tc::sdesc_sw128(sa + h * (p.halves ? HROWS : BM) * 128);
                     const uint64_t db = tc::sdesc_sw128(sa + p.a_bytes);
                     const uint32_t first = kb == 0 ? 0u : 1u;
-                    if (p.kw == 3) issue_stage_nk<NP, 3>(nk, d, a, db, first);
-                    else if (p.kw == 2) issue_stage_nk<NP, 2>(nk, d, a, db, first);
-                    else issue_stage_nk<NP, 1>(nk, d, a, db, first);
-                    tc::umma_commit(&empty[stage]);
+                    if (p.kw == 3) issue_stage_nk<NP, PAIR, 3>(nk, d, a, db, first);
+                    else if (p.kw == 2) issue_stage_nk<NP, PAIR, 2>(nk, d, a, db, first);
+                    else issue_stage_nk<NP, PAIR, 1>(nk, d, a, db, first);
+                    if constexpr (PAIR) tc::umma_commit_pair(&empty[stage], 3);
+                    else tc::umma_commit(&empty[stage]);
                     if (++stage == S) {
                         stage = 0;
                         phase ^= 1;
                     }
                 }
-                if (ok) tc::umma_commit(&tfull[buf]);
+                if (ok) {
+                    if constexpr (PAIR) tc::umma_commit_pair(&tfull[acc], 3);
+                    else tc::umma_commit(&tfull[acc]);
+                }
             }
             if (!ok) {
                 *abort_flag = 1;
                 atomicExch(p.err, 1);
             }
             // every MMA of this thread completes before TMEM is released
-            tc::umma_commit(&drain[h]);
+            if constexpr (PAIR) tc::umma_commit_pair(&drain[h], 1);
+            else tc::umma_commit(&drain[h]);
             tc::mbar_wait(&drain[h], 0, zero_flag, 1u << 22);
         }
     } else {
-        const int q = warp & 3; // the TMEM lane quarter this warp may read
+        // eight epilogue warps, two per SM sub-partition: warps 2..5 empty half 0's accumulator, warps 8..11
+        // half 1's, each warp the TMEM lane quarter warp % 4 (one output pixel per thread)
+        const int h = warp >= 8 ? 1 : 0;
+        const int q = warp & 3;
         const int row = q * 32 + lane;
+        float *wacc = sacc + (4 * h + q) * NP; // this warp's row of the mode 4 bias sums
+        const uint32_t tempty_c = PAIR ? tc::mapa(tc::smem_u32(&tempty[0]), 0) : 0u;
         int lt = 0;
-        for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
-            const int buf = lt & 1;
+        for (int u = u0; u < nsteps; u += ustep, ++lt) {
+            const bool tile_ok = tile_of(u) < p.num_tiles;
+            const int t = min(tile_of(u), p.num_tiles - 1);
+            const int acc = 2 * (lt & 1) + h; // accumulator: TMEM buffer lt & 1, half h
             const uint32_t use = (uint32_t)lt >> 1;
             int ok = 1;
-            if (lane == 0) ok = tc::mbar_wait(&tfull[buf], use & 1, abort_flag) ? 1 : 0;
+            if (lane == 0) ok = tc::mbar_wait(&tfull[acc], use & 1, abort_flag) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
-            __syncwarp();
             if (!ok) {
                 *abort_flag = 1;
                 atomicExch(p.err, 1);
                 break;
             }
             tc::fence_after_sync();
-            int himg[2], hy[2], hx0[2];
-            bool hok[2];
-            hok[0] = half_coords(p, t, 0, himg[0], hy[0], hx0[0]);
-            hok[1] = half_coords(p, t, 1, himg[1], hy[1], hx0[1]);
+            // hand the accumulator back to its issuer (a pair's barriers are the even CTA's): one arrive
+            // per warp once every lane's TMEM reads are done
+            auto release = [&]() {
+                tc::fence_before_sync();
+                __syncwarp();
+                if (lane == 0) {
+                    if constexpr (PAIR) tc::mbar_arrive_cluster(tempty_c + 8u * (uint32_t)acc);
+                    else tc::mbar_arrive(&tempty[acc]);
+                }
+            };
+            int img, y, x0;
+            const bool hok = half_coords(p, t, h, img, y, x0) && tile_ok;
+            const int x = x0 + row;
+            const bool valid = hok && x < p.Wo;
+            const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + acc * ACC_STRIDE;
+            const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
             if (p.mode == 4) {
-                uint4 ya[NP / 16][2], yb[NP / 16][2];
+                uint4 ya[NP / 16][2];
                 if (p.ysm) {
                     int got = 1;
                     if (lane == 0) got = tc::mbar_wait(yfull, (uint32_t)lt & 1u, abort_flag) ? 1 : 0;
@@ -468,150 +558,126 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         atomicExch(p.err, 1);
                         break;
                     }
-                    load_dz_y_smem<NP>(ybuf, p.y_boxes, 0, row, ya);
-                    load_dz_y_smem<NP>(ybuf, p.y_boxes, 1, row, yb);
-                    tc::mbar_arrive(yempty); // the buffer may take the next tile's activations
+                    load_dz_y_smem<NP>(ybuf, p.y_boxes, h, row, ya);
+                    __syncwarp();
+                    if (lane == 0) tc::mbar_arrive(yempty); // the buffer may take the next tile's activations
                 } else {
-                    load_dz_y<NP>(p, hok[0] && hx0[0] + row < p.Wo, himg[0], hy[0], hx0[0] + row, ya);
-                    load_dz_y<NP>(p, hok[1] && hx0[1] + row < p.Wo, himg[1], hy[1], hx0[1] + row, yb);
+                    load_dz_y<NP>(p, valid, img, y, x, ya);
                 }
-                const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf) * ACC_STRIDE;
-                bool vh[2];
-                size_t ph[2], qh[2];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int x = hx0[h] + row;
-                    vh[h] = hok[h] && x < p.Wo;
-                    ph[h] = ((size_t)himg[h] * p.Ho + hy[h]) * p.Wo + x;
-                    qh[h] = ((size_t)himg[h] * (p.Ho + 2 * p.o16_ph) + hy[h] + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x +
-                            p.o16_pw;
-                }
-                epilogue_dz<NP>(p, tq, vh, ph, qh, q, lane, sacc, ya, yb);
-                tc::fence_before_sync();
-                tc::mbar_arrive(&tempty[buf]);
+                const size_t q16 =
+                    ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
+                epilogue_dz<NP>(p, ta, valid, pix, q16, lane, wacc, ya);
+                release();
                 continue;
             }
-            float hv0[2] = {0.0f, 0.0f}, hv1[2] = {0.0f, 0.0f};
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int img = himg[h], y = hy[h], x = hx0[h] + row;
-                const bool valid = hok[h] && x < p.Wo;
-                const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + (2 * buf + h) * ACC_STRIDE;
-                float v[16];
-                // the TMEM reads are warp-collective: every lane runs them
-                float sc = 1.0f;
-                if (p.mode == 1) { // pass 1: squared norm of tanh(acc + bias)
-                    float s2 = 0.0f;
-#pragma unroll 1
-                    for (int c = 0; c < NP / 16; ++c) {
-                        tc::tmem_ld16(ta + c * 16, v);
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            const float f = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
-                            s2 = fmaf(f, f, s2);
-                        }
-                    }
-                    sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
-                }
-                const size_t pix = ((size_t)img * p.Ho + y) * p.Wo + x;
-                __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
-                float a0 = 0.0f, a1 = 0.0f;
+            // the TMEM reads are warp-collective: every lane runs them
+            float v[16];
+            float sc = 1.0f;
+            if (p.mode == 1) { // pass 1: squared norm of tanh(acc + bias)
+                float s2 = 0.0f;
 #pragma unroll 1
                 for (int c = 0; c < NP / 16; ++c) {
                     tc::tmem_ld16(ta + c * 16, v);
-                    if (p.mode == 3) {
-                        if (valid) {
-                            float *o = (float *)p.out + pix * p.cp_out + c * 16;
 #pragma unroll
-                            for (int g = 0; g < 4; ++g) {
-                                if (c * 16 + 4 * g + 3 < p.cout)
-                                    *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2],
-                                                                         v[4 * g + 3]);
-                                else
-#pragma unroll
-                                    for (int j = 0; j < 4; ++j)
-                                        if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
-                            }
-                        }
-                        continue;
-                    }
-#pragma unroll
-                    for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
-                    if (p.mode == 2) {
-#pragma unroll
-                        for (int j = 0; j < 16; ++j) {
-                            a0 = fmaf(v[j], shead[c * 16 + j], a0);
-                            a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
-                        }
-                        if (p.out16 && valid) { // the tanh outputs too (a training step's backward reads them)
-                            uint32_t u[8];
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                                u[j] = *(uint32_t *)&b2;
-                            }
-                            uint4 *d2 = (uint4 *)(p.out16 + pix * p.o16_cs + c * 16);
-                            d2[0] = make_uint4(u[0], u[1], u[2], u[3]);
-                            d2[1] = make_uint4(u[4], u[5], u[6], u[7]);
-                        }
-                    } else if (valid) {
-                        uint32_t u[8];
-#pragma unroll
-                        for (int j = 0; j < 8; ++j) {
-                            __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
-                            u[j] = *(uint32_t *)&b2;
-                        }
-                        uint4 *dst = (uint4 *)(o16 + c * 16);
-                        dst[0] = make_uint4(u[0], u[1], u[2], u[3]);
-                        dst[1] = make_uint4(u[4], u[5], u[6], u[7]);
-                        if (p.mode == 1 && p.out16) { // the features before the normalisation too
-#pragma unroll
-                            for (int j = 0; j < 8; ++j) {
-                                __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
-                                u[j] = *(uint32_t *)&b2;
-                            }
-                            uint4 *d2 = (uint4 *)(p.out16 + pix * p.o16_cs + c * 16);
-                            d2[0] = make_uint4(u[0], u[1], u[2], u[3]);
-                            d2[1] = make_uint4(u[4], u[5], u[6], u[7]);
-                        }
+                    for (int j = 0; j < 16; ++j) {
+                        const float f = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                        s2 = fmaf(f, f, s2);
                     }
                 }
-                hv0[h] = a0;
-                hv1[h] = a1;
+                sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
             }
-            tc::fence_before_sync();
-            tc::mbar_arrive(&tempty[buf]);
-            if (p.mode == 2) {
-                const size_t plane = (size_t)p.Ho * p.Wo;
+            __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
+            float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll 1
+            for (int c = 0; c < NP / 16; ++c) {
+                tc::tmem_ld16(ta + c * 16, v);
+                if (c == NP / 16 - 1) release(); // the accumulator's last read
+                if (p.mode == 3) {
+                    if (valid) {
+                        float *o = (float *)p.out + pix * p.cp_out + c * 16;
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    float *o = (float *)p.out + (size_t)himg[h] * 2 * plane; // [img][2][Ho][Wo]
-                    const int x = hx0[h] + row;
-                    if (hok[h] && x < p.Wo) {
-                        o[(size_t)hy[h] * p.Wo + x] = fabsf(hv0[h]);
-                        o[plane + (size_t)hy[h] * p.Wo + x] = fabsf(hv1[h]);
+                        for (int g = 0; g < 4; ++g) {
+                            if (c * 16 + 4 * g + 3 < p.cout)
+                                *(float4 *)(o + 4 * g) = make_float4(v[4 * g], v[4 * g + 1], v[4 * g + 2],
+                                                                     v[4 * g + 3]);
+                            else
+#pragma unroll
+                                for (int j = 0; j < 4; ++j)
+                                    if (c * 16 + 4 * g + j < p.cout) o[4 * g + j] = v[4 * g + j];
+                        }
                     }
+                    continue;
                 }
+#pragma unroll
+                for (int j = 0; j < 16; ++j) v[j] = tc::tanh_fast(v[j] + sbias[c * 16 + j]);
+                if (p.mode == 2) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        a0 = fmaf(v[j], shead[c * 16 + j], a0);
+                        a1 = fmaf(v[j], shead[NP + c * 16 + j], a1);
+                    }
+                    if (p.out16 && valid) // the tanh outputs too (a training step's backward reads them)
+                        store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
+                } else if (valid) {
+                    store_bf16_16(o16 + c * 16, v, sc);
+                    if (p.mode == 1 && p.out16) // the features before the normalisation too
+                        store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
+                }
+            }
+            if (p.mode == 2 && valid) { // [img][2][Ho][Wo]
+                const size_t plane = (size_t)p.Ho * p.Wo;
+                float *o = (float *)p.out + (size_t)img * 2 * plane;
+                o[(size_t)y * p.Wo + x] = fabsf(a0);
+                o[plane + (size_t)y * p.Wo + x] = fabsf(a1);
             }
         }
     }
     __syncthreads();
-    if (p.bias_part) // this CTA's four partial sums per channel
-        for (int i = threadIdx.x; i < 4 * p.cout; i += NUM_THREADS)
-            p.bias_part[((size_t)blockIdx.x * 4 + i / p.cout) * p.cout + i % p.cout] =
+    if (p.bias_part) // this CTA's eight partial sums per channel (one per epilogue warp)
+        for (int i = threadIdx.x; i < 8 * p.cout; i += NUM_THREADS)
+            p.bias_part[((size_t)blockIdx.x * 8 + i / p.cout) * p.cout + i % p.cout] =
                 sacc[(i / p.cout) * NP + i % p.cout];
+    if constexpr (PAIR) tc::cluster_sync(); // neither CTA leaves while the other may use its memory
     if (warp == 1) {
         tc::fence_after_sync();
-        tc::tmem_dealloc(tmem, TMEM_COLS);
+        if constexpr (PAIR) tc::tmem_dealloc_pair(tmem, TMEM_COLS);
+        else tc::tmem_dealloc(tmem, TMEM_COLS);
     }
 }
 
-template <int NP> int stage_bytes(int a_bytes, int kw) { return a_bytes + kw * NP * 128; }
+// NB: the weight rows a CTA stages per tap (NP, or NP / 2 in a pair)
+inline int stage_bytes(int a_bytes, int kw, int NB) { return a_bytes + kw * NB * 128; }
 
-template <int NP> size_t smem_bytes(int stages, int a_bytes, int kw, int mode, int ybytes = 0)
+inline size_t smem_bytes(int NP, int NB, int stages, int a_bytes, int kw, int mode, int ybytes = 0)
 {
-    return 1024 + (size_t)stages * stage_bytes<NP>(a_bytes, kw) + ybytes + (2 * stages + 8) * 8 + 16 +
-           (mode == 4 ? 7 : (mode == 2 ? 3 : 1)) * NP * 4;
+    return 1024 + (size_t)stages * stage_bytes(a_bytes, kw, NB) + ybytes + (2 * stages + 12) * 8 + 16 +
+           (mode == 4 ? 11 : (mode == 2 ? 3 : 1)) * NP * 4;
+}
+
+std::atomic<int> g_pairs{1}; // CTA pairs (cta_group::2) where the device can co-schedule them
+
+// Co-resident 2-CTA clusters of k_conv_tc<NP, true> at `smem` bytes per CTA (0: none), cached per size.
+template <int NP> int pair_clusters(size_t smem)
+{
+    static std::mutex mu;
+    static std::map<size_t, int> cache;
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(smem);
+    if (it != cache.end()) return it->second;
+    int n = 0;
+    if (cudaFuncSetAttribute(k_conv_tc<NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) ==
+        cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2, at[0].val.clusterDim.y = 1, at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(2, 1, 1), cfg.blockDim = dim3(NUM_THREADS, 1, 1), cfg.dynamicSmemBytes = smem;
+        cfg.attrs = at, cfg.numAttrs = 1;
+        if (cudaOccupancyMaxActiveClusters(&n, (void *)k_conv_tc<NP, true>, &cfg) != cudaSuccess) n = 0;
+    }
+    cudaGetLastError(); // a refused query leaves no sticky error: the single-CTA kernel runs instead
+    cache[smem] = n;
+    return n;
 }
 
 template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
@@ -632,24 +698,35 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     r = enc(&ma2, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)a.in, gA, sA, bA2, eA, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation tensor map (%d)", (int)r);
-    const int taps = a.kh * a.kw;
-    cuuint64_t gB[2] = {(cuuint64_t)taps * a.cp_in, (cuuint64_t)NP};
-    cuuint64_t sB[1] = {(cuuint64_t)taps * a.cp_in * 2};
-    cuuint32_t bB[2] = {64, (cuuint32_t)NP};
-    cuuint32_t eB[2] = {1, 1};
-    r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)a.wt, gB, sB, bB, eB, CU_TENSOR_MAP_INTERLEAVE_NONE,
-            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: weight tensor map (%d)", (int)r);
     int dev = 0, sms = 0, maxsm = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    p.stage_bytes = stage_bytes<NP>(p.a_bytes, a.kw);
     // mode 4: the layer-below activations through shared memory when the buffer fits beside two stages
     // (their global loads stalled the epilogue more than a third stage gains)
     p.y_boxes = (NP + 63) / 64;
     const int ybytes = 2 * p.y_boxes * Y_BOX;
-    p.ysm = a.mode == 4 && smem_bytes<NP>(2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
+    // CTA pairs when there are two tiles to pair and the device co-schedules the clusters
+    bool pair = g_pairs.load() != 0 && p.num_tiles >= 2;
+    int nclusters = 0;
+    if (pair) {
+        const int ysm = a.mode == 4 && smem_bytes(NP, NP / 2, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm;
+        int s = MAX_STAGES;
+        while (s > 2 && smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, ysm ? ybytes : 0) > (size_t)maxsm) --s;
+        nclusters = pair_clusters<NP>(smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, ysm ? ybytes : 0));
+        pair = nclusters > 0;
+    }
+    const int NB = pair ? NP / 2 : NP;
+    const int taps = a.kh * a.kw;
+    cuuint64_t gB[2] = {(cuuint64_t)taps * a.cp_in, (cuuint64_t)NP};
+    cuuint64_t sB[1] = {(cuuint64_t)taps * a.cp_in * 2};
+    cuuint32_t bB[2] = {64, (cuuint32_t)NB};
+    cuuint32_t eB[2] = {1, 1};
+    r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)a.wt, gB, sB, bB, eB, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: weight tensor map (%d)", (int)r);
+    p.stage_bytes = stage_bytes(p.a_bytes, a.kw, NB);
+    p.ysm = a.mode == 4 && smem_bytes(NP, NB, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
     CUtensorMap my = ma; // unused unless ysm
     if (p.ysm) {
         cuuint64_t gY[4] = {(cuuint64_t)a.aux_cs, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)a.n_img};
@@ -663,21 +740,41 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     const int yb = p.ysm ? ybytes : 0;
     p.stages = 0;
     for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
-        if (smem_bytes<NP>(s, p.a_bytes, a.kw, a.mode, yb) <= (size_t)maxsm) p.stages = s;
+        if (smem_bytes(NP, NB, s, p.a_bytes, a.kw, a.mode, yb) <= (size_t)maxsm) p.stages = s;
     if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
-    const size_t smem = smem_bytes<NP>(p.stages, p.a_bytes, a.kw, a.mode, yb);
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    int grid = std::min(p.num_tiles, sms);
-    if (a.bias_splits) *a.bias_splits = 4 * grid;
-    {
-        CNNCRF_PROF("conv_tc", st);
-        k_conv_tc<NP><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, my, p);
+    const size_t smem = smem_bytes(NP, NB, p.stages, p.a_bytes, a.kw, a.mode, yb);
+    if (pair) {
+        // one cluster per pair of co-resident SMs, each running tile pairs until the list ends
+        const int grid = 2 * std::min(nclusters, (p.num_tiles + 1) / 2);
+        if (a.bias_splits) *a.bias_splits = 8 * grid;
+        CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = 2, at[0].val.clusterDim.y = 1, at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3(grid, 1, 1), cfg.blockDim = dim3(NUM_THREADS, 1, 1), cfg.dynamicSmemBytes = smem;
+        cfg.stream = st, cfg.attrs = at, cfg.numAttrs = 1;
+        {
+            CNNCRF_PROF("conv_tc", st);
+            CNNCRF_CUDA(cudaLaunchKernelEx(&cfg, k_conv_tc<NP, true>, ma, ma2, mb, my, (const TcParams)p));
+        }
+    } else {
+        const int grid = std::min(p.num_tiles, sms);
+        if (a.bias_splits) *a.bias_splits = 8 * grid;
+        CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            CNNCRF_PROF("conv_tc", st);
+            k_conv_tc<NP, false><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, my, p);
+        }
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
 }
 
 } // namespace
+
+void conv_tc_set_pairs(bool on) { g_pairs.store(on ? 1 : 0); }
+bool conv_tc_pairs() { return g_pairs.load() != 0; }
 
 int conv_tc(const TcConvArgs &a, cudaStream_t st)
 {

@@ -67,11 +67,14 @@ struct TcConvArgs {
     void *out16 = nullptr;
     int aux_cs = 0, o16_cs = 0, o16_ph = 0, o16_pw = 0;
     // mode 4, optional: out (FP32) may be null; bias_part = the per-channel sums of the output, one row
-    // of cout floats per (CTA, epilogue warp), *bias_splits = their number (at most 4 x SMs)
+    // of cout floats per (CTA, epilogue warp), *bias_splits = their number (at most 8 x SMs)
     float *bias_part = nullptr;
     int *bias_splits = nullptr;
 };
 int conv_tc(const TcConvArgs &a, cudaStream_t st);
+// 2-CTA pairs (cta_group::2) for conv_tc where the device co-schedules them (default on)
+void conv_tc_set_pairs(bool on);
+bool conv_tc_pairs();
 
 // ------------------------------------------------------------ correlation
 // raw correlation (+ unary: -1 none, 0 -softmax, 1 one-minus) of NHWC FP32

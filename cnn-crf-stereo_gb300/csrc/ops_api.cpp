@@ -25,6 +25,19 @@ struct cnncrf_slackprop {
 
 extern "C" {
 
+int cnncrf_set_conv_pairs(int enable)
+{
+    k::conv_tc_set_pairs(enable != 0);
+    return CNNCRF_OK;
+}
+
+int cnncrf_get_conv_pairs(int *enable)
+{
+    if (!enable) return fail(CNNCRF_EINVAL, "null argument");
+    *enable = k::conv_tc_pairs() ? 1 : 0;
+    return CNNCRF_OK;
+}
+
 // StereoCorrelation::forward static entry (stereo/operators/stereocorrelation.cpp:146-152)
 int cnncrf_correlation_forward(const float *d_input0, const float *d_input1, const float *h_disparities,
                                float *d_output, int n, int c, int h, int w, int num_disps,

@@ -268,7 +268,7 @@ int cnncrf_train::build()
         int dev = 0, sms = 0;
         CNNCRF_CUDA(cudaGetDevice(&dev));
         CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        CNNCRF_TRY(bpart.reserve(sizeof(float) * 4 * (size_t)sms * 128));
+        CNNCRF_TRY(bpart.reserve(sizeof(float) * 8 * (size_t)sms * 128)); // conv_tc: 8 rows per CTA
     }
     const int ns = k::train_wgrad_splits(Pmax); // the most bias splits any layer uses
     CNNCRF_TRY(part.reserve(sizeof(float) * part_floats));

@@ -86,6 +86,15 @@ const char *cnncrf_last_error(void);
 /* Library ABI version (CNNCRF_ABI_VERSION). */
 int cnncrf_abi_version(void);
 
+/* The BF16 path's tensor-core convolutions (layers 2..L, the pairwise net's
+   second layer, a training step's input gradients) as 2-CTA pairs whose MMAs
+   span both SMs (tcgen05 cta_group::2): on by default where the device
+   co-schedules the clusters.  0 runs them on single CTAs.  Process-wide.  The
+   two forms differ at most in FP32 summation order.  No reference
+   counterpart (a GB300 execution choice). */
+int cnncrf_set_conv_pairs(int enable);
+int cnncrf_get_conv_pairs(int *enable);
+
 /* ---------------------------------------------------------------- StereoNet */
 
 typedef struct cnncrf_net *cnncrf_net_t;
