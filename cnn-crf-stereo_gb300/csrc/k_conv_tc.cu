@@ -69,6 +69,7 @@ constexpr int Y_BOX = 64 * BM * 2;      // one 64-channel x 128-pixel box of the
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t ACC_STRIDE = 128;    // columns per accumulator (>= NP)
 constexpr int MAX_STAGES = 4;
+constexpr int OBUF = 32 * 128;          // an epilogue warp's output staging: 32 pixels x 64 BF16 channels
 
 struct TcParams {
     int n_img, Hin, Win, Ho, Wo, kh, kw, cp_in, kchunks, kk_last, cout, cp_out, tiles_x, num_tiles, mode,
@@ -84,6 +85,7 @@ struct TcParams {
     int aux_cs, o16_cs, o16_ph, o16_pw;
     float *bias_part;         // mode 4 (optional): [gridDim.x * 8][cout] channel sums of the output
     int ysm, y_boxes;         // mode 4: aux through the shared buffer (y_boxes per half), else global loads
+    int ostage;               // mode 0: the output through shared memory and TMA stores (64-channel boxes)
 };
 
 // Output pixel coordinates of half h of tile t; false if the half is past
@@ -282,7 +284,8 @@ __device__ __forceinline__ void issue_stage_nk(int nk, uint32_t d, uint64_t a, u
 template <int NP, bool PAIR>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_conv_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmA2,
-              const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmY, const TcParams p)
+              const __grid_constant__ CUtensorMap tmB, const __grid_constant__ CUtensorMap tmY,
+              const __grid_constant__ CUtensorMap tmO, const TcParams p)
 {
     constexpr int NB = PAIR ? NP / 2 : NP; // weight rows (output channels) this CTA stages per tap
     constexpr int B_BYTES = NB * 128;      // one tap's 64-channel weight box
@@ -291,7 +294,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int S = p.stages;
     const int STAGE = p.stage_bytes;
     uint8_t *ybuf = smem + S * STAGE; // mode 4 with ysm: [2 halves][y_boxes][Y_BOX]
-    uint64_t *full = (uint64_t *)(ybuf + (p.ysm ? 2 * p.y_boxes * Y_BOX : 0));
+    uint8_t *obuf = ybuf + (p.ysm ? 2 * p.y_boxes * Y_BOX : 0); // ostage: [8 epilogue warps][OBUF]
+    uint64_t *full = (uint64_t *)(obuf + (p.ostage ? 8 * OBUF : 0));
     uint64_t *empty = full + S;
     uint64_t *tfull = empty + S;  // [buffer][half]
     uint64_t *tempty = tfull + 4; // [buffer][half]
@@ -325,6 +329,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         tc::prefetch_tmap(&tmA2);
         tc::prefetch_tmap(&tmB);
         if (p.ysm) tc::prefetch_tmap(&tmY);
+        if (p.ostage) tc::prefetch_tmap(&tmO);
     }
     for (int i = threadIdx.x; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
     if (p.mode == 2)
@@ -587,6 +592,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 sc = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
             }
             __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
+            // mode 0 through shared memory: the warp's 32 pixels x 64 channels per TMA store, in the 128-byte
+            // swizzle (16-byte unit j of pixel row r at unit j ^ (r & 7)), so every store is a whole box
+            uint8_t *obw = obuf + (4 * h + q) * OBUF, *ob = obw + lane * 128;
+            const bool tstore = p.ostage && p.mode == 0;
+            if (tstore) { // the previous tile's last store has read the buffer
+                if (lane == 0) tc::bulk_wait_read0();
+                __syncwarp();
+            }
             float a0 = 0.0f, a1 = 0.0f;
 #pragma unroll 1
             for (int c = 0; c < NP / 16; ++c) {
@@ -618,6 +631,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                     if (p.out16 && valid) // the tanh outputs too (a training step's backward reads them)
                         store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
+                } else if (tstore) {
+                    const int j0 = 2 * (c & 3), sw = lane & 7;
+                    uint32_t u[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                        u[j] = *(uint32_t *)&b2;
+                    }
+                    *(uint4 *)(ob + ((j0 ^ sw) << 4)) = make_uint4(u[0], u[1], u[2], u[3]);
+                    *(uint4 *)(ob + (((j0 + 1) ^ sw) << 4)) = make_uint4(u[4], u[5], u[6], u[7]);
+                    if ((c & 3) == 3 || c == NP / 16 - 1) { // the box is complete
+                        for (int j = j0 + 2; j < 8; ++j) // the padding channels past NP read as zero
+                            *(uint4 *)(ob + ((j ^ sw) << 4)) = make_uint4(0u, 0u, 0u, 0u);
+                        tc::fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0 && hok && x0 + q * 32 < p.Wo) {
+                            tc::tma_store_4d(&tmO, obw, 64 * (c >> 2), x0 + q * 32, y, img); // (x >= Wo: clipped)
+                            tc::bulk_commit();
+                        }
+                        if (c != NP / 16 - 1) { // the next box reuses the buffer
+                            if (lane == 0) tc::bulk_wait_read0();
+                            __syncwarp();
+                        }
+                    }
                 } else if (valid) {
                     store_bf16_16(o16 + c * 16, v, sc);
                     if (p.mode == 1 && p.out16) // the features before the normalisation too
@@ -631,6 +668,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 o[plane + (size_t)y * p.Wo + x] = fabsf(a1);
             }
         }
+        if (p.ostage && lane == 0) tc::bulk_wait0(); // the warp's stores are done before its buffer goes
     }
     __syncthreads();
     if (p.bias_part) // this CTA's eight partial sums per channel (one per epilogue warp)
@@ -706,14 +744,29 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     // (their global loads stalled the epilogue more than a third stage gains)
     p.y_boxes = (NP + 63) / 64;
     const int ybytes = 2 * p.y_boxes * Y_BOX;
+    // mode 0: the output through shared memory and TMA stores when whole 64-channel boxes fit the row
+    p.ostage = a.mode == 0 && a.cp_out % 8 == 0 && a.cp_out >= 64 * ((NP + 63) / 64) ? 1 : 0;
+    const int obytes = p.ostage ? 8 * OBUF : 0;
+    CUtensorMap mo = ma; // unused unless ostage
+    if (p.ostage) {
+        cuuint64_t gO[4] = {(cuuint64_t)a.cp_out, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)a.n_img};
+        cuuint64_t sO[3] = {(cuuint64_t)a.cp_out * 2, (cuuint64_t)p.Wo * a.cp_out * 2,
+                            (cuuint64_t)p.Ho * p.Wo * a.cp_out * 2};
+        cuuint32_t bO[4] = {64, 32, 1, 1}, eO[4] = {1, 1, 1, 1};
+        CUresult ro = enc(&mo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, a.out, gO, sO, bO, eO,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (ro != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: output tensor map (%d)", (int)ro);
+    }
     // CTA pairs when there are two tiles to pair and the device co-schedules the clusters
     bool pair = g_pairs.load() != 0 && p.num_tiles >= 2;
     int nclusters = 0;
     if (pair) {
         const int ysm = a.mode == 4 && smem_bytes(NP, NP / 2, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm;
+        const int extra = (ysm ? ybytes : 0) + obytes;
         int s = MAX_STAGES;
-        while (s > 2 && smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, ysm ? ybytes : 0) > (size_t)maxsm) --s;
-        nclusters = pair_clusters<NP>(smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, ysm ? ybytes : 0));
+        while (s > 2 && smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, extra) > (size_t)maxsm) --s;
+        nclusters = pair_clusters<NP>(smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, extra));
         pair = nclusters > 0;
     }
     const int NB = pair ? NP / 2 : NP;
@@ -737,7 +790,7 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation (mode 4) tensor map (%d)", (int)r);
     }
-    const int yb = p.ysm ? ybytes : 0;
+    const int yb = (p.ysm ? ybytes : 0) + obytes;
     p.stages = 0;
     for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
         if (smem_bytes(NP, NB, s, p.a_bytes, a.kw, a.mode, yb) <= (size_t)maxsm) p.stages = s;
@@ -756,7 +809,7 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
         cfg.stream = st, cfg.attrs = at, cfg.numAttrs = 1;
         {
             CNNCRF_PROF("conv_tc", st);
-            CNNCRF_CUDA(cudaLaunchKernelEx(&cfg, k_conv_tc<NP, true>, ma, ma2, mb, my, (const TcParams)p));
+            CNNCRF_CUDA(cudaLaunchKernelEx(&cfg, k_conv_tc<NP, true>, ma, ma2, mb, my, mo, (const TcParams)p));
         }
     } else {
         const int grid = std::min(p.num_tiles, sms);
@@ -764,7 +817,7 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
         CNNCRF_CUDA(cudaFuncSetAttribute(k_conv_tc<NP, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         {
             CNNCRF_PROF("conv_tc", st);
-            k_conv_tc<NP, false><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, my, p);
+            k_conv_tc<NP, false><<<grid, NUM_THREADS, smem, st>>>(ma, ma2, mb, my, mo, p);
         }
     }
     CNNCRF_CHECK_LAUNCH();
