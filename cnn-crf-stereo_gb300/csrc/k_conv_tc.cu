@@ -142,12 +142,50 @@ __device__ __forceinline__ void load_dz_y_smem(const uint8_t *ybuf, int y_boxes,
     }
 }
 
+__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
+
+// An epilogue warp's output staged for TMA stores: 32 pixel rows x 64 BF16
+// channels in the 128-byte swizzle (16-byte unit j of row r at unit j ^ (r & 7)),
+// so that every store is one whole box instead of 32 scattered pixel rows.
+struct OStage {
+    const CUtensorMap *map;
+    uint8_t *base; // the warp's buffer (1024-byte aligned)
+    bool store;    // false: the warp's pixels lie outside the tensor, nothing is stored
+    int x, y, img; // the warp's first pixel in the map's coordinates (pixels past the tensor are clipped)
+};
+
+// BF16 chunk c (16 channels) of this lane's pixel into the buffer; after a
+// box's last chunk (or chunk NC - 1) the channels past it are zeroed and the
+// box goes out by one TMA store.  Warp-collective.  The caller waits for the
+// buffer's previous stores to have read it before chunk 0.
+template <int NC>
+__device__ __forceinline__ void ostage_put(const OStage &o, int lane, int c, const uint32_t (&u)[8])
+{
+    uint8_t *row = o.base + lane * 128;
+    const int j0 = 2 * (c & 3), sw = lane & 7;
+    *(uint4 *)(row + ((j0 ^ sw) << 4)) = make_uint4(u[0], u[1], u[2], u[3]);
+    *(uint4 *)(row + (((j0 + 1) ^ sw) << 4)) = make_uint4(u[4], u[5], u[6], u[7]);
+    if ((c & 3) == 3 || c == NC - 1) {
+        for (int j = j0 + 2; j < 8; ++j) *(uint4 *)(row + ((j ^ sw) << 4)) = make_uint4(0u, 0u, 0u, 0u);
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0 && o.store) {
+            tc::tma_store_4d(o.map, o.base, 64 * (c >> 2), o.x, o.y, o.img);
+            tc::bulk_commit();
+        }
+        if (c != NC - 1) { // the next box reuses the buffer
+            if (lane == 0) tc::bulk_wait_read0();
+            __syncwarp();
+        }
+    }
+}
+
 // One half's chunk c of mode 4: the sums times 1 - y^2 into v (zero for an
 // invalid pixel, so it adds nothing to the bias sums), stored as BF16 into the
 // padded copy (and as FP32 if p.out).
 template <int NP>
 __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, bool valid, size_t pix, size_t q16,
-                                         const uint4 (&yc)[2], float (&v)[16])
+                                         const uint4 (&yc)[2], float (&v)[16], const OStage *os)
 {
     tc::tmem_ld16(ta + c * 16, v); // warp-collective
     const uint32_t yw[8] = {yc[0].x, yc[0].y, yc[0].z, yc[0].w, yc[1].x, yc[1].y, yc[1].z, yc[1].w};
@@ -157,16 +195,20 @@ __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, 
         v[2 * j] = valid ? v[2 * j] * (1.0f - a * a) : 0.0f;
         v[2 * j + 1] = valid ? v[2 * j + 1] * (1.0f - b * b) : 0.0f;
     }
-    if (!valid) return;
     uint32_t u[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
         __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
         u[j] = *(uint32_t *)&b2;
     }
-    uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
-    d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
-    d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
+    if (os) { // (warp-collective; an invalid pixel's zeros land in the border or past the tensor)
+        ostage_put<NP / 16>(*os, lane_id(), c, u);
+    } else if (valid) {
+        uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
+        d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
+        d16[1] = make_uint4(u[4], u[5], u[6], u[7]);
+    }
+    if (!valid) return;
     if (p.out) {
         float *o = (float *)p.out + pix * p.cp_out + c * 16;
 #pragma unroll
@@ -186,13 +228,13 @@ __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, 
 // activations), adding the warp's per-channel sums into wacc.
 template <int NP>
 __device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta, bool valid, size_t pix, size_t q16,
-                                            int lane, float *wacc, const uint4 (*ya)[2])
+                                            int lane, float *wacc, const uint4 (*ya)[2], const OStage *os)
 {
     constexpr int NC = NP / 16;
 #pragma unroll
     for (int c = 0; c < NC; ++c) {
         float v[16];
-        dz_chunk<NP>(p, ta, c, valid, pix, q16, ya[c], v);
+        dz_chunk<NP>(p, ta, c, valid, pix, q16, ya[c], v, os);
         if (p.bias_part) {
             // the warp's 32 pixels summed per channel: each exchange halves the values a lane keeps;
             // lane L ends with channel c * 16 + (L >> 1), twice
@@ -520,6 +562,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         const int q = warp & 3;
         const int row = q * 32 + lane;
         float *wacc = sacc + (4 * h + q) * NP; // this warp's row of the mode 4 bias sums
+        uint8_t *obw = obuf + (4 * h + q) * OBUF; // this warp's output staging (ostage)
         const uint32_t tempty_c = PAIR ? tc::mapa(tc::smem_u32(&tempty[0]), 0) : 0u;
         int lt = 0;
         for (int u = u0; u < nsteps; u += ustep, ++lt) {
@@ -571,7 +614,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 }
                 const size_t q16 =
                     ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
-                epilogue_dz<NP>(p, ta, valid, pix, q16, lane, wacc, ya);
+                // the padded copy through the staging buffer: boxes at (x + o16_pw, y + o16_ph) of the padded
+                // tensor (a pixel past Wo holds zeros, which is what the border holds)
+                const OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32 + p.o16_pw, y + p.o16_ph, img};
+                if (p.ostage) {
+                    if (lane == 0) tc::bulk_wait_read0();
+                    __syncwarp();
+                }
+                epilogue_dz<NP>(p, ta, valid, pix, q16, lane, wacc, ya, p.ostage ? &os : nullptr);
                 release();
                 continue;
             }
@@ -594,8 +644,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             __nv_bfloat16 *o16 = (__nv_bfloat16 *)p.out + pix * p.cp_out;
             // mode 0 through shared memory: the warp's 32 pixels x 64 channels per TMA store, in the 128-byte
             // swizzle (16-byte unit j of pixel row r at unit j ^ (r & 7)), so every store is a whole box
-            uint8_t *obw = obuf + (4 * h + q) * OBUF, *ob = obw + lane * 128;
-            const bool tstore = p.ostage && p.mode == 0;
+            const bool tstore = p.ostage && (p.mode == 0 || p.mode == 1);
+            const OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32, y, img};
             if (tstore) { // the previous tile's last store has read the buffer
                 if (lane == 0) tc::bulk_wait_read0();
                 __syncwarp();
@@ -632,29 +682,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     if (p.out16 && valid) // the tanh outputs too (a training step's backward reads them)
                         store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
                 } else if (tstore) {
-                    const int j0 = 2 * (c & 3), sw = lane & 7;
                     uint32_t u[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j) {
-                        __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+                        __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
                         u[j] = *(uint32_t *)&b2;
                     }
-                    *(uint4 *)(ob + ((j0 ^ sw) << 4)) = make_uint4(u[0], u[1], u[2], u[3]);
-                    *(uint4 *)(ob + (((j0 + 1) ^ sw) << 4)) = make_uint4(u[4], u[5], u[6], u[7]);
-                    if ((c & 3) == 3 || c == NP / 16 - 1) { // the box is complete
-                        for (int j = j0 + 2; j < 8; ++j) // the padding channels past NP read as zero
-                            *(uint4 *)(ob + ((j ^ sw) << 4)) = make_uint4(0u, 0u, 0u, 0u);
-                        tc::fence_proxy_async_smem();
-                        __syncwarp();
-                        if (lane == 0 && hok && x0 + q * 32 < p.Wo) {
-                            tc::tma_store_4d(&tmO, obw, 64 * (c >> 2), x0 + q * 32, y, img); // (x >= Wo: clipped)
-                            tc::bulk_commit();
-                        }
-                        if (c != NP / 16 - 1) { // the next box reuses the buffer
-                            if (lane == 0) tc::bulk_wait_read0();
-                            __syncwarp();
-                        }
-                    }
+                    ostage_put<NP / 16>(os, lane, c, u);
+                    if (p.mode == 1 && p.out16 && valid) // the features before the normalisation too
+                        store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
                 } else if (valid) {
                     store_bf16_16(o16 + c * 16, v, sc);
                     if (p.mode == 1 && p.out16) // the features before the normalisation too
@@ -740,36 +776,38 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    // mode 4: the layer-below activations through shared memory when the buffer fits beside two stages
-    // (their global loads stalled the epilogue more than a third stage gains)
+    // Shared-memory plan for nb weight rows per tap: mode 4's layer-below activations through a shared
+    // buffer when it fits beside two stages (their global loads stalled the epilogue more than a third stage
+    // gains), then the output staging for TMA stores if it fits too, then as many stages as fit.
     p.y_boxes = (NP + 63) / 64;
     const int ybytes = 2 * p.y_boxes * Y_BOX;
-    // mode 0: the output through shared memory and TMA stores when whole 64-channel boxes fit the row
-    p.ostage = a.mode == 0 && a.cp_out % 8 == 0 && a.cp_out >= 64 * ((NP + 63) / 64) ? 1 : 0;
-    const int obytes = p.ostage ? 8 * OBUF : 0;
-    CUtensorMap mo = ma; // unused unless ostage
-    if (p.ostage) {
-        cuuint64_t gO[4] = {(cuuint64_t)a.cp_out, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)a.n_img};
-        cuuint64_t sO[3] = {(cuuint64_t)a.cp_out * 2, (cuuint64_t)p.Wo * a.cp_out * 2,
-                            (cuuint64_t)p.Ho * p.Wo * a.cp_out * 2};
-        cuuint32_t bO[4] = {64, 32, 1, 1}, eO[4] = {1, 1, 1, 1};
-        CUresult ro = enc(&mo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, a.out, gO, sO, bO, eO,
-                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (ro != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: output tensor map (%d)", (int)ro);
-    }
+    // modes 0 and 1: the BF16 output (out, cp_out channels); mode 4: its padded BF16 copy (out16)
+    const bool m4 = a.mode == 4;
+    const int ocs = m4 ? a.o16_cs : a.cp_out, opw = m4 ? a.o16_pw : 0, oph = m4 ? a.o16_ph : 0;
+    const bool ost_ok = (a.mode == 0 || a.mode == 1 || m4) && ocs % 8 == 0 && ocs >= 64 * ((NP + 63) / 64);
+    auto plan = [&](int nb, int &ysm, int &ost, int &stages) -> size_t {
+        ysm = m4 && smem_bytes(NP, nb, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
+        const int yb = ysm ? ybytes : 0;
+        ost = ost_ok && smem_bytes(NP, nb, 2, p.a_bytes, a.kw, a.mode, yb + 8 * OBUF) <= (size_t)maxsm ? 1 : 0;
+        const int extra = yb + (ost ? 8 * OBUF : 0);
+        stages = 0;
+        for (int s = MAX_STAGES; s >= 2 && !stages; --s)
+            if (smem_bytes(NP, nb, s, p.a_bytes, a.kw, a.mode, extra) <= (size_t)maxsm) stages = s;
+        return smem_bytes(NP, nb, std::max(stages, 2), p.a_bytes, a.kw, a.mode, extra);
+    };
     // CTA pairs when there are two tiles to pair and the device co-schedules the clusters
     bool pair = g_pairs.load() != 0 && p.num_tiles >= 2;
     int nclusters = 0;
     if (pair) {
-        const int ysm = a.mode == 4 && smem_bytes(NP, NP / 2, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm;
-        const int extra = (ysm ? ybytes : 0) + obytes;
-        int s = MAX_STAGES;
-        while (s > 2 && smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, extra) > (size_t)maxsm) --s;
-        nclusters = pair_clusters<NP>(smem_bytes(NP, NP / 2, s, p.a_bytes, a.kw, a.mode, extra));
+        int ysm, ost, stages;
+        const size_t sm = plan(NP / 2, ysm, ost, stages);
+        nclusters = stages ? pair_clusters<NP>(sm) : 0;
         pair = nclusters > 0;
     }
     const int NB = pair ? NP / 2 : NP;
+    const size_t smem = plan(NB, p.ysm, p.ostage, p.stages);
+    p.stage_bytes = stage_bytes(p.a_bytes, a.kw, NB);
+    if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
     const int taps = a.kh * a.kw;
     cuuint64_t gB[2] = {(cuuint64_t)taps * a.cp_in, (cuuint64_t)NP};
     cuuint64_t sB[1] = {(cuuint64_t)taps * a.cp_in * 2};
@@ -778,8 +816,6 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     r = enc(&mb, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)a.wt, gB, sB, bB, eB, CU_TENSOR_MAP_INTERLEAVE_NONE,
             CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: weight tensor map (%d)", (int)r);
-    p.stage_bytes = stage_bytes(p.a_bytes, a.kw, NB);
-    p.ysm = a.mode == 4 && smem_bytes(NP, NB, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
     CUtensorMap my = ma; // unused unless ysm
     if (p.ysm) {
         cuuint64_t gY[4] = {(cuuint64_t)a.aux_cs, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)a.n_img};
@@ -790,12 +826,17 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
                 CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: activation (mode 4) tensor map (%d)", (int)r);
     }
-    const int yb = (p.ysm ? ybytes : 0) + obytes;
-    p.stages = 0;
-    for (int s = MAX_STAGES; s >= 2 && !p.stages; --s)
-        if (smem_bytes(NP, NB, s, p.a_bytes, a.kw, a.mode, yb) <= (size_t)maxsm) p.stages = s;
-    if (!p.stages) return fail(CNNCRF_EUNSUPPORTED, "conv_tc: two stages of %d bytes exceed shared memory", p.stage_bytes);
-    const size_t smem = smem_bytes(NP, NB, p.stages, p.a_bytes, a.kw, a.mode, yb);
+    CUtensorMap mo = ma; // unused unless ostage
+    if (p.ostage) {
+        const cuuint64_t ow = (cuuint64_t)p.Wo + 2 * opw, oh = (cuuint64_t)p.Ho + 2 * oph;
+        cuuint64_t gO[4] = {(cuuint64_t)ocs, ow, oh, (cuuint64_t)a.n_img};
+        cuuint64_t sO[3] = {(cuuint64_t)ocs * 2, ow * ocs * 2, oh * ow * ocs * 2};
+        cuuint32_t bO[4] = {64, 32, 1, 1}, eO[4] = {1, 1, 1, 1};
+        r = enc(&mo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, m4 ? a.out16 : a.out, gO, sO, bO, eO,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_tc: output tensor map (%d)", (int)r);
+    }
     if (pair) {
         // one cluster per pair of co-resident SMs, each running tile pairs until the list ends
         const int grid = 2 * std::min(nclusters, (p.num_tiles + 1) / 2);
