@@ -12,10 +12,14 @@
 // converted once per CTA into a resident B tile of the same layout.  A tile
 // is 128 consecutive output pixels of one row: ceil(K / 16) UMMA K-steps
 // (M = 128, N = NP) into the CTA's one 128-column TMEM accumulator, then the
-// epilogue (tcgen05.ld, bias, tanh, BF16 NHWC store).  The steps of a tile
+// epilogue (tcgen05.ld, bias, tanh, BF16 NHWC output; each warp stages its 32
+// pixels x 64 channels in shared memory and writes them by one TMA tensor store
+// per box instead of 32 scattered pixel rows).  The steps of a tile
 // run in order; four CTAs per SM (4 x 128 TMEM columns) hide each other's
 // gather and store latency.  128 threads; every mbarrier wait is bounded and
 // reports through the error flag.
+#include <cstring>
+
 #include <cuda_bf16.h>
 
 #include "common.h"
@@ -43,7 +47,9 @@ struct FirstParams {
     const float *wt, *bias;
     __nv_bfloat16 *out;
     int *err;
+    int ostage; // the output through shared memory and TMA stores (whole 64-channel boxes fit the row)
 };
+constexpr int OBUF = 32 * ROW; // a warp's output staging: 32 pixels x 64 BF16 channels
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d)
 {
@@ -58,14 +64,15 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi)
 
 template <int NP>
 __global__ void __launch_bounds__(NUM_THREADS)
-    k_conv_first_tc(const FirstParams p)
+    k_conv_first_tc(const __grid_constant__ CUtensorMap tmO, const FirstParams p)
 {
     constexpr uint32_t IDESC = tc::idesc_bf16(BM, NP);
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint8_t *sA = smem;                   // [128 rows][128 B]
     uint8_t *sB = smem + A_BYTES;         // [NP rows][128 B]
-    float *sbias = (float *)(sB + NP * ROW);
+    uint8_t *sO = sB + NP * ROW;          // [4 warps][OBUF] output staging (1024-byte aligned)
+    float *sbias = (float *)(sO + 4 * OBUF);
     uint64_t *done = (uint64_t *)(sbias + NP); // [1]: the tile's MMAs
     uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
@@ -108,6 +115,24 @@ __global__ void __launch_bounds__(NUM_THREADS)
         const uint32_t ta = tmem + ((uint32_t)(warp * 32) << 16);
         __nv_bfloat16 *o16 = p.out + img * p.out_img + ((long)y * p.Wo + x) * p.cp_out;
         float v[16];
+        if (p.ostage) {
+            const int xw = x - (tid & 31); // the warp's first pixel
+            const tc::OStage os{&tmO, sO + warp * OBUF, xw < p.Wo, xw, y, img};
+            const int lane = tid & 31;
+            if (lane == 0) tc::bulk_wait_read0(); // the previous tile's last store has read the buffer
+            __syncwarp();
+#pragma unroll 1
+            for (int c = 0; c < NP / 16; ++c) {
+                tc::tmem_ld16(ta + c * 16, v); // warp-collective: every lane runs it
+                uint32_t u[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j)
+                    u[j] = pack_bf16(tc::tanh_fast(v[2 * j] + sbias[c * 16 + 2 * j]),
+                                     tc::tanh_fast(v[2 * j + 1] + sbias[c * 16 + 2 * j + 1]));
+                tc::ostage_put<NP / 16>(os, lane, c, u); // (pixels past Wo are clipped by the store)
+            }
+            return;
+        }
 #pragma unroll 1
         for (int c = 0; c < NP / 16; ++c) {
             tc::tmem_ld16(ta + c * 16, v); // warp-collective: every lane runs it
@@ -178,6 +203,7 @@ __global__ void __launch_bounds__(NUM_THREADS)
         tc::fence_before_sync();
     }
     if (!ok && tid == 0) atomicExch(p.err, 1);
+    if (p.ostage && (tid & 31) == 0) tc::bulk_wait0(); // the warp's stores are done before its buffer goes
     tc::fence_before_sync();
     __syncthreads();
     if (warp == 0) {
@@ -186,10 +212,26 @@ __global__ void __launch_bounds__(NUM_THREADS)
     }
 }
 
-template <int NP> size_t smem_bytes() { return 1024 + A_BYTES + NP * ROW + NP * 4 + 2 * 8 + 16; }
+template <int NP> size_t smem_bytes() { return 1024 + A_BYTES + NP * ROW + 4 * OBUF + NP * 4 + 2 * 8 + 16; }
 
-template <int NP> int launch(const FirstParams &p, cudaStream_t st)
+template <int NP> int launch(FirstParams &p, cudaStream_t st)
 {
+    // the output as 4-D boxes of 64 channels x 32 pixels (whole boxes: cp_out >= 64 * ceil(NP / 64))
+    CUtensorMap mo;
+    std::memset(&mo, 0, sizeof mo);
+    p.ostage = p.cp_out % 8 == 0 && p.cp_out >= 64 * ((NP + 63) / 64) && (p.out_img * 2) % 16 == 0 &&
+               p.out_img >= (long)p.Ho * p.Wo * p.cp_out;
+    if (p.ostage) {
+        auto enc = tc::tensor_map_encoder();
+        if (!enc) return fail(CNNCRF_ECUDA, "conv_first_tc: cuTensorMapEncodeTiled unavailable");
+        cuuint64_t g[4] = {(cuuint64_t)p.cp_out, (cuuint64_t)p.Wo, (cuuint64_t)p.Ho, (cuuint64_t)p.n_img};
+        cuuint64_t s[3] = {(cuuint64_t)p.cp_out * 2, (cuuint64_t)p.Wo * p.cp_out * 2, (cuuint64_t)p.out_img * 2};
+        cuuint32_t b[4] = {64, 32, 1, 1}, e[4] = {1, 1, 1, 1};
+        const CUresult r = enc(&mo, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, p.out, g, s, b, e,
+                               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) return fail(CNNCRF_ECUDA, "conv_first_tc: output tensor map (%d)", (int)r);
+    }
     int dev = 0, sms = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
     CNNCRF_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -200,7 +242,7 @@ template <int NP> int launch(const FirstParams &p, cudaStream_t st)
     const int grid = std::min(p.num_tiles, CTAS_PER_SM * sms);
     {
         CNNCRF_PROF("conv_first_tc", st);
-        k_conv_first_tc<NP><<<grid, NUM_THREADS, smem, st>>>(p);
+        k_conv_first_tc<NP><<<grid, NUM_THREADS, smem, st>>>(mo, p);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

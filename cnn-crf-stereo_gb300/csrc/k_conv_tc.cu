@@ -142,50 +142,12 @@ __device__ __forceinline__ void load_dz_y_smem(const uint8_t *ybuf, int y_boxes,
     }
 }
 
-__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
-
-// An epilogue warp's output staged for TMA stores: 32 pixel rows x 64 BF16
-// channels in the 128-byte swizzle (16-byte unit j of row r at unit j ^ (r & 7)),
-// so that every store is one whole box instead of 32 scattered pixel rows.
-struct OStage {
-    const CUtensorMap *map;
-    uint8_t *base; // the warp's buffer (1024-byte aligned)
-    bool store;    // false: the warp's pixels lie outside the tensor, nothing is stored
-    int x, y, img; // the warp's first pixel in the map's coordinates (pixels past the tensor are clipped)
-};
-
-// BF16 chunk c (16 channels) of this lane's pixel into the buffer; after a
-// box's last chunk (or chunk NC - 1) the channels past it are zeroed and the
-// box goes out by one TMA store.  Warp-collective.  The caller waits for the
-// buffer's previous stores to have read it before chunk 0.
-template <int NC>
-__device__ __forceinline__ void ostage_put(const OStage &o, int lane, int c, const uint32_t (&u)[8])
-{
-    uint8_t *row = o.base + lane * 128;
-    const int j0 = 2 * (c & 3), sw = lane & 7;
-    *(uint4 *)(row + ((j0 ^ sw) << 4)) = make_uint4(u[0], u[1], u[2], u[3]);
-    *(uint4 *)(row + (((j0 + 1) ^ sw) << 4)) = make_uint4(u[4], u[5], u[6], u[7]);
-    if ((c & 3) == 3 || c == NC - 1) {
-        for (int j = j0 + 2; j < 8; ++j) *(uint4 *)(row + ((j ^ sw) << 4)) = make_uint4(0u, 0u, 0u, 0u);
-        tc::fence_proxy_async_smem();
-        __syncwarp();
-        if (lane == 0 && o.store) {
-            tc::tma_store_4d(o.map, o.base, 64 * (c >> 2), o.x, o.y, o.img);
-            tc::bulk_commit();
-        }
-        if (c != NC - 1) { // the next box reuses the buffer
-            if (lane == 0) tc::bulk_wait_read0();
-            __syncwarp();
-        }
-    }
-}
-
 // One half's chunk c of mode 4: the sums times 1 - y^2 into v (zero for an
 // invalid pixel, so it adds nothing to the bias sums), stored as BF16 into the
 // padded copy (and as FP32 if p.out).
 template <int NP>
 __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, bool valid, size_t pix, size_t q16,
-                                         const uint4 (&yc)[2], float (&v)[16], const OStage *os)
+                                         const uint4 (&yc)[2], float (&v)[16], const tc::OStage *os)
 {
     tc::tmem_ld16(ta + c * 16, v); // warp-collective
     const uint32_t yw[8] = {yc[0].x, yc[0].y, yc[0].z, yc[0].w, yc[1].x, yc[1].y, yc[1].z, yc[1].w};
@@ -202,7 +164,7 @@ __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, 
         u[j] = *(uint32_t *)&b2;
     }
     if (os) { // (warp-collective; an invalid pixel's zeros land in the border or past the tensor)
-        ostage_put<NP / 16>(*os, lane_id(), c, u);
+        tc::ostage_put<NP / 16>(*os, tc::lane_id(), c, u);
     } else if (valid) {
         uint4 *d16 = (uint4 *)(p.out16 + q16 * p.o16_cs + c * 16);
         d16[0] = make_uint4(u[0], u[1], u[2], u[3]);
@@ -228,7 +190,7 @@ __device__ __forceinline__ void dz_chunk(const TcParams &p, uint32_t ta, int c, 
 // activations), adding the warp's per-channel sums into wacc.
 template <int NP>
 __device__ __forceinline__ void epilogue_dz(const TcParams &p, uint32_t ta, bool valid, size_t pix, size_t q16,
-                                            int lane, float *wacc, const uint4 (*ya)[2], const OStage *os)
+                                            int lane, float *wacc, const uint4 (*ya)[2], const tc::OStage *os)
 {
     constexpr int NC = NP / 16;
 #pragma unroll
@@ -616,7 +578,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     ((size_t)img * (p.Ho + 2 * p.o16_ph) + y + p.o16_ph) * (p.Wo + 2 * p.o16_pw) + x + p.o16_pw;
                 // the padded copy through the staging buffer: boxes at (x + o16_pw, y + o16_ph) of the padded
                 // tensor (a pixel past Wo holds zeros, which is what the border holds)
-                const OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32 + p.o16_pw, y + p.o16_ph, img};
+                const tc::OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32 + p.o16_pw, y + p.o16_ph, img};
                 if (p.ostage) {
                     if (lane == 0) tc::bulk_wait_read0();
                     __syncwarp();
@@ -645,7 +607,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             // mode 0 through shared memory: the warp's 32 pixels x 64 channels per TMA store, in the 128-byte
             // swizzle (16-byte unit j of pixel row r at unit j ^ (r & 7)), so every store is a whole box
             const bool tstore = p.ostage && (p.mode == 0 || p.mode == 1);
-            const OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32, y, img};
+            const tc::OStage os{&tmO, obw, hok && x0 + q * 32 < p.Wo, x0 + q * 32, y, img};
             if (tstore) { // the previous tile's last store has read the buffer
                 if (lane == 0) tc::bulk_wait_read0();
                 __syncwarp();
@@ -688,7 +650,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         __nv_bfloat162 b2 = __floats2bfloat162_rn(v[2 * j] * sc, v[2 * j + 1] * sc);
                         u[j] = *(uint32_t *)&b2;
                     }
-                    ostage_put<NP / 16>(os, lane, c, u);
+                    tc::ostage_put<NP / 16>(os, lane, c, u);
                     if (p.mode == 1 && p.out16 && valid) // the features before the normalisation too
                         store_bf16_16(p.out16 + pix * p.o16_cs + c * 16, v, 1.0f);
                 } else if (valid) {

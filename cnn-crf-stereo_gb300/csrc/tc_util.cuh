@@ -374,5 +374,44 @@ __device__ __forceinline__ void umma_commit_pair(uint64_t *bar, uint16_t mask)
                  : "memory");
 }
 
+// ------------------------------------------------------------ staged output (TMA stores)
+__device__ __forceinline__ int lane_id() { return (int)(threadIdx.x & 31); }
+
+// An epilogue warp's output staged for TMA stores: 32 pixel rows x 64 BF16
+// channels in the 128-byte swizzle (16-byte unit j of row r at unit j ^ (r & 7)),
+// so that every store is one whole box instead of 32 scattered pixel rows.
+struct OStage {
+    const CUtensorMap *map;
+    uint8_t *base; // the warp's buffer (1024-byte aligned)
+    bool store;    // false: the warp's pixels lie outside the tensor, nothing is stored
+    int x, y, img; // the warp's first pixel in the map's coordinates (pixels past the tensor are clipped)
+};
+
+// BF16 chunk c (16 channels) of this lane's pixel into the buffer; after a
+// box's last chunk (or chunk NC - 1) the channels past it are zeroed and the
+// box goes out by one TMA store.  Warp-collective.  The caller waits for the
+// buffer's previous stores to have read it before chunk 0.
+template <int NC>
+__device__ __forceinline__ void ostage_put(const OStage &o, int lane, int c, const uint32_t (&u)[8])
+{
+    uint8_t *row = o.base + lane * 128;
+    const int j0 = 2 * (c & 3), sw = lane & 7;
+    *(uint4 *)(row + ((j0 ^ sw) << 4)) = make_uint4(u[0], u[1], u[2], u[3]);
+    *(uint4 *)(row + (((j0 + 1) ^ sw) << 4)) = make_uint4(u[4], u[5], u[6], u[7]);
+    if ((c & 3) == 3 || c == NC - 1) {
+        for (int j = j0 + 2; j < 8; ++j) *(uint4 *)(row + ((j ^ sw) << 4)) = make_uint4(0u, 0u, 0u, 0u);
+        tc::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0 && o.store) {
+            tc::tma_store_4d(o.map, o.base, 64 * (c >> 2), o.x, o.y, o.img);
+            tc::bulk_commit();
+        }
+        if (c != NC - 1) { // the next box reuses the buffer
+            if (lane == 0) tc::bulk_wait_read0();
+            __syncwarp();
+        }
+    }
+}
+
 } // namespace tc
 } // namespace cnncrf
