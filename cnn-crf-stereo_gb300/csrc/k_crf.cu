@@ -36,7 +36,7 @@ int crf_pass_ring8(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStr
 size_t crf_pass_smem(int P, int RING, int W, int H, bool hpass, int wpb)
 {
     const int n = hpass ? W : H;
-    return sizeof(float) * wpb * (size_t)(((n + 3) & ~3) + ring_floats(P, RING));
+    return sizeof(float) * wpb * (size_t)(((n + 3) & ~3) + ring_floats(P, RING, hpass));
 }
 
 namespace {
