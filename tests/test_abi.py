@@ -134,3 +134,19 @@ def test_config_file_parser():
     assert full["L1"] == 3.0          # command line wins (stereo/stereo_img.cpp:94-103)
     assert full["L2"] == 12.0         # default
     assert full["crf-iterations"] == 5
+
+
+def test_conv_pairs_switch(lib):
+    """The process-wide choice between the paired (cta_group::2) and the
+    single-CTA tensor-core convolution is a host flag: on by default, set and
+    read back without a GPU; a null output pointer is rejected."""
+    import cnncrf._lib as L
+    v = C.c_int(-1)
+    assert lib.cnncrf_get_conv_pairs(C.byref(v)) == L.OK and v.value == 1
+    try:
+        assert lib.cnncrf_set_conv_pairs(0) == L.OK
+        assert lib.cnncrf_get_conv_pairs(C.byref(v)) == L.OK and v.value == 0
+    finally:
+        assert lib.cnncrf_set_conv_pairs(1) == L.OK
+    assert lib.cnncrf_get_conv_pairs(C.byref(v)) == L.OK and v.value == 1
+    assert lib.cnncrf_get_conv_pairs(None) == L.EINVAL
