@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(NUM_THREADS)
     uint64_t *done = (uint64_t *)(sbias + NP); // [1]: the tile's MMAs
     uint32_t *tmem_slot = (uint32_t *)(done + 2);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
+    int *soff = (int *)(tmem_slot + 4); // [64]: patch element k's offset from the pixel's first input
 
     const int tid = threadIdx.x, warp = tid >> 5;
     const int nchunk = p.nk * 2; // 16-byte chunks of a row the MMAs read
@@ -93,6 +94,12 @@ __global__ void __launch_bounds__(NUM_THREADS)
         st_shared_v4(tc::smem_u32(sB + n * ROW + ((c ^ (n & 7)) << 4)), w[0], w[1], w[2], w[3]);
     }
     for (int i = tid; i < NP; i += NUM_THREADS) sbias[i] = p.bias ? p.bias[i] : 0.0f;
+    // k = (ky, kx, ci) ascending -> ky * in_row + kx * in_pix + ci, once per CTA instead of per element
+    for (int k = tid; k < p.K; k += NUM_THREADS) {
+        const int tap = k / p.Cin, ci = k - tap * p.Cin;
+        const int ky = tap / p.kw, kx = tap - ky * p.kw;
+        soff[k] = (int)(ky * p.in_row + kx * p.in_pix) + ci;
+    }
     if (tid == 0) {
         tc::mbar_init(&done[0], 1);
         *abort_flag = 0;
@@ -168,11 +175,7 @@ __global__ void __launch_bounds__(NUM_THREADS)
                     for (int e = 0; e < 2; ++e) {
                         const int k = 8 * c + 2 * j + e;
                         f[e] = 0.0f;
-                        if (k < p.K && x < p.Wo) {
-                            const int tap = k / p.Cin, ci = k - tap * p.Cin;
-                            const int ky = tap / p.kw, kx = tap - ky * p.kw;
-                            f[e] = __ldg(src + (long)ky * p.in_row + (long)kx * p.in_pix + ci);
-                        }
+                        if (k < p.K && x < p.Wo) f[e] = __ldg(src + soff[k]);
                     }
                     w[j] = pack_bf16(f[0], f[1]);
                 }
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(NUM_THREADS)
     }
 }
 
-template <int NP> size_t smem_bytes() { return 1024 + A_BYTES + NP * ROW + 4 * OBUF + NP * 4 + 2 * 8 + 16; }
+template <int NP> size_t smem_bytes() { return 1024 + A_BYTES + NP * ROW + 4 * OBUF + NP * 4 + 2 * 8 + 16 + 64 * 4; }
 
 template <int NP> int launch(FirstParams &p, cudaStream_t st)
 {
@@ -266,6 +269,8 @@ int conv_first_tc(const ConvArgs &a, int *err, cudaStream_t st)
     p.Ho = a.H - a.kh + 1, p.Wo = a.W - a.kw + 1;
     if (p.Ho < 1 || p.Wo < 1) return fail(CNNCRF_ESHAPE, "conv_first_tc: empty output");
     p.Cin = a.Cin, p.kw = a.kw, p.K = a.kh * a.kw * a.Cin, p.nk = ceil_div(p.K, 16);
+    if ((long)(a.kh - 1) * a.in_row + (long)(a.kw - 1) * a.in_pix + a.Cin >= (1L << 31))
+        return fail(CNNCRF_EUNSUPPORTED, "conv_first_tc: patch offsets beyond 32 bits");
     p.n_img = a.n_img, p.tiles_x = ceil_div(p.Wo, BM), p.num_tiles = a.n_img * p.Ho * p.tiles_x;
     p.cp_out = a.out_cs, p.out_img = a.out_img;
     p.wt = a.wt, p.bias = a.bias, p.out = (__nv_bfloat16 *)a.out16, p.err = err;
