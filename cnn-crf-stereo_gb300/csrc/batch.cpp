@@ -180,7 +180,8 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
         prev = g.cnn_done;
         CNNCRF_CUDA(cudaStreamWaitEvent(cs, g.cnn_done, 0));
         CNNCRF_TRY(k::crf_solve_batch(g.vol.as<float>(), g.pw.as<float>(), g.W, g.H, g.depth, n, p, iters,
-                                      g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, cs));
+                                      g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, cs,
+                                      false)); // labels and bounds only: the last phi is dead
         CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, cs));
         CNNCRF_CUDA(cudaEventRecord(g.done, cs));
         CNNCRF_CUDA(cudaStreamWaitEvent(work, g.done, 0));

@@ -125,11 +125,14 @@ CrfPassArgs pass_args(const float *cost, long wps, int W, int H, int D, int np, 
     a.lbuf = (float *)(ws + l.lbuf);
     a.W = W, a.H = H, a.D = D, a.np = np, a.wps = wps;
     a.rp = rp;
+    a.store_phi = 1;
     return a;
 }
 
+// keep_phi = false: the last V pass does not write phi (nothing reads C1 from this workspace afterwards)
 int run_passes(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
-               const Rho &rp, int delta, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st)
+               const Rho &rp, int delta, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st,
+               bool keep_phi = true)
 {
     if (delta < 1 || delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
     const CrfTile t = effective_tile(W, H, D, np, delta);
@@ -141,6 +144,7 @@ int run_passes(const float *cost, const float *wx, const float *wy, long wps, in
         a.wgt = wx, a.first = it == 0, a.labels = nullptr, a.cmin = cH;
         CNNCRF_TRY(pass(a, true, delta, t.ring_h, t.wpb_h, st));
         a.wgt = wy, a.first = 0, a.labels = it == iters - 1 ? labels : nullptr, a.cmin = cV;
+        a.store_phi = keep_phi || it != iters - 1;
         CNNCRF_TRY(pass(a, false, delta, t.ring_v, t.wpb_v, st));
     }
     {
@@ -175,7 +179,8 @@ int check_args(const float *cost, const float *wx, const float *wy, int W, int H
 }
 
 int solve_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
-               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st)
+               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st,
+               bool keep_phi = true)
 {
     CNNCRF_TRY(check_args(cost, wx, wy, W, H, D, np, p, ws, ws_bytes));
     if (!labels) return fail(CNNCRF_EINVAL, "crf: null pointer");
@@ -190,7 +195,7 @@ int solve_impl(const float *cost, const float *wx, const float *wy, long wps, in
         CNNCRF_CHECK_LAUNCH();
         return CNNCRF_OK;
     }
-    return run_passes(cost, wx, wy, wps, W, H, D, np, make_rho(p), p.delta, iters, labels, w, l, st);
+    return run_passes(cost, wx, wy, wps, W, H, D, np, make_rho(p), p.delta, iters, labels, w, l, st, keep_phi);
 }
 
 // time one H and one V pass of every candidate tile (events on `st`, best of
@@ -276,10 +281,10 @@ int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H,
 }
 
 int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs, const CrfParams &p,
-                    int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st)
+                    int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st, bool keep_phi)
 {
     const long N = (long)W * H;
-    return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st);
+    return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st, keep_phi);
 }
 
 int crf_autotune(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int npairs,

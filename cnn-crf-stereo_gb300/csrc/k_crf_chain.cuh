@@ -32,6 +32,7 @@ struct CrfPassArgs {
     long wps;
     Rho rp;
     int first;           // H pass of the first iteration: phi = 0, not read
+    int store_phi;       // 0: the pass's phi is dead (the last V pass when no caller reads C1), not written
     int32_t *labels;     // V pass of the last iteration: argmin labels, else null
     double *cmin;        // per chain minimum [np][chains]
 };
@@ -247,7 +248,7 @@ __host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass) { ret
 template <int P, int DELTA, bool HPASS, bool FULL, int RING>
 __global__ void __launch_bounds__(128)
     k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
-                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int nmax,
+                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int store_phi, int nmax,
                 int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
 {
     extern __shared__ float4 smem4[];
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(128)
             A[r] = __fsub_rn(A[r], h);
             ph[r] = HPASS ? __fadd_rn(ph[r], h) : A[r];
         }
-        store_vec<P>(phi + pix(i) * D, lane, D, ph);
+        if (store_phi) store_vec<P>(phi + pix(i) * D, lane, D, ph);
         if (i > 0) {
 #pragma unroll
             for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
@@ -381,7 +382,8 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
     {
         CNNCRF_PROF(hpass ? "crf_h" : "crf_v", st);
         kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.phi, a.wgt, a.lbuf, a.W, a.H, a.D, a.rp,
-                                                           a.first, nmax, a.labels, a.cmin, a.np, a.wps);
+                                                           a.first, a.store_phi, nmax, a.labels, a.cmin, a.np,
+                                                           a.wps);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

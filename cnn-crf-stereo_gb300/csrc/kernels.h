@@ -190,10 +190,12 @@ struct CrfParams {
 // workspace layout helpers
 size_t crf_workspace_bytes(int W, int H, int D, int npairs = 1);
 // npairs pairs at once: cost [n][H][W][D], weights [n][2][H][W] (wx, wy),
-// labels [n][H][W]; bounds stay in the workspace (crf_lb_device)
+// labels [n][H][W]; bounds stay in the workspace (crf_lb_device).  keep_phi =
+// false leaves the workspace's final phi unwritten (for callers that read the
+// labels and bounds only, never C1).
 int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs,
                     const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
-                    cudaStream_t st);
+                    cudaStream_t st, bool keep_phi = true);
 const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs);
 int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D,
               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,

@@ -411,7 +411,7 @@ int cnncrf_train::hinge(const int32_t *gt, double *loss, int32_t *yh_out)
     k::CrfParams cp;
     cp.L1 = d.L1, cp.L2 = d.L2, cp.delta = d.delta, cp.shape = d.crf_shape, cp.slack = d.crf_slack;
     CNNCRF_TRY(k::crf_solve_batch(aug.as<float>(), wts.as<float>(), W, H, D, n, cp, d.crf_iters, labels.as<int32_t>(),
-                                  crfws.get(), crfws_bytes, st));
+                                  crfws.get(), crfws_bytes, st, false)); // labels and bounds only
     float rho[9];
     rho[0] = 0.0f;
     for (int t = 1; t <= 8; ++t) rho[t] = d.crf_shape == 0 ? fminf(d.L1, d.L2) : fminf(d.L1 * (float)t, d.L2);
