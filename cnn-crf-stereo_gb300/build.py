@@ -24,7 +24,7 @@ NVCC = shutil.which("nvcc") or os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 # kernels that must match the oracle bit for bit
-EXACT = {"k_front.cu", "k_conv_simt.cu", "k_corr.cu", "k_crf.cu", "k_crf_r4.cu", "k_misc.cu", "k_census.cu"}
+EXACT = {"k_front.cu", "k_conv_simt.cu", "k_corr.cu", "k_crf.cu", "k_crf_r4.cu", "k_misc.cu", "k_census.cu", "k_tv.cu"}
 
 
 def _sources():

@@ -110,7 +110,8 @@ PROTOS = {
     "cnncrf_remap_solution": ([vp, vp, i32, i32, f32, f32, vp], i32),
     "cnncrf_warp_image": ([vp, vp, vp, i32, i32, vp], i32),
     "cnncrf_tv_fit": ([vp, vp, i32, i32, f32, f32, vp], i32),
-    "cnncrf_tv_iterate": ([vp, vp, vp, vp, vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp], i32),
+    "cnncrf_tv_workspace_size": ([i32, i32, C.POINTER(C.c_size_t)], i32),
+    "cnncrf_tv_iterate": ([vp, vp, vp, vp, vp, vp, vp, vp, i32, i32, f32, f32, f32, i32, vp, C.c_size_t, vp], i32),
     "cnncrf_rgb_to_gray": ([vp, vp, i32, i32, vp], i32),
     "cnncrf_census_volume": ([vp, vp, i32, i32, i32, f32, f32, i32, f32, vp, vp], i32),
     "cnncrf_edge_weights": ([vp, i32, i32, f32, f32, f32, vp, vp, vp], i32),
@@ -154,6 +155,7 @@ PROTOS = {
     "cnncrf_batch_set_images_device": ([vp, i32, vp, vp], i32),
     "cnncrf_batch_use_graph": ([vp, i32], i32),
     "cnncrf_batch_run": ([vp, f32, f32, f32, i32, f32], i32),
+    "cnncrf_batch_run_host": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), f32, f32, f32, i32, f32], i32),
     "cnncrf_batch_get_output": ([vp, i32, vp], i32),
     "cnncrf_batch_get_output_device": ([vp, i32, C.POINTER(vp)], i32),
     "cnncrf_batch_get_labels_device": ([vp, i32, C.POINTER(vp)], i32),

@@ -268,14 +268,18 @@ def tv_fit(vol3, disp_step, lambda_census, stream=None):
 
 
 def tv_iterate(u, u0, qf, wx, wy, C_, huber_eps, disp_step, iterations, stream=None):
-    """Runs the primal-dual loop in place on a copy of u; returns (u, u_, p, q)."""
+    """Runs the primal-dual loop (fused, several iterations per launch) on a
+    copy of u with p = q = 0 at the start; returns (u, u_, p, q)."""
     H, W = u.shape
     u = u.clone()
     u_ = torch.zeros_like(u)
     p = torch.zeros((H, W, 2), device="cuda", dtype=torch.float32)
     q = torch.zeros_like(p)
+    nb = C.c_size_t()
+    call("cnncrf_tv_workspace_size", W, H, C.byref(nb))
+    ws = torch.empty(nb.value, device="cuda", dtype=torch.uint8)
     call("cnncrf_tv_iterate", _ptr(u), _ptr(u_), _ptr(u0), _ptr(qf), _ptr(p), _ptr(q), _ptr(wx), _ptr(wy), W, H,
-         C_, huber_eps, disp_step, iterations, _stream_ptr(stream))
+         C_, huber_eps, disp_step, iterations, _ptr(ws), nb.value, _stream_ptr(stream))
     return u, u_, p, q
 
 
@@ -490,6 +494,18 @@ class StereoBatch:
 
     def run(self, L1, L2, delta, iterations, lambda_reg=1.0):
         call("cnncrf_batch_run", self._h, L1, L2, float(delta), iterations, lambda_reg)
+
+    def run_host(self, lefts, rights, outs, L1, L2, delta, iterations, lambda_reg=1.0):
+        """One run from host images to host disparities (cnncrf_batch_run_host):
+        lefts / rights / outs are per-pair CPU tensors (page-locked ones let a
+        graph replay; outs may be None); the copies overlap the other groups'
+        work.  The outputs are complete once the batch's stream is synchronised
+        (check())."""
+        n = len(lefts)
+        arr = lambda ts: (C.c_void_p * n)(*[None if t is None else t.data_ptr() for t in ts])
+        hl, hr = arr(lefts), arr(rights)
+        ho = None if outs is None else arr(outs)
+        call("cnncrf_batch_run_host", self._h, hl, hr, ho, L1, L2, float(delta), iterations, lambda_reg)
 
     def autotune(self, L1, L2, delta, iterations, lambda_reg=1.0):
         """Run once, tune every group's CRF tile (see cnncrf.tuning); returns

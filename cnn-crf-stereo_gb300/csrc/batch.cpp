@@ -17,6 +17,12 @@
 // back into the batch's stream; with graph capture on, the whole sequence is
 // captured once into a CUDA graph (node priorities kept) and replayed by
 // later runs with the same parameters.
+//
+// cnncrf_batch_run_host takes the pairs' images in host memory and returns
+// the disparities to host memory as part of the same pipeline: a copy stream
+// carries every group's host-to-device copies ahead of that group's CNN, so
+// group i+1's images travel while group i computes, and each group's
+// disparities are copied back on its CRF stream right after its remap.
 #include <cmath>
 #include <memory>
 #include <string>
@@ -38,11 +44,12 @@ struct Group {
     cnncrf_net_t net = nullptr;
     cudaStream_t stream = nullptr;     // CNN part (high priority)
     cudaStream_t crf_stream = nullptr; // CRF part (low priority)
-    cudaEvent_t cnn_done = nullptr, done = nullptr;
+    cudaEvent_t cnn_done = nullptr, done = nullptr, in_done = nullptr;
     size_t ws_bytes = 0;
     ~Group()
     {
         if (net) cnncrf_net_destroy(net);
+        if (in_done) cudaEventDestroy(in_done);
         if (done) cudaEventDestroy(done);
         if (cnn_done) cudaEventDestroy(cnn_done);
         if (stream) cudaStreamDestroy(stream);
@@ -67,6 +74,7 @@ struct cnncrf_batch {
     uint64_t seed = 0;
     cudaStream_t st = nullptr;   // the caller's stream
     cudaStream_t work = nullptr; // the batch's own stream (capturable even when `st` is the legacy stream)
+    cudaStream_t copy = nullptr; // host-to-device copies of run_host, ahead of the groups' CNN parts
     cudaEvent_t in_ev = nullptr, out_ev = nullptr;
     std::vector<std::unique_ptr<Group>> groups;
     std::vector<std::pair<int, int>> loc; // pair -> (group, slot)
@@ -79,6 +87,11 @@ struct cnncrf_batch {
     float gL1 = 0, gL2 = 0, gdelta = 0, glambda = 0;
     int giters = -1;
     bool ran_eager = false;
+    std::vector<const void *> gptrs; // host buffers of run_host baked into the graph (empty: run)
+
+    // host buffers of the current run_host call (null: images staged by set_images, no copy out)
+    const float *const *h_left = nullptr, *const *h_right = nullptr;
+    float *const *h_out = nullptr;
 
     ~cnncrf_batch()
     {
@@ -88,6 +101,7 @@ struct cnncrf_batch {
         if (out_ev) cudaEventDestroy(out_ev);
         groups.clear();
         if (work) cudaStreamDestroy(work);
+        if (copy) cudaStreamDestroy(copy);
     }
     void invalidate()
     {
@@ -98,6 +112,7 @@ struct cnncrf_batch {
     }
     int build();
     int enqueue(float L1, float L2, float delta, int iters, float lambda);
+    int run(float L1, float L2, float delta, int iterations, float lambda);
 };
 
 int cnncrf_batch::build()
@@ -129,6 +144,7 @@ int cnncrf_batch::build()
         if (!g.crf_stream) CNNCRF_CUDA(cudaStreamCreateWithPriority(&g.crf_stream, cudaStreamNonBlocking, prio_low));
         if (!g.done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
         if (!g.cnn_done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.cnn_done, cudaEventDisableTiming));
+        if (!g.in_done) CNNCRF_CUDA(cudaEventCreateWithFlags(&g.in_done, cudaEventDisableTiming));
         CNNCRF_TRY(cnncrf_net_set_stream(g.net, (cnncrf_stream_t)g.stream));
         for (int s = 0; s < 2; ++s) {
             CNNCRF_TRY(g.img[s].reserve(sizeof(float) * 4 * N * n));
@@ -150,6 +166,7 @@ int cnncrf_batch::build()
     if (!in_ev) CNNCRF_CUDA(cudaEventCreateWithFlags(&in_ev, cudaEventDisableTiming));
     if (!out_ev) CNNCRF_CUDA(cudaEventCreateWithFlags(&out_ev, cudaEventDisableTiming));
     if (!work) CNNCRF_CUDA(cudaStreamCreateWithFlags(&work, cudaStreamNonBlocking));
+    if (!copy) CNNCRF_CUDA(cudaStreamCreateWithFlags(&copy, cudaStreamNonBlocking));
     CNNCRF_CUDA(cudaDeviceSynchronize()); // parameter uploads done before any stream work
     built = true;
     return CNNCRF_OK;
@@ -164,6 +181,7 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
     if ((float)di != delta || di < 1 || di > 4) return fail(CNNCRF_EUNSUPPORTED, "batch: delta %g", delta);
     p.L1 = L1, p.L2 = L2, p.delta = di, p.shape = o.crf_shape, p.slack = o.crf_slack;
     CNNCRF_CUDA(cudaEventRecord(fork, work));
+    if (h_left) CNNCRF_CUDA(cudaStreamWaitEvent(copy, fork, 0));
     cudaEvent_t prev = fork;
     for (auto &gp : groups) {
         Group &g = *gp;
@@ -171,6 +189,18 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
         const long N = (long)g.W * g.H;
         cudaStream_t gs = g.stream, cs = g.crf_stream;
         CNNCRF_CUDA(cudaStreamWaitEvent(gs, prev, 0));
+        if (h_left) { // this group's images, on the copy stream in pipeline order
+            const size_t bytes = sizeof(float) * 4 * (size_t)N;
+            for (int m = 0; m < n; ++m) {
+                const int pair = g.members[m];
+                CNNCRF_CUDA(cudaMemcpyAsync((char *)g.img[0].get() + bytes * m, h_left[pair], bytes,
+                                            cudaMemcpyHostToDevice, copy));
+                CNNCRF_CUDA(cudaMemcpyAsync((char *)g.img[1].get() + bytes * m, h_right[pair], bytes,
+                                            cudaMemcpyHostToDevice, copy));
+            }
+            CNNCRF_CUDA(cudaEventRecord(g.in_done, copy));
+            CNNCRF_CUDA(cudaStreamWaitEvent(gs, g.in_done, 0));
+        }
         const int pad = g.net->pad;
         CNNCRF_TRY(k::pad_rgba(g.img[0].as<float>(), g.W, g.H, pad, g.padded[0].as<float>(), gs, n));
         CNNCRF_TRY(k::pad_rgba(g.img[1].as<float>(), g.W, g.H, pad, g.padded[1].as<float>(), gs, n));
@@ -183,6 +213,11 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
                                       g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, cs,
                                       false)); // labels and bounds only: the last phi is dead
         CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, cs));
+        if (h_out)
+            for (int m = 0; m < n; ++m)
+                if (h_out[g.members[m]])
+                    CNNCRF_CUDA(cudaMemcpyAsync(h_out[g.members[m]], g.out.as<float>() + N * m,
+                                                sizeof(float) * N, cudaMemcpyDeviceToHost, cs));
         CNNCRF_CUDA(cudaEventRecord(g.done, cs));
         CNNCRF_CUDA(cudaStreamWaitEvent(work, g.done, 0));
     }
@@ -350,58 +385,103 @@ int cnncrf_batch_group_shape(cnncrf_batch_t b, int group, int *width, int *heigh
     return CNNCRF_OK;
 }
 
-int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
+// one run of the whole batch from the caller's stream; with graphs on, the
+// first run with new parameters (or new run_host buffers) is eager, the next
+// one captures, later ones replay
+int cnncrf_batch::run(float L1, float L2, float delta, int iterations, float lambda_reg)
 {
-    clear_error();
-    if (!b) return fail(CNNCRF_EINVAL, "null batch");
-    if (b->loc.empty()) return fail(CNNCRF_ESTATE, "batch: no pairs");
-    if (!b->built) CNNCRF_TRY(b->build());
+    if (loc.empty()) return fail(CNNCRF_ESTATE, "batch: no pairs");
+    if (!built) CNNCRF_TRY(build());
+    // the host buffers of run_host go into the graph's copy nodes: a graph
+    // replays only with the same buffers, and only page-locked ones can be
+    // captured (pageable buffers run eagerly)
+    std::vector<const void *> ptrs;
+    bool capturable = true;
+    if (h_left) {
+        for (size_t i = 0; i < loc.size(); ++i) {
+            const void *pp[3] = {h_left[i], h_right[i], h_out ? h_out[i] : nullptr};
+            for (const void *q : pp) {
+                ptrs.push_back(q);
+                if (!q) continue;
+                cudaPointerAttributes at{};
+                if (cudaPointerGetAttributes(&at, q) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+                    (void)cudaGetLastError();
+                    capturable = false;
+                }
+            }
+        }
+    }
     // hand over from the caller's stream (image copies) to the batch's stream
-    CNNCRF_CUDA(cudaEventRecord(b->in_ev, b->st));
-    CNNCRF_CUDA(cudaStreamWaitEvent(b->work, b->in_ev, 0));
+    CNNCRF_CUDA(cudaEventRecord(in_ev, st));
+    CNNCRF_CUDA(cudaStreamWaitEvent(work, in_ev, 0));
     int rc = CNNCRF_OK;
-    const bool same = b->giters == iterations && b->gL1 == L1 && b->gL2 == L2 && b->gdelta == delta &&
-                      b->glambda == lambda_reg;
-    if (b->use_graph && b->exec && same) {
-        cudaError_t e = cudaGraphLaunch(b->exec, b->work);
+    const bool same = giters == iterations && gL1 == L1 && gL2 == L2 && gdelta == delta && glambda == lambda_reg &&
+                      gptrs == ptrs;
+    const bool graph = use_graph && capturable;
+    if (graph && exec && same) {
+        cudaError_t e = cudaGraphLaunch(exec, work);
         if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
-    } else if (!b->use_graph || !b->ran_eager || !same) {
+    } else if (!graph || !ran_eager || !same) {
         // eager (it also sets every kernel attribute); with graphs on, the
         // next run with the same parameters captures
-        if (b->exec) {
-            cudaGraphExecDestroy(b->exec);
-            b->exec = nullptr;
+        if (exec) {
+            cudaGraphExecDestroy(exec);
+            exec = nullptr;
         }
-        rc = b->enqueue(L1, L2, delta, iterations, lambda_reg);
-        b->ran_eager = rc == CNNCRF_OK;
-        b->giters = iterations, b->gL1 = L1, b->gL2 = L2, b->gdelta = delta, b->glambda = lambda_reg;
+        rc = enqueue(L1, L2, delta, iterations, lambda_reg);
+        ran_eager = rc == CNNCRF_OK;
+        giters = iterations, gL1 = L1, gL2 = L2, gdelta = delta, glambda = lambda_reg;
+        gptrs = ptrs;
     } else {
-        cudaGraph_t graph = nullptr;
-        cudaError_t e = cudaStreamBeginCapture(b->work, cudaStreamCaptureModeRelaxed);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(work, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) {
             rc = fail(CNNCRF_ECUDA, "batch: begin capture: %s", cudaGetErrorString(e));
         } else {
-            rc = b->enqueue(L1, L2, delta, iterations, lambda_reg);
-            e = cudaStreamEndCapture(b->work, &graph);
+            rc = enqueue(L1, L2, delta, iterations, lambda_reg);
+            e = cudaStreamEndCapture(work, &g);
             if (rc == CNNCRF_OK && e != cudaSuccess)
                 rc = fail(CNNCRF_ECUDA, "batch: graph capture failed: %s", cudaGetErrorString(e));
             if (rc == CNNCRF_OK) {
-                e = cudaGraphInstantiateWithFlags(&b->exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+                e = cudaGraphInstantiateWithFlags(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
                 if (e != cudaSuccess) {
-                    b->exec = nullptr;
+                    exec = nullptr;
                     rc = fail(CNNCRF_ECUDA, "batch: graph instantiation failed: %s", cudaGetErrorString(e));
                 }
             }
-            if (graph) cudaGraphDestroy(graph);
+            if (g) cudaGraphDestroy(g);
             if (rc == CNNCRF_OK) {
-                e = cudaGraphLaunch(b->exec, b->work);
+                e = cudaGraphLaunch(exec, work);
                 if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
             }
         }
     }
     // hand back: the caller's stream sees the results after this point
-    CNNCRF_CUDA(cudaEventRecord(b->out_ev, b->work));
-    CNNCRF_CUDA(cudaStreamWaitEvent(b->st, b->out_ev, 0));
+    CNNCRF_CUDA(cudaEventRecord(out_ev, work));
+    CNNCRF_CUDA(cudaStreamWaitEvent(st, out_ev, 0));
+    return rc;
+}
+
+int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
+{
+    clear_error();
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    b->h_left = b->h_right = nullptr;
+    b->h_out = nullptr;
+    return b->run(L1, L2, delta, iterations, lambda_reg);
+}
+
+int cnncrf_batch_run_host(cnncrf_batch_t b, const float *const *h_left, const float *const *h_right,
+                          float *const *h_out, float L1, float L2, float delta, int iterations, float lambda_reg)
+{
+    clear_error();
+    if (!b || !h_left || !h_right) return fail(CNNCRF_EINVAL, "run_host: null argument");
+    for (size_t i = 0; i < b->loc.size(); ++i)
+        if (!h_left[i] || !h_right[i]) return fail(CNNCRF_EINVAL, "run_host: null image of pair %zu", i);
+    b->h_left = h_left, b->h_right = h_right, b->h_out = h_out;
+    const int rc = b->run(L1, L2, delta, iterations, lambda_reg);
+    b->h_left = b->h_right = nullptr;
+    b->h_out = nullptr;
     return rc;
 }
 

@@ -15,17 +15,22 @@
 // W x H x D <= 8 million labels; larger ones are rejected.
 //
 // On the host the name g_crf_scratch is only a stand-in, not a device
-// address.  The first call on each device looks the real address up with
-// cudaGetSymbolAddress (with that device current) and caches it; make that
-// first call before any stream capture.
+// address.  The first call in each CUDA context (per device, and again after
+// the device's primary context was reset) looks the real address up with
+// cudaGetSymbolAddress, with that device current, and caches it under the
+// context's unique id; that first call must come before any stream capture,
+// and a first call made on a capturing stream is refused with ESTATE.
 //
 // All calls share the one array and it keeps whatever the last call left in
 // it; the solver writes every scratch value before it reads it, so nothing
 // has to start at zero.  Calls whose work overlaps on the GPU (different
 // streams, or different host threads on the same device) race on the array
 // and must be serialised by the caller.
+#include <cuda.h>
+
 #include <map>
 #include <mutex>
+#include <utility>
 
 #include "common.h"
 #include "kernels.h"
@@ -37,24 +42,69 @@ constexpr size_t kStaticScratchBytes = 64ull << 20;
 static __device__ __align__(256) unsigned char g_crf_scratch[kStaticScratchBytes];
 
 std::mutex g_mu;
-std::map<int, void *> g_addr; // device -> address of g_crf_scratch on it
+// (device, context id) -> address of g_crf_scratch in that context
+std::map<std::pair<int, unsigned long long>, void *> g_addr;
 
-int scratch_address(void **out)
+// The unique id of the calling thread's current context (cuCtxGetId), through
+// the runtime's driver entry points so the library needs no link to libcuda.
+// 0 when the driver does not offer it: the address is then looked up on
+// every call instead of cached.
+unsigned long long current_context_id()
+{
+    using GetCurrent = CUresult (*)(CUcontext *);
+    using GetId = CUresult (*)(CUcontext, unsigned long long *);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        cudaDriverEntryPointQueryResult q;
+        void *f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (GetCurrent)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (GetId)f;
+        (void)cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
+
+int scratch_address(cudaStream_t st, void **out)
 {
     int dev = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));
+    // a query that capture allows; it also makes the device's primary context
+    // current on this thread, so the context id below is the one the solve runs in
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    CNNCRF_CUDA(cudaStreamIsCapturing(st, &cs));
+    const unsigned long long ctx = current_context_id();
     std::lock_guard<std::mutex> lk(g_mu);
-    auto it = g_addr.find(dev);
-    if (it != g_addr.end()) {
-        *out = it->second;
-        return CNNCRF_OK;
+    if (ctx != 0) {
+        auto it = g_addr.find({dev, ctx});
+        if (it != g_addr.end()) {
+            *out = it->second;
+            return CNNCRF_OK;
+        }
     }
+    // the lookup may load this library's device code into the context, which
+    // a stream capture does not allow
+    if (cs != cudaStreamCaptureStatusNone)
+        return cnncrf::fail(CNNCRF_ESTATE,
+                            "crf_solve_static: the first call on device %d (and the first after a context reset) "
+                            "must run outside stream capture: it looks up the scratch array's address",
+                            dev);
     void *p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_crf_scratch);
     if (e != cudaSuccess || !p)
         return cnncrf::fail(CNNCRF_ECUDA, "crf_solve_static: cudaGetSymbolAddress failed on device %d: %s", dev,
                             cudaGetErrorString(e));
-    g_addr[dev] = p;
+    if (ctx != 0) g_addr[{dev, ctx}] = p;
     *out = p;
     return CNNCRF_OK;
 }
@@ -67,7 +117,10 @@ extern "C" int cnncrf_crf_solve_static(const float *d_cost, const float *d_wx, c
 {
     using namespace cnncrf;
     clear_error();
+    // the options first, in cnncrf_crf_solve's order, then the sizes
     if (!opt) return fail(CNNCRF_EINVAL, "crf_solve_static: null options");
+    k::CrfParams p;
+    CNNCRF_TRY(k::crf_params(opt, &p));
     if (width < 1 || height < 1 || depth < 1)
         return fail(CNNCRF_EINVAL, "crf_solve_static: bad size %dx%dx%d", width, height, depth);
     const size_t need = k::crf_workspace_bytes(width, height, depth);
@@ -76,19 +129,8 @@ extern "C" int cnncrf_crf_solve_static(const float *d_cost, const float *d_wx, c
                     "crf_solve_static: a %dx%dx%d problem needs %zu bytes of scratch, the built-in array holds "
                     "%zu (64 MiB); use cnncrf_crf_solve with a caller workspace",
                     width, height, depth, need, kStaticScratchBytes);
-    int delta = (int)opt->delta;
-    if ((float)delta != opt->delta || delta < 1 || delta > 4)
-        return fail(CNNCRF_EUNSUPPORTED, "crf_solve_static: delta %g must be an integer in 1..4", opt->delta);
-    if (opt->shape != CNNCRF_RHO_STEP && opt->shape != CNNCRF_RHO_LINEAR)
-        return fail(CNNCRF_EINVAL, "crf_solve_static: shape %d", opt->shape);
-    k::CrfParams p;
-    p.L1 = opt->L1;
-    p.L2 = opt->L2;
-    p.delta = delta;
-    p.shape = opt->shape;
-    p.slack = opt->slack;
     void *ws = nullptr;
-    CNNCRF_TRY(scratch_address(&ws));
+    CNNCRF_TRY(scratch_address((cudaStream_t)stream, &ws));
     return k::crf_solve(d_cost, d_wx, d_wy, width, height, depth, p, opt->total_it, d_labels, ws,
                         kStaticScratchBytes, lower_bound, (cudaStream_t)stream);
 }

@@ -6,6 +6,8 @@
 
 #include <cstdint>
 
+#include "../../include/cnncrf.h"
+
 namespace cnncrf {
 namespace k {
 
@@ -187,6 +189,11 @@ struct CrfParams {
     int shape;
     float slack;
 };
+// the solver's options as the C ABI passes them (ops slots L1, L2, delta,
+// total_it of stereo/stereo.cpp:149-152): EUNSUPPORTED for a delta that is not
+// an integer in 1..4, EINVAL for an unknown shape; shared by every entry point
+// that takes a cnncrf_crf_options so all of them check in the same order
+int crf_params(const cnncrf_crf_options *opt, CrfParams *p);
 // workspace layout helpers
 size_t crf_workspace_bytes(int W, int H, int D, int npairs = 1);
 // npairs pairs at once: cost [n][H][W][D], weights [n][2][H][W] (wx, wy),
@@ -228,9 +235,13 @@ int nchw_to_nhwc(const float *in, float *out, int C, long npx, cudaStream_t st);
 int bf16_to_f32(const void *in, int cs, int C, long npx, float *out, cudaStream_t st);
 int warp_rgba(float *out, const float *in, const float *u, int W, int H, cudaStream_t st);
 int tv_fit(const float *vol3, float *qf, int W, int H, float step, float lam, cudaStream_t st);
+// TV/Huber primal-dual iterations, fused (k_tv.cu): from (u, p, q), or from
+// (u, 0, 0) when pq_zero, `iters` iterations; the state ends in (u, p, q), the
+// last iteration's u_ in u_.  ws >= tv_workspace_bytes(W, H), 256-byte aligned.
+size_t tv_workspace_bytes(int W, int H);
 int tv_iterate(float *u, float *u_, const float *u0, const float *qf, float *p, float *q,
                const float *wx, const float *wy, int W, int H, float C, float eps, float step,
-               int iters, cudaStream_t st);
+               int iters, void *ws, size_t ws_bytes, bool pq_zero, cudaStream_t st);
 
 } // namespace k
 } // namespace cnncrf

@@ -23,6 +23,21 @@ struct cnncrf_slackprop {
     bool ran = false;
 };
 
+int cnncrf::k::crf_params(const cnncrf_crf_options *opt, k::CrfParams *p)
+{
+    int delta = (int)opt->delta;
+    if ((float)delta != opt->delta || delta < 1 || delta > 4)
+        return fail(CNNCRF_EUNSUPPORTED, "crf: delta %g must be an integer in 1..4", opt->delta);
+    if (opt->shape != CNNCRF_RHO_STEP && opt->shape != CNNCRF_RHO_LINEAR)
+        return fail(CNNCRF_EINVAL, "crf: shape %d", opt->shape);
+    p->L1 = opt->L1;
+    p->L2 = opt->L2;
+    p->delta = delta;
+    p->shape = opt->shape;
+    p->slack = opt->slack;
+    return CNNCRF_OK;
+}
+
 extern "C" {
 
 int cnncrf_set_conv_pairs(int enable)
@@ -90,20 +105,6 @@ int cnncrf_crf_workspace_size(int width, int height, int depth, size_t *bytes)
     return CNNCRF_OK;
 }
 
-static int crf_params(const cnncrf_crf_options *opt, k::CrfParams *p)
-{
-    int delta = (int)opt->delta;
-    if ((float)delta != opt->delta || delta < 1 || delta > 4)
-        return fail(CNNCRF_EUNSUPPORTED, "crf: delta %g must be an integer in 1..4", opt->delta);
-    if (opt->shape != CNNCRF_RHO_STEP && opt->shape != CNNCRF_RHO_LINEAR)
-        return fail(CNNCRF_EINVAL, "crf: shape %d", opt->shape);
-    p->L1 = opt->L1;
-    p->L2 = opt->L2;
-    p->delta = delta;
-    p->shape = opt->shape;
-    p->slack = opt->slack;
-    return CNNCRF_OK;
-}
 
 int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, int width, int height, int depth,
                      const cnncrf_crf_options *opt, int32_t *d_labels, double *lower_bound, void *d_workspace,
@@ -112,7 +113,7 @@ int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, 
     clear_error();
     if (!opt) return fail(CNNCRF_EINVAL, "crf: null options");
     k::CrfParams p;
-    CNNCRF_TRY(crf_params(opt, &p));
+    CNNCRF_TRY(k::crf_params(opt, &p));
     return k::crf_solve(d_cost, d_wx, d_wy, width, height, depth, p, opt->total_it, d_labels, d_workspace,
                         workspace_bytes, lower_bound, (cudaStream_t)stream);
 }
@@ -124,7 +125,7 @@ int cnncrf_crf_autotune(const float *d_cost, const float *d_wx, const float *d_w
     clear_error();
     if (!opt) return fail(CNNCRF_EINVAL, "crf: null options");
     k::CrfParams p;
-    CNNCRF_TRY(crf_params(opt, &p));
+    CNNCRF_TRY(k::crf_params(opt, &p));
     return k::crf_autotune(d_cost, d_wx, d_wy, 0, width, height, depth, 1, p, d_workspace, workspace_bytes,
                            (cudaStream_t)stream);
 }
@@ -190,7 +191,7 @@ int cnncrf_slackprop_execute(cnncrf_slackprop_t sp)
     if (!sp || !sp->cost) return fail(CNNCRF_ESTATE, "slackprop: execute before init");
     if (!sp->wx) return fail(CNNCRF_ESTATE, "slackprop: execute before update_W");
     k::CrfParams p;
-    CNNCRF_TRY(crf_params(&sp->ops, &p));
+    CNNCRF_TRY(k::crf_params(&sp->ops, &p));
     CNNCRF_TRY(k::crf_solve(sp->cost, sp->wx, sp->wy, sp->W, sp->H, sp->D, p, sp->ops.total_it, sp->labels,
                             sp->ws.get(), sp->ws.size(), &sp->lb, sp->st));
     sp->ran = true;
@@ -237,17 +238,24 @@ int cnncrf_tv_fit(const float *d_volume3, float *d_qf, int width, int height, fl
     return k::tv_fit(d_volume3, d_qf, width, height, disp_step, lambda_census, (cudaStream_t)stream);
 }
 
+int cnncrf_tv_workspace_size(int width, int height, size_t *bytes)
+{
+    if (!bytes || width < 1 || height < 1) return fail(CNNCRF_EINVAL, "tv_workspace_size: bad argument");
+    *bytes = k::tv_workspace_bytes(width, height);
+    return CNNCRF_OK;
+}
+
 int cnncrf_tv_iterate(float *d_u, float *d_u_, const float *d_u0, const float *d_qf, float *d_p, float *d_q,
                       const float *d_wx, const float *d_wy, int width, int height, float C, float huber_eps,
-                      float disp_step, int iterations, cnncrf_stream_t stream)
+                      float disp_step, int iterations, void *d_workspace, size_t workspace_bytes,
+                      cnncrf_stream_t stream)
 {
+    clear_error();
     if (!d_u || !d_u_ || !d_u0 || !d_qf || !d_p || !d_q || !d_wx || !d_wy)
         return fail(CNNCRF_EINVAL, "tv_iterate: null argument");
-    cudaStream_t st = (cudaStream_t)stream;
-    CNNCRF_CUDA(cudaMemsetAsync(d_p, 0, sizeof(float) * 2 * (size_t)width * height, st));
-    CNNCRF_CUDA(cudaMemsetAsync(d_q, 0, sizeof(float) * 2 * (size_t)width * height, st));
+    // p = q = 0 at the start (stereo/stereo.cu:1133-1135)
     return k::tv_iterate(d_u, d_u_, d_u0, d_qf, d_p, d_q, d_wx, d_wy, width, height, C, huber_eps, disp_step,
-                         iterations, st);
+                         iterations, d_workspace, workspace_bytes, true, (cudaStream_t)stream);
 }
 
 // ---------------------------------------------------------------- census, edge weights, QuadDirect, LR check

@@ -28,7 +28,7 @@ struct cnncrf_stereo {
     bool xavier = false;
     uint64_t seed = 0;
     int with_xy = 0;
-    DevBuf img[2], padded[2], warped, warped_pad, vol, pw, out, labels, out_, out0, qf, p, q, vol3;
+    DevBuf img[2], padded[2], warped, warped_pad, vol, pw, out, labels, out_, out0, qf, p, q, vol3, tvws;
     DevBuf gray[2], gtmp, gtmp2, gw, dlist; // census and edge weights
     std::vector<float> dlist_host;          // host copy of the census disparity list
     int filter_size = 7;                    // stereo/stereo_img.cpp:73
@@ -223,6 +223,7 @@ int cnncrf_stereo_initialize(cnncrf_stereo_t s, int width, int height, float dis
     CNNCRF_TRY(s->qf.reserve(2 * n * sizeof(float)));
     CNNCRF_TRY(s->p.reserve(2 * n * sizeof(float)));
     CNNCRF_TRY(s->q.reserve(2 * n * sizeof(float)));
+    CNNCRF_TRY(s->tvws.reserve(k::tv_workspace_bytes(width, height)));
     CNNCRF_TRY(s->vol3.reserve(3 * n * sizeof(float)));
     for (int i = 0; i < 2; ++i) CNNCRF_TRY(s->gray[i].reserve(n * sizeof(float)));
     CNNCRF_TRY(s->gtmp.reserve(n * sizeof(float)));
@@ -407,8 +408,6 @@ int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, floa
     float lam_c = 1.0f / lambda_reg; // stereo/stereo.cpp:395
     float step = s->dstep;
     float hq = (float)((double)step * 0.25), mn = (float)(-(double)step * 0.25);
-    CNNCRF_CUDA(cudaMemsetAsync(s->p.get(), 0, 2 * n * sizeof(float), st));
-    CNNCRF_CUDA(cudaMemsetAsync(s->q.get(), 0, 2 * n * sizeof(float), st));
     CNNCRF_TRY(k::pad_rgba(s->img[0].as<float>(), W, H, net->pad, s->padded[0].as<float>(), st));
     for (int w = 0; w < warps; ++w) {
         CNNCRF_TRY(k::warp_rgba(s->warped.as<float>(), s->img[1].as<float>(), s->out.as<float>(), W, H, st));
@@ -421,9 +420,10 @@ int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, floa
         CNNCRF_TRY(k::tv_fit(s->vol3.as<float>(), s->qf.as<float>(), W, H, step, lam_c, st));
         CNNCRF_CUDA(cudaMemcpyAsync(s->out0.get(), s->out.get(), n * sizeof(float), cudaMemcpyDeviceToDevice, st));
         // predict rewrote wx / wy (they alias the pairwise output) without lambda
+        // p = q = 0 before the first warp (stereo/stereo.cu:1133-1135); later warps continue from them
         CNNCRF_TRY(k::tv_iterate(s->out.as<float>(), s->out_.as<float>(), s->out0.as<float>(), s->qf.as<float>(),
                                  s->p.as<float>(), s->q.as<float>(), s->pw.as<float>(), s->pw.as<float>() + n, W, H, C,
-                                 s->o.huber_eps, step, iterations, st));
+                                 s->o.huber_eps, step, iterations, s->tvws.get(), s->tvws.size(), w == 0, st));
     }
     return s->record(3);
 }

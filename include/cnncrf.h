@@ -209,8 +209,11 @@ int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, 
  * loop that cannot afford a device-wide allocation stall.
  * Limit: cnncrf_crf_workspace_size(width, height, depth) <= 64 MiB (about
  * 8 million labels W*H*D); larger problems return CNNCRF_EINVAL.
- * The first call on each device looks up the array's address and caches it;
- * make that first call before any stream capture.
+ * Errors are checked in cnncrf_crf_solve's order: the options first, then the
+ * sizes.  The first call in each CUDA context (per device, and again after a
+ * reset of the device's primary context) looks up the array's address and
+ * caches it; make that first call before any stream capture: a first call on
+ * a capturing stream returns CNNCRF_ESTATE.
  * Nothing in the array has to start at zero.  All calls on a device share the
  * one array: calls that overlap on the GPU (other streams, other threads)
  * race and must be serialised by the caller. */
@@ -292,11 +295,16 @@ int cnncrf_tv_fit(const float *d_volume3, float *d_qf, int width, int height, fl
 /* The inner loop of cuda::fuseTHuberQuadFit (stereo/stereo.cu:1133-1135,1159-1166):
  * p = q = 0, then `iterations` x (u_ = u; primal; dual) with tau = sigma = 1/sqrt(8).
  * d_u, d_u_, d_u0: H x W; d_qf, d_p, d_q: H x W x 2; huber_eps = 0.1 in the
- * reference (stereo/stereo.cu:792). */
+ * reference (stereo/stereo.cu:792).  The iterations run fused, several per
+ * launch on tiles held on chip (the results equal the reference's
+ * per-iteration passes), and need a device workspace of
+ * cnncrf_tv_workspace_size bytes, 256-byte aligned; u, u_, p and q hold the
+ * final state on return. */
+int cnncrf_tv_workspace_size(int width, int height, size_t *bytes);
 int cnncrf_tv_iterate(float *d_u, float *d_u_, const float *d_u0, const float *d_qf, float *d_p,
                       float *d_q, const float *d_wx, const float *d_wy, int width, int height,
                       float C, float huber_eps, float disp_step, int iterations,
-                      cnncrf_stream_t stream);
+                      void *d_workspace, size_t workspace_bytes, cnncrf_stream_t stream);
 
 /* ---------------------------------------------------------------- census, edges, QuadDirect, LR */
 
@@ -523,6 +531,19 @@ int cnncrf_batch_use_graph(cnncrf_batch_t b, int enable);
  * for every pair; asynchronous on the batch's stream. */
 int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations,
                      float lambda_reg);
+/* cnncrf_batch_run with the images taken from and the disparities returned to
+ * host memory as part of the pipeline (no reference counterpart: Stereo's
+ * setColorImages / getOutput, stereo/stereo.cpp:117-126,412-416, per pair).
+ * h_left[i], h_right[i]: pair i's RGBA images (H x W x 4 floats); h_out[i]:
+ * pair i's H x W disparities, or h_out / h_out[i] NULL for none.  Each group's
+ * host-to-device copies run ahead of its CNN on a copy stream, its
+ * device-to-host copies right after its remap, so copies overlap the other
+ * groups' work.  Asynchronous: h_out holds the results once the batch's
+ * stream is synchronised (cnncrf_batch_check).  Graph replay needs the same
+ * buffers as the captured run and page-locked ones; other calls run eagerly. */
+int cnncrf_batch_run_host(cnncrf_batch_t b, const float *const *h_left, const float *const *h_right,
+                          float *const *h_out, float L1, float L2, float delta, int iterations,
+                          float lambda_reg);
 int cnncrf_batch_get_output(cnncrf_batch_t b, int pair, float *h_out);
 int cnncrf_batch_get_output_device(cnncrf_batch_t b, int pair, const float **d_out);
 int cnncrf_batch_get_labels_device(cnncrf_batch_t b, int pair, const int32_t **d_labels);

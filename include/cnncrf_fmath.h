@@ -22,7 +22,8 @@
  * -ffp-contract=off; device: explicit __fmaf_rn, --fmad=false) gives the same
  * result on x86-64, aarch64 and sm_103a.
  *
- * Accuracy (checked by tests/test_fmath.py against float64 references):
+ * Accuracy (checked by tests/test_oracle.py::test_tanh_exp_accuracy against
+ * float64 references):
  * exp, expm1 <= 2 ulp; tanh <= 3 ulp.  Results below FLT_MIN flush to 0.
  */
 #ifndef CNNCRF_FMATH_H

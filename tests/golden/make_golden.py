@@ -23,7 +23,8 @@ data/parameters/kitti-2015/7-layer/cnn+crf+full/params.npz (copied here as a
 fixture).  The CRF solver has no reference to pin against (absent
 dependency); see cnncrf_oracle.h.
 
-usage: python tests/golden/make_golden.py /root/reference
+usage: python tests/golden/make_golden.py REFERENCE_ROOT
+(REFERENCE_ROOT: the directory of the reference checkout, which holds data/)
 """
 import os
 import shutil
@@ -155,4 +156,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py REFERENCE_ROOT")
+    main(sys.argv[1])

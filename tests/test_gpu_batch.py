@@ -24,7 +24,10 @@ def single_run(L, scene, prec, dmax, layers, iters, crf):
 @pytest.mark.parametrize("prec_name,group_size", [("FP32", 0), ("BF16", 0), ("BF16", 2)])
 def test_batch_equals_single(cuda, prec_name, group_size):
     """group_size 2 splits the three same-shape pairs into a pipelined group of
-    two and a group of one."""
+    two and a group of one.  The batch's CRF skips the last V pass's phi
+    store (no caller of the batch reads C1) while the single-pair solve keeps
+    it, so the exact equality of labels and bounds here also pins that the
+    skipped store changes neither."""
     from cnncrf import scenes, _lib as L
     from cnncrf.api import StereoBatch
     prec = getattr(L, prec_name)

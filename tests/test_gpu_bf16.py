@@ -84,7 +84,7 @@ def test_bf16_features_and_weights_vs_fp32_oracle(cuda, oracle):
 
 def test_bf16_pipeline_label_change(cuda, oracle):
     """BF16 vs FP32 Stereo path on one KITTI-shaped scene: fraction of pixels
-    whose integer disparity changes (the metric's bound is 0.5%)."""
+    whose integer disparity changes, held to the metric's bound of 0.5 %."""
     from cnncrf import scenes, _lib as L
     from cnncrf.api import Stereo
     W, H, D = 320, 96, 64
@@ -102,4 +102,4 @@ def test_bf16_pipeline_label_change(cuda, oracle):
         labs.append(st.labels_device().cpu().numpy())
     changed = float((labs[0] != labs[1]).mean())
     print("BF16 vs FP32 label change: %.4f" % changed)
-    assert changed <= 0.01
+    assert changed <= 0.005

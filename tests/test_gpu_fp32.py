@@ -176,6 +176,51 @@ def test_remap_warp_fit_tv(cuda, oracle):
         assert np.array_equal(a.cpu().numpy(), b)
 
 
+@pytest.mark.parametrize("W,H", [(33, 21), (130, 70), (201, 97)])
+@pytest.mark.parametrize("iters", [1, 4, 8, 9, 17])
+def test_tv_fused_tiles_and_launches(cuda, oracle, W, H, iters):
+    """The fused TV kernel (K iterations per launch on 64 x 32 tiles with a
+    K-pixel halo, at most 8 per launch) against the oracle's per-iteration
+    loop, bit for bit in u, u_, p and q: one tile and many, ragged image
+    edges, one launch, two launches, three (the state then ends in the
+    caller's buffers from either ping-pong parity)."""
+    torch = cuda
+    from cnncrf import api
+    rng = np.random.default_rng(W * 1000 + H + iters)
+    u0 = (rng.random((H, W)) * 30).astype(np.float32)
+    qf = np.stack([rng.standard_normal((H, W)), rng.random((H, W)) * 3], -1).astype(np.float32)
+    wx = (rng.random((H, W)) * 2).astype(np.float32)
+    wy = (rng.random((H, W)) * 2).astype(np.float32)
+    g = api.tv_iterate(dev(u0, torch), dev(u0, torch), dev(qf, torch), dev(wx, torch), dev(wy, torch), 1.5, 0.01,
+                       1.0, iters)
+    o = oracle.tv_iterate(u0, u0, qf, wx, wy, 1.5, 0.01, 1.0, iters)
+    for name, a, b in zip(("u", "u_", "p", "q"), g, o):
+        assert np.array_equal(a.cpu().numpy(), b), name
+
+
+def test_refinement_two_warps_multi_tile(cuda, oracle):
+    """fuseTHuberQuadFit with two warps on an image of several TV tiles: the
+    second warp's TV iterations start from the first warp's p and q (the
+    reference zeroes them once, stereo/stereo.cu:1133-1135), 9 iterations =
+    two fused launches per warp."""
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import Stereo
+    W, H = 150, 70
+    s = scenes.voronoi_scene(W, H, 16, seed=8, cells=6, off_range=(1, 12), slope=0.05)
+    st = Stereo(precision=L.FP32, unary=0, topology=0, ref_depth_rounding=False, crf_shape=0)
+    st.initialize(W, H, 0.0, 1.0, 15.0)
+    st.set_matching_function(L.MATCH_COLORCNN_PAIRWISE)
+    st.set_num_layers(3)
+    st.set_xavier_seed(2)
+    st.set_color_images(s["left"], s["right"])
+    st.compute_slack_propagation(1.0, 5.0, 2, 3, 0.0, 0.0, 0.8)
+    st.fuse_thuber_quad_fit(0.8, 5.0, 9, 2)
+    cfg = oracle.make_cfg(num_layers=3, topology=0, unary=0, disp_max=15.0, lam=0.8, L1=1.0, L2=5.0, delta=2,
+                          crf_iters=3, crf_shape=0, warps=2, ref_iters=9, C=5.0)
+    r = oracle.run_pair(cfg, oracle.xavier_params(cfg, seed=2), s["left"], s["right"])
+    assert np.array_equal(st.get_output(), r["disp"])
+
+
 PIPE_CASES = [
     # topology, layers, unary, shape, rounding, D(max+1), refine
     dict(topology=0, layers=3, unary=0, shape=0, rounding=True, dmax=11.0, warps=2, L1=1.0, L2=5.0, delta=2),
