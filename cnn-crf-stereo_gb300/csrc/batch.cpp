@@ -80,14 +80,19 @@ struct cnncrf_batch {
     std::vector<std::pair<int, int>> loc; // pair -> (group, slot)
     int group_cap = 0;                    // most pairs per group (0: no cap)
     bool built = false;
-    // graph
+    // graphs: one per (parameters, run_host buffers) key, the most recent
+    // last; a key runs eagerly once (which also sets every kernel
+    // attribute), is captured by its second run and replayed after that
+    struct GraphEntry {
+        float L1, L2, delta, lambda;
+        int iters;
+        std::vector<const void *> ptrs; // host buffers baked into the copy nodes (empty: run)
+        cudaGraphExec_t exec;
+    };
+    static constexpr size_t kMaxGraphs = 4;
     bool use_graph = false;
-    cudaGraphExec_t exec = nullptr;
+    std::vector<GraphEntry> graphs;
     cudaEvent_t fork = nullptr;
-    float gL1 = 0, gL2 = 0, gdelta = 0, glambda = 0;
-    int giters = -1;
-    bool ran_eager = false;
-    std::vector<const void *> gptrs; // host buffers of run_host baked into the graph (empty: run)
 
     // host buffers of the current run_host call (null: images staged by set_images, no copy out)
     const float *const *h_left = nullptr, *const *h_right = nullptr;
@@ -95,7 +100,7 @@ struct cnncrf_batch {
 
     ~cnncrf_batch()
     {
-        if (exec) cudaGraphExecDestroy(exec);
+        invalidate();
         if (fork) cudaEventDestroy(fork);
         if (in_ev) cudaEventDestroy(in_ev);
         if (out_ev) cudaEventDestroy(out_ev);
@@ -105,10 +110,9 @@ struct cnncrf_batch {
     }
     void invalidate()
     {
-        if (exec) cudaGraphExecDestroy(exec);
-        exec = nullptr;
-        giters = -1;
-        ran_eager = false;
+        for (auto &g : graphs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+        graphs.clear();
     }
     int build();
     int enqueue(float L1, float L2, float delta, int iters, float lambda);
@@ -386,8 +390,8 @@ int cnncrf_batch_group_shape(cnncrf_batch_t b, int group, int *width, int *heigh
 }
 
 // one run of the whole batch from the caller's stream; with graphs on, the
-// first run with new parameters (or new run_host buffers) is eager, the next
-// one captures, later ones replay
+// first run of a (parameters, run_host buffers) key is eager, the next one
+// captures it, later ones replay its graph
 int cnncrf_batch::run(float L1, float L2, float delta, int iterations, float lambda_reg)
 {
     if (loc.empty()) return fail(CNNCRF_ESTATE, "batch: no pairs");
@@ -415,24 +419,26 @@ int cnncrf_batch::run(float L1, float L2, float delta, int iterations, float lam
     CNNCRF_CUDA(cudaEventRecord(in_ev, st));
     CNNCRF_CUDA(cudaStreamWaitEvent(work, in_ev, 0));
     int rc = CNNCRF_OK;
-    const bool same = giters == iterations && gL1 == L1 && gL2 == L2 && gdelta == delta && glambda == lambda_reg &&
-                      gptrs == ptrs;
-    const bool graph = use_graph && capturable;
-    if (graph && exec && same) {
-        cudaError_t e = cudaGraphLaunch(exec, work);
-        if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
-    } else if (!graph || !ran_eager || !same) {
-        // eager (it also sets every kernel attribute); with graphs on, the
-        // next run with the same parameters captures
-        if (exec) {
-            cudaGraphExecDestroy(exec);
-            exec = nullptr;
-        }
+    GraphEntry *ge = nullptr;
+    for (auto &g : graphs)
+        if (g.iters == iterations && g.L1 == L1 && g.L2 == L2 && g.delta == delta && g.lambda == lambda_reg &&
+            g.ptrs == ptrs)
+            ge = &g;
+    if (!use_graph || !capturable) {
         rc = enqueue(L1, L2, delta, iterations, lambda_reg);
-        ran_eager = rc == CNNCRF_OK;
-        giters = iterations, gL1 = L1, gL2 = L2, gdelta = delta, glambda = lambda_reg;
-        gptrs = ptrs;
-    } else {
+    } else if (ge && ge->exec) {
+        cudaError_t e = cudaGraphLaunch(ge->exec, work);
+        if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
+    } else if (!ge) { // first run of this key: eager
+        rc = enqueue(L1, L2, delta, iterations, lambda_reg);
+        if (rc == CNNCRF_OK) {
+            if (graphs.size() >= kMaxGraphs) {
+                if (graphs.front().exec) cudaGraphExecDestroy(graphs.front().exec);
+                graphs.erase(graphs.begin());
+            }
+            graphs.push_back(GraphEntry{L1, L2, delta, lambda_reg, iterations, ptrs, nullptr});
+        }
+    } else { // second run: capture, then launch
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamBeginCapture(work, cudaStreamCaptureModeRelaxed);
         if (e != cudaSuccess) {
@@ -443,15 +449,15 @@ int cnncrf_batch::run(float L1, float L2, float delta, int iterations, float lam
             if (rc == CNNCRF_OK && e != cudaSuccess)
                 rc = fail(CNNCRF_ECUDA, "batch: graph capture failed: %s", cudaGetErrorString(e));
             if (rc == CNNCRF_OK) {
-                e = cudaGraphInstantiateWithFlags(&exec, g, cudaGraphInstantiateFlagUseNodePriority);
+                e = cudaGraphInstantiateWithFlags(&ge->exec, g, cudaGraphInstantiateFlagUseNodePriority);
                 if (e != cudaSuccess) {
-                    exec = nullptr;
+                    ge->exec = nullptr;
                     rc = fail(CNNCRF_ECUDA, "batch: graph instantiation failed: %s", cudaGetErrorString(e));
                 }
             }
             if (g) cudaGraphDestroy(g);
             if (rc == CNNCRF_OK) {
-                e = cudaGraphLaunch(exec, work);
+                e = cudaGraphLaunch(ge->exec, work);
                 if (e != cudaSuccess) rc = fail(CNNCRF_ECUDA, "batch: graph launch: %s", cudaGetErrorString(e));
             }
         }

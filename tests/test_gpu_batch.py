@@ -73,6 +73,50 @@ def test_batch_graph_replay(cuda, group_size):
             assert np.array_equal(b.get_output(i), eager.get_output(i)), (rnd, i)
 
 
+@pytest.mark.parametrize("pinned", [True, False])
+def test_batch_run_host_equals_staged_run(cuda, pinned):
+    """cnncrf_batch_run_host (host images in, host disparities out, copies
+    pipelined with the groups' work) gives the same disparities as
+    set_images + run + get_output.  Page-locked buffers: the first call runs
+    eagerly, the second captures a graph, the third and fourth replay it with
+    new contents in the same buffers.  Pageable buffers run eagerly every
+    time.  A pair whose output pointer is null gets no copy."""
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import StereoBatch
+    torch = cuda
+    shapes = [(80, 32, 32)] * 3 + [(48, 24, 16)]
+    b = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=True, group_size=2)
+    ref = StereoBatch(precision=L.BF16, num_layers=3, seed=1, graph=False, group_size=2)
+    for (W, H, D) in shapes:
+        b.add_pair(W, H, 0.0, 1.0, float(D - 1))
+        ref.add_pair(W, H, 0.0, 1.0, float(D - 1))
+    host = (lambda t: t.pin_memory()) if pinned else (lambda t: t)
+    hl = [host(torch.zeros((H, W, 4), dtype=torch.float32)) for (W, H, D) in shapes]
+    hr = [host(torch.zeros((H, W, 4), dtype=torch.float32)) for (W, H, D) in shapes]
+    ho = [host(torch.full((H, W), -7.0, dtype=torch.float32)) for (W, H, D) in shapes]
+    for rnd in range(4):
+        sc = [scenes.voronoi_scene(W, H, D, seed=300 + 10 * rnd + i, cells=4, off_range=(1, D - 2))
+              for i, (W, H, D) in enumerate(shapes)]
+        for i, s in enumerate(sc):
+            hl[i].copy_(torch.from_numpy(s["left"]))
+            hr[i].copy_(torch.from_numpy(s["right"]))
+            ref.set_images(i, s["left"], s["right"])
+        outs = list(ho)
+        outs[1] = None  # no copy out for pair 1
+        ho[1].fill_(-7.0)
+        b.run_host(hl, hr, outs, 0.5, 1.5, 3, 4)
+        b.check()
+        ref.run(0.5, 1.5, 3, 4)
+        ref.check()
+        for i in range(len(shapes)):
+            want = ref.get_output(i)
+            if i == 1:
+                assert (ho[1].numpy() == -7.0).all()
+                assert np.array_equal(b.output_device(1).cpu().numpy(), want)
+            else:
+                assert np.array_equal(ho[i].numpy(), want), (rnd, i)
+
+
 def test_net_batch_of_two(cuda, oracle):
     """StereoNet with n = 2: each pair's volume equals the oracle's."""
     torch = cuda
