@@ -155,6 +155,7 @@ PROTOS = {
     "cnncrf_batch_set_images_device": ([vp, i32, vp, vp], i32),
     "cnncrf_batch_use_graph": ([vp, i32], i32),
     "cnncrf_batch_run": ([vp, f32, f32, f32, i32, f32], i32),
+    "cnncrf_batch_keep_volume": ([vp, i32], i32),
     "cnncrf_batch_run_host": ([vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), f32, f32, f32, i32, f32], i32),
     "cnncrf_batch_get_output": ([vp, i32, vp], i32),
     "cnncrf_batch_get_output_device": ([vp, i32, C.POINTER(vp)], i32),

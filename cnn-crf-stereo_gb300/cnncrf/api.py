@@ -454,7 +454,7 @@ class StereoBatch:
     def __init__(self, precision=L.BF16, unary=L.UNARY_ONE_MINUS_DOT, topology=L.TOPO_ALL3X3,
                  feat_channels=100, pw_channels=64, ref_depth_rounding=False, crf_shape=L.RHO_LINEAR,
                  crf_slack=0.5, matching=L.MATCH_COLORCNN_PAIRWISE, num_layers=7, with_xy=False,
-                 param_base=None, seed=0, graph=False, stream=None, group_size=0):
+                 param_base=None, seed=0, graph=False, stream=None, group_size=0, keep_volume=False):
         o = StereoOptions()
         call("cnncrf_stereo_default_options", C.byref(o))
         o.precision, o.unary, o.topology = precision, unary, topology
@@ -468,6 +468,8 @@ class StereoBatch:
              None if param_base is None else str(param_base).encode(), seed)
         call("cnncrf_batch_use_graph", self._h, 1 if graph else 0)
         call("cnncrf_batch_set_group_size", self._h, group_size)
+        # BF16: also write the FP32 volume (else only the CRF's 16-bit copy, and volume_device() fails)
+        call("cnncrf_batch_keep_volume", self._h, 1 if keep_volume else 0)
         self.shapes = []
 
     def __del__(self):

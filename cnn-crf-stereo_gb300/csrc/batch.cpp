@@ -40,12 +40,13 @@ struct Group {
     int W = 0, H = 0, depth = 0;
     float dmin = 0, dstep = 1, dmax = 0;
     std::vector<int> members; // global pair indices, in batch order
-    DevBuf img[2], padded[2], vol, pw, out, labels, ws;
+    DevBuf img[2], padded[2], vol, volq, pw, out, labels, ws;
     cnncrf_net_t net = nullptr;
     cudaStream_t stream = nullptr;     // CNN part (high priority)
     cudaStream_t crf_stream = nullptr; // CRF part (low priority)
     cudaEvent_t cnn_done = nullptr, done = nullptr, in_done = nullptr;
     size_t ws_bytes = 0;
+    bool vol_written = true; // the FP32 volume holds the last run's costs (else only volq does)
     ~Group()
     {
         if (net) cnncrf_net_destroy(net);
@@ -79,6 +80,7 @@ struct cnncrf_batch {
     std::vector<std::unique_ptr<Group>> groups;
     std::vector<std::pair<int, int>> loc; // pair -> (group, slot)
     int group_cap = 0;                    // most pairs per group (0: no cap)
+    bool keep_volume = false;             // BF16: also write the FP32 volume (cnncrf_batch_keep_volume)
     bool built = false;
     // graphs: one per (parameters, run_host buffers) key, the most recent
     // last; a key runs eagerly once (which also sets every kernel
@@ -155,12 +157,18 @@ int cnncrf_batch::build()
             CNNCRF_TRY(g.padded[s].reserve(sizeof(float) * 4 * (size_t)(g.W + 2 * pad) * (g.H + 2 * pad) * n));
         }
         CNNCRF_TRY(g.vol.reserve(sizeof(float) * N * g.depth * n));
+        // the BF16 path's CRF reads the volume's 16-bit fixed-point copy, which the correlation writes instead
+        // of the FP32 volume (no caller of the batch reads that; the CRF's winner-take-all at 0 iterations does)
+        k::UnaryQ16 uq;
+        if (o.precision == CNNCRF_BF16 && k::crf_reads_q16(g.depth) && k::unary_q16(o.unary, &uq))
+            CNNCRF_TRY(g.volq.reserve(2 * N * g.depth * n));
         CNNCRF_TRY(g.pw.reserve(sizeof(float) * 2 * N * n));
         CNNCRF_TRY(g.out.reserve(sizeof(float) * N * n));
         CNNCRF_TRY(g.labels.reserve(sizeof(int32_t) * N * n));
         g.ws_bytes = k::crf_workspace_bytes(g.W, g.H, g.depth, n);
         CNNCRF_TRY(g.ws.reserve(g.ws_bytes));
         CNNCRF_TRY(cnncrf_net_init(g.net, g.dmin, g.dmax, g.dstep, 0, g.vol.as<float>(), g.pw.as<float>()));
+        g.net->volq = g.volq.get();
         if (g.net->D != g.depth)
             return fail(CNNCRF_ESHAPE, "batch: disparity list has %d entries, volume depth %d", g.net->D, g.depth);
         if (xavier) CNNCRF_TRY(cnncrf_net_init_xavier(g.net, seed));
@@ -184,6 +192,8 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
     int di = (int)delta;
     if ((float)di != delta || di < 1 || di > 4) return fail(CNNCRF_EUNSUPPORTED, "batch: delta %g", delta);
     p.L1 = L1, p.L2 = L2, p.delta = di, p.shape = o.crf_shape, p.slack = o.crf_slack;
+    k::UnaryQ16 uq{1.0f, 0.0f};
+    k::unary_q16(o.unary, &uq);
     CNNCRF_CUDA(cudaEventRecord(fork, work));
     if (h_left) CNNCRF_CUDA(cudaStreamWaitEvent(copy, fork, 0));
     cudaEvent_t prev = fork;
@@ -208,14 +218,17 @@ int cnncrf_batch::enqueue(float L1, float L2, float delta, int iters, float lamb
         const int pad = g.net->pad;
         CNNCRF_TRY(k::pad_rgba(g.img[0].as<float>(), g.W, g.H, pad, g.padded[0].as<float>(), gs, n));
         CNNCRF_TRY(k::pad_rgba(g.img[1].as<float>(), g.W, g.H, pad, g.padded[1].as<float>(), gs, n));
+        g.net->vol_fp32 = keep_volume || iters <= 0;
         CNNCRF_TRY(g.net->predict(g.padded[0].as<float>(), g.padded[1].as<float>()));
+        g.vol_written = !(g.net->volq_valid && !g.net->vol_fp32);
         CNNCRF_TRY(k::scale(g.pw.as<float>(), 2 * N * n, lambda, gs)); // stereo/stereo.cpp:136-137
         CNNCRF_CUDA(cudaEventRecord(g.cnn_done, gs));
         prev = g.cnn_done;
         CNNCRF_CUDA(cudaStreamWaitEvent(cs, g.cnn_done, 0));
         CNNCRF_TRY(k::crf_solve_batch(g.vol.as<float>(), g.pw.as<float>(), g.W, g.H, g.depth, n, p, iters,
                                       g.labels.as<int32_t>(), g.ws.get(), g.ws_bytes, cs,
-                                      false)); // labels and bounds only: the last phi is dead
+                                      false, // labels and bounds only: the last phi is dead
+                                      g.net->volq_valid ? g.volq.get() : nullptr, uq));
         CNNCRF_TRY(k::remap(g.out.as<float>(), g.labels.as<int32_t>(), N * n, g.dmin, g.dstep, cs));
         if (h_out)
             for (int m = 0; m < n; ++m)
@@ -314,6 +327,14 @@ int cnncrf_batch_set_group_size(cnncrf_batch_t b, int max_pairs)
     return CNNCRF_OK;
 }
 
+int cnncrf_batch_keep_volume(cnncrf_batch_t b, int enable)
+{
+    if (!b) return fail(CNNCRF_EINVAL, "null batch");
+    b->keep_volume = enable != 0;
+    b->invalidate(); // the captured correlations write one volume or the other
+    return CNNCRF_OK;
+}
+
 int cnncrf_batch_num_pairs(cnncrf_batch_t b, int *n)
 {
     if (!b || !n) return fail(CNNCRF_EINVAL, "null argument");
@@ -363,11 +384,14 @@ int cnncrf_batch_autotune(cnncrf_batch_t b, float L1, float L2, float delta, int
     CNNCRF_TRY(cnncrf_batch_check(b));
     k::CrfParams p;
     p.L1 = L1, p.L2 = L2, p.delta = (int)delta, p.shape = b->o.crf_shape, p.slack = b->o.crf_slack;
+    k::UnaryQ16 uq{1.0f, 0.0f};
+    k::unary_q16(b->o.unary, &uq);
     for (auto &gp : b->groups) {
         Group &g = *gp;
         const long N = (long)g.W * g.H;
         CNNCRF_TRY(k::crf_autotune(g.vol.as<float>(), g.pw.as<float>(), g.pw.as<float>() + N, 2 * N, g.W, g.H,
-                                   g.depth, (int)g.members.size(), p, g.ws.get(), g.ws_bytes, b->work));
+                                   g.depth, (int)g.members.size(), p, g.ws.get(), g.ws_bytes, b->work, true,
+                                   g.net->volq_valid ? g.volq.get() : nullptr, uq));
     }
     b->invalidate(); // the captured launches carry the old tiles
     return CNNCRF_OK;
@@ -533,6 +557,9 @@ int cnncrf_batch_get_volume_device(cnncrf_batch_t b, int pair, const float **d_v
     size_t off;
     Group *g = group_of(b, pair, &off);
     if (!g || !d_vol) return fail(CNNCRF_EINVAL, "get_volume_device: bad pair");
+    if (!g->vol_written)
+        return fail(CNNCRF_ESTATE, "get_volume_device: the BF16 batch kept only the CRF's 16-bit copy of the "
+                                   "volume; call cnncrf_batch_keep_volume(b, 1) before the run");
     *d_vol = g->vol.as<float>() + off * g->depth;
     if (depth) *depth = g->depth;
     return CNNCRF_OK;

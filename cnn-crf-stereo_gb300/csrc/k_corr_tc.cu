@@ -71,9 +71,91 @@ struct CorrTcParams {
     int H, W, npairs, D, nkb, kk_last, tiles_x, num_tiles, unary, stages, nparts;
     int pk0[MAXPARTS], pD[MAXPARTS], pomin[MAXPARTS], pnch[MAXPARTS]; // per part: first k, count, band origin, chunks
     const float *list;
-    float *out;
+    float *out;        // the FP32 volume (null: not written)
+    uint16_t *outq;    // optional 16-bit fixed-point copy (the BF16 path's CRF unary), same layout
+    float qinv, qbias; // q = x / scale - offset / scale rounded to the nearest integer, saturated to 0..65535
     int *err;
 };
+
+// x * qinv is exact (qinv a power of two), so the FMA rounds once, like the
+// product plus qbias in FP32; the conversion rounds to nearest-even and saturates
+__device__ __forceinline__ uint16_t quantize_u16(float x, float qinv, float qbias)
+{
+    unsigned short q;
+    asm("cvt.rni.sat.u16.f32 %0, %1;" : "=h"(q) : "f"(__fmaf_rn(x, qinv, qbias)));
+    return q;
+}
+
+// The epilogue's per-pixel part for PP taps per lane (a part of Dp <= 32 PP
+// disparities): each pixel's band diagonal from the warp's staged rows, the
+// unary, and the stores: the FP32 volume (WF) and / or its 16-bit copy (WQ),
+// chosen at compile time so the per-element stores carry no branches.
+template <int PP, bool WF, bool WQ>
+__device__ __forceinline__ void store_pixels(const CorrTcParams &p, const float *sw, int lane, int npx, int Dp,
+                                             const int *off, float *obase, uint16_t *obaseq)
+{
+#pragma unroll 1
+    for (int i = 0; i < npx; ++i) {
+        const float *row = sw + i * SROW + i;
+        float cv[PP];
+#pragma unroll
+        for (int rr = 0; rr < PP; ++rr) cv[rr] = (lane + 32 * rr < Dp) ? row[off[rr]] : 0.0f;
+        float *o = WF ? obase + (size_t)i * p.D : nullptr;
+        uint16_t *oq = WQ ? obaseq + (size_t)i * p.D : nullptr;
+        if (p.unary == 0) {
+            float m = -FLT_MAX;
+#pragma unroll
+            for (int rr = 0; rr < PP; ++rr)
+                if (lane + 32 * rr < Dp) m = fmaxf(m, cv[rr]);
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
+            float sum = 0.0f;
+#pragma unroll
+            for (int rr = 0; rr < PP; ++rr) {
+                const float e = lane + 32 * rr < Dp ? cnncrf_expf(cv[rr] - m) : 0.0f;
+                cv[rr] = e;
+                sum = (rr == 0) ? e : sum + e;
+            }
+#pragma unroll
+            for (int s = 16; s >= 1; s >>= 1) sum = sum + __shfl_xor_sync(0xffffffffu, sum, s);
+#pragma unroll
+            for (int rr = 0; rr < PP; ++rr) {
+                const int kk = lane + 32 * rr;
+                if (kk < Dp) {
+                    const float u = -(cv[rr] / sum);
+                    if constexpr (WF) o[kk] = u;
+                    if constexpr (WQ) oq[kk] = quantize_u16(u, p.qinv, p.qbias);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int rr = 0; rr < PP; ++rr) {
+                const int kk = lane + 32 * rr;
+                if (kk < Dp) {
+                    const float u = p.unary == 1 ? 1.0f - cv[rr] : cv[rr];
+                    if constexpr (WF) o[kk] = u;
+                    if constexpr (WQ) oq[kk] = quantize_u16(u, p.qinv, p.qbias);
+                }
+            }
+        }
+    }
+}
+
+template <bool WF, bool WQ>
+__device__ __forceinline__ void store_part(const CorrTcParams &p, int P, const float *sw, int lane, int npx, int Dp,
+                                           const int *off, float *obase, uint16_t *obaseq)
+{
+    switch (P) {
+    case 1: store_pixels<1, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 2: store_pixels<2, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 3: store_pixels<3, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 4: store_pixels<4, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 5: store_pixels<5, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 6: store_pixels<6, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 7: store_pixels<7, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    default: store_pixels<8, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    }
+}
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     k_corr_tc(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR, const CorrTcParams p)
@@ -245,45 +327,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int pair = tt / tiles_per_pair, r = tt - pair * tiles_per_pair;
             const int y = r / p.tiles_x, xq = (r - y * p.tiles_x) * BM + q * 32;
             const int npx = min(32, p.W - xq);
-            float *obase = p.out + (((size_t)pair * p.H + y) * p.W + xq) * p.D + k0;
-#pragma unroll 1
-            for (int i = 0; i < npx; ++i) {
-                const float *row = sw + i * SROW + i;
-                float cv[MAXP];
-#pragma unroll
-                for (int rr = 0; rr < MAXP; ++rr) cv[rr] = (rr < P && lane + 32 * rr < Dp) ? row[off[rr]] : 0.0f;
-                float *o = obase + (size_t)i * p.D;
-                if (p.unary == 0) {
-                    float m = -FLT_MAX;
-#pragma unroll
-                    for (int rr = 0; rr < MAXP; ++rr)
-                        if (rr < P && lane + 32 * rr < Dp) m = fmaxf(m, cv[rr]);
-#pragma unroll
-                    for (int s = 16; s >= 1; s >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, s));
-                    float sum = 0.0f;
-#pragma unroll
-                    for (int rr = 0; rr < MAXP; ++rr) {
-                        if (rr < P) {
-                            const float e = lane + 32 * rr < Dp ? cnncrf_expf(cv[rr] - m) : 0.0f;
-                            cv[rr] = e;
-                            sum = (rr == 0) ? e : sum + e;
-                        }
-                    }
-#pragma unroll
-                    for (int s = 16; s >= 1; s >>= 1) sum = sum + __shfl_xor_sync(0xffffffffu, sum, s);
-#pragma unroll
-                    for (int rr = 0; rr < MAXP; ++rr) {
-                        const int kk = lane + 32 * rr;
-                        if (rr < P && kk < Dp) o[kk] = -(cv[rr] / sum);
-                    }
-                } else {
-#pragma unroll
-                    for (int rr = 0; rr < MAXP; ++rr) {
-                        const int kk = lane + 32 * rr;
-                        if (rr < P && kk < Dp) o[kk] = p.unary == 1 ? 1.0f - cv[rr] : cv[rr];
-                    }
-                }
-            }
+            const size_t obase_i = (((size_t)pair * p.H + y) * p.W + xq) * p.D + k0;
+            float *obase = p.out ? p.out + obase_i : nullptr;
+            uint16_t *obaseq = p.outq ? p.outq + obase_i : nullptr;
+            if (obaseq && obase) store_part<true, true>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
+            else if (obaseq) store_part<false, true>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
+            else store_part<true, false>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
             __syncwarp(); // the staging rows are rewritten by the next tile
         }
     }
@@ -337,6 +386,19 @@ bool corr_tc_plan(const float *h_list, int D, int unary, CorrTcPlan &pl)
 
 } // namespace
 
+bool unary_q16(int unary, UnaryQ16 *q)
+{
+    if (unary == 1) { // 1 - cosine in [0, 2] (a little outside where BF16 rounding lifts |cos| past 1)
+        q->scale = 1.0f / 32768.0f, q->offset = -1.0f / 256.0f;
+        return true;
+    }
+    if (unary == 0) { // -softmax in [-1, 0]
+        q->scale = 1.0f / 65536.0f, q->offset = -1.0f;
+        return true;
+    }
+    return false;
+}
+
 bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary)
 {
     CorrTcPlan pl;
@@ -344,13 +406,17 @@ bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary)
 }
 
 int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list,
-                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st)
+                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st, void *outq)
 {
     CorrTcPlan pl;
     if (!(cp % 64 == 0 && C >= 1 && C <= cp) || !corr_tc_plan(h_list, D, unary, pl))
         return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: C=%d cp=%d D=%d unary %d", C, cp, D, unary);
     if (npairs < 1 || H < 1 || W < 1) return fail(CNNCRF_EINVAL, "correlation_tc: bad size");
-    if (((uintptr_t)feat & 15) || !out || !err || !d_list) return fail(CNNCRF_EINVAL, "correlation_tc: bad pointer");
+    if (((uintptr_t)feat & 15) || (!out && !outq) || !err || !d_list)
+        return fail(CNNCRF_EINVAL, "correlation_tc: bad pointer");
+    UnaryQ16 uq{1.0f, 0.0f};
+    if (outq && !unary_q16(unary, &uq))
+        return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: no 16-bit copy of unary %d", unary);
     auto enc = tc::tensor_map_encoder();
     if (!enc) return fail(CNNCRF_ECUDA, "correlation_tc: cuTensorMapEncodeTiled unavailable");
     // features [2 * npairs][H][W][cp] BF16: left images first, then right images
@@ -379,7 +445,8 @@ int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, co
     p.tiles_x = ceil_div(W, BM);
     p.num_tiles = npairs * H * p.tiles_x * pl.nparts;
     p.unary = unary;
-    p.list = d_list, p.out = out, p.err = err;
+    p.list = d_list, p.out = out, p.outq = (uint16_t *)outq, p.err = err;
+    p.qinv = 1.0f / uq.scale, p.qbias = -uq.offset / uq.scale;
 
     int dev = 0, sms = 0, maxsm = 0;
     CNNCRF_CUDA(cudaGetDevice(&dev));

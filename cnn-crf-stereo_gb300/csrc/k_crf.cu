@@ -64,11 +64,11 @@ __global__ void k_wta(const float *__restrict__ cost, long npx, int D, int32_t *
     labels[i] = best;
 }
 
-__global__ void k_c1(const float *__restrict__ cost, const float *__restrict__ phi, long n,
-                     float *__restrict__ out)
+__global__ void k_c1(const float *__restrict__ cost, const uint16_t *__restrict__ costq, float qs, float qo,
+                     const float *__restrict__ phi, long n, float *__restrict__ out)
 {
     long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = __fsub_rn(cost[i], phi[i]);
+    if (i < n) out[i] = __fsub_rn(costq ? __fmaf_rn((float)costq[i], qs, qo) : cost[i], phi[i]);
 }
 
 struct Layout {
@@ -117,10 +117,12 @@ CrfTile effective_tile(int W, int H, int D, int np, int delta)
 }
 
 CrfPassArgs pass_args(const float *cost, long wps, int W, int H, int D, int np, const Rho &rp, char *ws,
-                      const Layout &l)
+                      const Layout &l, const void *costq, UnaryQ16 q)
 {
     CrfPassArgs a{};
     a.theta = cost;
+    a.thetaq = crf_reads_q16(D) ? (const uint16_t *)costq : nullptr;
+    a.qscale = q.scale, a.qoffset = q.offset;
     a.phi = (float *)(ws + l.phi);
     a.lbuf = (float *)(ws + l.lbuf);
     a.W = W, a.H = H, a.D = D, a.np = np, a.wps = wps;
@@ -132,14 +134,14 @@ CrfPassArgs pass_args(const float *cost, long wps, int W, int H, int D, int np, 
 // keep_phi = false: the last V pass does not write phi (nothing reads C1 from this workspace afterwards)
 int run_passes(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
                const Rho &rp, int delta, int iters, int32_t *labels, char *ws, const Layout &l, cudaStream_t st,
-               bool keep_phi = true)
+               bool keep_phi, const void *costq, UnaryQ16 q)
 {
     if (delta < 1 || delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
     const CrfTile t = effective_tile(W, H, D, np, delta);
     if (!fits(D, W, H, true, t.ring_h, t.wpb_h) || !fits(D, W, H, false, t.ring_v, t.wpb_v))
         return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
     double *cH = (double *)(ws + l.ch), *cV = (double *)(ws + l.cv), *lb = (double *)(ws + l.lb);
-    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, rp, ws, l);
+    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, rp, ws, l, costq, q);
     for (int it = 0; it < iters; ++it) {
         a.wgt = wx, a.first = it == 0, a.labels = nullptr, a.cmin = cH;
         CNNCRF_TRY(pass(a, true, delta, t.ring_h, t.wpb_h, st));
@@ -180,7 +182,7 @@ int check_args(const float *cost, const float *wx, const float *wy, int W, int H
 
 int solve_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
                const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st,
-               bool keep_phi = true)
+               bool keep_phi, const void *costq, UnaryQ16 q)
 {
     CNNCRF_TRY(check_args(cost, wx, wy, W, H, D, np, p, ws, ws_bytes));
     if (!labels) return fail(CNNCRF_EINVAL, "crf: null pointer");
@@ -195,7 +197,8 @@ int solve_impl(const float *cost, const float *wx, const float *wy, long wps, in
         CNNCRF_CHECK_LAUNCH();
         return CNNCRF_OK;
     }
-    return run_passes(cost, wx, wy, wps, W, H, D, np, make_rho(p), p.delta, iters, labels, w, l, st, keep_phi);
+    return run_passes(cost, wx, wy, wps, W, H, D, np, make_rho(p), p.delta, iters, labels, w, l, st, keep_phi,
+                      costq, q);
 }
 
 // time one H and one V pass of every candidate tile (events on `st`, best of
@@ -203,13 +206,13 @@ int solve_impl(const float *cost, const float *wx, const float *wy, long wps, in
 // afresh (its first H pass does not read them)
 int autotune_impl(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int np,
                   const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, CrfTile *best, float *ms_h,
-                  float *ms_v)
+                  float *ms_v, const void *costq, UnaryQ16 q)
 {
     CNNCRF_TRY(check_args(cost, wx, wy, W, H, D, np, p, ws, ws_bytes));
     if (p.delta < 1 || p.delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", p.delta);
     const Layout l = layout(W, H, D, np);
     char *w = (char *)ws;
-    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, make_rho(p), w, l);
+    CrfPassArgs a = pass_args(cost, wps, W, H, D, np, make_rho(p), w, l, costq, q);
     const int rings[2] = {8, 4}, wpbs[3] = {2, 1, 4}; // the default first: it wins ties
     const int reps = 3;
     struct Cand {
@@ -268,10 +271,17 @@ int autotune_impl(const float *cost, const float *wx, const float *wy, long wps,
 
 size_t crf_workspace_bytes(int W, int H, int D, int npairs) { return layout(W, H, D, npairs).total; }
 
-int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D, const CrfParams &p,
-              int iters, int32_t *labels, void *ws, size_t ws_bytes, double *h_lb, cudaStream_t st)
+bool crf_reads_q16(int D)
 {
-    CNNCRF_TRY(solve_impl(cost, wx, wy, 0, W, H, D, 1, p, iters, labels, ws, ws_bytes, st));
+    const int P = lane_labels(D);
+    return D == 32 * P && P % 2 == 0;
+}
+
+int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D, const CrfParams &p,
+              int iters, int32_t *labels, void *ws, size_t ws_bytes, double *h_lb, cudaStream_t st,
+              const void *costq, UnaryQ16 q)
+{
+    CNNCRF_TRY(solve_impl(cost, wx, wy, 0, W, H, D, 1, p, iters, labels, ws, ws_bytes, st, true, costq, q));
     if (h_lb) {
         Layout l = layout(W, H, D, 1);
         CNNCRF_CUDA(cudaMemcpyAsync(h_lb, (char *)ws + l.lb, sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -281,18 +291,21 @@ int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H,
 }
 
 int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs, const CrfParams &p,
-                    int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st, bool keep_phi)
+                    int iters, int32_t *labels, void *ws, size_t ws_bytes, cudaStream_t st, bool keep_phi,
+                    const void *costq, UnaryQ16 q)
 {
     const long N = (long)W * H;
-    return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st, keep_phi);
+    return solve_impl(cost, pw, pw + N, 2 * N, W, H, D, npairs, p, iters, labels, ws, ws_bytes, st, keep_phi,
+                      costq, q);
 }
 
 int crf_autotune(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int npairs,
-                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store)
+                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store, const void *costq,
+                 UnaryQ16 q)
 {
     CrfTile t;
     float mh = 0, mv = 0;
-    CNNCRF_TRY(autotune_impl(cost, wx, wy, wps, W, H, D, npairs, p, ws, ws_bytes, st, &t, &mh, &mv));
+    CNNCRF_TRY(autotune_impl(cost, wx, wy, wps, W, H, D, npairs, p, ws, ws_bytes, st, &t, &mh, &mv, costq, q));
     if (store) crf_tile_store(W, H, D, npairs, p.delta, t, mh, mv);
     return CNNCRF_OK;
 }
@@ -302,12 +315,14 @@ const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs)
     return (const double *)((const char *)ws + layout(W, H, D, npairs).lb);
 }
 
-int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st)
+int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st, int D, const void *costq,
+           UnaryQ16 q)
 {
     const float *phi = (const float *)ws;
+    const uint16_t *cq = (costq && crf_reads_q16(D)) ? (const uint16_t *)costq : nullptr;
     {
         CNNCRF_PROF("c1", st);
-        k_c1<<<ceil_div(n, 256), 256, 0, st>>>(cost, phi, n, out);
+        k_c1<<<ceil_div(n, 256), 256, 0, st>>>(cost, cq, q.scale, q.offset, phi, n, out);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;

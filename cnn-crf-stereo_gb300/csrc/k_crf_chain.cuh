@@ -25,6 +25,8 @@ struct Rho {
 // one pass over all chains of one direction (see k_crf_chain)
 struct CrfPassArgs {
     const float *theta; // the cost volume [np][H][W][D]
+    const uint16_t *thetaq; // its 16-bit fixed-point copy, read by the H pass instead of theta when set
+    float qscale, qoffset;  // theta = q * qscale + qoffset (exact in FP32)
     float *phi;         // H/V split of the unary, same layout
     const float *wgt;   // wx (H pass) or wy (V pass), pair stride wps
     float *lbuf;        // forward messages, same layout as phi
@@ -214,6 +216,39 @@ template <int P> __device__ __forceinline__ void lane_copy(float *dst, const flo
     }
 }
 
+// the same for a 16-bit unary vector: this lane's P values (2P bytes, P even:
+// 4-byte aligned at any lane) into the first half of its slot
+template <int P> __device__ __forceinline__ void lane_copy16(float *dst, const uint16_t *src, int lane)
+{
+    static_assert(P % 2 == 0, "16-bit theta copies need an even label count per lane");
+    const int k0 = lane * P;
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared((uint16_t *)dst + k0);
+    if constexpr (P % 8 == 0) {
+#pragma unroll
+        for (int i = 0; i < P / 8; ++i) cp_async16(d + 16 * i, src + k0 + 8 * i);
+    } else if constexpr (P % 4 == 0) {
+#pragma unroll
+        for (int i = 0; i < P / 4; ++i) cp_async8(d + 8 * i, src + k0 + 4 * i);
+    } else {
+#pragma unroll
+        for (int i = 0; i < P / 2; ++i) cp_async4(d + 4 * i, src + k0 + 2 * i, 4);
+    }
+}
+
+// dequantise: q * scale + offset is exact (q < 2^16, scale a power of two,
+// the sum a multiple of scale below 2^9 in magnitude)
+template <int P>
+__device__ __forceinline__ void lane_read16(const float *slot, int lane, float scale, float offset, float (&v)[P])
+{
+    const uint32_t *q = (const uint32_t *)((const uint16_t *)slot + lane * P);
+#pragma unroll
+    for (int i = 0; i < P / 2; ++i) {
+        const uint32_t w = q[i];
+        v[2 * i] = __fmaf_rn((float)(w & 0xffffu), scale, offset);
+        v[2 * i + 1] = __fmaf_rn((float)(w >> 16), scale, offset);
+    }
+}
+
 template <int P> __device__ __forceinline__ void lane_read(const float *slot, int lane, float (&v)[P])
 {
     const float *q = slot + lane * P; // 16-byte aligned for P % 4 == 0, 8-byte for P == 2
@@ -245,9 +280,10 @@ __host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass) { ret
 // Per step the pixel vectors come from a per-warp shared-memory ring filled
 // RING steps ahead with cp.async (each lane copies and reads only its own
 // labels), so the chain's dependent arithmetic does not wait on DRAM.
-template <int P, int DELTA, bool HPASS, bool FULL, int RING>
+template <int P, int DELTA, bool HPASS, bool FULL, int RING, bool T16 = false>
 __global__ void __launch_bounds__(128)
-    k_crf_chain(const float *__restrict__ theta, float *__restrict__ phi, const float *__restrict__ wgt,
+    k_crf_chain(const float *__restrict__ theta, const uint16_t *__restrict__ thetaq, float qscale, float qoffset,
+                float *__restrict__ phi, const float *__restrict__ wgt,
                 float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int store_phi, int nmax,
                 int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
 {
@@ -261,6 +297,7 @@ __global__ void __launch_bounds__(128)
     const int pair = gchain / nch, chain = gchain - pair * nch;
     const long pnd = (long)W * H * D * pair;
     theta += pnd;
+    if (T16) thetaq += pnd;
     phi += pnd;
     Lbuf += pnd;
     wgt += wps * pair;
@@ -279,7 +316,8 @@ __global__ void __launch_bounds__(128)
     // ---- forward: messages into each node, stored for the backward sweep
     auto issue_f = [&](int i) {
         if (i < n) {
-            if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
+            if constexpr (HPASS && T16) lane_copy16<P>(slot(i, 0), thetaq + pix(i) * D, lane);
+            else if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
             if (use_phi) lane_copy<P>(slot(i, 1), phi + pix(i) * D, lane, D);
         }
         cp_commit();
@@ -292,7 +330,8 @@ __global__ void __launch_bounds__(128)
     for (int i = 0; i < n; ++i) {
         issue_f(i + RING - 1);
         cp_wait<RING - 1>();
-        if (HPASS) lane_read<P>(slot(i, 0), lane, th);
+        if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset, th);
+        else if (HPASS) lane_read<P>(slot(i, 0), lane, th);
         if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
         store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
 #pragma unroll
@@ -313,7 +352,8 @@ __global__ void __launch_bounds__(128)
     auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j
         const int i = n - 1 - j;
         if (i >= 0) {
-            if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
+            if constexpr (HPASS && T16) lane_copy16<P>(slot(j, 0), thetaq + pix(i) * D, lane);
+            else if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
             if (use_phi) lane_copy<P>(slot(j, 1), phi + pix(i) * D, lane, D);
             lane_copy<P>(slot(j, 2), Lbuf + pix(i) * D, lane, D);
         }
@@ -327,7 +367,8 @@ __global__ void __launch_bounds__(128)
         const int i = n - 1 - j;
         issue_b(j + RING - 1);
         cp_wait<RING - 1>();
-        if (HPASS) lane_read<P>(slot(j, 0), lane, th);
+        if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset, th);
+        else if (HPASS) lane_read<P>(slot(j, 0), lane, th);
         if (use_phi) {
             lane_read<P>(slot(j, 1), lane, ph);
         } else {
@@ -377,11 +418,16 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
     const bool full = a.D == 32 * P;
     auto kern = hpass ? (full ? k_crf_chain<P, DELTA, true, true, RING> : k_crf_chain<P, DELTA, true, false, RING>)
                       : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
+    // the H pass on the 16-bit unary where each lane's labels are an even count (aligned copies)
+    const bool t16 = hpass && full && a.thetaq != nullptr && P % 2 == 0;
+    if constexpr (P % 2 == 0)
+        if (t16) kern = k_crf_chain<P, DELTA, true, true, RING, true>;
     CNNCRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long chains = (long)(hpass ? a.H : a.W) * a.np;
     {
         CNNCRF_PROF(hpass ? "crf_h" : "crf_v", st);
-        kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.phi, a.wgt, a.lbuf, a.W, a.H, a.D, a.rp,
+        kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.thetaq, a.qscale, a.qoffset, a.phi, a.wgt,
+                                                           a.lbuf, a.W, a.H, a.D, a.rp,
                                                            a.first, a.store_phi, nmax, a.labels, a.cmin, a.np,
                                                            a.wps);
     }

@@ -4,8 +4,8 @@
 // The reference runs every iteration as three full-image passes: a copy
 // u_ = u, ttvqf_primal_kernel (stereo/stereo.cu:701-729) and
 // thuberqf_dual_kernel (stereo/stereo.cu:773-796).  Here one launch runs K
-// iterations on a 64 x 32 pixel tile held on chip: each thread keeps eight
-// pixels' u, u0, the fit (a, b), the weights and p, q in registers, and the
+// iterations on a 64 x 32 pixel tile held on chip: each thread keeps four
+// pixels' u, the fit's per-pixel constants, the weights and p, q in registers, and the
 // values that neighbours read -- p.x - q.x, p.y - q.y (the primal's
 // divergence) and u_ (the dual's gradient) -- go through shared memory.  The
 // primal at (x, y) reads (x-1, y) and (x, y-1); the dual reads (x+1, y) and
@@ -18,9 +18,12 @@
 //
 // Tiles read the state (u, p, q) of the previous launch and write a second
 // copy (a workspace ping-pong), since a tile's halo belongs to other tiles.
-// The per-element arithmetic is the unfused kernels' (k_misc.cu), operation
-// for operation, so the results equal the CPU oracle bit for bit.  Compiled
-// with --fmad=false.
+// The per-element arithmetic is the reference kernels', operation for
+// operation -- the fused multiply-adds their default compilation contracts
+// are written out as __fmaf_rn, the rest is single IEEE operations -- and the
+// per-pixel constants of the primal update are the same operations hoisted
+// out of the iteration loop, so the results equal both the CPU oracle and the
+// reference's own kernels bit for bit.  Compiled with --fmad=false.
 #include "common.h"
 #include "kernels.h"
 
@@ -29,13 +32,13 @@ namespace k {
 
 namespace {
 
-constexpr int TX = 64, TY = 32, NT = 256, RPT = TX * TY / NT; // 8 rows per thread, 4 rows apart
+constexpr int TX = 64, TY = 32, NT = 512, RS = NT / TX, RPT = TY / RS; // 4 rows per thread, 8 rows apart
 constexpr int KMAX = 8;                                         // iterations per launch
 
 __device__ __forceinline__ float clampf(float v, float lo, float hi) { return fmaxf(lo, fminf(v, hi)); }
 __device__ __forceinline__ int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
-// prox_p with alpha = 0 (stereo/stereo.cu:752-757), as in k_misc.cu
+// prox_p with alpha = 0 (stereo/stereo.cu:752-757)
 __device__ __forceinline__ float prox_p0(float v, float beta, float sigma, float w)
 {
     if (fabsf(v) <= __fmul_rn(w, 0.0f)) return v;
@@ -70,23 +73,32 @@ __global__ void __launch_bounds__(NT, 2) k_tv_fused(const TvArgs a)
     const int cm = clampi((gx > 0 ? gx - 1 : 0) - ex, 0, TX - 1);
     const int cp = clampi((gx + 1 < W ? gx + 1 : W - 1) - ex, 0, TX - 1);
 
-    float u[RPT], uz[RPT], fa[RPT], fb[RPT], wxr[RPT], wyr[RPT], px[RPT], py[RPT], qx[RPT], qy[RPT], ub[RPT];
+    // per pixel: the state (u, u_, p, q) and the primal's per-pixel constants,
+    // computed once per launch with the operations the reference applies per
+    // iteration: inner = a - b u0, den = 1 + tau b, the box u0 -+ step / 2
+    float u[RPT], ub[RPT], px[RPT], py[RPT], qx[RPT], qy[RPT];
+    float inn[RPT], den[RPT], lo[RPT], hi[RPT], wxr[RPT], wyr[RPT];
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
-        const int r = r0 + 4 * j, gy = ey + r;
-        u[j] = uz[j] = fa[j] = fb[j] = wxr[j] = wyr[j] = px[j] = py[j] = qx[j] = qy[j] = ub[j] = 0.0f;
+        const int r = r0 + RS * j, gy = ey + r;
+        float uz = 0.0f, fa = 0.0f, fb = 0.0f;
+        u[j] = wxr[j] = wyr[j] = px[j] = py[j] = qx[j] = qy[j] = ub[j] = 0.0f;
         if (colin && gy >= 0 && gy < H) {
             const long i = (long)gy * W + gx;
             u[j] = a.u_in[i];
-            uz[j] = a.u0[i];
+            uz = a.u0[i];
             const float2 f = a.qf[i];
-            fa[j] = f.x, fb[j] = f.y;
+            fa = f.x, fb = f.y;
             wxr[j] = a.wx[i], wyr[j] = a.wy[i];
             if (a.p_in) {
                 const float2 pp = a.p_in[i], qq = a.q_in[i];
                 px[j] = pp.x, py[j] = pp.y, qx[j] = qq.x, qy[j] = qq.y;
             }
         }
+        inn[j] = __fmaf_rn(-fb, uz, fa);
+        den[j] = __fmaf_rn(a.tau, fb, 1.0f);
+        lo[j] = __fsub_rn(uz, a.half);
+        hi[j] = __fadd_rn(uz, a.half);
         sX[r][c] = __fsub_rn(px[j], qx[j]);
         sY[r][c] = __fsub_rn(py[j], qy[j]);
     }
@@ -96,34 +108,32 @@ __global__ void __launch_bounds__(NT, 2) k_tv_fused(const TvArgs a)
         // ---- primal (ttvqf_primal_kernel); u_ = u at the iteration's start
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            const int r = r0 + 4 * j, gy = ey + r;
+            const int r = r0 + RS * j, gy = ey + r;
             const int rm = clampi((gy > 0 ? gy - 1 : 0) - ey, 0, TY - 1);
             const float Px = __fsub_rn(px[j], qx[j]), Py = __fsub_rn(py[j], qy[j]);
             const float X = sX[r][cm], Y = sY[rm][c];
             const float div = __fsub_rn(__fadd_rn(__fsub_rn(Px, X), Py), Y);
             float un = __fmaf_rn(a.tau, div, u[j]);
-            const float inner = __fmaf_rn(-fb[j], uz[j], fa[j]);
-            const float num = __fmaf_rn(-a.tau, inner, un);
-            const float den = __fmaf_rn(a.tau, fb[j], 1.0f);
-            un = clampf(__fdiv_rn(num, den), __fsub_rn(uz[j], a.half), __fadd_rn(uz[j], a.half));
+            const float num = __fmaf_rn(-a.tau, inn[j], un);
+            un = clampf(__fdiv_rn(num, den[j]), lo[j], hi[j]);
             ub[j] = __fsub_rn(__fmul_rn(2.0f, un), u[j]);
             u[j] = un;
             sU[r][c] = ub[j];
         }
         __syncthreads();
         // ---- dual (thuberqf_dual_kernel), Huber parameter eps
-        const float den = __fmaf_rn(a.sigma, a.eps, 1.0f);
+        const float dd = __fmaf_rn(a.sigma, a.eps, 1.0f);
 #pragma unroll
         for (int j = 0; j < RPT; ++j) {
-            const int r = r0 + 4 * j, gy = ey + r;
+            const int r = r0 + RS * j, gy = ey + r;
             const int rp = clampi((gy + 1 < H ? gy + 1 : H - 1) - ey, 0, TY - 1);
             const float uc = ub[j];
             const float dx = __fsub_rn(sU[r][cp], uc);
             const float dy = __fsub_rn(sU[rp][c], uc);
             const float pnx = __fmaf_rn(a.sigma, dx, px[j]), pny = __fmaf_rn(a.sigma, dy, py[j]);
             const float qnx = __fmaf_rn(a.sigma, dx, qx[j]), qny = __fmaf_rn(a.sigma, dy, qy[j]);
-            px[j] = clampf(__fdiv_rn(pnx, den), -wxr[j], wxr[j]);
-            py[j] = clampf(__fdiv_rn(pny, den), -wyr[j], wyr[j]);
+            px[j] = clampf(__fdiv_rn(pnx, dd), -wxr[j], wxr[j]);
+            py[j] = clampf(__fdiv_rn(pny, dd), -wyr[j], wyr[j]);
             qx[j] = prox_p0(qnx, a.C, a.sigma, wxr[j]);
             qy[j] = prox_p0(qny, a.C, a.sigma, wyr[j]);
             // the primals of this iteration read sX / sY before the barrier above
@@ -137,7 +147,7 @@ __global__ void __launch_bounds__(NT, 2) k_tv_fused(const TvArgs a)
     if (!colin || c < K || c >= TX - K) return;
 #pragma unroll
     for (int j = 0; j < RPT; ++j) {
-        const int r = r0 + 4 * j, gy = ey + r;
+        const int r = r0 + RS * j, gy = ey + r;
         if (r < K || r >= TY - K || gy < 0 || gy >= H) continue;
         const long i = (long)gy * W + gx;
         a.u_out[i] = u[j];

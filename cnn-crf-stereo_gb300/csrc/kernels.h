@@ -94,10 +94,20 @@ int correlation_bf16(const void *fl, const void *fr, int H, int W, int C, int cs
 // images, then right), an integer disparity list (h_list on the host, d_list
 // its device copy) cut into at most 4 parts whose bands are <= 128 wide (one
 // part under the softmax unary); corr_tc_supported says whether a list
-// qualifies.  err: the bounded-wait error flag.
+// qualifies.  err: the bounded-wait error flag.  outq (optional): the
+// volume's 16-bit fixed-point copy (unary_q16), the BF16 path's CRF unary;
+// out may then be null (no FP32 volume written).
 bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary);
 int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, const float *d_list,
-                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st);
+                   const float *h_list, int D, int unary, float *out, int *err, cudaStream_t st,
+                   void *outq = nullptr);
+// The BF16 path's 16-bit fixed-point unary: x = q * scale + offset (q in
+// 0..65535), exact in FP32.  1 - <fL,fR> in [-2^-8, 2 - 2^-8] at 2^-15,
+// -softmax in [-1, 0] at 2^-16.  false for a unary with no fixed range.
+struct UnaryQ16 {
+    float scale, offset;
+};
+bool unary_q16(int unary, UnaryQ16 *q);
 
 // ------------------------------------------------------------ training step (k_train.cu)
 // npz layout w[co][ci][kh][kw] -> conv_simt's wt [K][128] (if wt), the input
@@ -199,16 +209,26 @@ size_t crf_workspace_bytes(int W, int H, int D, int npairs = 1);
 // npairs pairs at once: cost [n][H][W][D], weights [n][2][H][W] (wx, wy),
 // labels [n][H][W]; bounds stay in the workspace (crf_lb_device).  keep_phi =
 // false leaves the workspace's final phi unwritten (for callers that read the
-// labels and bounds only, never C1).
+// labels and bounds only, never C1).  costq (optional): the 16-bit
+// fixed-point copy of cost (unary_q16) that the H passes read instead -- the
+// BF16 path's unary; the solve is then the FP32 algorithm on the dequantised
+// unary -- where D / 32 is even (crf_reads_q16).  With costq no pass reads
+// cost (only the winner-take-all of iters <= 0 does).
 int crf_solve_batch(const float *cost, const float *pw, int W, int H, int D, int npairs,
                     const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
-                    cudaStream_t st, bool keep_phi = true);
+                    cudaStream_t st, bool keep_phi = true, const void *costq = nullptr,
+                    UnaryQ16 q = UnaryQ16{0.0f, 0.0f});
 const double *crf_lb_device(const void *ws, int W, int H, int D, int npairs);
 int crf_solve(const float *cost, const float *wx, const float *wy, int W, int H, int D,
               const CrfParams &p, int iters, int32_t *labels, void *ws, size_t ws_bytes,
-              double *h_lb, cudaStream_t st);
-// theta - phi of the last solve (get_C1)
-int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st);
+              double *h_lb, cudaStream_t st, const void *costq = nullptr, UnaryQ16 q = UnaryQ16{0.0f, 0.0f});
+// whether the H passes read a 16-bit cost copy at depth D (else they read the FP32 cost)
+bool crf_reads_q16(int D);
+// the slack_prop_2D_alg object of the C ABI reads costq instead of its cost when set
+void slackprop_set_costq(struct ::cnncrf_slackprop *sp, const void *costq, UnaryQ16 q);
+// theta - phi of the last solve (get_C1); costq: the 16-bit copy that solve read, if any
+int crf_c1(const float *cost, const void *ws, long n, float *out, cudaStream_t st, int D = 0,
+           const void *costq = nullptr, UnaryQ16 q = UnaryQ16{0.0f, 0.0f});
 
 // CRF tile: prefetch ring depth (4 or 8 chain steps) and chains (warps) per
 // CTA (1, 2 or 4) of the H and the V pass.  Every tile gives the same bits;
@@ -223,7 +243,8 @@ void crf_tile_store(int W, int H, int D, int npairs, int delta, const CrfTile &t
 // time every tile on this problem (one H and one V pass each, best of 3)
 // and, with store, enter the fastest per pass in the table; synchronises st
 int crf_autotune(const float *cost, const float *wx, const float *wy, long wps, int W, int H, int D, int npairs,
-                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store = true);
+                 const CrfParams &p, void *ws, size_t ws_bytes, cudaStream_t st, bool store = true,
+                 const void *costq = nullptr, UnaryQ16 q = UnaryQ16{0.0f, 0.0f});
 
 // ------------------------------------------------------------ small ops
 int remap(float *out, const int32_t *labels, long n, float dmin, float dstep, cudaStream_t st);

@@ -238,6 +238,7 @@ int cnncrf_net::predict(const float *left, const float *right)
     for (size_t i = 0; i < have.size(); ++i)
         if (!have[i]) return fail(CNNCRF_ESTATE, "parameter arr_%zu not set", i);
     if (!left || !right) return fail(CNNCRF_EINVAL, "predict: null image");
+    volq_valid = false;
     if (d.precision == CNNCRF_BF16) return predict_bf16(left, right);
     return predict_fp32(left, right);
 }

@@ -31,6 +31,13 @@ struct cnncrf_net {
     cnncrf::DevBuf vol_own;
     float *pwout = nullptr;
     cnncrf::DevBuf pw_own;
+    // BF16 path: an owner-supplied buffer for the volume's 16-bit fixed-point
+    // copy (the CRF's unary); volq_valid after a predict that wrote it (the
+    // tensor-core correlation writes it; its SIMT fallback does not).  With
+    // volq set and vol_fp32 false the FP32 volume is not written when the copy is.
+    void *volq = nullptr;
+    bool volq_valid = false;
+    bool vol_fp32 = true;
 
     // activations
     cnncrf::DevBuf norm[2], act[2][2], pwa, pwb, scratch;

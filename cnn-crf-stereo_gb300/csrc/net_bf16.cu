@@ -99,12 +99,17 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
     const size_t fimg = (size_t)H * W * cp;
     feat16 = f;
     const bool ip = interp || force_interp;
-    if (!ip && int_list && k::corr_tc_supported(F, cp, list.data(), D, d.unary))
-        CNNCRF_TRY(k::correlation_tc(f, n, H, W, F, cp, d_list.as<float>(), list.data(), D, d.unary, vol,
-                                     err.as<int>(), st));
-    else
+    volq_valid = false;
+    k::UnaryQ16 uq;
+    if (!ip && int_list && k::corr_tc_supported(F, cp, list.data(), D, d.unary)) {
+        void *q = (volq && k::unary_q16(d.unary, &uq)) ? volq : nullptr;
+        CNNCRF_TRY(k::correlation_tc(f, n, H, W, F, cp, d_list.as<float>(), list.data(), D, d.unary,
+                                     (q && !vol_fp32) ? nullptr : vol, err.as<int>(), st, q));
+        volq_valid = q != nullptr;
+    } else {
         CNNCRF_TRY(k::correlation_bf16(f, f + (size_t)n * fimg, H, W, F, cp, d_list.as<float>(), D, omin, omax, ip,
                                        d.unary, vol, st, n, (long)fimg));
+    }
     if (d.with_pairwise) {
         int cr = pad - 2;
         const float *in = norm[0].as<float>() + ((size_t)cr * w + cr) * ic;

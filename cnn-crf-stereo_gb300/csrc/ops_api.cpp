@@ -14,6 +14,8 @@ using namespace cnncrf;
 struct cnncrf_slackprop {
     cudaStream_t st = nullptr;
     const float *cost = nullptr;
+    const void *costq = nullptr; // a 16-bit fixed-point copy of cost the solve reads instead (BF16 Stereo path)
+    k::UnaryQ16 q{1.0f, 0.0f};
     int W = 0, H = 0, D = 0;
     int32_t *labels = nullptr;
     const float *wx = nullptr, *wy = nullptr;
@@ -36,6 +38,13 @@ int cnncrf::k::crf_params(const cnncrf_crf_options *opt, k::CrfParams *p)
     p->shape = opt->shape;
     p->slack = opt->slack;
     return CNNCRF_OK;
+}
+
+// The BF16 Stereo path hands the solver the 16-bit copy of its volume that the
+// correlation wrote (null: the FP32 volume); not part of the C ABI.
+void cnncrf::k::slackprop_set_costq(cnncrf_slackprop *sp, const void *costq, UnaryQ16 q)
+{
+    if (sp) sp->costq = costq, sp->q = q;
 }
 
 extern "C" {
@@ -193,7 +202,7 @@ int cnncrf_slackprop_execute(cnncrf_slackprop_t sp)
     k::CrfParams p;
     CNNCRF_TRY(k::crf_params(&sp->ops, &p));
     CNNCRF_TRY(k::crf_solve(sp->cost, sp->wx, sp->wy, sp->W, sp->H, sp->D, p, sp->ops.total_it, sp->labels,
-                            sp->ws.get(), sp->ws.size(), &sp->lb, sp->st));
+                            sp->ws.get(), sp->ws.size(), &sp->lb, sp->st, sp->costq, sp->q));
     sp->ran = true;
     return CNNCRF_OK;
 }
@@ -212,7 +221,7 @@ int cnncrf_slackprop_get_c1(cnncrf_slackprop_t sp, float **d_c1)
     if (!sp->ran || sp->ops.total_it <= 0) return fail(CNNCRF_ESTATE, "slackprop: get_C1 before execute");
     long n = (long)sp->W * sp->H * sp->D;
     CNNCRF_TRY(sp->c1.reserve(sizeof(float) * n));
-    CNNCRF_TRY(k::crf_c1(sp->cost, sp->ws.get(), n, sp->c1.as<float>(), sp->st));
+    CNNCRF_TRY(k::crf_c1(sp->cost, sp->ws.get(), n, sp->c1.as<float>(), sp->st, sp->D, sp->costq, sp->q));
     *d_c1 = sp->c1.as<float>();
     return CNNCRF_OK;
 }

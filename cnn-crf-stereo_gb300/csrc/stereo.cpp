@@ -29,6 +29,8 @@ struct cnncrf_stereo {
     uint64_t seed = 0;
     int with_xy = 0;
     DevBuf img[2], padded[2], warped, warped_pad, vol, pw, out, labels, out_, out0, qf, p, q, vol3, tvws;
+    DevBuf volq;          // BF16 path: the 16-bit fixed-point copy of vol the CRF reads
+    bool volq_ok = false; // volq holds the volume of the last compute_volume
     DevBuf gray[2], gtmp, gtmp2, gw, dlist; // census and edge weights
     std::vector<float> dlist_host;          // host copy of the census disparity list
     int filter_size = 7;                    // stereo/stereo_img.cpp:73
@@ -133,6 +135,7 @@ int cnncrf_stereo::compute_weights(float alpha, float beta, float lambda, int lr
 int cnncrf_stereo::compute_volume(int lr)
 {
     if (!inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
+    volq_ok = false;
     if (matching == CNNCRF_MATCH_LOAD) return CNNCRF_OK;
     if (matching == CNNCRF_MATCH_CENSUS) return census(lr);
     if (!net) {
@@ -151,7 +154,19 @@ int cnncrf_stereo::compute_volume(int lr)
     int a = lr ? 0 : 1;
     CNNCRF_TRY(k::pad_rgba(img[a].as<float>(), W, H, net->pad, padded[0].as<float>(), st));
     CNNCRF_TRY(k::pad_rgba(img[1 - a].as<float>(), W, H, net->pad, padded[1].as<float>(), st));
-    return net->predict(padded[0].as<float>(), padded[1].as<float>());
+    // the BF16 path writes a 16-bit copy of the volume beside it for the CRF
+    // (getVolume keeps the FP32 one); the refinement's 3-label predictions
+    // (into vol3) do not
+    k::UnaryQ16 uq;
+    if (o.precision == CNNCRF_BF16 && k::crf_reads_q16(depth) && k::unary_q16(o.unary, &uq)) {
+        CNNCRF_TRY(volq.reserve(2 * (size_t)W * H * depth));
+        net->volq = volq.get();
+        net->vol_fp32 = true;
+    }
+    const int rc = net->predict(padded[0].as<float>(), padded[1].as<float>());
+    volq_ok = rc == CNNCRF_OK && net->volq_valid;
+    net->volq = nullptr;
+    return rc;
 }
 
 extern "C" {
@@ -341,6 +356,9 @@ int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C
         CNNCRF_TRY(cnncrf_slackprop_init(s->solver, s->vol.as<float>(), s->W, s->H, s->depth, s->labels.as<int32_t>()));
     }
     cnncrf_slackprop_set_stream(s->solver, (cnncrf_stream_t)s->st);
+    k::UnaryQ16 uq{1.0f, 0.0f};
+    k::unary_q16(s->o.unary, &uq);
+    k::slackprop_set_costq(s->solver, s->volq_ok ? s->volq.get() : nullptr, uq);
     CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "L1", C1));
     CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "L2", C2));
     CNNCRF_TRY(cnncrf_slackprop_set_op(s->solver, "delta", delta));

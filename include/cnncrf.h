@@ -547,7 +547,13 @@ int cnncrf_batch_run_host(cnncrf_batch_t b, const float *const *h_left, const fl
 int cnncrf_batch_get_output(cnncrf_batch_t b, int pair, float *h_out);
 int cnncrf_batch_get_output_device(cnncrf_batch_t b, int pair, const float **d_out);
 int cnncrf_batch_get_labels_device(cnncrf_batch_t b, int pair, const int32_t **d_labels);
+/* The pair's FP32 cost volume.  In BF16 the batch's correlation writes, by
+ * default, only the 16-bit fixed-point copy its CRF reads (x = q * 2^-15 - 2^-8
+ * for the 1 - <fL,fR> unary, q * 2^-16 - 1 for -softmax, where D / 32 is even);
+ * the FP32 volume is then not written and this returns CNNCRF_ESTATE unless
+ * cnncrf_batch_keep_volume(b, 1) was set before the run. */
 int cnncrf_batch_get_volume_device(cnncrf_batch_t b, int pair, const float **d_volume, int *depth);
+int cnncrf_batch_keep_volume(cnncrf_batch_t b, int enable);
 int cnncrf_batch_lower_bound(cnncrf_batch_t b, int pair, double *lb);
 /* Synchronise and report a kernel that gave up on a bounded wait (ETIMEOUT). */
 int cnncrf_batch_check(cnncrf_batch_t b);

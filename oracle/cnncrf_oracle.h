@@ -10,9 +10,54 @@
  * and TV refinement follow the reference sources line by line (citations in
  * cnncrf_oracle.cpp) and are pinned against independent library
  * implementations of the same operators (tests/golden/make_golden.py).  The
+ * correlation, padding, grey conversion, census, argmin, remap, warp,
+ * quadratic fit, TV primal-dual iterations, left-right check and QuadDirect
+ * are also pinned bit for bit against the reference's own CUDA kernels run on
+ * a GPU (tests/golden/ref_kernels.npz, written by make_ref_golden.py).  The
  * CRF solver is an absent third-party dependency (SlackProp, un-vendored
  * submodule, no pinned version): its restatement here follows our own written
  * spec and is PARITY UNPINNED against the reference.
+ *
+ * The CRF spec and where it comes from.  SlackProp is the solver of
+ * A. Shekhovtsov, C. Reinbacher, G. Graber, T. Pock, "Solving Dense Image
+ * Matching in Real-Time using Discrete-Continuous Optimization", Computer
+ * Vision Winter Workshop 2016 (arXiv:1601.06274).  Taken from that published
+ * method (the paper is not in this tree, so no section is quoted):
+ *  - the energy: unaries plus pairwise terms on the 4-connected grid;
+ *  - the dual decomposition of the grid into horizontal and vertical chain
+ *    subproblems that share the unary through a dual variable phi (the
+ *    horizontal chains see theta - phi, the vertical ones phi), every chain
+ *    solved exactly by min-sum dynamic programming;
+ *  - the update: a chain's min-marginals are formed and a fraction of their
+ *    excess over the chain's minimum -- the "slack" -- is handed to the other
+ *    subproblem, which leaves the chain's minimum unchanged, so the sum of
+ *    the chain minima is a lower bound of the energy that never decreases.
+ * Our own choices where the published description leaves freedom, or that
+ * the reference's call sites (stereo/stereo.cpp:140-154) do not pin:
+ *  - the slack fraction handed over per node: 0.5 (option `slack`);
+ *  - the schedule: one iteration = a horizontal pass then a vertical pass;
+ *    a pass runs the forward messages of every chain, then a backward sweep
+ *    that hands over the slack node by node and propagates the reduced unary
+ *    backwards, so each node's min-marginal already includes the hand-over
+ *    of the nodes after it;
+ *  - the bound: the FP64 sum of the last vertical pass's chain minima and of
+ *    the horizontal pass before it (the horizontal minima are preserved by
+ *    its hand-over, so both are the dual objective at the same phi);
+ *  - the labels: the first argmin of the last vertical pass's min-marginals;
+ *  - the pairwise term w_ij rho(|x_i - x_j|): the options L1, L2, delta keep
+ *    the reference's names.  STEP (the reference configs' shape): rho(0) = 0,
+ *    rho(1..delta) = L1, rho(> delta) = L2 -- the shipped configs
+ *    (data/parameters/kitti-2015/7-layer/cnn+crf+full/*.cfg: L1 = 1.002,
+ *    L2 = 14.98, delta = 2) then charge L1 for jumps of one or two labels
+ *    and L2 for larger ones.  Whether the library reads delta as "<= delta"
+ *    or "< delta" is not visible from the reference; "<=" is our reading.
+ *    LINEAR: rho(t) = min(L1 t, L2) for t <= delta, L2 beyond (the truncated
+ *    linear model of the task's synthetic workloads).
+ * Properties the tests check: the chain DP equals brute force; energy >=
+ * bound; the bound never decreases; w = 0 gives the winner-take-all labels;
+ * ties break to the first minimum; on a problem that is a single chain the
+ * bound reaches the minimum energy and the labels are the exact minimiser
+ * (the decomposition is exact on trees).
  *
  * The float instantiation uses exactly the operation order of the GPU FP32
  * path (explicit fmaf, the shared exp/tanh of include/cnncrf_fmath.h), so the

@@ -126,6 +126,30 @@ def test_chain_equals_bruteforce(oracle):
         assert lb <= e_bf + 1e-5
 
 
+def test_crf_exact_on_single_chains(oracle):
+    """The decomposition is exact on a tree: on an image that is one row or
+    one column the dual bound reaches the minimum energy and the labels are
+    the exact minimiser.  A row is one horizontal chain, optimal from the
+    first pass; a column is one vertical chain whose unary the horizontal
+    single-node subproblems hand over a slack fraction at a time, so its bound
+    converges geometrically (30 iterations)."""
+    rng = np.random.default_rng(41)
+    for trial in range(30):
+        n, D = int(rng.integers(2, 7)), int(rng.integers(2, 5))
+        shape, delta = int(rng.integers(0, 2)), int(rng.integers(1, 4))
+        c = (rng.random((n, D)) * 3).astype(np.float32)
+        w = (rng.random(n) * 2).astype(np.float32)
+        e_bf, lab_bf = oracle.chain_bruteforce(c, w, 0.7, 2.5, delta, shape)
+        for orient in ("row", "column"):
+            if orient == "row":
+                cost, wx, wy = c[None], w[None], np.zeros((1, n), np.float32)
+            else:
+                cost, wx, wy = c[:, None, :], np.zeros((n, 1), np.float32), w[:, None]
+            lab, lb, lbi, _ = oracle.crf(cost, wx, wy, 0.7, 2.5, delta, 30, shape=shape)
+            assert abs(lb - e_bf) <= 1e-4 * max(1.0, abs(e_bf)), (trial, orient, lb, e_bf)
+            assert np.array_equal(lab.reshape(-1), lab_bf), (trial, orient)
+
+
 def test_crf_bound_monotone_and_below_energy(oracle):
     rng = np.random.default_rng(5)
     for shape in (0, 1):
