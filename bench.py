@@ -82,6 +82,15 @@ def conv_flops(W, H, layers=7, feat=100, ic=3, pw=64, k=3):
     return tc, simt
 
 
+def conv_forms_summary():
+    """The tuned launch forms of the tensor-core convolutions (after autotune):
+    per layer shape, 2-CTA pairs or single CTAs, the stages and the best launch time."""
+    from cnncrf import tuning
+    return [{"layer": "%d img %dx%d %d->%d k%dx%d mode %d" % (f["n_img"], f["Win"], f["Hin"], f["cin"], f["cout"],
+                                                            f["kh"], f["kw"], f["mode"]),
+             "pair": f["pair"], "stages": f["stages"], "ms": round(f["ms"], 4)} for f in tuning.conv_forms()]
+
+
 def crf_bytes_per_pass(W, H, D):
     """Algorithmic bytes of one chain pass as counted for the roofline: three
     N*D float arrays (the subproblem's unary inputs read once, phi written)."""
@@ -729,6 +738,7 @@ def uneven_line(args, steps, rank=0, world=1, local=0):
         "roofline": crf_roof, "conv_roofline": roof, "kernels": kernels, "per_shape": per_shape, "clocks": clk,
         "crf_tiles": [dict(shape="%dx%d_d%d x%d" % (t["W"], t["H"], t["D"], t["npairs"]), **t["tile"])
                       for t in tiles],
+        "conv_forms": conv_forms_summary(),
         "cpu_baseline": None,
         "disparity_stats": {"kitti_bad3px_5pct_mean": bad,
                             "definition": "eval/compute_numbers_kitti.py computeError on PNG16-quantised maps, "
@@ -997,6 +1007,7 @@ def kitti_line(args, rank, world, local):
         "roofline": crf_roof, "conv_roofline": roof,
         "crf_tiles": [dict(shape="%dx%d_d%d x%d" % (t["W"], t["H"], t["D"], t["npairs"]), **t["tile"])
                       for t in tiles],
+        "conv_forms": conv_forms_summary(),
         "kernels": kernels, "kernel_profile_ms_per_step": p_ms / nprof, "clocks": clk,
         "cpu_baseline": cpu,
         "precision_check": cmp,

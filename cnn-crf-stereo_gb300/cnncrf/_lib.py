@@ -94,6 +94,9 @@ PROTOS = {
     "cnncrf_crf_tuning_get": ([i32, i32, i32, i32, i32, C.POINTER(CrfTile), C.POINTER(i32), C.POINTER(f32),
                                C.POINTER(f32)], i32),
     "cnncrf_crf_tuning_clear": ([], i32),
+    "cnncrf_conv_tuning_count": ([C.POINTER(i32)], i32),
+    "cnncrf_conv_tuning_get": ([i32, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), C.POINTER(f32)], i32),
+    "cnncrf_conv_tuning_clear": ([], i32),
     "cnncrf_crf_tuning_count": ([C.POINTER(i32)], i32),
     "cnncrf_crf_tuning_save": ([C.c_char_p], i32),
     "cnncrf_crf_tuning_load": ([C.c_char_p], i32),

@@ -43,3 +43,26 @@ def save(path):
 
 def load(path):
     call("cnncrf_crf_tuning_load", str(path).encode())
+
+
+CONV_KEY = ("n_img", "Hin", "Win", "cp_in", "cin", "np", "cout", "kh", "kw", "mode")
+
+
+def conv_forms():
+    """The tensor-core convolutions' tuned launch forms (cnncrf_conv_tuning_*):
+    one dict per layer shape, with pair (1: 2-CTA pairs, 0: single CTAs),
+    stages and the measured ms of one launch."""
+    n = C.c_int()
+    call("cnncrf_conv_tuning_count", C.byref(n))
+    out = []
+    for i in range(n.value):
+        shape, pair, stages, ms = (C.c_int * 10)(), C.c_int(), C.c_int(), C.c_float()
+        call("cnncrf_conv_tuning_get", i, shape, C.byref(pair), C.byref(stages), C.byref(ms))
+        d = dict(zip(CONV_KEY, shape[:]))
+        d.update(pair=pair.value, stages=stages.value, ms=ms.value)
+        out.append(d)
+    return out
+
+
+def clear_conv():
+    call("cnncrf_conv_tuning_clear")

@@ -393,7 +393,9 @@ int cnncrf_batch_autotune(cnncrf_batch_t b, float L1, float L2, float delta, int
                                    g.depth, (int)g.members.size(), p, g.ws.get(), g.ws_bytes, b->work, true,
                                    g.net->volq_valid ? g.volq.get() : nullptr, uq));
     }
-    b->invalidate(); // the captured launches carry the old tiles
+    // the tensor-core convolutions' launch forms, per layer shape of every group's net
+    for (auto &gp : b->groups) CNNCRF_TRY(gp->net->autotune_conv());
+    b->invalidate(); // the captured launches carry the old tiles and forms
     return CNNCRF_OK;
 }
 

@@ -44,9 +44,13 @@
 // overlaps the MMAs of tile i+1.  Every mbarrier wait is bounded: on timeout
 // the role raises the CTA abort flag and the global error flag, in-flight
 // copies and MMAs are drained (again bounded) and TMEM is freed before exit.
+#include <algorithm>
+#include <array>
 #include <atomic>
+#include <iterator>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -692,6 +696,28 @@ inline size_t smem_bytes(int NP, int NB, int stages, int a_bytes, int kw, int mo
 
 std::atomic<int> g_pairs{1}; // CTA pairs (cta_group::2) where the device can co-schedule them
 
+// the conv tuning table: layer shape -> fastest form (conv_tc_autotune)
+struct ConvTuned {
+    ConvForm form;
+    float ms;
+};
+std::mutex g_tune_mu;
+std::map<std::array<int, CONV_KEY>, ConvTuned> g_tune;
+
+std::array<int, CONV_KEY> conv_key(const TcConvArgs &a)
+{
+    return {a.n_img, a.Hin, a.Win, a.cp_in, a.cin, a.np, a.cout, a.kh, a.kw, a.mode};
+}
+
+bool conv_form_lookup(const TcConvArgs &a, ConvForm *f)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(conv_key(a));
+    if (it == g_tune.end()) return false;
+    *f = it->second.form;
+    return true;
+}
+
 // Co-resident 2-CTA clusters of k_conv_tc<NP, true> at `smem` bytes per CTA (0: none), cached per size.
 template <int NP> int pair_clusters(size_t smem)
 {
@@ -747,18 +773,22 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
     const bool m4 = a.mode == 4;
     const int ocs = m4 ? a.o16_cs : a.cp_out, opw = m4 ? a.o16_pw : 0, oph = m4 ? a.o16_ph : 0;
     const bool ost_ok = (a.mode == 0 || a.mode == 1 || m4) && ocs % 8 == 0 && ocs >= 64 * ((NP + 63) / 64);
+    // the form: the caller's, else the tuned one for this shape, else the defaults
+    ConvForm form = a.form;
+    if (form.pair < 0 && form.stages == 0) conv_form_lookup(a, &form);
+    const int smax = form.stages >= 2 ? std::min(form.stages, MAX_STAGES) : MAX_STAGES;
     auto plan = [&](int nb, int &ysm, int &ost, int &stages) -> size_t {
         ysm = m4 && smem_bytes(NP, nb, 2, p.a_bytes, a.kw, a.mode, ybytes) <= (size_t)maxsm ? 1 : 0;
         const int yb = ysm ? ybytes : 0;
         ost = ost_ok && smem_bytes(NP, nb, 2, p.a_bytes, a.kw, a.mode, yb + 8 * OBUF) <= (size_t)maxsm ? 1 : 0;
         const int extra = yb + (ost ? 8 * OBUF : 0);
         stages = 0;
-        for (int s = MAX_STAGES; s >= 2 && !stages; --s)
+        for (int s = smax; s >= 2 && !stages; --s)
             if (smem_bytes(NP, nb, s, p.a_bytes, a.kw, a.mode, extra) <= (size_t)maxsm) stages = s;
         return smem_bytes(NP, nb, std::max(stages, 2), p.a_bytes, a.kw, a.mode, extra);
     };
     // CTA pairs when there are two tiles to pair and the device co-schedules the clusters
-    bool pair = g_pairs.load() != 0 && p.num_tiles >= 2;
+    bool pair = (form.pair < 0 ? g_pairs.load() != 0 : form.pair != 0) && p.num_tiles >= 2;
     int nclusters = 0;
     if (pair) {
         int ysm, ost, stages;
@@ -831,6 +861,72 @@ template <int NP> int launch(const TcConvArgs &a, TcParams &p, cudaStream_t st)
 
 void conv_tc_set_pairs(bool on) { g_pairs.store(on ? 1 : 0); }
 bool conv_tc_pairs() { return g_pairs.load() != 0; }
+
+int conv_forms_count()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    return (int)g_tune.size();
+}
+
+bool conv_form_entry(int i, int key[CONV_KEY], ConvForm *f, float *ms)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    if (i < 0 || i >= (int)g_tune.size()) return false;
+    auto it = g_tune.begin();
+    std::advance(it, i);
+    for (int j = 0; j < CONV_KEY; ++j) key[j] = it->first[j];
+    *f = it->second.form;
+    *ms = it->second.ms;
+    return true;
+}
+
+void conv_forms_clear()
+{
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+}
+
+int conv_tc_autotune(const TcConvArgs &a, cudaStream_t st)
+{
+    if (a.mode < 0 || a.mode > 2) return fail(CNNCRF_EINVAL, "conv_tc_autotune: inference modes 0-2 only");
+    // the default form first: it wins ties
+    std::vector<ConvForm> cands;
+    const int first_pair = g_pairs.load() != 0 ? 1 : 0;
+    for (int pr : {first_pair, 1 - first_pair})
+        for (int s = MAX_STAGES; s >= 2; --s) cands.push_back(ConvForm{pr, s});
+    const int reps = 3;
+    std::vector<cudaEvent_t> ev(cands.size() * reps * 2, nullptr);
+    int rc = CNNCRF_OK;
+    for (auto &e : ev)
+        if (rc == CNNCRF_OK && cudaEventCreate(&e) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "conv tune: event");
+    TcConvArgs b = a;
+    for (int r = 0; r < reps && rc == CNNCRF_OK; ++r)
+        for (size_t c = 0; c < cands.size() && rc == CNNCRF_OK; ++c) {
+            b.form = cands[c];
+            cudaEvent_t *e = &ev[(c * reps + r) * 2];
+            if (cudaEventRecord(e[0], st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "conv tune: record");
+            if (rc == CNNCRF_OK) rc = conv_tc(b, st);
+            if (rc == CNNCRF_OK && cudaEventRecord(e[1], st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "conv tune: record");
+        }
+    if (rc == CNNCRF_OK && cudaStreamSynchronize(st) != cudaSuccess) rc = fail(CNNCRF_ECUDA, "conv tune: sync");
+    ConvForm best = cands[0];
+    float bms = 1e30f;
+    for (size_t c = 0; c < cands.size() && rc == CNNCRF_OK; ++c) {
+        float m = 1e30f;
+        for (int r = 0; r < reps; ++r) {
+            float x = 0;
+            cudaEventElapsedTime(&x, ev[(c * reps + r) * 2], ev[(c * reps + r) * 2 + 1]);
+            m = std::min(m, x);
+        }
+        if (m < bms) bms = m, best = cands[c];
+    }
+    for (auto &e : ev)
+        if (e) cudaEventDestroy(e);
+    if (rc != CNNCRF_OK) return rc;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[conv_key(a)] = ConvTuned{best, bms};
+    return CNNCRF_OK;
+}
 
 int conv_tc(const TcConvArgs &a, cudaStream_t st)
 {

@@ -48,6 +48,13 @@ int conv_head2(const float *in, int npx, int Cin, const float *w /*[2][Cin]*/, f
 int l2norm(float *f, long npx, int C, cudaStream_t st);
 
 // ------------------------------------------------------------ BF16 tensor-core conv
+// A tensor-core convolution's launch form: 2-CTA pairs (cta_group::2) or
+// single CTAs, and the pipeline stages (0: as many as fit in shared memory).
+// Every form gives the same bits; only the speed differs.
+struct ConvForm {
+    int pair = -1; // -1: the process-wide switch (conv_tc_set_pairs)
+    int stages = 0;
+};
 struct TcConvArgs {
     const void *in; // BF16 NHWC [n_img][Hin][Win][cp_in], channels >= cin zero
     int n_img, Hin, Win, cp_in, cin;
@@ -72,11 +79,23 @@ struct TcConvArgs {
     // of cout floats per (CTA, epilogue warp), *bias_splits = their number (at most 8 x SMs)
     float *bias_part = nullptr;
     int *bias_splits = nullptr;
+    ConvForm form; // unset: the tuning table's form for this shape, else the defaults
 };
+// a.form unset (pair -1, stages 0): the form of the process-wide tuning
+// table for this layer shape if it has one, else the switch and the most stages
 int conv_tc(const TcConvArgs &a, cudaStream_t st);
 // 2-CTA pairs (cta_group::2) for conv_tc where the device co-schedules them (default on)
 void conv_tc_set_pairs(bool on);
 bool conv_tc_pairs();
+// Time every form of this launch (pair or single CTAs x 2..4 stages, best of
+// 3, CUDA events on st; synchronises) and enter the fastest in the table.
+// Inference modes 0-2 only: the launch's outputs are rewritten, with the same bits.
+int conv_tc_autotune(const TcConvArgs &a, cudaStream_t st);
+// the conv tuning table: key = n_img, Hin, Win, cp_in, cin, np, cout, kh, kw, mode
+constexpr int CONV_KEY = 10;
+int conv_forms_count();
+bool conv_form_entry(int i, int key[CONV_KEY], ConvForm *f, float *ms);
+void conv_forms_clear();
 
 // ------------------------------------------------------------ correlation
 // raw correlation (+ unary: -1 none, 0 -softmax, 1 one-minus) of NHWC FP32

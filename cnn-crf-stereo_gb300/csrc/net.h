@@ -4,6 +4,7 @@
 #include <vector>
 
 #include "common.h"
+#include "kernels.h"
 
 struct cnncrf_net {
     struct Layer {
@@ -51,6 +52,11 @@ struct cnncrf_net {
     const void *feat16 = nullptr; // [2][H][W][cp_feat] after predict
     int alloc_bf16();
     int check_error();
+    // the tensor-core convolutions of the last BF16 predict, for autotune_conv
+    std::vector<cnncrf::k::TcConvArgs> tc_calls;
+    // time every launch form of those convolutions and enter the fastest in
+    // the process-wide conv tuning table (synchronises; rewrites the outputs)
+    int autotune_conv();
 
     int num_params() const { return (int)host.size(); }
     int expected_shape(int i, int64_t s[4], int *nd) const;

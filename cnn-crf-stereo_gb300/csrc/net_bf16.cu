@@ -60,6 +60,7 @@ int cnncrf_net::check_error()
 
 int cnncrf_net::predict_bf16(const float *left, const float *right)
 {
+    tc_calls.clear();
     if (d.num_layers < 2) return fail(CNNCRF_EUNSUPPORTED, "BF16 path needs >= 2 feature layers");
     const float *img[2] = {left, right};
     const int ic = d.in_channels, F = d.feat_channels, cp = cp_feat;
@@ -91,6 +92,7 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
         t.cp_out = cp;
         t.err = err.as<int>();
         CNNCRF_TRY(k::conv_tc(t, st));
+        tc_calls.push_back(t);
         hin -= L.kh - 1, win -= L.kw - 1;
         cur ^= 1;
     }
@@ -132,6 +134,14 @@ int cnncrf_net::predict_bf16(const float *left, const float *right)
         t.cp_out = 0;
         t.err = err.as<int>();
         CNNCRF_TRY(k::conv_tc(t, st));
+        tc_calls.push_back(t);
     }
     return CNNCRF_OK;
+}
+
+int cnncrf_net::autotune_conv()
+{
+    if (d.precision != CNNCRF_BF16) return CNNCRF_OK;
+    for (const auto &t : tc_calls) CNNCRF_TRY(cnncrf::k::conv_tc_autotune(t, st));
+    return check_error();
 }

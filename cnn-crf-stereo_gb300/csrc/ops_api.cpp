@@ -115,6 +115,28 @@ int cnncrf_crf_workspace_size(int width, int height, int depth, size_t *bytes)
 }
 
 
+int cnncrf_conv_tuning_count(int *n)
+{
+    if (!n) return fail(CNNCRF_EINVAL, "null argument");
+    *n = k::conv_forms_count();
+    return CNNCRF_OK;
+}
+
+int cnncrf_conv_tuning_get(int index, int shape[10], int *pair, int *stages, float *ms)
+{
+    if (!shape || !pair || !stages || !ms) return fail(CNNCRF_EINVAL, "null argument");
+    k::ConvForm f;
+    if (!k::conv_form_entry(index, shape, &f, ms)) return fail(CNNCRF_EINVAL, "conv tuning: no entry %d", index);
+    *pair = f.pair, *stages = f.stages;
+    return CNNCRF_OK;
+}
+
+int cnncrf_conv_tuning_clear(void)
+{
+    k::conv_forms_clear();
+    return CNNCRF_OK;
+}
+
 int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, int width, int height, int depth,
                      const cnncrf_crf_options *opt, int32_t *d_labels, double *lower_bound, void *d_workspace,
                      size_t workspace_bytes, cnncrf_stream_t stream)

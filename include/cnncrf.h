@@ -94,6 +94,15 @@ int cnncrf_abi_version(void);
    counterpart (a GB300 execution choice). */
 int cnncrf_set_conv_pairs(int enable);
 int cnncrf_get_conv_pairs(int *enable);
+/* The tensor-core convolutions' tuned launch forms (no reference
+ * counterpart).  cnncrf_batch_autotune times every form of each of its nets'
+ * convolutions -- 2-CTA pairs or single CTAs, 2 to 4 pipeline stages -- and
+ * enters the fastest per layer shape in a process-wide table that later
+ * launches of that shape use (every form gives the same bits).
+ * shape = n_img, Hin, Win, cp_in, cin, np, cout, kh, kw, mode. */
+int cnncrf_conv_tuning_count(int *n);
+int cnncrf_conv_tuning_get(int index, int shape[10], int *pair, int *stages, float *ms);
+int cnncrf_conv_tuning_clear(void);
 
 /* ---------------------------------------------------------------- StereoNet */
 

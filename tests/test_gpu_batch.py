@@ -176,3 +176,39 @@ def test_uneven_batch_full_size_equals_single(cuda):
         assert np.array_equal(b.labels_device(i).cpu().numpy(), lab), i
         assert np.array_equal(b.get_output(i), disp), i
         assert b.lower_bound(i) == lb, i
+
+
+def test_batch_autotune_tunes_conv_forms_and_changes_no_bit(cuda):
+    """StereoBatch.autotune times every launch form of the tensor-core
+    convolutions (2-CTA pairs or single CTAs, 2-4 stages) per layer shape and
+    enters the fastest in the process-wide table, beside the CRF tiles; the
+    run after it (using the tuned forms and tiles) gives the same bits."""
+    from cnncrf import scenes, tuning, _lib as L
+    from cnncrf.api import StereoBatch
+    torch = cuda
+    tuning.clear_conv()
+    shapes = [(300, 40, 32), (300, 40, 32), (140, 24, 16)]
+    sc = [scenes.voronoi_scene(W, H, D, seed=70 + i, cells=4, off_range=(1, D - 2)) for i, (W, H, D) in
+          enumerate(shapes)]
+    b = StereoBatch(precision=L.BF16, num_layers=3, seed=0, graph=True)
+    for (W, H, D) in shapes:
+        b.add_pair(W, H, 0.0, 1.0, float(D - 1))
+    for i, s in enumerate(sc):
+        b.set_images(i, s["left"], s["right"])
+    b.run(0.5, 1.5, 3, 4)
+    b.check()
+    before = [b.get_output(i).copy() for i in range(len(shapes))]
+    b.autotune(0.5, 1.5, 3, 4)
+    forms = tuning.conv_forms()
+    # per group: feature layers 2..3 and the pairwise layer 2, each its own shape
+    assert len(forms) >= 6, forms
+    for f in forms:
+        assert f["pair"] in (0, 1) and 2 <= f["stages"] <= 4 and f["ms"] > 0
+    for rnd in range(2):  # eager with the tuned forms, then capture and replay
+        for i, s in enumerate(sc):
+            b.set_images(i, s["left"], s["right"])
+        b.run(0.5, 1.5, 3, 4)
+        b.check()
+        for i in range(len(shapes)):
+            assert np.array_equal(b.get_output(i), before[i]), (rnd, i)
+    tuning.clear_conv()
