@@ -192,6 +192,7 @@ PROTOS = {
     "cnncrf_profile_reset": ([], i32),
     "cnncrf_profile_query": ([C.c_char_p, C.POINTER(i32), C.POINTER(C.c_double)], i32),
     "cnncrf_profile_kernels": ([C.c_char_p, C.c_size_t], i32),
+    "cnncrf_selftest_bounded_wait": ([i32, i32, vp], i32),
 }
 
 _lib = None
@@ -246,3 +247,9 @@ def profile_kernels():
     buf = C.create_string_buffer(8192)
     call("cnncrf_profile_kernels", buf, 8192)
     return [k for k in buf.value.decode().split("\n") if k]
+
+
+def selftest_bounded_wait(polls, arrive, stream=None):
+    """Run the bounded-wait probe; returns the raw status (OK, or ETIMEOUT when
+    the wait on a barrier nothing completes gave up) without raising."""
+    return lib().cnncrf_selftest_bounded_wait(int(polls), 1 if arrive else 0, stream)

@@ -283,5 +283,9 @@ int tv_iterate(float *u, float *u_, const float *u0, const float *qf, float *p, 
                const float *wx, const float *wy, int W, int H, float C, float eps, float step,
                int iters, void *ws, size_t ws_bytes, bool pq_zero, cudaStream_t st);
 
+// Bounded-wait self-test (k_selftest.cu): CNNCRF_ETIMEOUT when the probe's wait
+// on a barrier that nothing completes (arrive == 0) gave up after `polls` polls.
+int selftest_bounded_wait(int polls, int arrive, cudaStream_t st);
+
 } // namespace k
 } // namespace cnncrf

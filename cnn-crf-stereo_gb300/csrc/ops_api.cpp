@@ -137,6 +137,12 @@ int cnncrf_conv_tuning_clear(void)
     return CNNCRF_OK;
 }
 
+int cnncrf_selftest_bounded_wait(int polls, int arrive, cnncrf_stream_t stream)
+{
+    clear_error();
+    return k::selftest_bounded_wait(polls, arrive, (cudaStream_t)stream);
+}
+
 int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, int width, int height, int depth,
                      const cnncrf_crf_options *opt, int32_t *d_labels, double *lower_bound, void *d_workspace,
                      size_t workspace_bytes, cnncrf_stream_t stream)

@@ -592,6 +592,17 @@ int cnncrf_profile_query(const char *kernel, int *launches, double *total_ms);
 /* Newline-separated names of the kernels timed since the last reset. */
 int cnncrf_profile_kernels(char *buf, size_t len);
 
+/* No counterpart in the reference (its kernels have no device-side waits).
+ * Self-test of the bounded waits and of the error path they feed: one warp
+ * waits on a shared-memory mbarrier through the same bounded wait the
+ * tensor-core kernels use, giving up after `polls` polls (1 .. 2^20).  With
+ * arrive != 0 the barrier completes before the wait and the call returns
+ * CNNCRF_OK; with arrive == 0 nothing completes it, the wait runs out, the
+ * kernel raises its error flag and the call returns CNNCRF_ETIMEOUT.  The
+ * probe moves no data and holds no tensor memory, so the context stays usable
+ * after a timeout.  Synchronises the stream. */
+int cnncrf_selftest_bounded_wait(int polls, int arrive, cnncrf_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

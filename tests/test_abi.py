@@ -150,3 +150,11 @@ def test_conv_pairs_switch(lib):
         assert lib.cnncrf_set_conv_pairs(1) == L.OK
     assert lib.cnncrf_get_conv_pairs(C.byref(v)) == L.OK and v.value == 1
     assert lib.cnncrf_get_conv_pairs(None) == L.EINVAL
+
+
+def test_selftest_poll_limit_checked_on_host(lib):
+    """The bounded-wait probe refuses a poll limit outside 1 .. 2^20 before it
+    touches the device."""
+    import cnncrf._lib as L
+    for polls in (0, -3, (1 << 20) + 1):
+        assert L.selftest_bounded_wait(polls, arrive=False) == L.EINVAL
