@@ -116,14 +116,14 @@ def q16_unary(torch, vol, unary):
     return q * scale + offset
 
 
-@pytest.mark.parametrize("D,unary", [(64, 1), (96, 1), (128, 1), (128, 0)])
+@pytest.mark.parametrize("D,unary", [(64, 1), (96, 1), (128, 1), (128, 0), (192, 1)])
 def test_bf16_crf_reads_the_16bit_unary(cuda, D, unary):
     """The BF16 path's CRF reads a 16-bit fixed-point copy of the unary volume
     that the tensor-core correlation writes beside the FP32 one (half the
     bytes of the horizontal passes' two unary reads; 2^-15 resolution for the
     1 - <fL,fR> unary, 2^-16 for -softmax), where each lane's labels are an
-    even count (D = 64, 128: 2 and 4 per lane); at D = 96 (3 per lane) it
-    reads the FP32 volume.  Either way its labels and bound equal those of the
+    even count (D = 64, 128, 192: 2, 4 and 6 per lane); at D = 96 (3 per
+    lane) it reads the FP32 volume.  Either way its labels and bound equal those of the
     FP32 solver (the C ABI's cnncrf_crf_solve) on the volume as the CRF read
     it -- dequantised where the copy is used -- bit for bit; the solve itself
     stays FP32 (messages) and FP64 (bound)."""
