@@ -18,7 +18,9 @@ MATCH_COLORCNN, MATCH_GRAYCNN, MATCH_CONCATCNN, MATCH_GRAYCNN_PAIRWISE, MATCH_CO
     MATCH_CONCATCNN_PAIRWISE, MATCH_CENSUS, MATCH_LOAD = range(8)
 FP32, BF16 = 0, 1
 UNARY_NEG_SOFTMAX, UNARY_ONE_MINUS_DOT = 0, 1
-TOPO_REF, TOPO_ALL3X3 = 0, 1
+TOPO_REF, TOPO_ALL3X3, TOPO_CONCAT = 0, 1, 2
+# ConcatStereoNet's growth rate per depth (the library's table)
+CONCAT_GROWTH = {3: 33, 5: 20, 7: 14, 10: 10, 15: 7, 20: 5, 25: 4, 33: 3, 50: 2, 100: 1}
 RHO_STEP, RHO_LINEAR = 0, 1
 
 

@@ -52,11 +52,16 @@ def _stream_ptr(stream):
 
 
 class StereoNet:
-    """StereoNet(numLayers, n, c, h, w) / ColorStereoNet; h, w are the padded size."""
+    """StereoNet(numLayers, n, c, h, w) / ColorStereoNet / ConcatStereoNet
+    (topology TOPO_CONCAT); h, w are the padded size.  feat_channels defaults
+    to 100, or to the concatenated width (growth rate x layers) for
+    TOPO_CONCAT."""
 
-    def __init__(self, num_layers, n, c, h, w, topology=L.TOPO_REF, feat_channels=100,
+    def __init__(self, num_layers, n, c, h, w, topology=L.TOPO_REF, feat_channels=None,
                  unary=L.UNARY_NEG_SOFTMAX, precision=L.FP32, with_pairwise=False, pw_channels=64,
                  stream=None):
+        if feat_channels is None:
+            feat_channels = L.CONCAT_GROWTH.get(num_layers, 0) * num_layers if topology == L.TOPO_CONCAT else 100
         d = NetDesc(num_layers, topology, c, feat_channels, unary, precision,
                     1 if with_pairwise else 0, pw_channels)
         self._h = C.c_void_p()

@@ -123,24 +123,25 @@ struct cnncrf_batch {
 
 int cnncrf_batch::build()
 {
-    if (matching != CNNCRF_MATCH_COLORCNN_PAIRWISE && matching != CNNCRF_MATCH_GRAYCNN_PAIRWISE)
-        return fail(CNNCRF_EUNSUPPORTED, "batch: only the pairwise (COLORPAIR) matching is batched");
+    if (matching != CNNCRF_MATCH_COLORCNN_PAIRWISE && matching != CNNCRF_MATCH_GRAYCNN_PAIRWISE &&
+        matching != CNNCRF_MATCH_CONCATCNN_PAIRWISE)
+        return fail(CNNCRF_EUNSUPPORTED, "batch: only the pairwise matchings (COLORPAIR) are batched");
     bool gray = matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
+    const bool concat = matching == CNNCRF_MATCH_CONCATCNN_PAIRWISE; // FP32 only
     for (auto &gp : groups) {
         Group &g = *gp;
         const int n = (int)g.members.size();
         const size_t N = (size_t)g.W * g.H;
         cnncrf_net_desc d{};
         d.num_layers = num_layers;
-        d.topology = o.topology;
+        d.topology = concat ? CNNCRF_TOPO_CONCAT : o.topology;
         d.in_channels = gray ? 1 : (with_xy ? 5 : 3);
-        d.feat_channels = o.feat_channels;
+        d.feat_channels = concat ? 0 : o.feat_channels;
         d.unary = o.unary;
         d.precision = o.precision;
         d.with_pairwise = 1;
         d.pw_channels = o.pw_channels;
-        int loss = 2 + (num_layers - 1) * (o.topology == CNNCRF_TOPO_REF ? 1 : 2);
-        int pad = loss / 2;
+        const int pad = net_padding(d);
         if (g.net) cnncrf_net_destroy(g.net);
         g.net = nullptr;
         CNNCRF_TRY(cnncrf_net_create(&g.net, &d, n, g.H + 2 * pad, g.W + 2 * pad));

@@ -26,6 +26,7 @@ __device__ __forceinline__ float act_fn(float v, int act)
 {
     if (act == 1) return cnncrf_tanhf(v);
     if (act == 2) return fabsf(v);
+    if (act == 3) return fabsf(cnncrf_tanhf(v));
     return v;
 }
 
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
         int p = (i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4);
         int ox = ox0 + p;
         if (ox >= Wo) continue;
-        float *dst = a.out16 ? nullptr : a.out + ((long)oy * Wo + ox) * a.Cout;
+        float *dst = a.out16 ? nullptr : a.out + (long)oy * a.out_row + (long)ox * a.out_pix;
         __nv_bfloat16 *dst16 = a.out16 ? (__nv_bfloat16 *)a.out16 + ((long)oy * Wo + ox) * a.out_cs : nullptr;
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
                 if (a.bias) v = __fadd_rn(v, a.bias[co]);
                 v = act_fn(v, a.act);
                 if (dst16) dst16[co] = __float2bfloat16_rn(v);
-                else dst[co] = v;
+                else dst[(long)co * a.out_ch] = v;
             }
         }
     }
@@ -222,13 +223,16 @@ __global__ void k_l2norm(float *__restrict__ f, long npx, int C)
 
 } // namespace
 
-int conv_simt(const ConvArgs &a, cudaStream_t st)
+int conv_simt(const ConvArgs &args, cudaStream_t st)
 {
+    ConvArgs a = args;
     if (a.Cout > BN) return fail(CNNCRF_EINVAL, "conv_simt: Cout %d > %d", a.Cout, BN);
     int Ho = a.H - a.kh + 1, Wo = a.W - a.kw + 1;
     if (Ho <= 0 || Wo <= 0) return fail(CNNCRF_ESHAPE, "conv_simt: empty output");
     int K = a.kh * a.kw * a.Cin;
-    if (K <= 45 && (a.Cout == 100 || a.Cout == 64) && a.Cout == (a.Cout & ~1)) {
+    const bool dense = a.out_pix == 0;
+    if (dense) a.out_pix = a.Cout, a.out_row = (long)Wo * a.Cout, a.out_ch = 1;
+    if (dense && K <= 45 && (a.Cout == 100 || a.Cout == 64) && a.Cout == (a.Cout & ~1)) {
         dim3 g(ceil_div(Wo, 128), Ho, a.n_img);
         size_t smem = sizeof(float) * (size_t)K * ((a.Cout + 3) & ~3);
         if (a.Cout == 100) {

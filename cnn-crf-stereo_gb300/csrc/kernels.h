@@ -29,12 +29,15 @@ struct ConvArgs {
     long in_pix, in_row;  // element strides of a pixel and of a row
     const float *wt;      // [K][128] flipped, transposed, zero padded
     const float *bias;    // [128] or nullptr
-    int Cout, kh, kw, act; // act: 0 none, 1 tanh, 2 abs
-    float *out;           // NHWC dense [Ho][Wo][Cout]
+    int Cout, kh, kw, act; // act: 0 none, 1 tanh, 2 abs, 3 |tanh|
+    float *out;           // NHWC dense [Ho][Wo][Cout], unless strides are given below
     void *out16 = nullptr; // if set: BF16 NHWC output [Ho][Wo][out_cs] instead of `out`
     int out_cs = 0;
     int n_img = 1;         // images of a batch: input / output element strides
     long in_img = 0, out_img = 0;
+    // FP32 output element strides of a pixel, a row and a channel (out_pix = 0:
+    // dense NHWC); e.g. a channel slice of a wider tensor, or planar [C][Ho][Wo]
+    long out_pix = 0, out_row = 0, out_ch = 1;
 };
 int conv_simt(const ConvArgs &a, cudaStream_t st);
 // BF16 path: a thin first layer (kh*kw*Cin <= 64, Cout 100 or 64, tanh, BF16

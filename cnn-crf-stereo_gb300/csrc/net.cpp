@@ -40,6 +40,20 @@ void build_layers(cnncrf_net *n)
     int F = d.feat_channels;
     n->feat.clear();
     n->pw.clear();
+    if (d.topology == CNNCRF_TOPO_CONCAT) {
+        // stereo/concatstereonet.cpp:72-127: 3x3 convs to the growth rate g, each
+        // fed the previous layer's g channels, every layer tanh; the pairwise
+        // weights one 3x3 conv of the concatenated features to 2 channels, no bias,
+        // |tanh| (non-negative, as the CRF needs)
+        const int g = n->growth;
+        n->feat.push_back({d.in_channels, g, 3, 3, 1, 0, 1});
+        for (int l = 1; l < d.num_layers; ++l) n->feat.push_back({g, g, 3, 3, 1, 2 * l, 2 * l + 1});
+        if (d.with_pairwise) n->pw.push_back({F, 2, 3, 3, 3, 2 * d.num_layers, -1});
+        const int nparams = 2 * d.num_layers + (d.with_pairwise ? 1 : 0);
+        n->host.assign(nparams, {});
+        n->have.assign(nparams, 0);
+        return;
+    }
     // stereo/stereonet.cpp:69-133: 3x3 first, 2x2 after (REF), every layer tanh
     n->feat.push_back({d.in_channels, F, 3, 3, 1, 0, 1});
     int k = d.topology == CNNCRF_TOPO_REF ? 2 : 3;
@@ -232,6 +246,55 @@ int cnncrf_net::predict_fp32(const float *left, const float *right)
     return CNNCRF_OK;
 }
 
+// ConcatStereoNet (FP32): every layer a 3x3 conv with zero padding 1 to the
+// growth rate g.  Layer l writes channels [l g, (l+1) g) of one zero-bordered
+// tensor cz [n][h+2][w+2][g L] and reads layer l-1's channels of it, so the
+// border supplies the padding and the concatenation needs no copy.  The
+// correlation reads the features cropped to [n][H][W][g L]; the pairwise conv
+// reads the bordered left features (before any L2 normalisation).
+int cnncrf_net::predict_concat(const float *left, const float *right)
+{
+    const float *img[2] = {left, right};
+    const int ic = d.in_channels, C = d.feat_channels, g = growth;
+    const long bw = w + 2, bh = h + 2;
+    const long x_img = bh * bw * ic, z_img = bh * bw * C;
+    for (int s = 0; s < 2; ++s) {
+        CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
+        float *x = cx[s].as<float>(), *z = cz[s].as<float>();
+        for (int i = 0; i < n; ++i)
+            CNNCRF_CUDA(cudaMemcpy2DAsync(x + i * x_img + (bw + 1) * ic, sizeof(float) * bw * ic,
+                                          norm[s].as<float>() + (long)i * h * w * ic, sizeof(float) * w * ic,
+                                          sizeof(float) * w * ic, h, cudaMemcpyDeviceToDevice, st));
+        for (size_t l = 0; l < feat.size(); ++l) {
+            Layer &L = feat[l];
+            const bool first = l == 0;
+            k::ConvArgs a{first ? x : z + (l - 1) * g, (int)bh, (int)bw, L.cin, first ? (long)ic : (long)C,
+                          bw * (first ? ic : C), L.wt.as<float>(), L.bias.as<float>(), L.cout, 3, 3, L.act,
+                          z + (bw + 1) * C + (long)l * g};
+            a.n_img = n, a.in_img = first ? x_img : z_img, a.out_img = z_img;
+            a.out_pix = C, a.out_row = bw * C, a.out_ch = 1;
+            CNNCRF_TRY(k::conv_simt(a, st));
+        }
+        for (int i = 0; i < n; ++i)
+            CNNCRF_CUDA(cudaMemcpy2DAsync(cf[s].as<float>() + (long)i * H * W * C, sizeof(float) * W * C,
+                                          z + i * z_img + (bw + 1) * C, sizeof(float) * bw * C, sizeof(float) * W * C,
+                                          H, cudaMemcpyDeviceToDevice, st));
+        feats[s] = cf[s].as<float>();
+    }
+    if (d.with_pairwise) {
+        Layer &P = pw[0];
+        k::ConvArgs a{cz[0].as<float>(), (int)bh, (int)bw, C, (long)C, bw * C, P.wt.as<float>(), nullptr, 2, 3, 3,
+                      P.act, pwout};
+        a.n_img = n, a.in_img = z_img, a.out_img = 2L * H * W;
+        a.out_pix = 1, a.out_row = W, a.out_ch = (long)H * W; // planar [2][H][W]
+        CNNCRF_TRY(k::conv_simt(a, st));
+    }
+    if (d.unary == CNNCRF_UNARY_ONE_MINUS_DOT)
+        for (int s = 0; s < 2; ++s) CNNCRF_TRY(k::l2norm(feats[s], (long)H * W * n, C, st));
+    return k::correlation(feats[0], feats[1], H, W, C, d_list.as<float>(), D, omin, omax, interp || force_interp,
+                          d.unary, vol, st, n, (long)H * W * C);
+}
+
 int cnncrf_net::predict(const float *left, const float *right)
 {
     if (!inited) return fail(CNNCRF_ESTATE, "predict before initNet");
@@ -239,8 +302,33 @@ int cnncrf_net::predict(const float *left, const float *right)
         if (!have[i]) return fail(CNNCRF_ESTATE, "parameter arr_%zu not set", i);
     if (!left || !right) return fail(CNNCRF_EINVAL, "predict: null image");
     volq_valid = false;
+    if (d.topology == CNNCRF_TOPO_CONCAT) return predict_concat(left, right);
     if (d.precision == CNNCRF_BF16) return predict_bf16(left, right);
     return predict_fp32(left, right);
+}
+
+int cnncrf::concat_growth(int layers)
+{
+    switch (layers) {
+    case 3: return 33;
+    case 5: return 20;
+    case 7: return 14;
+    case 10: return 10;
+    case 15: return 7;
+    case 20: return 5;
+    case 25: return 4;
+    case 33: return 3;
+    case 50: return 2;
+    case 100: return 1;
+    default: return 0;
+    }
+}
+
+int cnncrf::net_padding(const cnncrf_net_desc &d)
+{
+    if (d.topology == CNNCRF_TOPO_CONCAT) return 0;
+    const int loss = 2 + (d.num_layers - 1) * (d.topology == CNNCRF_TOPO_REF ? 1 : 2);
+    return loss / 2;
 }
 
 // ---------------------------------------------------------------- C ABI
@@ -254,12 +342,21 @@ int cnncrf_net_create(cnncrf_net_t *out, const cnncrf_net_desc *desc, int n, int
     *out = nullptr;
     const cnncrf_net_desc &d = *desc;
     if (n < 1 || n > 256) return fail(CNNCRF_EINVAL, "net_create: batch n = %d outside 1..256", n);
-    if (d.num_layers < 1 || d.num_layers > 16) return fail(CNNCRF_EINVAL, "net_create: num_layers %d", d.num_layers);
-    if (d.topology != CNNCRF_TOPO_REF && d.topology != CNNCRF_TOPO_ALL3X3)
+    const bool concat = d.topology == CNNCRF_TOPO_CONCAT;
+    if (d.topology != CNNCRF_TOPO_REF && d.topology != CNNCRF_TOPO_ALL3X3 && !concat)
         return fail(CNNCRF_EINVAL, "net_create: topology %d", d.topology);
+    const int growth = concat ? concat_growth(d.num_layers) : 0;
+    if (concat && growth == 0) // stereo/concatstereonet.cpp:52-55
+        return fail(CNNCRF_EINVAL, "ConcatStereoNet must have one of the following numbers of layers: 3, 5, 7, 10, "
+                                   "15, 20, 25, 33, 50, 100 (got %d)", d.num_layers);
+    if (!concat && (d.num_layers < 1 || d.num_layers > 16))
+        return fail(CNNCRF_EINVAL, "net_create: num_layers %d", d.num_layers);
     if (d.in_channels != 1 && d.in_channels != 3 && d.in_channels != 5)
         return fail(CNNCRF_EINVAL, "net_create: in_channels must be 1, 3 or 5");
-    if (d.feat_channels < 1 || d.feat_channels > 128)
+    if (concat && d.feat_channels != 0 && d.feat_channels != growth * d.num_layers)
+        return fail(CNNCRF_EINVAL, "net_create: the concatenating net's features are %d x %d = %d channels, not %d",
+                    d.num_layers, growth, growth * d.num_layers, d.feat_channels);
+    if (!concat && (d.feat_channels < 1 || d.feat_channels > 128))
         return fail(CNNCRF_EINVAL, "net_create: feat_channels %d outside 1..128", d.feat_channels);
     if (d.with_pairwise && (d.pw_channels < 1 || d.pw_channels > 128))
         return fail(CNNCRF_EINVAL, "net_create: pw_channels %d outside 1..128", d.pw_channels);
@@ -267,8 +364,23 @@ int cnncrf_net_create(cnncrf_net_t *out, const cnncrf_net_desc *desc, int n, int
         return fail(CNNCRF_EINVAL, "net_create: unary %d", d.unary);
     if (d.precision != CNNCRF_FP32 && d.precision != CNNCRF_BF16)
         return fail(CNNCRF_EINVAL, "net_create: precision %d", d.precision);
+    if (concat && d.precision != CNNCRF_FP32)
+        return fail(CNNCRF_EUNSUPPORTED, "net_create: the concatenating net runs in FP32 only");
     auto *net = new cnncrf_net;
     net->d = d;
+    if (concat) {
+        net->growth = growth;
+        net->d.feat_channels = growth * d.num_layers;
+        build_layers(net);
+        net->pad = 0; // stereo/stereo.cpp:214-216
+        net->n = n, net->h = h, net->w = w, net->H = h, net->W = w;
+        if (h < 1 || w < 1) {
+            delete net;
+            return fail(CNNCRF_ESHAPE, "net_create: empty %dx%d input", w, h);
+        }
+        *out = net;
+        return CNNCRF_OK;
+    }
     build_layers(net);
     int loss = 0;
     for (auto &L : net->feat) loss += L.kh - 1;
@@ -314,7 +426,7 @@ int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step
     size_t np = (size_t)h * w * nb;
     for (int s = 0; s < 2; ++s) CNNCRF_TRY(net->norm[s].reserve(np * ic * sizeof(float)));
     size_t amax = 0;
-    {
+    if (net->d.topology != CNNCRF_TOPO_CONCAT) { // valid convs: each layer shrinks the maps
         int ch = h, cw = w;
         for (auto &L : net->feat) {
             ch -= L.kh - 1, cw -= L.kw - 1;
@@ -322,13 +434,24 @@ int cnncrf_net_init(cnncrf_net_t net, float min_disp, float max_disp, float step
         }
     }
     const bool fp32 = net->d.precision == CNNCRF_FP32;
+    const bool concat = net->d.topology == CNNCRF_TOPO_CONCAT;
     for (int s = 0; s < 2; ++s)
         for (int b = 0; b < 2; ++b)
-            if (fp32) CNNCRF_TRY(net->act[s][b].reserve(amax * nb * sizeof(float)));
+            if (fp32 && !concat) CNNCRF_TRY(net->act[s][b].reserve(amax * nb * sizeof(float)));
+    if (concat) { // the borders stay zero: predict writes only the interiors
+        const size_t bpx = (size_t)(h + 2) * (w + 2) * nb, C = net->d.feat_channels;
+        for (int s = 0; s < 2; ++s) {
+            CNNCRF_TRY(net->cx[s].reserve(bpx * ic * sizeof(float)));
+            CNNCRF_TRY(net->cz[s].reserve(bpx * C * sizeof(float)));
+            CNNCRF_TRY(net->cf[s].reserve((size_t)H * W * nb * C * sizeof(float)));
+            CNNCRF_CUDA(cudaMemsetAsync(net->cx[s].get(), 0, bpx * ic * sizeof(float), net->st));
+            CNNCRF_CUDA(cudaMemsetAsync(net->cz[s].get(), 0, bpx * C * sizeof(float), net->st));
+        }
+    }
     CNNCRF_TRY(net->scratch.reserve(k::normalize_scratch_bytes(h, nb)));
     if (net->d.with_pairwise) {
         int P = net->d.pw_channels;
-        if (fp32) {
+        if (fp32 && !concat) {
             CNNCRF_TRY(net->pwa.reserve((size_t)(H + 2) * (W + 2) * P * nb * sizeof(float)));
             CNNCRF_TRY(net->pwb.reserve((size_t)H * W * P * nb * sizeof(float)));
         }

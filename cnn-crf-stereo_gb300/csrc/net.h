@@ -44,6 +44,12 @@ struct cnncrf_net {
     cnncrf::DevBuf norm[2], act[2][2], pwa, pwb, scratch;
     float *feats[2] = {nullptr, nullptr};
     bool inited = false;
+    // the concatenating topology: growth rate g, the zero-bordered input
+    // [n][h+2][w+2][ic] and features [n][h+2][w+2][g L] of each side, and
+    // the features cropped to [n][H][W][g L] for the correlation
+    int growth = 0;
+    cnncrf::DevBuf cx[2], cz[2], cf[2];
+    int predict_concat(const float *left, const float *right);
 
     // tensor-core path: BF16 NHWC activations of both images, channel
     // padded to cp_feat (feature net) / cp_pw (pairwise net)
@@ -67,3 +73,11 @@ struct cnncrf_net {
     int pairwise_fp32();
     int set_disparities(float mn, float mx, float step, float *d_out);
 };
+
+namespace cnncrf {
+// ConcatStereoNet's growth rate for a depth (stereo/concatstereonet.cpp:28-56); 0 for any other depth
+int concat_growth(int layers);
+// mirror padding a net of this description needs around its images
+// (stereo/stereo.cpp:204-217): the receptive-field loss / 2, 0 for the concatenating net
+int net_padding(const cnncrf_net_desc &d);
+} // namespace cnncrf

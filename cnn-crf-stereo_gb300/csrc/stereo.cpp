@@ -54,7 +54,8 @@ struct cnncrf_stereo {
     }
     bool pairwise() const
     {
-        return matching == CNNCRF_MATCH_COLORCNN_PAIRWISE || matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
+        return matching == CNNCRF_MATCH_COLORCNN_PAIRWISE || matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE ||
+               matching == CNNCRF_MATCH_CONCATCNN_PAIRWISE;
     }
     int record(int i)
     {
@@ -80,22 +81,20 @@ int cnncrf_stereo::build_net()
 {
     if (matching == CNNCRF_MATCH_CENSUS)
         return fail(CNNCRF_EUNSUPPORTED, "CENSUS matching is not on the CNN path and is not built");
-    if (matching == CNNCRF_MATCH_CONCATCNN || matching == CNNCRF_MATCH_CONCATCNN_PAIRWISE)
-        return fail(CNNCRF_EUNSUPPORTED, "ConcatStereoNet is not compiled in the reference either");
+    const bool concat = matching == CNNCRF_MATCH_CONCATCNN || matching == CNNCRF_MATCH_CONCATCNN_PAIRWISE;
     bool gray = matching == CNNCRF_MATCH_GRAYCNN || matching == CNNCRF_MATCH_GRAYCNN_PAIRWISE;
-    if (o.topology == CNNCRF_TOPO_REF && num_layers != 3 && num_layers != 5 && num_layers != 7)
+    if (!concat && o.topology == CNNCRF_TOPO_REF && num_layers != 3 && num_layers != 5 && num_layers != 7)
         return fail(CNNCRF_EINVAL, "Only {3,5,7} layers are allowed"); // stereo/stereo.cpp:198-202
     cnncrf_net_desc d{};
     d.num_layers = num_layers;
-    d.topology = o.topology;
+    d.topology = concat ? CNNCRF_TOPO_CONCAT : o.topology; // CONCATCNN: a ConcatStereoNet of num_layers
     d.in_channels = gray ? 1 : (with_xy ? 5 : 3);
-    d.feat_channels = o.feat_channels;
+    d.feat_channels = concat ? 0 : o.feat_channels;
     d.unary = o.unary;
     d.precision = o.precision;
     d.with_pairwise = pairwise() ? 1 : 0;
     d.pw_channels = o.pw_channels;
-    int loss = 2 + (num_layers - 1) * (o.topology == CNNCRF_TOPO_REF ? 1 : 2);
-    int pad = loss / 2;
+    const int pad = net_padding(d);
     CNNCRF_TRY(cnncrf_net_create(&net, &d, 1, H + 2 * pad, W + 2 * pad));
     CNNCRF_TRY(cnncrf_net_set_stream(net, (cnncrf_stream_t)st));
     net->force_interp = false;

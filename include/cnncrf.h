@@ -51,10 +51,10 @@ typedef enum cnncrf_status {
 typedef enum cnncrf_matching {
     CNNCRF_MATCH_COLORCNN = 0,
     CNNCRF_MATCH_GRAYCNN = 1,
-    CNNCRF_MATCH_CONCATCNN = 2,          /* dead code in the reference: EUNSUPPORTED */
+    CNNCRF_MATCH_CONCATCNN = 2,          /* ConcatStereoNet (CNNCRF_TOPO_CONCAT), FP32 */
     CNNCRF_MATCH_GRAYCNN_PAIRWISE = 3,
     CNNCRF_MATCH_COLORCNN_PAIRWISE = 4,  /* "COLORPAIR" on the command line */
-    CNNCRF_MATCH_CONCATCNN_PAIRWISE = 5, /* EUNSUPPORTED */
+    CNNCRF_MATCH_CONCATCNN_PAIRWISE = 5, /* the same with its pairwise weights */
     CNNCRF_MATCH_CENSUS = 6,             /* census cost + image-gradient edge weights */
     CNNCRF_MATCH_LOAD = 7                /* volume supplied by the caller */
 } cnncrf_matching;
@@ -70,8 +70,23 @@ typedef enum cnncrf_unary {
 } cnncrf_unary;
 
 typedef enum cnncrf_topology {
-    CNNCRF_TOPO_REF = 0,   /* 3x3 first layer, 2x2 layers after (stereo/stereonet.cpp:69-133) */
-    CNNCRF_TOPO_ALL3X3 = 1 /* every layer 3x3 */
+    CNNCRF_TOPO_REF = 0,    /* 3x3 first layer, 2x2 layers after (stereo/stereonet.cpp:69-133) */
+    CNNCRF_TOPO_ALL3X3 = 1, /* every layer 3x3 */
+    /* ConcatStereoNet (stereo/concatstereonet.cpp:28-127), FP32 only: num_layers
+       one of 3, 5, 7, 10, 15, 20, 25, 33, 50, 100, with the growth rate g the
+       reference's constructor gives that depth (33, 20, 14, 10, 7, 5, 4, 3, 2,
+       1).  Every layer is a 3x3 conv with zero padding 1 to g channels, bias and
+       tanh, fed the previous layer's output; the features are all layers'
+       outputs side by side, g * num_layers channels (feat_channels must be 0 or
+       that number).  No mirror padding (cnncrf_net_padding 0,
+       stereo/stereo.cpp:214-216).  The pairwise weights: one 3x3 conv of the
+       features to 2 channels, zero padding 1, no bias, |tanh|.  The reference
+       declares this net but never runs it (stereo/stereo.cpp:237-254 builds
+       only ColorStereoNet; its correlation is declared on the input's channels
+       and its pairwise conv on 100), so these are this library's readings:
+       the correlation over the concatenated features, the pairwise conv over
+       them, and |.| to keep the CRF's weights non-negative. */
+    CNNCRF_TOPO_CONCAT = 2
 } cnncrf_topology;
 
 typedef enum cnncrf_pairwise_shape {

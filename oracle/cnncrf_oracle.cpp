@@ -39,10 +39,44 @@ struct Layer {
     int cin, cout, kh, kw, act, wslot, bslot;
 };
 
-// stereo/stereonet.cpp:69-133 (feature net), 159-167 (pairwise net)
+// ConcatStereoNet's growth rate per depth (stereo/concatstereonet.cpp:28-56); 0: no such net
+int growth_rate(int layers)
+{
+    switch (layers) {
+    case 3: return 33;
+    case 5: return 20;
+    case 7: return 14;
+    case 10: return 10;
+    case 15: return 7;
+    case 20: return 5;
+    case 25: return 4;
+    case 33: return 3;
+    case 50: return 2;
+    case 100: return 1;
+    default: return 0;
+    }
+}
+
+// channels of the features the correlation reads
+int feature_width(const oracle_cfg *c)
+{
+    return c->topology == 2 ? growth_rate(c->num_layers) * c->num_layers : c->feat_channels;
+}
+
+// stereo/stereonet.cpp:69-133 (feature net), 159-167 (pairwise net);
+// topology 2: ConcatStereoNet (stereo/concatstereonet.cpp:72-127), every layer
+// a 3x3 conv with zero padding 1 to the growth rate g, fed the previous
+// layer's output; the features are all L layer outputs side by side (g L
+// channels, layer 1 first)
 std::vector<Layer> feature_layers(const oracle_cfg *c)
 {
     std::vector<Layer> v;
+    if (c->topology == 2) {
+        int g = growth_rate(c->num_layers);
+        v.push_back({c->in_channels, g, 3, 3, 1, 0, 1});
+        for (int l = 1; l < c->num_layers; ++l) v.push_back({g, g, 3, 3, 1, 2 * l, 2 * l + 1});
+        return v;
+    }
     int F = c->feat_channels;
     v.push_back({c->in_channels, F, 3, 3, 1, 0, 1});
     int k = c->topology == 0 ? 2 : 3;
@@ -53,6 +87,10 @@ std::vector<Layer> feature_layers(const oracle_cfg *c)
 std::vector<Layer> pairwise_layers(const oracle_cfg *c)
 {
     std::vector<Layer> v;
+    if (c->topology == 2) { // a 3x3 conv of the features to 2 channels, zero padding 1, no bias, |tanh|
+        v.push_back({feature_width(c), 2, 3, 3, 3, 2 * c->num_layers, -1});
+        return v;
+    }
     int base = 2 * c->num_layers;
     int pc = c->in_channels == 1 ? 1 : 3;
     int P = c->pw_channels;
@@ -175,6 +213,7 @@ void conv_T(const T *in, int H, int W, int Cin, const float *w, const float *b, 
                 if (b) v = v + (T)b[co];
                 if (act == 1) v = tanhT<T>(v);
                 else if (act == 2) v = std::fabs(v);
+                else if (act == 3) v = std::fabs(tanhT<T>(v));
                 dst[co] = v;
             }
         }
@@ -294,10 +333,67 @@ template <> void unary_T<double>(double *vol, long npx, int D, int unary)
 // ---------------------------------------------------------------- predict
 // ColorStereoNet::predict (stereo/colorstereonet.cpp:38-133) +
 // StereoNet::performPrediction (stereo/stereonet.cpp:250-421).
+// [H][W][C] -> [H+2][W+2][C] with a zero border (a 3x3 conv with zero padding 1
+// is the valid conv of this)
+template <class T> std::vector<T> zero_border(const T *src, int H, int W, int C)
+{
+    std::vector<T> o((size_t)(H + 2) * (W + 2) * C, (T)0);
+    for (int y = 0; y < H; ++y)
+        std::memcpy(&o[((size_t)(y + 1) * (W + 2) + 1) * C], src + (size_t)y * W * C, sizeof(T) * (size_t)W * C);
+    return o;
+}
+
+// ConcatStereoNet::initNet + ColorStereoNet::predict (stereo/concatstereonet.cpp:72-127,
+// stereo/colorstereonet.cpp:38-77) as this library builds the net: no mirror
+// padding (stereo/stereo.cpp:214-216 sets it to 0), every conv zero-padded,
+// the correlation over all g L feature channels, and the pairwise weights
+// |tanh(conv3x3(features))| from the raw (not normalised) left features.
+template <class T>
+int predict_concat_T(const oracle_cfg *cfg, const float *const *params, const float *lp, const float *rp,
+                     int w, int h, const float *list, int D, int force_interp, T *vol, T *pw)
+{
+    const int H = h, W = w, ic = cfg->in_channels;
+    const int g = growth_rate(cfg->num_layers), C = feature_width(cfg);
+    if (g == 0) return 3;
+    auto layers = feature_layers(cfg);
+    std::vector<T> feat[2];
+    const float *img[2] = {lp, rp};
+    for (int s = 0; s < 2; ++s) {
+        std::vector<T> n((size_t)W * H * ic), t((size_t)W * H * g);
+        normalize_T<T>(img[s], w, h, ic, n.data());
+        feat[s].assign((size_t)W * H * C, (T)0);
+        std::vector<T> cur = zero_border<T>(n.data(), H, W, ic);
+        for (size_t l = 0; l < layers.size(); ++l) {
+            const Layer &L = layers[l];
+            conv_T<T>(cur.data(), H + 2, W + 2, L.cin, params[L.wslot], params[L.bslot], g, 3, 3, L.act, t.data());
+            for (long i = 0; i < (long)H * W; ++i)
+                for (int c = 0; c < g; ++c) feat[s][(size_t)i * C + l * g + c] = t[(size_t)i * g + c];
+            cur = zero_border<T>(t.data(), H, W, g);
+        }
+    }
+    if (cfg->with_pairwise && pw) {
+        const Layer P = pairwise_layers(cfg)[0];
+        std::vector<T> z = zero_border<T>(feat[0].data(), H, W, C), t((size_t)W * H * 2);
+        conv_T<T>(z.data(), H + 2, W + 2, C, params[P.wslot], nullptr, 2, 3, 3, P.act, t.data());
+        for (long i = 0; i < (long)H * W; ++i) {
+            pw[i] = t[(size_t)i * 2];
+            pw[(size_t)H * W + i] = t[(size_t)i * 2 + 1];
+        }
+    }
+    if (cfg->unary == 1) {
+        l2norm_T<T>(feat[0].data(), (long)H * W, C);
+        l2norm_T<T>(feat[1].data(), (long)H * W, C);
+    }
+    correlation_T<T>(feat[0].data(), feat[1].data(), H, W, C, list, D, force_interp, vol);
+    unary_T<T>(vol, (long)H * W, D, cfg->unary);
+    return 0;
+}
+
 template <class T>
 int predict_T(const oracle_cfg *cfg, const float *const *params, const float *lp, const float *rp,
               int w, int h, const float *list, int D, int force_interp, T *vol, T *pw)
 {
+    if (cfg->topology == 2) return predict_concat_T<T>(cfg, params, lp, rp, w, h, list, D, force_interp, vol, pw);
     int p = oracle_padding(cfg);
     if (p < 0) return 1;
     int H = h - 2 * p, W = w - 2 * p;
@@ -455,11 +551,12 @@ extern "C" {
 
 int oracle_num_params(const oracle_cfg *cfg)
 {
-    return 2 * cfg->num_layers + (cfg->with_pairwise ? 5 : 0);
+    return 2 * cfg->num_layers + (cfg->with_pairwise ? (cfg->topology == 2 ? 1 : 5) : 0);
 }
 
 int oracle_padding(const oracle_cfg *cfg)
 {
+    if (cfg->topology == 2) return growth_rate(cfg->num_layers) ? 0 : -1;
     int loss = 0;
     for (auto &L : feature_layers(cfg)) loss += L.kh - 1;
     if (loss % 2) return -1;
@@ -828,7 +925,7 @@ int oracle_run_pair(const oracle_cfg *cfg, const float *const *params, const flo
 {
     set_threads(cfg->threads);
     int p = oracle_padding(cfg);
-    if (p < 2 && cfg->with_pairwise) return 1;
+    if (p < 0 || (cfg->topology != 2 && p < 2 && cfg->with_pairwise)) return 1;
     int D = oracle_disparity_list(cfg->disp_min, cfg->disp_max, cfg->disp_step, nullptr, 0);
     std::vector<float> list((size_t)D);
     oracle_disparity_list(cfg->disp_min, cfg->disp_max, cfg->disp_step, list.data(), D);
@@ -1120,6 +1217,7 @@ int oracle_predict_backward(const oracle_cfg *cfg, const float *const *params, c
 {
     if (cfg->unary != 1) return 3;
     if (oracle_disp_is_float(list, D)) return 4;
+    if (cfg->topology == 2) return 5; // the concatenating net has no training path
     const int p = oracle_padding(cfg);
     if (p < 0) return 1;
     const int H = h - 2 * p, W = w - 2 * p, ic = cfg->in_channels, C = cfg->feat_channels;

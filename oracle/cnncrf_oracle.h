@@ -77,7 +77,7 @@ extern "C" {
 typedef struct oracle_cfg {
     /* network */
     int num_layers;
-    int topology;      /* 0 ref (3x3 then 2x2), 1 all 3x3 */
+    int topology;      /* 0 ref (3x3 then 2x2), 1 all 3x3, 2 ConcatStereoNet (zero-padded, concatenated) */
     int in_channels;   /* 1, 3, 5 */
     int feat_channels; /* 100 */
     int unary;         /* 0 -softmax, 1 one-minus-dot (L2-normalised features) */

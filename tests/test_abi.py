@@ -158,3 +158,38 @@ def test_selftest_poll_limit_checked_on_host(lib):
     import cnncrf._lib as L
     for polls in (0, -3, (1 << 20) + 1):
         assert L.selftest_bounded_wait(polls, arrive=False) == L.EINVAL
+
+
+def test_concat_net_shapes_and_checks(lib):
+    """ConcatStereoNet (TOPO_CONCAT): the reference constructor's depth /
+    growth-rate table, zero padding, 2 L + 1 parameters with the pairwise
+    conv over the g L concatenated channels; other depths, a wrong channel
+    count and BF16 are refused before anything is allocated."""
+    import cnncrf._lib as L
+    h = C.c_void_p()
+    n, s, nd, pad = C.c_int(), (C.c_int64 * 4)(), C.c_int(), C.c_int()
+    for layers, g in L.CONCAT_GROWTH.items():
+        d = L.NetDesc(layers, L.TOPO_CONCAT, 3, 0, 0, 0, 1, 64)
+        assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 1, 40, 30) == L.OK, lib.cnncrf_last_error()
+        lib.cnncrf_net_num_params(h, C.byref(n))
+        assert n.value == 2 * layers + 1
+        lib.cnncrf_net_padding(h, C.byref(pad))
+        assert pad.value == 0
+        lib.cnncrf_net_param_shape(h, 0, s, C.byref(nd))
+        assert tuple(s[:nd.value]) == (g, 3, 3, 3)
+        lib.cnncrf_net_param_shape(h, 1, s, C.byref(nd))
+        assert tuple(s[:nd.value]) == (g,)
+        if layers > 1:
+            lib.cnncrf_net_param_shape(h, 2, s, C.byref(nd))
+            assert tuple(s[:nd.value]) == (g, g, 3, 3)
+        lib.cnncrf_net_param_shape(h, 2 * layers, s, C.byref(nd))
+        assert tuple(s[:nd.value]) == (2, g * layers, 3, 3)
+        lib.cnncrf_net_destroy(h)
+    for d, rc in [(L.NetDesc(4, L.TOPO_CONCAT, 3, 0, 0, 0, 0, 64), L.EINVAL),   # not in the table
+                  (L.NetDesc(7, L.TOPO_CONCAT, 3, 100, 0, 0, 0, 64), L.EINVAL),  # 7 x 14 = 98 channels
+                  (L.NetDesc(7, L.TOPO_CONCAT, 3, 98, 0, L.BF16, 0, 64), L.EUNSUPPORTED)]:
+        assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 1, 40, 30) == rc
+        assert lib.cnncrf_last_error()
+    d = L.NetDesc(7, L.TOPO_CONCAT, 3, 98, 0, 0, 0, 64)
+    assert lib.cnncrf_net_create(C.byref(h), C.byref(d), 1, 40, 30) == L.OK
+    lib.cnncrf_net_destroy(h)

@@ -266,13 +266,22 @@ def test_stereo_argmax_and_errors(cuda, oracle):
     from cnncrf.api import Stereo, CnnCrfError
     W, H = 40, 24
     s = scenes.voronoi_scene(W, H, 8, seed=9, cells=3, off_range=(1, 6), slope=0.0)
-    st = Stereo()
+    st = Stereo(precision=L.BF16)
     st.initialize(W, H, 0.0, 1.0, 7.0)
-    st.set_matching_function(L.MATCH_CONCATCNN)  # not compiled in the reference either
+    st.set_matching_function(L.MATCH_CONCATCNN)  # the concatenating net runs in FP32 only
+    st.set_num_layers(7)
     st.set_color_images(s["left"], s["right"])
     with pytest.raises(CnnCrfError) as e:
         st.compute_argmax()
     assert e.value.status == L.EUNSUPPORTED
+    st = Stereo()
+    st.initialize(W, H, 0.0, 1.0, 7.0)
+    st.set_matching_function(L.MATCH_CONCATCNN)
+    st.set_num_layers(4)  # not a ConcatStereoNet depth
+    st.set_color_images(s["left"], s["right"])
+    with pytest.raises(CnnCrfError) as e:
+        st.compute_argmax()
+    assert e.value.status == L.EINVAL
     st.set_matching_function(L.MATCH_COLORCNN)
     st.set_num_layers(3)
     st.set_xavier_seed(1)

@@ -172,6 +172,46 @@ def test_crf_zero_weights_is_wta(oracle):
     np.testing.assert_allclose(lb, cost.min(axis=2).astype(np.float64).sum(), rtol=1e-6)
 
 
+def test_concat_net_matches_numpy(oracle):
+    """The oracle's ConcatStereoNet against an independent FP64 numpy
+    restatement: each layer a true (flipped-kernel) 3x3 convolution of the
+    zero-padded previous output plus bias, tanh; the features all layers'
+    outputs in order; the correlation and unary of the oracle's own, pinned
+    elsewhere, applied to them; the pairwise weights |tanh| of a 3x3
+    convolution of the zero-padded raw left features (no bias)."""
+    from cnncrf import scenes
+    W, H, D, layers = 23, 17, 7, 5
+    g = 20
+    s = scenes.voronoi_scene(W, H, D, seed=2, cells=3, off_range=(1, D - 2))
+    for unary in (0, 1):
+        cfg = oracle.make_cfg(num_layers=layers, topology=2, in_channels=3, unary=unary, disp_max=float(D - 1),
+                              with_pairwise=1, precision=64)
+        params = oracle.xavier_params(cfg, seed=5)
+        lst = oracle.disparity_list(0.0, float(D - 1), 1.0)
+        vol, pw = oracle.predict(cfg, params, s["left"], s["right"], lst)
+
+        def conv_same(x, w, b):
+            xp = np.pad(x, ((1, 1), (1, 1), (0, 0)))
+            win = np.lib.stride_tricks.sliding_window_view(xp, (3, 3), axis=(0, 1))  # H, W, Cin, 3, 3
+            y = np.einsum("hwcij,ocij->hwo", win, w[:, :, ::-1, ::-1].astype(np.float64))
+            return y if b is None else y + b.astype(np.float64)
+
+        feats = []
+        for img in (s["left"], s["right"]):
+            x = oracle.normalize(img, 3, precision=64)
+            outs = []
+            for l in range(layers):
+                x = np.tanh(conv_same(x, params[2 * l], params[2 * l + 1]))
+                outs.append(x)
+            feats.append(np.concatenate(outs, axis=2))
+        assert feats[0].shape == (H, W, g * layers)
+        opw = np.abs(np.tanh(conv_same(feats[0], params[2 * layers], None))).transpose(2, 0, 1)
+        np.testing.assert_allclose(pw, opw, rtol=1e-9, atol=1e-12)
+        f = [oracle.l2norm(x, precision=64) if unary == 1 else x for x in feats]
+        ref = oracle.unary(oracle.correlation(f[0], f[1], lst, precision=64), unary, precision=64)
+        np.testing.assert_allclose(vol, ref, rtol=1e-9, atol=1e-12)
+
+
 def test_crf_ties_take_first_minimum(oracle):
     cost = np.zeros((3, 4, 6), np.float32)
     z = np.zeros((3, 4), np.float32)
