@@ -131,6 +131,148 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
     }
 }
 
+// The same convolution with the channel tile cut to the layer's width (TN =
+// 32, 64 or 112 output channels, for Cout <= TN) and the index arithmetic
+// taken out of the k loop.  2 TN threads, each an 8 x 8 register tile (8
+// pixels x 8 channels); k-slices of TK (7 at TN = 112, else 8), so that every
+// thread loads one fixed k offset of each slice, for 128 TK / (2 TN) pixels
+// whose offsets it computes once, and steps its (ky, kx, ci) from slice to
+// slice without a division.  Per output the terms are accumulated in
+// ascending k with one fmaf each, then + bias and the activation, as in
+// k_conv_simt: the same bits.
+template <int TN, int TK>
+__global__ void __launch_bounds__(2 * TN) k_conv_nt(ConvArgs a, int Ho, int Wo, int K)
+{
+    constexpr int NT = 2 * TN;      // threads
+    constexpr int PA = BM * TK / NT; // pixels a thread loads per slice
+    constexpr int PS = NT / TK;      // their stride
+    constexpr int B4 = TK * TN / 4;  // float4 of a weight slice
+    constexpr int BR = (B4 + NT - 1) / NT; // of them per thread
+    static_assert(NT % TK == 0 && (BM * TK) % NT == 0, "k_conv_nt tile");
+    __shared__ __align__(16) float As[2][TK][BM + APAD];
+    __shared__ __align__(16) float Bs[2][TK][TN];
+    const int tid = threadIdx.x;
+    const int oy = blockIdx.y, ox0 = blockIdx.x * BM;
+    a.in += (long)blockIdx.z * a.in_img; // image of the batch
+    if (a.out16) a.out16 = (char *)a.out16 + (long)blockIdx.z * a.out_img * 2;
+    else a.out += (long)blockIdx.z * a.out_img;
+    const float *inb = a.in + (long)oy * a.in_row;
+    // loader roles: k offset lk of every slice at pixels lp + PS j; weight float4s tid + NT r
+    const int lk = tid % TK, lp = tid / TK;
+    // compute roles: 16 pixel groups x TN / 8 channel groups, the pixel group
+    // fastest, so that a quarter warp's 128-bit fragment loads read 128
+    // contiguous bytes of the pixel row and the channel fragments are broadcasts
+    const int ty = tid % 16, tx = tid / 16;
+    long poff[PA];
+    uint32_t pvalid = 0;
+#pragma unroll
+    for (int j = 0; j < PA; ++j) {
+        const int ox = ox0 + lp + PS * j;
+        poff[j] = (long)ox * a.in_pix;
+        if (ox < Wo) pvalid |= 1u << j;
+    }
+    // (ky, kx, ci) of this thread's k in the current slice
+    int kk = lk, ci = 0, kx = 0, ky = 0;
+    if (kk < K) {
+        const int tap = kk / a.Cin;
+        ci = kk - tap * a.Cin;
+        ky = tap / a.kw;
+        kx = tap - ky * a.kw;
+    }
+    const int nfull = K / TK, nsl = (K + TK - 1) / TK;
+
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+
+    float ra[PA];
+    float4 rb[BR];
+    auto loadA = [&]() {
+        const bool kv = kk < K;
+        const float *src = inb + (long)ky * a.in_row + (long)kx * a.in_pix + ci;
+#pragma unroll
+        for (int j = 0; j < PA; ++j) ra[j] = (kv && (pvalid >> j & 1u)) ? __ldg(src + poff[j]) : 0.0f;
+    };
+    auto loadB = [&](int s) {
+#pragma unroll
+        for (int r = 0; r < BR; ++r) {
+            const int f = tid + NT * r, k = s * TK + f / (TN / 4), n = (f % (TN / 4)) * 4;
+            rb[r] = (f < B4 && k < K) ? __ldg((const float4 *)(a.wt + (long)k * BN + n)) : make_float4(0, 0, 0, 0);
+        }
+    };
+    auto storeAB = [&](int buf) {
+#pragma unroll
+        for (int j = 0; j < PA; ++j) As[buf][lk][lp + PS * j] = ra[j];
+#pragma unroll
+        for (int r = 0; r < BR; ++r) {
+            const int f = tid + NT * r;
+            if (f < B4) *(float4 *)&Bs[buf][f / (TN / 4)][(f % (TN / 4)) * 4] = rb[r];
+        }
+    };
+    auto advance = [&]() { // this thread's k of the next slice
+        kk += TK;
+        ci += TK;
+        while (ci >= a.Cin) {
+            ci -= a.Cin;
+            if (++kx == a.kw) kx = 0, ++ky;
+        }
+    };
+    auto step = [&](int cur, int k) {
+        const float4 a0 = *(const float4 *)&As[cur][k][ty * 4];
+        const float4 a1 = *(const float4 *)&As[cur][k][64 + ty * 4];
+        const float4 b0 = *(const float4 *)&Bs[cur][k][tx * 4];
+        const float4 b1 = *(const float4 *)&Bs[cur][k][TN / 2 + tx * 4];
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+            for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
+    };
+
+    loadA();
+    loadB(0);
+    storeAB(0);
+    __syncthreads();
+    for (int s = 0; s < nsl; ++s) {
+        const int cur = s & 1;
+        if (s + 1 < nsl) {
+            advance();
+            loadA();
+            loadB(s + 1);
+        }
+        if (s < nfull) {
+#pragma unroll
+            for (int k = 0; k < TK; ++k) step(cur, k);
+        } else {
+            for (int k = 0; k < K - nfull * TK; ++k) step(cur, k);
+        }
+        if (s + 1 < nsl) storeAB(cur ^ 1);
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const int ox = ox0 + ((i < 4) ? ty * 4 + i : 64 + ty * 4 + (i - 4));
+        if (ox >= Wo) continue;
+        float *dst = a.out16 ? nullptr : a.out + (long)oy * a.out_row + (long)ox * a.out_pix;
+        __nv_bfloat16 *dst16 = a.out16 ? (__nv_bfloat16 *)a.out16 + ((long)oy * Wo + ox) * a.out_cs : nullptr;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int co = (j < 4) ? tx * 4 + j : TN / 2 + tx * 4 + (j - 4);
+            if (co < a.Cout) {
+                float v = acc[i][j];
+                if (a.bias) v = __fadd_rn(v, a.bias[co]);
+                v = act_fn(v, a.act);
+                if (dst16) dst16[co] = __float2bfloat16_rn(v);
+                else dst[(long)co * a.out_ch] = v;
+            }
+        }
+    }
+}
+
 // First layers (Cin <= 5): one thread per output pixel holds all COUT
 // accumulators; its 3x3xCin patch sits in registers and the weights are read
 // from shared memory as broadcast float4.  Same per-output order as above:
@@ -248,7 +390,10 @@ int conv_simt(const ConvArgs &args, cudaStream_t st)
     dim3 grid(ceil_div(Wo, BM), Ho, a.n_img);
     {
         CNNCRF_PROF("conv_simt", st);
-        k_conv_simt<<<grid, 256, 0, st>>>(a, Ho, Wo, K);
+        if (a.Cout <= 32) k_conv_nt<32, 8><<<grid, 64, 0, st>>>(a, Ho, Wo, K);
+        else if (a.Cout <= 64) k_conv_nt<64, 8><<<grid, 128, 0, st>>>(a, Ho, Wo, K);
+        else if (a.Cout <= 112) k_conv_nt<112, 14><<<grid, 224, 0, st>>>(a, Ho, Wo, K);
+        else k_conv_simt<<<grid, 256, 0, st>>>(a, Ho, Wo, K);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
