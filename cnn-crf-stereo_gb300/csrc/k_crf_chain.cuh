@@ -267,9 +267,13 @@ template <int P> __device__ __forceinline__ void lane_read(const float *slot, in
     }
 }
 
-// ring slots per step: theta, phi and the forward message (H pass); phi and the message (V pass, no theta)
-__host__ __device__ constexpr int ring_slots(bool hpass) { return hpass ? 3 : 2; }
-__host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass) { return RING * ring_slots(hpass) * 32 * P; }
+// floats of the ring per step: theta, phi and the forward message (H pass); phi and the message (V pass, no theta)
+// (the theta slot holds 16-bit codes when t16: half the floats)
+__host__ __device__ constexpr int theta_floats(int P, bool hpass, bool t16) { return hpass ? (t16 ? 16 * P : 32 * P) : 0; }
+__host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass, bool t16 = false)
+{
+    return RING * (theta_floats(P, hpass, t16) + 64 * P);
+}
 
 // One pass over the chains of one direction; one warp per chain.
 //   HPASS: chain = row y over x (weights wx[y][x] on edge x -> x+1), unary
@@ -303,15 +307,15 @@ __global__ void __launch_bounds__(128)
     wgt += wps * pair;
     if (labels) labels += (long)W * H * pair;
     cmin_out += (long)nch * pair;
-    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P, RING, HPASS));
+    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P, RING, HPASS, T16));
     float *ring = wsm + nmax;
     auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
     for (int i = lane; i < n; i += 32) wsm[i] = wgt[pix(i)];
     __syncwarp();
     const bool use_phi = !(HPASS && first);
     // slot a of step i: 0 theta (H pass only), 1 phi, 2 the forward message
-    constexpr int NS = ring_slots(HPASS);
-    auto slot = [&](int i, int a) { return ring + ((i % RING) * NS + (HPASS ? a : a - 1)) * (32 * P); };
+    constexpr int TF = theta_floats(P, HPASS, T16), SF = TF + 64 * P;
+    auto slot = [&](int i, int a) { return ring + (i % RING) * SF + (a == 0 ? 0 : TF + (a - 1) * 32 * P); };
 
     // ---- forward: messages into each node, stored for the backward sweep
     auto issue_f = [&](int i) {
@@ -413,13 +417,13 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
 {
     const int n = hpass ? a.W : a.H;
     const int nmax = (n + 3) & ~3;
-    const size_t sm = sizeof(float) * wpb * (size_t)(nmax + ring_floats(P, RING, hpass));
-    if (sm > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
     const bool full = a.D == 32 * P;
-    auto kern = hpass ? (full ? k_crf_chain<P, DELTA, true, true, RING> : k_crf_chain<P, DELTA, true, false, RING>)
-                      : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
     // the H pass on the 16-bit unary where each lane's labels are an even count (aligned copies)
     const bool t16 = hpass && full && a.thetaq != nullptr && P % 2 == 0;
+    const size_t sm = sizeof(float) * wpb * (size_t)(nmax + ring_floats(P, RING, hpass, t16));
+    if (sm > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
+    auto kern = hpass ? (full ? k_crf_chain<P, DELTA, true, true, RING> : k_crf_chain<P, DELTA, true, false, RING>)
+                      : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
     if constexpr (P % 2 == 0)
         if (t16) kern = k_crf_chain<P, DELTA, true, true, RING, true>;
     CNNCRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
