@@ -352,15 +352,35 @@ __global__ void k_head2(const float *__restrict__ in, int npx, int Cin, const fl
     out[(long)npx + p] = fabsf(a1);
 }
 
-__global__ void k_l2norm(float *__restrict__ f, long npx, int C)
+// Per pixel x / |x|, |x| = sqrt of the channel sum of squares in ascending c
+// (one fmaf per term).  A CTA stages L2N pixels' channels in shared memory
+// (row stride C + 1, odd: the per-pixel reads hit distinct banks) so the
+// global reads and writes are contiguous, and one thread per pixel keeps the
+// sequential sum.
+constexpr int L2N = 64;
+__global__ void __launch_bounds__(L2N) k_l2norm(float *__restrict__ f, long npx, int C)
 {
-    long p = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= npx) return;
-    float *x = f + p * C;
-    float s = 0.0f;
-    for (int c = 0; c < C; ++c) s = __fmaf_rn(x[c], x[c], s);
-    float n = __fsqrt_rn(s);
-    for (int c = 0; c < C; ++c) x[c] = n > 0.0f ? __fdiv_rn(x[c], n) : 0.0f;
+    extern __shared__ float xs[]; // [L2N][C + 1]
+    const long p0 = (long)blockIdx.x * L2N;
+    const int n = (int)min((long)L2N, npx - p0), CS = C + 1;
+    float *g = f + p0 * C;
+    for (int i = threadIdx.x; i < n * C; i += L2N) {
+        const int q = i / C;
+        xs[q * CS + (i - q * C)] = g[i];
+    }
+    __syncthreads();
+    if (threadIdx.x < n) {
+        float *x = xs + threadIdx.x * CS;
+        float s = 0.0f;
+        for (int c = 0; c < C; ++c) s = __fmaf_rn(x[c], x[c], s);
+        const float nr = __fsqrt_rn(s);
+        for (int c = 0; c < C; ++c) x[c] = nr > 0.0f ? __fdiv_rn(x[c], nr) : 0.0f;
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n * C; i += L2N) {
+        const int q = i / C;
+        g[i] = xs[q * CS + (i - q * C)];
+    }
 }
 
 } // namespace
@@ -413,7 +433,9 @@ int l2norm(float *f, long npx, int C, cudaStream_t st)
 {
     {
         CNNCRF_PROF("l2norm", st);
-        k_l2norm<<<ceil_div(npx, 256), 256, 0, st>>>(f, npx, C);
+        const size_t sm = sizeof(float) * L2N * (size_t)(C + 1);
+        if (sm > 48 * 1024) return fail(CNNCRF_EINVAL, "l2norm: %d channels", C);
+        k_l2norm<<<ceil_div(npx, L2N), L2N, sm, st>>>(f, npx, C);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
