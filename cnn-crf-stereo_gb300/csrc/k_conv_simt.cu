@@ -131,6 +131,20 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
     }
 }
 
+// Packed FP32: two IEEE fmas, each rounded once (fma.rn.f32x2), on a pair of
+// floats held in one 64-bit register -- the same values as two __fmaf_rn at
+// half the instruction issue.
+__device__ __forceinline__ unsigned long long pack2(float lo, float hi)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ void fma2(unsigned long long &acc, unsigned long long a, unsigned long long b)
+{
+    asm("fma.rn.f32x2 %0, %1, %2, %0;" : "+l"(acc) : "l"(a), "l"(b));
+}
+
 // The same convolution with the channel tile cut to the layer's width (TN =
 // 32, 64 or 112 output channels, for Cout <= TN) and the index arithmetic
 // taken out of the k loop.  2 TN threads, each an 8 x 8 register tile (8
@@ -141,7 +155,7 @@ __global__ void __launch_bounds__(256) k_conv_simt(ConvArgs a, int Ho, int Wo, i
 // ascending k with one fmaf each, then + bias and the activation, as in
 // k_conv_simt: the same bits.
 template <int TN, int TK>
-__global__ void __launch_bounds__(2 * TN) k_conv_nt(ConvArgs a, int Ho, int Wo, int K)
+__global__ void __launch_bounds__(2 * TN, 2) k_conv_nt(ConvArgs a, int Ho, int Wo, int K)
 {
     constexpr int NT = 2 * TN;      // threads
     constexpr int PA = BM * TK / NT; // pixels a thread loads per slice
@@ -181,11 +195,12 @@ __global__ void __launch_bounds__(2 * TN) k_conv_nt(ConvArgs a, int Ho, int Wo, 
     }
     const int nfull = K / TK, nsl = (K + TK - 1) / TK;
 
-    float acc[8][8];
+    // accumulators of 8 pixels x 4 channel pairs (channels 2m, 2m+1 of the thread's 8)
+    unsigned long long acc2[8][4];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+        for (int m = 0; m < 4; ++m) acc2[i][m] = 0ull;
 
     float ra[PA];
     float4 rb[BR];
@@ -222,14 +237,16 @@ __global__ void __launch_bounds__(2 * TN) k_conv_nt(ConvArgs a, int Ho, int Wo, 
     auto step = [&](int cur, int k) {
         const float4 a0 = *(const float4 *)&As[cur][k][ty * 4];
         const float4 a1 = *(const float4 *)&As[cur][k][64 + ty * 4];
-        const float4 b0 = *(const float4 *)&Bs[cur][k][tx * 4];
-        const float4 b1 = *(const float4 *)&Bs[cur][k][TN / 2 + tx * 4];
+        const ulonglong2 b0 = *(const ulonglong2 *)&Bs[cur][k][tx * 4];
+        const ulonglong2 b1 = *(const ulonglong2 *)&Bs[cur][k][TN / 2 + tx * 4];
         const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+        const unsigned long long bp[4] = {b0.x, b0.y, b1.x, b1.y};
 #pragma unroll
-        for (int i = 0; i < 8; ++i)
+        for (int i = 0; i < 8; ++i) {
+            const unsigned long long ap = pack2(av[i], av[i]);
 #pragma unroll
-            for (int j = 0; j < 8; ++j) acc[i][j] = __fmaf_rn(av[i], bv[j], acc[i][j]);
+            for (int m = 0; m < 4; ++m) fma2(acc2[i][m], ap, bp[m]);
+        }
     };
 
     loadA();
@@ -259,11 +276,14 @@ __global__ void __launch_bounds__(2 * TN) k_conv_nt(ConvArgs a, int Ho, int Wo, 
         if (ox >= Wo) continue;
         float *dst = a.out16 ? nullptr : a.out + (long)oy * a.out_row + (long)ox * a.out_pix;
         __nv_bfloat16 *dst16 = a.out16 ? (__nv_bfloat16 *)a.out16 + ((long)oy * Wo + ox) * a.out_cs : nullptr;
+        float accf[8];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) asm("mov.b64 {%0, %1}, %2;" : "=f"(accf[2 * m]), "=f"(accf[2 * m + 1]) : "l"(acc2[i][m]));
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const int co = (j < 4) ? tx * 4 + j : TN / 2 + tx * 4 + (j - 4);
             if (co < a.Cout) {
-                float v = acc[i][j];
+                float v = accf[j];
                 if (a.bias) v = __fadd_rn(v, a.bias[co]);
                 v = act_fn(v, a.act);
                 if (dst16) dst16[co] = __float2bfloat16_rn(v);
