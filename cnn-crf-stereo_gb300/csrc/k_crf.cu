@@ -35,8 +35,8 @@ int crf_pass_ring8(const CrfPassArgs &a, bool hpass, int delta, int wpb, cudaStr
 
 size_t crf_pass_smem(int P, int RING, int W, int H, bool hpass, int wpb)
 {
-    const int n = hpass ? W : H;
-    return sizeof(float) * wpb * (size_t)(((n + 3) & ~3) + ring_floats(P, RING, hpass));
+    (void)W, (void)H; // the chains' weights stream through registers: no per-node shared memory
+    return sizeof(float) * wpb * (size_t)ring_floats(P, RING, hpass);
 }
 
 namespace {
@@ -139,7 +139,7 @@ int run_passes(const float *cost, const float *wx, const float *wy, long wps, in
     if (delta < 1 || delta > 4) return fail(CNNCRF_EUNSUPPORTED, "crf: delta %d outside 1..4", delta);
     const CrfTile t = effective_tile(W, H, D, np, delta);
     if (!fits(D, W, H, true, t.ring_h, t.wpb_h) || !fits(D, W, H, false, t.ring_v, t.wpb_v))
-        return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
+        return fail(CNNCRF_EUNSUPPORTED, "crf: the chain ring of this tile exceeds shared memory");
     double *cH = (double *)(ws + l.ch), *cV = (double *)(ws + l.cv), *lb = (double *)(ws + l.lb);
     CrfPassArgs a = pass_args(cost, wps, W, H, D, np, rp, ws, l, costq, q);
     for (int it = 0; it < iters; ++it) {

@@ -288,7 +288,7 @@ template <int P, int DELTA, bool HPASS, bool FULL, int RING, bool T16 = false>
 __global__ void __launch_bounds__(128)
     k_crf_chain(const float *__restrict__ theta, const uint16_t *__restrict__ thetaq, float qscale, float qoffset,
                 float *__restrict__ phi, const float *__restrict__ wgt,
-                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int store_phi, int nmax,
+                float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int store_phi,
                 int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
 {
     extern __shared__ float4 smem4[];
@@ -307,11 +307,16 @@ __global__ void __launch_bounds__(128)
     wgt += wps * pair;
     if (labels) labels += (long)W * H * pair;
     cmin_out += (long)nch * pair;
-    float *wsm = (float *)smem4 + (size_t)wib * (nmax + ring_floats(P, RING, HPASS, T16));
-    float *ring = wsm + nmax;
+    float *ring = (float *)smem4 + (size_t)wib * ring_floats(P, RING, HPASS, T16);
     auto pix = [&](int i) -> long { return HPASS ? (long)chain * W + i : (long)i * W + chain; };
-    for (int i = lane; i < n; i += 32) wsm[i] = wgt[pix(i)];
-    __syncwarp();
+    // Edge weights in registers: lane l holds the weight of edge 32 b + l of
+    // the sweep's current block b (wc) and of the block it reaches next (wn),
+    // one load per lane and block; a step's weight is a shuffle that depends
+    // on no chain state, so shared memory does not grow with the chain.
+    auto wload = [&](int b) -> float {
+        const int e = 32 * b + lane;
+        return (b >= 0 && e < n) ? __ldg(wgt + pix(e)) : 0.0f;
+    };
     const bool use_phi = !(HPASS && first);
     // slot a of step i: 0 theta (H pass only), 1 phi, 2 the forward message
     constexpr int TF = theta_floats(P, HPASS, T16), SF = TF + 64 * P;
@@ -331,7 +336,14 @@ __global__ void __launch_bounds__(128)
     for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
     for (int i = 0; i < RING - 1; ++i) issue_f(i);
     double acc = 0.0, cmin = 0.0;
-    for (int i = 0; i < n; ++i) {
+    float wn = wload(0);
+    // blocks of 32 nodes: the block's weights in wc, the next block's loading into wn
+    for (int b = 0, i = 0; i < n; ++b) {
+    const float wc = wn;
+    wn = wload(b + 1);
+    const int iend = min(n, i + 32);
+#pragma unroll 1
+    for (; i < iend; ++i) {
         issue_f(i + RING - 1);
         cp_wait<RING - 1>();
         if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset, th);
@@ -348,7 +360,8 @@ __global__ void __launch_bounds__(128)
             if (i < n - 1) acc += (double)g;
             else cmin = acc + (double)g;
         }
-        if (i < n - 1) minconv<P, DELTA, FULL>(v, g, wsm[i], rp, lane, D, L);
+        if (i < n - 1) minconv<P, DELTA, FULL>(v, g, __shfl_sync(0xffffffffu, wc, i & 31), rp, lane, D, L);
+    }
     }
     cp_wait<0>();
 
@@ -367,8 +380,16 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int r = 0; r < P; ++r) R[r] = 0.0f;
     for (int j = 0; j < RING - 1; ++j) issue_b(j);
-    for (int j = 0; j < n; ++j) {
-        const int i = n - 1 - j;
+    // the sweep reads edges n-2 down to 0, in blocks of 32 edges from the top;
+    // node 0 (no edge below it) comes last, in a block of its own
+    wn = wload((n - 2) >> 5);
+    for (int eb = (n - 2) >> 5, j = 0; j < n; --eb) {
+    const float wc = wn;
+    wn = wload(eb - 1);
+    const int jend = eb >= 0 ? n - 1 - 32 * eb : n; // nodes i = e + 1 for the block's edges e
+#pragma unroll 1
+    for (; j < jend; ++j) {
+        const int i = n - 1 - j, e = i - 1; // edge e -> i
         issue_b(j + RING - 1);
         cp_wait<RING - 1>();
         if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset, th);
@@ -405,8 +426,9 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
             for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
             const float g = warp_min<P>(v);
-            minconv<P, DELTA, FULL>(v, g, wsm[i - 1], rp, lane, D, R);
+            minconv<P, DELTA, FULL>(v, g, __shfl_sync(0xffffffffu, wc, e & 31), rp, lane, D, R);
         }
+    }
     }
     cp_wait<0>();
     if (lane == 0) cmin_out[chain] = cmin;
@@ -415,13 +437,11 @@ __global__ void __launch_bounds__(128)
 template <int P, int DELTA, int RING>
 int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
 {
-    const int n = hpass ? a.W : a.H;
-    const int nmax = (n + 3) & ~3;
     const bool full = a.D == 32 * P;
     // the H pass on the 16-bit unary where each lane's labels are an even count (aligned copies)
     const bool t16 = hpass && full && a.thetaq != nullptr && P % 2 == 0;
-    const size_t sm = sizeof(float) * wpb * (size_t)(nmax + ring_floats(P, RING, hpass, t16));
-    if (sm > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: chains longer than the shared-memory weight cache");
+    const size_t sm = sizeof(float) * wpb * (size_t)ring_floats(P, RING, hpass, t16);
+    if (sm > 227 * 1024) return fail(CNNCRF_EUNSUPPORTED, "crf: %zu bytes of ring per CTA", sm);
     auto kern = hpass ? (full ? k_crf_chain<P, DELTA, true, true, RING> : k_crf_chain<P, DELTA, true, false, RING>)
                       : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
     if constexpr (P % 2 == 0)
@@ -432,7 +452,7 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
         CNNCRF_PROF(hpass ? "crf_h" : "crf_v", st);
         kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.thetaq, a.qscale, a.qoffset, a.phi, a.wgt,
                                                            a.lbuf, a.W, a.H, a.D, a.rp,
-                                                           a.first, a.store_phi, nmax, a.labels, a.cmin, a.np,
+                                                           a.first, a.store_phi, a.labels, a.cmin, a.np,
                                                            a.wps);
     }
     CNNCRF_CHECK_LAUNCH();

@@ -1,7 +1,7 @@
 """GPU tests of the CRF tiles (prefetch depth and chains per CTA of the H and
 V passes): every tile gives the oracle's labels and bound bit for bit, the
-autotuners enter valid tiles and change no result, and a tuned tile that does
-not fit a long chain's shared memory falls back to the default."""
+autotuners enter valid tiles and change no result, and chains far longer than
+any image row run at every tile."""
 import numpy as np
 import pytest
 
@@ -96,19 +96,22 @@ def test_batch_autotune_changes_no_result(cuda):
         tuning.clear()
 
 
-def test_tile_too_large_for_a_long_chain_falls_back(cuda):
-    """An 8400-pixel row with 256 labels: 4 chains per CTA with the 8-step ring
-    need more than 227 KB of shared memory, so the H pass runs the default."""
+def test_long_chains_at_every_tile(cuda, oracle):
+    """A 60000-pixel row: the chains' edge weights stream through registers,
+    so a chain's shared memory does not grow with its length and every tile
+    runs it, with the oracle's labels and bound."""
     torch = cuda
     from cnncrf import tuning
     from cnncrf.api import crf_solve
-    D, H, W = 256, 2, 8400
-    cost, wx, wy = (dev(a, torch) for a in problem(D, H, W, seed=5))
-    tuning.clear()
+    D, H, W = 64, 2, 60000
+    cost, wx, wy = problem(D, H, W, seed=5)
+    olab, olb, _, _ = oracle.crf(cost, wx, wy, 0.5, 1.5, 2, 2, shape=1)
     try:
-        lab0, lb0 = crf_solve(cost, wx, wy, L1=0.5, L2=1.5, delta=2, total_it=2, shape=1)
-        set_tile(tuning, W, H, D, 1, 2, (8, 4, 4, 4))
-        lab1, lb1 = crf_solve(cost, wx, wy, L1=0.5, L2=1.5, delta=2, total_it=2, shape=1)
-        assert torch.equal(lab0, lab1) and lb0 == lb1
+        for t in TILES:
+            set_tile(tuning, W, H, D, 1, 2, t)
+            lab, lb = crf_solve(dev(cost, torch), dev(wx, torch), dev(wy, torch), L1=0.5, L2=1.5, delta=2,
+                                total_it=2, shape=1)
+            assert np.array_equal(lab.cpu().numpy(), olab), t
+            assert lb == olb, t
     finally:
         tuning.clear()
