@@ -313,26 +313,29 @@ __global__ void __launch_bounds__(128) k_conv_first(ConvArgs a, int Ho, int Wo, 
     a.in += (long)blockIdx.z * a.in_img; // image of the batch
     if (a.out16) a.out16 = (char *)a.out16 + (long)blockIdx.z * a.out_img * 2;
     else a.out += (long)blockIdx.z * a.out_img;
-    float acc[CP];
+    // channel pairs (2m, 2m+1), one packed fma per pair and term
+    unsigned long long acc2[CP / 2];
 #pragma unroll
-    for (int co = 0; co < CP; ++co) acc[co] = 0.0f;
+    for (int m = 0; m < CP / 2; ++m) acc2[m] = 0ull;
     for (int ky = 0; ky < a.kh; ++ky)
         for (int kx = 0; kx < a.kw; ++kx) {
             const float *src = a.in + (long)(oy + ky) * a.in_row + (long)(ox + kx) * a.in_pix;
             const int kb = (ky * a.kw + kx) * a.Cin;
             for (int ci = 0; ci < a.Cin; ++ci) {
                 const float xv = __ldg(src + ci);
-                const float4 *w = (const float4 *)(wsm + (kb + ci) * CP);
+                const unsigned long long xp = pack2(xv, xv);
+                const ulonglong2 *w = (const ulonglong2 *)(wsm + (kb + ci) * CP);
 #pragma unroll
                 for (int q = 0; q < CP / 4; ++q) {
-                    const float4 wv = w[q];
-                    acc[4 * q + 0] = __fmaf_rn(wv.x, xv, acc[4 * q + 0]);
-                    acc[4 * q + 1] = __fmaf_rn(wv.y, xv, acc[4 * q + 1]);
-                    acc[4 * q + 2] = __fmaf_rn(wv.z, xv, acc[4 * q + 2]);
-                    acc[4 * q + 3] = __fmaf_rn(wv.w, xv, acc[4 * q + 3]);
+                    const ulonglong2 wv = w[q];
+                    fma2(acc2[2 * q], xp, wv.x);
+                    fma2(acc2[2 * q + 1], xp, wv.y);
                 }
             }
         }
+    float acc[CP];
+#pragma unroll
+    for (int m = 0; m < CP / 2; ++m) asm("mov.b64 {%0, %1}, %2;" : "=f"(acc[2 * m]), "=f"(acc[2 * m + 1]) : "l"(acc2[m]));
 #pragma unroll
     for (int co = 0; co < CP; ++co) {
         float v = acc[co];

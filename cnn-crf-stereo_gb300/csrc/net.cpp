@@ -217,11 +217,14 @@ int cnncrf_net::pairwise_fp32()
     return k::conv_head2(pwb.as<float>(), H * W, pw[2].cin, pw[2].wt.as<float>(), pwout, st, n);
 }
 
-int cnncrf_net::predict_fp32(const float *left, const float *right)
+int cnncrf_net::predict_fp32(const float *left, const float *right, bool reuse_left_features)
 {
     const float *img[2] = {left, right};
     int ic = d.in_channels;
+    const bool reuse = reuse_left_features && left_ok;
+    left_ok = false;
     for (int s = 0; s < 2; ++s) {
+        if (s == 0 && reuse) continue; // feats[0] and norm[0] still hold this input's features
         CNNCRF_TRY(k::normalize(img[s], w, h, ic, norm[s].as<float>(), scratch.get(), st, n));
         const float *cur = norm[s].as<float>();
         int ch = h, cw = w, cc = ic;
@@ -243,6 +246,7 @@ int cnncrf_net::predict_fp32(const float *left, const float *right)
     CNNCRF_TRY(k::correlation(feats[0], feats[1], H, W, d.feat_channels, d_list.as<float>(), D, omin, omax,
                               interp || force_interp, d.unary, vol, st, n, (long)H * W * d.feat_channels));
     if (d.with_pairwise) CNNCRF_TRY(pairwise_fp32());
+    left_ok = true;
     return CNNCRF_OK;
 }
 
@@ -302,9 +306,13 @@ int cnncrf_net::predict(const float *left, const float *right)
         if (!have[i]) return fail(CNNCRF_ESTATE, "parameter arr_%zu not set", i);
     if (!left || !right) return fail(CNNCRF_EINVAL, "predict: null image");
     volq_valid = false;
-    if (d.topology == CNNCRF_TOPO_CONCAT) return predict_concat(left, right);
-    if (d.precision == CNNCRF_BF16) return predict_bf16(left, right);
-    return predict_fp32(left, right);
+    const bool reuse = reuse_left;
+    reuse_left = false;
+    if (d.topology == CNNCRF_TOPO_CONCAT || d.precision == CNNCRF_BF16) {
+        left_ok = false;
+        return d.topology == CNNCRF_TOPO_CONCAT ? predict_concat(left, right) : predict_bf16(left, right);
+    }
+    return predict_fp32(left, right, reuse);
 }
 
 int cnncrf::concat_growth(int layers)

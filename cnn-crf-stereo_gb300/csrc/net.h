@@ -68,7 +68,12 @@ struct cnncrf_net {
     int expected_shape(int i, int64_t s[4], int *nd) const;
     int upload(int slot);
     int predict(const float *left, const float *right);
-    int predict_fp32(const float *left, const float *right);
+    int predict_fp32(const float *left, const float *right, bool reuse_left);
+    // FP32 path: the next predict's left input is the last predict's (same
+    // padded image): keep its left features (and normalised image) instead of
+    // recomputing them.  One-shot; honoured only while left_ok.
+    bool reuse_left = false;
+    bool left_ok = false; // feats[0] / norm[0] are those of the last completed FP32 predict
     int predict_bf16(const float *left, const float *right);
     int pairwise_fp32();
     int set_disparities(float mn, float mx, float step, float *d_out);

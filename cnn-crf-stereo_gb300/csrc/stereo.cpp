@@ -35,6 +35,10 @@ struct cnncrf_stereo {
     std::vector<float> dlist_host;          // host copy of the census disparity list
     int filter_size = 7;                    // stereo/stereo_img.cpp:73
     cnncrf_net_t net = nullptr;
+    // the net's left features are those of img[0] as it is now (an FP32
+    // left-referenced compute_volume since the last image upload): the
+    // refinement's re-match keeps them instead of recomputing the same values
+    bool left_feats = false;
     cnncrf_slackprop_t solver = nullptr;
     double lb = 0.0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -49,6 +53,7 @@ struct cnncrf_stereo {
     }
     void destroy_net()
     {
+        left_feats = false;
         if (net) cnncrf_net_destroy(net);
         net = nullptr;
     }
@@ -135,6 +140,7 @@ int cnncrf_stereo::compute_volume(int lr)
 {
     if (!inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
     volq_ok = false;
+    left_feats = false;
     if (matching == CNNCRF_MATCH_LOAD) return CNNCRF_OK;
     if (matching == CNNCRF_MATCH_CENSUS) return census(lr);
     if (!net) {
@@ -164,6 +170,7 @@ int cnncrf_stereo::compute_volume(int lr)
     }
     const int rc = net->predict(padded[0].as<float>(), padded[1].as<float>());
     volq_ok = rc == CNNCRF_OK && net->volq_valid;
+    left_feats = rc == CNNCRF_OK && lr && net->left_ok;
     net->volq = nullptr;
     return rc;
 }
@@ -311,6 +318,7 @@ int cnncrf_stereo_set_color_images(cnncrf_stereo_t s, const float *h_left, const
     if (!s || !h_left || !h_right) return fail(CNNCRF_EINVAL, "set_color_images: null argument");
     if (!s->inited) return fail(CNNCRF_ESTATE, "setColorImages before initialize");
     size_t b = sizeof(float) * 4 * (size_t)s->W * s->H;
+    s->left_feats = false;
     CNNCRF_CUDA(cudaMemcpyAsync(s->img[0].get(), h_left, b, cudaMemcpyHostToDevice, s->st));
     CNNCRF_CUDA(cudaMemcpyAsync(s->img[1].get(), h_right, b, cudaMemcpyHostToDevice, s->st));
     return CNNCRF_OK;
@@ -321,6 +329,7 @@ int cnncrf_stereo_set_color_images_device(cnncrf_stereo_t s, const float *d_left
     if (!s || !d_left || !d_right) return fail(CNNCRF_EINVAL, "set_color_images_device: null argument");
     if (!s->inited) return fail(CNNCRF_ESTATE, "setColorImages before initialize");
     size_t b = sizeof(float) * 4 * (size_t)s->W * s->H;
+    s->left_feats = false;
     CNNCRF_CUDA(cudaMemcpyAsync(s->img[0].get(), d_left, b, cudaMemcpyDeviceToDevice, s->st));
     CNNCRF_CUDA(cudaMemcpyAsync(s->img[1].get(), d_right, b, cudaMemcpyDeviceToDevice, s->st));
     return CNNCRF_OK;
@@ -432,7 +441,11 @@ int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, floa
         net->force_interp = s->o.refine_interp != 0;
         CNNCRF_TRY(net->set_disparities(mn, hq, hq, s->vol3.as<float>()));
         if (net->D != 3) return fail(CNNCRF_ESHAPE, "refinement volume has %d labels, expected 3", net->D);
-        CNNCRF_TRY(net->predict(s->padded[0].as<float>(), s->warped_pad.as<float>()));
+        // the left input is padded[0] of img[0] as in the matching: its features stay valid
+        net->reuse_left = s->left_feats;
+        const int rc = net->predict(s->padded[0].as<float>(), s->warped_pad.as<float>());
+        s->left_feats = rc == CNNCRF_OK && net->left_ok;
+        CNNCRF_TRY(rc);
         net->force_interp = false;
         CNNCRF_TRY(k::tv_fit(s->vol3.as<float>(), s->qf.as<float>(), W, H, step, lam_c, st));
         CNNCRF_CUDA(cudaMemcpyAsync(s->out0.get(), s->out.get(), n * sizeof(float), cudaMemcpyDeviceToDevice, st));

@@ -292,3 +292,42 @@ def test_stereo_argmax_and_errors(cuda, oracle):
     with pytest.raises(CnnCrfError) as e:
         st.compute_volume()
     assert e.value.status == L.EINVAL
+
+
+def test_refinement_reuses_left_features(cuda, oracle):
+    """The refinement's re-match runs the CNN on (left, warped right); the left
+    input is the matching's padded left image, so its features are kept, not
+    recomputed: each warp launches the convolutions of the right image and the
+    pairwise net only (layers + 2), and the refined disparities still equal the
+    oracle's (which recomputes them).  After a new image upload the first warp
+    recomputes both sides."""
+    from cnncrf import scenes, _lib as L
+    from cnncrf.api import Stereo
+    W, H, layers, warps = 52, 30, 5, 2
+    s = scenes.voronoi_scene(W, H, 16, seed=8, cells=5, off_range=(1, 12), slope=0.05)
+    st = Stereo(precision=L.FP32, unary=L.UNARY_ONE_MINUS_DOT, topology=L.TOPO_ALL3X3, ref_depth_rounding=False,
+                crf_shape=L.RHO_LINEAR)
+    st.initialize(W, H, 0.0, 1.0, 15.0)
+    st.set_matching_function(L.MATCH_COLORCNN_PAIRWISE)
+    st.set_num_layers(layers)
+    st.set_xavier_seed(3)
+
+    def convs_in_refinement():
+        L.profile_reset()
+        L.profile_enable(True)
+        try:
+            st.fuse_thuber_quad_fit(0.8, 1.5, 4, warps)
+            return sum(L.profile_query(k)[0] for k in ("conv_simt", "conv_first"))
+        finally:
+            L.profile_enable(False)
+
+    st.set_color_images(s["left"], s["right"])
+    st.compute_slack_propagation(0.5, 1.5, 3, 3, 20.0, 0.9, 0.8)
+    assert convs_in_refinement() == warps * (layers + 2)
+    cfg = oracle.make_cfg(num_layers=layers, topology=1, unary=1, disp_max=15.0, lam=0.8, L1=0.5, L2=1.5, delta=3,
+                          crf_iters=3, crf_shape=1, warps=warps, ref_iters=4, C=1.5)
+    r = oracle.run_pair(cfg, oracle.xavier_params(cfg, seed=3), s["left"], s["right"])
+    assert np.array_equal(st.get_output(), r["disp"])
+    # new images without a new matching: the first warp recomputes both sides, the next one keeps them
+    st.set_color_images(s["right"], s["left"])
+    assert convs_in_refinement() == (2 * layers + 2) + (warps - 1) * (layers + 2)
