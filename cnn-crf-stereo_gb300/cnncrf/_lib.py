@@ -7,6 +7,8 @@ raises.
 import ctypes as C
 import os
 
+import numpy as np
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcnncrf.so")
 
@@ -189,6 +191,11 @@ PROTOS = {
     "cnncrf_train_backward": ([vp, vp, vp], i32),
     "cnncrf_train_sgd": ([vp, f32, f32], i32),
     "cnncrf_train_step": ([vp, vp, vp, vp, f32, f32, C.POINTER(C.c_double)], i32),
+    "cnncrf_train_save": ([vp, C.c_char_p], i32),
+    "cnncrf_train_load": ([vp, C.c_char_p], i32),
+    "cnncrf_npz_read": ([C.c_char_p, C.c_char_p, C.POINTER(C.c_int64), C.POINTER(i32), vp, C.c_size_t], i32),
+    "cnncrf_npz_write": ([C.c_char_p, i32, C.POINTER(C.c_char_p), C.POINTER(vp), C.POINTER(C.c_int64),
+                          C.POINTER(i32)], i32),
     "cnncrf_kernel_launches": ([C.POINTER(C.c_uint64)], i32),
     "cnncrf_profile_enable": ([i32], i32),
     "cnncrf_profile_reset": ([], i32),
@@ -255,3 +262,32 @@ def selftest_bounded_wait(polls, arrive, stream=None):
     """Run the bounded-wait probe; returns the raw status (OK, or ETIMEOUT when
     the wait on a barrier nothing completes gave up) without raising."""
     return lib().cnncrf_selftest_bounded_wait(int(polls), 1 if arrive else 0, stream)
+
+
+def npz_read(path, key):
+    """Member `key` of an npz archive as a float32 array, through the library's own reader."""
+    s = (C.c_int64 * 4)()
+    nd = C.c_int()
+    call("cnncrf_npz_read", os.fsencode(path), key.encode(), s, C.byref(nd), None, 0)
+    out = np.empty(tuple(s[k] for k in range(nd.value)), np.float32)
+    call("cnncrf_npz_read", os.fsencode(path), key.encode(), s, C.byref(nd), out.ctypes.data_as(C.c_void_p),
+         out.size)
+    return out
+
+
+def npz_write(path, arrays):
+    """Write {key: array} as an uncompressed npz through the library's own writer (float32, C order)."""
+    keys = list(arrays)
+    data = [np.array(arrays[k], np.float32, order="C") for k in keys]  # keeps 0-d arrays 0-d
+    if any(a.ndim > 4 for a in data):
+        raise ValueError("npz_write: at most 4 dimensions")
+    n = len(keys)
+    ks = (C.c_char_p * max(n, 1))(*[k.encode() for k in keys])
+    ps = (C.c_void_p * max(n, 1))(*[a.ctypes.data for a in data])
+    shp = (C.c_int64 * max(4 * n, 1))()
+    nds = (C.c_int * max(n, 1))()
+    for i, a in enumerate(data):
+        nds[i] = a.ndim
+        for j, d in enumerate(a.shape):
+            shp[4 * i + j] = d
+    call("cnncrf_npz_write", os.fsencode(path), n, ks, ps, shp, nds)

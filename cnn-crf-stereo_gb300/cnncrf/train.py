@@ -15,6 +15,7 @@ optimizer:
 The reference ships no training code (its weights were trained elsewhere).
 """
 import ctypes as C
+import os
 
 import numpy as np
 import torch
@@ -74,6 +75,14 @@ class Trainer:
 
     def init_xavier(self, seed=0):
         call("cnncrf_train_init_xavier", self._h, seed)
+
+    def save(self, path):
+        """Checkpoint: weights as arr_i (a parameter file for inference too) and momentum as mom_i."""
+        call("cnncrf_train_save", self._h, os.fsencode(path))
+
+    def load(self, path):
+        """Resume from save()'s file, or start from a plain parameter file (zero momentum)."""
+        call("cnncrf_train_load", self._h, os.fsencode(path))
 
     def set_param(self, i, a):
         """Host array or CUDA tensor of the slot's shape."""

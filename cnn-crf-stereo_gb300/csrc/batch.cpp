@@ -497,6 +497,7 @@ int cnncrf_batch::run(float L1, float L2, float delta, int iterations, float lam
 
 int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iterations, float lambda_reg)
 {
+    CNNCRF_RANGE("batch_run");
     clear_error();
     if (!b) return fail(CNNCRF_EINVAL, "null batch");
     b->h_left = b->h_right = nullptr;
@@ -507,6 +508,7 @@ int cnncrf_batch_run(cnncrf_batch_t b, float L1, float L2, float delta, int iter
 int cnncrf_batch_run_host(cnncrf_batch_t b, const float *const *h_left, const float *const *h_right,
                           float *const *h_out, float L1, float L2, float delta, int iterations, float lambda_reg)
 {
+    CNNCRF_RANGE("batch_run_host");
     clear_error();
     if (!b || !h_left || !h_right) return fail(CNNCRF_EINVAL, "run_host: null argument");
     for (size_t i = 0; i < b->loc.size(); ++i)

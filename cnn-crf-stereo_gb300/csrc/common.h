@@ -84,9 +84,11 @@ class DevBuf {
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }
 
 // Kernel-launch instrumentation.  Every launch site is wrapped in a
-// CNNCRF_PROF scope: it counts the launch and, while timing is enabled
-// (cnncrf_profile_enable), records a CUDA event pair around it on the
-// launching stream, filed under the kernel's name.
+// CNNCRF_PROF scope: it counts the launch, opens an NVTX range named after
+// the kernel in the "cnncrf" domain (a no-op unless a tool such as ncu with
+// --nvtx is attached) and, while timing is enabled (cnncrf_profile_enable),
+// records a CUDA event pair around it on the launching stream, filed under
+// the kernel's name.
 class Prof {
   public:
     Prof(const char *name, cudaStream_t st);
@@ -98,5 +100,14 @@ class Prof {
     cudaEvent_t a_ = nullptr;
 };
 #define CNNCRF_PROF(name, st) ::cnncrf::Prof prof__(name, st)
+
+// An NVTX range around a whole stage of an API call (the volume, the CRF,
+// the refinement, a batch run, a training step), nesting the kernels' ranges.
+class Range {
+  public:
+    explicit Range(const char *name);
+    ~Range();
+};
+#define CNNCRF_RANGE(name) ::cnncrf::Range range__(name)
 
 } // namespace cnncrf

@@ -561,6 +561,7 @@ int cnncrf_net_num_disparities(cnncrf_net_t net, int *num)
 
 int cnncrf_net_predict(cnncrf_net_t net, const float *d_left_rgba, const float *d_right_rgba, float **d_volume)
 {
+    CNNCRF_RANGE("net_predict");
     clear_error();
     if (!net) return fail(CNNCRF_EINVAL, "null net");
     CNNCRF_TRY(net->predict(d_left_rgba, d_right_rgba));

@@ -1,4 +1,5 @@
-// npz.cpp -- .npz (zip of .npy) reader with a small DEFLATE decoder.
+// npz.cpp -- .npz (zip of .npy) reader with a small DEFLATE decoder, and a
+// writer of uncompressed archives (training checkpoints).
 //
 // The zip structures (end-of-central-directory, central directory, local
 // headers, ZIP64 extra field 0x0001) follow PKWARE's APPNOTE.TXT; the .npy
@@ -11,6 +12,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <string>
 
 #include "common.h"
 
@@ -305,4 +307,164 @@ int npz_load(const std::string &path, const std::string &key, NpyArray *out)
     return fail(CNNCRF_EIO, "%s: no array %s", path.c_str(), key.c_str());
 }
 
+namespace {
+
+// CRC-32 of the zip format (reflected polynomial 0xEDB88320, initial and
+// final XOR 0xFFFFFFFF; APPNOTE.TXT 4.4.7), table-driven
+uint32_t crc32_update(uint32_t crc, const uint8_t *p, size_t n)
+{
+    static uint32_t table[256];
+    static bool init = false;
+    if (!init) {
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            table[i] = c;
+        }
+        init = true;
+    }
+    crc = ~crc;
+    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
+    return ~crc;
+}
+
+void put16(std::vector<uint8_t> &b, uint32_t v)
+{
+    b.push_back((uint8_t)v);
+    b.push_back((uint8_t)(v >> 8));
+}
+void put32(std::vector<uint8_t> &b, uint32_t v)
+{
+    put16(b, v & 0xffffu);
+    put16(b, v >> 16);
+}
+
+// .npy format 1.0 header: magic, version, header length, the dict padded
+// with spaces and ended by '\n' so that the data starts 64-byte aligned
+std::vector<uint8_t> npy_header(const std::vector<int64_t> &shape)
+{
+    std::string dict = "{'descr': '<f4', 'fortran_order': False, 'shape': (";
+    for (size_t i = 0; i < shape.size(); ++i) {
+        dict += std::to_string((long long)shape[i]);
+        if (shape.size() == 1 || i + 1 < shape.size()) dict += ",";
+        if (i + 1 < shape.size()) dict += " ";
+    }
+    dict += "), }";
+    size_t total = 10 + dict.size() + 1;
+    dict.append((64 - total % 64) % 64, ' ');
+    dict += '\n';
+    std::vector<uint8_t> h = {0x93, 'N', 'U', 'M', 'P', 'Y', 1, 0};
+    put16(h, (uint32_t)dict.size());
+    h.insert(h.end(), dict.begin(), dict.end());
+    return h;
+}
+
+} // namespace
+
+int npz_save(const std::string &path, const std::vector<NpzMember> &members)
+{
+    if (members.size() > 0xFFFEu) return fail(CNNCRF_EUNSUPPORTED, "npz_save: %zu members", members.size());
+    const std::string tmp = path + ".tmp";
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if (!f) return fail(CNNCRF_EIO, "npz_save: cannot create %s", tmp.c_str());
+    std::vector<uint8_t> cdir;
+    uint64_t off = 0;
+    bool ok = true;
+    for (const NpzMember &m : members) {
+        int64_t n = 1;
+        for (int64_t s : m.shape) {
+            if (s < 0) ok = false;
+            n *= s;
+        }
+        if (!ok || (n > 0 && !m.data)) {
+            fclose(f);
+            remove(tmp.c_str());
+            return fail(CNNCRF_EINVAL, "npz_save: member %s has a bad shape or no data", m.key.c_str());
+        }
+        const std::string name = m.key + ".npy";
+        const std::vector<uint8_t> hdr = npy_header(m.shape);
+        const uint64_t size = hdr.size() + (uint64_t)n * 4;
+        if (off + 30 + name.size() + size >= 0xFFFFFFFFull) {
+            fclose(f);
+            remove(tmp.c_str());
+            return fail(CNNCRF_EUNSUPPORTED, "npz_save: archive above 4 GiB at member %s", m.key.c_str());
+        }
+        uint32_t crc = crc32_update(0, hdr.data(), hdr.size());
+        crc = crc32_update(crc, (const uint8_t *)m.data, (size_t)n * 4);
+        // local file header (APPNOTE 4.3.7): version 2.0, no flags, STORED, 1980-01-01 00:00
+        std::vector<uint8_t> lh;
+        put32(lh, 0x04034b50u);
+        put16(lh, 20), put16(lh, 0), put16(lh, 0), put16(lh, 0), put16(lh, 0x21);
+        put32(lh, crc), put32(lh, (uint32_t)size), put32(lh, (uint32_t)size);
+        put16(lh, (uint32_t)name.size()), put16(lh, 0);
+        lh.insert(lh.end(), name.begin(), name.end());
+        ok = fwrite(lh.data(), 1, lh.size(), f) == lh.size() && fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size() &&
+             (n == 0 || fwrite(m.data, 4, (size_t)n, f) == (size_t)n);
+        if (!ok) break;
+        // its central directory entry (APPNOTE 4.3.12)
+        put32(cdir, 0x02014b50u);
+        put16(cdir, 20), put16(cdir, 20), put16(cdir, 0), put16(cdir, 0), put16(cdir, 0), put16(cdir, 0x21);
+        put32(cdir, crc), put32(cdir, (uint32_t)size), put32(cdir, (uint32_t)size);
+        put16(cdir, (uint32_t)name.size()), put16(cdir, 0), put16(cdir, 0), put16(cdir, 0), put16(cdir, 0);
+        put32(cdir, 0), put32(cdir, (uint32_t)off);
+        cdir.insert(cdir.end(), name.begin(), name.end());
+        off += lh.size() + size;
+    }
+    if (ok) {
+        // end of central directory record (APPNOTE 4.3.16)
+        std::vector<uint8_t> end;
+        put32(end, 0x06054b50u);
+        put16(end, 0), put16(end, 0), put16(end, (uint32_t)members.size()), put16(end, (uint32_t)members.size());
+        put32(end, (uint32_t)cdir.size()), put32(end, (uint32_t)off), put16(end, 0);
+        ok = off + cdir.size() < 0xFFFFFFFFull && fwrite(cdir.data(), 1, cdir.size(), f) == cdir.size() &&
+             fwrite(end.data(), 1, end.size(), f) == end.size();
+    }
+    ok = (fclose(f) == 0) && ok;
+    if (!ok || rename(tmp.c_str(), path.c_str()) != 0) {
+        remove(tmp.c_str());
+        return fail(CNNCRF_EIO, "npz_save: cannot write %s", path.c_str());
+    }
+    return CNNCRF_OK;
+}
+
 } // namespace cnncrf
+
+extern "C" {
+
+int cnncrf_npz_read(const char *npz_path, const char *key, int64_t shape[4], int *ndim, float *h_data,
+                    size_t capacity)
+{
+    using namespace cnncrf;
+    clear_error();
+    if (!npz_path || !key || !shape || !ndim) return fail(CNNCRF_EINVAL, "null argument");
+    NpyArray a;
+    CNNCRF_TRY(npz_load(npz_path, key, &a));
+    if (a.shape.size() > 4) return fail(CNNCRF_ESHAPE, "npz_read: %s has %zu dimensions", key, a.shape.size());
+    *ndim = (int)a.shape.size();
+    for (size_t i = 0; i < a.shape.size(); ++i) shape[i] = a.shape[i];
+    if (h_data) {
+        if (capacity < a.data.size())
+            return fail(CNNCRF_ESHAPE, "npz_read: %s has %zu values, the buffer %zu", key, a.data.size(), capacity);
+        std::memcpy(h_data, a.data.data(), a.data.size() * sizeof(float));
+    }
+    return CNNCRF_OK;
+}
+
+int cnncrf_npz_write(const char *npz_path, int count, const char *const *keys, const float *const *h_data,
+                     const int64_t *shapes, const int *ndims)
+{
+    using namespace cnncrf;
+    clear_error();
+    if (!npz_path || count < 0 || (count > 0 && (!keys || !h_data || !shapes || !ndims)))
+        return fail(CNNCRF_EINVAL, "null argument");
+    std::vector<NpzMember> m((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        if (!keys[i] || ndims[i] < 0 || ndims[i] > 4) return fail(CNNCRF_EINVAL, "npz_write: member %d", i);
+        m[i].key = keys[i];
+        m[i].data = h_data[i];
+        m[i].shape.assign(shapes + 4 * i, shapes + 4 * i + ndims[i]);
+    }
+    return npz_save(npz_path, m);
+}
+
+} // extern "C"

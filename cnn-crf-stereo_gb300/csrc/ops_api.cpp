@@ -147,6 +147,7 @@ int cnncrf_crf_solve(const float *d_cost, const float *d_wx, const float *d_wy, 
                      const cnncrf_crf_options *opt, int32_t *d_labels, double *lower_bound, void *d_workspace,
                      size_t workspace_bytes, cnncrf_stream_t stream)
 {
+    CNNCRF_RANGE("crf_solve");
     clear_error();
     if (!opt) return fail(CNNCRF_EINVAL, "crf: null options");
     k::CrfParams p;

@@ -1,7 +1,11 @@
-// prof.cpp -- launch counter and optional per-kernel CUDA-event timing
-// behind cnncrf_kernel_launches / cnncrf_profile_* (instrumentation; no
-// counterpart in the reference, whose only timer was iu::IuCudaTimer around
-// whole stages, stereo/stereonet.cpp:258-315).
+// prof.cpp -- launch counter, NVTX ranges and optional per-kernel CUDA-event
+// timing behind cnncrf_kernel_launches / cnncrf_profile_* (instrumentation;
+// no counterpart in the reference, whose only timer was iu::IuCudaTimer
+// around whole stages, stereo/stereonet.cpp:258-315).  NVTX is the CUDA
+// toolkit's header-only NVTX 3: without an attached tool each range is one
+// check of an unset function pointer.
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <map>
 #include <mutex>
@@ -22,6 +26,22 @@ struct Rec {
 std::map<std::string, std::vector<Rec>> g_recs;
 std::vector<cudaEvent_t> g_pool;
 
+nvtxDomainHandle_t domain()
+{
+    static nvtxDomainHandle_t d = nvtxDomainCreateA("cnncrf");
+    return d;
+}
+
+void range_push(const char *name)
+{
+    nvtxEventAttributes_t a = {};
+    a.version = NVTX_VERSION;
+    a.size = NVTX_EVENT_ATTRIB_STRUCT_SIZE;
+    a.messageType = NVTX_MESSAGE_TYPE_ASCII;
+    a.message.ascii = name;
+    nvtxDomainRangePushEx(domain(), &a);
+}
+
 cudaEvent_t get_event()
 {
     if (!g_pool.empty()) {
@@ -35,8 +55,12 @@ cudaEvent_t get_event()
 }
 } // namespace
 
+Range::Range(const char *name) { range_push(name); }
+Range::~Range() { nvtxDomainRangePop(domain()); }
+
 Prof::Prof(const char *name, cudaStream_t st) : name_(name), st_(st)
 {
+    range_push(name);
     if (g_enabled.load(std::memory_order_relaxed)) {
         std::lock_guard<std::mutex> lk(g_mu);
         a_ = get_event();
@@ -46,6 +70,7 @@ Prof::Prof(const char *name, cudaStream_t st) : name_(name), st_(st)
 
 Prof::~Prof()
 {
+    nvtxDomainRangePop(domain());
     g_launches.fetch_add(1, std::memory_order_relaxed);
     if (a_) {
         std::lock_guard<std::mutex> lk(g_mu);

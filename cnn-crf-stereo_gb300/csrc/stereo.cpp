@@ -337,6 +337,7 @@ int cnncrf_stereo_set_color_images_device(cnncrf_stereo_t s, const float *d_left
 
 int cnncrf_stereo_compute_volume(cnncrf_stereo_t s, int lr)
 {
+    CNNCRF_RANGE("stereo_compute_volume");
     clear_error();
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->inited) return fail(CNNCRF_ESTATE, "computeVolume before initialize");
@@ -348,6 +349,7 @@ int cnncrf_stereo_compute_volume(cnncrf_stereo_t s, int lr)
 int cnncrf_stereo_compute_slack_propagation(cnncrf_stereo_t s, float C1, float C2, float delta, int iterations,
                                             float alpha, float beta, float lambda_reg, int lr)
 {
+    CNNCRF_RANGE("stereo_compute_slack_propagation");
     clear_error();
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->inited) return fail(CNNCRF_ESTATE, "computeSlackPropagation before initialize");
@@ -399,6 +401,7 @@ int cnncrf_stereo_compute_weights(cnncrf_stereo_t s, float alpha, float beta, fl
 
 int cnncrf_stereo_fuse_quad_fit_direct(cnncrf_stereo_t s)
 {
+    CNNCRF_RANGE("stereo_fuse_quad_fit_direct");
     clear_error();
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->solver) return fail(CNNCRF_ESTATE, "fuseQuadFitDirect needs a computeSlackPropagation first");
@@ -409,6 +412,7 @@ int cnncrf_stereo_fuse_quad_fit_direct(cnncrf_stereo_t s)
 
 int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr)
 {
+    CNNCRF_RANGE("stereo_compute_argmax");
     clear_error();
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->inited) return fail(CNNCRF_ESTATE, "computeArgMax before initialize");
@@ -423,6 +427,7 @@ int cnncrf_stereo_compute_argmax(cnncrf_stereo_t s, int lr)
 
 int cnncrf_stereo_fuse_thuber_quad_fit(cnncrf_stereo_t s, float lambda_reg, float C, int iterations, int warps)
 {
+    CNNCRF_RANGE("stereo_fuse_thuber_quad_fit");
     clear_error();
     if (!s) return fail(CNNCRF_EINVAL, "null stereo");
     if (!s->net || !s->pairwise())

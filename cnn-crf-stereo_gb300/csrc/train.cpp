@@ -14,12 +14,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/cnncrf.h"
 #include "../../include/cnncrf_xavier.h"
 #include "common.h"
 #include "kernels.h"
+#include "npz.h"
 
 using namespace cnncrf;
 
@@ -741,6 +743,7 @@ int cnncrf_train_get_grad(cnncrf_train_t t, int i, float *data, size_t count)
 
 int cnncrf_train_forward(cnncrf_train_t t, const float *d_left, const float *d_right)
 {
+    CNNCRF_RANGE("train_forward");
     clear_error();
     if (!t || !d_left || !d_right) return fail(CNNCRF_EINVAL, "null argument");
     return t->forward(d_left, d_right);
@@ -758,6 +761,7 @@ int cnncrf_train_outputs(cnncrf_train_t t, const float **d_volume, const float *
 
 int cnncrf_train_hinge(cnncrf_train_t t, const int32_t *d_gt, double *h_loss, int32_t *d_labels)
 {
+    CNNCRF_RANGE("train_hinge");
     clear_error();
     if (!t || !d_gt) return fail(CNNCRF_EINVAL, "null argument");
     return t->hinge(d_gt, h_loss, d_labels);
@@ -789,6 +793,7 @@ int cnncrf_train_hinge_grads(cnncrf_train_t t, const float **d_gvol, const float
 
 int cnncrf_train_backward(cnncrf_train_t t, const float *d_gvol, const float *d_gpw)
 {
+    CNNCRF_RANGE("train_backward");
     clear_error();
     if (!t) return fail(CNNCRF_EINVAL, "null train");
     if (!d_gvol && d_gpw) return fail(CNNCRF_EINVAL, "train: pairwise gradient without a volume gradient");
@@ -797,6 +802,7 @@ int cnncrf_train_backward(cnncrf_train_t t, const float *d_gvol, const float *d_
 
 int cnncrf_train_sgd(cnncrf_train_t t, float lr, float momentum)
 {
+    CNNCRF_RANGE("train_sgd");
     clear_error();
     if (!t) return fail(CNNCRF_EINVAL, "null train");
     if (!(lr >= 0.0f) || !(momentum >= 0.0f) || momentum >= 1.0f)
@@ -808,9 +814,68 @@ int cnncrf_train_sgd(cnncrf_train_t t, float lr, float momentum)
     return CNNCRF_OK;
 }
 
+// Checkpoints: the master weights as arr_i (the parameter-file layout) and
+// the momentum as mom_i, both copied through one host staging array.
+int cnncrf_train_save(cnncrf_train_t t, const char *npz_path)
+{
+    clear_error();
+    if (!t || !npz_path) return fail(CNNCRF_EINVAL, "null argument");
+    CNNCRF_CUDA(cudaStreamSynchronize(t->st));
+    std::vector<float> w(t->total), v(t->total);
+    CNNCRF_CUDA(cudaMemcpy(w.data(), t->theta.get(), t->total * sizeof(float), cudaMemcpyDeviceToHost));
+    CNNCRF_CUDA(cudaMemcpy(v.data(), t->vel.get(), t->total * sizeof(float), cudaMemcpyDeviceToHost));
+    const int n = (int)t->off.size();
+    std::vector<NpzMember> m;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int i = 0; i < n; ++i) {
+            int64_t s[4];
+            int nd = 0;
+            CNNCRF_TRY(cnncrf_train_param_shape(t, i, s, &nd));
+            NpzMember a;
+            a.key = (pass == 0 ? "arr_" : "mom_") + std::to_string(i);
+            a.data = (pass == 0 ? w.data() : v.data()) + t->off[i];
+            a.shape.assign(s, s + nd);
+            m.push_back(std::move(a));
+        }
+    return npz_save(npz_path, m);
+}
+
+int cnncrf_train_load(cnncrf_train_t t, const char *npz_path)
+{
+    clear_error();
+    if (!t || !npz_path) return fail(CNNCRF_EINVAL, "null argument");
+    std::vector<float> w(t->total), v(t->total, 0.0f);
+    const int n = (int)t->off.size();
+    for (int i = 0; i < n; ++i) {
+        int64_t s[4];
+        int nd = 0;
+        CNNCRF_TRY(cnncrf_train_param_shape(t, i, s, &nd));
+        NpyArray a;
+        CNNCRF_TRY(npz_load(npz_path, "arr_" + std::to_string(i), &a));
+        if (a.shape != std::vector<int64_t>(s, s + nd) || a.data.size() != t->cnt[i])
+            return fail(CNNCRF_ESHAPE, "train_load: %s: arr_%d does not have the slot's shape", npz_path, i);
+        std::memcpy(w.data() + t->off[i], a.data.data(), t->cnt[i] * sizeof(float));
+        // the momentum is optional: a plain parameter file has none
+        NpyArray mo;
+        if (npz_load(npz_path, "mom_" + std::to_string(i), &mo) == CNNCRF_OK) {
+            if (mo.shape != a.shape)
+                return fail(CNNCRF_ESHAPE, "train_load: %s: mom_%d does not have the slot's shape", npz_path, i);
+            std::memcpy(v.data() + t->off[i], mo.data.data(), t->cnt[i] * sizeof(float));
+        }
+    }
+    clear_error(); // the absent mom_i lookups above are not errors
+    CNNCRF_CUDA(cudaStreamSynchronize(t->st));
+    CNNCRF_CUDA(cudaMemcpy(t->theta.get(), w.data(), t->total * sizeof(float), cudaMemcpyHostToDevice));
+    CNNCRF_CUDA(cudaMemcpy(t->vel.get(), v.data(), t->total * sizeof(float), cudaMemcpyHostToDevice));
+    CNNCRF_TRY(t->refresh());
+    t->forwarded = t->hinged = false;
+    return CNNCRF_OK;
+}
+
 int cnncrf_train_step(cnncrf_train_t t, const float *d_left, const float *d_right, const int32_t *d_gt, float lr,
                       float momentum, double *h_loss)
 {
+    CNNCRF_RANGE("train_step");
     clear_error();
     if (!t || !d_left || !d_right || !d_gt) return fail(CNNCRF_EINVAL, "null argument");
     CNNCRF_TRY(t->forward(d_left, d_right));

@@ -157,6 +157,19 @@ int cnncrf_net_set_all_params(cnncrf_net_t net, const char *npz_path);
  * index = the arr_<index> slot; shape as in the npz (4-D filter or 1-D bias). */
 int cnncrf_net_set_param(cnncrf_net_t net, int index, const float *h_data, const int64_t *shape,
                          int ndim);
+/* Host-side npz access (no device work; the reference's cnpy::npz_load,
+ * stereo/operators/operator.cpp:55-85, and a writer it does not have).
+ * cnncrf_npz_read: member `key` (".npy" appended) of a STORED or DEFLATE
+ * archive of little-endian float32 C-order arrays; fills shape[0..ndim-1]
+ * (ndim <= 4, else ESHAPE) and, when h_data is not NULL, copies the values
+ * (capacity in floats; ESHAPE when too small).  EIO for a missing file or
+ * member.  cnncrf_npz_write: `count` members keys[i] of shapes
+ * shapes[4 i .. 4 i + ndims[i] - 1] from host arrays, uncompressed (numpy.load
+ * reads it), written beside `npz_path` and renamed over it. */
+int cnncrf_npz_read(const char *npz_path, const char *key, int64_t shape[4], int *ndim, float *h_data,
+                    size_t capacity);
+int cnncrf_npz_write(const char *npz_path, int count, const char *const *keys, const float *const *h_data,
+                     const int64_t *shapes, const int *ndims);
 /* Number of parameter arrays (filters + biases) the net expects. */
 int cnncrf_net_num_params(cnncrf_net_t net, int *count);
 /* Shape of arr_<index>. */
@@ -440,6 +453,19 @@ int cnncrf_train_sgd(cnncrf_train_t t, float lr, float momentum);
 /* forward + hinge + backward + sgd */
 int cnncrf_train_step(cnncrf_train_t t, const float *d_left, const float *d_right, const int32_t *d_gt, float lr,
                       float momentum, double *h_loss);
+/* Training checkpoint (no counterpart in the reference, which has no save
+ * path and no training state; its weights load through cnpy, stereo/operators/
+ * operator.cpp:55-85).  Save writes an uncompressed npz: arr_0 .. arr_{n-1},
+ * the FP32 master weights in the slot order and shapes of
+ * cnncrf_net_set_all_params, so the file is also a parameter file for
+ * inference (cnncrf_net_set_all_params, Stereo's parameter-file); and
+ * mom_0 .. mom_{n-1}, the SGD momentum.  The file is written beside `path`
+ * and renamed over it.  Load reads arr_i (shapes checked: ESHAPE) and mom_i
+ * when present (zero momentum when absent, so a plain parameter file starts
+ * a fresh run from those weights).  A loaded trainer continues bit for bit
+ * as the saved one would have.  Both synchronise the trainer's stream. */
+int cnncrf_train_save(cnncrf_train_t t, const char *npz_path);
+int cnncrf_train_load(cnncrf_train_t t, const char *npz_path);
 
 /* ---------------------------------------------------------------- Stereo */
 

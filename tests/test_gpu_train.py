@@ -131,6 +131,61 @@ def test_sgd_momentum_and_training_progress(cuda, oracle):
     assert np.mean(hist[-3:]) < hist[0], hist
 
 
+@pytest.mark.parametrize("prec", ["FP32", "BF16"])
+def test_checkpoint_resume_is_exact(cuda, oracle, tmp_path, prec):
+    """Two steps, a checkpoint, then a third step on the saved trainer and on a
+    fresh one loaded from the file: the same loss and the same weights and
+    momentum bit for bit.  The file is also a parameter file: the inference
+    net loads its arr_i, and a trainer loading a plain parameter file (no
+    mom_i) starts with zero momentum."""
+    torch = cuda
+    from cnncrf import _lib as L
+    from cnncrf.api import StereoNet
+    from cnncrf.train import Trainer
+    P = getattr(L, prec)
+    cfg, params, t, left, right, pads, gt, lst = setup(oracle, n=2, precision=P, P=16)
+    g_t = torch.from_numpy(gt).cuda()
+    for _ in range(2):
+        t.step(left, right, g_t, lr=0.01, momentum=0.9)
+    ck = tmp_path / "ck.npz"
+    t.save(str(ck))
+    u = Trainer(2, 40, 22, num_layers=3, topology=1, feat_channels=16, pw_channels=16, disp_max=9.0,
+                mean_loss=False, precision=P, checkpoint_every=0)
+    u.load(str(ck))
+    la = t.step(left, right, g_t, lr=0.01, momentum=0.9)
+    lb = u.step(left, right, g_t, lr=0.01, momentum=0.9)
+    assert np.array_equal(la, lb)
+    for i in range(t.num_params()):
+        assert np.array_equal(t.get_param(i), u.get_param(i)), i
+    t.save(str(tmp_path / "a.npz"))
+    u.save(str(tmp_path / "b.npz"))
+    with np.load(tmp_path / "a.npz") as za, np.load(tmp_path / "b.npz") as zb:
+        assert sorted(za.files) == sorted(zb.files)
+        for k in za.files:
+            assert np.array_equal(za[k], zb[k]), k
+        assert any(za["mom_%d" % i].any() for i in range(t.num_params()))
+        plain = {"arr_%d" % i: za["arr_%d" % i] for i in range(t.num_params())}
+    # the checkpoint as an inference parameter file
+    net = StereoNet(3, 1, 3, 22 + 6, 40 + 6, feat_channels=16, pw_channels=16, topology=1,
+                    unary=L.UNARY_ONE_MINUS_DOT, with_pairwise=True)
+    net.set_all_params(str(ck))
+    # a plain parameter file: the weights, zero momentum
+    np.savez(tmp_path / "plain.npz", **plain)
+    w = Trainer(2, 40, 22, num_layers=3, topology=1, feat_channels=16, pw_channels=16, disp_max=9.0,
+                mean_loss=False, precision=P, checkpoint_every=0)
+    w.load(str(tmp_path / "plain.npz"))
+    w.save(str(tmp_path / "c.npz"))
+    with np.load(tmp_path / "c.npz") as zc:
+        for i in range(t.num_params()):
+            assert np.array_equal(zc["arr_%d" % i], plain["arr_%d" % i]) and not zc["mom_%d" % i].any()
+    bad = dict(plain)
+    bad["arr_0"] = bad["arr_0"][:1]
+    np.savez(tmp_path / "bad.npz", **bad)
+    with pytest.raises(L.CnnCrfError) as e:
+        w.load(str(tmp_path / "bad.npz"))
+    assert e.value.status == L.ESHAPE
+
+
 def test_autograd_equals_fused_step(cuda, oracle):
     torch = cuda
     from cnncrf.train import HingeLossFunction, StereoNetsFunction
