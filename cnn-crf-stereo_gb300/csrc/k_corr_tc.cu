@@ -22,18 +22,22 @@
 // features comes from L2.  The channel softmax needs all D taps of a pixel in
 // one warp and so takes single-part lists only; 1 - <fL,fR> takes any.
 //
-// Persistent, warp-specialised CTA (192 threads, one per SM):
+// Persistent, warp-specialised CTA (576 threads, one per SM):
 //   warp 0      TMA: per 64-channel block, a 4-D box (64 ch x 128 px) of the
 //               left features and one (64 ch x 256 px) of the right
 //               features, 128-byte swizzle; a ring of `stages` blocks
 //   warp 1      TMEM allocation + single-thread tcgen05.mma (M=128, N=256,
 //               K=16 steps) into one of two 256-column accumulators
-//   warps 2..5  epilogue: warp q owns TMEM lanes (pixels) 32q..32q+31 and
-//               reads the 32 + omax - omin columns they touch into shared
-//               memory (one row per pixel); then per pixel the whole warp
-//               gathers the D taps along the band (lane j: k = j + 32 r),
-//               applies the unary and stores the pixel's D costs with
-//               coalesced 128-byte writes
+//   warps 2..17 epilogue, four warps per TMEM lane quarter q = warp % 4
+//               (pixels 32q..32q+31): the four read the 32 + omax - omin
+//               columns those pixels touch into shared memory (one row per
+//               pixel; each warp every fourth 32-column chunk), meet at a
+//               named barrier, and then each warp takes every fourth pixel:
+//               the whole warp gathers the pixel's D taps along the band
+//               (lane j: k = j + 32 r), applies the unary and stores its D
+//               costs with coalesced writes.  Sixteen warps instead of four
+//               hide the gather's latency; the four agree on every exit so
+//               none waits at the barrier for a partner that left.
 // Every mbarrier wait is bounded; on timeout the role raises the CTA abort
 // flag and the global error flag, drains what it issued and TMEM is freed.
 #include <algorithm>
@@ -58,7 +62,9 @@ constexpr int BN = 256;                    // band columns per tile (UMMA N)
 constexpr int A_BYTES = BM * 128;          // 128 px x 64 bf16
 constexpr int B_BYTES = BN * 128;          // 256 px x 64 bf16
 constexpr int STAGE = A_BYTES + B_BYTES;   // one 64-channel block of a tile
-constexpr int NUM_THREADS = 192;
+// epilogue warps per TMEM lane quarter.  Per KITTI step of 8 pairs the kernel
+// took 1.13 ms with 1, 0.80 with 2, 0.73 with 3 and 0.70 with 4 (GB300)
+constexpr int EPI_WARPS = 4;
 constexpr uint32_t TMEM_COLS = 2 * BN;     // two accumulators
 constexpr int SROW = 161;                  // staged row stride in floats (odd: no bank conflicts)
 constexpr int SCOLS = 160;                 // columns staged per warp: 32 + max band spread
@@ -90,12 +96,12 @@ __device__ __forceinline__ uint16_t quantize_u16(float x, float qinv, float qbia
 // disparities): each pixel's band diagonal from the warp's staged rows, the
 // unary, and the stores: the FP32 volume (WF) and / or its 16-bit copy (WQ),
 // chosen at compile time so the per-element stores carry no branches.
-template <int PP, bool WF, bool WQ>
-__device__ __forceinline__ void store_pixels(const CorrTcParams &p, const float *sw, int lane, int npx, int Dp,
-                                             const int *off, float *obase, uint16_t *obaseq)
+template <int EPW, int PP, bool WF, bool WQ>
+__device__ __forceinline__ void store_pixels(const CorrTcParams &p, const float *sw, int lane, int i0, int npx,
+                                             int Dp, const int *off, float *obase, uint16_t *obaseq)
 {
 #pragma unroll 1
-    for (int i = 0; i < npx; ++i) {
+    for (int i = i0; i < npx; i += EPW) {
         const float *row = sw + i * SROW + i;
         float cv[PP];
 #pragma unroll
@@ -141,23 +147,25 @@ __device__ __forceinline__ void store_pixels(const CorrTcParams &p, const float 
     }
 }
 
-template <bool WF, bool WQ>
-__device__ __forceinline__ void store_part(const CorrTcParams &p, int P, const float *sw, int lane, int npx, int Dp,
-                                           const int *off, float *obase, uint16_t *obaseq)
+// pixels i0, i0 + EPW, ... of the warp's 32 (the EPW warps of a lane quarter split them)
+template <int EPW, bool WF, bool WQ>
+__device__ __forceinline__ void store_part(const CorrTcParams &p, int P, const float *sw, int lane, int i0, int npx,
+                                           int Dp, const int *off, float *obase, uint16_t *obaseq)
 {
     switch (P) {
-    case 1: store_pixels<1, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 2: store_pixels<2, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 3: store_pixels<3, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 4: store_pixels<4, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 5: store_pixels<5, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 6: store_pixels<6, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    case 7: store_pixels<7, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
-    default: store_pixels<8, WF, WQ>(p, sw, lane, npx, Dp, off, obase, obaseq); break;
+    case 1: store_pixels<EPW, 1, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 2: store_pixels<EPW, 2, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 3: store_pixels<EPW, 3, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 4: store_pixels<EPW, 4, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 5: store_pixels<EPW, 5, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 6: store_pixels<EPW, 6, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    case 7: store_pixels<EPW, 7, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
+    default: store_pixels<EPW, 8, WF, WQ>(p, sw, lane, i0, npx, Dp, off, obase, obaseq); break;
     }
 }
 
-__global__ void __launch_bounds__(NUM_THREADS, 1)
+template <int EPW>
+__global__ void __launch_bounds__(64 + 128 * EPW, 1)
     k_corr_tc(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR, const CorrTcParams p)
 {
     extern __shared__ uint8_t smem_raw[];
@@ -173,6 +181,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
     volatile int *zero_flag = abort_flag + 1;
     int *coff = (int *)(tmem_slot + 4); // [D] band column offset of disparity k
+    volatile int *okq = (volatile int *)(coff + p.D); // [4][EPW] each epilogue warp's tfull wait result
+    constexpr int NUM_THREADS = 64 + 128 * EPW;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
@@ -182,7 +192,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             tc::mbar_init(&tfull[b], 1);
-            tc::mbar_init(&tempty[b], 128);
+            tc::mbar_init(&tempty[b], 128 * EPW);
         }
         tc::mbar_init(drain, 1);
         *abort_flag = 0;
@@ -287,7 +297,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc::mbar_wait(drain, 0, zero_flag, 1u << 22);
         }
     } else {
-        const int q = warp & 3; // the TMEM lane quarter this warp may read
+        const int q = warp & 3;         // the TMEM lane quarter this warp may read
+        const int h = (warp - 2) >> 2;  // which of the quarter's EPW warps
         float *sw = stg + q * 32 * SROW;
         int lt = 0;
         for (int t = blockIdx.x; t < p.num_tiles; t += gridDim.x, ++lt) {
@@ -302,27 +313,35 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             }
             const int buf = lt & 1;
             const uint32_t use = (uint32_t)lt >> 1;
+            // both warps wait (bounded) and publish the result; both then act on
+            // the pair's combined result, so they leave the loop together
             int ok = 1;
             if (lane == 0) ok = tc::mbar_wait(&tfull[buf], use & 1, abort_flag) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (lane == 0) okq[EPW * q + h] = ok;
+            // the pair's barrier: both results published, and the partner is done
+            // gathering from the staged rows of the previous tile
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + q), "n"(32 * EPW) : "memory");
+#pragma unroll
+            for (int e = 0; e < EPW; ++e) ok &= okq[EPW * q + e];
             if (!ok) {
                 *abort_flag = 1;
                 atomicExch(p.err, 1);
                 break;
             }
             tc::fence_after_sync();
-            // rows 32q.. of the accumulator, columns 32q .. 32q + 32*nchunks
+            // rows 32q.. of the accumulator, columns 32q .. 32q + 32*nchunks; this warp's chunks h, h + 2, ..
             const uint32_t ta = tmem + ((uint32_t)(q * 32) << 16) + buf * BN + q * 32;
             float v[32];
 #pragma unroll 1
-            for (int c = 0; c < p.pnch[part]; ++c) {
+            for (int c = h; c < p.pnch[part]; c += EPW) {
                 tc::tmem_ld32(ta + c * 32, v); // warp-collective: every lane runs it
 #pragma unroll
                 for (int j = 0; j < 32; ++j) sw[lane * SROW + c * 32 + j] = v[j];
             }
             tc::fence_before_sync();
             tc::mbar_arrive(&tempty[buf]);
-            __syncwarp();
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + q), "n"(32 * EPW) : "memory"); // all chunks staged
 
             const int pair = tt / tiles_per_pair, r = tt - pair * tiles_per_pair;
             const int y = r / p.tiles_x, xq = (r - y * p.tiles_x) * BM + q * 32;
@@ -330,10 +349,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const size_t obase_i = (((size_t)pair * p.H + y) * p.W + xq) * p.D + k0;
             float *obase = p.out ? p.out + obase_i : nullptr;
             uint16_t *obaseq = p.outq ? p.outq + obase_i : nullptr;
-            if (obaseq && obase) store_part<true, true>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
-            else if (obaseq) store_part<false, true>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
-            else store_part<true, false>(p, P, sw, lane, npx, Dp, off, obase, obaseq);
-            __syncwarp(); // the staging rows are rewritten by the next tile
+            if (obaseq && obase) store_part<EPW, true, true>(p, P, sw, lane, h, npx, Dp, off, obase, obaseq);
+            else if (obaseq) store_part<EPW, false, true>(p, P, sw, lane, h, npx, Dp, off, obase, obaseq);
+            else store_part<EPW, true, false>(p, P, sw, lane, h, npx, Dp, off, obase, obaseq);
+            // the next tile's first barrier keeps its staging behind the partner's gather
         }
     }
     __syncthreads();
@@ -345,7 +364,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
 size_t smem_bytes(int stages, int D)
 {
-    return 1024 + (size_t)stages * STAGE + STG_BYTES + (2 * (size_t)stages + 5) * 8 + 16 + (size_t)D * 4;
+    return 1024 + (size_t)stages * STAGE + STG_BYTES + (2 * (size_t)stages + 5) * 8 + 16 + (size_t)D * 4 + 64;
 }
 
 struct CorrTcPlan {
@@ -455,11 +474,12 @@ int correlation_tc(const void *feat, int npairs, int H, int W, int C, int cp, co
     p.stages = smem_bytes(3, D) <= (size_t)maxsm ? 3 : 2;
     const size_t smem = smem_bytes(p.stages, D);
     if (smem > (size_t)maxsm) return fail(CNNCRF_EUNSUPPORTED, "correlation_tc: %zu bytes of shared memory", smem);
-    CNNCRF_CUDA(cudaFuncSetAttribute(k_corr_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    auto kern = k_corr_tc<EPI_WARPS>;
+    CNNCRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = std::min(p.num_tiles, sms);
     {
         CNNCRF_PROF("corr_tc", st);
-        k_corr_tc<<<grid, NUM_THREADS, smem, st>>>(ml, mr, p);
+        kern<<<grid, 64 + 128 * EPI_WARPS, smem, st>>>(ml, mr, p);
     }
     CNNCRF_CHECK_LAUNCH();
     return CNNCRF_OK;
