@@ -311,20 +311,23 @@ namespace {
 
 // CRC-32 of the zip format (reflected polynomial 0xEDB88320, initial and
 // final XOR 0xFFFFFFFF; APPNOTE.TXT 4.4.7), table-driven
-uint32_t crc32_update(uint32_t crc, const uint8_t *p, size_t n)
-{
-    static uint32_t table[256];
-    static bool init = false;
-    if (!init) {
+struct Crc32Table {
+    uint32_t t[256];
+    Crc32Table()
+    {
         for (uint32_t i = 0; i < 256; ++i) {
             uint32_t c = i;
             for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-            table[i] = c;
+            t[i] = c;
         }
-        init = true;
     }
+};
+
+uint32_t crc32_update(uint32_t crc, const uint8_t *p, size_t n)
+{
+    static const Crc32Table table; // initialised once, thread-safe
     crc = ~crc;
-    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
+    for (size_t i = 0; i < n; ++i) crc = table.t[(crc ^ p[i]) & 0xffu] ^ (crc >> 8);
     return ~crc;
 }
 
