@@ -127,6 +127,27 @@ def test_crf_bitexact(cuda, oracle, D, delta, shape):
         assert lb == olb
 
 
+@pytest.mark.parametrize("H,W,D,shape,delta", [(4, 5, 16, 1, 3), (5, 4, 40, 0, 2), (3, 6, 33, 1, 4),
+                                                (6, 3, 128, 1, 3)])
+def test_crf_bound_reaches_the_lp_relaxation(cuda, H, W, D, shape, delta):
+    """The GPU solver's bound, after 300 iterations, equals the optimum of the
+    energy's local-polytope LP relaxation as scipy's HiGHS solves it: the
+    solver maximises the dual of that LP (weak duality keeps every bound at or
+    below it; see tests/test_oracle.py), here to within 1e-5."""
+    pytest.importorskip("scipy")
+    torch = cuda
+    from cnncrf.api import crf_solve
+    from test_oracle import _local_polytope_lp
+    rng = np.random.default_rng(H * 100 + D)
+    cost = (rng.random((H, W, D)) * 3).astype(np.float32)
+    wx = (rng.random((H, W)) * 2).astype(np.float32)
+    wy = (rng.random((H, W)) * 2).astype(np.float32)
+    lp = _local_polytope_lp(cost, wx, wy, 0.6, 1.7, delta, shape)
+    _, lb = crf_solve(dev(cost, torch), dev(wx, torch), dev(wy, torch), L1=0.6, L2=1.7, delta=delta,
+                      total_it=300, shape=shape, slack=0.5)
+    assert abs(lb - lp) <= 1e-5 * max(1.0, abs(lp)), (lb, lp)
+
+
 def test_slackprop_object(cuda, oracle):
     torch = cuda
     from cnncrf.api import SlackProp
