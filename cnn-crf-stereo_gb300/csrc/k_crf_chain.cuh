@@ -49,21 +49,18 @@ namespace {
 
 #define INF CUDART_INF_F
 
-// Order-preserving map of (non-NaN) floats to signed ints, and back: the
-// warp minimum is then one redux.sync.min.s32, exact like a float min.
-__device__ __forceinline__ int f2ord(float f)
-{
-    const int b = __float_as_int(f);
-    return b ^ ((b >> 31) & 0x7fffffff);
-}
-__device__ __forceinline__ float ord2f(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7fffffff)); }
-
+// The warp minimum of the lanes' minima: one redux.sync.min.f32 (sm_100 and
+// later), exact like a float min.  The chain values are never NaN (pads are
+// +inf); a zero may come back with either sign, which no later operation
+// distinguishes (the labels compare values, the bound adds them).
 template <int P> __device__ __forceinline__ float warp_min(const float (&v)[P])
 {
     float m = v[0];
 #pragma unroll
     for (int r = 1; r < P; ++r) m = fminf(m, v[r]);
-    return ord2f(__reduce_min_sync(0xffffffffu, f2ord(m)));
+    float w;
+    asm("redux.sync.min.f32 %0, %1, 0xffffffff;" : "=f"(w) : "f"(m));
+    return w;
 }
 
 template <int P> __device__ __forceinline__ void load_vec(const float *p, int lane, int D, float (&v)[P])
