@@ -409,13 +409,14 @@ bool unary_q16(int unary, UnaryQ16 *q)
 {
     if (unary == 1) { // 1 - cosine in [0, 2] (a little outside where BF16 rounding lifts |cos| past 1)
         q->scale = 1.0f / 32768.0f, q->offset = -1.0f / 256.0f;
-        return true;
-    }
-    if (unary == 0) { // -softmax in [-1, 0]
+    } else if (unary == 0) { // -softmax in [-1, 0]
         q->scale = 1.0f / 65536.0f, q->offset = -1.0f;
-        return true;
+    } else {
+        return false;
     }
-    return false;
+    // the CRF's dequantisation computes (2^23 + q) scale + (offset - 2^23 scale):
+    // that offset must be exact in FP32 (it is for both codes above)
+    return (double)(q->offset - 8388608.0f * q->scale) == (double)q->offset - 8388608.0 * (double)q->scale;
 }
 
 bool corr_tc_supported(int C, int cp, const float *h_list, int D, int unary)

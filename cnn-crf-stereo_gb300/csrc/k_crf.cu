@@ -123,6 +123,9 @@ CrfPassArgs pass_args(const float *cost, long wps, int W, int H, int D, int np, 
     a.theta = cost;
     a.thetaq = crf_reads_q16(D) ? (const uint16_t *)costq : nullptr;
     a.qscale = q.scale, a.qoffset = q.offset;
+    // the kernels' dequantisation folds 2^23 scale into the offset (exact:
+    // unary_q16 only hands out codes for which it is)
+    a.qoffset23 = q.offset - 8388608.0f * q.scale;
     a.phi = (float *)(ws + l.phi);
     a.lbuf = (float *)(ws + l.lbuf);
     a.W = W, a.H = H, a.D = D, a.np = np, a.wps = wps;

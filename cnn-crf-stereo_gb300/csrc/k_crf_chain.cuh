@@ -27,6 +27,7 @@ struct CrfPassArgs {
     const float *theta; // the cost volume [np][H][W][D]
     const uint16_t *thetaq; // its 16-bit fixed-point copy, read by the H pass instead of theta when set
     float qscale, qoffset;  // theta = q * qscale + qoffset (exact in FP32)
+    float qoffset23;        // qoffset - 2^23 qscale, exact: theta = (2^23 + q) * qscale + qoffset23
     float *phi;         // H/V split of the unary, same layout
     const float *wgt;   // wx (H pass) or wy (V pass), pair stride wps
     float *lbuf;        // forward messages, same layout as phi
@@ -233,16 +234,23 @@ template <int P> __device__ __forceinline__ void lane_copy16(float *dst, const u
 }
 
 // dequantise: q * scale + offset is exact (q < 2^16, scale a power of two,
-// the sum a multiple of scale below 2^9 in magnitude)
+// the sum a multiple of scale below 2^9 in magnitude).  The code goes into
+// the low mantissa bits of 2^23 by one byte permute, which makes the float
+// 2^23 + q exactly, and offset23 = offset - 2^23 scale (exact, checked on the
+// host) takes the 2^23 back out inside the one rounding of the fma:
+// (2^23 + q) scale + offset23 = q scale + offset.  Two instructions per label
+// instead of a mask or shift, a conversion and the fma.
 template <int P>
-__device__ __forceinline__ void lane_read16(const float *slot, int lane, float scale, float offset, float (&v)[P])
+__device__ __forceinline__ void lane_read16(const float *slot, int lane, float scale, float offset23, float (&v)[P])
 {
     const uint32_t *q = (const uint32_t *)((const uint16_t *)slot + lane * P);
 #pragma unroll
     for (int i = 0; i < P / 2; ++i) {
         const uint32_t w = q[i];
-        v[2 * i] = __fmaf_rn((float)(w & 0xffffu), scale, offset);
-        v[2 * i + 1] = __fmaf_rn((float)(w >> 16), scale, offset);
+        const float lo = __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7410)); // bytes w0, w1, 0x00, 0x4B
+        const float hi = __int_as_float((int)__byte_perm(w, 0x4B000000u, 0x7432)); // bytes w2, w3, 0x00, 0x4B
+        v[2 * i] = __fmaf_rn(lo, scale, offset23);
+        v[2 * i + 1] = __fmaf_rn(hi, scale, offset23);
     }
 }
 
@@ -283,7 +291,7 @@ __host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass, bool 
 // labels), so the chain's dependent arithmetic does not wait on DRAM.
 template <int P, int DELTA, bool HPASS, bool FULL, int RING, bool T16 = false>
 __global__ void __launch_bounds__(128)
-    k_crf_chain(const float *__restrict__ theta, const uint16_t *__restrict__ thetaq, float qscale, float qoffset,
+    k_crf_chain(const float *__restrict__ theta, const uint16_t *__restrict__ thetaq, float qscale, float qoffset23,
                 float *__restrict__ phi, const float *__restrict__ wgt,
                 float *__restrict__ Lbuf, int W, int H, int D, Rho rp, int first, int store_phi,
                 int32_t *__restrict__ labels, double *__restrict__ cmin_out, int npairs, long wps)
@@ -343,7 +351,7 @@ __global__ void __launch_bounds__(128)
     for (; i < iend; ++i) {
         issue_f(i + RING - 1);
         cp_wait<RING - 1>();
-        if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset, th);
+        if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(i, 0), lane, th);
         if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
         store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
@@ -389,7 +397,7 @@ __global__ void __launch_bounds__(128)
         const int i = n - 1 - j, e = i - 1; // edge e -> i
         issue_b(j + RING - 1);
         cp_wait<RING - 1>();
-        if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset, th);
+        if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(j, 0), lane, th);
         if (use_phi) {
             lane_read<P>(slot(j, 1), lane, ph);
@@ -447,7 +455,7 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
     const long chains = (long)(hpass ? a.H : a.W) * a.np;
     {
         CNNCRF_PROF(hpass ? "crf_h" : "crf_v", st);
-        kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.thetaq, a.qscale, a.qoffset, a.phi, a.wgt,
+        kern<<<ceil_div(chains, wpb), 32 * wpb, sm, st>>>(a.theta, a.thetaq, a.qscale, a.qoffset23, a.phi, a.wgt,
                                                            a.lbuf, a.W, a.H, a.D, a.rp,
                                                            a.first, a.store_phi, a.labels, a.cmin, a.np,
                                                            a.wps);
