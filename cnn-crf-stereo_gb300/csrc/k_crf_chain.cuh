@@ -347,7 +347,7 @@ __global__ void __launch_bounds__(128)
     const float wc = wn;
     wn = wload(b + 1);
     const int iend = min(n, i + 32);
-#pragma unroll 1
+#pragma unroll (HPASS ? 1 : 2)
     for (; i < iend; ++i) {
         issue_f(i + RING - 1);
         cp_wait<RING - 1>();
@@ -392,7 +392,7 @@ __global__ void __launch_bounds__(128)
     const float wc = wn;
     wn = wload(eb - 1);
     const int jend = eb >= 0 ? n - 1 - 32 * eb : n; // nodes i = e + 1 for the block's edges e
-#pragma unroll 1
+#pragma unroll (HPASS ? 1 : 2)
     for (; j < jend; ++j) {
         const int i = n - 1 - j, e = i - 1; // edge e -> i
         issue_b(j + RING - 1);
