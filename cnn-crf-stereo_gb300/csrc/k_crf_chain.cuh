@@ -340,13 +340,19 @@ __global__ void __launch_bounds__(128)
 #pragma unroll
     for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
     for (int i = 0; i < RING - 1; ++i) issue_f(i);
-    double acc = 0.0, cmin = 0.0;
+    // the chain's minimum in FP64: lane l sums the node minima g_i of i = l mod 32
+    // in ascending i, and the 32 partial sums are added in lane order at the end
+    // of the sweep.  Within a block of 32 nodes lane l keeps node 32 b + l's
+    // minimum as a float (gb) and adds it once, at the block's end: one FP64
+    // conversion and add per 32 nodes, none on the message chain
+    double acc = 0.0;
     float wn = wload(0);
     // blocks of 32 nodes: the block's weights in wc, the next block's loading into wn
     for (int b = 0, i = 0; i < n; ++b) {
     const float wc = wn;
     wn = wload(b + 1);
-    const int iend = min(n, i + 32);
+    const int iend = min(n, i + 32), nb = iend - i;
+    float gb = 0.0f;
 #pragma unroll (HPASS ? 1 : 2)
     for (; i < iend; ++i) {
         issue_f(i + RING - 1);
@@ -361,14 +367,18 @@ __global__ void __launch_bounds__(128)
             v[r] = (FULL || lane * P + r < D) ? __fadd_rn(L[r], un) : INF;
         }
         const float g = warp_min<P>(v);
-        if (lane == 0) { // the FP64 bound lives in lane 0 only (off the message chain)
-            if (i < n - 1) acc += (double)g;
-            else cmin = acc + (double)g;
-        }
+        gb = lane == (i & 31) ? g : gb;
         if (i < n - 1) minconv<P, DELTA, FULL>(v, g, __shfl_sync(0xffffffffu, wc, i & 31), rp, lane, D, L);
     }
+    if (lane < nb) acc += (double)gb;
     }
     cp_wait<0>();
+    double cmin = acc; // lane 0: ((p0 + p1) + p2) + ... + p31
+#pragma unroll 1
+    for (int l = 1; l < 32; ++l) {
+        const double pl = __shfl_sync(0xffffffffu, acc, l);
+        if (lane == 0) cmin += pl;
+    }
 
     // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
     auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j

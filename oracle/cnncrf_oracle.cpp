@@ -507,18 +507,19 @@ double chain_pass(int n, int D, const float *w, long wstride, const Rho &r, floa
     Lbuf.assign((size_t)n * D, 0.0f);
     std::vector<float> L((size_t)D, 0.0f), v((size_t)D), R((size_t)D, 0.0f), m((size_t)D),
         A((size_t)D), tmp((size_t)D);
-    double acc = 0.0, cmin = 0.0;
+    // the chain minimum in FP64, summed in the GPU kernel's order: 32 partial
+    // sums, partial l taking the node minima g_i with i = l mod 32 in ascending
+    // i, then ((p0 + p1) + p2) + ... + p31
+    double part[32] = {0.0};
     for (int i = 0; i < n; ++i) {
         std::memcpy(&Lbuf[(size_t)i * D], L.data(), sizeof(float) * D);
         for (int k = 0; k < D; ++k) v[k] = L[k] + unary(i, k);
         float g = vmin(v.data(), D);
-        if (i < n - 1) {
-            acc += (double)g;
-            minconv(v.data(), g, w[(long)i * wstride], r, D, L.data());
-        } else {
-            cmin = acc + (double)g;
-        }
+        part[i & 31] += (double)g;
+        if (i < n - 1) minconv(v.data(), g, w[(long)i * wstride], r, D, L.data());
     }
+    double cmin = part[0];
+    for (int l = 1; l < 32; ++l) cmin += part[l];
     for (int i = n - 1; i >= 0; --i) {
         for (int k = 0; k < D; ++k) {
             A[k] = unary(i, k);

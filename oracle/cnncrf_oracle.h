@@ -42,7 +42,10 @@
  *    of the nodes after it;
  *  - the bound: the FP64 sum of the last vertical pass's chain minima and of
  *    the horizontal pass before it (the horizontal minima are preserved by
- *    its hand-over, so both are the dual objective at the same phi);
+ *    its hand-over, so both are the dual objective at the same phi); a
+ *    chain's minimum is the sum of its forward sweep's per-node minima, in
+ *    the order the GPU kernel adds them: 32 FP64 partial sums, partial l
+ *    taking the nodes i = l mod 32 in ascending i, then added in order;
  *  - the labels: the first argmin of the last vertical pass's min-marginals;
  *  - the pairwise term w_ij rho(|x_i - x_j|): the options L1, L2, delta keep
  *    the reference's names.  STEP (the reference configs' shape): rho(0) = 0,
