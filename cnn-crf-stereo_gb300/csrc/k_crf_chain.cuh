@@ -327,19 +327,24 @@ __global__ void __launch_bounds__(128)
     constexpr int TF = theta_floats(P, HPASS, T16), SF = TF + 64 * P;
     auto slot = [&](int i, int a) { return ring + (i % RING) * SF + (a == 0 ? 0 : TF + (a - 1) * 32 * P); };
 
+    // element offsets of the chain's nodes: node i at cb + i ns; the sweeps
+    // step running offsets by ns instead of multiplying per node
+    const long cb = pix(0) * D, ns = (HPASS ? 1L : (long)W) * D;
+
     // ---- forward: messages into each node, stored for the backward sweep
-    auto issue_f = [&](int i) {
+    auto issue_f = [&](int i, long o) { // node i, at element offset o
         if (i < n) {
-            if constexpr (HPASS && T16) lane_copy16<P>(slot(i, 0), thetaq + pix(i) * D, lane);
-            else if (HPASS) lane_copy<P>(slot(i, 0), theta + pix(i) * D, lane, D);
-            if (use_phi) lane_copy<P>(slot(i, 1), phi + pix(i) * D, lane, D);
+            if constexpr (HPASS && T16) lane_copy16<P>(slot(i, 0), thetaq + o, lane);
+            else if (HPASS) lane_copy<P>(slot(i, 0), theta + o, lane, D);
+            if (use_phi) lane_copy<P>(slot(i, 1), phi + o, lane, D);
         }
         cp_commit();
     };
     float L[P], v[P], th[P], ph[P];
 #pragma unroll
     for (int r = 0; r < P; ++r) L[r] = 0.0f, th[r] = 0.0f, ph[r] = 0.0f;
-    for (int i = 0; i < RING - 1; ++i) issue_f(i);
+    long po = cb, so = cb; // the node being prefetched, the node being stored
+    for (int i = 0; i < RING - 1; ++i, po += ns) issue_f(i, po);
     // the chain's minimum in FP64: lane l sums the node minima g_i of i = l mod 32
     // in ascending i, and the 32 partial sums are added in lane order at the end
     // of the sweep.  Within a block of 32 nodes lane l keeps node 32 b + l's
@@ -355,12 +360,14 @@ __global__ void __launch_bounds__(128)
     float gb = 0.0f;
 #pragma unroll (HPASS ? 1 : 2)
     for (; i < iend; ++i) {
-        issue_f(i + RING - 1);
+        issue_f(i + RING - 1, po);
+        po += ns;
         cp_wait<RING - 1>();
         if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(i, 0), lane, th);
         if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
-        store_vec<P>(Lbuf + pix(i) * D, lane, D, L);
+        store_vec<P>(Lbuf + so, lane, D, L);
+        so += ns;
 #pragma unroll
         for (int r = 0; r < P; ++r) {
             const float un = HPASS ? __fsub_rn(th[r], ph[r]) : ph[r];
@@ -381,20 +388,21 @@ __global__ void __launch_bounds__(128)
     }
 
     // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
-    auto issue_b = [&](int j) { // j-th step of the sweep = node n-1-j
-        const int i = n - 1 - j;
-        if (i >= 0) {
-            if constexpr (HPASS && T16) lane_copy16<P>(slot(j, 0), thetaq + pix(i) * D, lane);
-            else if (HPASS) lane_copy<P>(slot(j, 0), theta + pix(i) * D, lane, D);
-            if (use_phi) lane_copy<P>(slot(j, 1), phi + pix(i) * D, lane, D);
-            lane_copy<P>(slot(j, 2), Lbuf + pix(i) * D, lane, D);
+    auto issue_b = [&](int j, long o) { // j-th step of the sweep = node n-1-j, at element offset o
+        if (j < n) {
+            if constexpr (HPASS && T16) lane_copy16<P>(slot(j, 0), thetaq + o, lane);
+            else if (HPASS) lane_copy<P>(slot(j, 0), theta + o, lane, D);
+            if (use_phi) lane_copy<P>(slot(j, 1), phi + o, lane, D);
+            lane_copy<P>(slot(j, 2), Lbuf + o, lane, D);
         }
         cp_commit();
     };
     float R[P], Lx[P], m[P], A[P];
 #pragma unroll
     for (int r = 0; r < P; ++r) R[r] = 0.0f;
-    for (int j = 0; j < RING - 1; ++j) issue_b(j);
+    po = so = cb + (long)(n - 1) * ns;                 // both sweep down from node n-1
+    long lpix = pix(n - 1);                            // the label's pixel (V pass)
+    for (int j = 0; j < RING - 1; ++j, po -= ns) issue_b(j, po);
     // the sweep reads edges n-2 down to 0, in blocks of 32 edges from the top;
     // node 0 (no edge below it) comes last, in a block of its own
     wn = wload((n - 2) >> 5);
@@ -405,7 +413,8 @@ __global__ void __launch_bounds__(128)
 #pragma unroll (HPASS ? 1 : 2)
     for (; j < jend; ++j) {
         const int i = n - 1 - j, e = i - 1; // edge e -> i
-        issue_b(j + RING - 1);
+        issue_b(j + RING - 1, po);
+        po -= ns;
         cp_wait<RING - 1>();
         if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(j, 0), lane, th);
@@ -428,7 +437,8 @@ __global__ void __launch_bounds__(128)
             for (int r = P - 1; r >= 0; --r)
                 if (m[r] == mu && (FULL || lane * P + r < D)) best = lane * P + r;
             best = __reduce_min_sync(0xffffffffu, best);
-            if (lane == 0) labels[pix(i)] = best;
+            if (lane == 0) labels[lpix] = best;
+            lpix -= W;
         }
 #pragma unroll
         for (int r = 0; r < P; ++r) {
@@ -436,7 +446,8 @@ __global__ void __launch_bounds__(128)
             A[r] = __fsub_rn(A[r], h);
             ph[r] = HPASS ? __fadd_rn(ph[r], h) : A[r];
         }
-        if (store_phi) store_vec<P>(phi + pix(i) * D, lane, D, ph);
+        if (store_phi) store_vec<P>(phi + so, lane, D, ph);
+        so -= ns;
         if (i > 0) {
 #pragma unroll
             for (int r = 0; r < P; ++r) v[r] = (FULL || lane * P + r < D) ? __fadd_rn(A[r], R[r]) : INF;
