@@ -17,7 +17,7 @@
 //
 // GPU layout: one warp per chain (a row for H, a column for V); lane j holds
 // labels k = j*P .. j*P+P-1 in registers; neighbours across lanes come from
-// warp shuffles, the minimum over labels from an xor-shuffle butterfly.  All
+// warp shuffles, the minimum over labels from one redux.sync.min.f32.  All
 // operations are exact (min) or single IEEE ops in the oracle's order, so the
 // labels equal the oracle's bit for bit.  Compiled with --fmad=false.
 #include <algorithm>
