@@ -569,10 +569,10 @@ def run_profile(args):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) measured with ncu on one-pair launches
 # of this workload, scaled to a launch of the 8-pair step (traffic grows with the images / chains):
-# k_conv_tc layer 3 over 2 images 449.9 MB; k_crf_chain H pass (reading the 16-bit unary) 1309.3 MB and
-# V pass 1067.8 MB per pair.
+# k_conv_tc layer 3 over 2 images 449.9 MB; k_crf_chain H pass (reading the 16-bit unary) 1311.8 MB and
+# V pass 1069.9 MB per pair.
 CONV_TC_BYTES_PER_IMAGE = 449.9e6 / 2
-CRF_H_BYTES_PER_PAIR, CRF_V_BYTES_PER_PAIR = 1309.3e6, 1067.8e6
+CRF_H_BYTES_PER_PAIR, CRF_V_BYTES_PER_PAIR = 1311.8e6, 1069.9e6
 
 
 def make_batch(cnncrf, wl, B, precision, graph, stream, seed0, group_size=0):
