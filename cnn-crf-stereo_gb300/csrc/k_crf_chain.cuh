@@ -233,6 +233,22 @@ template <int P> __device__ __forceinline__ void lane_copy16(float *dst, const u
     }
 }
 
+// The whole warp copies one pixel vector of NB bytes (a multiple of 16, the
+// source 16-byte aligned) into its ring slot in 16-byte chunks, lane l taking
+// chunks l, l + 32, ..: one or two copy instructions per lane where the lane's
+// own labels (3 or 6 of them) would take three.  Other lanes' chunks are
+// visible to a lane after its wait and a __syncwarp.
+template <int NB> __device__ __forceinline__ void warp_copy(void *dst, const void *src, int lane)
+{
+    static_assert(NB % 16 == 0, "whole 16-byte chunks");
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+#pragma unroll
+    for (int ch = 0; ch < (NB / 16 + 31) / 32; ++ch) {
+        const int k = lane + 32 * ch;
+        if (k < NB / 16) cp_async16(d + 16 * k, (const char *)src + 16 * k);
+    }
+}
+
 // dequantise: q * scale + offset is exact (q < 2^16, scale a power of two,
 // the sum a multiple of scale below 2^9 in magnitude).  The code goes into
 // the low mantissa bits of 2^23 by one byte permute, which makes the float
@@ -289,7 +305,7 @@ __host__ __device__ constexpr int ring_floats(int P, int RING, bool hpass, bool 
 // Per step the pixel vectors come from a per-warp shared-memory ring filled
 // RING steps ahead with cp.async (each lane copies and reads only its own
 // labels), so the chain's dependent arithmetic does not wait on DRAM.
-template <int P, int DELTA, bool HPASS, bool FULL, int RING, bool T16 = false>
+template <int P, int DELTA, bool HPASS, bool FULL, int RING, bool T16 = false, bool COOP = false>
 __global__ void __launch_bounds__(128)
     k_crf_chain(const float *__restrict__ theta, const uint16_t *__restrict__ thetaq, float qscale, float qoffset23,
                 float *__restrict__ phi, const float *__restrict__ wgt,
@@ -332,11 +348,20 @@ __global__ void __launch_bounds__(128)
     const long cb = pix(0) * D, ns = (HPASS ? 1L : (long)W) * D;
 
     // ---- forward: messages into each node, stored for the backward sweep
+    // COOP (3 or 6 labels per lane in whole warps, 16-byte aligned vectors): the
+    // warp copies each vector in 16-byte chunks instead of each lane its labels
+    static_assert(!COOP || (FULL && (P == 3 || P == 6)), "cooperative copies: D = 96 or 192");
     auto issue_f = [&](int i, long o) { // node i, at element offset o
         if (i < n) {
-            if constexpr (HPASS && T16) lane_copy16<P>(slot(i, 0), thetaq + o, lane);
-            else if (HPASS) lane_copy<P>(slot(i, 0), theta + o, lane, D);
-            if (use_phi) lane_copy<P>(slot(i, 1), phi + o, lane, D);
+            if constexpr (COOP) {
+                if constexpr (HPASS && T16) warp_copy<64 * P>(slot(i, 0), thetaq + o, lane);
+                else if (HPASS) warp_copy<128 * P>(slot(i, 0), theta + o, lane);
+                if (use_phi) warp_copy<128 * P>(slot(i, 1), phi + o, lane);
+            } else {
+                if constexpr (HPASS && T16) lane_copy16<P>(slot(i, 0), thetaq + o, lane);
+                else if (HPASS) lane_copy<P>(slot(i, 0), theta + o, lane, D);
+                if (use_phi) lane_copy<P>(slot(i, 1), phi + o, lane, D);
+            }
         }
         cp_commit();
     };
@@ -363,6 +388,7 @@ __global__ void __launch_bounds__(128)
         issue_f(i + RING - 1, po);
         po += ns;
         cp_wait<RING - 1>();
+        if constexpr (COOP) __syncwarp(); // the other lanes' chunks of node i
         if constexpr (HPASS && T16) lane_read16<P>(slot(i, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(i, 0), lane, th);
         if (use_phi) lane_read<P>(slot(i, 1), lane, ph);
@@ -390,10 +416,17 @@ __global__ void __launch_bounds__(128)
     // ---- backward: min-marginals, slack hand-over, reduced unary propagated back
     auto issue_b = [&](int j, long o) { // j-th step of the sweep = node n-1-j, at element offset o
         if (j < n) {
-            if constexpr (HPASS && T16) lane_copy16<P>(slot(j, 0), thetaq + o, lane);
-            else if (HPASS) lane_copy<P>(slot(j, 0), theta + o, lane, D);
-            if (use_phi) lane_copy<P>(slot(j, 1), phi + o, lane, D);
-            lane_copy<P>(slot(j, 2), Lbuf + o, lane, D);
+            if constexpr (COOP) {
+                if constexpr (HPASS && T16) warp_copy<64 * P>(slot(j, 0), thetaq + o, lane);
+                else if (HPASS) warp_copy<128 * P>(slot(j, 0), theta + o, lane);
+                if (use_phi) warp_copy<128 * P>(slot(j, 1), phi + o, lane);
+                warp_copy<128 * P>(slot(j, 2), Lbuf + o, lane);
+            } else {
+                if constexpr (HPASS && T16) lane_copy16<P>(slot(j, 0), thetaq + o, lane);
+                else if (HPASS) lane_copy<P>(slot(j, 0), theta + o, lane, D);
+                if (use_phi) lane_copy<P>(slot(j, 1), phi + o, lane, D);
+                lane_copy<P>(slot(j, 2), Lbuf + o, lane, D);
+            }
         }
         cp_commit();
     };
@@ -416,6 +449,7 @@ __global__ void __launch_bounds__(128)
         issue_b(j + RING - 1, po);
         po -= ns;
         cp_wait<RING - 1>();
+        if constexpr (COOP) __syncwarp();
         if constexpr (HPASS && T16) lane_read16<P>(slot(j, 0), lane, qscale, qoffset23, th);
         else if (HPASS) lane_read<P>(slot(j, 0), lane, th);
         if (use_phi) {
@@ -472,6 +506,16 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
                       : (full ? k_crf_chain<P, DELTA, false, true, RING> : k_crf_chain<P, DELTA, false, false, RING>);
     if constexpr (P % 2 == 0)
         if (t16) kern = k_crf_chain<P, DELTA, true, true, RING, true>;
+    // cooperative 16-byte copies where the vectors allow them (the workspace's phi and messages are 256-byte
+    // aligned; a caller's cost volume may not be)
+    if constexpr (P == 3 || P == 6) {
+        const bool aligned = (((uintptr_t)a.theta | (uintptr_t)a.thetaq | (uintptr_t)a.phi | (uintptr_t)a.lbuf) & 15) == 0;
+        if (full && aligned) {
+            if (!hpass) kern = k_crf_chain<P, DELTA, false, true, RING, false, true>;
+            else if (t16) kern = k_crf_chain<P, DELTA, true, true, RING, P % 2 == 0, true>;
+            else kern = k_crf_chain<P, DELTA, true, true, RING, false, true>;
+        }
+    }
     CNNCRF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     const long chains = (long)(hpass ? a.H : a.W) * a.np;
     {
