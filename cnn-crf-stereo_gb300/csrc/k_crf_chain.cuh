@@ -235,9 +235,10 @@ template <int P> __device__ __forceinline__ void lane_copy16(float *dst, const u
 
 // The whole warp copies one pixel vector of NB bytes (a multiple of 16, the
 // source 16-byte aligned) into its ring slot in 16-byte chunks, lane l taking
-// chunks l, l + 32, ..: one or two copy instructions per lane where the lane's
-// own labels (3 or 6 of them) would take three.  Other lanes' chunks are
-// visible to a lane after its wait and a __syncwarp.
+// chunks l, l + 32, ..: one or two copy instructions per lane, with the
+// chunk count known at compile time, where a lane copying its own labels
+// takes up to three smaller copies and a run-time check of the label count.
+// Other lanes' chunks are visible to a lane after its wait and a __syncwarp.
 template <int NB> __device__ __forceinline__ void warp_copy(void *dst, const void *src, int lane)
 {
     static_assert(NB % 16 == 0, "whole 16-byte chunks");
@@ -348,9 +349,9 @@ __global__ void __launch_bounds__(128)
     const long cb = pix(0) * D, ns = (HPASS ? 1L : (long)W) * D;
 
     // ---- forward: messages into each node, stored for the backward sweep
-    // COOP (3 or 6 labels per lane in whole warps, 16-byte aligned vectors): the
+    // COOP (label counts that fill whole warps, 16-byte aligned vectors): the
     // warp copies each vector in 16-byte chunks instead of each lane its labels
-    static_assert(!COOP || (FULL && (P == 3 || P == 6)), "cooperative copies: D = 96 or 192");
+    static_assert(!COOP || FULL, "cooperative copies: label counts that fill whole warps");
     auto issue_f = [&](int i, long o) { // node i, at element offset o
         if (i < n) {
             if constexpr (COOP) {
@@ -508,7 +509,7 @@ int launch_pass(const CrfPassArgs &a, bool hpass, int wpb, cudaStream_t st)
         if (t16) kern = k_crf_chain<P, DELTA, true, true, RING, true>;
     // cooperative 16-byte copies where the vectors allow them (the workspace's phi and messages are 256-byte
     // aligned; a caller's cost volume may not be)
-    if constexpr (P == 3 || P == 6) {
+    {
         const bool aligned = (((uintptr_t)a.theta | (uintptr_t)a.thetaq | (uintptr_t)a.phi | (uintptr_t)a.lbuf) & 15) == 0;
         if (full && aligned) {
             if (!hpass) kern = k_crf_chain<P, DELTA, false, true, RING, false, true>;
