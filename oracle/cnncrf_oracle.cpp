@@ -746,10 +746,16 @@ void oracle_crf(const float *cost, const float *wx, const float *wy, int W, int 
                                    (last && labels) ? labels + x : nullptr, W, Lbuf);
             }
         }
-        double sh = 0.0, sv = 0.0;
-        for (int y = 0; y < H; ++y) sh += cH[y];
-        for (int x = 0; x < W; ++x) sv += cV[x];
-        lbv = sh + sv;
+        // each sum in the GPU's order (k_lb): 32 partial sums, partial l over the chains l, l + 32, ..
+        // in ascending order, then the partials in order
+        auto sum32 = [](const std::vector<double> &c) {
+            double part[32] = {0.0};
+            for (size_t i = 0; i < c.size(); ++i) part[i & 31] += c[i];
+            double s = part[0];
+            for (int l = 1; l < 32; ++l) s += part[l];
+            return s;
+        };
+        lbv = sum32(cH) + sum32(cV);
         if (lb_iters) lb_iters[it] = lbv;
     }
     if (lb) *lb = lbv;

@@ -45,7 +45,9 @@
  *    its hand-over, so both are the dual objective at the same phi); a
  *    chain's minimum is the sum of its forward sweep's per-node minima, in
  *    the order the GPU kernel adds them: 32 FP64 partial sums, partial l
- *    taking the nodes i = l mod 32 in ascending i, then added in order;
+ *    taking the nodes i = l mod 32 in ascending i, then added in order; the
+ *    chain minima of each direction are summed the same way (partial l over
+ *    the chains l, l + 32, ..), and the bound is the H sum plus the V sum;
  *  - the labels: the first argmin of the last vertical pass's min-marginals;
  *  - the pairwise term w_ij rho(|x_i - x_j|): the options L1, L2, delta keep
  *    the reference's names.  STEP (the reference configs' shape): rho(0) = 0,
